@@ -1,0 +1,340 @@
+/*
+ * fh_oracle.c -- CPU oracle (test infrastructure only; see fh_oracle.h).
+ *
+ * Plain C99 restatement of the reference solvers' hot path.  Nothing in the
+ * CUDA product path links this file.  Loops follow the reference's order so
+ * that results reproduce the reference to rounding; weights for psi != t and
+ * the Atangana-Baleanu kernel are evaluated to convergence in long double.
+ */
+#include "fh_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ weights */
+
+/* y^a * sum_j (1-b)_j y^j / (j! (a+j))  -- lower incomplete beta B(y; a, b). */
+static long double ib_lower(long double y, long double a, long double b) {
+  if (y <= 0.0L) return 0.0L;
+  long double s = 0.0L, c = 1.0L, yj = 1.0L;
+  for (int j = 0; j < 4000; ++j) {
+    long double t = c * yj / (a + (long double)j);
+    s += t;
+    if (fabsl(t) <= 1e-24L * fabsl(s)) break;
+    c *= ((long double)(j + 1) - b) / (long double)(j + 1);
+    yj *= y;
+    if (c == 0.0L) break;
+  }
+  return powl(y, a) * s;
+}
+
+/* Upper tail B(1;a,b) - B(y;a,b) written in c = 1-y:  c^b sum_j (1-a)_j c^j/(j!(b+j)). */
+static long double ib_upper(long double c, long double a, long double b) {
+  if (c <= 0.0L) return 0.0L;
+  long double s = 0.0L, d = 1.0L, cj = 1.0L;
+  for (int j = 0; j < 4000; ++j) {
+    long double t = d * cj / (b + (long double)j);
+    s += t;
+    if (fabsl(t) <= 1e-24L * fabsl(s)) break;
+    d *= ((long double)(j + 1) - a) / (long double)(j + 1);
+    cj *= c;
+    if (d == 0.0L) break;
+  }
+  return powl(c, b) * s;
+}
+
+double fho_psi_int(double x0, double x1, double X, double tau, double alpha, double beta) {
+  if (beta == 1.0) {
+    /* H_solver::_kb_row, branch g(t1) <= gtj (mt_psi_caputo.cpp:506-515): one term,
+     * since inv_g_der(.,n>=2,.) == 0 for psi = t. */
+    double t0 = tau * x0, t1 = tau * x1, gtj = tau * X;
+    double v = gtj / gtj; /* inv_g_der(gtj,1,inv_g_der(gtj,0,1)) = der/t with der = t */
+    v *= pow(gtj, 1 - alpha);
+    double v3 = pow(fabs(1.0 - t1 / gtj), 1 - alpha);
+    double v4 = pow(fabs(1.0 - t0 / gtj), 1 - alpha);
+    double v2 = -(v3 - v4) / (1 - alpha);
+    double sum = 0.0;
+    sum += v2 * v;
+    return sum;
+  }
+  /* int_{t0}^{t1} (T^b - s^b)^(-a) ds = T^(1-a b)/b * [B(y1; 1/b, 1-a) - B(y0; 1/b, 1-a)],
+   * y = (s/T)^beta; complements 1-y taken through expm1/log1p. */
+  long double a = 1.0L / (long double)beta, b = 1.0L - (long double)alpha;
+  long double Xl = (long double)X;
+  long double y0 = powl((long double)x0 / Xl, (long double)beta);
+  long double y1 = powl((long double)x1 / Xl, (long double)beta);
+  long double c0 = (x0 >= X) ? 0.0L : -expm1l((long double)beta * log1pl(((long double)x0 - Xl) / Xl));
+  long double c1 = (x1 >= X) ? 0.0L : -expm1l((long double)beta * log1pl(((long double)x1 - Xl) / Xl));
+  long double diff;
+  if (y1 <= 0.5L) {
+    diff = ib_lower(y1, a, b) - ib_lower(y0, a, b);
+  } else if (y0 > 0.5L) {
+    diff = ib_upper(c0, a, b) - ib_upper(c1, a, b);
+  } else {
+    long double btot = expl(lgammal(a) + lgammal(b) - lgammal(a + b));
+    diff = (btot - ib_upper(c1, a, b)) - ib_lower(y0, a, b);
+  }
+  long double T = Xl * (long double)tau;
+  long double pre = powl(T, 1.0L - (long double)alpha * (long double)beta) / (long double)beta;
+  return (double)(pre * diff);
+}
+
+double fho_l1_b(int k, double alpha) {
+  /* mt_minimal.cpp:930: kv = pow(os-t, 1-alpha) - pow(os-t-1, 1-alpha) with k = os-t-1 */
+  return pow((double)(k + 1), 1.0 - alpha) - pow((double)k, 1.0 - alpha);
+}
+
+double fho_mittag_leffler(double a, double b, double z) {
+  long double s = 0.0L, mx = 0.0L;
+  long double lz = logl(fabsl((long double)z));
+  for (int k = 0; k < 5000; ++k) {
+    long double p = (long double)a * k + (long double)b;
+    long double t;
+    if (z == 0.0) {
+      t = (k == 0) ? 1.0L / tgammal(p) : 0.0L;
+    } else {
+      t = expl((long double)k * lz - lgammal(p));
+      if (z < 0.0 && (k & 1)) t = -t;
+      /* 1/Gamma(p) changes sign for p < 0 only; p > 0 here for a, b > 0 */
+    }
+    s += t;
+    if (fabsl(t) > mx) mx = fabsl(t);
+    if (k > 4 && fabsl(t) <= 1e-24L * fabsl(s) && fabsl(t) < mx) break;
+  }
+  if (s != 0.0L && mx / fabsl(s) > 1e6L) return NAN;
+  return (double)s;
+}
+
+double fho_ab_int(int lag, double tau, double alpha) {
+  /* I(lag) = sum_k (-lam)^k / Gamma(a k + 2) * (x1^(a k + 1) - x0^(a k + 1)),
+   * lam = a/(1-a), x1 = lag*tau, x0 = (lag-1)*tau: the ML series of
+   * MF_int (MF_int_series.cpp:436-455) integrated term by term. */
+  long double a = alpha, lam = a / (1.0L - a);
+  long double x1 = (long double)lag * (long double)tau;
+  long double lx1 = logl(x1), llam = logl(lam);
+  long double lr = (lag >= 2) ? log1pl(-1.0L / (long double)lag) : 0.0L;
+  long double s = 0.0L, mx = 0.0L;
+  for (int k = 0; k < 5000; ++k) {
+    long double p = a * k + 1.0L;
+    long double frac = (lag >= 2) ? -expm1l(p * lr) : 1.0L; /* 1 - (x0/x1)^p */
+    long double mag = expl((long double)k * llam + p * lx1 - lgammal(p + 1.0L));
+    long double t = mag * frac;
+    if (k & 1) t = -t;
+    s += t;
+    if (fabsl(t) > mx) mx = fabsl(t);
+    if (k > 4 && fabsl(t) <= 1e-24L * fabsl(s) && fabsl(t) < mx) break;
+  }
+  if (s == 0.0L || mx / fabsl(s) > 1e6L) return NAN;
+  return (double)s;
+}
+
+/* --------------------------------------------------------------- primitives */
+
+void fho_history_sum_layers(const double *H, int K, int ld, int P, const double *w, double *S) {
+  for (int p = 0; p < P; ++p) {
+    double ts = 0.0;
+    for (int t = 0; t < K; ++t) ts += w[t] * (H[(size_t)(t + 1) * ld + p] - H[(size_t)t * ld + p]);
+    S[p] = ts;
+  }
+}
+
+void fho_thomas(int N, const double *A, const double *R, const double *B, const double *Om,
+                double al1, double bt1, int right_mode, double u_right, double *u) {
+  double *Al = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+  double *Bt = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+  Al[1] = al1;
+  Bt[1] = bt1;
+  for (int i = 1; i < N; ++i) Al[i + 1] = B[i] / (R[i] - A[i] * Al[i]);
+  for (int i = 1; i < N; ++i) {
+    if (Al[i + 1] == 0.0 && B[i] == 0.0)
+      Bt[i + 1] = (A[i] * Bt[i] - Om[i]) / (R[i] - A[i] * Al[i]);
+    else
+      Bt[i + 1] = (Al[i + 1] / B[i]) * (A[i] * Bt[i] - Om[i]);
+  }
+  u[N] = right_mode == 0 ? u_right : Bt[N] / (1.0 - Al[N]);
+  for (int i = N - 1; i >= 0; --i) u[i] = Al[i + 1] * u[i + 1] + Bt[i + 1];
+  u[N + 1] = u[N];
+  free(Al);
+  free(Bt);
+}
+
+/* ------------------------------------------------------- 1D H_solver path */
+
+int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
+  const int N = p->N, ld = N + 2;
+  const double dL = p->L / N;
+  const double Dg = pow(dL, -2.0); /* pow(dL,-1-gamma)/Gamma(2-gamma), gamma = 1 */
+  const double a = p->alpha;
+  /* reset_D: mt_minimal.cpp:744-749 (tau^-a) / mt_psi_caputo.cpp:1176-1181 (tau^-1) */
+  const double Da = (p->weights == FHO_W_L1) ? pow(p->tau, -a) / tgamma(2.0 - a)
+                                             : pow(p->tau, -1.0) / tgamma(2.0 - a);
+  double *K = (double *)malloc(sizeof(double) * ld);
+  double *Ac = (double *)malloc(sizeof(double) * ld);
+  double *Bc = (double *)malloc(sizeof(double) * ld);
+  double *Rc = (double *)malloc(sizeof(double) * ld);
+  double *Om = (double *)malloc(sizeof(double) * ld);
+  double *w = (double *)malloc(sizeof(double) * (size_t)(steps + 2));
+  if (!K || !Ac || !Bc || !Rc || !Om || !w) return 1;
+  int nsaved = 0;
+  for (int tstep = 1; tstep <= steps; ++tstep) {
+    const int os = nsaved;
+    double wc;
+    if (p->weights == FHO_W_L1) {
+      wc = 1.0;
+      for (int t = 0; t < os - 1; ++t)
+        w[t] = pow((double)(os - t), 1.0 - a) - pow((double)(os - t - 1), 1.0 - a);
+    } else {
+      /* kb_time[aa] = calc_int(alpha, aa, aa+1, tstep+1, tau, 1)  (mt_psi_caputo.cpp:1481-1489) */
+      wc = fho_psi_int(tstep, tstep + 1, tstep + 1, p->tau, a, p->beta) * (1 - a);
+      for (int t = 0; t < os - 1; ++t) w[t] = fho_psi_int(t, t + 1, tstep + 1, p->tau, a, p->beta) * (1 - a);
+    }
+    for (int i = 0; i <= N; ++i) K[i] = (p->kmodel == FHO_K_CONST) ? p->kc : p->kc * exp(p->kgam * U[i]);
+    for (int i = 1; i < N; ++i) {
+      Ac[i] = Dg * K[i - 1] * p->cinv;
+      Bc[i] = Dg * K[i + 1] * p->cinv;
+      Rc[i] = p->cinv * (K[i + 1] + K[i - 1]) * Dg + Da * wc;
+      Om[i] = -Da * wc * U[i];
+      if (p->gravity) Om[i] += (K[i + 1] - K[i]) / dL;
+      double ts = 0.0;
+      if (os >= 2) {
+        /* The reference walks `double **oldp = &old[0][1]` with prev = oldp[0][id]
+         * (mt_minimal.cpp:913-917, mt_psi_caputo.cpp:1321-1326): term t reads
+         * cur = layer[t+1] against the previous read, i.e. w[t]*(layer[t+1]-layer[t])
+         * for t >= 1, while the t = 0 term is layer[1]-layer[1] = 0.  The oldest
+         * difference layer[1]-layer[0] therefore never enters the sum. */
+        const double *oldp = hist + (size_t)1 * ld;
+        double prev = oldp[i];
+        for (int t = 0; t < os - 1; ++t, oldp += ld) {
+          double cur = oldp[i];
+          ts += w[t] * (cur - prev);
+          prev = cur;
+        }
+      }
+      Om[i] += Da * ts;
+    }
+    fho_thomas(N, Ac, Rc, Bc, Om, p->al_left, p->bt_left, 0, p->u_right, U);
+    memcpy(hist + (size_t)os * ld, U, sizeof(double) * ld);
+    nsaved++;
+  }
+  free(K); free(Ac); free(Bc); free(Rc); free(Om); free(w);
+  return 0;
+}
+
+/* --------------------------------------------------- 2D TG_solver ADI path */
+
+int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work) {
+  const int sN = p->sN, M = p->M, ld = sN + 2;
+  const size_t P = (size_t)(sN + 2) * (M + 2);
+  const int nmax = (sN > M ? sN : M) + 2;
+  const double a = p->alpha, st = p->sigma / p->tau;
+  const double Da = 1.0 / tgamma(1.0 - a); /* TG_solver ctor, fr_d_t_g_2d.cpp:2391-2394 */
+  double *A = (double *)malloc(sizeof(double) * nmax), *B = (double *)malloc(sizeof(double) * nmax);
+  double *R = (double *)malloc(sizeof(double) * nmax), *Om = (double *)malloc(sizeof(double) * nmax);
+  double *u = (double *)malloc(sizeof(double) * nmax);
+  double *wx = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+  double *wy = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+  if (!A || !B || !R || !Om || !u || !wx || !wy) return 1;
+  memcpy(work, C, sizeof(double) * P); /* full-step layer 0 (TG_solver::initial) */
+#define KB(s, ja, sa, l) (Da * fho_psi_int((double)(s) + (sa), (double)(s) + (sa) + (l), (double)j + (ja), p->tau, a, p->beta))
+  for (int j = 0; j < steps; ++j) {
+    /* weights of TG_solver_::kb (fr_d_t_g_2d.cpp:3059-3239), dt_alg 0 */
+    const double kx = KB(j, 0.5, 0.0, 0.5), ky = KB(j, 1.0, 0.5, 0.5), kyh = KB(j, 1.0, 0.0, 0.5);
+    for (int k = 0; k < j; ++k) { wx[k] = KB(k, 0.5, 0.0, 1.0); wy[k] = KB(k, 1.0, 0.0, 1.0); }
+    /* x half-step: lines jj = 1..M-1, unknowns along i (fr_d_t_g_2d.cpp:2577-2590) */
+    const int os_x = 2 * j + 1;
+    for (int jj = 1; jj < M; ++jj) {
+      const int N = sN;
+      const double dl = p->dL;
+      for (int i = 1; i < N; ++i) {
+        const size_t id = (size_t)i + (size_t)jj * ld;
+        A[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) + 0.5);
+        B[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) - 0.5);
+        R[i] = st * (kx + 0.0) + A[i] + B[i];
+        Om[i] = -st * (kx + 0.0) * C[id];
+        Om[i] += p->S * 0.5;
+        double ts = 0.0;
+        if (os_x >= 3)
+          for (int k = j - 1; k >= 0; --k) ts += wx[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
+        Om[i] += st * ts;
+      }
+      for (int i = 0; i <= N + 1; ++i) u[i] = C[(size_t)i + (size_t)jj * ld];
+      fho_thomas(N, A, R, B, Om, 0.0, p->C1, 1, 0.0, u);
+      for (int i = 0; i <= N + 1; ++i) C[(size_t)i + (size_t)jj * ld] = u[i];
+    }
+    /* y half-step: lines ii = 1..sN-1, unknowns along j (fr_d_t_g_2d.cpp:2634-2648) */
+    const int os_y = 2 * j + 2;
+    for (int ii = 1; ii < sN; ++ii) {
+      const int N = M;
+      const double dl = p->dLx;
+      for (int q = 1; q < N; ++q) {
+        const size_t id = (size_t)ii + (size_t)q * ld;
+        A[q] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
+        B[q] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
+        R[q] = st * (ky + 0.0) + A[q] + B[q];
+        Om[q] = -st * (ky + 0.0) * C[id];
+        Om[q] += p->S * 0.5;
+        double ts = 0.0;
+        if (os_y >= 3)
+          for (int k = j - 1; k >= 0; --k) ts += wy[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
+        /* half-step term with the reference's operand order old[size-2]-old[size-1] (3479-3481) */
+        ts += (kyh + 0.0) * (work[(size_t)j * P + id] - C[id]);
+        Om[q] += st * ts;
+      }
+      for (int q = 0; q <= N + 1; ++q) u[q] = C[(size_t)ii + (size_t)q * ld];
+      fho_thomas(N, A, R, B, Om, 1.0, 0.0, 1, 0.0, u);
+      for (int q = 0; q <= N + 1; ++q) C[(size_t)ii + (size_t)q * ld] = u[q];
+    }
+    memcpy(work + (size_t)(j + 1) * P, C, sizeof(double) * P);
+  }
+#undef KB
+  free(A); free(B); free(R); free(Om); free(u); free(wx); free(wy);
+  return 0;
+}
+
+/* ------------------------------------------- 1D Atangana-Baleanu solve path */
+
+int fho_ab_solve(int m, int n, double tau, double alpha, const double *w, const double *src,
+                 const double *bl, const double *br, double *C, const double *exact, double *err) {
+  const double h = 1.0 / m, a = alpha;
+  const double A = -(1.0 / (h * h)) - (1.0 / (2.0 * h));
+  const double Cc = -(1.0 / (h * h)) + (1.0 / (2.0 * h));
+  const double Ii = w[0]; /* current-step coefficient (the reference's Ii, equal to I(1)) */
+  const double Bd = (Ii / (1.0 - a)) + (2.0 / (h * h));
+  double *prevC = (double *)calloc((size_t)(m + 1), sizeof(double));
+  double *Rp = (double *)calloc((size_t)(m + 1), sizeof(double));
+  double *al = (double *)calloc((size_t)(m + 1), sizeof(double));
+  double *bt = (double *)calloc((size_t)(m + 1), sizeof(double));
+  double *dts = (double *)calloc((size_t)(m + 1) * (size_t)(n + 1), sizeof(double));
+  if (!prevC || !Rp || !al || !bt || !dts) return 1;
+  double e = 0.0;
+  for (int i = 1; i <= n; ++i) {
+    for (int j = 0; j <= m; ++j) {
+      Rp[j] = (Ii / (1.0 - a)) * C[j] + src[(size_t)(i - 1) * (m + 1) + j];
+      if (i >= 2) {
+        double prev_dtC = (C[j] - prevC[j]) / tau;
+        dts[(size_t)j * (n + 1) + (i - 2)] = prev_dtC;
+        double ret = 0.0;
+        for (int tt = 0; tt < i - 1; ++tt) ret += dts[(size_t)j * (n + 1) + tt] * w[i - tt];
+        Rp[j] -= ret / (1.0 - a);
+      }
+    }
+    for (int j = 0; j <= m; ++j) prevC[j] = C[j];
+    al[0] = 0;
+    bt[0] = bl[i - 1];
+    for (int j = 1; j <= m; ++j) {
+      al[j] = Cc / (Bd - A * al[j - 1]);
+      bt[j] = (Rp[j] - A * bt[j - 1]) / (Bd - A * al[j - 1]);
+    }
+    C[m] = br[i - 1];
+    for (int j = m - 1; j >= 0; --j) C[j] = bt[j] - al[j] * C[j + 1];
+    if (exact)
+      for (int j = 0; j <= m; ++j) {
+        double d = fabs(C[j] - exact[(size_t)(i - 1) * (m + 1) + j]);
+        e += d * d;
+      }
+  }
+  if (err) *err = e / ((m + 1.0) * n);
+  free(prevC); free(Rp); free(al); free(bt); free(dts);
+  return 0;
+}

@@ -1,0 +1,124 @@
+"""Pins the CPU oracle against golden vectors produced by the reference itself
+(tests/golden/make_golden.py runs the reference solvers compiled from their own
+sources).  CPU only."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    with open(os.path.join(G, name)) as f:
+        return json.load(f)
+
+
+def relmax(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("name,weights,beta", [
+    ("h_minimal_l1.json", O.W_L1, 1.0),   # mt_minimal.cpp H_solver
+    ("h_psi_t.json", O.W_PSI, 1.0),       # mt_psi_caputo.cpp H_solver, psi = t
+    ("h_psi_t07.json", O.W_PSI, 0.7),     # psi = t^0.7, reference series at eps 1e-15
+    ("h_psi_t15.json", O.W_PSI, 1.5),     # psi = t^1.5
+])
+def test_h_solver_matches_reference(name, weights, beta):
+    g = load(name)
+    N = g["N"]
+    p = dict(N=N, L=g["L"], tau=g["tau"], alpha=g["alpha"], weights=weights, beta=beta,
+             kmodel=O.K_CONST, kc=g["k"], kgam=0.0, cinv=20.0, gravity=1, al_left=1.0,
+             bt_left=-g["uc"], u_right=g["Hbottom"])
+    U0 = np.zeros(N + 2)
+    U0[:N + 1] = g["U0"]
+    U, _ = O.h_solve(p, U0, g["steps"])
+    # the solution moved by O(1): the comparison is not trivially satisfied
+    assert np.max(np.abs(np.array(g["U"])[:N + 1] - np.array(g["U0"]))) > 0.5
+    assert relmax(U, g["U"]) <= 1e-12
+
+
+def test_tg_adi_matches_reference():
+    g = load("tg_adi.json")
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"],
+             d=g["d"], C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), g["steps"])
+    assert np.max(np.abs(np.array(g["C"]) - np.array(g["C0"]))) > 0.1
+    assert relmax(C, g["C"]) <= 1e-13
+
+
+def test_psi_weights_match_reference_series():
+    """calc_int (mt_psi_caputo.cpp:720-741) at eps 1e-15 against the converged
+    incomplete-beta value.  The reference series does not converge on the very
+    first interval [0, tau] of step 1 (both endpoints singular, ratio 1 in
+    _kb_row); that entry is pinned against the closed Beta-function value."""
+    for key, v in load("psi_weights.json").items():
+        a_, b_ = v["alpha"], v["beta"]
+        for a, t0, val in v["w"]:
+            o = O.psi_int(t0, t0 + 1, a, v["tau"], a_, b_)
+            if a == 1 and t0 == 0:
+                exact = (v["tau"] ** (1 - a_ * b_) / b_) * math.exp(
+                    math.lgamma(1 / b_) + math.lgamma(1 - a_) - math.lgamma(1 / b_ + 1 - a_))
+                assert abs(o - exact) <= 1e-13 * abs(exact), (key, a, t0)
+            else:
+                assert abs(o - val) <= 1e-9 * abs(val), (key, a, t0, o, val)
+
+
+def test_psi_t_is_l1():
+    """For psi = t the psi-Caputo weight is the L1 coefficient times tau^(1-a)/(1-a)."""
+    for alpha in (0.3, 0.7, 0.95):
+        for n in (1, 5, 200, 4000):
+            for k in (0, n // 2, n):
+                w = O.psi_int(k, k + 1, n + 1, 1e-3, alpha, 1.0)
+                b = O.l1_b(n - k, alpha) * (1e-3) ** (1 - alpha) / (1 - alpha)
+                assert abs(w - b) <= 1e-11 * abs(b)
+
+
+def test_mittag_leffler_matches_reference_and_identities():
+    for a, b, z, v in load("ab.json")["ml"]:
+        assert abs(O.mittag_leffler(a, b, z) - v) <= 1e-14 * abs(v)
+    for z in (-3.0, -0.5, 0.0, 0.7, 2.0):
+        assert abs(O.mittag_leffler(1.0, 1.0, z) - math.exp(z)) <= 1e-14 * math.exp(z)
+    for x in (0.3, 1.0, 2.5):
+        assert abs(O.mittag_leffler(2.0, 1.0, -x * x) - math.cos(x)) <= 1e-13
+
+
+def test_ab_lag_weights_match_reference():
+    """MF_int_choice series (MF_int_series.cpp:436-455) at the lags the history
+    sum uses (lag >= 2; MF_intF_simple sums tt <= n-2)."""
+    v = load("ab.json")["abw"]
+    for lag, val in v["w"]:
+        if lag >= 2:
+            assert abs(O.ab_int(lag, v["tau"], v["alpha"]) - val) <= 1e-12 * abs(val)
+
+
+def test_ab_solve_matches_reference():
+    s = load("ab.json")["solve"]
+    m, n, a = s["m"], s["n"], s["alpha"]
+    tau = s["T"] / n
+    w = O.ab_weights(n, tau, a)
+    w[0] = s["ii"]
+    lam = -a / (1 - a)
+    src = np.array([[(24.0 / (1 - a)) * (i * tau) ** 4 * O.mittag_leffler(a, 5.0, lam * (i * tau) ** a)
+                     for _ in range(m + 1)] for i in range(1, n + 1)])
+    ex = np.array([[(i * tau) ** 4 for _ in range(m + 1)] for i in range(1, n + 1)])
+    _, err = O.ab_solve(m, n, tau, a, w, src, ex[:, 0].copy(), ex[:, -1].copy(), np.zeros(m + 1), ex)
+    assert abs(err - s["err"]) <= 1e-12 * s["err"]
+
+
+def test_thomas_solves_system():
+    rng = np.random.default_rng(0)
+    N = 37
+    A = rng.uniform(0.5, 1.0, N + 1)
+    B = rng.uniform(0.5, 1.0, N + 1)
+    R = A + B + rng.uniform(0.1, 1.0, N + 1)
+    Om = rng.normal(size=N + 1)
+    u = O.thomas(A, R, B, Om, 0.0, 0.25, 0, -0.5, np.zeros(N + 2))
+    res = A[1:N] * u[0:N - 1] - R[1:N] * u[1:N] + B[1:N] * u[2:N + 1] - Om[1:N]
+    assert np.max(np.abs(res)) < 1e-12
+    assert u[0] == 0.25 and u[N] == -0.5 and u[N + 1] == u[N]
