@@ -1,0 +1,199 @@
+/*
+ * fhist.h -- C ABI of libfhist, the GB300 (sm_103a) implementation of the
+ * fractional-derivative history path of sevaboh/theses_code:
+ *   per time step, the weighted sum over all stored time layers (L1
+ *   Caputo-Gerasimov, psi-Caputo or Atangana-Baleanu weights), then the
+ *   implicit tridiagonal solve of every grid line (ADI x/y sweeps in 2D).
+ *
+ * Conventions
+ *  - Plain C types only; every array argument is a DEVICE pointer unless the
+ *    parameter name ends in _host.  Sizes are element counts.
+ *  - Every call returns an int status (FH_OK on success) and never aborts;
+ *    fh_last_error() gives a one-line reason.  Work is enqueued on the
+ *    context's stream; host-buffer calls synchronise that stream.
+ *  - Calls on one context are not thread-safe; use one context per thread.
+ *  - Each entry point names the reference interface it replaces (file:line in
+ *    the reference repository).
+ */
+#ifndef FHIST_H
+#define FHIST_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FH_OK 0
+#define FH_EINVAL 1      /* bad argument                                  */
+#define FH_ENOMEM 2      /* device allocation failed / history full      */
+#define FH_ECUDA 3       /* CUDA runtime error                            */
+#define FH_ENONFINITE 4  /* non-finite value in a result                  */
+#define FH_ETIMEOUT 5    /* a bounded device wait ran out                 */
+#define FH_ERANGE 6      /* argument outside the evaluated range          */
+#define FH_ENOTSUP 7     /* combination not supported                     */
+
+typedef struct fh_ctx fh_ctx;
+
+/* ------------------------------------------------------------- context */
+/* Replaces the reference offload wrapper (OpenCL_program / OpenCL_commandqueue,
+ * opencl_cuda_base.cpp:353-455, 212-318; CUDA backend 467-752). */
+int fh_version(void);
+int fh_ctx_create(int device, fh_ctx **out);
+int fh_ctx_destroy(fh_ctx *ctx);
+const char *fh_last_error(const fh_ctx *ctx);
+int fh_ctx_sync(fh_ctx *ctx);
+int fh_ctx_set_stream(fh_ctx *ctx, void *cuda_stream);
+void *fh_ctx_get_stream(fh_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+long long fh_ctx_launch_count(const fh_ctx *ctx);
+
+/* Live kernel timing with CUDA events recorded on the context stream around
+ * each launch of a kernel class (off by default; enabling clears the totals).
+ * FH_PROF_HISTORY: history-sum kernels; FH_PROF_SWEEP: line-sweep kernels;
+ * FH_PROF_WEIGHTS: per-step weight kernels.  _read synchronises the stream. */
+#define FH_PROF_HISTORY 0
+#define FH_PROF_SWEEP 1
+#define FH_PROF_WEIGHTS 2
+int fh_ctx_profile(fh_ctx *ctx, int enable);
+int fh_ctx_profile_read(fh_ctx *ctx, int kind, double *total_ms, long long *launches);
+
+/* ------------------------------------------------------------- weights */
+/* w[k] = scale * int_{(x0+k)tau}^{(x0+k+len)tau} (psi(X tau) - psi(s))^(-alpha) ds,
+ * k = 0..K-1, psi(t) = t^beta.  Replaces H_solver::kb/calc_int/_kb_row/_kb_row2
+ * (mt_psi_caputo.cpp:435-747), TG_solver_::kb (fr_d_t_g_2d.cpp:3059-3239) and the
+ * OpenCL calc_kb kernels (fr_d_t_g_2d.cpp:1492-1547).  beta == 1 uses the
+ * reference's closed form; other beta the converged integral. */
+int fh_weights_psi(fh_ctx *ctx, int K, double x0, double len, double X, double tau,
+                   double alpha, double beta, double scale, double *w);
+
+/* L1 Caputo-Gerasimov coefficients of H_solver::Om1 (mt_minimal.cpp:926-934):
+ * w[t] = (os-t)^(1-alpha) - (os-t-1)^(1-alpha), t = 0..os-2. */
+int fh_weights_l1(fh_ctx *ctx, int os, double alpha, double *w);
+
+/* Atangana-Baleanu lag weights of MF_intF_simple (MF_int_series.cpp:614-718,
+ * MF_int_choice 523-530): w[lag] = int_{(lag-1)tau}^{lag tau} E_alpha(-alpha/(1-alpha) u^alpha) du
+ * for lag = 1..n, and w[0] = w[1].  FH_ERANGE if the series would cancel badly. */
+int fh_weights_ab(fh_ctx *ctx, int n, double tau, double alpha, double *w);
+
+/* out[i] = E_{a,b}(z[i]) (mittag_leffler, mittag-lefler.cpp:239-293). */
+int fh_mittag_leffler(fh_ctx *ctx, int n, double a, double b, const double *z, double *out);
+
+/* ------------------------------------------------------------- history */
+/* S[m*ldS + p] = sum_{k<K} W[m*ldw + k] * D[k*ldd + p], m < M (M = 1 or 2), p < P.
+ * D holds layer differences (layer k+1 minus layer k), point index contiguous.
+ * Replaces the history loops of H_solver::Om1 (mt_psi_caputo.cpp:1315-1342),
+ * TG_solver_::Om1 (fr_d_t_g_2d.cpp:3340-3490), H_solver::time_summing
+ * (irrigation_fractional.cpp:4099-4177) and the GPU Sum kernels
+ * (irrigation_fractional.cpp:1224-1495).  P and ldd must be even, D 16-byte aligned. */
+int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
+                   const double *D, long long ldd, double *S, long long ldS);
+
+/* Reference Sum-kernel form on stored layers (fr_ocl_call_sum,
+ * irrigation_fractional.cpp:1828-1896): S[p] = sum_{t<K} w[t]*(H[(t+1)ldh+p] - H[t ldh+p]). */
+int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H,
+                          long long ldh, double *S);
+
+/* --------------------------------------------------------- tridiagonal */
+/* nsys systems A_i u_{i-1} - R_i u_i + B_i u_{i+1} = Om_i, i = 1..N-1, with
+ * u_0 = al1[s] u_1 + bt1[s] and u_N = u_right[s] (right_mode 0) or
+ * u_N = Bt_N/(1-Al_N) (right_mode 1); u_{N+1} = u_N.  System s uses entries
+ * [s*lds, s*lds + N] of A, R, B, Om and [s*ldu, s*ldu + N+1] of u.
+ * Replaces H_solver::al1/bt1/U1 (mt_minimal.cpp:829-858, 942-1031) and
+ * TG_solver::U1 (fr_d_t_g_2d.cpp:2523-2551). */
+int fh_tridiag_batched(fh_ctx *ctx, int nsys, int N, const double *A, const double *R,
+                       const double *B, const double *Om, long long lds, const double *al1,
+                       const double *bt1, int right_mode, const double *u_right, double *u,
+                       long long ldu);
+
+/* Parallel cyclic reduction with the semantics of pcr_solver (nvidia_pcr.cpp:424-458):
+ * a_i x_{i-1} + b_i x_i + c_i x_{i+1} = d_i for nsys systems of n unknowns stored
+ * back to back (a_0 and c_{n-1} ignored).  n <= 2048. */
+int fh_pcr_solver(fh_ctx *ctx, const double *a, const double *b, const double *c, const double *d,
+                  double *x, int n, int nsys);
+
+/* ------------------------------------------------ 1D H_solver, batched */
+#define FH_W_L1 0   /* mt_minimal.cpp H_solver: L1 weights, Da = tau^-a/Gamma(2-a)        */
+#define FH_W_PSI 1  /* mt_psi_caputo.cpp H_solver: psi-Caputo weights, Da = 1/(tau Gamma(2-a)) */
+#define FH_K_CONST 0
+#define FH_K_EXP 1
+
+typedef struct {
+  int N;            /* intervals; nodes 0..N plus ghost N+1             */
+  double L;         /* domain length, dL = L/N                          */
+  double tau;       /* time step                                        */
+  double alpha;     /* time-derivative order, 0 < alpha < 1             */
+  int weights;      /* FH_W_L1 or FH_W_PSI                              */
+  double beta;      /* psi(t) = t^beta (FH_W_PSI)                       */
+  int kmodel;       /* FH_K_CONST: K = kc ; FH_K_EXP: K = kc exp(kgam u) */
+  double kc, kgam;
+  double cinv;      /* constant 1/(dw/dh) factor                        */
+  int gravity;      /* add (K_i - K_{i-1})/dL to the right part         */
+  double al_left, bt_left; /* u_0 = al_left u_1 + bt_left               */
+  double u_right;   /* Dirichlet value at node N                        */
+} fh_h_params;
+
+typedef struct fh_h_batch fh_h_batch;
+
+/* A batch of independent H_solver instances (mt_psi_caputo.cpp:369-1507 /
+ * mt_minimal.cpp:276-1048 with gamma = 1) advanced in lock step, one history
+ * ring per batch.  max_steps bounds the stored history. */
+int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, int max_steps,
+                      fh_h_batch **out);
+int fh_h_batch_destroy(fh_h_batch *b);
+/* Total number of doubles of the concatenated state (sum of N_i + 2). */
+long long fh_h_batch_state_size(const fh_h_batch *b);
+/* Concatenated per-instance U arrays (N_i + 2 each, instance order). */
+int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host);
+int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host);
+/* H_solver::calc_step repeated nsteps times (tstep starts at 1). */
+int fh_h_batch_step(fh_h_batch *b, int nsteps);
+int fh_h_batch_tstep(const fh_h_batch *b);
+
+/* ------------------------------------------------------ 2D TG_solver ADI */
+typedef struct {
+  int sN, M;        /* i = 0..sN, j = 0..M, array (sN+2)x(M+2), idx = i + j*(sN+2) */
+  double tau, alpha, beta;
+  double sigma, d, C1, S;
+  double dL, dLx;   /* steps of the x sweep (along i) and y sweep (along j) */
+} fh_tg_params;
+
+#define FH_TG_FP64 0      /* plain FP64 history sum                          */
+#define FH_TG_BLOCKED 1   /* blocked history: tensor-core contraction of old layers */
+
+typedef struct fh_tg_solver fh_tg_solver;
+
+/* TG_solver_<func,1,kform> with dt_alg 0 (fr_d_t_g_2d.cpp:2037-4052): fixed
+ * diffusion coefficient d, psi(t) = t^beta, full history. */
+int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh_tg_solver **out);
+int fh_tg_destroy(fh_tg_solver *s);
+/* V2 = |v|^2 per node and the initial field, (sN+2)*(M+2) each. */
+int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C_host);
+/* Device-pointer variant (inputs already resident in HBM). */
+int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C);
+/* TG_solver::calc_step repeated nsteps times. */
+int fh_tg_step(fh_tg_solver *s, int nsteps);
+int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);
+/* Device pointer to the current field ((sN+2)*(M+2) doubles, owned by the solver). */
+const double *fh_tg_field(const fh_tg_solver *s);
+int fh_tg_tstep(const fh_tg_solver *s);
+
+/* ----------------------------------------- 1D Atangana-Baleanu solver */
+typedef struct fh_ab_solver fh_ab_solver;
+
+/* solve_and_check (MF_int_series.cpp:875-958) with MF_intF_simple history:
+ * m intervals on [0,1], A C_{j-1} + Bd C_j + Cc C_{j+1} = Rp_j, Dirichlet ends. */
+int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh_ab_solver **out);
+int fh_ab_destroy(fh_ab_solver *s);
+/* Source rows src_host[r*(m+1) + j]; step i uses row min(i-1, nrows-1).
+ * Boundary values bl_host/br_host likewise per row. */
+int fh_ab_set_source_host(fh_ab_solver *s, int nrows, const double *src_host, const double *bl_host,
+                          const double *br_host);
+int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host);
+/* Override the current-step coefficient Ii (default: the lag-1 weight). */
+int fh_ab_set_current_coef(fh_ab_solver *s, double Ii);
+int fh_ab_step(fh_ab_solver *s, int nsteps);
+int fh_ab_get_c_host(fh_ab_solver *s, double *C_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FHIST_H */

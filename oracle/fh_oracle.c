@@ -195,7 +195,7 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
       Bc[i] = Dg * K[i + 1] * p->cinv;
       Rc[i] = p->cinv * (K[i + 1] + K[i - 1]) * Dg + Da * wc;
       Om[i] = -Da * wc * U[i];
-      if (p->gravity) Om[i] += (K[i + 1] - K[i]) / dL;
+      if (p->gravity) Om[i] += (K[i] - K[i - 1]) / dL; /* (KK(p)-KK(p-1))/dL, mt_minimal.cpp:904 */
       double ts = 0.0;
       if (os >= 2) {
         /* The reference walks `double **oldp = &old[0][1]` with prev = oldp[0][id]
@@ -223,72 +223,74 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
 
 /* --------------------------------------------------- 2D TG_solver ADI path */
 
-int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work) {
+/* One x line (dir 0, line jj) or y line (dir 1, line ii) of TG_solver::calc_step. */
+static void tg_line(const fho_tg_params *p, const double *V2, double *C, const double *work, int j, int dir, int line,
+                    double kcur, double kyh, const double *wk, double *A, double *B, double *R, double *Om, double *u) {
   const int sN = p->sN, M = p->M, ld = sN + 2;
   const size_t P = (size_t)(sN + 2) * (M + 2);
+  const double st = p->sigma / p->tau;
+  const int N = dir == 0 ? sN : M;
+  const double dl = dir == 0 ? p->dL : p->dLx;
+  for (int i = 1; i < N; ++i) {
+    const size_t id = dir == 0 ? (size_t)i + (size_t)line * ld : (size_t)line + (size_t)i * ld;
+    if (dir == 0) {
+      A[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) + 0.5);
+      B[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) - 0.5);
+    } else {
+      A[i] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
+      B[i] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
+    }
+    R[i] = st * (kcur + 0.0) + A[i] + B[i];
+    Om[i] = -st * (kcur + 0.0) * C[id];
+    Om[i] += p->S * 0.5;
+    double ts = 0.0;
+    if (2 * j + 1 + dir >= 3)
+      for (int k = j - 1; k >= 0; --k) ts += wk[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
+    /* y half-step term with the reference's operand order old[size-2]-old[size-1] (3479-3481) */
+    if (dir == 1) ts += (kyh + 0.0) * (work[(size_t)j * P + id] - C[id]);
+    Om[i] += st * ts;
+  }
+  for (int i = 0; i <= N + 1; ++i)
+    u[i] = C[dir == 0 ? (size_t)i + (size_t)line * ld : (size_t)line + (size_t)i * ld];
+  fho_thomas(N, A, R, B, Om, dir == 0 ? 0.0 : 1.0, dir == 0 ? p->C1 : 0.0, 1, 0.0, u);
+  for (int i = 0; i <= N + 1; ++i)
+    C[dir == 0 ? (size_t)i + (size_t)line * ld : (size_t)line + (size_t)i * ld] = u[i];
+}
+
+int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work) {
+  const int sN = p->sN, M = p->M;
+  const size_t P = (size_t)(sN + 2) * (M + 2);
   const int nmax = (sN > M ? sN : M) + 2;
-  const double a = p->alpha, st = p->sigma / p->tau;
+  const double a = p->alpha;
   const double Da = 1.0 / tgamma(1.0 - a); /* TG_solver ctor, fr_d_t_g_2d.cpp:2391-2394 */
-  double *A = (double *)malloc(sizeof(double) * nmax), *B = (double *)malloc(sizeof(double) * nmax);
-  double *R = (double *)malloc(sizeof(double) * nmax), *Om = (double *)malloc(sizeof(double) * nmax);
-  double *u = (double *)malloc(sizeof(double) * nmax);
   double *wx = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
   double *wy = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
-  if (!A || !B || !R || !Om || !u || !wx || !wy) return 1;
+  if (!wx || !wy) return 1;
   memcpy(work, C, sizeof(double) * P); /* full-step layer 0 (TG_solver::initial) */
 #define KB(s, ja, sa, l) (Da * fho_psi_int((double)(s) + (sa), (double)(s) + (sa) + (l), (double)j + (ja), p->tau, a, p->beta))
   for (int j = 0; j < steps; ++j) {
     /* weights of TG_solver_::kb (fr_d_t_g_2d.cpp:3059-3239), dt_alg 0 */
     const double kx = KB(j, 0.5, 0.0, 0.5), ky = KB(j, 1.0, 0.5, 0.5), kyh = KB(j, 1.0, 0.0, 0.5);
     for (int k = 0; k < j; ++k) { wx[k] = KB(k, 0.5, 0.0, 1.0); wy[k] = KB(k, 1.0, 0.0, 1.0); }
-    /* x half-step: lines jj = 1..M-1, unknowns along i (fr_d_t_g_2d.cpp:2577-2590) */
-    const int os_x = 2 * j + 1;
-    for (int jj = 1; jj < M; ++jj) {
-      const int N = sN;
-      const double dl = p->dL;
-      for (int i = 1; i < N; ++i) {
-        const size_t id = (size_t)i + (size_t)jj * ld;
-        A[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) + 0.5);
-        B[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) - 0.5);
-        R[i] = st * (kx + 0.0) + A[i] + B[i];
-        Om[i] = -st * (kx + 0.0) * C[id];
-        Om[i] += p->S * 0.5;
-        double ts = 0.0;
-        if (os_x >= 3)
-          for (int k = j - 1; k >= 0; --k) ts += wx[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
-        Om[i] += st * ts;
+    /* x half-step: lines jj = 1..M-1 (fr_d_t_g_2d.cpp:2577-2590); y half-step: lines
+     * ii = 1..sN-1 (2634-2648).  Lines are independent, so they run in parallel. */
+    for (int dir = 0; dir < 2; ++dir) {
+      const int nlines = dir == 0 ? M : sN;
+#pragma omp parallel
+      {
+        double *A = (double *)malloc(sizeof(double) * nmax), *B = (double *)malloc(sizeof(double) * nmax);
+        double *R = (double *)malloc(sizeof(double) * nmax), *Om = (double *)malloc(sizeof(double) * nmax);
+        double *u = (double *)malloc(sizeof(double) * nmax);
+#pragma omp for schedule(static)
+        for (int line = 1; line < nlines; ++line)
+          tg_line(p, V2, C, work, j, dir, line, dir == 0 ? kx : ky, kyh, dir == 0 ? wx : wy, A, B, R, Om, u);
+        free(A); free(B); free(R); free(Om); free(u);
       }
-      for (int i = 0; i <= N + 1; ++i) u[i] = C[(size_t)i + (size_t)jj * ld];
-      fho_thomas(N, A, R, B, Om, 0.0, p->C1, 1, 0.0, u);
-      for (int i = 0; i <= N + 1; ++i) C[(size_t)i + (size_t)jj * ld] = u[i];
-    }
-    /* y half-step: lines ii = 1..sN-1, unknowns along j (fr_d_t_g_2d.cpp:2634-2648) */
-    const int os_y = 2 * j + 2;
-    for (int ii = 1; ii < sN; ++ii) {
-      const int N = M;
-      const double dl = p->dLx;
-      for (int q = 1; q < N; ++q) {
-        const size_t id = (size_t)ii + (size_t)q * ld;
-        A[q] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
-        B[q] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
-        R[q] = st * (ky + 0.0) + A[q] + B[q];
-        Om[q] = -st * (ky + 0.0) * C[id];
-        Om[q] += p->S * 0.5;
-        double ts = 0.0;
-        if (os_y >= 3)
-          for (int k = j - 1; k >= 0; --k) ts += wy[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
-        /* half-step term with the reference's operand order old[size-2]-old[size-1] (3479-3481) */
-        ts += (kyh + 0.0) * (work[(size_t)j * P + id] - C[id]);
-        Om[q] += st * ts;
-      }
-      for (int q = 0; q <= N + 1; ++q) u[q] = C[(size_t)ii + (size_t)q * ld];
-      fho_thomas(N, A, R, B, Om, 1.0, 0.0, 1, 0.0, u);
-      for (int q = 0; q <= N + 1; ++q) C[(size_t)ii + (size_t)q * ld] = u[q];
     }
     memcpy(work + (size_t)(j + 1) * P, C, sizeof(double) * P);
   }
 #undef KB
-  free(A); free(B); free(R); free(Om); free(u); free(wx); free(wy);
+  free(wx); free(wy);
   return 0;
 }
 

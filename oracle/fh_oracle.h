@@ -69,7 +69,7 @@ typedef struct {
   int kmodel;     /* FHO_K_CONST: K=kc ; FHO_K_EXP: K = kc*exp(kgam*u)            */
   double kc, kgam;
   double cinv;    /* constant 1/(dw/dh) multiplier                                */
-  int gravity;    /* add (K(i+1)-K(i))/dL to the right part                       */
+  int gravity;    /* add (K(i)-K(i-1))/dL to the right part                       */
   double al_left, bt_left; /* u_0 = al_left*u_1 + bt_left                         */
   double u_right; /* Dirichlet value at node N                                    */
 } fho_h_params;

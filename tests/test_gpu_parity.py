@@ -1,0 +1,335 @@
+"""GPU parity: every libfhist entry point against the CPU oracle and the
+reference golden vectors.  FP64 tolerance (the plain path's contract):
+relative max-norm <= 1e-12 for solver states, tighter for primitives."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+TOL_SOLVER = 1e-12
+
+
+def relmax(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from theses_code_gb300._lib import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def torch_mod():
+    import torch
+    return torch
+
+
+def dev(torch, a):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+# ------------------------------------------------------------------ weights
+@pytest.mark.parametrize("alpha,beta", [(0.7, 1.0), (0.3, 1.0), (0.95, 1.0), (0.6, 0.5), (0.8, 2.0),
+                                        (0.55, 1.37), (0.9, 0.75)])
+def test_weights_psi(ctx, torch_mod, alpha, beta):
+    torch = torch_mod
+    for X, tau in [(7.0, 1e-3), (500.5, 5e-4), (4001.0, 1e-2)]:
+        K = int(X - 1.0)
+        w = torch.zeros(K, dtype=torch.float64, device="cuda")
+        ctx.call("fh_weights_psi", K, 0.0, 1.0, X, tau, alpha, beta, 2.5, w.data_ptr())
+        ctx.sync()
+        got = w.cpu().numpy()
+        ref = np.array([2.5 * O.psi_int(k, k + 1.0, X, tau, alpha, beta) for k in range(K)])
+        # the closed form subtracts nearly equal powers: a 1-ulp pow difference
+        # (CUDA vs glibc) grows to ~eps * X / (1 - alpha) relative
+        tol = max(1e-13, 4e-16 * X / (1 - alpha)) if beta == 1.0 else 2e-10
+        assert np.all(np.abs(got - ref) <= tol * np.abs(ref)), (X, np.max(np.abs(got - ref) / np.abs(ref)))
+
+
+def test_weights_l1(ctx, torch_mod):
+    torch = torch_mod
+    for os_ in (0, 1, 2, 3, 1000):
+        w = torch.zeros(max(os_, 1), dtype=torch.float64, device="cuda")
+        ctx.call("fh_weights_l1", os_, 0.8, w.data_ptr())
+        ctx.sync()
+        got = w.cpu().numpy()[:max(os_ - 1, 0)]
+        ref = np.array([O.l1_b(os_ - t - 1, 0.8) for t in range(os_ - 1)])
+        # (k+1)^0.2 - k^0.2 cancels: 1-ulp pow differences grow like eps * k / (1 - alpha)
+        lag = np.arange(os_ - 1, 0, -1, dtype=float)
+        assert np.all(np.abs(got - ref) <= 4e-16 * np.maximum(lag, 1.0) / 0.2 * np.abs(ref))
+
+
+def test_weights_ab(ctx, torch_mod):
+    torch = torch_mod
+    for alpha, tau, n in [(0.6, 1e-4, 3000), (0.5, 0.01, 50), (0.3, 1e-3, 800)]:
+        w = torch.zeros(n + 1, dtype=torch.float64, device="cuda")
+        ctx.call("fh_weights_ab", n, tau, alpha, w.data_ptr())
+        ctx.sync()
+        got = w.cpu().numpy()
+        lags = [1, 2, 3, 10, n // 2, n - 1, n]
+        for lag in lags:
+            ref = O.ab_int(lag, tau, alpha)
+            assert abs(got[lag] - ref) <= 1e-12 * abs(ref), (alpha, lag, got[lag], ref)
+        assert got[0] == got[1]
+
+
+def test_weights_ab_reference_golden(ctx, torch_mod):
+    """Lag weights against the reference MF_int_choice series (lags the history uses)."""
+    torch = torch_mod
+    g = json.load(open(os.path.join(G, "ab.json")))["abw"]
+    n = g["n"]
+    w = torch.zeros(n + 1, dtype=torch.float64, device="cuda")
+    ctx.call("fh_weights_ab", n, g["tau"], g["alpha"], w.data_ptr())
+    ctx.sync()
+    got = w.cpu().numpy()
+    for lag, val in g["w"]:
+        if lag >= 2:
+            assert abs(got[lag] - val) <= 1e-12 * abs(val)
+
+
+def test_mittag_leffler(ctx, torch_mod):
+    torch = torch_mod
+    g = json.load(open(os.path.join(G, "ab.json")))["ml"]
+    for a, b, z, val in g:
+        zz = dev(torch, [z])
+        out = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ctx.call("fh_mittag_leffler", 1, a, b, zz.data_ptr(), out.data_ptr())
+        ctx.sync()
+        assert abs(out.item() - val) <= 2e-14 * abs(val)
+    zs = np.linspace(-3, 1, 41)
+    zz = dev(torch, zs)
+    out = torch.zeros(41, dtype=torch.float64, device="cuda")
+    ctx.call("fh_mittag_leffler", 41, 1.0, 1.0, zz.data_ptr(), out.data_ptr())
+    ctx.sync()
+    assert relmax(out.cpu().numpy(), np.exp(zs)) < 1e-14
+
+
+# ------------------------------------------------------------------ history
+@pytest.mark.parametrize("M", [1, 2])
+@pytest.mark.parametrize("K,P", [(0, 64), (1, 2), (5, 130), (137, 1000), (2049, 4096)])
+def test_history_sum(ctx, torch_mod, M, K, P):
+    torch = torch_mod
+    rng = np.random.default_rng(K * 7 + P + M)
+    D = rng.normal(size=(max(K, 1), P))
+    W = rng.uniform(0.1, 1.0, size=(M, max(K, 1)))
+    Dd, Wd = dev(torch, D), dev(torch, W)
+    S = torch.full((M, P), 7.0, dtype=torch.float64, device="cuda")
+    ctx.call("fh_history_sum", M, K, P, Wd.data_ptr(), W.shape[1], Dd.data_ptr(), P, S.data_ptr(), P)
+    ctx.sync()
+    ref = W[:, :K] @ D[:K] if K > 0 else np.zeros((M, P))
+    scale = np.abs(W[:, :K]) @ np.abs(D[:K]) if K > 0 else np.ones((M, P))
+    assert np.all(np.abs(S.cpu().numpy() - ref) <= 1e-14 * np.maximum(scale, 1e-300) * max(K, 1) ** 0.5 + 0.0)
+
+
+def test_history_sum_rejects_odd_and_misaligned(ctx, torch_mod):
+    torch = torch_mod
+    from theses_code_gb300._lib import FhError
+    D = torch.zeros(10, dtype=torch.float64, device="cuda")
+    W = torch.ones(2, dtype=torch.float64, device="cuda")
+    S = torch.zeros(10, dtype=torch.float64, device="cuda")
+    with pytest.raises(FhError):
+        ctx.call("fh_history_sum", 1, 2, 3, W.data_ptr(), 2, D.data_ptr(), 4, S.data_ptr(), 4)
+    with pytest.raises(FhError):
+        ctx.call("fh_history_sum", 3, 2, 4, W.data_ptr(), 2, D.data_ptr(), 4, S.data_ptr(), 4)
+
+
+def test_history_sum_layers(ctx, torch_mod):
+    torch = torch_mod
+    rng = np.random.default_rng(3)
+    K, P = 41, 333
+    H = rng.normal(size=(K + 1, P))
+    w = rng.uniform(size=K)
+    S = torch.zeros(P, dtype=torch.float64, device="cuda")
+    ctx.call("fh_history_sum_layers", K, P, dev(torch, w).data_ptr(), dev(torch, H).data_ptr(), P, S.data_ptr())
+    ctx.sync()
+    assert relmax(S.cpu().numpy(), O.history_sum_layers(H, w)) < 1e-13
+
+
+# ------------------------------------------------------------- tridiagonal
+@pytest.mark.parametrize("N,right_mode", [(1, 0), (2, 1), (37, 0), (513, 1)])
+def test_tridiag_batched(ctx, torch_mod, N, right_mode):
+    torch = torch_mod
+    rng = np.random.default_rng(N)
+    nsys = 5
+    A = rng.uniform(0.2, 1.0, (nsys, N + 1))
+    B = rng.uniform(0.2, 1.0, (nsys, N + 1))
+    B[:, 3 % (N + 1)] = 0.0  # exercise the zero-B branch
+    R = A + B + rng.uniform(0.1, 1.0, (nsys, N + 1))
+    Om = rng.normal(size=(nsys, N + 1))
+    al1 = rng.uniform(0, 1, nsys)
+    bt1 = rng.normal(size=nsys)
+    ur = rng.normal(size=nsys)
+    u = torch.zeros((nsys, N + 2), dtype=torch.float64, device="cuda")
+    t = [dev(torch, x) for x in (A, R, B, Om, al1, bt1, ur)]
+    ctx.call("fh_tridiag_batched", nsys, N, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), t[3].data_ptr(),
+             N + 1, t[4].data_ptr(), t[5].data_ptr(), right_mode, t[6].data_ptr(), u.data_ptr(), N + 2)
+    ctx.sync()
+    got = u.cpu().numpy()
+    for s in range(nsys):
+        ref = O.thomas(A[s], R[s], B[s], Om[s], al1[s], bt1[s], right_mode, ur[s], np.zeros(N + 2))
+        assert relmax(got[s], ref) < 1e-13
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 513, 2048])
+def test_pcr(ctx, torch_mod, n):
+    torch = torch_mod
+    rng = np.random.default_rng(n)
+    nsys = 3
+    a = rng.uniform(-1, 1, (nsys, n))
+    c = rng.uniform(-1, 1, (nsys, n))
+    b = np.abs(a) + np.abs(c) + rng.uniform(0.5, 1.5, (nsys, n))
+    d = rng.normal(size=(nsys, n))
+    x = torch.zeros((nsys, n), dtype=torch.float64, device="cuda")
+    t = [dev(torch, v) for v in (a, b, c, d)]
+    ctx.call("fh_pcr_solver", *[v.data_ptr() for v in t], x.data_ptr(), n, nsys)
+    ctx.sync()
+    got = x.cpu().numpy()
+    for s in range(nsys):
+        Mx = np.diag(b[s]) + np.diag(a[s, 1:], -1) + np.diag(c[s, :-1], 1)
+        assert relmax(got[s], np.linalg.solve(Mx, d[s])) < 1e-12
+
+
+# ---------------------------------------------------------------- 1D solver
+@pytest.mark.parametrize("name,weights,beta", [("h_minimal_l1.json", 0, 1.0), ("h_psi_t.json", 1, 1.0),
+                                               ("h_psi_t07.json", 1, 0.7), ("h_psi_t15.json", 1, 1.5)])
+def test_h_solver_reference_golden(ctx, name, weights, beta):
+    from theses_code_gb300.solvers import HSolverBatch
+    g = json.load(open(os.path.join(G, name)))
+    N = g["N"]
+    p = dict(N=N, L=g["L"], tau=g["tau"], alpha=g["alpha"], weights=weights, beta=beta, kmodel=0,
+             kc=g["k"], kgam=0.0, cinv=20.0, gravity=1, al_left=1.0, bt_left=-g["uc"], u_right=g["Hbottom"])
+    U0 = np.zeros(N + 2)
+    U0[:N + 1] = g["U0"]
+    s = HSolverBatch(ctx, [p, p], g["steps"] + 1)
+    s.set_u([U0, U0])
+    s.calc_step(g["steps"])
+    u = s.get_u()
+    assert relmax(u[0], g["U"]) <= TOL_SOLVER
+    assert np.array_equal(u[0], u[1])
+
+
+def test_h_solver_caputo_1d_vs_oracle(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    p, U0 = workloads.caputo_1d(200, 0.8, 1.0, 1e-3)
+    steps = 300
+    s = HSolverBatch(ctx, [p], steps + 1)
+    s.set_u([U0])
+    s.calc_step(steps)
+    ref, _ = O.h_solve(p, U0, steps)
+    assert relmax(s.get_u()[0], ref) <= TOL_SOLVER
+
+
+def test_h_solver_psi_batch_vs_oracle(ctx):
+    """Ragged batch of psi-Caputo instances with D(u) = D0 exp(gamma u): each
+    instance matches the oracle run alone."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=6, seed=3, Nmin=17, Nmax=90, tau=2e-3)
+    steps = 60
+    s = HSolverBatch(ctx, params, steps + 1)
+    s.set_u(U0s)
+    s.calc_step(steps)
+    got = s.get_u()
+    for p, U0, g in zip(params, U0s, got):
+        ref, _ = O.h_solve(p, U0, steps)
+        assert relmax(g, ref) <= 1e-11, (p["alpha"], p["beta"])
+
+
+def test_h_solver_history_full_is_reported(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FhError
+    from theses_code_gb300.solvers import HSolverBatch
+    p, U0 = workloads.caputo_1d(10)
+    s = HSolverBatch(ctx, [p], 3)
+    s.set_u([U0])
+    s.calc_step(3)
+    with pytest.raises(FhError):
+        s.calc_step(1)
+
+
+# ---------------------------------------------------------------- 2D solver
+def test_tg_reference_golden(ctx):
+    from theses_code_gb300.solvers import TGSolver
+    g = json.load(open(os.path.join(G, "tg_adi.json")))
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+             C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+    s = TGSolver(ctx, p, g["steps"])
+    s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+    s.calc_step(g["steps"])
+    assert relmax(s.get_c(), g["C"]) <= TOL_SOLVER
+
+
+@pytest.mark.parametrize("sN,M,steps", [(64, 48, 40), (130, 97, 25)])
+def test_tg_vs_oracle(ctx, sN, M, steps):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(sN, M, alpha=0.7, tau=5e-4, d=0.1, seed=sN, C1=0.2, S=0.01)
+    s = TGSolver(ctx, p, steps)
+    s.set_state(V2, C0)
+    s.calc_step(steps)
+    ref, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(s.get_c(), ref) <= TOL_SOLVER
+
+
+def test_tg_psi_beta_vs_oracle(ctx):
+    """psi(t) = t^1.3: the factorization is rebuilt every step."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 33, alpha=0.6, tau=1e-3, seed=4, C1=0.1)
+    p["beta"] = 1.3
+    s = TGSolver(ctx, p, 20)
+    s.set_state(V2, C0)
+    s.calc_step(20)
+    ref, _ = O.tg_solve(p, V2, C0, 20)
+    assert relmax(s.get_c(), ref) <= 1e-11
+
+
+# ------------------------------------------------------------------ AB solve
+def test_ab_reference_golden(ctx):
+    """solve_and_check error of the reference run (with its own Ii)."""
+    from theses_code_gb300.solvers import ABSolver
+    s_ = json.load(open(os.path.join(G, "ab.json")))["solve"]
+    m, n, a = s_["m"], s_["n"], s_["alpha"]
+    tau = s_["T"] / n
+    lam = -a / (1 - a)
+    src = np.array([[(24.0 / (1 - a)) * (i * tau) ** 4 * O.mittag_leffler(a, 5.0, lam * (i * tau) ** a)
+                     for _ in range(m + 1)] for i in range(1, n + 1)])
+    ex = np.array([[(i * tau) ** 4 for _ in range(m + 1)] for i in range(1, n + 1)])
+    s = ABSolver(ctx, m, n, tau, a)
+    s.set_source(src, ex[:, 0].copy(), ex[:, -1].copy())
+    s.set_c(np.zeros(m + 1))
+    s.set_current_coef(s_["ii"])
+    err = 0.0
+    for i in range(n):
+        s.calc_step(1)
+        err += float(np.sum((s.get_c() - ex[i]) ** 2))
+    err /= (m + 1.0) * n
+    assert abs(err - s_["err"]) <= 1e-10 * s_["err"]
+
+
+def test_ab_vs_oracle(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import ABSolver
+    cfg, src, bl, br, C0 = workloads.ab_1d(m=256, alpha=0.6, tau=1e-3, seed=2)
+    n = 400
+    s = ABSolver(ctx, cfg["m"], n, cfg["tau"], cfg["alpha"])
+    s.set_source(src, bl, br)
+    s.set_c(C0)
+    s.calc_step(n)
+    w = O.ab_weights(n, cfg["tau"], cfg["alpha"])
+    srcs = np.repeat(src, n, axis=0)
+    ref, _ = O.ab_solve(cfg["m"], n, cfg["tau"], cfg["alpha"], w, srcs, np.zeros(n), np.zeros(n), C0)
+    assert relmax(s.get_c(), ref) <= TOL_SOLVER

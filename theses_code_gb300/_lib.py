@@ -1,0 +1,162 @@
+"""ctypes binding of libfhist.so (the C ABI declared in include/fhist.h).
+
+Loading fails loudly: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libfhist.so")
+
+FH_OK, FH_EINVAL, FH_ENOMEM, FH_ECUDA, FH_ENONFINITE, FH_ETIMEOUT, FH_ERANGE, FH_ENOTSUP = range(8)
+FH_W_L1, FH_W_PSI = 0, 1
+FH_K_CONST, FH_K_EXP = 0, 1
+FH_TG_FP64, FH_TG_BLOCKED = 0, 1
+FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS = 0, 1, 2
+
+_vp = C.c_void_p
+_dp = C.c_void_p  # device or host double*, passed as raw addresses
+_i, _ll, _d = C.c_int, C.c_longlong, C.c_double
+
+
+class HParams(C.Structure):
+    _fields_ = [("N", _i), ("L", _d), ("tau", _d), ("alpha", _d), ("weights", _i), ("beta", _d),
+                ("kmodel", _i), ("kc", _d), ("kgam", _d), ("cinv", _d), ("gravity", _i),
+                ("al_left", _d), ("bt_left", _d), ("u_right", _d)]
+
+
+class TGParams(C.Structure):
+    _fields_ = [("sN", _i), ("M", _i), ("tau", _d), ("alpha", _d), ("beta", _d), ("sigma", _d),
+                ("d", _d), ("C1", _d), ("S", _d), ("dL", _d), ("dLx", _d)]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "fh_version": (_i, []),
+    "fh_ctx_create": (_i, [_i, C.POINTER(_vp)]),
+    "fh_ctx_destroy": (_i, [_vp]),
+    "fh_last_error": (C.c_char_p, [_vp]),
+    "fh_ctx_sync": (_i, [_vp]),
+    "fh_ctx_set_stream": (_i, [_vp, _vp]),
+    "fh_ctx_get_stream": (_vp, [_vp]),
+    "fh_ctx_launch_count": (_ll, [_vp]),
+    "fh_ctx_profile": (_i, [_vp, _i]),
+    "fh_ctx_profile_read": (_i, [_vp, _i, C.POINTER(_d), C.POINTER(_ll)]),
+    "fh_weights_psi": (_i, [_vp, _i, _d, _d, _d, _d, _d, _d, _d, _dp]),
+    "fh_weights_l1": (_i, [_vp, _i, _d, _dp]),
+    "fh_weights_ab": (_i, [_vp, _i, _d, _d, _dp]),
+    "fh_mittag_leffler": (_i, [_vp, _i, _d, _d, _dp, _dp]),
+    "fh_history_sum": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
+    "fh_history_sum_layers": (_i, [_vp, _i, _ll, _dp, _dp, _ll, _dp]),
+    "fh_tridiag_batched": (_i, [_vp, _i, _i, _dp, _dp, _dp, _dp, _ll, _dp, _dp, _i, _dp, _dp, _ll]),
+    "fh_pcr_solver": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _i, _i]),
+    "fh_h_batch_create": (_i, [_vp, _i, C.POINTER(HParams), _i, C.POINTER(_vp)]),
+    "fh_h_batch_destroy": (_i, [_vp]),
+    "fh_h_batch_state_size": (_ll, [_vp]),
+    "fh_h_batch_set_u_host": (_i, [_vp, _dp]),
+    "fh_h_batch_get_u_host": (_i, [_vp, _dp]),
+    "fh_h_batch_step": (_i, [_vp, _i]),
+    "fh_h_batch_tstep": (_i, [_vp]),
+    "fh_tg_create": (_i, [_vp, C.POINTER(TGParams), _i, _i, C.POINTER(_vp)]),
+    "fh_tg_destroy": (_i, [_vp]),
+    "fh_tg_set_state_host": (_i, [_vp, _dp, _dp]),
+    "fh_tg_set_state": (_i, [_vp, _dp, _dp]),
+    "fh_tg_step": (_i, [_vp, _i]),
+    "fh_tg_get_c_host": (_i, [_vp, _dp]),
+    "fh_tg_field": (_vp, [_vp]),
+    "fh_tg_tstep": (_i, [_vp]),
+    "fh_ab_create": (_i, [_vp, _i, _i, _d, _d, C.POINTER(_vp)]),
+    "fh_ab_destroy": (_i, [_vp]),
+    "fh_ab_set_source_host": (_i, [_vp, _i, _dp, _dp, _dp]),
+    "fh_ab_set_c_host": (_i, [_vp, _dp]),
+    "fh_ab_set_current_coef": (_i, [_vp, _d]),
+    "fh_ab_step": (_i, [_vp, _i]),
+    "fh_ab_get_c_host": (_i, [_vp, _dp]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libfhist.so; raises if it is missing (build it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libfhist.so not built ({path}); run __graft_entry__.build()")
+    L = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+class FhError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libfhist error {code}: {msg}")
+        self.code = code
+
+
+def check(rc: int, ctx=None):
+    if rc != FH_OK:
+        L = load()
+        msg = L.fh_last_error(ctx)
+        raise FhError(rc, msg.decode() if msg else "")
+
+
+class Context:
+    """Owns an fh_ctx (one CUDA stream)."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        h = _vp()
+        check(L.fh_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if self.h:
+            self.L.fh_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        check(self.L.fh_ctx_sync(self.h), self.h)
+
+    @property
+    def stream(self) -> int:
+        return self.L.fh_ctx_get_stream(self.h) or 0
+
+    def set_stream(self, stream_handle: int):
+        check(self.L.fh_ctx_set_stream(self.h, _vp(stream_handle)), self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.L.fh_ctx_launch_count(self.h)
+
+    def profile(self, enable: bool):
+        check(self.L.fh_ctx_profile(self.h, int(bool(enable))), self.h)
+
+    def profile_read(self, kind: int):
+        ms, n = _d(0.0), _ll(0)
+        check(self.L.fh_ctx_profile_read(self.h, int(kind), C.byref(ms), C.byref(n)), self.h)
+        return ms.value, n.value
+
+    def call(self, name, *args):
+        rc = getattr(self.L, name)(self.h, *args)
+        check(rc, self.h)
+        return rc

@@ -1,0 +1,242 @@
+// fh_ab.cu -- 1D Atangana-Baleanu convection-diffusion solve of
+// MF_int_series.cpp:875-958 (solve_and_check, simple = 1): per step i
+//   Rp_j = (Ii/(1-a)) C_j + f_j - (1/(1-a)) sum_{tt<=i-2} dC_tt/tau * I(i-tt)
+//   A C_{j-1} + Bd C_j + Cc C_{j+1} = Rp_j, Dirichlet at both ends.
+// The lag weights I(.) are computed once on the device (fh_weights_ab); the
+// history stores dC_t/tau = (C^{t+1}-C^t)/tau per node.  The matrix is the same
+// every step, so its elimination coefficients are built once and every step
+// runs the two affine recurrences with one warp (see fh_linescan.cuh).
+#include "fh_internal.h"
+#include "fh_common.cuh"
+#include "fh_linescan.cuh"
+
+struct fh_ab_solver {
+  fh_ctx *ctx = nullptr;
+  int m = 0, max_steps = 0, step = 0, nrows = 0, max_splits = 1024;
+  long long P = 0;  // m+1 rounded up to even
+  double tau = 0, alpha = 0, A = 0, Bd = 0, Cc = 0;
+  fh_dbuf w, ii, al, den, C, D, W, part, S, src, bl, br;
+};
+
+// al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
+__global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__restrict__ al, double *__restrict__ den) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double a = 0.0;
+  al[0] = 0.0;
+  den[0] = 1.0;
+  for (int j = 1; j <= m; ++j) {
+    const double d = Bd - A * a;
+    a = Cc / d;
+    al[j] = a;
+    den[j] = d;
+  }
+}
+
+// W[tt] = w[i - tt], tt = 0..i-2
+__global__ void k_ab_stepweights(int i, const double *__restrict__ w, double *__restrict__ W) {
+  const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tt < i - 1) W[tt] = w[i - tt];
+}
+
+__global__ void k_ab_line(int m, double oma, double A, const double *__restrict__ ii, const double *__restrict__ al,
+                          const double *__restrict__ den, const double *__restrict__ src, const double *__restrict__ blp,
+                          const double *__restrict__ brp, double *C, const double *__restrict__ S,
+                          double *__restrict__ Dnew, double tau) {
+  extern __shared__ double sm[];
+  double *rp = sm, *bt = sm + (m + 1);
+  const int lane = threadIdx.x & 31;
+  const double cI = ii[0] / oma;  // Ii/(1-a)
+  const double bl = blp[0], br = brp[0];
+  // forward: bt[j] = (Rp_j - A bt[j-1]) / den_j, j = 1..m
+  const int ch = (m + 31) / 32;
+  const int f0 = 1 + lane * ch, f1 = min(m + 1, f0 + ch);
+  fh_aff F{1.0, 0.0};
+  for (int j = f0; j < f1; ++j) {
+    double r = cI * C[j] + src[j];
+    if (S) r -= S[j] / oma;  // MF_intF_simple returns ret/(1-a)
+    rp[j] = r;
+    const double dj = den[j];
+    F = fh_aff_compose(fh_aff{-A / dj, r / dj}, F);
+  }
+  const fh_aff Pf = fh_warp_exclusive_affine(F);
+  double b = fma(Pf.a, bl, Pf.b);
+  for (int j = f0; j < f1; ++j) {
+    b = (rp[j] - A * b) / den[j];
+    bt[j] = b;
+  }
+  if (lane == 0) bt[0] = bl;
+  __syncwarp();
+  // backward: C[j] = bt[j] - al[j] C[j+1], j = m-1..0, C[m] = br
+  const int chb = (m + 31) / 32;
+  const int b0 = lane * chb, b1 = min(m, b0 + chb);
+  fh_aff G{1.0, 0.0};
+  for (int j = b1 - 1; j >= b0; --j) G = fh_aff_compose(fh_aff{-al[j], bt[j]}, G);
+  const fh_aff Pb = fh_warp_exclusive_affine_rev(G);
+  double c = fma(Pb.a, br, Pb.b);
+  for (int j = b1 - 1; j >= b0; --j) {
+    c = bt[j] - al[j] * c;
+    const double old = C[j];
+    C[j] = c;
+    if (Dnew) Dnew[j] = (c - old) / tau;
+  }
+  if (lane == 0) {
+    const double old = C[m];
+    C[m] = br;
+    if (Dnew) Dnew[m] = (br - old) / tau;
+  }
+}
+
+__global__ void k_reduce_splits(int splits, long long P, const double *__restrict__ part, long long ldpart,
+                                double *__restrict__ S) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double acc = 0.0;
+  for (int s = 0; s < splits; ++s) acc += part[(long long)s * ldpart + p];
+  S[p] = acc;
+}
+
+static int ab_one_step(fh_ab_solver *s) {
+  fh_ctx *ctx = s->ctx;
+  const int i = s->step + 1;  // reference step index (1-based)
+  const int K = i - 1;        // history entries dC_0 .. dC_{i-2}
+  const int row = (i - 1 < s->nrows - 1) ? i - 1 : s->nrows - 1;
+  int rc;
+  const double *S = nullptr;
+  if (K > 0) {
+    k_ab_stepweights<<<(unsigned)fh_ceil_div(K, 256), 256, 0, ctx->stream>>>(i, s->w.as<double>(), s->W.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_ab_stepweights"))) return rc;
+    int splits, kchunk;
+    fh_hist_plan(s->P, K, s->max_splits, &splits, &kchunk);
+    if ((rc = fh_launch_hist_sum_partials(ctx, 1, K, s->P, s->W.as<double>(), s->max_steps + 1, s->D.as<double>(),
+                                          s->P, splits, kchunk, s->part.as<double>(), s->P)))
+      return rc;
+    k_reduce_splits<<<(unsigned)fh_ceil_div(s->P, 256), 256, 0, ctx->stream>>>(splits, s->P, s->part.as<double>(),
+                                                                               s->P, s->S.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_reduce_splits"))) return rc;
+    S = s->S.as<double>();
+  }
+  const size_t smem = sizeof(double) * 2 * (size_t)(s->m + 1);
+  k_ab_line<<<1, 32, smem, ctx->stream>>>(s->m, 1.0 - s->alpha, s->A, s->ii.as<double>(), s->al.as<double>(),
+                                          s->den.as<double>(), s->src.as<double>() + (long long)row * (s->m + 1),
+                                          s->bl.as<double>() + row, s->br.as<double>() + row, s->C.as<double>(), S,
+                                          s->D.as<double>() + (long long)s->step * s->P, s->tau);
+  if ((rc = fh_after_launch(ctx, "k_ab_line"))) return rc;
+  s->step++;
+  return FH_OK;
+}
+
+extern "C" {
+
+int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh_ab_solver **out) {
+  FH_REQUIRE(ctx, ctx && out, FH_EINVAL, "fh_ab_create: null argument");
+  *out = nullptr;
+  FH_REQUIRE(ctx, m >= 2 && m <= 12000 && max_steps >= 1 && tau > 0 && alpha > 0 && alpha < 1, FH_EINVAL,
+             "fh_ab_create: need 2 <= m <= 12000, max_steps >= 1, tau > 0, 0 < alpha < 1");
+  fh_ab_solver *s = new fh_ab_solver();
+  s->ctx = ctx;
+  s->m = m;
+  s->max_steps = max_steps;
+  s->tau = tau;
+  s->alpha = alpha;
+  s->P = ((long long)m + 1 + 1) & ~1LL;
+  const double h = 1.0 / m;
+  s->A = -(1.0 / (h * h)) - (1.0 / (2.0 * h));
+  s->Cc = -(1.0 / (h * h)) + (1.0 / (2.0 * h));
+  int rc;
+  const size_t fld = sizeof(double) * (size_t)s->P;
+  if ((rc = fh_alloc(ctx, s->w, sizeof(double) * (size_t)(max_steps + 2))) || (rc = fh_alloc(ctx, s->ii, 16)) ||
+      (rc = fh_alloc(ctx, s->al, fld)) || (rc = fh_alloc(ctx, s->den, fld)) || (rc = fh_alloc(ctx, s->C, fld)) ||
+      (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
+      (rc = fh_alloc(ctx, s->W, sizeof(double) * (size_t)(max_steps + 1))) ||
+      (rc = fh_alloc(ctx, s->part, fld * (size_t)s->max_splits, false)) || (rc = fh_alloc(ctx, s->S, fld))) {
+    delete s;
+    return rc;
+  }
+  if ((rc = fh_weights_ab(ctx, max_steps + 1, tau, alpha, s->w.as<double>()))) {
+    delete s;
+    return rc;
+  }
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->ii.p, s->w.p, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  // Bd = Ii/(1-a) + 2/h^2 with Ii from the device weights
+  double ii_h = 0.0;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(&ii_h, s->w.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->Bd = (ii_h / (1.0 - alpha)) + (2.0 / (h * h));
+  k_ab_factor<<<1, 1, 0, ctx->stream>>>(m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>());
+  if ((rc = fh_after_launch(ctx, "k_ab_factor"))) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return FH_OK;
+}
+
+int fh_ab_destroy(fh_ab_solver *s) {
+  if (!s) return FH_OK;
+  if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
+  delete s;
+  return FH_OK;
+}
+
+int fh_ab_set_source_host(fh_ab_solver *s, int nrows, const double *src_host, const double *bl_host,
+                          const double *br_host) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, nrows >= 1 && src_host && bl_host && br_host, FH_EINVAL, "fh_ab_set_source_host: bad args");
+  int rc;
+  if ((rc = fh_alloc(ctx, s->src, sizeof(double) * (size_t)nrows * (s->m + 1), false)) ||
+      (rc = fh_alloc(ctx, s->bl, sizeof(double) * nrows, false)) ||
+      (rc = fh_alloc(ctx, s->br, sizeof(double) * nrows, false)))
+    return rc;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->src.p, src_host, sizeof(double) * (size_t)nrows * (s->m + 1),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->bl.p, bl_host, sizeof(double) * nrows, cudaMemcpyHostToDevice, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->br.p, br_host, sizeof(double) * nrows, cudaMemcpyHostToDevice, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->nrows = nrows;
+  return FH_OK;
+}
+
+int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, C_host, FH_EINVAL, "fh_ab_set_c_host: null pointer");
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, sizeof(double) * (s->m + 1), cudaMemcpyHostToDevice, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->step = 0;
+  return FH_OK;
+}
+
+int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->ii.p, &Ii, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const double h = 1.0 / s->m;
+  s->Bd = (Ii / (1.0 - s->alpha)) + (2.0 / (h * h));
+  k_ab_factor<<<1, 1, 0, ctx->stream>>>(s->m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>());
+  return fh_after_launch(ctx, "k_ab_factor");
+}
+
+int fh_ab_step(fh_ab_solver *s, int nsteps) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, s->nrows >= 1, FH_EINVAL, "fh_ab_step: source not set");
+  FH_REQUIRE(ctx, nsteps >= 0 && s->step + nsteps <= s->max_steps, FH_ENOMEM, "fh_ab_step: history full");
+  for (int n = 0; n < nsteps; ++n) {
+    int rc = ab_one_step(s);
+    if (rc) return rc;
+  }
+  return FH_OK;
+}
+
+int fh_ab_get_c_host(fh_ab_solver *s, double *C_host) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, C_host, FH_EINVAL, "fh_ab_get_c_host: null pointer");
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(C_host, s->C.p, sizeof(double) * (s->m + 1), cudaMemcpyDeviceToHost, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,336 @@
+// fh_h.cu -- batched 1D H_solver path (mt_minimal.cpp:276-1048 and
+// mt_psi_caputo.cpp:369-1507 with gamma = 1): per step
+//   1. k_h_weights      per-instance history weights and current weight
+//   2. k_hist_tiles     history sum per instance segment (split-K partials)
+//   3. k_h_line         one thread per instance: coefficients, right part,
+//                       Thomas sweep, back substitution, history append
+//
+// All instances advance in lock step.  The concatenated state holds each
+// instance's N_i+2 nodes in a segment padded to an even length; the history
+// stores layer differences d_t = layer[t+1] - layer[t] at slot t for the
+// concatenated state (layer-major), so the history loads coalesce across
+// neighbouring nodes and instances.
+#include <vector>
+
+#include "fh_internal.h"
+#include "fh_common.cuh"
+#include "fh_weights.cuh"
+
+struct fh_h_dev_inst {
+  int N, weights, kmodel, gravity;
+  long long off;  // segment start in the concatenated state
+  double dL, Dg, Da, tau, alpha, beta, kc, kgam, cinv, al_left, bt_left, u_right;
+};
+
+struct fh_h_tile {
+  int inst;
+  int start;  // first node of the tile inside the segment
+  int len;    // nodes in the tile (even)
+};
+
+struct fh_h_batch {
+  fh_ctx *ctx = nullptr;
+  int n = 0, max_steps = 0, tstep = 1, nsaved = 0, max_splits = 8, max_weights = 0;
+  long long Ptot = 0;
+  std::vector<fh_h_params> hp;
+  std::vector<long long> off;
+  std::vector<fh_h_tile> tiles;
+  fh_dbuf inst, tl, U, D, W, wc, part, Al, Bt;
+};
+
+static constexpr int kTileThreads = 256;  // 512 nodes per tile
+
+// ------------------------------------------------------------------ kernels
+
+// Row b of W: the weights of instance b for the history slots t = 0..os-2.
+// The reference's t = 0 term multiplies layer1 - layer1 (its layer pointer
+// starts at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
+__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
+                            int ldw, double *__restrict__ wc) {
+  const int b = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const fh_h_dev_inst I = inst[b];
+  if (t < os - 1) {
+    double w;
+    if (t == 0)
+      w = 0.0;
+    else if (I.weights == FH_W_L1)
+      w = pow((double)(os - t), 1.0 - I.alpha) - pow((double)(os - t - 1), 1.0 - I.alpha);
+    else
+      w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
+    W[(long long)b * ldw + t] = w;
+  }
+  if (t == 0) {
+    wc[b] = (I.weights == FH_W_L1)
+                ? 1.0
+                : fh_psi_int((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) *
+                      (1 - I.alpha);
+  }
+}
+
+// part[s][p] = sum_{k in split s} W[inst][k] * D[k][p] over one tile of one instance.
+__global__ void __launch_bounds__(kTileThreads) k_hist_tiles(const fh_h_tile *__restrict__ tiles,
+                                                             const fh_h_dev_inst *__restrict__ inst,
+                                                             const double *__restrict__ D, long long ldd, int K,
+                                                             const double *__restrict__ W, int ldw, int kchunk,
+                                                             double *__restrict__ part, long long ldpart) {
+  extern __shared__ double ws[];
+  const fh_h_tile T = tiles[blockIdx.x];
+  const int s = blockIdx.y;
+  const int k0 = s * kchunk;
+  const int nk = min(K, k0 + kchunk) - k0;
+  const double *wrow = W + (long long)T.inst * ldw + k0;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) ws[i] = wrow[i];
+  __syncthreads();
+  const int q = threadIdx.x * 2;
+  if (q >= T.len) return;
+  const long long p = inst[T.inst].off + T.start + q;
+  double a0 = 0.0, a1 = 0.0;
+  const double *d = D + (long long)k0 * ldd + p;
+  int k = 0;
+  for (; k + 4 <= nk; k += 4) {
+    const double2 v0 = fh_ld_stream2(d), v1 = fh_ld_stream2(d + ldd);
+    const double2 v2 = fh_ld_stream2(d + 2 * ldd), v3 = fh_ld_stream2(d + 3 * ldd);
+    d += 4 * ldd;
+    a0 = fma(ws[k], v0.x, a0);
+    a1 = fma(ws[k], v0.y, a1);
+    a0 = fma(ws[k + 1], v1.x, a0);
+    a1 = fma(ws[k + 1], v1.y, a1);
+    a0 = fma(ws[k + 2], v2.x, a0);
+    a1 = fma(ws[k + 2], v2.y, a1);
+    a0 = fma(ws[k + 3], v3.x, a0);
+    a1 = fma(ws[k + 3], v3.y, a1);
+  }
+  for (; k < nk; ++k) {
+    const double2 v = fh_ld_stream2(d);
+    d += ldd;
+    a0 = fma(ws[k], v.x, a0);
+    a1 = fma(ws[k], v.y, a1);
+  }
+  double2 o;
+  o.x = a0;
+  o.y = a1;
+  *reinterpret_cast<double2 *>(part + (long long)s * ldpart + p) = o;
+}
+
+__device__ __forceinline__ double fh_h_K(const fh_h_dev_inst &I, double u) {
+  return I.kmodel == FH_K_CONST ? I.kc : I.kc * exp(I.kgam * u);
+}
+
+// H_solver::U1 for one instance per thread: al1, Om1 (time part from the
+// partial sums), bt1, bottom Dirichlet, back substitution, history append.
+__global__ void k_h_line(const fh_h_dev_inst *__restrict__ inst, int n, double *__restrict__ U,
+                         const double *__restrict__ wc, const double *__restrict__ part, long long ldpart, int splits,
+                         double *__restrict__ Al, double *__restrict__ Bt, double *__restrict__ Dnew, int append) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const fh_h_dev_inst I = inst[b];
+  double *u = U + I.off;
+  double *al = Al + I.off, *bt = Bt + I.off;
+  const int N = I.N;
+  const double w0 = wc[b];
+  const double DaW = I.Da * w0;
+  double alv = I.al_left, btv = I.bt_left;
+  al[1] = alv;
+  bt[1] = btv;
+  double Km = fh_h_K(I, u[0]), Kc = fh_h_K(I, u[1]);
+  for (int i = 1; i < N; ++i) {
+    const double Kp = fh_h_K(I, u[i + 1]);
+    const double A = I.Dg * Km * I.cinv;
+    const double B = I.Dg * Kp * I.cinv;
+    const double R = I.cinv * (Kp + Km) * I.Dg + DaW;
+    double om = -DaW * u[i];
+    if (I.gravity) om += (Kc - Km) / I.dL;
+    double ts = 0.0;
+    for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + I.off + i];
+    om += I.Da * ts;
+    const double aln = B / (R - A * alv);
+    const double btn = (aln / B) * (A * btv - om);
+    al[i + 1] = aln;
+    bt[i + 1] = btn;
+    alv = aln;
+    btv = btn;
+    Km = Kc;
+    Kc = Kp;
+  }
+  double un = I.u_right;
+  double old = u[N];
+  u[N] = un;
+  if (append) Dnew[I.off + N] = un - old;
+  for (int i = N - 1; i >= 0; --i) {
+    un = al[i + 1] * un + bt[i + 1];
+    old = u[i];
+    u[i] = un;
+    if (append) Dnew[I.off + i] = un - old;
+  }
+  old = u[N + 1];
+  u[N + 1] = u[N];
+  if (append) Dnew[I.off + N + 1] = u[N + 1] - old;
+}
+
+// ------------------------------------------------------------------- host
+
+static int h_one_step(fh_h_batch *B) {
+  fh_ctx *ctx = B->ctx;
+  const int os = B->nsaved;
+  const int K = os >= 2 ? os - 1 : 0;
+  int rc;
+  dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, 128), (unsigned)B->n);
+  k_h_weights<<<gw, 128, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
+                                           B->max_weights, B->wc.as<double>());
+  if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
+  int splits = 0, kchunk = 0;
+  if (K > 0) {
+    fh_hist_plan(B->Ptot, K, B->max_splits, &splits, &kchunk);
+    // tiles are per instance: keep the CTA count close to the generic plan
+    dim3 g((unsigned)B->tiles.size(), (unsigned)splits);
+    const size_t smem = sizeof(double) * (size_t)kchunk;
+    FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
+    k_hist_tiles<<<g, kTileThreads, smem, ctx->stream>>>(B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
+                                                         B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
+                                                         B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+    if ((rc = fh_after_launch(ctx, "k_hist_tiles"))) return rc;
+  }
+  const int append = os >= 1;
+  double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
+  k_h_line<<<(unsigned)fh_ceil_div(B->n, 64), 64, 0, ctx->stream>>>(
+      B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wc.as<double>(), B->part.as<double>(), B->Ptot,
+      splits, B->Al.as<double>(), B->Bt.as<double>(), Dnew, append);
+  if ((rc = fh_after_launch(ctx, "k_h_line"))) return rc;
+  B->nsaved++;
+  B->tstep++;
+  return FH_OK;
+}
+
+extern "C" {
+
+int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, int max_steps, fh_h_batch **out) {
+  FH_REQUIRE(ctx, ctx && params_host && out, FH_EINVAL, "fh_h_batch_create: null argument");
+  *out = nullptr;
+  FH_REQUIRE(ctx, ninst >= 1 && max_steps >= 1, FH_EINVAL, "fh_h_batch_create: need ninst >= 1, max_steps >= 1");
+  fh_h_batch *B = new fh_h_batch();
+  B->ctx = ctx;
+  B->n = ninst;
+  B->max_steps = max_steps;
+  B->max_weights = max_steps + 1;
+  B->hp.assign(params_host, params_host + ninst);
+  std::vector<fh_h_dev_inst> di(ninst);
+  long long off = 0;
+  for (int b = 0; b < ninst; ++b) {
+    const fh_h_params &p = params_host[b];
+    if (!(p.N >= 2 && p.N <= (1 << 20) && p.L > 0 && p.tau > 0 && p.alpha > 0 && p.alpha < 1 &&
+          (p.weights == FH_W_L1 || p.weights == FH_W_PSI) && (p.kmodel == FH_K_CONST || p.kmodel == FH_K_EXP) &&
+          (p.weights == FH_W_L1 || p.beta > 0))) {
+      delete B;
+      return fh_set_error(ctx, FH_EINVAL, "fh_h_batch_create: bad parameters for instance %d", b);
+    }
+    fh_h_dev_inst &I = di[b];
+    I.N = p.N;
+    I.weights = p.weights;
+    I.kmodel = p.kmodel;
+    I.gravity = p.gravity;
+    I.off = off;
+    I.dL = p.L / p.N;
+    I.Dg = pow(I.dL, -2.0);
+    I.Da = p.weights == FH_W_L1 ? pow(p.tau, -p.alpha) / tgamma(2.0 - p.alpha)
+                                : pow(p.tau, -1.0) / tgamma(2.0 - p.alpha);
+    I.tau = p.tau;
+    I.alpha = p.alpha;
+    I.beta = p.beta;
+    I.kc = p.kc;
+    I.kgam = p.kgam;
+    I.cinv = p.cinv;
+    I.al_left = p.al_left;
+    I.bt_left = p.bt_left;
+    I.u_right = p.u_right;
+    B->off.push_back(off);
+    const int seg = ((p.N + 2) + 1) & ~1;
+    for (int st = 0; st < seg; st += 2 * kTileThreads) B->tiles.push_back({b, st, seg - st < 2 * kTileThreads ? seg - st : 2 * kTileThreads});
+    off += seg;
+  }
+  B->Ptot = off;
+  int rc;
+  const size_t st = sizeof(double) * (size_t)B->Ptot;
+  if ((rc = fh_alloc(ctx, B->inst, sizeof(fh_h_dev_inst) * ninst, false)) ||
+      (rc = fh_alloc(ctx, B->tl, sizeof(fh_h_tile) * B->tiles.size(), false)) || (rc = fh_alloc(ctx, B->U, st)) ||
+      (rc = fh_alloc(ctx, B->Al, st)) || (rc = fh_alloc(ctx, B->Bt, st)) ||
+      (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
+      (rc = fh_alloc(ctx, B->W, sizeof(double) * (size_t)ninst * B->max_weights)) ||
+      (rc = fh_alloc(ctx, B->wc, sizeof(double) * ninst)) ||
+      (rc = fh_alloc(ctx, B->part, st * (size_t)B->max_splits, false))) {
+    delete B;
+    return rc;
+  }
+  cudaError_t e1 = cudaMemcpyAsync(B->inst.p, di.data(), sizeof(fh_h_dev_inst) * ninst, cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e2 = cudaMemcpyAsync(B->tl.p, B->tiles.data(), sizeof(fh_h_tile) * B->tiles.size(), cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    delete B;
+    return fh_set_error(ctx, FH_ECUDA, "fh_h_batch_create: upload failed");
+  }
+  *out = B;
+  return FH_OK;
+}
+
+int fh_h_batch_destroy(fh_h_batch *b) {
+  if (!b) return FH_OK;
+  if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return FH_OK;
+}
+
+long long fh_h_batch_state_size(const fh_h_batch *b) {
+  if (!b) return -1;
+  long long s = 0;
+  for (const auto &p : b->hp) s += p.N + 2;
+  return s;
+}
+
+int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, U_host, FH_EINVAL, "fh_h_batch_set_u_host: null pointer");
+  long long src = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const size_t cnt = (size_t)b->hp[i].N + 2;
+    FH_CUDA_TRY(ctx, cudaMemcpyAsync(b->U.as<double>() + b->off[i], U_host + src, sizeof(double) * cnt,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    src += (long long)cnt;
+  }
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  b->tstep = 1;
+  b->nsaved = 0;
+  return FH_OK;
+}
+
+int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, U_host, FH_EINVAL, "fh_h_batch_get_u_host: null pointer");
+  long long dst = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const size_t cnt = (size_t)b->hp[i].N + 2;
+    FH_CUDA_TRY(ctx, cudaMemcpyAsync(U_host + dst, b->U.as<double>() + b->off[i], sizeof(double) * cnt,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    dst += (long long)cnt;
+  }
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FH_OK;
+}
+
+int fh_h_batch_step(fh_h_batch *b, int nsteps) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_h_batch_step: nsteps < 0");
+  FH_REQUIRE(ctx, b->nsaved + nsteps <= b->max_steps, FH_ENOMEM, "fh_h_batch_step: history full (%d + %d > %d)",
+             b->nsaved, nsteps, b->max_steps);
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = h_one_step(b);
+    if (rc) return rc;
+  }
+  return FH_OK;
+}
+
+int fh_h_batch_tstep(const fh_h_batch *b) { return b ? b->tstep : -1; }
+
+}  // extern "C"

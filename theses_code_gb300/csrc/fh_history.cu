@@ -1,0 +1,180 @@
+// fh_history.cu -- FP64 history sums S_m[p] = sum_k W[m][k] * D[k][p].
+//
+// Layout: D is layer-major (layer k at D + k*ldd), point index contiguous, so a
+// warp reads 32 consecutive double2 (512 B) per layer.  Each CTA owns a tile of
+// 2*blockDim points and one K-chunk ("split"); it stages its chunk of weights
+// in shared memory and writes one partial sum per (split, m, point).  The
+// consumer adds the partials in split order, so results do not depend on
+// scheduling (no atomics).
+//
+// Cost model: every element of D is read once per step and used in M FMAs.
+// On GB300 the FP64 pipe, not HBM, bounds this loop once M >= 1.
+#include "fh_internal.h"
+#include "fh_common.cuh"
+
+static constexpr int kHistThreads = 256;
+
+template <int M>
+__global__ void __launch_bounds__(kHistThreads) k_hist_sum(const double *__restrict__ D, long long ldd, long long P,
+                                                           int K, const double *__restrict__ W, int ldw, int kchunk,
+                                                           double *__restrict__ part, long long ldpart) {
+  extern __shared__ double ws[];  // [M][kchunk]
+  const int s = blockIdx.y;
+  const int k0 = s * kchunk;
+  const int nk = min(K, k0 + kchunk) - k0;
+  for (int i = threadIdx.x; i < M * nk; i += blockDim.x) {
+    const int m = i / nk, k = i - m * nk;
+    ws[m * kchunk + k] = W[(long long)m * ldw + k0 + k];
+  }
+  __syncthreads();
+  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (p >= P) return;
+  double acc0[M], acc1[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) acc0[m] = acc1[m] = 0.0;
+  const double *d = D + (long long)k0 * ldd + p;
+  int k = 0;
+  for (; k + 4 <= nk; k += 4) {
+    const double2 v0 = fh_ld_stream2(d);
+    const double2 v1 = fh_ld_stream2(d + ldd);
+    const double2 v2 = fh_ld_stream2(d + 2 * ldd);
+    const double2 v3 = fh_ld_stream2(d + 3 * ldd);
+    d += 4 * ldd;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const double *wm = ws + m * kchunk + k;
+      acc0[m] = fma(wm[0], v0.x, acc0[m]);
+      acc1[m] = fma(wm[0], v0.y, acc1[m]);
+      acc0[m] = fma(wm[1], v1.x, acc0[m]);
+      acc1[m] = fma(wm[1], v1.y, acc1[m]);
+      acc0[m] = fma(wm[2], v2.x, acc0[m]);
+      acc1[m] = fma(wm[2], v2.y, acc1[m]);
+      acc0[m] = fma(wm[3], v3.x, acc0[m]);
+      acc1[m] = fma(wm[3], v3.y, acc1[m]);
+    }
+  }
+  for (; k < nk; ++k) {
+    const double2 v = fh_ld_stream2(d);
+    d += ldd;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      acc0[m] = fma(ws[m * kchunk + k], v.x, acc0[m]);
+      acc1[m] = fma(ws[m * kchunk + k], v.y, acc1[m]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    double2 o;
+    o.x = acc0[m];
+    o.y = acc1[m];
+    *reinterpret_cast<double2 *>(part + ((long long)s * M + m) * ldpart + p) = o;
+  }
+}
+
+// out[m*ldS + p] = sum_s part[(s*M+m)*ldpart + p]
+__global__ void k_hist_reduce(int M, int splits, long long P, const double *__restrict__ part, long long ldpart,
+                              double *__restrict__ S, long long ldS) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  for (int m = 0; m < M; ++m) {
+    double acc = 0.0;
+    for (int s = 0; s < splits; ++s) acc += part[((long long)s * M + m) * ldpart + p];
+    S[(long long)m * ldS + p] = acc;
+  }
+}
+
+// Layer form: S[p] = sum_t w[t] * (H[(t+1) ldh + p] - H[t ldh + p]) (reference Sum kernel semantics).
+__global__ void k_hist_sum_layers(int K, long long P, const double *__restrict__ w, const double *__restrict__ H,
+                                  long long ldh, double *__restrict__ S) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double acc = 0.0;
+  double prev = H[p];
+  for (int t = 0; t < K; ++t) {
+    const double cur = __ldcs(H + (long long)(t + 1) * ldh + p);
+    acc = fma(__ldg(w + t), cur - prev, acc);
+    prev = cur;
+  }
+  S[p] = acc;
+}
+
+void fh_hist_plan(long long P, int K, int max_splits, int *splits, int *kchunk) {
+  // Enough CTAs for ~3 waves of 8 resident 256-thread CTAs on 152 SMs, but at
+  // least 32 layers per split so the partial traffic stays small.
+  const long long tiles = fh_ceil_div(P, 2LL * kHistThreads);
+  const long long target = 3LL * 152 * 8;
+  int s = (int)fh_ceil_div(target, tiles);
+  if (s > max_splits) s = max_splits;
+  if (s > K / 32) s = K / 32;
+  if (s < 1) s = 1;
+  int kc = (int)fh_ceil_div(K, s);
+  kc = (int)fh_ceil_div(kc, 4) * 4;
+  s = (int)fh_ceil_div(K, kc);
+  *splits = s;
+  *kchunk = kc;
+}
+
+int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw, const double *D,
+                                long long ldd, int splits, int kchunk, double *part, long long ldpart) {
+  if (K <= 0 || P <= 0) return FH_OK;
+  dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
+  const size_t smem = sizeof(double) * (size_t)M * (size_t)kchunk;
+  if (smem > 48 * 1024) {
+    // large chunks: opt in to more dynamic shared memory once per kernel
+    static bool attr_set[3] = {false, false, false};
+    if (!attr_set[M]) {
+      if (M == 1) cudaFuncSetAttribute(k_hist_sum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      else cudaFuncSetAttribute(k_hist_sum<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_set[M] = true;
+    }
+    FH_REQUIRE(ctx, smem <= 200 * 1024, FH_EINVAL, "history chunk too large (%d layers)", kchunk);
+  }
+  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  if (M == 1)
+    k_hist_sum<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+  else
+    k_hist_sum<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  return fh_after_launch(ctx, "k_hist_sum");
+}
+
+extern "C" {
+
+int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw, const double *D, long long ldd,
+                   double *S, long long ldS) {
+  FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
+  FH_REQUIRE(ctx, M == 1 || M == 2, FH_EINVAL, "fh_history_sum: M must be 1 or 2");
+  FH_REQUIRE(ctx, K >= 0 && P >= 0 && ldS >= P && ldd >= P, FH_EINVAL, "fh_history_sum: bad sizes");
+  FH_REQUIRE(ctx, (P % 2) == 0 && (ldd % 2) == 0, FH_EINVAL, "fh_history_sum: P and ldd must be even");
+  FH_REQUIRE(ctx, ((uintptr_t)D % 16) == 0, FH_EINVAL, "fh_history_sum: D must be 16-byte aligned");
+  if (P == 0) return FH_OK;
+  FH_REQUIRE(ctx, S && (K == 0 || (W && D && ldw >= K)), FH_EINVAL, "fh_history_sum: null pointer");
+  if (K == 0) {
+    for (int m = 0; m < M; ++m)
+      FH_CUDA_TRY(ctx, cudaMemsetAsync(S + (long long)m * ldS, 0, sizeof(double) * P, ctx->stream));
+    return FH_OK;
+  }
+  int splits, kchunk;
+  fh_hist_plan(P, K, 16, &splits, &kchunk);
+  fh_dbuf part;
+  int rc = fh_alloc(ctx, part, sizeof(double) * (size_t)splits * M * (size_t)P, false);
+  if (rc) return rc;
+  if ((rc = fh_launch_hist_sum_partials(ctx, M, K, P, W, ldw, D, ldd, splits, kchunk, part.as<double>(), P)))
+    return rc;
+  k_hist_reduce<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(M, splits, P, part.as<double>(), P, S, ldS);
+  if ((rc = fh_after_launch(ctx, "k_hist_reduce"))) return rc;
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // before the scratch buffer is released
+  return FH_OK;
+}
+
+int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H, long long ldh,
+                          double *S) {
+  FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
+  FH_REQUIRE(ctx, K >= 0 && P >= 0 && ldh >= P, FH_EINVAL, "fh_history_sum_layers: bad sizes");
+  if (P == 0) return FH_OK;
+  FH_REQUIRE(ctx, S && H && (K == 0 || w), FH_EINVAL, "fh_history_sum_layers: null pointer");
+  k_hist_sum_layers<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(K, P, w, H, ldh, S);
+  return fh_after_launch(ctx, "k_hist_sum_layers");
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// fh_linescan.cuh -- one warp solves one grid line whose Thomas factorization
+// (the alpha coefficients and the pivots) is already known.  Both remaining
+// recurrences are affine maps:
+//   forward   Bt[i+1] = g_i (A_i Bt[i] - Om_i)          i = 1..N-1
+//   backward  u_i     = Al[i+1] u_{i+1} + Bt[i+1]       i = N-1..0
+// Each lane composes the maps of a contiguous chunk, a warp scan gives every
+// lane its starting value, and the lane then walks its chunk with the
+// reference's own arithmetic.  The serial chain per line drops from ~2N to
+// ~2N/32 + 10 dependent steps.
+#pragma once
+#include "fh_common.cuh"
+
+// Reverse exclusive scan: lane l receives G_{l+1} o G_{l+2} o ... o G_31
+// (identity for lane 31), i.e. the maps of all higher lanes applied first.
+__device__ __forceinline__ fh_aff fh_warp_exclusive_affine_rev(fh_aff f) {
+  const unsigned lane = threadIdx.x & 31u;
+  fh_aff g = f;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    double pa = __shfl_down_sync(0xffffffffu, g.a, d);
+    double pb = __shfl_down_sync(0xffffffffu, g.b, d);
+    if (lane + d < 32u) g = fh_aff_compose(g, fh_aff{pa, pb});
+  }
+  double ea = __shfl_down_sync(0xffffffffu, g.a, 1);
+  double eb = __shfl_down_sync(0xffffffffu, g.b, 1);
+  if (lane == 31u) {
+    ea = 1.0;
+    eb = 0.0;
+  }
+  return fh_aff{ea, eb};
+}
+
+// Line accessor contract (all lanes call with the same line):
+//   double om(int i)      right part Om_i, i = 1..N-1
+//   double A(int i)       sub-diagonal A_i
+//   double g(int i)       pivot factor g_i = Al[i+1]/B_i (or 1/(R_i - A_i Al_i) when Al[i+1] = B_i = 0)
+//   double al(int i)      Al[i+1] for i = 1..N-1
+//   void   store(int i, double u)   writes u_i, i = 0..N+1
+// buf: per-warp shared scratch of N+1 doubles.
+template <class Line>
+__device__ __forceinline__ void fh_line_solve_cached(const Line &L, int N, double al1, double bt1, double *buf) {
+  const int lane = threadIdx.x & 31;
+  // ---- forward: Bt[i+1] for i = 1..N-1, stored at buf[i]; buf[0] = Bt[1]
+  const int nf = N - 1;
+  const int chf = (nf + 31) / 32;
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  fh_aff F{1.0, 0.0};
+  for (int i = f0; i < f1; ++i) {
+    const double om = L.om(i), a = L.A(i), g = L.g(i);
+    buf[i] = om;
+    F = fh_aff_compose(fh_aff{g * a, -g * om}, F);
+  }
+  const fh_aff Pf = fh_warp_exclusive_affine(F);
+  double bt = fma(Pf.a, bt1, Pf.b);
+  for (int i = f0; i < f1; ++i) {
+    bt = L.g(i) * (L.A(i) * bt - buf[i]);
+    buf[i] = bt;
+  }
+  if (lane == 0) buf[0] = bt1;
+  __syncwarp();
+  // ---- u_N = Bt[N] / (1 - Al[N])
+  const double alN = (N >= 2) ? L.al(N - 1) : al1;
+  const double uN = buf[N - 1] / (1.0 - alN);
+  // ---- backward: u_i = Al[i+1] u_{i+1} + Bt[i+1], i = N-1..0
+  const int chb = (N + 31) / 32;
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  // chunk map G = h_{b0} o h_{b0+1} o ... o h_{b1-1} (h_{b1-1} applied first)
+  fh_aff G{1.0, 0.0};
+  for (int i = b1 - 1; i >= b0; --i) {
+    const double ali = (i >= 1) ? L.al(i) : al1;
+    G = fh_aff_compose(fh_aff{ali, buf[i]}, G);
+  }
+  const fh_aff Pb = fh_warp_exclusive_affine_rev(G);
+  double u = fma(Pb.a, uN, Pb.b);  // u at index b1
+  for (int i = b1 - 1; i >= b0; --i) {
+    const double ali = (i >= 1) ? L.al(i) : al1;
+    u = ali * u + buf[i];
+    L.store(i, u);
+  }
+  if (lane == 0) {
+    L.store(N, uN);
+    L.store(N + 1, uN);
+  }
+  __syncwarp();
+}

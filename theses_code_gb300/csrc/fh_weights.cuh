@@ -1,0 +1,68 @@
+// fh_weights.cuh -- device evaluation of the history weights (FP64).
+#pragma once
+#include "fh_common.cuh"
+
+// Lower incomplete beta B(y; a, b) = y^a sum_j (1-b)_j y^j / (j! (a+j)), y <= 1/2.
+__device__ __forceinline__ double fh_ib_lower(double y, double a, double b) {
+  if (y <= 0.0) return 0.0;
+  double s = 0.0, c = 1.0, yj = 1.0;
+  for (int j = 0; j < 400; ++j) {
+    const double t = c * yj / (a + (double)j);
+    s += t;
+    if (fabs(t) <= 1e-17 * fabs(s)) break;
+    c *= ((double)(j + 1) - b) / (double)(j + 1);
+    yj *= y;
+    if (c == 0.0) break;
+  }
+  return pow(y, a) * s;
+}
+
+// Upper tail B(1;a,b) - B(y;a,b) in c = 1-y: c^b sum_j (1-a)_j c^j / (j! (b+j)), c <= 1/2.
+__device__ __forceinline__ double fh_ib_upper(double c, double a, double b) {
+  if (c <= 0.0) return 0.0;
+  double s = 0.0, d = 1.0, cj = 1.0;
+  for (int j = 0; j < 400; ++j) {
+    const double t = d * cj / (b + (double)j);
+    s += t;
+    if (fabs(t) <= 1e-17 * fabs(s)) break;
+    d *= ((double)(j + 1) - a) / (double)(j + 1);
+    cj *= c;
+    if (d == 0.0) break;
+  }
+  return pow(c, b) * s;
+}
+
+// int_{x0 tau}^{x1 tau} (psi(X tau) - psi(s))^(-alpha) ds with psi(t) = t^beta.
+// beta == 1: the closed form in the operation order of H_solver::_kb_row
+// (mt_psi_caputo.cpp:506-515; TG_solver_::_kb_row fr_d_t_g_2d.cpp:2960-2985).
+// beta != 1: T^(1-alpha beta)/beta * [B(y1; 1/beta, 1-alpha) - B(y0; 1/beta, 1-alpha)],
+// y = (s/T)^beta, evaluated on the side (y or 1-y) where its series converges.
+__device__ __forceinline__ double fh_psi_int(double x0, double x1, double X, double tau, double alpha,
+                                             double beta) {
+  if (beta == 1.0) {
+    const double t0 = tau * x0, t1 = tau * x1, gtj = tau * X;
+    double v = gtj / gtj;
+    v *= pow(gtj, 1 - alpha);
+    const double v3 = pow(fabs(1.0 - t1 / gtj), 1 - alpha);
+    const double v4 = pow(fabs(1.0 - t0 / gtj), 1 - alpha);
+    const double v2 = -(v3 - v4) / (1 - alpha);
+    double sum = 0.0;
+    sum += v2 * v;
+    return sum;
+  }
+  const double a = 1.0 / beta, b = 1.0 - alpha;
+  const double y0 = pow(x0 / X, beta), y1 = pow(x1 / X, beta);
+  const double c0 = (x0 >= X) ? 0.0 : -expm1(beta * log1p((x0 - X) / X));
+  const double c1 = (x1 >= X) ? 0.0 : -expm1(beta * log1p((x1 - X) / X));
+  double diff;
+  if (y1 <= 0.5) {
+    diff = fh_ib_lower(y1, a, b) - fh_ib_lower(y0, a, b);
+  } else if (y0 > 0.5) {
+    diff = fh_ib_upper(c0, a, b) - fh_ib_upper(c1, a, b);
+  } else {
+    const double btot = exp(lgamma(a) + lgamma(b) - lgamma(a + b));
+    diff = (btot - fh_ib_upper(c1, a, b)) - fh_ib_lower(y0, a, b);
+  }
+  const double T = X * tau;
+  return pow(T, 1.0 - alpha * beta) / beta * diff;
+}

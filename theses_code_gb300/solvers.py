@@ -1,0 +1,159 @@
+"""Host-side mirror of the reference solver classes over the libfhist C ABI.
+
+Names follow the reference:
+  HSolverBatch  -- H_solver (mt_minimal.cpp / mt_psi_caputo.cpp), many instances
+  TGSolver      -- TG_solver_<func,1,kform> 2D ADI (fr_d_t_g_2d.cpp)
+  ABSolver      -- solve_and_check Atangana-Baleanu solve (MF_int_series.cpp)
+Every compute call goes to the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Context, HParams, TGParams, check
+
+
+def _hptr(a: np.ndarray) -> int:
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data
+
+
+class HSolverBatch:
+    """A batch of H_solver instances advanced in lock step (calc_step)."""
+
+    def __init__(self, ctx: Context, params: list[dict], max_steps: int):
+        self.ctx = ctx
+        self.params = [HParams(**p) for p in params]
+        arr = (HParams * len(params))(*self.params)
+        h = C.c_void_p()
+        check(ctx.L.fh_h_batch_create(ctx.h, len(params), arr, int(max_steps), C.byref(h)), ctx.h)
+        self.h = h
+        self.sizes = [p.N + 2 for p in self.params]
+        self.total = int(ctx.L.fh_h_batch_state_size(h))
+
+    def close(self):
+        if self.h:
+            self.ctx.L.fh_h_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_u(self, U: np.ndarray | list):
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(u, dtype=np.float64) for u in U])
+                                    if isinstance(U, list) else U, dtype=np.float64)
+        assert flat.size == self.total
+        check(self.ctx.L.fh_h_batch_set_u_host(self.h, _hptr(flat)), self.ctx.h)
+
+    def get_u(self) -> list[np.ndarray]:
+        out = np.empty(self.total)
+        check(self.ctx.L.fh_h_batch_get_u_host(self.h, _hptr(out)), self.ctx.h)
+        res, o = [], 0
+        for s in self.sizes:
+            res.append(out[o:o + s].copy())
+            o += s
+        return res
+
+    def calc_step(self, n: int = 1):
+        check(self.ctx.L.fh_h_batch_step(self.h, int(n)), self.ctx.h)
+
+    @property
+    def tstep(self) -> int:
+        return self.ctx.L.fh_h_batch_tstep(self.h)
+
+
+class TGSolver:
+    """TG_solver_ 2D ADI with full fractional history."""
+
+    def __init__(self, ctx: Context, params: dict, max_steps: int, mode: int = _lib.FH_TG_FP64):
+        self.ctx = ctx
+        self.p = TGParams(**params)
+        h = C.c_void_p()
+        check(ctx.L.fh_tg_create(ctx.h, C.byref(self.p), int(max_steps), int(mode), C.byref(h)), ctx.h)
+        self.h = h
+        self.shape = (self.p.M + 2, self.p.sN + 2)  # [j][i], idx = i + j*(sN+2)
+
+    def close(self):
+        if self.h:
+            self.ctx.L.fh_tg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, V2: np.ndarray, C0: np.ndarray):
+        V2 = np.ascontiguousarray(V2, dtype=np.float64).reshape(-1)
+        C0 = np.ascontiguousarray(C0, dtype=np.float64).reshape(-1)
+        check(self.ctx.L.fh_tg_set_state_host(self.h, _hptr(V2), _hptr(C0)), self.ctx.h)
+
+    def set_state_device(self, V2_ptr: int, C_ptr: int):
+        check(self.ctx.L.fh_tg_set_state(self.h, C.c_void_p(V2_ptr), C.c_void_p(C_ptr)), self.ctx.h)
+
+    def calc_step(self, n: int = 1):
+        check(self.ctx.L.fh_tg_step(self.h, int(n)), self.ctx.h)
+
+    def get_c(self) -> np.ndarray:
+        out = np.empty(self.shape[0] * self.shape[1])
+        check(self.ctx.L.fh_tg_get_c_host(self.h, _hptr(out)), self.ctx.h)
+        return out
+
+    @property
+    def field_ptr(self) -> int:
+        return self.ctx.L.fh_tg_field(self.h)
+
+    @property
+    def tstep(self) -> int:
+        return self.ctx.L.fh_tg_tstep(self.h)
+
+
+class ABSolver:
+    """solve_and_check-style Atangana-Baleanu convection-diffusion solve."""
+
+    def __init__(self, ctx: Context, m: int, max_steps: int, tau: float, alpha: float):
+        self.ctx = ctx
+        self.m = m
+        h = C.c_void_p()
+        check(ctx.L.fh_ab_create(ctx.h, int(m), int(max_steps), float(tau), float(alpha), C.byref(h)), ctx.h)
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.ctx.L.fh_ab_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_source(self, src: np.ndarray, bl: np.ndarray, br: np.ndarray):
+        src = np.ascontiguousarray(src, dtype=np.float64).reshape(-1, self.m + 1)
+        bl = np.ascontiguousarray(bl, dtype=np.float64)
+        br = np.ascontiguousarray(br, dtype=np.float64)
+        check(self.ctx.L.fh_ab_set_source_host(self.h, src.shape[0], _hptr(src), _hptr(bl), _hptr(br)),
+              self.ctx.h)
+
+    def set_c(self, C0: np.ndarray):
+        C0 = np.ascontiguousarray(C0, dtype=np.float64)
+        check(self.ctx.L.fh_ab_set_c_host(self.h, _hptr(C0)), self.ctx.h)
+
+    def set_current_coef(self, Ii: float):
+        check(self.ctx.L.fh_ab_set_current_coef(self.h, float(Ii)), self.ctx.h)
+
+    def calc_step(self, n: int = 1):
+        check(self.ctx.L.fh_ab_step(self.h, int(n)), self.ctx.h)
+
+    def get_c(self) -> np.ndarray:
+        out = np.empty(self.m + 1)
+        check(self.ctx.L.fh_ab_get_c_host(self.h, _hptr(out)), self.ctx.h)
+        return out
