@@ -92,6 +92,23 @@ int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int 
 int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H,
                           long long ldh, double *S);
 
+/* Allocation-free variant of fh_history_sum (same arguments, same result).
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * when they need the sum: applications that hand all device memory to their
+ * own pool or admit work against a fixed memory budget, and step loops where
+ * a cudaMalloc/cudaFree pair would synchronise the device.  The split-K partial
+ * sums go to a fixed array of FH_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) that
+ * every GPU loading the library reserves until the process exits; the call
+ * never allocates.  Limit: M*P <= FH_NOALLOC_SCRATCH_DOUBLES, else FH_ERANGE.
+ * The first call on a device looks up the array's device address (and loads
+ * the library's device code there): make that first call before any stream
+ * capture.  All calls on a device share the array and it keeps the last
+ * call's partials; calls whose GPU work overlaps (other streams or contexts
+ * on the same device) race on it and must be serialised by the caller. */
+#define FH_NOALLOC_SCRATCH_DOUBLES 2097152LL
+int fh_history_sum_noalloc(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
+                           const double *D, long long ldd, double *S, long long ldS);
+
 /* --------------------------------------------------------- tridiagonal */
 /* nsys systems A_i u_{i-1} - R_i u_i + B_i u_{i+1} = Om_i, i = 1..N-1, with
  * u_0 = al1[s] u_1 + bt1[s] and u_N = u_right[s] (right_mode 0) or

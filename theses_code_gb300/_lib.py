@@ -15,6 +15,7 @@ FH_W_L1, FH_W_PSI = 0, 1
 FH_K_CONST, FH_K_EXP = 0, 1
 FH_TG_FP64, FH_TG_BLOCKED = 0, 1
 FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS = 0, 1, 2
+FH_NOALLOC_SCRATCH_DOUBLES = 2097152
 
 _vp = C.c_void_p
 _dp = C.c_void_p  # device or host double*, passed as raw addresses
@@ -50,6 +51,7 @@ _SIGS = {
     "fh_mittag_leffler": (_i, [_vp, _i, _d, _d, _dp, _dp]),
     "fh_history_sum": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_history_sum_layers": (_i, [_vp, _i, _ll, _dp, _dp, _ll, _dp]),
+    "fh_history_sum_noalloc": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_tridiag_batched": (_i, [_vp, _i, _i, _dp, _dp, _dp, _dp, _ll, _dp, _dp, _i, _dp, _dp, _ll]),
     "fh_pcr_solver": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _i, _i]),
     "fh_h_batch_create": (_i, [_vp, _i, C.POINTER(HParams), _i, C.POINTER(_vp)]),
