@@ -8,6 +8,11 @@ solve / seconds).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--mode fp64|blocked] [--solve-steps S] [--grid G]
+                  [--config tg2d|caputo1d|psi_batch|ab1d]
+
+Other configurations (not the default line): caputo1d (1D L1, N=200, 1000
+steps), psi_batch (4096 ragged psi-Caputo instances, 500-step sample of the
+5000-step solve), ab1d (Atangana-Baleanu, N=2048, 20000 steps).
 
 --impl reference times the CPU implementation of the same path (the oracle
 port of the reference solver, all host threads) on a bounded sample and prints
@@ -39,12 +44,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="fp64", choices=["fp64", "blocked"])
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "df64", "blocked"])
     ap.add_argument("--solve-steps", type=int, default=2000)
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-grid", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="tg2d", choices=["tg2d", "caputo1d", "psi_batch", "ab1d", "serve"])
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--budget-gb", type=float, default=64.0)
+    ap.add_argument("--instances", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -108,6 +118,12 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def aggregate_value(world_size: int, units_per_rank: float, steps: int, t_max_ms: float) -> float:
+    """Replicas: every rank processes the same number of units; the job's
+    throughput is all ranks' units over the slowest rank's time."""
+    return world_size * units_per_rank * steps / (t_max_ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -137,12 +153,158 @@ def cpu_baseline(args, threads: int | None = None):
 
 
 # ------------------------------------------------------------------- GB300
+class Workload:
+    """One benchmark configuration: device solve, host-API (e2e) solve, units."""
+    name = ""
+    gps = 0.0            # grid-point-steps per bench step
+    h2d = d2h = 0        # bytes per e2e step
+    alg_hist_bytes = 0.0  # algorithmic bytes of all history-sum launches per bench step
+    config = {}
+
+    def solve_device(self):
+        raise NotImplementedError
+
+    def solve_host(self):
+        raise NotImplementedError
+
+
+class TG2D(Workload):
+    def __init__(self, ctx, args, dev, rank):
+        import torch
+        from theses_code_gb300 import workloads
+        from theses_code_gb300._lib import FH_TG_BLOCKED, FH_TG_DF64, FH_TG_FP64
+        from theses_code_gb300.solvers import TGSolver
+        G, S = args.grid, args.solve_steps
+        p, V2, C0 = workloads.convection_2d(G, G, alpha=0.7, tau=5e-4, d=0.1, seed=11 + rank)
+        mode = {"blocked": FH_TG_BLOCKED, "df64": FH_TG_DF64}.get(args.mode, FH_TG_FP64)
+        self.solver = TGSolver(ctx, p, S, mode)
+        self.V2_d = torch.as_tensor(V2, device=f"cuda:{dev}").contiguous()
+        self.C0_d = torch.as_tensor(C0, device=f"cuda:{dev}").contiguous()
+        P = V2.size
+        self.V2_h = torch.from_numpy(V2.reshape(-1)).pin_memory()
+        self.C0_h = torch.from_numpy(C0.reshape(-1)).pin_memory()
+        self.out_h = torch.empty(P, dtype=torch.float64).pin_memory()
+        self.S = S
+        self.gps = float(G) * G * S
+        self.h2d, self.d2h = 2 * P * 8, P * 8
+        pint = (G - 1) * (G - 1)
+        if args.mode == "blocked":
+            # FP64 near part: the layers of the current 64-step block; far part: the
+            # tensor-core contraction reads each history layer once per block (3 bf16 planes)
+            near = sum(8.0 * (j % 64) * pint + 16.0 * pint for j in range(1, S))
+            far = sum(6.0 * j0 * pint + 128 * 8.0 * pint for j0 in range(64, S, 64))
+            self.alg_hist_bytes = near + far
+        else:
+            self.alg_hist_bytes = sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))
+        self.name = f"tg2d_adi_{G}x{G}_{S}steps"
+        self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
+                       "d": 0.1, "velocity_modes": 8, "mode": args.mode,
+                       "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
+        self.kernel = {"blocked": "k_far_gemm (tcgen05, exact bf16 slices) + k_hist_sum_df<2> near",
+                       "df64": "k_hist_sum_df<2>"}.get(args.mode, "k_hist_sum<2>")
+
+    def solve_device(self):
+        self.solver.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
+        self.solver.calc_step(self.S)
+
+    def solve_host(self):
+        L, h = self.solver.ctx.L, self.solver.h
+        L.fh_tg_set_state_host(h, self.V2_h.data_ptr(), self.C0_h.data_ptr())
+        L.fh_tg_step(h, self.S)
+        L.fh_tg_get_c_host(h, self.out_h.data_ptr())
+        return self.out_h.numpy()
+
+
+class H1D(Workload):
+    """1D H_solver batches: caputo1d (N=200, 1000 steps, L1) or psi_batch
+    (4096 ragged psi-Caputo instances; bounded sample of the 5000 steps)."""
+
+    def __init__(self, ctx, args, dev, rank, kind):
+        import torch
+        from theses_code_gb300 import workloads
+        from theses_code_gb300.solvers import HSolverBatch
+        if kind == "caputo1d":
+            p, U0 = workloads.caputo_1d(200, 0.8, 1.0, 1e-3)
+            params, U0s, S = [p], [U0], args.solve_steps if args.solve_steps != 2000 else 1000
+            self.name = f"caputo1d_l1_N200_{S}steps"
+        else:
+            params, U0s = workloads.psi_batch(n=args.instances, seed=7 + rank)
+            S = args.solve_steps if args.solve_steps != 2000 else 500
+            self.name = f"psi_batch_{args.instances}inst_{S}steps"
+        self.solver = HSolverBatch(ctx, params, S + 1)
+        flat = np.concatenate(U0s)
+        self.U_d = torch.as_tensor(flat, device=f"cuda:{dev}")
+        self.U_h = torch.from_numpy(flat).pin_memory()
+        self.out_h = torch.empty(flat.size, dtype=torch.float64).pin_memory()
+        self.S = S
+        npts = sum(p["N"] - 1 for p in params)
+        self.gps = float(npts) * S
+        self.h2d = self.d2h = flat.size * 8
+        seg = sum(((p["N"] + 2) + 1) & ~1 for p in params)
+        self.alg_hist_bytes = sum(8.0 * max(os_ - 1, 0) * npts + 8.0 * npts for os_ in range(S))
+        self.config = {"workload": self.name, "instances": len(params), "interior_points": npts,
+                       "solve_steps": S, "state_doubles": seg,
+                       "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
+        self.kernel = "k_hist_tiles"
+
+    def solve_device(self):
+        self.solver.set_u_device(self.U_d.data_ptr())
+        self.solver.calc_step(self.S)
+
+    def solve_host(self):
+        L, h = self.solver.ctx.L, self.solver.h
+        L.fh_h_batch_set_u_host(h, self.U_h.data_ptr())
+        L.fh_h_batch_step(h, self.S)
+        L.fh_h_batch_get_u_host(h, self.out_h.data_ptr())
+        return self.out_h.numpy()
+
+
+class AB1D(Workload):
+    def __init__(self, ctx, args, dev, rank):
+        import torch
+        from theses_code_gb300 import workloads
+        from theses_code_gb300.solvers import ABSolver
+        S = args.solve_steps if args.solve_steps != 2000 else 20000
+        cfg, src, bl, br, C0 = workloads.ab_1d(m=2048, alpha=0.6, tau=1e-4, seed=5 + rank)
+        self.solver = ABSolver(ctx, cfg["m"], S, cfg["tau"], cfg["alpha"])
+        self.solver.set_source(src, bl, br)
+        self.C_d = torch.as_tensor(C0, device=f"cuda:{dev}")
+        self.C_h = torch.from_numpy(C0.copy()).pin_memory()
+        self.out_h = torch.empty(C0.size, dtype=torch.float64).pin_memory()
+        self.S = S
+        self.gps = float(cfg["m"] - 1) * S
+        self.h2d = self.d2h = C0.size * 8
+        self.alg_hist_bytes = sum(8.0 * (i - 1) * (cfg["m"] + 1) + 8.0 * (cfg["m"] + 1) for i in range(2, S + 1))
+        self.name = f"ab1d_N2048_{S}steps"
+        self.config = {"workload": self.name, "m": cfg["m"], "alpha": 0.6, "tau": 1e-4, "solve_steps": S,
+                       "source_modes": 16, "l2": "history %.0f MB" % (8 * 2050 * S / 1e6)}
+        self.kernel = "k_hist_sum<1>"
+
+    def solve_device(self):
+        self.solver.set_c_device(self.C_d.data_ptr())
+        self.solver.calc_step(self.S)
+
+    def solve_host(self):
+        L, h = self.solver.ctx.L, self.solver.h
+        L.fh_ab_set_c_host(h, self.C_h.data_ptr())
+        L.fh_ab_step(h, self.S)
+        L.fh_ab_get_c_host(h, self.out_h.data_ptr())
+        return self.out_h.numpy()
+
+
+def make_workload(ctx, args, dev, rank):
+    if args.config == "tg2d":
+        return TG2D(ctx, args, dev, rank)
+    if args.config in ("caputo1d", "psi_batch"):
+        return H1D(ctx, args, dev, rank, args.config)
+    if args.config == "ab1d":
+        return AB1D(ctx, args, dev, rank)
+    raise SystemExit(f"unknown config {args.config}")
+
+
 def run_gb300(args):
     import torch
-    from theses_code_gb300 import workloads
-    from theses_code_gb300._lib import FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, FH_TG_BLOCKED, FH_TG_FP64, \
-        Context
-    from theses_code_gb300.solvers import TGSolver
+    from theses_code_gb300._lib import FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, Context
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -151,23 +313,12 @@ def run_gb300(args):
         dist.init_process_group("nccl")
     dev = local
     torch.cuda.set_device(dev)
-    G, S = args.grid, args.solve_steps
-    p, V2, C0 = workloads.convection_2d(G, G, alpha=0.7, tau=5e-4, d=0.1, seed=11 + rank)
     ctx = Context(dev)
-    mode = FH_TG_BLOCKED if args.mode == "blocked" else FH_TG_FP64
-    solver = TGSolver(ctx, p, S, mode)
-    V2_d = torch.as_tensor(V2, device=f"cuda:{dev}").contiguous()
-    C0_d = torch.as_tensor(C0, device=f"cuda:{dev}").contiguous()
+    wl = make_workload(ctx, args, dev, rank)
     stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
-    P = V2.size
-    gps = float(G) * G * S  # grid-point-steps per solve
-
-    def solve_device():
-        solver.set_state_device(V2_d.data_ptr(), C0_d.data_ptr())
-        solver.calc_step(S)
 
     for _ in range(args.warmup):
-        solve_device()
+        wl.solve_device()
     ctx.sync()
 
     def barrier():
@@ -175,6 +326,14 @@ def run_gb300(args):
             import torch.distributed as dist
             dist.barrier()
         torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        tt = torch.tensor([x], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
 
     clocks = ClockSampler(dev)
     ctx.profile(True)
@@ -185,7 +344,7 @@ def run_gb300(args):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        solve_device()
+        wl.solve_device()
     e1.record(stream)
     e1.synchronize()
     barrier()
@@ -196,77 +355,84 @@ def run_gb300(args):
     sweep_ms, _ = ctx.profile_read(FH_PROF_SWEEP)
     w_ms, _ = ctx.profile_read(FH_PROF_WEIGHTS)
     ctx.profile(False)
-    t_max = t_ms
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms], device=f"cuda:{dev}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = ws * gps * args.steps / (t_max / 1e3)
+    t_max = max_over_ranks(t_ms)
+    value = aggregate_value(ws, wl.gps, args.steps, t_max)
 
-    # end to end through the C ABI with pinned host buffers
-    V2_h = torch.from_numpy(V2.reshape(-1)).pin_memory()
-    C0_h = torch.from_numpy(C0.reshape(-1)).pin_memory()
-    out_h = torch.empty(P, dtype=torch.float64).pin_memory()
-    L = ctx.L
+    # end to end through the C ABI with pinned host buffers (H2D inputs, D2H result)
     barrier()
     t0 = time.perf_counter()
+    out = None
     for _ in range(args.e2e_steps):
-        L.fh_tg_set_state_host(solver.h, V2_h.data_ptr(), C0_h.data_ptr())
-        L.fh_tg_step(solver.h, S)
-        L.fh_tg_get_c_host(solver.h, out_h.data_ptr())
+        out = wl.solve_host()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    assert np.isfinite(out_h.numpy()).all(), "non-finite result"
-    e2e = {"value": ws * gps * args.e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 2 * P * 8,
-           "d2h_bytes_per_step": P * 8}
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    assert out is not None and np.isfinite(out).all(), "non-finite result"
+    e2e = {"value": ws * wl.gps * args.e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": wl.h2d,
+           "d2h_bytes_per_step": wl.d2h}
 
-    # roofline of the dominant kernel (history sum): algorithmic bytes = the
-    # K history layers read once per step plus the two sums written, over the
-    # (G-1)^2 interior points where the sums are needed
-    pint = (G - 1) * (G - 1)
-    alg_bytes_solve = sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))
-    achieved = alg_bytes_solve * args.steps / (hist_ms / 1e3) / 1e9 if hist_ms > 0 else None
+    achieved = wl.alg_hist_bytes * args.steps / (hist_ms / 1e3) / 1e9 if hist_ms > 0 else None
     peak, peak_kind = peaks()
     traffic = None
-    tp = os.path.join(REPO, "profiles", "hist_sum_traffic.txt")
-    if os.path.exists(tp):
-        # "ratio <dram bytes / algorithmic bytes>" of the captured launch, scaled to the mean launch
+    tp = os.path.join(REPO, "profiles", "k_hist_sum_fp64_tg512x300.md")
+    if args.config == "tg2d" and args.mode == "fp64" and os.path.exists(tp):
+        # dram bytes / algorithmic bytes of the captured launch, scaled to the mean launch
         for line in open(tp):
-            if line.startswith("ratio"):
-                traffic = float(line.split()[1]) * alg_bytes_solve / (S - 1)
+            if line.startswith("traffic_ratio:"):
+                traffic = float(line.split()[1]) * wl.alg_hist_bytes / max(hist_n / max(args.steps, 1), 1)
+    cfg = dict(wl.config)
+    cfg["parallelism"] = f"replicas x{ws}"
     result = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"tg2d_adi_{G}x{G}_{S}steps", "grid": [G, G], "solve_steps": S, "alpha": 0.7,
-                   "tau": 5e-4, "d": 0.1, "velocity_modes": 8, "mode": args.mode,
-                   "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9),
-                   "parallelism": f"replicas x{ws}"},
-        "e2e": e2e,
-        "gpu_launches": int(launches),
+        "dtype": "f64", "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_hist_sum<2>", "peak_kind": peak_kind,
-                     "launches": int(hist_n), "kernel_ms": hist_ms, "sweep_ms": sweep_ms, "weights_ms": w_ms,
+                     "kernel": wl.kernel, "peak_kind": peak_kind, "launches": int(hist_n),
+                     "kernel_ms": hist_ms, "sweep_ms": sweep_ms, "weights_ms": w_ms,
                      "note": "achieved = sum of per-launch algorithmic bytes / summed event time of the "
                              "history-sum launches over the timed region; traffic is per mean launch"},
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.config == "tg2d":
         result["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
         print(json.dumps(result))
-    solver.close()
     ctx.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_serve(args):
+    """Poisson stream of mixed 1D/2D solves through theses_code_gb300.serve:
+    admission by history memory, cohorts of 1D requests, 2D requests on their
+    own streams (blocked history).  Reports solves/s and p50/p99 latency."""
+    import torch
+    from theses_code_gb300 import serve
+    from theses_code_gb300._lib import FH_TG_BLOCKED
+    torch.cuda.set_device(0)
+    reqs = serve.make_mix(args.requests, rate=args.rate, seed=3, mode_2d=FH_TG_BLOCKED)
+    warm = serve.make_mix(6, rate=args.rate, seed=101, max_2d=64, steps=(100, 200), nrange=(64, 256))
+    srv = serve.Server(args.budget_gb * 1e9, chunk=250, max_cohort=512, max_active=16)
+    srv.run(warm)
+    clocks = ClockSampler(0)
+    clocks.start()
+    done, st = srv.run(reqs, realtime=True)
+    clk = clocks.stop()
+    gps = 0.0
+    for r in reqs:
+        pts = (r.params["N"] - 1) if r.kind == "1d" else r.params["sN"] * r.params["M"]
+        gps += pts * r.steps
+    res = {"metric": "solves/s", "value": st["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+           "steps": len(done), "warmup": len(warm), "ms_per_step": 1e3 * st["wall_s"] / max(len(done), 1),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"serve_poisson_{args.requests}req", "rate_per_s": args.rate,
+                      "mix": "60% 1D (L1/psi-Caputo, N 64-2048), 40% 2D (64^2-512^2, blocked history)",
+                      "steps": [500, 5000], "budget_gb": args.budget_gb},
+           "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"]},
+           "grid_point_steps_per_s": gps / st["wall_s"], "clocks": clk,
+           "scheduler": {k: st[k] for k in ("peak_active_solvers", "scheduler_passes", "wall_s")}}
+    print(json.dumps(res))
 
 
 def run_reference(args):
@@ -302,6 +468,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "serve":
+        run_serve(args)
     else:
         run_gb300(args)
 

@@ -12,6 +12,7 @@
  *    fh_last_error() gives a one-line reason.  Work is enqueued on the
  *    context's stream; host-buffer calls synchronise that stream.
  *  - Calls on one context are not thread-safe; use one context per thread.
+ *  - Destroy solver objects before the context they were created on.
  *  - Each entry point names the reference interface it replaces (file:line in
  *    the reference repository).
  */
@@ -41,6 +42,12 @@ int fh_ctx_create(int device, fh_ctx **out);
 int fh_ctx_destroy(fh_ctx *ctx);
 const char *fh_last_error(const fh_ctx *ctx);
 int fh_ctx_sync(fh_ctx *ctx);
+/* A multi-step call that starts from the initial state (fh_*_step right after
+ * setting the state) is recorded once as a CUDA graph and replayed by later
+ * identical calls (on by default; off while kernel profiling is on). */
+int fh_ctx_set_graphs(fh_ctx *ctx, int enable);
+/* Non-blocking: 1 if all work enqueued on the context finished, 0 if not, < 0 on error. */
+int fh_ctx_query(fh_ctx *ctx);
 int fh_ctx_set_stream(fh_ctx *ctx, void *cuda_stream);
 void *fh_ctx_get_stream(fh_ctx *ctx);
 /* Number of kernels this context has launched so far. */
@@ -91,6 +98,15 @@ int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int 
  * irrigation_fractional.cpp:1828-1896): S[p] = sum_{t<K} w[t]*(H[(t+1)ldh+p] - H[t ldh+p]). */
 int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H,
                           long long ldh, double *S);
+
+/* Blocked contraction on the tensor cores: S[m*ldS + p] = sum_{k<K} W[m*ldw + k] D[k*ldd + p]
+ * for m < 128, computed from three-way bf16 splits of W and D (six products,
+ * FP32 accumulation per 128 layers, carried in double-float), FP64 result.
+ * K must be a positive multiple of 64.  Error ~1e-7 of sum_k |W||D|.  This is
+ * the far-history GEMM of the blocked form of fr_d_t_g_2d.cpp:3340-3384 (one
+ * weight row per future half step); it allocates its own plane storage. */
+int fh_history_contract_bf16x3(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
+                               const double *D, long long ldd, double *S, long long ldS);
 
 /* Allocation-free variant of fh_history_sum (same arguments, same result).
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
@@ -158,9 +174,12 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
 int fh_h_batch_destroy(fh_h_batch *b);
 /* Total number of doubles of the concatenated state (sum of N_i + 2). */
 long long fh_h_batch_state_size(const fh_h_batch *b);
-/* Concatenated per-instance U arrays (N_i + 2 each, instance order). */
+/* Concatenated per-instance U arrays (N_i + 2 each, instance order); resets tstep to 1. */
 int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host);
+int fh_h_batch_set_u(fh_h_batch *b, const double *U);
 int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host);
+/* U of instances [first, first+count) only (concatenated), synchronising the stream. */
+int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_host);
 /* H_solver::calc_step repeated nsteps times (tstep starts at 1). */
 int fh_h_batch_step(fh_h_batch *b, int nsteps);
 int fh_h_batch_tstep(const fh_h_batch *b);
@@ -173,8 +192,9 @@ typedef struct {
   double dL, dLx;   /* steps of the x sweep (along i) and y sweep (along j) */
 } fh_tg_params;
 
-#define FH_TG_FP64 0      /* plain FP64 history sum                          */
-#define FH_TG_BLOCKED 1   /* blocked history: tensor-core contraction of old layers */
+#define FH_TG_FP64 0      /* FP64 history, FP64 FMA sums (bit-faithful arithmetic)        */
+#define FH_TG_BLOCKED 1   /* far history on the tensor cores (exact bf16 slices), near in DF64 */
+#define FH_TG_DF64 2      /* history as (hi, lo) FP32 pairs, double-float sums on the FP32 pipe */
 
 typedef struct fh_tg_solver fh_tg_solver;
 
@@ -205,6 +225,7 @@ int fh_ab_destroy(fh_ab_solver *s);
 int fh_ab_set_source_host(fh_ab_solver *s, int nrows, const double *src_host, const double *bl_host,
                           const double *br_host);
 int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host);
+int fh_ab_set_c(fh_ab_solver *s, const double *C);
 /* Override the current-step coefficient Ii (default: the lag-1 weight). */
 int fh_ab_set_current_coef(fh_ab_solver *s, double Ii);
 int fh_ab_step(fh_ab_solver *s, int nsteps);

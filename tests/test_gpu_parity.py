@@ -152,7 +152,8 @@ def test_history_sum_layers(ctx, torch_mod):
     H = rng.normal(size=(K + 1, P))
     w = rng.uniform(size=K)
     S = torch.zeros(P, dtype=torch.float64, device="cuda")
-    ctx.call("fh_history_sum_layers", K, P, dev(torch, w).data_ptr(), dev(torch, H).data_ptr(), P, S.data_ptr())
+    wd, Hd = dev(torch, w), dev(torch, H)  # keep the device buffers alive until the kernel ran
+    ctx.call("fh_history_sum_layers", K, P, wd.data_ptr(), Hd.data_ptr(), P, S.data_ptr())
     ctx.sync()
     assert relmax(S.cpu().numpy(), O.history_sum_layers(H, w)) < 1e-13
 
@@ -272,12 +273,13 @@ def test_tg_reference_golden(ctx):
     assert relmax(s.get_c(), g["C"]) <= TOL_SOLVER
 
 
-@pytest.mark.parametrize("sN,M,steps", [(64, 48, 40), (130, 97, 25)])
-def test_tg_vs_oracle(ctx, sN, M, steps):
+@pytest.mark.parametrize("mode", [0, 2])  # FH_TG_FP64, FH_TG_DF64 (double-float history)
+@pytest.mark.parametrize("sN,M,steps", [(64, 48, 40), (130, 97, 25), (40, 40, 150)])
+def test_tg_vs_oracle(ctx, sN, M, steps, mode):
     from theses_code_gb300 import workloads
     from theses_code_gb300.solvers import TGSolver
     p, V2, C0 = workloads.convection_2d(sN, M, alpha=0.7, tau=5e-4, d=0.1, seed=sN, C1=0.2, S=0.01)
-    s = TGSolver(ctx, p, steps)
+    s = TGSolver(ctx, p, steps, mode)
     s.set_state(V2, C0)
     s.calc_step(steps)
     ref, _ = O.tg_solve(p, V2, C0, steps)

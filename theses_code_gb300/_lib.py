@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libfhist.so")
@@ -13,7 +14,7 @@ LIB_PATH = os.path.join(_PKG, "libfhist.so")
 FH_OK, FH_EINVAL, FH_ENOMEM, FH_ECUDA, FH_ENONFINITE, FH_ETIMEOUT, FH_ERANGE, FH_ENOTSUP = range(8)
 FH_W_L1, FH_W_PSI = 0, 1
 FH_K_CONST, FH_K_EXP = 0, 1
-FH_TG_FP64, FH_TG_BLOCKED = 0, 1
+FH_TG_FP64, FH_TG_BLOCKED, FH_TG_DF64 = 0, 1, 2
 FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS = 0, 1, 2
 FH_NOALLOC_SCRATCH_DOUBLES = 2097152
 
@@ -40,6 +41,8 @@ _SIGS = {
     "fh_ctx_destroy": (_i, [_vp]),
     "fh_last_error": (C.c_char_p, [_vp]),
     "fh_ctx_sync": (_i, [_vp]),
+    "fh_ctx_query": (_i, [_vp]),
+    "fh_ctx_set_graphs": (_i, [_vp, _i]),
     "fh_ctx_set_stream": (_i, [_vp, _vp]),
     "fh_ctx_get_stream": (_vp, [_vp]),
     "fh_ctx_launch_count": (_ll, [_vp]),
@@ -52,6 +55,7 @@ _SIGS = {
     "fh_history_sum": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_history_sum_layers": (_i, [_vp, _i, _ll, _dp, _dp, _ll, _dp]),
     "fh_history_sum_noalloc": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
+    "fh_history_contract_bf16x3": (_i, [_vp, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_tridiag_batched": (_i, [_vp, _i, _i, _dp, _dp, _dp, _dp, _ll, _dp, _dp, _i, _dp, _dp, _ll]),
     "fh_pcr_solver": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _i, _i]),
     "fh_h_batch_create": (_i, [_vp, _i, C.POINTER(HParams), _i, C.POINTER(_vp)]),
@@ -59,6 +63,8 @@ _SIGS = {
     "fh_h_batch_state_size": (_ll, [_vp]),
     "fh_h_batch_set_u_host": (_i, [_vp, _dp]),
     "fh_h_batch_get_u_host": (_i, [_vp, _dp]),
+    "fh_h_batch_set_u": (_i, [_vp, _dp]),
+    "fh_h_batch_get_u_range_host": (_i, [_vp, _i, _i, _dp]),
     "fh_h_batch_step": (_i, [_vp, _i]),
     "fh_h_batch_tstep": (_i, [_vp]),
     "fh_tg_create": (_i, [_vp, C.POINTER(TGParams), _i, _i, C.POINTER(_vp)]),
@@ -73,6 +79,7 @@ _SIGS = {
     "fh_ab_destroy": (_i, [_vp]),
     "fh_ab_set_source_host": (_i, [_vp, _i, _dp, _dp, _dp]),
     "fh_ab_set_c_host": (_i, [_vp, _dp]),
+    "fh_ab_set_c": (_i, [_vp, _dp]),
     "fh_ab_set_current_coef": (_i, [_vp, _d]),
     "fh_ab_step": (_i, [_vp, _i]),
     "fh_ab_get_c_host": (_i, [_vp, _dp]),
@@ -124,9 +131,16 @@ class Context:
         check(L.fh_ctx_create(device, C.byref(h)))
         self.h = h
         self.L = L
+        self._children = weakref.WeakSet()
+
+    def adopt(self, obj):
+        """Solver objects register here so that close() destroys them first."""
+        self._children.add(obj)
 
     def close(self):
         if self.h:
+            for ch in list(self._children):
+                ch.close()
             self.L.fh_ctx_destroy(self.h)
             self.h = None
 
@@ -138,6 +152,15 @@ class Context:
 
     def sync(self):
         check(self.L.fh_ctx_sync(self.h), self.h)
+
+    def set_graphs(self, enable: bool):
+        check(self.L.fh_ctx_set_graphs(self.h, int(bool(enable))), self.h)
+
+    def idle(self) -> bool:
+        r = self.L.fh_ctx_query(self.h)
+        if r < 0:
+            check(-r, self.h)
+        return r == 1
 
     @property
     def stream(self) -> int:

@@ -16,6 +16,7 @@ struct fh_ab_solver {
   long long P = 0;  // m+1 rounded up to even
   double tau = 0, alpha = 0, A = 0, Bd = 0, Cc = 0;
   fh_dbuf w, ii, al, den, C, D, W, part, S, src, bl, br;
+  fh_graph_cache graph;
 };
 
 // al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
@@ -207,6 +208,15 @@ int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host) {
   return FH_OK;
 }
 
+int fh_ab_set_c(fh_ab_solver *s, const double *C) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, C, FH_EINVAL, "fh_ab_set_c: null pointer");
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, sizeof(double) * (s->m + 1), cudaMemcpyDeviceToDevice, ctx->stream));
+  s->step = 0;
+  return FH_OK;
+}
+
 int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
   FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
   fh_ctx *ctx = s->ctx;
@@ -223,6 +233,18 @@ int fh_ab_step(fh_ab_solver *s, int nsteps) {
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, s->nrows >= 1, FH_EINVAL, "fh_ab_step: source not set");
   FH_REQUIRE(ctx, nsteps >= 0 && s->step + nsteps <= s->max_steps, FH_ENOMEM, "fh_ab_step: history full");
+  if (ctx->graphs && s->step == 0 && nsteps > 1 && !ctx->prof) {
+    int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
+      for (int n = 0; n < nsteps; ++n) {
+        int r = ab_one_step(s);
+        if (r) return r;
+      }
+      return (int)FH_OK;
+    });
+    if (rc) return rc;
+    s->step = nsteps;
+    return FH_OK;
+  }
   for (int n = 0; n < nsteps; ++n) {
     int rc = ab_one_step(s);
     if (rc) return rc;

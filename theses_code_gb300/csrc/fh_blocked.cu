@@ -1,0 +1,489 @@
+// fh_blocked.cu -- blocked history contraction on the 5th-generation tensor
+// cores (tcgen05 + TMEM + TMA), the far part of the history sum for a block of
+// 64 future steps:
+//
+//   S_far[m][p] = sum_{k<K} W[m][k] * D[k][p],   m < 128 (x/y weights of 64 steps)
+//
+// Exact-product scheme (Ozaki-style, bf16 slices): every chunk of 64 layers
+// has a power-of-two scale per weight row (2^Ew[m][c]) and per point
+// (2^Ed[c][p]); scaled values have |y| < 128 and are cut into four integer
+// slices y = a0 + a1/2^8 + a2/2^16 + a3/2^24 with |a_i| <= 128, which bf16
+// holds exactly.  Products a_i*b_j are exact in FP32 and so are the per-chunk
+// sums of each level l = i + j <= 3 (|sum| <= 4*64*2^14 = 2^22): the
+// tensor-core accumulation cannot round or truncate.  Per chunk the epilogue
+// combines the four level sums exactly (double-float with one
+// renormalisation), scales by 2^(Ew+Ed) and adds into a double-float running
+// sum.  The only approximation is the slicing (~2^-32 of the chunk maxima,
+// round to nearest, unbiased); the near layers of the block are summed
+// separately in double-float.
+//
+// Data layout: K-major planes (point p holds its layers contiguously; one
+// 64-layer chunk = one 128-byte swizzle row), loaded by TMA with 128-byte
+// swizzle; exponents as int8 tables Ed[c][Ppad], Ew[c][128].
+//
+// CTA (320 threads, one per SM): warp 0 issues TMA loads into a 2-stage ring
+// (96 KiB per stage: 4 weight tiles 128x64 + 4 history tiles 64x64 bf16), warp
+// 1 owns TMEM (512 columns; 2 buffers x 4 levels x 64 columns) and issues the
+// MMAs from one thread, warps 2-9 run the epilogue (two warps per TMEM lane
+// quarter, 32 columns each).  Every mbarrier wait is bounded by a %globaltimer
+// deadline; on expiry the kernel records FH_ETIMEOUT, waits (bounded) for its
+// own copies and MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "fh_common.cuh"
+#include "fh_internal.h"
+#include "fh_sm100.cuh"
+#include "fh_weights.cuh"
+
+namespace {
+constexpr int kBM = 128;  // weight rows per block (2 x 64 steps)
+constexpr int kBN = 64;   // points per CTA
+constexpr int kBK = 64;   // layers per chunk / pipeline stage (one 128-byte row)
+constexpr int kStages = 2;
+constexpr uint32_t kTileA = kBM * kBK * 2;          // 16 KiB
+constexpr uint32_t kTileB = kBN * kBK * 2;          // 8 KiB
+constexpr int kSlices = 4;
+constexpr int kLevels = kSlices;                     // levels l = i + j <= 3
+constexpr uint32_t kStageBytes = kSlices * (kTileA + kTileB);  // 96 KiB
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr uint32_t kTmemCols = 512;
+constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
+}  // namespace
+
+// x = 2^E (a0 + a1/2^8 + a2/2^16 + a3/2^24) with integer |a_i| <= 128 given |x| < 2^(E+7).
+__device__ __forceinline__ void fh_slice4(double x, int E, __nv_bfloat16 (&b)[kSlices]) {
+  double r = ldexp(x, -E);
+#pragma unroll
+  for (int i = 0; i < kSlices; ++i) {
+    const double a = rint(r);
+    b[i] = __double2bfloat16(a);
+    r = (r - a) * 256.0;
+  }
+}
+
+// Exponent E with max|x| < 2^(E+7); 0 for an all-zero chunk.
+__device__ __forceinline__ int fh_chunk_exp(double mx) {
+  if (!(mx > 0.0)) return 0;
+  int q;
+  frexp(mx, &q);  // mx = f 2^q, f in [0.5, 1)
+  return q - 7;
+}
+
+__device__ __forceinline__ float fh_exp2i(int e) {
+  // 2^e as float (0 below the normal range; e stays far below the overflow range here)
+  if (e < -126) return 0.0f;
+  return __int_as_float((e + 127) << 23);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_far_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, long long P,
+               const int8_t *__restrict__ Ew, const int8_t *__restrict__ Ed, long long Ppad,
+               double *__restrict__ out, long long ldo, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  const uint32_t raw = fh_smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t *gbase = smem_raw + (base - raw);
+  const uint32_t bars = base + kStages * kStageBytes;
+  uint8_t *gbars = gbase + kStages * kStageBytes;
+  auto full = [&](int s) { return bars + 8u * s; };
+  auto empty = [&](int s) { return bars + 8u * (kStages + s); };
+  auto accfull = [&](int b) { return bars + 8u * (2 * kStages + b); };
+  auto accempty = [&](int b) { return bars + 8u * (2 * kStages + 2 + b); };
+  const uint32_t mmadone = bars + 8u * (2 * kStages + 4);
+  const uint32_t tslot = bars + 8u * (2 * kStages + 5);
+  volatile uint32_t *tslot_g = reinterpret_cast<volatile uint32_t *>(gbars + 8 * (2 * kStages + 5));
+  volatile int *sh_err = reinterpret_cast<volatile int *>(gbars + 8 * (2 * kStages + 6));
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long p0 = (long long)blockIdx.x * kBN;
+  const int nchunks = K / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      fh_mbar_init(full(s), 1);
+      fh_mbar_init(empty(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      fh_mbar_init(accfull(b), 1);
+      fh_mbar_init(accempty(b), 32 * kEpiWarps);
+    }
+    fh_mbar_init(mmadone, 1);
+    *sh_err = 0;
+    fh_fence_mbar_init();
+  }
+  if (warp == 1) {
+    fh_tmem_alloc(tslot, kTmemCols);
+    fh_tmem_relinquish();
+  }
+  fh_tc_fence_before();
+  __syncthreads();
+  fh_tc_fence_after();
+  const uint32_t tmem = *tslot_g;
+  bool ok = true;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int last_issued[kStages];
+      for (int s = 0; s < kStages; ++s) last_issued[s] = -1;
+      for (int c = 0; c < nchunks; ++c) {
+        const int s = c % kStages;
+        if (c >= kStages && !fh_mbar_wait(empty(s), ((c / kStages) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        fh_mbar_arrive_expect_tx(full(s), kStageBytes);
+        const uint32_t sb = base + s * kStageBytes;
+        for (int pl = 0; pl < kSlices; ++pl) fh_tma_load_3d(sb + pl * kTileA, &tmA, c * kBK, 0, pl, full(s));
+        for (int pl = 0; pl < kSlices; ++pl)
+          fh_tma_load_3d(sb + kSlices * kTileA + pl * kTileB, &tmB, c * kBK, (int)p0, pl, full(s));
+        last_issued[s] = c;
+      }
+      if (!ok) {
+        *sh_err = 1;
+        for (int s = 0; s < kStages; ++s)
+          if (last_issued[s] >= 0) fh_mbar_wait(full(s), (last_issued[s] / kStages) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = fh_idesc_bf16_f32(kBM, kBN);
+      for (int c = 0; c < nchunks; ++c) {
+        const int s = c % kStages, b = c & 1;
+        if (c >= 2 && !fh_mbar_wait(accempty(b), ((c >> 1) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        if (!fh_mbar_wait(full(s), (c / kStages) & 1)) {
+          ok = false;
+          break;
+        }
+        fh_tc_fence_after();
+        const uint32_t sb = base + s * kStageBytes;
+        const uint32_t lv0 = tmem + (uint32_t)(b * kLevels * kBN);
+        uint32_t first[kLevels] = {0, 0, 0, 0};
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk) {
+          // level l = i + j collects the slice products a_i b_j (exact integers)
+          const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+          const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+#pragma unroll
+          for (int q = 0; q < 10; ++q) {
+            const int l = ia[q] + ib[q];
+            const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileA + kk * 32);
+            const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileA + ib[q] * kTileB + kk * 32);
+            fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
+            first[l] = 1;
+          }
+        }
+        fh_mma_commit(empty(s));
+        fh_mma_commit(accfull(b));
+      }
+      fh_mma_commit(mmadone);
+      if (!fh_mbar_wait(mmadone, 0)) ok = false;
+      if (!ok) *sh_err = 1;
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4)..+31 (row m); the two warps of
+    // a lane quarter split the 64 columns
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const uint32_t lanebase = (uint32_t)(32 * q) << 16;
+    const int m = 32 * q + lane;
+    const int col0 = 32 * half;
+    float HI[32], LO[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) HI[i] = LO[i] = 0.f;
+    for (int c = 0; c < nchunks; ++c) {
+      const int b = c & 1;
+      if (!__all_sync(0xffffffffu, fh_mbar_wait(accfull(b), (c >> 1) & 1))) {
+        ok = false;
+        break;
+      }
+      fh_tc_fence_after();
+      const int ew = (int)Ew[(long long)c * kBM + m];
+      const int8_t *edc = Ed + (long long)c * Ppad + p0 + col0;
+#pragma unroll 1
+      for (int t = 0; t < 2; ++t) {
+        float L0[16], L1[16], L2[16], L3[16];
+        const uint32_t cb = tmem + lanebase + (uint32_t)(b * kLevels * kBN + col0 + 16 * t);
+        fh_tmem_ld16(cb, L0);
+        fh_tmem_ld16(cb + kBN, L1);
+        fh_tmem_ld16(cb + 2 * kBN, L2);
+        fh_tmem_ld16(cb + 3 * kBN, L3);
+        fh_tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          // T = L0 + L1/2^8 + L2/2^16 + L3/2^24 exactly as (th, tl):
+          // TwoSum of the first two levels, L2 joins the error term exactly,
+          // a fast two-sum renormalises, then L3 joins exactly.
+          const float x1 = L1[i] * 0.00390625f;
+          float th = L0[i] + x1;
+          const float bb = th - L0[i];
+          float tl = (L0[i] - (th - bb)) + (x1 - bb);
+          tl += L2[i] * 1.52587890625e-05f;
+          const float tr = th + tl;
+          tl = tl - (tr - th);
+          th = tr;
+          tl += L3[i] * 5.9604644775390625e-08f;
+          const float sc = fh_exp2i(ew + (int)edc[16 * t + i]);
+          const float vh = th * sc, vl = tl * sc;
+          // (HI, LO) += (vh, vl)
+          const int k = 16 * t + i;
+          const float s = HI[k] + vh;
+          const float bs = s - HI[k];
+          const float e = (HI[k] - (s - bs)) + (vh - bs);
+          HI[k] = s;
+          LO[k] += e + vl;
+        }
+      }
+      fh_tc_fence_before();
+      fh_mbar_arrive(accempty(b));
+    }
+    if (ok && nchunks > 0) {
+      double *o = out + (long long)m * ldo + p0 + col0;
+#pragma unroll
+      for (int k = 0; k < 32; ++k)
+        if (p0 + col0 + k < P) o[k] = (double)HI[k] + (double)LO[k];
+    }
+    if (!ok) *sh_err = 1;
+  }
+  fh_tc_fence_before();
+  __syncthreads();
+  fh_tc_fence_after();
+  if (threadIdx.x == 0 && *sh_err) atomicOr(err, 1);
+  if (warp == 1) fh_tmem_dealloc(tmem, kTmemCols);
+}
+
+// Weight planes of a TG block: row m = 2r + {0: x, 1: y} of step j0 + r,
+// A3[s][m][k] (K-major) and Ew[c][m]; one warp per (row, 64-layer chunk).
+__global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, double alpha, double beta,
+                              __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
+  const int c = blockIdx.x;
+  const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= kBM) return;
+  const double X = (double)(j0 + (m >> 1)) + ((m & 1) ? 1.0 : 0.5);
+  double w[2];
+  double mx = 0.0;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = c * kBK + lane + 32 * h;
+    w[h] = 0.0;
+    if (k < K) {
+      const double s0 = (double)k + 0.0;
+      w[h] = Da * fh_psi_int(s0, s0 + 1.0, X, tau, alpha, beta);
+    }
+    mx = fmax(mx, fabs(w[h]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int E = fh_chunk_exp(mx);
+  if (lane == 0) Ew[(long long)c * kBM + m] = (int8_t)E;
+  const long long plane = (long long)kBM * Kcap;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = c * kBK + lane + 32 * h;
+    __nv_bfloat16 bs[kSlices];
+    fh_slice4(w[h], E, bs);
+    const long long o = (long long)m * Kcap + k;
+#pragma unroll
+    for (int i = 0; i < kSlices; ++i) A3[i * plane + o] = bs[i];
+  }
+}
+
+// Generic weight rows (standalone contraction): W[m*ldw + k], k < K.
+__global__ void k_blk_split_rows(const double *__restrict__ W, int ldw, int K, int Kcap,
+                                 __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
+  const int c = blockIdx.x;
+  const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= kBM) return;
+  double w[2];
+  double mx = 0.0;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = c * kBK + lane + 32 * h;
+    w[h] = (k < K) ? W[(long long)m * ldw + k] : 0.0;
+    mx = fmax(mx, fabs(w[h]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int E = fh_chunk_exp(mx);
+  if (lane == 0) Ew[(long long)c * kBM + m] = (int8_t)E;
+  const long long plane = (long long)kBM * Kcap;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = c * kBK + lane + 32 * h;
+    __nv_bfloat16 bs[kSlices];
+    fh_slice4(w[h], E, bs);
+    const long long o = (long long)m * Kcap + k;
+#pragma unroll
+    for (int i = 0; i < kSlices; ++i) A3[i * plane + o] = bs[i];
+  }
+}
+
+// Layers [k0, k0+64) of D (layer-major FP64, pitch ldd, P valid points) into
+// the K-major planes H3[s][p][k] and the exponents Ed[k0/64][p].  One thread
+// per point, the 64 values pass through a 64 KiB shared tile.
+__global__ void __launch_bounds__(128) k_blk_convert(const double *__restrict__ D, long long ldd, long long P,
+                                                     long long Ppad, int k0, int Kcap, int df,
+                                                     __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
+  extern __shared__ double tile[];  // [64][128]
+  const long long pb = (long long)blockIdx.x * 128;
+  const int t = threadIdx.x;
+  const long long p = pb + t;
+  double mx = 0.0;
+  for (int k = 0; k < kBK; ++k) {
+    double v = 0.0;
+    if (p < P) {
+      if (df) {  // (hi, lo) FP32 pair storage
+        const float2 hl = __ldcs(reinterpret_cast<const float2 *>(D) + (long long)(k0 + k) * ldd + p);
+        v = (double)hl.x + (double)hl.y;
+      } else {
+        v = __ldcs(D + (long long)(k0 + k) * ldd + p);
+      }
+    }
+    tile[k * 128 + t] = v;
+    mx = fmax(mx, fabs(v));
+  }
+  const int E = fh_chunk_exp(mx);
+  if (p < Ppad) Ed[(long long)(k0 / kBK) * Ppad + p] = (int8_t)E;
+  const long long plane = Ppad * (long long)Kcap;
+  if (p >= Ppad) return;
+#pragma unroll 1
+  for (int v = 0; v < kBK / 8; ++v) {
+    __align__(16) __nv_bfloat16 c[kSlices][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      __nv_bfloat16 bs[kSlices];
+      fh_slice4(tile[(v * 8 + i) * 128 + t], E, bs);
+#pragma unroll
+      for (int q = 0; q < kSlices; ++q) c[q][i] = bs[q];
+    }
+#pragma unroll
+    for (int q = 0; q < kSlices; ++q)
+      reinterpret_cast<uint4 *>(H3 + q * plane + p * Kcap + k0)[v] = *reinterpret_cast<const uint4 *>(c[q]);
+  }
+}
+
+// ------------------------------------------------------------------- host
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static int get_encode(fh_ctx *ctx) {
+  if (g_encode) return FH_OK;
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+    return fh_set_error(ctx, FH_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return FH_OK;
+}
+
+// 3D bf16 tensor {d0 (contiguous), d1, 3 planes}, box {64, rows, 1}, 128-byte swizzle.
+static int make_map(fh_ctx *ctx, CUtensorMap *map, void *base, unsigned long long d0, unsigned long long d1,
+                    unsigned rows) {
+  int rc = get_encode(ctx);
+  if (rc) return rc;
+  cuuint64_t dims[3] = {d0, d1, (cuuint64_t)kSlices};
+  cuuint64_t strides[2] = {d0 * 2, d0 * d1 * 2};
+  cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fh_set_error(ctx, FH_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FH_OK;
+}
+
+// Plane storage, exponent tables and tensor maps of one blocked contraction.
+struct fh_blk {
+  long long P = 0, Ppad = 0;
+  int Kcap = 0;
+  fh_dbuf H3, A3, Ed, Ew, err;
+  CUtensorMap mapA, mapB;
+};
+
+fh_blk *fh_blk_new() { return new fh_blk(); }
+void fh_blk_delete(fh_blk *b) { delete b; }
+long long fh_blk_ppad(const fh_blk &b) { return b.Ppad; }
+
+int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
+  FH_REQUIRE(ctx, Kcap % kBK == 0 && Kcap > 0, FH_EINVAL, "blocked contraction: capacity must be a multiple of 64");
+  b.P = P;
+  b.Ppad = fh_ceil_div(P, 128) * 128;
+  b.Kcap = Kcap;
+  int rc;
+  if ((rc = fh_alloc(ctx, b.H3, sizeof(__nv_bfloat16) * kSlices * (size_t)b.Ppad * Kcap)) ||
+      (rc = fh_alloc(ctx, b.A3, sizeof(__nv_bfloat16) * kSlices * (size_t)kBM * Kcap)) ||
+      (rc = fh_alloc(ctx, b.Ed, (size_t)b.Ppad * (Kcap / kBK))) ||
+      (rc = fh_alloc(ctx, b.Ew, (size_t)kBM * (Kcap / kBK))) || (rc = fh_alloc(ctx, b.err, sizeof(int))))
+    return rc;
+  if ((rc = make_map(ctx, &b.mapA, b.A3.p, (unsigned long long)Kcap, kBM, kBM))) return rc;
+  if ((rc = make_map(ctx, &b.mapB, b.H3.p, (unsigned long long)Kcap, (unsigned long long)b.Ppad, kBN))) return rc;
+  static bool attr = false;
+  if (!attr) {
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_far_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(sizeof(double) * kBK * 128)));
+    attr = true;
+  }
+  return FH_OK;
+}
+
+// Converts layers [k0, k0+64) of the FP64 history into the planes and exponents.
+int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df) {
+  FH_REQUIRE(ctx, k0 % kBK == 0 && k0 + kBK <= b.Kcap, FH_EINVAL, "blocked contraction: bad layer block %d", k0);
+  k_blk_convert<<<(unsigned)(b.Ppad / 128), 128, sizeof(double) * kBK * 128, ctx->stream>>>(
+      D, ldd, b.P, b.Ppad, k0, b.Kcap, df, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+  return fh_after_launch(ctx, "k_blk_convert");
+}
+
+// Weight planes of the TG block starting at step j0 (K = j0 history layers).
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta) {
+  dim3 g((unsigned)(j0 / kBK), kBM / 8);
+  k_blk_weights<<<g, 256, 0, ctx->stream>>>(j0, j0, b.Kcap, Da, tau, alpha, beta, b.A3.as<__nv_bfloat16>(),
+                                           b.Ew.as<int8_t>());
+  return fh_after_launch(ctx, "k_blk_weights");
+}
+
+// S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p].
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, double *out, long long ldo) {
+  FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  k_far_gemm<<<(unsigned)(b.Ppad / kBN), kThreads, kSmemBytes, ctx->stream>>>(
+      b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, b.err.as<int>());
+  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  return fh_after_launch(ctx, "k_far_gemm");
+}
+
+int fh_blk_check(fh_ctx *ctx, fh_blk &b) {
+  int h = 0;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(&h, b.err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) return fh_set_error(ctx, FH_ETIMEOUT, "blocked contraction: a bounded wait expired");
+  return FH_OK;
+}
+
+extern "C" int fh_history_contract_bf16x3(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
+                                          const double *D, long long ldd, double *S, long long ldS) {
+  FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
+  FH_REQUIRE(ctx, K > 0 && K % kBK == 0 && K <= 65536, FH_EINVAL,
+             "fh_history_contract_bf16x3: K must be a positive multiple of 64");
+  FH_REQUIRE(ctx, P > 0 && ldd >= P && ldS >= P && ldw >= K, FH_EINVAL, "fh_history_contract_bf16x3: bad sizes");
+  FH_REQUIRE(ctx, W && D && S, FH_EINVAL, "fh_history_contract_bf16x3: null pointer");
+  fh_blk b;
+  int rc = fh_blk_init(ctx, b, P, K);
+  if (rc) return rc;
+  dim3 g((unsigned)(K / kBK), kBM / 8);
+  k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(W, ldw, K, K, b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
+  if ((rc = fh_after_launch(ctx, "k_blk_split_rows"))) return rc;
+  for (int k0 = 0; k0 < K; k0 += kBK)
+    if ((rc = fh_blk_convert(ctx, b, D, ldd, k0, 0))) return rc;
+  if ((rc = fh_blk_gemm(ctx, b, K, S, ldS))) return rc;
+  return fh_blk_check(ctx, b);
+}

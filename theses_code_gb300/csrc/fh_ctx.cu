@@ -135,6 +135,24 @@ int fh_ctx_sync(fh_ctx *ctx) {
   return FH_OK;
 }
 
+int fh_ctx_set_graphs(fh_ctx *ctx, int enable) {
+  FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
+  ctx->graphs = enable != 0;
+  return FH_OK;
+}
+
+int fh_ctx_query(fh_ctx *ctx) {
+  if (!ctx) return -FH_EINVAL;
+  const cudaError_t e = cudaStreamQuery(ctx->stream);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) {
+    cudaGetLastError();
+    return 0;
+  }
+  fh_set_error(ctx, FH_ECUDA, "cudaStreamQuery: %s", cudaGetErrorString(e));
+  return -FH_ECUDA;
+}
+
 int fh_ctx_set_stream(fh_ctx *ctx, void *stream) {
   FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
   if (ctx->own_stream && ctx->stream) {

@@ -36,6 +36,8 @@ struct fh_h_batch {
   std::vector<long long> off;
   std::vector<fh_h_tile> tiles;
   fh_dbuf inst, tl, U, D, W, wc, part, Al, Bt;
+  fh_graph_cache graph;
+  bool use_graph = true;
 };
 
 static constexpr int kTileThreads = 256;  // 512 nodes per tile
@@ -303,6 +305,22 @@ int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host) {
   return FH_OK;
 }
 
+int fh_h_batch_set_u(fh_h_batch *b, const double *U) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, U, FH_EINVAL, "fh_h_batch_set_u: null pointer");
+  long long src = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const size_t cnt = (size_t)b->hp[i].N + 2;
+    FH_CUDA_TRY(ctx, cudaMemcpyAsync(b->U.as<double>() + b->off[i], U + src, sizeof(double) * cnt,
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
+    src += (long long)cnt;
+  }
+  b->tstep = 1;
+  b->nsaved = 0;
+  return FH_OK;
+}
+
 int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
   fh_ctx *ctx = b->ctx;
@@ -318,12 +336,42 @@ int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host) {
   return FH_OK;
 }
 
+int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_host) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, U_host && first >= 0 && count >= 0 && first + count <= b->n, FH_EINVAL,
+             "fh_h_batch_get_u_range_host: bad range");
+  long long dst = 0;
+  for (int i = first; i < first + count; ++i) {
+    const size_t cnt = (size_t)b->hp[i].N + 2;
+    FH_CUDA_TRY(ctx, cudaMemcpyAsync(U_host + dst, b->U.as<double>() + b->off[i], sizeof(double) * cnt,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    dst += (long long)cnt;
+  }
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FH_OK;
+}
+
 int fh_h_batch_step(fh_h_batch *b, int nsteps) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
   fh_ctx *ctx = b->ctx;
   FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_h_batch_step: nsteps < 0");
   FH_REQUIRE(ctx, b->nsaved + nsteps <= b->max_steps, FH_ENOMEM, "fh_h_batch_step: history full (%d + %d > %d)",
              b->nsaved, nsteps, b->max_steps);
+  if (b->use_graph && ctx->graphs && b->nsaved == 0 && nsteps > 1 && !ctx->prof) {
+    // whole solve from the initial state: capture once, replay afterwards
+    int rc = fh_graph_run(ctx, b->graph, nsteps, [&]() {
+      for (int i = 0; i < nsteps; ++i) {
+        int r = h_one_step(b);
+        if (r) return r;
+      }
+      return (int)FH_OK;
+    });
+    if (rc) return rc;
+    b->tstep = 1 + nsteps;
+    b->nsaved = nsteps;
+    return FH_OK;
+  }
   for (int i = 0; i < nsteps; ++i) {
     int rc = h_one_step(b);
     if (rc) return rc;

@@ -71,6 +71,104 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum(const double *__restr
   }
 }
 
+// Double-float variant: D holds (hi, lo) FP32 pairs (value = hi + lo, 2^-48
+// relative), the weights are split into pairs in shared memory, and the M sums
+// are carried as double-float with TwoSum on the FP32 pipe; partials are
+// written as FP64 (hi + lo).  On GB300 the FP32 pipe delivers ~56x the FP64
+// FMA rate, so this form streams the history at HBM speed.
+template <int M>
+__global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__restrict__ D, long long ldd, long long P,
+                                                              int K, const double *__restrict__ W, int ldw,
+                                                              int kchunk, double *__restrict__ part,
+                                                              long long ldpart) {
+  extern __shared__ float2 wsf[];  // [M][kchunk] (hi, lo)
+  const int s = blockIdx.y;
+  const int k0 = s * kchunk;
+  const int nk = min(K, k0 + kchunk) - k0;
+  for (int i = threadIdx.x; i < M * nk; i += blockDim.x) {
+    const int m = i / nk, k = i - m * nk;
+    const double w = W[(long long)m * ldw + k0 + k];
+    const float wh = __double2float_rn(w);
+    wsf[m * kchunk + k] = make_float2(wh, __double2float_rn(w - (double)wh));
+  }
+  __syncthreads();
+  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (p >= P) return;
+  float ah[M][2], al[M][2];
+#pragma unroll
+  for (int m = 0; m < M; ++m) ah[m][0] = ah[m][1] = al[m][0] = al[m][1] = 0.f;
+  const float4 *d = reinterpret_cast<const float4 *>(D + (long long)k0 * ldd + p);
+  const long long ld4 = ldd / 2;  // float4 = two points
+  auto acc = [&](const float2 w, const float dh, const float dl, float &sh, float &sl) {
+    const float ph = w.x * dh;
+    float pl = fmaf(w.x, dh, -ph);
+    pl = fmaf(w.x, dl, pl);
+    pl = fmaf(w.y, dh, pl);
+    const float t = sh + ph;
+    const float bb = t - sh;
+    const float e = (sh - (t - bb)) + (ph - bb);
+    sh = t;
+    sl += e + pl;
+  };
+  int k = 0;
+  for (; k + 2 <= nk; k += 2) {
+    const float4 v0 = __ldcs(d);
+    const float4 v1 = __ldcs(d + ld4);
+    d += 2 * ld4;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const float2 w0 = wsf[m * kchunk + k], w1 = wsf[m * kchunk + k + 1];
+      acc(w0, v0.x, v0.y, ah[m][0], al[m][0]);
+      acc(w0, v0.z, v0.w, ah[m][1], al[m][1]);
+      acc(w1, v1.x, v1.y, ah[m][0], al[m][0]);
+      acc(w1, v1.z, v1.w, ah[m][1], al[m][1]);
+    }
+    if ((k & 15) == 14) {
+#pragma unroll
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {  // renormalise (fast two-sum, |ah| >= |al|)
+          const float t = ah[m][q] + al[m][q];
+          al[m][q] = al[m][q] - (t - ah[m][q]);
+          ah[m][q] = t;
+        }
+    }
+  }
+  for (; k < nk; ++k) {
+    const float4 v = __ldcs(d);
+    d += ld4;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const float2 w = wsf[m * kchunk + k];
+      acc(w, v.x, v.y, ah[m][0], al[m][0]);
+      acc(w, v.z, v.w, ah[m][1], al[m][1]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    double2 o;
+    o.x = (double)ah[m][0] + (double)al[m][0];
+    o.y = (double)ah[m][1] + (double)al[m][1];
+    *reinterpret_cast<double2 *>(part + ((long long)s * M + m) * ldpart + p) = o;
+  }
+}
+
+int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
+                                   const float2 *D, long long ldd, int splits, int kchunk, double *part,
+                                   long long ldpart) {
+  if (K <= 0 || P <= 0) return FH_OK;
+  dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
+  const size_t smem = sizeof(float2) * (size_t)M * (size_t)kchunk;
+  FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large (%d layers)", kchunk);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  if (M == 1)
+    k_hist_sum_df<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+  else
+    k_hist_sum_df<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  return fh_after_launch(ctx, "k_hist_sum_df");
+}
+
 // out[m*ldS + p] = sum_s part[(s*M+m)*ldpart + p]
 __global__ void k_hist_reduce(int M, int splits, long long P, const double *__restrict__ part, long long ldpart,
                               double *__restrict__ S, long long ldS) {

@@ -22,6 +22,7 @@ struct fh_ctx {
   bool own_stream = false;
   long long launches = 0;
   bool prof = false;
+  bool graphs = true;  // whole solves from the initial state replay a captured graph
   fh_prof_kind pk[3];
   char err[512] = {0};
 };
@@ -47,6 +48,53 @@ int fh_after_launch(fh_ctx *ctx, const char *what);
     if (!(cond)) return fh_set_error((ctx), (code), __VA_ARGS__); \
   } while (0)
 
+// Replays a captured launch sequence: the first run of `nsteps` steps from the
+// initial state is recorded by stream capture and instantiated; later runs
+// from the same initial state launch the graph.
+struct fh_graph_cache {
+  cudaGraphExec_t exec = nullptr;
+  int nsteps = -1;
+  ~fh_graph_cache() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+// Runs body() (which enqueues the launches of `nsteps` steps on ctx->stream)
+// under capture the first time and replays it afterwards.  body must only
+// enqueue work (no synchronisation, no allocation).
+template <class Body>
+int fh_graph_run(fh_ctx *ctx, fh_graph_cache &gc, int nsteps, Body body) {
+  if (gc.exec && gc.nsteps == nsteps) {
+    cudaError_t e = cudaGraphLaunch(gc.exec, ctx->stream);
+    if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+    ctx->launches += 1;
+    return FH_OK;
+  }
+  if (gc.exec) {
+    cudaGraphExecDestroy(gc.exec);
+    gc.exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+  const int rc = body();
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&gc.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    gc.exec = nullptr;
+    return fh_set_error(ctx, FH_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  }
+  gc.nsteps = nsteps;
+  e = cudaGraphLaunch(gc.exec, ctx->stream);
+  if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+  return FH_OK;
+}
+
 // Device allocation owned by an object; freed in its destructor.
 struct fh_dbuf {
   void *p = nullptr;
@@ -69,5 +117,8 @@ int fh_launch_weights_psi(fh_ctx *ctx, int K, double x0, double len, double X, d
 int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                 const double *D, long long ldd, int splits, int kchunk, double *part,
                                 long long ldpart);
+int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
+                                   const float2 *D, long long ldd, int splits, int kchunk, double *part,
+                                   long long ldpart);
 // Chooses the split count for a K x P history sum given a partial-buffer capacity.
 void fh_hist_plan(long long P, int K, int max_splits, int *splits, int *kchunk);

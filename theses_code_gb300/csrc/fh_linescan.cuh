@@ -83,3 +83,47 @@ __device__ __forceinline__ void fh_line_solve_cached(const Line &L, int N, doubl
   }
   __syncwarp();
 }
+
+// ------------------------------------------------------------------------
+// Staged variant: the line's coefficients already sit in shared memory.
+// Index skew sk(i) = i + i/16 keeps the per-lane chunks (16 consecutive
+// equations per lane for lines up to 513 nodes) on distinct bank pairs.
+__device__ __forceinline__ int fh_sk(int i) { return i + (i >> 4); }
+
+// fa/fb: forward maps Bt[i+1] = fa_i Bt[i] + fb_i (i = 1..N-1); al: Al[i+1]
+// (i = 1..N-1).  bt: scratch; u: result u_i (i = 0..N+1), may alias fa.
+__device__ __forceinline__ void fh_line_solve_staged(int N, const double *fa, const double *fb, const double *al,
+                                                     double al1, double bt1, double *bt, double *u) {
+  const int lane = threadIdx.x & 31;
+  const int nf = N - 1;
+  const int chf = (nf + 31) / 32;
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  fh_aff F{1.0, 0.0};
+  for (int i = f0; i < f1; ++i) F = fh_aff_compose(fh_aff{fa[fh_sk(i)], fb[fh_sk(i)]}, F);
+  const fh_aff Pf = fh_warp_exclusive_affine(F);
+  double b = fma(Pf.a, bt1, Pf.b);
+  for (int i = f0; i < f1; ++i) {
+    b = fma(fa[fh_sk(i)], b, fb[fh_sk(i)]);
+    bt[fh_sk(i)] = b;
+  }
+  if (lane == 0) bt[fh_sk(0)] = bt1;
+  __syncwarp();
+  const double alN = (N >= 2) ? al[fh_sk(N - 1)] : al1;
+  const double uN = bt[fh_sk(N - 1)] / (1.0 - alN);
+  const int chb = (N + 31) / 32;
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  fh_aff G{1.0, 0.0};
+  for (int i = b1 - 1; i >= b0; --i) G = fh_aff_compose(fh_aff{(i >= 1) ? al[fh_sk(i)] : al1, bt[fh_sk(i)]}, G);
+  const fh_aff Pb = fh_warp_exclusive_affine_rev(G);
+  double v = fma(Pb.a, uN, Pb.b);
+  __syncwarp();  // u may alias fa: all forward reads are done
+  for (int i = b1 - 1; i >= b0; --i) {
+    v = fma((i >= 1) ? al[fh_sk(i)] : al1, v, bt[fh_sk(i)]);
+    u[fh_sk(i)] = v;
+  }
+  if (lane == 0) {
+    u[fh_sk(N)] = uN;
+    u[fh_sk(N + 1)] = uN;
+  }
+  __syncwarp();
+}

@@ -23,6 +23,17 @@
 #include "fh_linescan.cuh"
 #include "fh_weights.cuh"
 
+// blocked contraction helpers (fh_blocked.cu)
+struct fh_blk;
+fh_blk *fh_blk_new();
+void fh_blk_delete(fh_blk *b);
+int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
+int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta);
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, double *out, long long ldo);
+long long fh_blk_ppad(const fh_blk &b);
+static constexpr int kTgBlock = 64;  // steps per block (128 weight rows)
+
 struct fh_tg_dev {
   int sN, M, ld;
   long long P;
@@ -34,26 +45,36 @@ struct fh_tg_solver {
   fh_tg_params p{};
   fh_tg_dev dv{};
   int mode = FH_TG_FP64;
+  bool df = false;        // history stored as (hi, lo) FP32 pairs
   int max_steps = 0;
   int tstep = 0;
   bool have_state = false;
   bool factor_fixed = false;
   int max_splits = 8;
-  fh_dbuf C, Cfull, V2, D, W, cw, part, alx, gx, aly, gy;
+  fh_dbuf C, Cfull, V2, D, W, cw, part, alx, gx, aly, gy, far;
+  bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
+  fh_blk *blk = nullptr;  // blocked mode: bf16x3 planes and tensor maps
+  int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
+  long long ldfar = 0;
+  fh_graph_cache graph;
+  ~fh_tg_solver() {
+    if (blk) fh_blk_delete(blk);
+  }
 };
 
 // ---------------------------------------------------------------- kernels
 
 // W[0][k] = kb(k,0.5,0.0,1.0), W[1][k] = kb(k,1.0,0.0,1.0) for k < j;
 // cw = {kb(j,0.5,0.0,0.5), kb(j,1.0,0.5,0.5), kb(j,1.0,0.0,0.5)} (TG_solver_::kb).
-__global__ void k_tg_weights(fh_tg_dev g, int j, double *__restrict__ W, int ldw, double *__restrict__ cw) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_tg_weights(fh_tg_dev g, int j, int kstart, double *__restrict__ W, int ldw,
+                             double *__restrict__ cw) {
+  const int k = kstart + blockIdx.x * blockDim.x + threadIdx.x;
   if (k < j) {
     const double s0 = (double)k + 0.0;
     W[k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta);
     W[ldw + k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta);
   }
-  if (k == 0) {
+  if (k == kstart) {
     const double jj = (double)j;
     cw[0] = g.Da * fh_psi_int(jj + 0.0, jj + 0.0 + 0.5, jj + 0.5, g.tau, g.alpha, g.beta);
     cw[1] = g.Da * fh_psi_int(jj + 0.5, jj + 0.5 + 0.5, jj + 1.0, g.tau, g.alpha, g.beta);
@@ -94,132 +115,146 @@ __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2,
   }
 }
 
-struct TgXLine {
-  long long base;  // line j: point i at base + i
-  const double *V2, *C, *part, *gg;
-  double *Cw;
-  long long ldp;
-  int splits;
-  double dl, d, st, S, kx;
-  __device__ double A(int i) const { return (V2[base + i] / dl) * ((0.5 * (d + d) / dl) + 0.5); }
-  __device__ double om(int i) const {
+// All step weights of a solve in one launch: row j of Wall holds
+// [kb(k,0.5,0,1) for k < j | kb(k,1,0,1) for k < j] (x and y rows, pitch ldw),
+// cwall[4j..4j+2] the three current weights of step j.
+__global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ Wall, int ldw,
+                                 double *__restrict__ cwall) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (j >= nsteps) return;
+  double *W = Wall + (long long)j * 2 * ldw;
+  if (k < j) {
+    const double s0 = (double)k + 0.0;
+    W[k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta);
+    W[ldw + k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta);
+  }
+  if (k == 0) {
+    const double jj = (double)j;
+    cwall[4 * j + 0] = g.Da * fh_psi_int(jj + 0.0, jj + 0.0 + 0.5, jj + 0.5, g.tau, g.alpha, g.beta);
+    cwall[4 * j + 1] = g.Da * fh_psi_int(jj + 0.5, jj + 0.5 + 0.5, jj + 1.0, g.tau, g.alpha, g.beta);
+    cwall[4 * j + 2] = g.Da * fh_psi_int(jj + 0.0, jj + 0.0 + 0.5, jj + 1.0, g.tau, g.alpha, g.beta);
+  }
+}
+
+// Shared-memory footprint of one staged line: 5 arrays of fh_sk(N+2)+1 doubles.
+__host__ __device__ inline int tg_line_stride(int N) { return (N + 2) + ((N + 2) >> 4) + 2; }
+
+// x half-step (fr_d_t_g_2d.cpp:2577-2590): one warp per line j = 1..M-1, the
+// line staged with coalesced loads, then solved from shared memory.
+__global__ void k_tg_xsweep(fh_tg_dev g, const double *__restrict__ V2, double *C, const double *__restrict__ part,
+                            long long ldp, int splits, const double *__restrict__ alx, const double *__restrict__ gx,
+                            const double *__restrict__ cw, const double *__restrict__ far) {
+  extern __shared__ double sbuf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int line = 1 + blockIdx.x * (blockDim.x >> 5) + warp;
+  if (line >= g.M) return;  // whole warp exits together
+  const int N = g.sN;
+  const int L = tg_line_stride(N);
+  double *fa = sbuf + (size_t)warp * 4 * L, *fb = fa + L, *al = fb + L, *bt = al + L;
+  const long long base = (long long)line * g.ld;
+  const double kx = cw[0], dl = g.dL;
+  const double cA = (0.5 * (g.d + g.d) / dl) + 0.5;
+  for (int i = 1 + lane; i < N; i += 32) {
     const long long id = base + i;
     double ts = 0.0;
     for (int s = 0; s < splits; ++s) ts += part[(long long)(2 * s) * ldp + id];
-    double o = -st * (kx + 0.0) * C[id];
-    o += S * 0.5;
-    o += st * ts;
-    return o;
+    if (far) ts += far[id];
+    double om = -g.st * (kx + 0.0) * C[id];
+    om += g.S * 0.5;
+    om += g.st * ts;
+    const double A = (V2[id] / dl) * cA;
+    const double gi = gx[id];
+    fa[fh_sk(i)] = gi * A;
+    fb[fh_sk(i)] = -gi * om;
+    al[fh_sk(i)] = alx[id];
   }
-  __device__ double g(int i) const { return gg[base + i]; }
-  __device__ double al(int i) const { return al_[base + i]; }
-  const double *al_;
-  __device__ void store(int i, double u) const { Cw[base + i] = u; }
-};
-
-__global__ void k_tg_xsweep(fh_tg_dev g, const double *__restrict__ V2, double *C,
-                            const double *__restrict__ part, long long ldp, int splits,
-                            const double *__restrict__ al, const double *__restrict__ gg,
-                            const double *__restrict__ cw) {
-  extern __shared__ double sbuf[];
-  const int warp = threadIdx.x >> 5;
-  const int line = 1 + blockIdx.x * (blockDim.x >> 5) + warp;
-  if (line >= g.M) return;  // whole warp exits together
-  double *buf = sbuf + (size_t)warp * (g.sN + 1);
-  TgXLine L;
-  L.base = (long long)line * g.ld;
-  L.V2 = V2;
-  L.C = C;
-  L.part = part;
-  L.al_ = al;
-  L.gg = gg;
-  L.Cw = C;
-  L.ldp = ldp;
-  L.splits = splits;
-  L.dl = g.dL;
-  L.d = g.d;
-  L.st = g.st;
-  L.S = g.S;
-  L.kx = cw[0];
-  fh_line_solve_cached(L, g.sN, 0.0, g.C1, buf);
+  __syncwarp();
+  fh_line_solve_staged(N, fa, fb, al, 0.0, g.C1, bt, fa);
+  for (int i = lane; i <= N + 1; i += 32) C[base + i] = fa[fh_sk(i)];
 }
 
-struct TgYLine {
-  long long base, ld;  // line i: element q at base + q*ld
-  const double *V2, *C, *part, *al_, *gg;
-  double *Cw, *Cfull, *Dj;
-  long long ldp;
-  int splits, M;
-  double dl, d, st, S, ky, kyh;
-  __device__ long long id(int q) const { return base + (long long)q * ld; }
-  __device__ double A(int q) const { return (V2[id(q)] / (dl * dl)) * 0.5 * (d + d); }
-  __device__ double om(int q) const {
-    const long long k = id(q);
-    double ts = 0.0;
-    for (int s = 0; s < splits; ++s) ts += part[(long long)(2 * s + 1) * ldp + k];
-    const double c = C[k];
-    ts += (kyh + 0.0) * (Cfull[k] - c);  // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
-    double o = -st * (ky + 0.0) * c;
-    o += S * 0.5;
-    o += st * ts;
-    return o;
-  }
-  __device__ double g(int q) const { return gg[id(q)]; }
-  __device__ double al(int q) const { return al_[id(q)]; }
-  __device__ void store(int q, double u) const {
-    const long long k = id(q);
-    if (q >= 1 && q < M) {
-      Dj[k] = u - Cfull[k];
-      Cfull[k] = u;
-    }
-    Cw[k] = u;
-  }
-};
-
-__global__ void k_tg_ysweep(fh_tg_dev g, const double *__restrict__ V2, double *C,
-                            double *Cfull, double *__restrict__ Dj, const double *__restrict__ part,
-                            long long ldp, int splits, const double *__restrict__ al,
-                            const double *__restrict__ gg, const double *__restrict__ cw) {
+// y half-step (fr_d_t_g_2d.cpp:2634-2648): 4 adjacent lines i per CTA so the
+// strided column loads share sectors; one warp solves one line.  Appends the
+// full-step difference D_j = C^{j+1} - C^j and refreshes Cfull.
+__global__ void __launch_bounds__(128) k_tg_ysweep(fh_tg_dev g, const double *__restrict__ V2, double *C,
+                                                   double *Cfull, double *__restrict__ Dj,
+                                                   const double *__restrict__ part, long long ldp, int splits,
+                                                   const double *__restrict__ aly, const double *__restrict__ gy,
+                                                   const double *__restrict__ cw, const double *__restrict__ far,
+                                                   int dfstore) {
   extern __shared__ double sbuf[];
   const int warp = threadIdx.x >> 5;
-  const int line = 1 + blockIdx.x * (blockDim.x >> 5) + warp;
-  if (line >= g.sN) return;
-  double *buf = sbuf + (size_t)warp * (g.M + 1);
-  TgYLine L;
-  L.base = line;
-  L.ld = g.ld;
-  L.V2 = V2;
-  L.C = C;
-  L.part = part;
-  L.al_ = al;
-  L.gg = gg;
-  L.Cw = C;
-  L.Cfull = Cfull;
-  L.Dj = Dj;
-  L.ldp = ldp;
-  L.splits = splits;
-  L.M = g.M;
-  L.dl = g.dLx;
-  L.d = g.d;
-  L.st = g.st;
-  L.S = g.S;
-  L.ky = cw[1];
-  L.kyh = cw[2];
-  fh_line_solve_cached(L, g.M, 1.0, 0.0, buf);
+  const int N = g.M;
+  const int L = tg_line_stride(N);
+  const int i0 = 1 + blockIdx.x * 4;
+  const double ky = cw[1], kyh = cw[2], dl = g.dLx;
+  const double cA = 0.5 * (g.d + g.d) / (dl * dl);
+  // staging: thread t handles column t%4 and rows t/4, t/4 + 32, ...
+  const int col = threadIdx.x & 3;
+  const int line = i0 + col;
+  double *fa = sbuf + (size_t)col * 5 * L, *fb = fa + L, *al = fb + L, *bt = al + L, *cf = bt + L;
+  if (line < g.sN) {
+    for (int q = (threadIdx.x >> 2); q <= N + 1; q += 32) {
+      const long long id = line + (long long)q * g.ld;
+      const double c = C[id];
+      if (q >= 1 && q < N) {
+        double ts = 0.0;
+        for (int s = 0; s < splits; ++s) ts += part[(long long)(2 * s + 1) * ldp + id];
+        if (far) ts += far[id];
+        const double f = Cfull[id];
+        ts += (kyh + 0.0) * (f - c);  // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
+        double om = -g.st * (ky + 0.0) * c;
+        om += g.S * 0.5;
+        om += g.st * ts;
+        const double A = V2[id] * cA;
+        const double gi = gy[id];
+        fa[fh_sk(q)] = gi * A;
+        fb[fh_sk(q)] = -gi * om;
+        al[fh_sk(q)] = aly[id];
+        cf[fh_sk(q)] = f;
+      }
+    }
+  }
+  __syncthreads();
+  const int wline = i0 + warp;
+  if (wline < g.sN) {
+    double *wfa = sbuf + (size_t)warp * 5 * L;
+    fh_line_solve_staged(N, wfa, wfa + L, wfa + 2 * L, 1.0, 0.0, wfa + 3 * L, wfa);
+  }
+  __syncthreads();
+  if (line < g.sN) {
+    for (int q = (threadIdx.x >> 2); q <= N + 1; q += 32) {
+      const long long id = line + (long long)q * g.ld;
+      const double u = fa[fh_sk(q)];
+      C[id] = u;
+      if (q >= 1 && q < N) {
+        const double dd = u - cf[fh_sk(q)];
+        if (dfstore) {  // (hi, lo) FP32 pair, 2^-48 relative
+          const float h = __double2float_rn(dd);
+          reinterpret_cast<float2 *>(Dj)[id] = make_float2(h, __double2float_rn(dd - (double)h));
+        } else {
+          Dj[id] = dd;
+        }
+        Cfull[id] = u;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------------ host
 
 static constexpr int kSweepWarps = 4;
+static constexpr int kWeightTableMaxSteps = 4096;  // 2 x 4096^2 doubles = 268 MB
 
-static int tg_factor(fh_tg_solver *s) {
+static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), s->cw.as<double>(),
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), cwj,
                                                                      s->alx.as<double>(), s->gx.as<double>());
   int rc = fh_after_launch(ctx, "k_tg_factor(x)");
   if (rc) return rc;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), s->cw.as<double>(),
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), cwj,
                                                                       s->aly.as<double>(), s->gy.as<double>());
   return fh_after_launch(ctx, "k_tg_factor(y)");
 }
@@ -230,34 +265,82 @@ static int tg_one_step(fh_tg_solver *s) {
   const int j = s->tstep;
   const int ldw = s->max_steps;
   int rc;
-  fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
-  k_tg_weights<<<(unsigned)fh_ceil_div(j > 0 ? j : 1, 128), 128, 0, ctx->stream>>>(g, j, s->W.as<double>(), ldw,
-                                                                                   s->cw.as<double>());
-  fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
-  if ((rc = fh_after_launch(ctx, "k_tg_weights"))) return rc;
+  const bool blocked = s->blk != nullptr;
+  if (blocked && j > 0 && j % kTgBlock == 0) {
+    // new block: planes for layers [j-64, j), weight planes for steps j..j+63,
+    // far rows S_far[2r + {0,1}] = sum_{k<j} w_{j+r}(k) D[k] on the tensor cores
+    fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
+    if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), g.P, j - kTgBlock, s->df ? 1 : 0))) return rc;
+    if ((rc = fh_blk_tg_weights(ctx, *s->blk, j, g.Da, g.tau, g.alpha, g.beta))) return rc;
+    fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
+    if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<double>(), s->ldfar))) return rc;
+    s->j0 = j;
+  }
+  const int kstart = blocked ? s->j0 : 0;  // history layers summed in FP64 this step
+  const int knear = j - kstart;
+  const double *Wj;
+  if (s->wtab) {
+    if (j == 0) {
+      fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
+      dim3 gw((unsigned)fh_ceil_div(s->max_steps, 128), (unsigned)s->max_steps);
+      k_tg_weights_all<<<gw, 128, 0, ctx->stream>>>(g, s->max_steps, s->W.as<double>(), ldw, s->cw.as<double>());
+      fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
+      if ((rc = fh_after_launch(ctx, "k_tg_weights_all"))) return rc;
+    }
+    Wj = s->W.as<double>() + (long long)j * 2 * ldw;
+  } else {
+    fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
+    k_tg_weights<<<(unsigned)fh_ceil_div(knear > 0 ? knear : 1, 128), 128, 0, ctx->stream>>>(
+        g, j, kstart, s->W.as<double>(), ldw, s->cw.as<double>());
+    fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
+    if ((rc = fh_after_launch(ctx, "k_tg_weights"))) return rc;
+    Wj = s->W.as<double>();
+  }
+  const double *cwj = s->wtab ? s->cw.as<double>() + 4LL * j : s->cw.as<double>();
   if (!s->factor_fixed || j == 0)
-    if ((rc = tg_factor(s))) return rc;
+    if ((rc = tg_factor(s, cwj))) return rc;
   int splits = 0, kchunk = 0;
-  if (j >= 1) {
-    fh_hist_plan(g.P, j, s->max_splits, &splits, &kchunk);
-    if ((rc = fh_launch_hist_sum_partials(ctx, 2, j, g.P, s->W.as<double>(), ldw, s->D.as<double>(), g.P, splits,
-                                          kchunk, s->part.as<double>(), g.P)))
-      return rc;
+  if (knear >= 1) {
+    fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
+    if (s->df)
+      rc = fh_launch_hist_sum_df_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
+                                          reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P,
+                                          g.P, splits, kchunk, s->part.as<double>(), g.P);
+    else
+      rc = fh_launch_hist_sum_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
+                                       s->D.as<double>() + (long long)kstart * g.P, g.P, splits, kchunk,
+                                       s->part.as<double>(), g.P);
+    if (rc) return rc;
+  }
+  const double *farx = nullptr, *fary = nullptr;
+  if (blocked && s->j0 > 0) {
+    const long long r = j - s->j0;
+    farx = s->far.as<double>() + (2 * r) * s->ldfar;
+    fary = s->far.as<double>() + (2 * r + 1) * s->ldfar;
   }
   const unsigned thr = 32 * kSweepWarps;
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-  size_t smx = sizeof(double) * (size_t)kSweepWarps * (g.sN + 1);
+  const size_t smx = sizeof(double) * (size_t)kSweepWarps * 4 * tg_line_stride(g.sN);
   k_tg_xsweep<<<(unsigned)fh_ceil_div(g.M - 1, kSweepWarps), thr, smx, ctx->stream>>>(
       g, s->V2.as<double>(), s->C.as<double>(), s->part.as<double>(), g.P, splits, s->alx.as<double>(),
-      s->gx.as<double>(), s->cw.as<double>());
+      s->gx.as<double>(), cwj, farx);
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
-  size_t smy = sizeof(double) * (size_t)kSweepWarps * (g.M + 1);
-  k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, kSweepWarps), thr, smy, ctx->stream>>>(
+  const size_t smy = sizeof(double) * 4 * 5 * (size_t)tg_line_stride(g.M);
+  k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), 128, smy, ctx->stream>>>(
       g, s->V2.as<double>(), s->C.as<double>(), s->Cfull.as<double>(), s->D.as<double>() + (long long)j * g.P,
-      s->part.as<double>(), g.P, splits, s->aly.as<double>(), s->gy.as<double>(), s->cw.as<double>());
+      s->part.as<double>(), g.P, splits, s->aly.as<double>(), s->gy.as<double>(), cwj, fary, s->df ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
   s->tstep++;
+  return FH_OK;
+}
+
+static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
+  const int smx = (int)(sizeof(double) * (size_t)kSweepWarps * 4 * tg_line_stride(sN));
+  const int smy = (int)(sizeof(double) * 4 * 5 * (size_t)tg_line_stride(M));
+  FH_REQUIRE(ctx, smx <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL, "fh_tg_create: grid too large for the sweeps");
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
   return FH_OK;
 }
 
@@ -272,11 +355,17 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
              "fh_tg_create: need 0 < alpha < 1, beta > 0, tau > 0");
   FH_REQUIRE(ctx, p->dL > 0.0 && p->dLx > 0.0 && p->sigma > 0.0, FH_EINVAL, "fh_tg_create: bad geometry");
   FH_REQUIRE(ctx, max_steps >= 1, FH_EINVAL, "fh_tg_create: max_steps >= 1");
-  FH_REQUIRE(ctx, mode == FH_TG_FP64, FH_ENOTSUP, "fh_tg_create: mode %d not available in this build", mode);
+  FH_REQUIRE(ctx, mode == FH_TG_FP64 || mode == FH_TG_BLOCKED || mode == FH_TG_DF64, FH_EINVAL,
+             "fh_tg_create: unknown mode %d", mode);
+  {
+    const int rc0 = tg_set_smem_attrs(ctx, p->sN, p->M);
+    if (rc0) return rc0;
+  }
   fh_tg_solver *s = new fh_tg_solver();
   s->ctx = ctx;
   s->p = *p;
   s->mode = mode;
+  s->df = (mode != FH_TG_FP64);
   s->max_steps = max_steps;
   fh_tg_dev &g = s->dv;
   g.sN = p->sN;
@@ -295,16 +384,31 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
   g.dL = p->dL;
   g.dLx = p->dLx;
   s->factor_fixed = (p->beta == 1.0);
+  s->wtab = max_steps <= kWeightTableMaxSteps;
   const size_t fld = sizeof(double) * (size_t)g.P;
   int rc;
   if ((rc = fh_alloc(ctx, s->C, fld)) || (rc = fh_alloc(ctx, s->Cfull, fld)) || (rc = fh_alloc(ctx, s->V2, fld)) ||
       (rc = fh_alloc(ctx, s->alx, fld)) || (rc = fh_alloc(ctx, s->gx, fld)) || (rc = fh_alloc(ctx, s->aly, fld)) ||
       (rc = fh_alloc(ctx, s->gy, fld)) || (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
-      (rc = fh_alloc(ctx, s->W, sizeof(double) * 2 * (size_t)max_steps)) ||
-      (rc = fh_alloc(ctx, s->cw, sizeof(double) * 4)) ||
+      (rc = fh_alloc(ctx, s->W, sizeof(double) * 2 * (size_t)max_steps *
+                                    (max_steps <= kWeightTableMaxSteps ? (size_t)max_steps : 1))) ||
+      (rc = fh_alloc(ctx, s->cw, sizeof(double) * 4 * (max_steps <= kWeightTableMaxSteps ? (size_t)max_steps : 1))) ||
       (rc = fh_alloc(ctx, s->part, fld * 2 * (size_t)s->max_splits, false))) {
     delete s;
     return rc;
+  }
+  if (mode == FH_TG_BLOCKED && max_steps > kTgBlock) {
+    s->blk = fh_blk_new();
+    const int kcap = (int)fh_ceil_div(max_steps, kTgBlock) * kTgBlock;
+    if ((rc = fh_blk_init(ctx, *s->blk, g.P, kcap))) {
+      delete s;
+      return rc;
+    }
+    s->ldfar = fh_blk_ppad(*s->blk);
+    if ((rc = fh_alloc(ctx, s->far, sizeof(double) * 2 * kTgBlock * (size_t)s->ldfar, false))) {
+      delete s;
+      return rc;
+    }
   }
   *out = s;
   return FH_OK;
@@ -326,6 +430,7 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->Cfull.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
   s->tstep = 0;
+  s->j0 = 0;
   s->have_state = true;
   return FH_OK;
 }
@@ -340,6 +445,7 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->Cfull.p, s->C.p, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->tstep = 0;
+  s->j0 = 0;
   s->have_state = true;
   return FH_OK;
 }
@@ -351,6 +457,19 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
   FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_tg_step: nsteps < 0");
   FH_REQUIRE(ctx, s->tstep + nsteps <= s->max_steps, FH_ENOMEM, "fh_tg_step: history full (%d + %d > %d)", s->tstep,
              nsteps, s->max_steps);
+  if (ctx->graphs && s->tstep == 0 && nsteps > 1 && !ctx->prof) {
+    int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
+      for (int n = 0; n < nsteps; ++n) {
+        int r = tg_one_step(s);
+        if (r) return r;
+      }
+      return (int)FH_OK;
+    });
+    if (rc) return rc;
+    s->tstep = nsteps;
+    s->j0 = (s->blk && nsteps > kTgBlock) ? ((nsteps - 1) / kTgBlock) * kTgBlock : 0;
+    return FH_OK;
+  }
   for (int n = 0; n < nsteps; ++n) {
     int rc = tg_one_step(s);
     if (rc) return rc;

@@ -31,13 +31,14 @@ class HSolverBatch:
         h = C.c_void_p()
         check(ctx.L.fh_h_batch_create(ctx.h, len(params), arr, int(max_steps), C.byref(h)), ctx.h)
         self.h = h
+        ctx.adopt(self)
         self.sizes = [p.N + 2 for p in self.params]
         self.total = int(ctx.L.fh_h_batch_state_size(h))
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.L.fh_h_batch_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -51,11 +52,24 @@ class HSolverBatch:
         assert flat.size == self.total
         check(self.ctx.L.fh_h_batch_set_u_host(self.h, _hptr(flat)), self.ctx.h)
 
+    def set_u_device(self, ptr: int):
+        check(self.ctx.L.fh_h_batch_set_u(self.h, C.c_void_p(ptr)), self.ctx.h)
+
     def get_u(self) -> list[np.ndarray]:
         out = np.empty(self.total)
         check(self.ctx.L.fh_h_batch_get_u_host(self.h, _hptr(out)), self.ctx.h)
         res, o = [], 0
         for s in self.sizes:
+            res.append(out[o:o + s].copy())
+            o += s
+        return res
+
+    def get_u_range(self, first: int, count: int) -> list[np.ndarray]:
+        sizes = self.sizes[first:first + count]
+        out = np.empty(sum(sizes))
+        check(self.ctx.L.fh_h_batch_get_u_range_host(self.h, int(first), int(count), _hptr(out)), self.ctx.h)
+        res, o = [], 0
+        for s in sizes:
             res.append(out[o:o + s].copy())
             o += s
         return res
@@ -77,12 +91,13 @@ class TGSolver:
         h = C.c_void_p()
         check(ctx.L.fh_tg_create(ctx.h, C.byref(self.p), int(max_steps), int(mode), C.byref(h)), ctx.h)
         self.h = h
+        ctx.adopt(self)
         self.shape = (self.p.M + 2, self.p.sN + 2)  # [j][i], idx = i + j*(sN+2)
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.L.fh_tg_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -124,11 +139,12 @@ class ABSolver:
         h = C.c_void_p()
         check(ctx.L.fh_ab_create(ctx.h, int(m), int(max_steps), float(tau), float(alpha), C.byref(h)), ctx.h)
         self.h = h
+        ctx.adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.L.fh_ab_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -146,6 +162,9 @@ class ABSolver:
     def set_c(self, C0: np.ndarray):
         C0 = np.ascontiguousarray(C0, dtype=np.float64)
         check(self.ctx.L.fh_ab_set_c_host(self.h, _hptr(C0)), self.ctx.h)
+
+    def set_c_device(self, ptr: int):
+        check(self.ctx.L.fh_ab_set_c(self.h, C.c_void_p(ptr)), self.ctx.h)
 
     def set_current_coef(self, Ii: float):
         check(self.ctx.L.fh_ab_set_current_coef(self.h, float(Ii)), self.ctx.h)
