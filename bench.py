@@ -2,17 +2,23 @@
 
 Default workload (N=1): the 2D Caputo-Gerasimov convection-diffusion ADI solve
 on a 512x512 grid, alpha 0.7, tau 5e-4, 2000 time steps with the full history
-(fr_d_t_g_2d.cpp TG_solver path).  One bench step = one complete 2000-step
-solve from the initial plume.  Metric: grid-point-steps/s (512*512*2000 per
-solve / seconds).
+(fr_d_t_g_2d.cpp TG_solver path), history in blocked form: the layers older
+than the current 64-step block are contracted on the tensor cores (exact bf16
+slices), the current block's layers in double-float.  One bench step = one
+complete 2000-step solve from the initial plume.  Metric: grid-point-steps/s
+(512*512*2000 per solve / seconds).  The same inputs are also solved once by
+the plain FP64 path and by the double-float path; the line reports their
+throughput and every result's relative max-norm difference to the FP64 path
+(the FP64 path itself matches the CPU oracle to <= 1e-12 in the parity tests).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--mode fp64|blocked] [--solve-steps S] [--grid G]
-                  [--config tg2d|caputo1d|psi_batch|ab1d]
+                  [--mode blocked|df64|fp64] [--solve-steps S] [--grid G]
+                  [--config tg2d|caputo1d|psi_batch|ab1d|serve] [--no-compare]
 
 Other configurations (not the default line): caputo1d (1D L1, N=200, 1000
-steps), psi_batch (4096 ragged psi-Caputo instances, 500-step sample of the
-5000-step solve), ab1d (Atangana-Baleanu, N=2048, 20000 steps).
+steps), psi_batch (4096 ragged psi-Caputo instances, sample of the 5000-step
+solve), ab1d (Atangana-Baleanu, N=2048, 20000 steps), serve (Poisson stream of
+mixed solves, p50/p99 latency).
 
 --impl reference times the CPU implementation of the same path (the oracle
 port of the reference solver, all host threads) on a bounded sample and prints
@@ -44,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="fp64", choices=["fp64", "df64", "blocked"])
+    ap.add_argument("--mode", default="blocked", choices=["fp64", "df64", "blocked"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the one-solve FP64 / double-float comparison")
     ap.add_argument("--solve-steps", type=int, default=2000)
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -110,12 +117,24 @@ class ClockSampler:
 
 
 def peaks():
+    """HBM GB/s and dense bf16 TFLOP/s (burst) of this GPU model."""
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        return {"hbm": float(d["hbm_gbs"]), "bf16": float(d["bf16_tflops"]), "kind": "measured"}
     except Exception:
-        return 6800.0, "fallback"
+        return {"hbm": 6800.0, "bf16": 1900.0, "kind": "fallback"}
+
+
+def profile_traffic_ratio(name: str):
+    """dram bytes / algorithmic bytes of an ncu capture summarised in profiles/<name>."""
+    tp = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(tp):
+        return None
+    for line in open(tp):
+        if line.startswith("traffic_ratio:"):
+            return float(line.split()[1])
+    return None
 
 
 def aggregate_value(world_size: int, units_per_rank: float, steps: int, t_max_ms: float) -> float:
@@ -159,6 +178,7 @@ class Workload:
     gps = 0.0            # grid-point-steps per bench step
     h2d = d2h = 0        # bytes per e2e step
     alg_hist_bytes = 0.0  # algorithmic bytes of all history-sum launches per bench step
+    alg = {}              # algorithmic work per bench step by kernel class
     config = {}
 
     def solve_device(self):
@@ -176,8 +196,9 @@ class TG2D(Workload):
         from theses_code_gb300.solvers import TGSolver
         G, S = args.grid, args.solve_steps
         p, V2, C0 = workloads.convection_2d(G, G, alpha=0.7, tau=5e-4, d=0.1, seed=11 + rank)
-        mode = {"blocked": FH_TG_BLOCKED, "df64": FH_TG_DF64}.get(args.mode, FH_TG_FP64)
-        self.solver = TGSolver(ctx, p, S, mode)
+        self.modes = {"blocked": FH_TG_BLOCKED, "df64": FH_TG_DF64, "fp64": FH_TG_FP64}
+        self.p = p
+        self.solver = TGSolver(ctx, p, S, self.modes[args.mode])
         self.V2_d = torch.as_tensor(V2, device=f"cuda:{dev}").contiguous()
         self.C0_d = torch.as_tensor(C0, device=f"cuda:{dev}").contiguous()
         P = V2.size
@@ -188,19 +209,31 @@ class TG2D(Workload):
         self.gps = float(G) * G * S
         self.h2d, self.d2h = 2 * P * 8, P * 8
         pint = (G - 1) * (G - 1)
-        if args.mode == "blocked":
-            # FP64 near part: the layers of the current 64-step block; far part: the
-            # tensor-core contraction reads each history layer once per block (3 bf16 planes)
-            near = sum(8.0 * (j % 64) * pint + 16.0 * pint for j in range(1, S))
-            far = sum(6.0 * j0 * pint + 128 * 8.0 * pint for j0 in range(64, S, 64))
-            self.alg_hist_bytes = near + far
+        ppad = -(-P // 128) * 128
+        blocked = args.mode == "blocked"
+        # algorithmic work per solve, by kernel class (interior points; per point-step:
+        # 8 B per history layer read, the far pair and the two sums written)
+        if blocked:
+            self.alg = {
+                "history": sum(8.0 * (j % 64) * pint + (32.0 if j >= 64 else 16.0) * pint
+                               for j in range(1, S) if j % 64),
+                # far contraction: FP64-equivalent flops 2*128*K*P per 64-step block; the
+                # tensor cores execute 10 bf16 slice products per FP64 product on Ppad columns
+                "gemm_flops": sum(2.0 * 128 * j0 * pint for j0 in range(64, S, 64)),
+                "gemm_tc_flops": sum(10 * 2.0 * 128 * j0 * ppad for j0 in range(64, S, 64)),
+                "gemm_bytes": sum(8.0 * j0 * ppad + 8.0 * 128 * ppad + 8.0 * 128 * j0 for j0 in range(64, S, 64)),
+            }
         else:
-            self.alg_hist_bytes = sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))
+            self.alg = {"history": sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))}
+        # sweeps: x reads C, fa, g, al, one partial, writes Ch; y reads Ch, C, fa, g, al,
+        # one partial, writes C and the new history layer
+        self.alg["sweep"] = 112.0 * pint * S
+        self.alg_hist_bytes = self.alg["history"]
         self.name = f"tg2d_adi_{G}x{G}_{S}steps"
         self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
                        "d": 0.1, "velocity_modes": 8, "mode": args.mode,
                        "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
-        self.kernel = {"blocked": "k_far_gemm (tcgen05, exact bf16 slices) + k_hist_sum_df<2> near",
+        self.kernel = {"blocked": "k_hist_sum_df<2> (current block) + k_far_gemm (tcgen05, exact bf16 slices)",
                        "df64": "k_hist_sum_df<2>"}.get(args.mode, "k_hist_sum<2>")
 
     def solve_device(self):
@@ -213,6 +246,40 @@ class TG2D(Workload):
         L.fh_tg_step(h, self.S)
         L.fh_tg_get_c_host(h, self.out_h.data_ptr())
         return self.out_h.numpy()
+
+    def compare(self, ctx, stream, main_mode):
+        """One solve of the same inputs by every other mode (CUDA-event timed on the
+        context stream, graphs on); relative max-norm differences to the FP64 path."""
+        import torch
+        from theses_code_gb300.solvers import TGSolver
+        self.solve_device()
+        res = {main_mode: self.solver.get_c()}
+        times = {}
+        for m in ("fp64", "df64", "blocked"):
+            if m == main_mode:
+                continue
+            sv = TGSolver(ctx, self.p, self.S, self.modes[m])
+            sv.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
+            sv.calc_step(self.S)  # first call captures the graph
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sv.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
+            e0.record(stream)
+            sv.calc_step(self.S)
+            e1.record(stream)
+            e1.synchronize()
+            times[m] = e0.elapsed_time(e1)
+            res[m] = sv.get_c()
+            sv.close()
+        ref = res["fp64"]
+        den = float(np.max(np.abs(ref)))
+        out = {}
+        for m, c in res.items():
+            d = {"rel_err_vs_fp64": float(np.max(np.abs(c - ref)) / den)}
+            if m in times:
+                d["value"] = self.gps / (times[m] / 1e3)
+                d["ms_per_solve"] = times[m]
+            out[m] = d
+        return out
 
 
 class H1D(Workload):
@@ -242,6 +309,7 @@ class H1D(Workload):
         self.h2d = self.d2h = flat.size * 8
         seg = sum(((p["N"] + 2) + 1) & ~1 for p in params)
         self.alg_hist_bytes = sum(8.0 * max(os_ - 1, 0) * npts + 8.0 * npts for os_ in range(S))
+        self.alg = {"history": self.alg_hist_bytes}
         self.config = {"workload": self.name, "instances": len(params), "interior_points": npts,
                        "solve_steps": S, "state_doubles": seg,
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
@@ -275,6 +343,7 @@ class AB1D(Workload):
         self.gps = float(cfg["m"] - 1) * S
         self.h2d = self.d2h = C0.size * 8
         self.alg_hist_bytes = sum(8.0 * (i - 1) * (cfg["m"] + 1) + 8.0 * (cfg["m"] + 1) for i in range(2, S + 1))
+        self.alg = {"history": self.alg_hist_bytes}
         self.name = f"ab1d_N2048_{S}steps"
         self.config = {"workload": self.name, "m": cfg["m"], "alpha": 0.6, "tau": 1e-4, "solve_steps": S,
                        "source_modes": 16, "l2": "history %.0f MB" % (8 * 2050 * S / 1e6)}
@@ -304,7 +373,7 @@ def make_workload(ctx, args, dev, rank):
 
 def run_gb300(args):
     import torch
-    from theses_code_gb300._lib import FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, Context
+    from theses_code_gb300._lib import FH_PROF_GEMM, FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, Context
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -335,6 +404,8 @@ def run_gb300(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         return float(tt.item())
 
+    # timed region: K solves, each kernel class bracketed by events on the
+    # context stream (fh_ctx_profile); whole-solve time from events around all K
     clocks = ClockSampler(dev)
     ctx.profile(True)
     launches0 = ctx.launches
@@ -351,9 +422,8 @@ def run_gb300(args):
     clk = clocks.stop()
     launches = ctx.launches - launches0
     t_ms = e0.elapsed_time(e1)
-    hist_ms, hist_n = ctx.profile_read(FH_PROF_HISTORY)
-    sweep_ms, _ = ctx.profile_read(FH_PROF_SWEEP)
-    w_ms, _ = ctx.profile_read(FH_PROF_WEIGHTS)
+    kt = {k: ctx.profile_read(c) for k, c in (("history", FH_PROF_HISTORY), ("sweep", FH_PROF_SWEEP),
+                                               ("weights", FH_PROF_WEIGHTS), ("gemm", FH_PROF_GEMM))}
     ctx.profile(False)
     t_max = max_over_ranks(t_ms)
     value = aggregate_value(ws, wl.gps, args.steps, t_max)
@@ -370,29 +440,51 @@ def run_gb300(args):
     e2e = {"value": ws * wl.gps * args.e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": wl.h2d,
            "d2h_bytes_per_step": wl.d2h}
 
-    achieved = wl.alg_hist_bytes * args.steps / (hist_ms / 1e3) / 1e9 if hist_ms > 0 else None
-    peak, peak_kind = peaks()
+    # per kernel class: algorithmic work / summed event time over the timed region
+    pk = peaks()
+    K = args.steps
+    kernels = {}
+    for name, (ms, n) in kt.items():
+        if n == 0 or ms <= 0:
+            continue
+        d = {"ms_per_solve": ms / K, "launches_per_solve": n / K, "share_of_solve": ms / t_ms}
+        if name == "gemm":
+            tc = wl.alg["gemm_tc_flops"] * K / (ms / 1e3) / 1e12
+            d.update({"bound": "tensor", "achieved": tc, "peak": pk["bf16"], "unit": "TFLOP/s",
+                      "frac": tc / pk["bf16"],
+                      "fp64_equiv_tflops": wl.alg["gemm_flops"] * K / (ms / 1e3) / 1e12,
+                      "hbm_gbs": wl.alg["gemm_bytes"] * K / (ms / 1e3) / 1e9})
+        elif name in wl.alg:
+            a = wl.alg[name] * K / (ms / 1e3) / 1e9
+            d.update({"bound": "hbm", "achieved": a, "peak": pk["hbm"], "unit": "GB/s", "frac": a / pk["hbm"]})
+        kernels[name] = d
+    hist = kernels.get("history", {})
     traffic = None
-    tp = os.path.join(REPO, "profiles", "k_hist_sum_fp64_tg512x300.md")
-    if args.config == "tg2d" and args.mode == "fp64" and os.path.exists(tp):
-        # dram bytes / algorithmic bytes of the captured launch, scaled to the mean launch
-        for line in open(tp):
-            if line.startswith("traffic_ratio:"):
-                traffic = float(line.split()[1]) * wl.alg_hist_bytes / max(hist_n / max(args.steps, 1), 1)
+    ratio = profile_traffic_ratio({"fp64": "k_hist_sum_fp64_tg512x300.md",
+                                   "df64": "k_hist_sum_df_tg512.md",
+                                   "blocked": "k_hist_sum_df_tg512.md"}.get(getattr(args, "mode", ""), ""))
+    if args.config == "tg2d" and ratio is not None and kt["history"][1] > 0:
+        traffic = ratio * wl.alg["history"] / (kt["history"][1] / K)  # dram bytes per mean launch
+    roofline = {"bound": "hbm", "achieved": hist.get("achieved"), "peak": pk["hbm"], "unit": "GB/s",
+                "frac": hist.get("frac"), "traffic": traffic, "kernel": wl.kernel, "peak_kind": pk["kind"],
+                "launches": int(kt["history"][1]),
+                "note": "achieved = algorithmic bytes of all history-sum launches (8 B per stored layer "
+                        "and point read, sums and far pairs) / their summed event time; traffic per mean "
+                        "launch from the committed ncu capture"}
     cfg = dict(wl.config)
     cfg["parallelism"] = f"replicas x{ws}"
     result = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": int(launches),
-        "clocks": clk,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": wl.kernel, "peak_kind": peak_kind, "launches": int(hist_n),
-                     "kernel_ms": hist_ms, "sweep_ms": sweep_ms, "weights_ms": w_ms,
-                     "note": "achieved = sum of per-launch algorithmic bytes / summed event time of the "
-                             "history-sum launches over the timed region; traffic is per mean launch"},
+        "clocks": clk, "roofline": roofline, "kernels": kernels,
     }
+    if args.config == "tg2d" and not args.no_compare and rank == 0:
+        cmp = wl.compare(ctx, stream, args.mode)
+        result["modes"] = cmp
+        if "fp64" in cmp and "value" in cmp["fp64"]:
+            result["speedup_vs_plain_fp64"] = value / cmp["fp64"]["value"]
+        result["rel_err_vs_fp64"] = cmp[args.mode]["rel_err_vs_fp64"]
     if rank == 0 and not args.no_cpu_baseline and args.config == "tg2d":
         result["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:

@@ -55,11 +55,16 @@ long long fh_ctx_launch_count(const fh_ctx *ctx);
 
 /* Live kernel timing with CUDA events recorded on the context stream around
  * each launch of a kernel class (off by default; enabling clears the totals).
- * FH_PROF_HISTORY: history-sum kernels; FH_PROF_SWEEP: line-sweep kernels;
- * FH_PROF_WEIGHTS: per-step weight kernels.  _read synchronises the stream. */
+ * FH_PROF_HISTORY: history-sum kernels (FP64 / double-float, CUDA cores);
+ * FH_PROF_SWEEP: line-sweep kernels; FH_PROF_WEIGHTS: weight kernels and, in
+ * blocked mode, the per-block slicing of weights and history layers;
+ * FH_PROF_GEMM: the tensor-core far-history contraction.  _read synchronises
+ * the stream. */
 #define FH_PROF_HISTORY 0
 #define FH_PROF_SWEEP 1
 #define FH_PROF_WEIGHTS 2
+#define FH_PROF_GEMM 3
+#define FH_PROF_KINDS 4
 int fh_ctx_profile(fh_ctx *ctx, int enable);
 int fh_ctx_profile_read(fh_ctx *ctx, int kind, double *total_ms, long long *launches);
 
@@ -100,12 +105,14 @@ int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, cons
                           long long ldh, double *S);
 
 /* Blocked contraction on the tensor cores: S[m*ldS + p] = sum_{k<K} W[m*ldw + k] D[k*ldd + p]
- * for m < 128, computed from three-way bf16 splits of W and D (six products,
- * FP32 accumulation per 128 layers, carried in double-float), FP64 result.
- * K must be a positive multiple of 64.  Error ~1e-7 of sum_k |W||D|.  This is
- * the far-history GEMM of the blocked form of fr_d_t_g_2d.cpp:3340-3384 (one
- * weight row per future half step); it allocates its own plane storage. */
-int fh_history_contract_bf16x3(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
+ * for m < 128.  Every 64-layer chunk of W rows and D points gets a power-of-two
+ * scale and is cut into four integer bf16 slices; the ten slice products up to
+ * level 3 are summed exactly in the FP32 tensor-core accumulators and combined
+ * in double-float, FP64 result.  K must be a positive multiple of 64.  Error
+ * ~2^-32 of the chunk maxima of |W||D|.  This is the far-history GEMM of the
+ * blocked form of fr_d_t_g_2d.cpp:3340-3384 (one weight row per future half
+ * step); it allocates its own plane storage. */
+int fh_history_contract_bf16(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
                                const double *D, long long ldd, double *S, long long ldS);
 
 /* Allocation-free variant of fh_history_sum (same arguments, same result).

@@ -1,10 +1,10 @@
 """Tensor-core blocked contraction (tcgen05, exact bf16 slices) against FP64.
 
 The slices are exact integers relative to per-chunk power-of-two scales, so the
-tensor-core sums are exact; what remains is the slicing, ~2^-24 of the chunk
-MAXIMA (max_k |W| and max_k |D| over each 64-layer chunk) per term, which for
-zero-mean random data is up to ~10x the per-term magnitude.  Bound used:
-1e-6 * sum_k |W[m,k]| |D[k,p]| elementwise (measured: typical 2e-8, max 2.6e-7)."""
+tensor-core sums are exact; what remains is the slicing into four 8-bit slices,
+~2^-32 of the chunk MAXIMA (max_k |W| and max_k |D| over each 64-layer chunk)
+per term, which for zero-mean random data is up to ~10x the per-term magnitude.
+Bound used: 2e-8 * sum_k |W[m,k]| |D[k,p]| elementwise (measured max 1.3e-9)."""
 import numpy as np
 import pytest
 
@@ -20,7 +20,7 @@ def ctx():
 
 
 @pytest.mark.parametrize("K,P", [(64, 128), (128, 100), (192, 1000), (640, 5000), (1984, 2222)])
-def test_contract_bf16x3_matches_fp64(ctx, K, P):
+def test_contract_bf16_matches_fp64(ctx, K, P):
     import torch
     rng = np.random.default_rng(K + P)
     W = rng.uniform(0.0, 1.0, size=(128, K)) * np.exp(-np.arange(K) / 300.0)[None, :]
@@ -28,7 +28,7 @@ def test_contract_bf16x3_matches_fp64(ctx, K, P):
     Wd = torch.as_tensor(W, device="cuda")
     Dd = torch.as_tensor(D, device="cuda")
     S = torch.full((128, P), np.nan, dtype=torch.float64, device="cuda")
-    ctx.call("fh_history_contract_bf16x3", K, P, Wd.data_ptr(), K, Dd.data_ptr(), P, S.data_ptr(), P)
+    ctx.call("fh_history_contract_bf16", K, P, Wd.data_ptr(), K, Dd.data_ptr(), P, S.data_ptr(), P)
     ctx.sync()
     got = S.cpu().numpy()
     ref = W @ D
@@ -36,7 +36,7 @@ def test_contract_bf16x3_matches_fp64(ctx, K, P):
     assert np.isfinite(got).all()
     err = np.abs(got - ref) / scale
     print(f"K={K} P={P} max rel err {err.max():.3e}")
-    assert err.max() <= 1e-6, err.max()
+    assert err.max() <= 2e-8, err.max()
 
 
 def test_contract_rejects_bad_k(ctx):
@@ -46,13 +46,14 @@ def test_contract_rejects_bad_k(ctx):
     D = torch.zeros((100, 10), dtype=torch.float64, device="cuda")
     S = torch.zeros((128, 10), dtype=torch.float64, device="cuda")
     with pytest.raises(FhError):
-        ctx.call("fh_history_contract_bf16x3", 100, 10, W.data_ptr(), 100, D.data_ptr(), 10, S.data_ptr(), 10)
+        ctx.call("fh_history_contract_bf16", 100, 10, W.data_ptr(), 100, D.data_ptr(), 10, S.data_ptr(), 10)
 
 
 @pytest.mark.parametrize("sN,M,steps", [(64, 48, 200), (96, 80, 330)])
 def test_tg_blocked_mode_vs_fp64_oracle(ctx, sN, M, steps):
-    """Blocked 2D ADI (far history on the tensor cores, near 63 layers in FP64)
-    against the FP64 oracle: relative max-norm <= 1e-9 (the mixed-precision bound)."""
+    """Blocked 2D ADI (far history on the tensor cores, the layers of the current
+    64-step block in double-float) against the FP64 oracle: relative max-norm
+    <= 1e-9 (the mixed-precision bound)."""
     from oracle import oracle as O
     from theses_code_gb300 import workloads
     from theses_code_gb300._lib import FH_TG_BLOCKED
@@ -64,4 +65,5 @@ def test_tg_blocked_mode_vs_fp64_oracle(ctx, sN, M, steps):
     got = s.get_c()
     ref, _ = O.tg_solve(p, V2, C0, steps)
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    print(f"blocked {sN}x{M} {steps} steps: rel max-norm err {err:.3e}")
     assert err <= 1e-9, err

@@ -286,6 +286,27 @@ def test_tg_vs_oracle(ctx, sN, M, steps, mode):
     assert relmax(s.get_c(), ref) <= TOL_SOLVER
 
 
+def test_tg_solvers_of_different_sizes_coexist(ctx):
+    """A smaller solver created after a larger one must not break the larger
+    one's sweeps (their shared-memory needs differ)."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    pb, V2b, C0b = workloads.convection_2d(320, 300, alpha=0.7, tau=5e-4, d=0.1, seed=2)
+    big = TGSolver(ctx, pb, 3)
+    big.set_state(V2b, C0b)
+    ps, V2s, C0s = workloads.convection_2d(40, 40, alpha=0.7, tau=5e-4, d=0.1, seed=3)
+    small = TGSolver(ctx, ps, 3)
+    small.set_state(V2s, C0s)
+    big.calc_step(3)
+    small.calc_step(3)
+    ref, _ = O.tg_solve(pb, V2b, C0b, 3)
+    assert relmax(big.get_c(), ref) <= TOL_SOLVER
+    ref, _ = O.tg_solve(ps, V2s, C0s, 3)
+    assert relmax(small.get_c(), ref) <= TOL_SOLVER
+    big.close()
+    small.close()
+
+
 def test_tg_psi_beta_vs_oracle(ctx):
     """psi(t) = t^1.3: the factorization is rebuilt every step."""
     from theses_code_gb300 import workloads

@@ -15,7 +15,7 @@ FH_OK, FH_EINVAL, FH_ENOMEM, FH_ECUDA, FH_ENONFINITE, FH_ETIMEOUT, FH_ERANGE, FH
 FH_W_L1, FH_W_PSI = 0, 1
 FH_K_CONST, FH_K_EXP = 0, 1
 FH_TG_FP64, FH_TG_BLOCKED, FH_TG_DF64 = 0, 1, 2
-FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS = 0, 1, 2
+FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, FH_PROF_GEMM = 0, 1, 2, 3
 FH_NOALLOC_SCRATCH_DOUBLES = 2097152
 
 _vp = C.c_void_p
@@ -55,7 +55,7 @@ _SIGS = {
     "fh_history_sum": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_history_sum_layers": (_i, [_vp, _i, _ll, _dp, _dp, _ll, _dp]),
     "fh_history_sum_noalloc": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
-    "fh_history_contract_bf16x3": (_i, [_vp, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
+    "fh_history_contract_bf16": (_i, [_vp, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_tridiag_batched": (_i, [_vp, _i, _i, _dp, _dp, _dp, _dp, _ll, _dp, _dp, _i, _dp, _dp, _ll]),
     "fh_pcr_solver": (_i, [_vp, _dp, _dp, _dp, _dp, _dp, _i, _i]),
     "fh_h_batch_create": (_i, [_vp, _i, C.POINTER(HParams), _i, C.POINTER(_vp)]),

@@ -233,7 +233,7 @@ int fh_ab_step(fh_ab_solver *s, int nsteps) {
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, s->nrows >= 1, FH_EINVAL, "fh_ab_step: source not set");
   FH_REQUIRE(ctx, nsteps >= 0 && s->step + nsteps <= s->max_steps, FH_ENOMEM, "fh_ab_step: history full");
-  if (ctx->graphs && s->step == 0 && nsteps > 1 && !ctx->prof) {
+  if (ctx->graphs && s->step == 0 && nsteps > 1) {
     int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
       for (int n = 0; n < nsteps; ++n) {
         int r = ab_one_step(s);

@@ -81,7 +81,7 @@ __device__ __forceinline__ float fh_exp2i(int e) {
 __global__ void __launch_bounds__(kThreads, 1)
     k_far_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, long long P,
                const int8_t *__restrict__ Ew, const int8_t *__restrict__ Ed, long long Ppad,
-               double *__restrict__ out, long long ldo, int *__restrict__ err) {
+               float2 *__restrict__ out, long long ldo, int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   const uint32_t raw = fh_smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       fh_tc_fence_after();
       const int ew = (int)Ew[(long long)c * kBM + m];
       const int8_t *edc = Ed + (long long)c * Ppad + p0 + col0;
-#pragma unroll 1
+#pragma unroll
       for (int t = 0; t < 2; ++t) {
         float L0[16], L1[16], L2[16], L3[16];
         const uint32_t cb = tmem + lanebase + (uint32_t)(b * kLevels * kBN + col0 + 16 * t);
@@ -242,13 +242,24 @@ __global__ void __launch_bounds__(kThreads, 1)
       fh_tc_fence_before();
       fh_mbar_arrive(accempty(b));
     }
-    if (ok && nchunks > 0) {
-      double *o = out + (long long)m * ldo + p0 + col0;
+    // every MMA has completed (the last accfull), so the stage ring is free:
+    // stage the 128 x 64 tile of (hi, lo) pairs and store it row by row
+    float2 *tile = reinterpret_cast<float2 *>(gbase);
+    constexpr int kPitch = kBN + 1;  // pairs per staged row: 130 words, lanes hit distinct banks
+    if (ok) {
 #pragma unroll
-      for (int k = 0; k < 32; ++k)
-        if (p0 + col0 + k < P) o[k] = (double)HI[k] + (double)LO[k];
+      for (int k = 0; k < 32; ++k) tile[m * kPitch + col0 + k] = make_float2(HI[k], LO[k]);
     }
     if (!ok) *sh_err = 1;
+    fh_named_barrier(1, 32 * kEpiWarps);
+    if (!*sh_err && nchunks > 0) {
+      const int et = threadIdx.x - 64;  // 0..255
+      for (int r = et >> 5; r < kBM; r += kEpiWarps) {
+        float2 *o = out + (long long)r * ldo + p0;
+        for (int cc = lane; cc < kBN; cc += 32)
+          if (p0 + cc < P) o[cc] = tile[r * kPitch + cc];
+      }
+    }
   }
   fh_tc_fence_before();
   __syncthreads();
@@ -294,8 +305,9 @@ __global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, do
   }
 }
 
-// Generic weight rows (standalone contraction): W[m*ldw + k], k < K.
-__global__ void k_blk_split_rows(const double *__restrict__ W, int ldw, int K, int Kcap,
+// Weight rows W[m*ldw + k], k < K, rows m >= mrows are zero (standalone
+// contraction, or a block of the per-solve weight table).
+__global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, int K, int Kcap, int mrows,
                                  __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
   const int c = blockIdx.x;
   const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -306,7 +318,7 @@ __global__ void k_blk_split_rows(const double *__restrict__ W, int ldw, int K, i
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int k = c * kBK + lane + 32 * h;
-    w[h] = (k < K) ? W[(long long)m * ldw + k] : 0.0;
+    w[h] = (k < K && m < mrows) ? W[(long long)m * ldw + k] : 0.0;
     mx = fmax(mx, fabs(w[h]));
   }
 #pragma unroll
@@ -322,6 +334,95 @@ __global__ void k_blk_split_rows(const double *__restrict__ W, int ldw, int K, i
     const long long o = (long long)m * Kcap + k;
 #pragma unroll
     for (int i = 0; i < kSlices; ++i) A3[i * plane + o] = bs[i];
+  }
+}
+
+// Slices of a double-float value (hi, lo) scaled by 2^-E, |hi + lo| < 2^(E+7):
+// integer bf16 slices a0..a3 with |a_i| <= 128 and (hi + lo) 2^-E =
+// a0 + a1/2^8 + a2/2^16 + a3/2^24 + r, |r| <= 2^-25 (+ the pair's own rounding).
+// FP32 arithmetic only: the scaling is exact, each remainder is kept exactly as
+// a renormalised pair.
+__device__ __forceinline__ void fh_slice4_pair(float hi, float lo, float scale, __nv_bfloat16 (&b)[kSlices]) {
+  float rh = hi * scale, rl = lo * scale;
+#pragma unroll
+  for (int i = 0; i < kSlices; ++i) {
+    const float a = rintf(rh);
+    b[i] = __float2bfloat16_rn(a);
+    const float th = (rh - a) * 256.0f;  // exact: |rh - a| <= 1/2 and a is the integer nearest rh
+    const float tl = rl * 256.0f;
+    rh = th + tl;                        // fast two-sum (|th| >= |tl| or th == 0)
+    rl = tl - (rh - th);
+  }
+}
+
+// 2^e as float for -126 <= e <= 127.
+__device__ __forceinline__ float fh_exp2f_int(int e) { return __int_as_float((e + 127) << 23); }
+
+// Layers [k0, k0+64) of the double-float history (layer-major (hi, lo) pairs,
+// pitch ldd, P valid points) into the K-major planes H3[s][p][k] and the
+// exponents Ed[k0/64][p].  64 points per CTA, 4 threads per point (16 layers
+// each): coalesced pair loads, FP32 slicing in registers, the 64 x 64 bf16
+// tile of each plane staged in shared memory (pitch 66: conflict-free) and
+// written as full 128-byte rows.  Chunks whose maximum is below 2^-100 are
+// scaled as if it were 2^-100 (their slices carry the value to 2^-132).
+constexpr int kCvPts = 64;
+__global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict__ D, long long ldd, long long P,
+                                                        long long Ppad, int k0, int Kcap,
+                                                        __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
+  constexpr int kPitch = kBK + 2;  // bf16 per staged row
+  __shared__ __align__(16) __nv_bfloat16 out[kSlices][kCvPts * kPitch];
+  __shared__ float qmax[4][kCvPts];
+  const long long p0 = (long long)blockIdx.x * kCvPts;
+  const int pt = threadIdx.x & (kCvPts - 1);
+  const int qh = threadIdx.x >> 6;  // layers qh*16 .. qh*16+15
+  const long long p = p0 + pt;
+  float hi[16], lo[16];
+  float mx = 0.f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    float2 v = make_float2(0.f, 0.f);
+    if (p < P) v = __ldcs(D + (long long)(k0 + qh * 16 + i) * ldd + p);
+    hi[i] = v.x;
+    lo[i] = v.y;
+    mx = fmaxf(mx, fabsf(v.x));
+  }
+  qmax[qh][pt] = mx;
+  __syncthreads();
+  mx = fmaxf(fmaxf(qmax[0][pt], qmax[1][pt]), fmaxf(qmax[2][pt], qmax[3][pt]));
+  // frexp exponent q of mx (mx < 2^q), floored at -100; E = q - 7
+  int q = -100;
+  if (mx >= 7.888609052210118e-31f) q = ((__float_as_int(mx) >> 23) & 0xff) - 126;  // 2^-100
+  const int E = q - 7;
+  if (qh == 0 && p < Ppad) Ed[(long long)(k0 / kBK) * Ppad + p] = (int8_t)E;
+  const float scale = fh_exp2f_int(-E);  // -E <= 107
+#pragma unroll
+  for (int i = 0; i < 16; i += 2) {
+    __nv_bfloat16 s0[kSlices], s1[kSlices];
+    fh_slice4_pair(hi[i], lo[i], scale, s0);
+    fh_slice4_pair(hi[i + 1], lo[i + 1], scale, s1);
+#pragma unroll
+    for (int c = 0; c < kSlices; ++c) {
+      __nv_bfloat162 w;
+      w.x = s0[c];
+      w.y = s1[c];
+      *reinterpret_cast<__nv_bfloat162 *>(&out[c][pt * kPitch + qh * 16 + i]) = w;
+    }
+  }
+  __syncthreads();
+  // rows of 64 layers (128 B) per point and plane; a warp writes 4 rows per pass
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long plane = Ppad * (long long)Kcap;
+  for (int r = warp * 4 + (lane >> 3); r < kSlices * kCvPts; r += 8 * 4) {
+    const int c = r / kCvPts, row = r - c * kCvPts;
+    const long long pr = p0 + row;
+    if (pr >= Ppad) continue;
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&out[c][row * kPitch + (lane & 7) * 8]);
+    uint4 v;
+    v.x = src[0];
+    v.y = src[1];
+    v.z = src[2];
+    v.w = src[3];
+    reinterpret_cast<uint4 *>(H3 + c * plane + pr * Kcap + k0)[lane & 7] = v;
   }
 }
 
@@ -438,27 +539,50 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
 // Converts layers [k0, k0+64) of the FP64 history into the planes and exponents.
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df) {
   FH_REQUIRE(ctx, k0 % kBK == 0 && k0 + kBK <= b.Kcap, FH_EINVAL, "blocked contraction: bad layer block %d", k0);
+  if (df) {
+    k_blk_convert_df<<<(unsigned)(b.Ppad / kCvPts), 256, 0, ctx->stream>>>(
+        reinterpret_cast<const float2 *>(D), ldd, b.P, b.Ppad, k0, b.Kcap, b.H3.as<__nv_bfloat16>(),
+        b.Ed.as<int8_t>());
+    return fh_after_launch(ctx, "k_blk_convert_df");
+  }
   k_blk_convert<<<(unsigned)(b.Ppad / 128), 128, sizeof(double) * kBK * 128, ctx->stream>>>(
       D, ldd, b.P, b.Ppad, k0, b.Kcap, df, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_convert");
 }
 
 // Weight planes of the TG block starting at step j0 (K = j0 history layers).
-int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta) {
+// With a weight table (row 2j: x weights of step j, row 2j+1: y weights, pitch
+// ldw, nsteps steps) the rows are taken from it instead of being recomputed.
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta,
+                      const double *table, int ldw, int nsteps) {
   dim3 g((unsigned)(j0 / kBK), kBM / 8);
+  if (table) {
+    const int mrows = 2 * (nsteps - j0) < kBM ? 2 * (nsteps - j0) : kBM;
+    k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(table + (long long)j0 * 2 * ldw, ldw, j0, b.Kcap, mrows,
+                                                 b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
+    return fh_after_launch(ctx, "k_blk_split_rows");
+  }
   k_blk_weights<<<g, 256, 0, ctx->stream>>>(j0, j0, b.Kcap, Da, tau, alpha, beta, b.A3.as<__nv_bfloat16>(),
                                            b.Ew.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_weights");
 }
 
-// S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p].
-int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, double *out, long long ldo) {
+// S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p] as (hi, lo) pairs.
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo) {
   FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
-  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  fh_prof_mark(ctx, FH_PROF_GEMM, false);
   k_far_gemm<<<(unsigned)(b.Ppad / kBN), kThreads, kSmemBytes, ctx->stream>>>(
       b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, b.err.as<int>());
-  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  fh_prof_mark(ctx, FH_PROF_GEMM, true);
   return fh_after_launch(ctx, "k_far_gemm");
+}
+
+__global__ void k_pairs_to_double(const float2 *__restrict__ in, long long ldi, long long P, double *__restrict__ out,
+                                  long long ldo) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const float2 v = in[(long long)blockIdx.y * ldi + p];
+  out[(long long)blockIdx.y * ldo + p] = (double)v.x + (double)v.y;
 }
 
 int fh_blk_check(fh_ctx *ctx, fh_blk &b) {
@@ -469,21 +593,26 @@ int fh_blk_check(fh_ctx *ctx, fh_blk &b) {
   return FH_OK;
 }
 
-extern "C" int fh_history_contract_bf16x3(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
+extern "C" int fh_history_contract_bf16(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
                                           const double *D, long long ldd, double *S, long long ldS) {
   FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
   FH_REQUIRE(ctx, K > 0 && K % kBK == 0 && K <= 65536, FH_EINVAL,
-             "fh_history_contract_bf16x3: K must be a positive multiple of 64");
-  FH_REQUIRE(ctx, P > 0 && ldd >= P && ldS >= P && ldw >= K, FH_EINVAL, "fh_history_contract_bf16x3: bad sizes");
-  FH_REQUIRE(ctx, W && D && S, FH_EINVAL, "fh_history_contract_bf16x3: null pointer");
+             "fh_history_contract_bf16: K must be a positive multiple of 64");
+  FH_REQUIRE(ctx, P > 0 && ldd >= P && ldS >= P && ldw >= K, FH_EINVAL, "fh_history_contract_bf16: bad sizes");
+  FH_REQUIRE(ctx, W && D && S, FH_EINVAL, "fh_history_contract_bf16: null pointer");
   fh_blk b;
   int rc = fh_blk_init(ctx, b, P, K);
   if (rc) return rc;
   dim3 g((unsigned)(K / kBK), kBM / 8);
-  k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(W, ldw, K, K, b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
+  k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(W, ldw, K, K, kBM, b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
   if ((rc = fh_after_launch(ctx, "k_blk_split_rows"))) return rc;
   for (int k0 = 0; k0 < K; k0 += kBK)
     if ((rc = fh_blk_convert(ctx, b, D, ldd, k0, 0))) return rc;
-  if ((rc = fh_blk_gemm(ctx, b, K, S, ldS))) return rc;
+  fh_dbuf pairs;
+  if ((rc = fh_alloc(ctx, pairs, sizeof(float2) * (size_t)kBM * b.Ppad, false))) return rc;
+  if ((rc = fh_blk_gemm(ctx, b, K, pairs.as<float2>(), b.Ppad))) return rc;
+  k_pairs_to_double<<<dim3((unsigned)fh_ceil_div(P, 256), kBM), 256, 0, ctx->stream>>>(pairs.as<float2>(), b.Ppad, P,
+                                                                                      S, ldS);
+  if ((rc = fh_after_launch(ctx, "k_pairs_to_double"))) return rc;
   return fh_blk_check(ctx, b);
 }

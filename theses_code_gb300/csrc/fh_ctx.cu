@@ -35,6 +35,19 @@ int fh_alloc(fh_ctx *ctx, fh_dbuf &b, size_t bytes, bool zero) {
 
 void fh_prof_mark(fh_ctx *ctx, int kind, bool stop) {
   if (!ctx->prof) return;
+  if (ctx->capturing) {
+    // inside a capture: a fresh event per mark, recorded as a graph node
+    std::vector<cudaEvent_t> &v = ctx->capturing->pev[kind];
+    if (stop != ((v.size() & 1) == 1)) return;  // unbalanced mark: ignore
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    v.push_back(e);
+    cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal);
+    return;
+  }
   fh_prof_kind &k = ctx->pk[kind];
   if (k.used == k.ev.size()) {
     cudaEvent_t e;
@@ -60,6 +73,21 @@ static void prof_collect(fh_ctx *ctx, int kind) {
     }
   }
   k.used = 0;
+}
+
+void fh_prof_collect_graph(fh_ctx *ctx, fh_graph_cache &gc) {
+  for (int kind = 0; kind < FH_PROF_KINDS; ++kind) {
+    const std::vector<cudaEvent_t> &v = gc.pev[kind];
+    for (size_t i = 0; i + 1 < v.size(); i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, v[i], v[i + 1]) == cudaSuccess) {
+        ctx->pk[kind].total_ms += ms;
+        ctx->pk[kind].count++;
+      } else {
+        cudaGetLastError();
+      }
+    }
+  }
 }
 
 static void prof_free(fh_ctx *ctx) {
@@ -88,9 +116,9 @@ int fh_ctx_profile(fh_ctx *ctx, int enable) {
 
 int fh_ctx_profile_read(fh_ctx *ctx, int kind, double *total_ms, long long *launches) {
   FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
-  FH_REQUIRE(ctx, kind >= 0 && kind < 3, FH_EINVAL, "fh_ctx_profile_read: bad kind");
+  FH_REQUIRE(ctx, kind >= 0 && kind < FH_PROF_KINDS, FH_EINVAL, "fh_ctx_profile_read: bad kind");
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  for (int k = 0; k < 3; ++k) prof_collect(ctx, k);
+  for (int k = 0; k < FH_PROF_KINDS; ++k) prof_collect(ctx, k);
   if (total_ms) *total_ms = ctx->pk[kind].total_ms;
   if (launches) *launches = ctx->pk[kind].count;
   return FH_OK;

@@ -358,7 +358,7 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
   FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_h_batch_step: nsteps < 0");
   FH_REQUIRE(ctx, b->nsaved + nsteps <= b->max_steps, FH_ENOMEM, "fh_h_batch_step: history full (%d + %d > %d)",
              b->nsaved, nsteps, b->max_steps);
-  if (b->use_graph && ctx->graphs && b->nsaved == 0 && nsteps > 1 && !ctx->prof) {
+  if (b->use_graph && ctx->graphs && b->nsaved == 0 && nsteps > 1) {
     // whole solve from the initial state: capture once, replay afterwards
     int rc = fh_graph_run(ctx, b->graph, nsteps, [&]() {
       for (int i = 0; i < nsteps; ++i) {

@@ -80,7 +80,8 @@ template <int M>
 __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__restrict__ D, long long ldd, long long P,
                                                               int K, const double *__restrict__ W, int ldw,
                                                               int kchunk, double *__restrict__ part,
-                                                              long long ldpart) {
+                                                              long long ldpart, const float2 *__restrict__ far,
+                                                              long long ldfar) {
   extern __shared__ float2 wsf[];  // [M][kchunk] (hi, lo)
   const int s = blockIdx.y;
   const int k0 = s * kchunk;
@@ -96,7 +97,17 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
   if (p >= P) return;
   float ah[M][2], al[M][2];
 #pragma unroll
-  for (int m = 0; m < M; ++m) ah[m][0] = ah[m][1] = al[m][0] = al[m][1] = 0.f;
+  for (int m = 0; m < M; ++m) {
+    if (far && s == 0) {  // split 0 starts from the far-history pair of row m
+      const float4 f = *reinterpret_cast<const float4 *>(far + (long long)m * ldfar + p);
+      ah[m][0] = f.x;
+      al[m][0] = f.y;
+      ah[m][1] = f.z;
+      al[m][1] = f.w;
+    } else {
+      ah[m][0] = ah[m][1] = al[m][0] = al[m][1] = 0.f;
+    }
+  }
   const float4 *d = reinterpret_cast<const float4 *>(D + (long long)k0 * ldd + p);
   const long long ld4 = ldd / 2;  // float4 = two points
   auto acc = [&](const float2 w, const float dh, const float dl, float &sh, float &sl) {
@@ -111,19 +122,20 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
     sl += e + pl;
   };
   int k = 0;
-  for (; k + 2 <= nk; k += 2) {
-    const float4 v0 = __ldcs(d);
-    const float4 v1 = __ldcs(d + ld4);
-    d += 2 * ld4;
+  for (; k + 4 <= nk; k += 4) {  // four layers (64 B per thread) in flight
+    float4 v[4];
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-      const float2 w0 = wsf[m * kchunk + k], w1 = wsf[m * kchunk + k + 1];
-      acc(w0, v0.x, v0.y, ah[m][0], al[m][0]);
-      acc(w0, v0.z, v0.w, ah[m][1], al[m][1]);
-      acc(w1, v1.x, v1.y, ah[m][0], al[m][0]);
-      acc(w1, v1.z, v1.w, ah[m][1], al[m][1]);
-    }
-    if ((k & 15) == 14) {
+    for (int u = 0; u < 4; ++u) v[u] = __ldcs(d + u * ld4);
+    d += 4 * ld4;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+        const float2 w = wsf[m * kchunk + k + u];
+        acc(w, v[u].x, v[u].y, ah[m][0], al[m][0]);
+        acc(w, v[u].z, v[u].w, ah[m][1], al[m][1]);
+      }
+    if ((k & 15) == 12) {
 #pragma unroll
       for (int m = 0; m < M; ++m)
 #pragma unroll
@@ -155,16 +167,18 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
 
 int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                    const float2 *D, long long ldd, int splits, int kchunk, double *part,
-                                   long long ldpart) {
+                                   long long ldpart, const float2 *far, long long ldfar) {
   if (K <= 0 || P <= 0) return FH_OK;
   dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
   const size_t smem = sizeof(float2) * (size_t)M * (size_t)kchunk;
   FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large (%d layers)", kchunk);
   fh_prof_mark(ctx, FH_PROF_HISTORY, false);
   if (M == 1)
-    k_hist_sum_df<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+    k_hist_sum_df<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
+                                                                  ldfar);
   else
-    k_hist_sum_df<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
+    k_hist_sum_df<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
+                                                                  ldfar);
   fh_prof_mark(ctx, FH_PROF_HISTORY, true);
   return fh_after_launch(ctx, "k_hist_sum_df");
 }

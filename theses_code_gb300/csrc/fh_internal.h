@@ -16,6 +16,8 @@ struct fh_prof_kind {
   long long count = 0;
 };
 
+struct fh_graph_cache;
+
 struct fh_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -23,7 +25,8 @@ struct fh_ctx {
   long long launches = 0;
   bool prof = false;
   bool graphs = true;  // whole solves from the initial state replay a captured graph
-  fh_prof_kind pk[3];
+  fh_prof_kind pk[FH_PROF_KINDS];
+  fh_graph_cache *capturing = nullptr;  // graph being captured (profiling marks become graph nodes)
   char err[512] = {0};
 };
 
@@ -50,48 +53,79 @@ int fh_after_launch(fh_ctx *ctx, const char *what);
 
 // Replays a captured launch sequence: the first run of `nsteps` steps from the
 // initial state is recorded by stream capture and instantiated; later runs
-// from the same initial state launch the graph.
+// from the same initial state launch the graph.  With profiling on, the
+// start/stop marks are captured as external event-record nodes; after every
+// replay the stream is synchronised and their intervals are added to the
+// context's totals.
 struct fh_graph_cache {
   cudaGraphExec_t exec = nullptr;
   int nsteps = -1;
+  bool prof = false;                        // captured with profiling marks
+  long long kernels = 0;                    // kernel launches in the graph
+  std::vector<cudaEvent_t> pev[FH_PROF_KINDS];  // start/stop pairs baked into the graph
+  void release_events() {
+    for (auto &v : pev) {
+      for (auto e : v) cudaEventDestroy(e);
+      v.clear();
+    }
+  }
   ~fh_graph_cache() {
     if (exec) cudaGraphExecDestroy(exec);
+    release_events();
   }
 };
+
+// Adds the intervals of the graph's profiling pairs (after a synchronised replay).
+void fh_prof_collect_graph(fh_ctx *ctx, fh_graph_cache &gc);
+
 // Runs body() (which enqueues the launches of `nsteps` steps on ctx->stream)
 // under capture the first time and replays it afterwards.  body must only
 // enqueue work (no synchronisation, no allocation).
 template <class Body>
 int fh_graph_run(fh_ctx *ctx, fh_graph_cache &gc, int nsteps, Body body) {
-  if (gc.exec && gc.nsteps == nsteps) {
-    cudaError_t e = cudaGraphLaunch(gc.exec, ctx->stream);
-    if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
-    ctx->launches += 1;
-    return FH_OK;
+  if (!(gc.exec && gc.nsteps == nsteps && gc.prof == ctx->prof)) {
+    if (gc.exec) {
+      cudaGraphExecDestroy(gc.exec);
+      gc.exec = nullptr;
+    }
+    gc.release_events();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+    const long long l0 = ctx->launches;
+    ctx->capturing = &gc;
+    const int rc = body();
+    ctx->capturing = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &graph);
+    gc.kernels = ctx->launches - l0;
+    ctx->launches = l0;  // counted when the graph runs
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      gc.release_events();
+      return rc;
+    }
+    if (e != cudaSuccess) {
+      gc.release_events();
+      return fh_set_error(ctx, FH_ECUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(&gc.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      gc.exec = nullptr;
+      gc.release_events();
+      return fh_set_error(ctx, FH_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    gc.nsteps = nsteps;
+    gc.prof = ctx->prof;
   }
-  if (gc.exec) {
-    cudaGraphExecDestroy(gc.exec);
-    gc.exec = nullptr;
-  }
-  cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
-  const int rc = body();
-  e = cudaStreamEndCapture(ctx->stream, &graph);
-  if (rc) {
-    if (graph) cudaGraphDestroy(graph);
-    return rc;
-  }
-  if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&gc.exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) {
-    gc.exec = nullptr;
-    return fh_set_error(ctx, FH_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
-  }
-  gc.nsteps = nsteps;
-  e = cudaGraphLaunch(gc.exec, ctx->stream);
+  cudaError_t e = cudaGraphLaunch(gc.exec, ctx->stream);
   if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+  ctx->launches += gc.kernels;
+  if (gc.prof) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "graph replay: %s", cudaGetErrorString(e));
+    fh_prof_collect_graph(ctx, gc);
+  }
   return FH_OK;
 }
 
@@ -117,8 +151,10 @@ int fh_launch_weights_psi(fh_ctx *ctx, int K, double x0, double len, double X, d
 int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                 const double *D, long long ldd, int splits, int kchunk, double *part,
                                 long long ldpart);
+// History stored as (hi, lo) FP32 pairs, double-float accumulation; split 0
+// starts from far[m*ldfar + p] (a (hi, lo) pair per point) when far != null.
 int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                    const float2 *D, long long ldd, int splits, int kchunk, double *part,
-                                   long long ldpart);
+                                   long long ldpart, const float2 *far, long long ldfar);
 // Chooses the split count for a K x P history sum given a partial-buffer capacity.
 void fh_hist_plan(long long P, int K, int max_splits, int *splits, int *kchunk);

@@ -138,3 +138,8 @@ __device__ __forceinline__ uint64_t fh_desc_kmajor_sw128(uint32_t smem_addr) {
 __host__ __device__ constexpr uint32_t fh_idesc_bf16_f32(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+
+// Barrier over a subset of the CTA's warps (id 1..15; id 0 is __syncthreads).
+__device__ __forceinline__ void fh_named_barrier(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}

@@ -2,22 +2,28 @@
 // path of fr_d_t_g_2d.cpp with dt_alg 0 (fr_d_t_g_2d.cpp:2552-2718, 3242-3553).
 //
 // Per time step j (launches on the context stream):
-//   1. k_tg_weights   x/y history weights for k < j and the three current weights
-//   2. history sum    S_x, S_y over the j stored full-step differences, one pass
-//                     (the reference reads the layers once per half step)
-//   3. k_tg_xsweep    one warp per x line (j = 1..M-1), unknowns along i
-//   4. k_tg_ysweep    one warp per y line (i = 1..sN-1), unknowns along j; also
-//                     appends the new full-step difference to the history and
-//                     keeps a copy of the full-step field
+//   1. weights        x/y history weights for k < j and the three current
+//                     weights (a per-solve table when it fits, else per step)
+//   2. history sum    S_x, S_y over the stored full-step differences, one pass
+//                     (the reference reads the layers once per half step);
+//                     in blocked mode only the layers of the current 64-step
+//                     block, the older ones come from the tensor-core rows
+//   3. k_tg_xsweep    one CTA per x line (j = 1..M-1), unknowns along i; writes
+//                     the half-step field Ch
+//   4. k_tg_ysweep    four y lines per CTA (i = 1..sN-1), unknowns along j;
+//                     writes the new full-step field C and appends the new
+//                     full-step difference to the history
 // The Thomas factorization of both sweep directions depends only on V2, d and
 // the current weight; for psi = t that weight is the same every step, so the
 // factorization is built once (k_tg_factor) and each step only runs the two
 // affine recurrences (fh_linescan.cuh).  For psi != t it is rebuilt per step.
 //
-// Storage (HBM): C, Cfull, V2 and the factor tables are (sN+2)(M+2) doubles in
+// Storage (HBM): C, Ch, V2 and the factor tables are (sN+2)(M+2) doubles in
 // the reference layout idx = i + j*(sN+2); the history holds one difference
 // layer per full step, D[k] = C^{k+1} - C^k (the half-step layers the
-// reference also stores are only read through C itself).
+// reference also stores are only read through Ch).
+#include <mutex>
+
 #include "fh_internal.h"
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
@@ -29,8 +35,9 @@ fh_blk *fh_blk_new();
 void fh_blk_delete(fh_blk *b);
 int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
-int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta);
-int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, double *out, long long ldo);
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta,
+                      const double *table, int ldw, int nsteps);
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo);
 long long fh_blk_ppad(const fh_blk &b);
 static constexpr int kTgBlock = 64;  // steps per block (128 weight rows)
 
@@ -51,9 +58,9 @@ struct fh_tg_solver {
   bool have_state = false;
   bool factor_fixed = false;
   int max_splits = 8;
-  fh_dbuf C, Cfull, V2, D, W, cw, part, alx, gx, aly, gy, far;
+  fh_dbuf C, Ch, V2, D, W, cw, part, alx, gx, fax, aly, gy, fay, far;
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
-  fh_blk *blk = nullptr;  // blocked mode: bf16x3 planes and tensor maps
+  fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
   long long ldfar = 0;
   fh_graph_cache graph;
@@ -82,10 +89,12 @@ __global__ void k_tg_weights(fh_tg_dev g, int j, int kstart, double *__restrict_
   }
 }
 
-// Serial factorization of every line (one thread per line): Al[i+1] and g_i,
-// stored at the point of equation i.  dir 0: x lines, dir 1: y lines.
+// Serial factorization of every line (one thread per line): Al[i+1], the
+// pivot factor g_i and the forward-map slope fa_i = g_i A_i, stored at the
+// point of equation i.  dir 0: x lines, dir 1: y lines.  A, B, R in the
+// reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
 __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2, const double *__restrict__ cw,
-                            double *__restrict__ al, double *__restrict__ gg) {
+                            double *__restrict__ al, double *__restrict__ gg, double *__restrict__ fa) {
   const int line = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int nlines = dir == 0 ? g.M : g.sN;
   if (line >= nlines) return;
@@ -109,8 +118,10 @@ __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2,
     const double R = g.st * (kcur + 0.0) + A + B;
     const double den = R - A * alv;
     const double aln = B / den;
+    const double gi = (aln == 0.0 && B == 0.0) ? 1.0 / den : aln / B;
     al[id] = aln;
-    gg[id] = (aln == 0.0 && B == 0.0) ? 1.0 / den : aln / B;
+    gg[id] = gi;
+    fa[id] = gi * A;
     alv = aln;
   }
 }
@@ -137,94 +148,148 @@ __global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ W
   }
 }
 
-// Shared-memory footprint of one staged line: 5 arrays of fh_sk(N+2)+1 doubles.
+// Shared-memory footprint of one staged line array: fh_sk(N+1)+1 doubles.
 __host__ __device__ inline int tg_line_stride(int N) { return (N + 2) + ((N + 2) >> 4) + 2; }
 
-// x half-step (fr_d_t_g_2d.cpp:2577-2590): one warp per line j = 1..M-1, the
-// line staged with coalesced loads, then solved from shared memory.
-__global__ void k_tg_xsweep(fh_tg_dev g, const double *__restrict__ V2, double *C, const double *__restrict__ part,
-                            long long ldp, int splits, const double *__restrict__ alx, const double *__restrict__ gx,
-                            const double *__restrict__ cw, const double *__restrict__ far) {
+static constexpr int kXThreads = 128;  // one x line per CTA
+static constexpr int kYThreads = 512;  // four adjacent y lines per CTA
+static constexpr int kUnroll = 4;      // equations staged per thread per round
+
+// x half-step (fr_d_t_g_2d.cpp:2577-2590): one CTA per line j = 1..M-1.  All
+// threads stage the line's forward maps into shared memory with independent,
+// coalesced loads (kUnroll equations per thread in flight), warp 0 solves it,
+// all threads write the half-step field Ch.  The boundary nodes i = 0, N, N+1
+// are also written into C, which otherwise keeps the full-step field.
+__global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C, double *__restrict__ Ch,
+                                                        const double *__restrict__ part, long long ldp, int splits,
+                                                        const double *__restrict__ fax,
+                                                        const double *__restrict__ gx,
+                                                        const double *__restrict__ alx,
+                                                        const double *__restrict__ cw,
+                                                        const float2 *__restrict__ far) {
   extern __shared__ double sbuf[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int line = 1 + blockIdx.x * (blockDim.x >> 5) + warp;
-  if (line >= g.M) return;  // whole warp exits together
+  const int line = 1 + blockIdx.x;
   const int N = g.sN;
   const int L = tg_line_stride(N);
-  double *fa = sbuf + (size_t)warp * 4 * L, *fb = fa + L, *al = fb + L, *bt = al + L;
+  double *fa = sbuf, *fb = fa + L, *al = fb + L, *bt = al + L;
   const long long base = (long long)line * g.ld;
-  const double kx = cw[0], dl = g.dL;
-  const double cA = (0.5 * (g.d + g.d) / dl) + 0.5;
-  for (int i = 1 + lane; i < N; i += 32) {
-    const long long id = base + i;
-    double ts = 0.0;
-    for (int s = 0; s < splits; ++s) ts += part[(long long)(2 * s) * ldp + id];
-    if (far) ts += far[id];
-    double om = -g.st * (kx + 0.0) * C[id];
-    om += g.S * 0.5;
-    om += g.st * ts;
-    const double A = (V2[id] / dl) * cA;
-    const double gi = gx[id];
-    fa[fh_sk(i)] = gi * A;
-    fb[fh_sk(i)] = -gi * om;
-    al[fh_sk(i)] = alx[id];
+  const double kst = -g.st * (cw[0] + 0.0), S2 = g.S * 0.5, st = g.st;
+  for (int r0 = 1; r0 < N; r0 += kXThreads * kUnroll) {
+    double ts[kUnroll], c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll];
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int i = r0 + threadIdx.x + e * kXThreads;
+      const long long id = base + (i < N ? i : 1);
+      c[e] = C[id];
+      a[e] = fax[id];
+      gi[e] = gx[id];
+      l[e] = alx[id];
+      ts[e] = 0.0;
+      if (far) {
+        const float2 fp = far[id];
+        ts[e] = (double)fp.x + (double)fp.y;
+      }
+    }
+    for (int s = 0; s < splits; ++s)
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = r0 + threadIdx.x + e * kXThreads;
+        ts[e] += part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)];
+      }
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int i = r0 + threadIdx.x + e * kXThreads;
+      if (i < N) {
+        double om = kst * c[e];
+        om += S2;
+        om += st * ts[e];
+        fa[fh_sk(i)] = a[e];
+        fb[fh_sk(i)] = -gi[e] * om;
+        al[fh_sk(i)] = l[e];
+      }
+    }
   }
-  __syncwarp();
-  fh_line_solve_staged(N, fa, fb, al, 0.0, g.C1, bt, fa);
-  for (int i = lane; i <= N + 1; i += 32) C[base + i] = fa[fh_sk(i)];
+  __syncthreads();
+  if (threadIdx.x < 32) fh_line_solve_staged(N, fa, fb, al, 0.0, g.C1, bt, fa);
+  __syncthreads();
+  for (int i = threadIdx.x; i <= N + 1; i += kXThreads) {
+    const double u = fa[fh_sk(i)];
+    Ch[base + i] = u;
+    if (i == 0 || i >= N) C[base + i] = u;
+  }
 }
 
-// y half-step (fr_d_t_g_2d.cpp:2634-2648): 4 adjacent lines i per CTA so the
-// strided column loads share sectors; one warp solves one line.  Appends the
-// full-step difference D_j = C^{j+1} - C^j and refreshes Cfull.
-__global__ void __launch_bounds__(128) k_tg_ysweep(fh_tg_dev g, const double *__restrict__ V2, double *C,
-                                                   double *Cfull, double *__restrict__ Dj,
-                                                   const double *__restrict__ part, long long ldp, int splits,
-                                                   const double *__restrict__ aly, const double *__restrict__ gy,
-                                                   const double *__restrict__ cw, const double *__restrict__ far,
-                                                   int dfstore) {
+// y half-step (fr_d_t_g_2d.cpp:2634-2648): four adjacent lines i per CTA so
+// that the strided column loads share 32-byte sectors; 128 threads stage each
+// line (kUnroll rows per thread in flight), one warp per line solves it.  Reads
+// the half-step field Ch and the full-step field C, writes the new full-step
+// field into C and appends the difference D_j = C^{j+1} - C^j.
+__global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C, const double *__restrict__ Ch,
+                                                        double *__restrict__ Dj, const double *__restrict__ part,
+                                                        long long ldp, int splits, const double *__restrict__ fay,
+                                                        const double *__restrict__ gy,
+                                                        const double *__restrict__ aly,
+                                                        const double *__restrict__ cw,
+                                                        const float2 *__restrict__ far, int dfstore) {
   extern __shared__ double sbuf[];
   const int warp = threadIdx.x >> 5;
   const int N = g.M;
   const int L = tg_line_stride(N);
   const int i0 = 1 + blockIdx.x * 4;
-  const double ky = cw[1], kyh = cw[2], dl = g.dLx;
-  const double cA = 0.5 * (g.d + g.d) / (dl * dl);
-  // staging: thread t handles column t%4 and rows t/4, t/4 + 32, ...
+  const double kst = -g.st * (cw[1] + 0.0), kyh = cw[2], S2 = g.S * 0.5, st = g.st;
   const int col = threadIdx.x & 3;
+  const int rg = threadIdx.x >> 2;  // row group 0..127
+  constexpr int kRows = kYThreads / 4;
   const int line = i0 + col;
+  const bool live = line < g.sN;
   double *fa = sbuf + (size_t)col * 5 * L, *fb = fa + L, *al = fb + L, *bt = al + L, *cf = bt + L;
-  if (line < g.sN) {
-    for (int q = (threadIdx.x >> 2); q <= N + 1; q += 32) {
-      const long long id = line + (long long)q * g.ld;
-      const double c = C[id];
-      if (q >= 1 && q < N) {
-        double ts = 0.0;
-        for (int s = 0; s < splits; ++s) ts += part[(long long)(2 * s + 1) * ldp + id];
-        if (far) ts += far[id];
-        const double f = Cfull[id];
-        ts += (kyh + 0.0) * (f - c);  // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
-        double om = -g.st * (ky + 0.0) * c;
-        om += g.S * 0.5;
-        om += g.st * ts;
-        const double A = V2[id] * cA;
-        const double gi = gy[id];
-        fa[fh_sk(q)] = gi * A;
-        fb[fh_sk(q)] = -gi * om;
-        al[fh_sk(q)] = aly[id];
-        cf[fh_sk(q)] = f;
+  for (int r0 = 1; r0 < N; r0 += kRows * kUnroll) {
+    double ts[kUnroll], c[kUnroll], f[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll];
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int q = r0 + rg + e * kRows;
+      const long long id = (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld;
+      c[e] = Ch[id];
+      f[e] = C[id];
+      a[e] = fay[id];
+      gi[e] = gy[id];
+      l[e] = aly[id];
+      ts[e] = 0.0;
+      if (far) {
+        const float2 fp = far[id];
+        ts[e] = (double)fp.x + (double)fp.y;
+      }
+    }
+    for (int s = 0; s < splits; ++s)
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int q = r0 + rg + e * kRows;
+        ts[e] += part[(long long)(2 * s + 1) * ldp + (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld];
+      }
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int q = r0 + rg + e * kRows;
+      if (live && q < N) {
+        double t = ts[e];
+        t += (kyh + 0.0) * (f[e] - c[e]);  // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
+        double om = kst * c[e];
+        om += S2;
+        om += st * t;
+        fa[fh_sk(q)] = a[e];
+        fb[fh_sk(q)] = -gi[e] * om;
+        al[fh_sk(q)] = l[e];
+        cf[fh_sk(q)] = f[e];
       }
     }
   }
   __syncthreads();
-  const int wline = i0 + warp;
-  if (wline < g.sN) {
+  if (warp < 4 && i0 + warp < g.sN) {
     double *wfa = sbuf + (size_t)warp * 5 * L;
     fh_line_solve_staged(N, wfa, wfa + L, wfa + 2 * L, 1.0, 0.0, wfa + 3 * L, wfa);
   }
   __syncthreads();
-  if (line < g.sN) {
-    for (int q = (threadIdx.x >> 2); q <= N + 1; q += 32) {
+  if (live) {
+    for (int q = rg; q <= N + 1; q += kRows) {
       const long long id = line + (long long)q * g.ld;
       const double u = fa[fh_sk(q)];
       C[id] = u;
@@ -236,7 +301,6 @@ __global__ void __launch_bounds__(128) k_tg_ysweep(fh_tg_dev g, const double *__
         } else {
           Dj[id] = dd;
         }
-        Cfull[id] = u;
       }
     }
   }
@@ -244,18 +308,17 @@ __global__ void __launch_bounds__(128) k_tg_ysweep(fh_tg_dev g, const double *__
 
 // ------------------------------------------------------------------ host
 
-static constexpr int kSweepWarps = 4;
 static constexpr int kWeightTableMaxSteps = 4096;  // 2 x 4096^2 doubles = 268 MB
 
 static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), cwj,
-                                                                     s->alx.as<double>(), s->gx.as<double>());
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(
+      g, 0, s->V2.as<double>(), cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>());
   int rc = fh_after_launch(ctx, "k_tg_factor(x)");
   if (rc) return rc;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), cwj,
-                                                                      s->aly.as<double>(), s->gy.as<double>());
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(
+      g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>());
   return fh_after_launch(ctx, "k_tg_factor(y)");
 }
 
@@ -271,9 +334,11 @@ static int tg_one_step(fh_tg_solver *s) {
     // far rows S_far[2r + {0,1}] = sum_{k<j} w_{j+r}(k) D[k] on the tensor cores
     fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
     if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), g.P, j - kTgBlock, s->df ? 1 : 0))) return rc;
-    if ((rc = fh_blk_tg_weights(ctx, *s->blk, j, g.Da, g.tau, g.alpha, g.beta))) return rc;
+    if ((rc = fh_blk_tg_weights(ctx, *s->blk, j, g.Da, g.tau, g.alpha, g.beta, s->wtab ? s->W.as<double>() : nullptr,
+                                s->max_steps, s->max_steps)))
+      return rc;
     fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
-    if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<double>(), s->ldfar))) return rc;
+    if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<float2>(), s->ldfar))) return rc;
     s->j0 = j;
   }
   const int kstart = blocked ? s->j0 : 0;  // history layers summed in FP64 this step
@@ -299,48 +364,65 @@ static int tg_one_step(fh_tg_solver *s) {
   const double *cwj = s->wtab ? s->cw.as<double>() + 4LL * j : s->cw.as<double>();
   if (!s->factor_fixed || j == 0)
     if ((rc = tg_factor(s, cwj))) return rc;
+  // far-history rows of this step ((hi, lo) pairs, x row 2r, y row 2r+1)
+  const float2 *far = nullptr;
+  if (blocked && s->j0 > 0) far = s->far.as<float2>() + 2LL * (j - s->j0) * s->ldfar;
   int splits = 0, kchunk = 0;
   if (knear >= 1) {
     fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
     if (s->df)
       rc = fh_launch_hist_sum_df_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                           reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P,
-                                          g.P, splits, kchunk, s->part.as<double>(), g.P);
+                                          g.P, splits, kchunk, s->part.as<double>(), g.P, far, s->ldfar);
     else
       rc = fh_launch_hist_sum_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                        s->D.as<double>() + (long long)kstart * g.P, g.P, splits, kchunk,
                                        s->part.as<double>(), g.P);
     if (rc) return rc;
   }
-  const double *farx = nullptr, *fary = nullptr;
-  if (blocked && s->j0 > 0) {
-    const long long r = j - s->j0;
-    farx = s->far.as<double>() + (2 * r) * s->ldfar;
-    fary = s->far.as<double>() + (2 * r + 1) * s->ldfar;
+  // the near kernel has folded the far rows in; otherwise the sweeps add them
+  const float2 *farx = nullptr, *fary = nullptr;
+  if (far && !(knear >= 1 && s->df)) {
+    farx = far;
+    fary = far + s->ldfar;
   }
-  const unsigned thr = 32 * kSweepWarps;
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-  const size_t smx = sizeof(double) * (size_t)kSweepWarps * 4 * tg_line_stride(g.sN);
-  k_tg_xsweep<<<(unsigned)fh_ceil_div(g.M - 1, kSweepWarps), thr, smx, ctx->stream>>>(
-      g, s->V2.as<double>(), s->C.as<double>(), s->part.as<double>(), g.P, splits, s->alx.as<double>(),
-      s->gx.as<double>(), cwj, farx);
+  const size_t smx = sizeof(double) * 4 * (size_t)tg_line_stride(g.sN);
+  k_tg_xsweep<<<(unsigned)(g.M - 1), kXThreads, smx, ctx->stream>>>(
+      g, s->C.as<double>(), s->Ch.as<double>(), s->part.as<double>(), g.P, splits, s->fax.as<double>(),
+      s->gx.as<double>(), s->alx.as<double>(), cwj, farx);
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
   const size_t smy = sizeof(double) * 4 * 5 * (size_t)tg_line_stride(g.M);
-  k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), 128, smy, ctx->stream>>>(
-      g, s->V2.as<double>(), s->C.as<double>(), s->Cfull.as<double>(), s->D.as<double>() + (long long)j * g.P,
-      s->part.as<double>(), g.P, splits, s->aly.as<double>(), s->gy.as<double>(), cwj, fary, s->df ? 1 : 0);
+  k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
+      g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (long long)j * g.P, s->part.as<double>(), g.P,
+      splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), cwj, fary, s->df ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
   s->tstep++;
   return FH_OK;
 }
 
+// The sweeps' dynamic shared memory grows with the line length.  The limit is
+// a per-function attribute of the device, shared by every solver in the
+// process, so it only ever grows (a smaller solver created later must not
+// lower it below what an earlier, larger one launches with).
 static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
-  const int smx = (int)(sizeof(double) * (size_t)kSweepWarps * 4 * tg_line_stride(sN));
+  static std::mutex mu;
+  static int cur_x[64], cur_y[64];
+  const int smx = (int)(sizeof(double) * 4 * (size_t)tg_line_stride(sN));
   const int smy = (int)(sizeof(double) * 4 * 5 * (size_t)tg_line_stride(M));
-  FH_REQUIRE(ctx, smx <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL, "fh_tg_create: grid too large for the sweeps");
-  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
-  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
+  FH_REQUIRE(ctx, smx <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL,
+             "fh_tg_create: grid too large for the sweeps (sN, M <= 1200)");
+  FH_REQUIRE(ctx, ctx->device >= 0 && ctx->device < 64, FH_EINVAL, "fh_tg_create: device index");
+  std::lock_guard<std::mutex> lk(mu);
+  if (smx > cur_x[ctx->device]) {
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
+    cur_x[ctx->device] = smx;
+  }
+  if (smy > cur_y[ctx->device]) {
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
+    cur_y[ctx->device] = smy;
+  }
   return FH_OK;
 }
 
@@ -387,9 +469,10 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
   s->wtab = max_steps <= kWeightTableMaxSteps;
   const size_t fld = sizeof(double) * (size_t)g.P;
   int rc;
-  if ((rc = fh_alloc(ctx, s->C, fld)) || (rc = fh_alloc(ctx, s->Cfull, fld)) || (rc = fh_alloc(ctx, s->V2, fld)) ||
-      (rc = fh_alloc(ctx, s->alx, fld)) || (rc = fh_alloc(ctx, s->gx, fld)) || (rc = fh_alloc(ctx, s->aly, fld)) ||
-      (rc = fh_alloc(ctx, s->gy, fld)) || (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
+  if ((rc = fh_alloc(ctx, s->C, fld)) || (rc = fh_alloc(ctx, s->Ch, fld)) || (rc = fh_alloc(ctx, s->V2, fld)) ||
+      (rc = fh_alloc(ctx, s->alx, fld)) || (rc = fh_alloc(ctx, s->gx, fld)) || (rc = fh_alloc(ctx, s->fax, fld)) ||
+      (rc = fh_alloc(ctx, s->aly, fld)) || (rc = fh_alloc(ctx, s->gy, fld)) || (rc = fh_alloc(ctx, s->fay, fld)) ||
+      (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, s->W, sizeof(double) * 2 * (size_t)max_steps *
                                     (max_steps <= kWeightTableMaxSteps ? (size_t)max_steps : 1))) ||
       (rc = fh_alloc(ctx, s->cw, sizeof(double) * 4 * (max_steps <= kWeightTableMaxSteps ? (size_t)max_steps : 1))) ||
@@ -405,7 +488,7 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
       return rc;
     }
     s->ldfar = fh_blk_ppad(*s->blk);
-    if ((rc = fh_alloc(ctx, s->far, sizeof(double) * 2 * kTgBlock * (size_t)s->ldfar, false))) {
+    if ((rc = fh_alloc(ctx, s->far, sizeof(float2) * 2 * kTgBlock * (size_t)s->ldfar, false))) {
       delete s;
       return rc;
     }
@@ -428,7 +511,6 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
-  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->Cfull.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
   s->tstep = 0;
   s->j0 = 0;
   s->have_state = true;
@@ -442,7 +524,6 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
-  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->Cfull.p, s->C.p, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->tstep = 0;
   s->j0 = 0;
@@ -457,7 +538,7 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
   FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_tg_step: nsteps < 0");
   FH_REQUIRE(ctx, s->tstep + nsteps <= s->max_steps, FH_ENOMEM, "fh_tg_step: history full (%d + %d > %d)", s->tstep,
              nsteps, s->max_steps);
-  if (ctx->graphs && s->tstep == 0 && nsteps > 1 && !ctx->prof) {
+  if (ctx->graphs && s->tstep == 0 && nsteps > 1) {
     int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
       for (int n = 0; n < nsteps; ++n) {
         int r = tg_one_step(s);
