@@ -44,7 +44,8 @@ const char *fh_last_error(const fh_ctx *ctx);
 int fh_ctx_sync(fh_ctx *ctx);
 /* A multi-step call that starts from the initial state (fh_*_step right after
  * setting the state) is recorded once as a CUDA graph and replayed by later
- * identical calls (on by default; off while kernel profiling is on). */
+ * identical calls (on by default).  With kernel profiling on, the profiling
+ * marks are recorded into the graph and each replay synchronises the stream. */
 int fh_ctx_set_graphs(fh_ctx *ctx, int enable);
 /* Non-blocking: 1 if all work enqueued on the context finished, 0 if not, < 0 on error. */
 int fh_ctx_query(fh_ctx *ctx);

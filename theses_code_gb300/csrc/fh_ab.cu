@@ -15,12 +15,18 @@ struct fh_ab_solver {
   int m = 0, max_steps = 0, step = 0, nrows = 0, max_splits = 1024;
   long long P = 0;  // m+1 rounded up to even
   double tau = 0, alpha = 0, A = 0, Bd = 0, Cc = 0;
-  fh_dbuf w, ii, al, den, C, D, W, part, S, src, bl, br;
+  fh_dbuf w, ii, al, den, inv, sl, pf, pb, C, D, W, part, S, src, bl, br;
   fh_graph_cache graph;
 };
 
 // al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
-__global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__restrict__ al, double *__restrict__ den) {
+// The matrix is fixed, so the step-independent parts of both recurrences are
+// tabulated here once: inv[j] = 1/den[j], the forward slope sl[j] = -A inv[j],
+// and the per-lane chunk prefix products of the forward slopes (pf) and of the
+// backward slopes -al[j] (pb) in the chunking of k_ab_line.
+__global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__restrict__ al, double *__restrict__ den,
+                            double *__restrict__ inv, double *__restrict__ sl, double *__restrict__ pf,
+                            double *__restrict__ pb) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   double a = 0.0;
   al[0] = 0.0;
@@ -30,6 +36,20 @@ __global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__res
     a = Cc / d;
     al[j] = a;
     den[j] = d;
+    inv[j] = 1.0 / d;
+    sl[j] = -A * inv[j];
+  }
+  const int ch = (m + 31) / 32;
+  double p = 1.0;
+  for (int j = 1; j <= m; ++j) {
+    p = ((j - 1) % ch == 0) ? sl[j] : p * sl[j];
+    pf[j] = p;
+  }
+  double q = 1.0;
+  for (int j = m - 1; j >= 0; --j) {
+    const int b1 = min(m, (j / ch + 1) * ch);
+    q = (j == b1 - 1) ? -al[j] : q * -al[j];
+    pb[j] = q;
   }
 }
 
@@ -39,61 +59,81 @@ __global__ void k_ab_stepweights(int i, const double *__restrict__ w, double *__
   if (tt < i - 1) W[tt] = w[i - tt];
 }
 
-__global__ void k_ab_line(int m, double oma, double A, const double *__restrict__ ii, const double *__restrict__ al,
-                          const double *__restrict__ den, const double *__restrict__ src, const double *__restrict__ blp,
-                          const double *__restrict__ brp, double *C, const double *__restrict__ S,
-                          double *__restrict__ Dnew, double tau) {
+// One step of the tridiagonal solve (the line has m+1 nodes):
+//   forward   bt[j] = (Rp_j - A bt[j-1]) / den_j = sl_j bt[j-1] + Rp_j inv_j
+//   backward  C[j]  = bt[j] - al[j] C[j+1],  C[m] = right boundary value
+// All threads stage the right parts and the tabulated coefficients into
+// shared memory with coalesced loads (skewed by i / chunk so that the 32
+// lanes' chunks fall on distinct banks), warp 0 walks its lanes' chunks from
+// a zero start and adds prefix * start value after a warp scan of the chunk
+// maps (fh_line_solve_prefix scheme), then all threads write C and the new
+// history entry.
+constexpr int kAbThreads = 256;
+__global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const double *__restrict__ ii,
+                                                        const double *__restrict__ alg,
+                                                        const double *__restrict__ invg,
+                                                        const double *__restrict__ slg,
+                                                        const double *__restrict__ pfg,
+                                                        const double *__restrict__ pbg,
+                                                        const double *__restrict__ src,
+                                                        const double *__restrict__ blp,
+                                                        const double *__restrict__ brp, double *C,
+                                                        const double *__restrict__ S, double *__restrict__ Dnew,
+                                                        double tau) {
   extern __shared__ double sm[];
-  double *rp = sm, *bt = sm + (m + 1);
-  const int lane = threadIdx.x & 31;
-  const double cI = ii[0] / oma;  // Ii/(1-a)
-  const double bl = blp[0], br = brp[0];
-  // forward: bt[j] = (Rp_j - A bt[j-1]) / den_j, j = 1..m
   const int ch = (m + 31) / 32;
-  const int f0 = 1 + lane * ch, f1 = min(m + 1, f0 + ch);
-  fh_aff F{1.0, 0.0};
-  for (int j = f0; j < f1; ++j) {
-    double r = cI * C[j] + src[j];
-    if (S) r -= S[j] / oma;  // MF_intF_simple returns ret/(1-a)
-    rp[j] = r;
-    const double dj = den[j];
-    F = fh_aff_compose(fh_aff{-A / dj, r / dj}, F);
+  const int Lm = m + 2 + m / ch + 1;
+  double *rb = sm, *sl = rb + Lm, *pf = sl + Lm, *al = pf + Lm, *pb = al + Lm, *bt = pb + Lm, *cv = bt + Lm;
+  auto sk = [ch](int j) { return j + j / ch; };
+  const double cI = ii[0] / oma;  // Ii/(1-a)
+  const double ioma = 1.0 / oma, itau = 1.0 / tau;
+  for (int j = threadIdx.x; j <= m; j += kAbThreads) {
+    double r = fma(cI, C[j], src[j]);
+    if (S) r -= S[j] * ioma;  // MF_intF_simple returns ret/(1-a)
+    rb[sk(j)] = r * invg[j];
+    sl[sk(j)] = slg[j];
+    pf[sk(j)] = pfg[j];
+    al[sk(j)] = alg[j];
+    pb[sk(j)] = pbg[j];
   }
-  const fh_aff Pf = fh_warp_exclusive_affine(F);
-  double b = fma(Pf.a, bl, Pf.b);
-  for (int j = f0; j < f1; ++j) {
-    b = (rp[j] - A * b) / den[j];
-    bt[j] = b;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const double bl = blp[0], br = brp[0];
+    const int f0 = 1 + lane * ch, f1 = min(m + 1, f0 + ch);
+    double b = 0.0;
+    for (int j = f0; j < f1; ++j) {
+      b = fma(sl[sk(j)], b, rb[sk(j)]);
+      bt[sk(j)] = b;
+    }
+    const fh_aff Pf = fh_warp_exclusive_affine(f1 > f0 ? fh_aff{pf[sk(f1 - 1)], b} : fh_aff{1.0, 0.0});
+    const double s0 = fma(Pf.a, bl, Pf.b);  // bt[f0 - 1]
+    for (int j = f0; j < f1; ++j) bt[sk(j)] = fma(pf[sk(j)], s0, bt[sk(j)]);
+    if (lane == 0) bt[sk(0)] = bl;
+    __syncwarp();
+    const int b0 = lane * ch, b1 = min(m, b0 + ch);
+    double c = 0.0;
+    for (int j = b1 - 1; j >= b0; --j) {
+      c = fma(-al[sk(j)], c, bt[sk(j)]);
+      cv[sk(j)] = c;
+    }
+    const fh_aff Pb = fh_warp_exclusive_affine_rev(b1 > b0 ? fh_aff{pb[sk(b0)], c} : fh_aff{1.0, 0.0});
+    const double t = fma(Pb.a, br, Pb.b);  // C[b1]
+    for (int j = b0; j < b1; ++j) cv[sk(j)] = fma(pb[sk(j)], t, cv[sk(j)]);
+    if (lane == 0) cv[sk(m)] = br;
   }
-  if (lane == 0) bt[0] = bl;
-  __syncwarp();
-  // backward: C[j] = bt[j] - al[j] C[j+1], j = m-1..0, C[m] = br
-  const int chb = (m + 31) / 32;
-  const int b0 = lane * chb, b1 = min(m, b0 + chb);
-  fh_aff G{1.0, 0.0};
-  for (int j = b1 - 1; j >= b0; --j) G = fh_aff_compose(fh_aff{-al[j], bt[j]}, G);
-  const fh_aff Pb = fh_warp_exclusive_affine_rev(G);
-  double c = fma(Pb.a, br, Pb.b);
-  for (int j = b1 - 1; j >= b0; --j) {
-    c = bt[j] - al[j] * c;
+  __syncthreads();
+  for (int j = threadIdx.x; j <= m; j += kAbThreads) {
+    const double v = cv[sk(j)];
     const double old = C[j];
-    C[j] = c;
-    if (Dnew) Dnew[j] = (c - old) / tau;
-  }
-  if (lane == 0) {
-    const double old = C[m];
-    C[m] = br;
-    if (Dnew) Dnew[m] = (br - old) / tau;
+    C[j] = v;
+    if (Dnew) Dnew[j] = (v - old) * itau;
   }
 }
 
-__global__ void k_reduce_splits(int splits, long long P, const double *__restrict__ part, long long ldpart,
-                                double *__restrict__ S) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  double acc = 0.0;
-  for (int s = 0; s < splits; ++s) acc += part[(long long)s * ldpart + p];
-  S[p] = acc;
+static size_t ab_line_smem(int m) {
+  const int ch = (m + 31) / 32;
+  return sizeof(double) * 7 * (size_t)(m + 2 + m / ch + 1);
 }
 
 static int ab_one_step(fh_ab_solver *s) {
@@ -111,16 +151,16 @@ static int ab_one_step(fh_ab_solver *s) {
     if ((rc = fh_launch_hist_sum_partials(ctx, 1, K, s->P, s->W.as<double>(), s->max_steps + 1, s->D.as<double>(),
                                           s->P, splits, kchunk, s->part.as<double>(), s->P)))
       return rc;
-    k_reduce_splits<<<(unsigned)fh_ceil_div(s->P, 256), 256, 0, ctx->stream>>>(splits, s->P, s->part.as<double>(),
-                                                                               s->P, s->S.as<double>());
-    if ((rc = fh_after_launch(ctx, "k_reduce_splits"))) return rc;
+    if ((rc = fh_launch_reduce_splits(ctx, splits, s->P, s->part.as<double>(), s->P, s->S.as<double>()))) return rc;
     S = s->S.as<double>();
   }
-  const size_t smem = sizeof(double) * 2 * (size_t)(s->m + 1);
-  k_ab_line<<<1, 32, smem, ctx->stream>>>(s->m, 1.0 - s->alpha, s->A, s->ii.as<double>(), s->al.as<double>(),
-                                          s->den.as<double>(), s->src.as<double>() + (long long)row * (s->m + 1),
+  fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+  k_ab_line<<<1, kAbThreads, ab_line_smem(s->m), ctx->stream>>>(s->m, 1.0 - s->alpha, s->ii.as<double>(), s->al.as<double>(),
+                                          s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
+                                          s->pb.as<double>(), s->src.as<double>() + (long long)row * (s->m + 1),
                                           s->bl.as<double>() + row, s->br.as<double>() + row, s->C.as<double>(), S,
                                           s->D.as<double>() + (long long)s->step * s->P, s->tau);
+  fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_ab_line"))) return rc;
   s->step++;
   return FH_OK;
@@ -131,8 +171,13 @@ extern "C" {
 int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh_ab_solver **out) {
   FH_REQUIRE(ctx, ctx && out, FH_EINVAL, "fh_ab_create: null argument");
   *out = nullptr;
-  FH_REQUIRE(ctx, m >= 2 && m <= 12000 && max_steps >= 1 && tau > 0 && alpha > 0 && alpha < 1, FH_EINVAL,
-             "fh_ab_create: need 2 <= m <= 12000, max_steps >= 1, tau > 0, 0 < alpha < 1");
+  FH_REQUIRE(ctx, m >= 2 && m <= 3500 && max_steps >= 1 && tau > 0 && alpha > 0 && alpha < 1, FH_EINVAL,
+             "fh_ab_create: need 2 <= m <= 3500, max_steps >= 1, tau > 0, 0 < alpha < 1");
+  {
+    const size_t sm = ab_line_smem(m);
+    FH_REQUIRE(ctx, sm <= 200 * 1024, FH_EINVAL, "fh_ab_create: m too large for the staged line (m <= 3500)");
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ab_line, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  }
   fh_ab_solver *s = new fh_ab_solver();
   s->ctx = ctx;
   s->m = m;
@@ -146,7 +191,9 @@ int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh
   int rc;
   const size_t fld = sizeof(double) * (size_t)s->P;
   if ((rc = fh_alloc(ctx, s->w, sizeof(double) * (size_t)(max_steps + 2))) || (rc = fh_alloc(ctx, s->ii, 16)) ||
-      (rc = fh_alloc(ctx, s->al, fld)) || (rc = fh_alloc(ctx, s->den, fld)) || (rc = fh_alloc(ctx, s->C, fld)) ||
+      (rc = fh_alloc(ctx, s->al, fld)) || (rc = fh_alloc(ctx, s->den, fld)) || (rc = fh_alloc(ctx, s->inv, fld)) ||
+      (rc = fh_alloc(ctx, s->sl, fld)) || (rc = fh_alloc(ctx, s->pf, fld)) || (rc = fh_alloc(ctx, s->pb, fld)) ||
+      (rc = fh_alloc(ctx, s->C, fld)) ||
       (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, s->W, sizeof(double) * (size_t)(max_steps + 1))) ||
       (rc = fh_alloc(ctx, s->part, fld * (size_t)s->max_splits, false)) || (rc = fh_alloc(ctx, s->S, fld))) {
@@ -163,7 +210,9 @@ int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(&ii_h, s->w.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->Bd = (ii_h / (1.0 - alpha)) + (2.0 / (h * h));
-  k_ab_factor<<<1, 1, 0, ctx->stream>>>(m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>());
+  k_ab_factor<<<1, 1, 0, ctx->stream>>>(m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>(),
+                                        s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
+                                        s->pb.as<double>());
   if ((rc = fh_after_launch(ctx, "k_ab_factor"))) {
     delete s;
     return rc;
@@ -224,7 +273,9 @@ int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   const double h = 1.0 / s->m;
   s->Bd = (Ii / (1.0 - s->alpha)) + (2.0 / (h * h));
-  k_ab_factor<<<1, 1, 0, ctx->stream>>>(s->m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>());
+  k_ab_factor<<<1, 1, 0, ctx->stream>>>(s->m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>(),
+                                        s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
+                                        s->pb.as<double>());
   return fh_after_launch(ctx, "k_ab_factor");
 }
 

@@ -45,5 +45,47 @@ __device__ __forceinline__ fh_aff fh_warp_exclusive_affine(fh_aff f) {
   return fh_aff{ea, eb};
 }
 
+// ------------------------------------------------------ Moebius maps
+// x -> (m00 x + m01) / (m10 x + m11) as a 2x2 matrix acting on (x, 1).  The
+// Thomas alpha recurrence Al[i+1] = B_i / (R_i - A_i Al[i]) is the matrix
+// [[0, B_i], [-A_i, R_i]]; chunks compose by matrix products, rescaled by a
+// power of two (exact) to keep the entries in range.
+struct fh_mob {
+  double m00, m01, m10, m11;
+};
+__device__ __forceinline__ fh_mob fh_mob_normalise(fh_mob t) {
+  const double mx = fmax(fmax(fabs(t.m00), fabs(t.m01)), fmax(fabs(t.m10), fabs(t.m11)));
+  if (!(mx > 0.0) || !isfinite(mx)) return t;
+  int e;
+  frexp(mx, &e);
+  return fh_mob{ldexp(t.m00, -e), ldexp(t.m01, -e), ldexp(t.m10, -e), ldexp(t.m11, -e)};
+}
+// f2 o f1 (f1 applied first) = M2 * M1
+__device__ __forceinline__ fh_mob fh_mob_compose(fh_mob f2, fh_mob f1) {
+  return fh_mob{fma(f2.m00, f1.m00, f2.m01 * f1.m10), fma(f2.m00, f1.m01, f2.m01 * f1.m11),
+                fma(f2.m10, f1.m00, f2.m11 * f1.m10), fma(f2.m10, f1.m01, f2.m11 * f1.m11)};
+}
+// Exclusive warp scan: lane l receives f_{l-1} o ... o f_0 (identity for lane 0).
+__device__ __forceinline__ fh_mob fh_warp_exclusive_mob(fh_mob f) {
+  const unsigned lane = threadIdx.x & 31u;
+  fh_mob g = fh_mob_normalise(f);
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    fh_mob p;
+    p.m00 = __shfl_up_sync(0xffffffffu, g.m00, d);
+    p.m01 = __shfl_up_sync(0xffffffffu, g.m01, d);
+    p.m10 = __shfl_up_sync(0xffffffffu, g.m10, d);
+    p.m11 = __shfl_up_sync(0xffffffffu, g.m11, d);
+    if (lane >= (unsigned)d) g = fh_mob_normalise(fh_mob_compose(g, p));
+  }
+  fh_mob e;
+  e.m00 = __shfl_up_sync(0xffffffffu, g.m00, 1);
+  e.m01 = __shfl_up_sync(0xffffffffu, g.m01, 1);
+  e.m10 = __shfl_up_sync(0xffffffffu, g.m10, 1);
+  e.m11 = __shfl_up_sync(0xffffffffu, g.m11, 1);
+  if (lane == 0) e = fh_mob{1.0, 0.0, 0.0, 1.0};
+  return e;
+}
+
 // ----------------------------------------------------------- misc
 __host__ __device__ __forceinline__ long long fh_ceil_div(long long a, long long b) { return (a + b - 1) / b; }

@@ -2,8 +2,9 @@
 // mt_psi_caputo.cpp:369-1507 with gamma = 1): per step
 //   1. k_h_weights      per-instance history weights and current weight
 //   2. k_hist_tiles     history sum per instance segment (split-K partials)
-//   3. k_h_line         one thread per instance: coefficients, right part,
-//                       Thomas sweep, back substitution, history append
+//   3. k_h_line_warp    one warp per instance: coefficients, right part,
+//                       Thomas sweep as warp scans, back substitution,
+//                       history append
 //
 // All instances advance in lock step.  The concatenated state holds each
 // instance's N_i+2 nodes in a segment padded to an even length; the history
@@ -14,10 +15,12 @@
 
 #include "fh_internal.h"
 #include "fh_common.cuh"
+#include "fh_linescan.cuh"
 #include "fh_weights.cuh"
 
 struct fh_h_dev_inst {
   int N, weights, kmodel, gravity;
+  int fixed;  // coefficients independent of u and of the step: factor once
   long long off;  // segment start in the concatenated state
   double dL, Dg, Da, tau, alpha, beta, kc, kgam, cinv, al_left, bt_left, u_right;
 };
@@ -30,12 +33,12 @@ struct fh_h_tile {
 
 struct fh_h_batch {
   fh_ctx *ctx = nullptr;
-  int n = 0, max_steps = 0, tstep = 1, nsaved = 0, max_splits = 8, max_weights = 0;
+  int n = 0, max_steps = 0, tstep = 1, nsaved = 0, max_splits = 64, max_weights = 0;
   long long Ptot = 0;
   std::vector<fh_h_params> hp;
   std::vector<long long> off;
   std::vector<fh_h_tile> tiles;
-  fh_dbuf inst, tl, U, D, W, wc, part, Al, Bt;
+  fh_dbuf inst, tl, U, D, W, Lb, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
 };
@@ -48,7 +51,7 @@ static constexpr int kTileThreads = 256;  // 512 nodes per tile
 // The reference's t = 0 term multiplies layer1 - layer1 (its layer pointer
 // starts at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
 __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
-                            int ldw, double *__restrict__ wc) {
+                            int ldw, double *__restrict__ wc, const double *__restrict__ Lb) {
   const int b = blockIdx.y;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const fh_h_dev_inst I = inst[b];
@@ -57,7 +60,7 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
     if (t == 0)
       w = 0.0;
     else if (I.weights == FH_W_L1)
-      w = pow((double)(os - t), 1.0 - I.alpha) - pow((double)(os - t - 1), 1.0 - I.alpha);
+      w = Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
     else
       w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
     W[(long long)b * ldw + t] = w;
@@ -68,6 +71,16 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
                 : fh_psi_int((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) *
                       (1 - I.alpha);
   }
+}
+
+// Lag table of the L1 instances: Lb[b][l] = (l+1)^(1-a) - l^(1-a) (mt_minimal.cpp:930),
+// the weight of the layer difference l steps back.
+__global__ void k_h_lagtab(const fh_h_dev_inst *__restrict__ inst, int nlag, double *__restrict__ Lb, int ldw) {
+  const int b = blockIdx.y;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const fh_h_dev_inst I = inst[b];
+  if (I.weights != FH_W_L1 || l >= nlag) return;
+  Lb[(long long)b * ldw + l] = pow((double)(l + 1), 1.0 - I.alpha) - pow((double)l, 1.0 - I.alpha);
 }
 
 // part[s][p] = sum_{k in split s} W[inst][k] * D[k][p] over one tile of one instance.
@@ -119,55 +132,130 @@ __device__ __forceinline__ double fh_h_K(const fh_h_dev_inst &I, double u) {
   return I.kmodel == FH_K_CONST ? I.kc : I.kc * exp(I.kgam * u);
 }
 
-// H_solver::U1 for one instance per thread: al1, Om1 (time part from the
-// partial sums), bt1, bottom Dirichlet, back substitution, history append.
-__global__ void k_h_line(const fh_h_dev_inst *__restrict__ inst, int n, double *__restrict__ U,
-                         const double *__restrict__ wc, const double *__restrict__ part, long long ldpart, int splits,
-                         double *__restrict__ Al, double *__restrict__ Bt, double *__restrict__ Dnew, int append) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= n) return;
+// H_solver::U1 with one warp per instance (al1, Om1, bt1, bottom Dirichlet,
+// back substitution, history append).  The serial recurrences become warp
+// scans over per-lane chunks of consecutive equations:
+//   Al[i+1] = B_i / (R_i - A_i Al[i])            Moebius maps (matrix scan)
+//   Bt[i+1] = (Al[i+1]/B_i)(A_i Bt[i] - Om_i)    affine maps
+//   u_i     = Al[i+1] u_{i+1} + Bt[i+1]           affine maps, reverse order
+// after which every lane re-walks its chunk with the reference's arithmetic
+// from the scanned start value.  The coefficients are kept in the scratch
+// arrays sA, sB, sR (reused for Al[i+1]/B_i) and sOm at the equation's node.
+__global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__restrict__ inst, int n,
+                                                     double *__restrict__ U, const double *__restrict__ wc,
+                                                     const double *__restrict__ part, long long ldpart, int splits,
+                                                     double *__restrict__ Al, double *__restrict__ Bt,
+                                                     double *__restrict__ sA, double *__restrict__ sB,
+                                                     double *__restrict__ sR, double *__restrict__ sOm,
+                                                     double *__restrict__ Dnew, int append, int first) {
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= n) return;  // whole warp
   const fh_h_dev_inst I = inst[b];
-  double *u = U + I.off;
-  double *al = Al + I.off, *bt = Bt + I.off;
+  const long long o = I.off;
+  double *u = U + o;
   const int N = I.N;
-  const double w0 = wc[b];
-  const double DaW = I.Da * w0;
-  double alv = I.al_left, btv = I.bt_left;
-  al[1] = alv;
-  bt[1] = btv;
-  double Km = fh_h_K(I, u[0]), Kc = fh_h_K(I, u[1]);
-  for (int i = 1; i < N; ++i) {
-    const double Kp = fh_h_K(I, u[i + 1]);
-    const double A = I.Dg * Km * I.cinv;
-    const double B = I.Dg * Kp * I.cinv;
-    const double R = I.cinv * (Kp + Km) * I.Dg + DaW;
-    double om = -DaW * u[i];
-    if (I.gravity) om += (Kc - Km) / I.dL;
-    double ts = 0.0;
-    for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + I.off + i];
-    om += I.Da * ts;
-    const double aln = B / (R - A * alv);
-    const double btn = (aln / B) * (A * btv - om);
-    al[i + 1] = aln;
-    bt[i + 1] = btn;
-    alv = aln;
-    btv = btn;
-    Km = Kc;
-    Kc = Kp;
+  const double DaW = I.Da * wc[b];
+  // ---- pass 1: coefficients of equations i in [f0, f1), chunk Moebius map
+  const int chf = (N - 1 + 31) / 32;
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  fh_mob T{1.0, 0.0, 0.0, 1.0};
+  if (f0 < f1) {
+    double Km = fh_h_K(I, u[f0 - 1]), Kc = fh_h_K(I, u[f0]);
+    for (int i = f0; i < f1; ++i) {
+      const double Kp = fh_h_K(I, u[i + 1]);
+      const double A = I.Dg * Km * I.cinv;
+      const double B = I.Dg * Kp * I.cinv;
+      const double R = I.cinv * (Kp + Km) * I.Dg + DaW;
+      double om = -DaW * u[i];
+      if (I.gravity) om += (Kc - Km) / I.dL;
+      double ts = 0.0;
+      for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + o + i];
+      om += I.Da * ts;
+      sOm[o + i] = om;
+      if (!I.fixed || first) {
+        sA[o + i] = A;
+        sB[o + i] = B;
+        sR[o + i] = R;
+      }
+      if (!I.fixed) {
+        T = fh_mob_compose(fh_mob{0.0, B, -A, R}, T);
+        if (((i - f0) & 7) == 7) T = fh_mob_normalise(T);
+      }
+      Km = Kc;
+      Kc = Kp;
+    }
   }
-  double un = I.u_right;
-  double old = u[N];
-  u[N] = un;
-  if (append) Dnew[I.off + N] = un - old;
-  for (int i = N - 1; i >= 0; --i) {
-    un = al[i + 1] * un + bt[i + 1];
-    old = u[i];
+  fh_aff F{1.0, 0.0};
+  if (I.fixed) {
+    // constant coefficients: Al[i+1] and Al[i+1]/B_i are computed once,
+    // serially in the reference order, and kept (Al, sR) for later steps
+    if (first) {
+      __syncwarp();
+      if (lane == 0) {
+        double a = I.al_left;
+        Al[o + 1] = a;
+        for (int i = 1; i < N; ++i) {
+          const double B = sB[o + i];
+          a = B / (sR[o + i] - sA[o + i] * a);
+          Al[o + i + 1] = a;
+          sR[o + i] = a / B;
+        }
+      }
+      __syncwarp();
+    }
+    for (int i = f0; i < f1; ++i) {
+      const double gq = sR[o + i];
+      F = fh_aff_compose(fh_aff{gq * sA[o + i], -(gq * sOm[o + i])}, F);
+    }
+  } else {
+    // ---- Al: Moebius scan, re-walk with the reference arithmetic, chunk affine map of Bt
+    const fh_mob PT = fh_warp_exclusive_mob(T);
+    double alv = (lane == 0) ? I.al_left : fma(PT.m00, I.al_left, PT.m01) / fma(PT.m10, I.al_left, PT.m11);
+    for (int i = f0; i < f1; ++i) {
+      const double A = sA[o + i], B = sB[o + i], R = sR[o + i], om = sOm[o + i];
+      const double aln = B / (R - A * alv);
+      const double gq = aln / B;
+      Al[o + i + 1] = aln;
+      sR[o + i] = gq;
+      F = fh_aff_compose(fh_aff{gq * A, -(gq * om)}, F);
+      alv = aln;
+    }
+    if (lane == 0) Al[o + 1] = I.al_left;
+  }
+  // ---- Bt: scan, re-walk Bt[i+1] = (Al[i+1]/B)(A Bt[i] - Om)
+  const fh_aff PF = fh_warp_exclusive_affine(F);
+  double btv = (lane == 0) ? I.bt_left : fma(PF.a, I.bt_left, PF.b);
+  for (int i = f0; i < f1; ++i) {
+    btv = sR[o + i] * (sA[o + i] * btv - sOm[o + i]);
+    Bt[o + i + 1] = btv;
+  }
+  if (lane == 0) Bt[o + 1] = I.bt_left;
+  __syncwarp();
+  // ---- back substitution u_i = Al[i+1] u_{i+1} + Bt[i+1], i = N-1..0; u_N = u_right
+  const double uN = I.u_right;
+  const int chb = (N + 31) / 32;
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  fh_aff G{1.0, 0.0};
+  for (int i = b1 - 1; i >= b0; --i) G = fh_aff_compose(fh_aff{Al[o + i + 1], Bt[o + i + 1]}, G);
+  const fh_aff PG = fh_warp_exclusive_affine_rev(G);
+  double un = fma(PG.a, uN, PG.b);  // u at node b1
+  // every lane reads the old values of its own nodes before writing them
+  for (int i = b1 - 1; i >= b0; --i) {
+    un = Al[o + i + 1] * un + Bt[o + i + 1];
+    const double old = u[i];
     u[i] = un;
-    if (append) Dnew[I.off + i] = un - old;
+    if (append) Dnew[o + i] = un - old;
   }
-  old = u[N + 1];
-  u[N + 1] = u[N];
-  if (append) Dnew[I.off + N + 1] = u[N + 1] - old;
+  if (lane == 0) {
+    const double oldN = u[N], oldG = u[N + 1];
+    u[N] = uN;
+    u[N + 1] = uN;
+    if (append) {
+      Dnew[o + N] = uN - oldN;
+      Dnew[o + N + 1] = uN - oldG;
+    }
+  }
 }
 
 // ------------------------------------------------------------------- host
@@ -178,8 +266,10 @@ static int h_one_step(fh_h_batch *B) {
   const int K = os >= 2 ? os - 1 : 0;
   int rc;
   dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, 128), (unsigned)B->n);
+  fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
   k_h_weights<<<gw, 128, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
-                                           B->max_weights, B->wc.as<double>());
+                                           B->max_weights, B->wc.as<double>(), B->Lb.as<double>());
+  fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
   if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
   int splits = 0, kchunk = 0;
   if (K > 0) {
@@ -188,17 +278,27 @@ static int h_one_step(fh_h_batch *B) {
     dim3 g((unsigned)B->tiles.size(), (unsigned)splits);
     const size_t smem = sizeof(double) * (size_t)kchunk;
     FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
     k_hist_tiles<<<g, kTileThreads, smem, ctx->stream>>>(B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
                                                          B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
                                                          B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
     if ((rc = fh_after_launch(ctx, "k_hist_tiles"))) return rc;
+    if (splits > 2) {  // fold the partial sums into split 0 (in split order)
+      if ((rc = fh_launch_reduce_splits(ctx, splits, B->Ptot, B->part.as<double>(), B->Ptot, B->part.as<double>())))
+        return rc;
+      splits = 1;
+    }
   }
   const int append = os >= 1;
   double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
-  k_h_line<<<(unsigned)fh_ceil_div(B->n, 64), 64, 0, ctx->stream>>>(
+  fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+  k_h_line_warp<<<(unsigned)fh_ceil_div(B->n, 4), 128, 0, ctx->stream>>>(
       B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wc.as<double>(), B->part.as<double>(), B->Ptot,
-      splits, B->Al.as<double>(), B->Bt.as<double>(), Dnew, append);
-  if ((rc = fh_after_launch(ctx, "k_h_line"))) return rc;
+      splits, B->Al.as<double>(), B->Bt.as<double>(), B->sA.as<double>(), B->sB.as<double>(), B->sR.as<double>(),
+      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0);
+  fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+  if ((rc = fh_after_launch(ctx, "k_h_line_warp"))) return rc;
   B->nsaved++;
   B->tstep++;
   return FH_OK;
@@ -231,6 +331,7 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     I.weights = p.weights;
     I.kmodel = p.kmodel;
     I.gravity = p.gravity;
+    I.fixed = (p.kmodel == FH_K_CONST) && (p.weights == FH_W_L1 || p.beta == 1.0);
     I.off = off;
     I.dL = p.L / p.N;
     I.Dg = pow(I.dL, -2.0);
@@ -255,9 +356,11 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
   const size_t st = sizeof(double) * (size_t)B->Ptot;
   if ((rc = fh_alloc(ctx, B->inst, sizeof(fh_h_dev_inst) * ninst, false)) ||
       (rc = fh_alloc(ctx, B->tl, sizeof(fh_h_tile) * B->tiles.size(), false)) || (rc = fh_alloc(ctx, B->U, st)) ||
-      (rc = fh_alloc(ctx, B->Al, st)) || (rc = fh_alloc(ctx, B->Bt, st)) ||
+      (rc = fh_alloc(ctx, B->Al, st)) || (rc = fh_alloc(ctx, B->Bt, st)) || (rc = fh_alloc(ctx, B->sA, st)) ||
+      (rc = fh_alloc(ctx, B->sB, st)) || (rc = fh_alloc(ctx, B->sR, st)) || (rc = fh_alloc(ctx, B->sOm, st)) ||
       (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, B->W, sizeof(double) * (size_t)ninst * B->max_weights)) ||
+      (rc = fh_alloc(ctx, B->Lb, sizeof(double) * (size_t)ninst * B->max_weights, false)) ||
       (rc = fh_alloc(ctx, B->wc, sizeof(double) * ninst)) ||
       (rc = fh_alloc(ctx, B->part, st * (size_t)B->max_splits, false))) {
     delete B;
@@ -269,6 +372,12 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     delete B;
     return fh_set_error(ctx, FH_ECUDA, "fh_h_batch_create: upload failed");
+  }
+  k_h_lagtab<<<dim3((unsigned)fh_ceil_div(B->max_weights, 128), (unsigned)ninst), 128, 0, ctx->stream>>>(
+      B->inst.as<fh_h_dev_inst>(), B->max_weights, B->Lb.as<double>(), B->max_weights);
+  if ((rc = fh_after_launch(ctx, "k_h_lagtab"))) {
+    delete B;
+    return rc;
   }
   *out = B;
   return FH_OK;

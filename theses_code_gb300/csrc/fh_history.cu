@@ -210,6 +210,39 @@ __global__ void k_hist_sum_layers(int K, long long P, const double *__restrict__
   S[p] = acc;
 }
 
+// S[p] = sum_s part[s][p] in split order: 8 warps take every 8th split for 32
+// points (coalesced), then the 8 warp sums are added in warp order.
+__global__ void __launch_bounds__(256) k_reduce_splits(int splits, long long P, const double *part,
+                                                       long long ldpart, double *S) {
+  __shared__ double acc8[8][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long p = (long long)blockIdx.x * 32 + lane;
+  double a0 = 0.0, a1 = 0.0;
+  if (p < P) {
+    int s = warp;
+    for (; s + 8 < splits; s += 16) {
+      a0 += part[(long long)s * ldpart + p];
+      a1 += part[(long long)(s + 8) * ldpart + p];
+    }
+    if (s < splits) a0 += part[(long long)s * ldpart + p];
+  }
+  acc8[warp][lane] = a0 + a1;
+  __syncthreads();
+  if (warp == 0 && p < P) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += acc8[w][lane];
+    S[p] = t;
+  }
+}
+
+int fh_launch_reduce_splits(fh_ctx *ctx, int splits, long long P, const double *part, long long ldpart, double *S) {
+  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  k_reduce_splits<<<(unsigned)fh_ceil_div(P, 32), 256, 0, ctx->stream>>>(splits, P, part, ldpart, S);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  return fh_after_launch(ctx, "k_reduce_splits");
+}
+
 void fh_hist_plan(long long P, int K, int max_splits, int *splits, int *kchunk) {
   // Enough CTAs for ~3 waves of 8 resident 256-thread CTAs on 152 SMs, but at
   // least 32 layers per split so the partial traffic stays small.

@@ -151,6 +151,8 @@ int fh_launch_weights_psi(fh_ctx *ctx, int K, double x0, double len, double X, d
 int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                 const double *D, long long ldd, int splits, int kchunk, double *part,
                                 long long ldpart);
+// S[p] = sum_s part[s*ldpart + p] in split order (S may alias split 0).
+int fh_launch_reduce_splits(fh_ctx *ctx, int splits, long long P, const double *part, long long ldpart, double *S);
 // History stored as (hi, lo) FP32 pairs, double-float accumulation; split 0
 // starts from far[m*ldfar + p] (a (hi, lo) pair per point) when far != null.
 int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,

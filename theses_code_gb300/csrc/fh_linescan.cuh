@@ -127,3 +127,55 @@ __device__ __forceinline__ void fh_line_solve_staged(int N, const double *fa, co
   }
   __syncwarp();
 }
+
+// ------------------------------------------------------------------------
+// Prefix variant for a factorization that is fixed over many solves: the
+// per-lane chunk products of the forward slopes (pf) and of the backward
+// slopes (pb) are precomputed (fh_line_prefix_products), so each phase walks
+// its chunk once from a zero start and then adds prefix * start value:
+//   forward   Bt[i+1] = b0_i + pf_i Bt[f0]       pf_i = fa_{f0} ... fa_i
+//   backward  u_i     = v0_i + pb_i u_{b1}       pb_i = al'_i ... al'_{b1-1}
+// Two FP64 operations per equation and phase instead of three.  Chunking as in
+// fh_line_solve_staged: lane l owns forward equations [1 + l chf, 1 + (l+1) chf)
+// and backward nodes [l chb, (l+1) chb), chf = ceil((N-1)/32), chb = ceil(N/32).
+__host__ __device__ inline int fh_chunk_f(int N) { return (N - 1 + 31) / 32; }
+__host__ __device__ inline int fh_chunk_b(int N) { return (N + 31) / 32; }
+
+// fa, fb, al, pf, pb: staged (skewed) arrays of the line; bt: scratch;
+// u: result u_i (i = 0..N+1), may alias fa.
+__device__ __forceinline__ void fh_line_solve_prefix(int N, const double *fa, const double *fb, const double *al,
+                                                     const double *pf, const double *pb, double al1, double bt1,
+                                                     double *bt, double *u) {
+  const int lane = threadIdx.x & 31;
+  const int chf = fh_chunk_f(N);
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  double b = 0.0;
+  for (int i = f0; i < f1; ++i) {
+    b = fma(fa[fh_sk(i)], b, fb[fh_sk(i)]);
+    bt[fh_sk(i)] = b;
+  }
+  const fh_aff Pf = fh_warp_exclusive_affine(f1 > f0 ? fh_aff{pf[fh_sk(f1 - 1)], b} : fh_aff{1.0, 0.0});
+  const double s = fma(Pf.a, bt1, Pf.b);  // Bt[f0]
+  for (int i = f0; i < f1; ++i) bt[fh_sk(i)] = fma(pf[fh_sk(i)], s, bt[fh_sk(i)]);
+  if (lane == 0) bt[fh_sk(0)] = bt1;
+  __syncwarp();
+  const double alN = (N >= 2) ? al[fh_sk(N - 1)] : al1;
+  const double uN = bt[fh_sk(N - 1)] / (1.0 - alN);
+  const int chb = fh_chunk_b(N);
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  double v = 0.0;
+  __syncwarp();  // u may alias fa: all forward reads are done
+  for (int i = b1 - 1; i >= b0; --i) {
+    v = fma((i >= 1) ? al[fh_sk(i)] : al1, v, bt[fh_sk(i)]);
+    u[fh_sk(i)] = v;
+  }
+  const fh_aff Pb = fh_warp_exclusive_affine_rev(b1 > b0 ? fh_aff{pb[fh_sk(b0)], v} : fh_aff{1.0, 0.0});
+  const double t = fma(Pb.a, uN, Pb.b);  // u_{b1}
+  for (int i = b0; i < b1; ++i) u[fh_sk(i)] = fma(pb[fh_sk(i)], t, u[fh_sk(i)]);
+  if (lane == 0) {
+    u[fh_sk(N)] = uN;
+    u[fh_sk(N + 1)] = uN;
+  }
+  __syncwarp();
+}
+

@@ -58,7 +58,7 @@ struct fh_tg_solver {
   bool have_state = false;
   bool factor_fixed = false;
   int max_splits = 8;
-  fh_dbuf C, Ch, V2, D, W, cw, part, alx, gx, fax, aly, gy, fay, far;
+  fh_dbuf C, Ch, V2, D, W, cw, part, alx, gx, fax, pfx, pbx, aly, gy, fay, pfy, pby, far;
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
   fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
@@ -94,7 +94,8 @@ __global__ void k_tg_weights(fh_tg_dev g, int j, int kstart, double *__restrict_
 // point of equation i.  dir 0: x lines, dir 1: y lines.  A, B, R in the
 // reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
 __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2, const double *__restrict__ cw,
-                            double *__restrict__ al, double *__restrict__ gg, double *__restrict__ fa) {
+                            double *__restrict__ al, double *__restrict__ gg, double *__restrict__ fa,
+                            double *__restrict__ pf, double *__restrict__ pb) {
   const int line = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int nlines = dir == 0 ? g.M : g.sN;
   if (line >= nlines) return;
@@ -124,6 +125,24 @@ __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2,
     fa[id] = gi * A;
     alv = aln;
   }
+  // chunk prefix products of the forward slopes and of the backward slopes in
+  // the lane chunking of fh_line_solve_prefix
+  const int chf = fh_chunk_f(N), chb = fh_chunk_b(N);
+  double p = 1.0;
+  for (int i = 1; i < N; ++i) {
+    const long long id = base + i * stride;
+    p = ((i - 1) % chf == 0) ? fa[id] : p * fa[id];
+    pf[id] = p;
+  }
+  const double al1 = dir == 0 ? 0.0 : 1.0;
+  double q = 1.0;
+  for (int i = N - 1; i >= 0; --i) {
+    const long long id = base + i * stride;
+    const int b1 = min(N, (i / chb + 1) * chb);
+    const double a = (i >= 1) ? al[id] : al1;
+    q = (i == b1 - 1) ? a : q * a;
+    pb[id] = q;
+  }
 }
 
 // All step weights of a solve in one launch: row j of Wall holds
@@ -151,84 +170,259 @@ __global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ W
 // Shared-memory footprint of one staged line array: fh_sk(N+1)+1 doubles.
 __host__ __device__ inline int tg_line_stride(int N) { return (N + 2) + ((N + 2) >> 4) + 2; }
 
-static constexpr int kXThreads = 128;  // one x line per CTA
+static constexpr int kXLines = 4;       // x lines per CTA, one warp each
+static constexpr int kXThreads = 32 * kXLines;
 static constexpr int kYThreads = 512;  // four adjacent y lines per CTA
 static constexpr int kUnroll = 4;      // equations staged per thread per round
 
-// x half-step (fr_d_t_g_2d.cpp:2577-2590): one CTA per line j = 1..M-1.  All
-// threads stage the line's forward maps into shared memory with independent,
-// coalesced loads (kUnroll equations per thread in flight), warp 0 solves it,
-// all threads write the half-step field Ch.  The boundary nodes i = 0, N, N+1
-// are also written into C, which otherwise keeps the full-step field.
+// x half-step (fr_d_t_g_2d.cpp:2577-2590): four lines j per CTA.  All threads
+// stage the four lines' forward maps into shared memory with independent,
+// coalesced loads, then warp w solves line w (the four solving warps sit on
+// the SM's four sub-partitions, so the FP64 work of the solves runs in
+// parallel), then all threads write the half-step field Ch.  The boundary
+// nodes i = 0, N, N+1 are also written into C, which otherwise keeps the
+// full-step field.
 __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C, double *__restrict__ Ch,
                                                         const double *__restrict__ part, long long ldp, int splits,
                                                         const double *__restrict__ fax,
                                                         const double *__restrict__ gx,
                                                         const double *__restrict__ alx,
+                                                        const double *__restrict__ pfx,
+                                                        const double *__restrict__ pbx,
                                                         const double *__restrict__ cw,
                                                         const float2 *__restrict__ far) {
   extern __shared__ double sbuf[];
-  const int line = 1 + blockIdx.x;
+  const int warp = threadIdx.x >> 5;
+  const int line0 = 1 + blockIdx.x * kXLines;
   const int N = g.sN;
   const int L = tg_line_stride(N);
-  double *fa = sbuf, *fb = fa + L, *al = fb + L, *bt = al + L;
-  const long long base = (long long)line * g.ld;
   const double kst = -g.st * (cw[0] + 0.0), S2 = g.S * 0.5, st = g.st;
-  for (int r0 = 1; r0 < N; r0 += kXThreads * kUnroll) {
-    double ts[kUnroll], c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll];
-#pragma unroll
-    for (int e = 0; e < kUnroll; ++e) {
-      const int i = r0 + threadIdx.x + e * kXThreads;
-      const long long id = base + (i < N ? i : 1);
-      c[e] = C[id];
-      a[e] = fax[id];
-      gi[e] = gx[id];
-      l[e] = alx[id];
-      ts[e] = 0.0;
-      if (far) {
-        const float2 fp = far[id];
-        ts[e] = (double)fp.x + (double)fp.y;
-      }
-    }
-    for (int s = 0; s < splits; ++s)
+  for (int ln = 0; ln < kXLines; ++ln) {
+    const int line = line0 + ln;
+    if (line >= g.M) break;
+    double *fa = sbuf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
+    const long long base = (long long)line * g.ld;
+    for (int r0 = 1; r0 < N; r0 += kXThreads * kUnroll) {
+      double ts[kUnroll], c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
 #pragma unroll
       for (int e = 0; e < kUnroll; ++e) {
         const int i = r0 + threadIdx.x + e * kXThreads;
-        ts[e] += part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)];
+        const long long id = base + (i < N ? i : 1);
+        c[e] = C[id];
+        a[e] = fax[id];
+        gi[e] = gx[id];
+        l[e] = alx[id];
+        qf[e] = pfx[id];
+        qb[e] = pbx[id];
+        ts[e] = 0.0;
+        if (far) {
+          const float2 fp = far[id];
+          ts[e] = (double)fp.x + (double)fp.y;
+        }
       }
+      for (int s = 0; s < splits; ++s)
 #pragma unroll
-    for (int e = 0; e < kUnroll; ++e) {
-      const int i = r0 + threadIdx.x + e * kXThreads;
-      if (i < N) {
-        double om = kst * c[e];
-        om += S2;
-        om += st * ts[e];
-        fa[fh_sk(i)] = a[e];
-        fb[fh_sk(i)] = -gi[e] * om;
-        al[fh_sk(i)] = l[e];
+        for (int e = 0; e < kUnroll; ++e) {
+          const int i = r0 + threadIdx.x + e * kXThreads;
+          ts[e] += part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)];
+        }
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = r0 + threadIdx.x + e * kXThreads;
+        if (i < N) {
+          double om = kst * c[e];
+          om += S2;
+          om += st * ts[e];
+          fa[fh_sk(i)] = a[e];
+          fb[fh_sk(i)] = -gi[e] * om;
+          al[fh_sk(i)] = l[e];
+          pf[fh_sk(i)] = qf[e];
+          pb[fh_sk(i)] = qb[e];
+        }
+      }
+    }
+    // node 0 belongs to lane 0's backward chunk: its prefix product
+    if (threadIdx.x == 0) pb[fh_sk(0)] = pbx[base];
+  }
+  __syncthreads();
+  if (line0 + warp < g.M) {
+    double *fa = sbuf + (size_t)warp * 5 * L;
+    // bt scratch reuses pf's slots only after pf is consumed: use a separate
+    // region, the fb array, which the forward walk overwrites in place
+    fh_line_solve_prefix(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, 0.0, g.C1, fa + L, fa);
+  }
+  __syncthreads();
+  for (int ln = 0; ln < kXLines; ++ln) {
+    const int line = line0 + ln;
+    if (line >= g.M) break;
+    const double *u = sbuf + (size_t)ln * 5 * L;
+    const long long base = (long long)line * g.ld;
+    for (int i = threadIdx.x; i <= N + 1; i += kXThreads) {
+      const double v = u[fh_sk(i)];
+      Ch[base + i] = v;
+      if (i == 0 || i >= N) C[base + i] = v;
+    }
+  }
+}
+
+// x half-step fused with the short history sum of the double-float modes
+// (layers [kstart, j) with j - kstart <= 64, plus the far-history pairs of the
+// blocked mode).  The CTA's four x lines are one contiguous range of 4 (sN+2)
+// points; phase A streams their history layers once and accumulates both the
+// x and the y sums in double-float (the y sums go to Sy for the y sweep), then
+// the x sweep proceeds as in k_tg_xsweep with the x sums from shared memory.
+static constexpr int kXNThreads = 512;
+static constexpr int kNearMax = 64;
+__global__ void __launch_bounds__(kXNThreads) k_tg_xsweep_near(
+    fh_tg_dev g, double *C, double *__restrict__ Ch, const float2 *__restrict__ D, int knear,
+    const double *__restrict__ Wx, const double *__restrict__ Wy, const float2 *__restrict__ farx,
+    const float2 *__restrict__ fary, double *__restrict__ Sy, const double *__restrict__ fax,
+    const double *__restrict__ gx, const double *__restrict__ alx, const double *__restrict__ pfx,
+    const double *__restrict__ pbx, const double *__restrict__ cw) {
+  extern __shared__ double sbuf[];
+  __shared__ float2 wsx[kNearMax], wsy[kNearMax];
+  const int warp = threadIdx.x >> 5;
+  const int line0 = 1 + blockIdx.x * kXLines;
+  const int N = g.sN;
+  const int L = tg_line_stride(N);
+  const int ld = g.ld;
+  double *Sx = sbuf + (size_t)kXLines * 5 * L;  // [4][ld]
+  if (threadIdx.x < knear) {
+    const double a = Wx[threadIdx.x], b = Wy[threadIdx.x];
+    const float ah = __double2float_rn(a), bh = __double2float_rn(b);
+    wsx[threadIdx.x] = make_float2(ah, __double2float_rn(a - (double)ah));
+    wsy[threadIdx.x] = make_float2(bh, __double2float_rn(b - (double)bh));
+  }
+  __syncthreads();
+  // ---- phase A: double-float history sums of the 4 rows (4 points per thread in flight)
+  const int nrows = min(kXLines, g.M - line0);
+  const int npts = nrows * ld;
+  const long long p0 = (long long)line0 * ld;
+  auto acc = [](const float2 w, const float2 d, float &sh, float &sl) {
+    const float ph = w.x * d.x;
+    float pl = fmaf(w.x, d.x, -ph);
+    pl = fmaf(w.x, d.y, pl);
+    pl = fmaf(w.y, d.x, pl);
+    const float t = sh + ph;
+    const float bb = t - sh;
+    const float e = (sh - (t - bb)) + (ph - bb);
+    sh = t;
+    sl += e + pl;
+  };
+  for (int base = 0; base < npts; base += kXNThreads * 4) {
+    float xh[4], xl[4], yh[4], yl[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = base + threadIdx.x + e * kXNThreads;
+      xh[e] = xl[e] = yh[e] = yl[e] = 0.f;
+      if (idx < npts && farx) {
+        const float2 fx = farx[p0 + idx], fy = fary[p0 + idx];
+        xh[e] = fx.x;
+        xl[e] = fx.y;
+        yh[e] = fy.x;
+        yl[e] = fy.y;
+      }
+    }
+    auto renorm = [&]() {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {  // fast two-sum
+        float t = xh[e] + xl[e];
+        xl[e] = xl[e] - (t - xh[e]);
+        xh[e] = t;
+        t = yh[e] + yl[e];
+        yl[e] = yl[e] - (t - yh[e]);
+        yh[e] = t;
+      }
+    };
+    int k = 0;
+    for (; k + 4 <= knear; k += 4) {  // 4 layers x 4 points = 16 loads in flight
+      float2 d[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int idx = base + threadIdx.x + e * kXNThreads;
+          d[u][e] = idx < npts ? __ldcs(D + (long long)(k + u) * g.P + p0 + idx) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float2 wx = wsx[k + u], wy = wsy[k + u];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          acc(wx, d[u][e], xh[e], xl[e]);
+          acc(wy, d[u][e], yh[e], yl[e]);
+        }
+      }
+      if (((k + 4) & 15) == 0) renorm();
+    }
+    for (; k < knear; ++k) {
+      const float2 wx = wsx[k], wy = wsy[k];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int idx = base + threadIdx.x + e * kXNThreads;
+        const float2 d = idx < npts ? __ldcs(D + (long long)k * g.P + p0 + idx) : make_float2(0.f, 0.f);
+        acc(wx, d, xh[e], xl[e]);
+        acc(wy, d, yh[e], yl[e]);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = base + threadIdx.x + e * kXNThreads;
+      if (idx < npts) {
+        Sx[idx] = (double)xh[e] + (double)xl[e];
+        Sy[p0 + idx] = (double)yh[e] + (double)yl[e];
       }
     }
   }
   __syncthreads();
-  if (threadIdx.x < 32) fh_line_solve_staged(N, fa, fb, al, 0.0, g.C1, bt, fa);
+  // ---- phase B: stage the four lines' forward maps (x sums from shared memory)
+  const double kst = -g.st * (cw[0] + 0.0), S2 = g.S * 0.5, st = g.st;
+  for (int ln = 0; ln < nrows; ++ln) {
+    const int line = line0 + ln;
+    double *fa = sbuf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
+    const long long base = (long long)line * ld;
+    for (int i = 1 + threadIdx.x; i < N; i += kXNThreads) {
+      const long long id = base + i;
+      double om = kst * C[id];
+      om += S2;
+      om += st * Sx[ln * ld + i];
+      fa[fh_sk(i)] = fax[id];
+      fb[fh_sk(i)] = -gx[id] * om;
+      al[fh_sk(i)] = alx[id];
+      pf[fh_sk(i)] = pfx[id];
+      pb[fh_sk(i)] = pbx[id];
+    }
+    if (threadIdx.x == 0) pb[fh_sk(0)] = pbx[base];
+  }
   __syncthreads();
-  for (int i = threadIdx.x; i <= N + 1; i += kXThreads) {
-    const double u = fa[fh_sk(i)];
-    Ch[base + i] = u;
-    if (i == 0 || i >= N) C[base + i] = u;
+  if (warp < nrows) {
+    double *fa = sbuf + (size_t)warp * 5 * L;
+    fh_line_solve_prefix(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, 0.0, g.C1, fa + L, fa);
+  }
+  __syncthreads();
+  for (int ln = 0; ln < nrows; ++ln) {
+    const double *u = sbuf + (size_t)ln * 5 * L;
+    const long long base = (long long)(line0 + ln) * ld;
+    for (int i = threadIdx.x; i <= N + 1; i += kXNThreads) {
+      const double v = u[fh_sk(i)];
+      Ch[base + i] = v;
+      if (i == 0 || i >= N) C[base + i] = v;
+    }
   }
 }
 
 // y half-step (fr_d_t_g_2d.cpp:2634-2648): four adjacent lines i per CTA so
 // that the strided column loads share 32-byte sectors; 128 threads stage each
-// line (kUnroll rows per thread in flight), one warp per line solves it.  Reads
-// the half-step field Ch and the full-step field C, writes the new full-step
-// field into C and appends the difference D_j = C^{j+1} - C^j.
+// line (kUnroll rows per thread in flight), warp w solves line w.  Reads the
+// half-step field Ch and the full-step field C, writes the new full-step field
+// into C and appends the difference D_j = C^{j+1} - C^j.
 __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C, const double *__restrict__ Ch,
                                                         double *__restrict__ Dj, const double *__restrict__ part,
                                                         long long ldp, int splits, const double *__restrict__ fay,
                                                         const double *__restrict__ gy,
                                                         const double *__restrict__ aly,
+                                                        const double *__restrict__ pfy,
+                                                        const double *__restrict__ pby,
                                                         const double *__restrict__ cw,
                                                         const float2 *__restrict__ far, int dfstore) {
   extern __shared__ double sbuf[];
@@ -242,9 +436,9 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
   constexpr int kRows = kYThreads / 4;
   const int line = i0 + col;
   const bool live = line < g.sN;
-  double *fa = sbuf + (size_t)col * 5 * L, *fb = fa + L, *al = fb + L, *bt = al + L, *cf = bt + L;
+  double *fa = sbuf + (size_t)col * 6 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L, *cf = pb + L;
   for (int r0 = 1; r0 < N; r0 += kRows * kUnroll) {
-    double ts[kUnroll], c[kUnroll], f[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll];
+    double ts[kUnroll], c[kUnroll], f[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
 #pragma unroll
     for (int e = 0; e < kUnroll; ++e) {
       const int q = r0 + rg + e * kRows;
@@ -254,6 +448,8 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
       a[e] = fay[id];
       gi[e] = gy[id];
       l[e] = aly[id];
+      qf[e] = pfy[id];
+      qb[e] = pby[id];
       ts[e] = 0.0;
       if (far) {
         const float2 fp = far[id];
@@ -278,14 +474,17 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
         fa[fh_sk(q)] = a[e];
         fb[fh_sk(q)] = -gi[e] * om;
         al[fh_sk(q)] = l[e];
+        pf[fh_sk(q)] = qf[e];
+        pb[fh_sk(q)] = qb[e];
         cf[fh_sk(q)] = f[e];
       }
     }
   }
+  if (live && rg == 0) pb[fh_sk(0)] = pby[line];  // node 0: lane 0's backward chunk
   __syncthreads();
   if (warp < 4 && i0 + warp < g.sN) {
-    double *wfa = sbuf + (size_t)warp * 5 * L;
-    fh_line_solve_staged(N, wfa, wfa + L, wfa + 2 * L, 1.0, 0.0, wfa + 3 * L, wfa);
+    double *wfa = sbuf + (size_t)warp * 6 * L;
+    fh_line_solve_prefix(N, wfa, wfa + L, wfa + 2 * L, wfa + 3 * L, wfa + 4 * L, 1.0, 0.0, wfa + L, wfa);
   }
   __syncthreads();
   if (live) {
@@ -314,11 +513,13 @@ static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
   k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(
-      g, 0, s->V2.as<double>(), cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>());
+      g, 0, s->V2.as<double>(), cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(),
+      s->pfx.as<double>(), s->pbx.as<double>());
   int rc = fh_after_launch(ctx, "k_tg_factor(x)");
   if (rc) return rc;
   k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(
-      g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>());
+      g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(),
+      s->pfy.as<double>(), s->pby.as<double>());
   return fh_after_launch(ctx, "k_tg_factor(y)");
 }
 
@@ -368,6 +569,30 @@ static int tg_one_step(fh_tg_solver *s) {
   const float2 *far = nullptr;
   if (blocked && s->j0 > 0) far = s->far.as<float2>() + 2LL * (j - s->j0) * s->ldfar;
   int splits = 0, kchunk = 0;
+  const bool fused = s->df && knear <= kNearMax && (knear >= 1 || far);
+  if (fused) {
+    // short double-float history (and the far pairs) inside the x sweep;
+    // profiled as a history-sum launch
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+    const size_t smn = sizeof(double) * ((size_t)kXLines * 5 * tg_line_stride(g.sN) + (size_t)kXLines * g.ld);
+    k_tg_xsweep_near<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXNThreads, smn, ctx->stream>>>(
+        g, s->C.as<double>(), s->Ch.as<double>(),
+        reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P, knear, Wj + kstart,
+        Wj + ldw + kstart, far, far ? far + s->ldfar : nullptr, s->part.as<double>(), s->fax.as<double>(),
+        s->gx.as<double>(), s->alx.as<double>(), s->pfx.as<double>(), s->pbx.as<double>(), cwj);
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+    if ((rc = fh_after_launch(ctx, "k_tg_xsweep_near"))) return rc;
+    fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+    const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
+    k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
+        g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (long long)j * g.P, s->part.as<double>(), 0,
+        1, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(), s->pby.as<double>(),
+        cwj, nullptr, 1);
+    fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+    if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
+    s->tstep++;
+    return FH_OK;
+  }
   if (knear >= 1) {
     fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
     if (s->df)
@@ -387,15 +612,16 @@ static int tg_one_step(fh_tg_solver *s) {
     fary = far + s->ldfar;
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-  const size_t smx = sizeof(double) * 4 * (size_t)tg_line_stride(g.sN);
-  k_tg_xsweep<<<(unsigned)(g.M - 1), kXThreads, smx, ctx->stream>>>(
+  const size_t smx = sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
+  k_tg_xsweep<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXThreads, smx, ctx->stream>>>(
       g, s->C.as<double>(), s->Ch.as<double>(), s->part.as<double>(), g.P, splits, s->fax.as<double>(),
-      s->gx.as<double>(), s->alx.as<double>(), cwj, farx);
+      s->gx.as<double>(), s->alx.as<double>(), s->pfx.as<double>(), s->pbx.as<double>(), cwj, farx);
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
-  const size_t smy = sizeof(double) * 4 * 5 * (size_t)tg_line_stride(g.M);
+  const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
   k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
       g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (long long)j * g.P, s->part.as<double>(), g.P,
-      splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), cwj, fary, s->df ? 1 : 0);
+      splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(),
+      s->pby.as<double>(), cwj, fary, s->df ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
   s->tstep++;
@@ -408,16 +634,21 @@ static int tg_one_step(fh_tg_solver *s) {
 // lower it below what an earlier, larger one launches with).
 static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   static std::mutex mu;
-  static int cur_x[64], cur_y[64];
-  const int smx = (int)(sizeof(double) * 4 * (size_t)tg_line_stride(sN));
-  const int smy = (int)(sizeof(double) * 4 * 5 * (size_t)tg_line_stride(M));
-  FH_REQUIRE(ctx, smx <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL,
-             "fh_tg_create: grid too large for the sweeps (sN, M <= 1200)");
+  static int cur_x[64], cur_y[64], cur_n[64];
+  const int smx = (int)(sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(sN));
+  const int smn = smx + (int)(sizeof(double) * kXLines * (size_t)(sN + 2));
+  const int smy = (int)(sizeof(double) * 4 * 6 * (size_t)tg_line_stride(M));
+  FH_REQUIRE(ctx, smn <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL,
+             "fh_tg_create: grid too large for the sweeps (sN <= 1170, M <= 970)");
   FH_REQUIRE(ctx, ctx->device >= 0 && ctx->device < 64, FH_EINVAL, "fh_tg_create: device index");
   std::lock_guard<std::mutex> lk(mu);
   if (smx > cur_x[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
     cur_x[ctx->device] = smx;
+  }
+  if (smn > cur_n[ctx->device]) {
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep_near, cudaFuncAttributeMaxDynamicSharedMemorySize, smn));
+    cur_n[ctx->device] = smn;
   }
   if (smy > cur_y[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
@@ -471,7 +702,9 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
   int rc;
   if ((rc = fh_alloc(ctx, s->C, fld)) || (rc = fh_alloc(ctx, s->Ch, fld)) || (rc = fh_alloc(ctx, s->V2, fld)) ||
       (rc = fh_alloc(ctx, s->alx, fld)) || (rc = fh_alloc(ctx, s->gx, fld)) || (rc = fh_alloc(ctx, s->fax, fld)) ||
-      (rc = fh_alloc(ctx, s->aly, fld)) || (rc = fh_alloc(ctx, s->gy, fld)) || (rc = fh_alloc(ctx, s->fay, fld)) ||
+      (rc = fh_alloc(ctx, s->pfx, fld)) || (rc = fh_alloc(ctx, s->pbx, fld)) || (rc = fh_alloc(ctx, s->aly, fld)) ||
+      (rc = fh_alloc(ctx, s->gy, fld)) || (rc = fh_alloc(ctx, s->fay, fld)) || (rc = fh_alloc(ctx, s->pfy, fld)) ||
+      (rc = fh_alloc(ctx, s->pby, fld)) ||
       (rc = fh_alloc(ctx, s->D, fld * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, s->W, sizeof(double) * 2 * (size_t)max_steps *
                                     (max_steps <= kWeightTableMaxSteps ? (size_t)max_steps : 1))) ||
