@@ -214,12 +214,11 @@ class TG2D(Workload):
         # algorithmic work per solve, by kernel class (interior points; per point-step:
         # 8 B per history layer read, the far pair and the two sums written)
         if blocked:
-            # the short double-float sums run fused with the x sweep (one launch per
-            # step): 8 B per layer and point, the far pairs (16 B), the y sum written
-            # (8 B) and the x sweep's own 48 B
+            # near part: the layers of the current 64-step block (double-float pairs,
+            # 8 B each), the far pairs read (16 B) and the two sums written (16 B)
             self.alg = {
-                "history": sum(8.0 * (j % 64) * pint + (16.0 if j >= 64 else 0.0) * pint + 56.0 * pint
-                               for j in range(1, S)),
+                "history": sum(8.0 * (j % 64) * pint + (32.0 if j >= 64 else 16.0) * pint
+                               for j in range(1, S) if j % 64),
                 # far contraction: FP64-equivalent flops 2*128*K*P per 64-step block; the
                 # tensor cores execute 10 bf16 slice products per FP64 product on Ppad columns
                 "gemm_flops": sum(2.0 * 128 * j0 * pint for j0 in range(64, S, 64)),
@@ -229,15 +228,14 @@ class TG2D(Workload):
         else:
             self.alg = {"history": sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))}
         # sweeps: x reads C, fa, g, al, one partial, writes Ch; y reads Ch, C, fa, g, al,
-        # one partial, writes C and the new history layer (blocked: y sweep only)
-        self.alg["sweep"] = (64.0 if blocked else 112.0) * pint * S
+        # one partial, writes C and the new history layer
+        self.alg["sweep"] = 112.0 * pint * S
         self.alg_hist_bytes = self.alg["history"]
         self.name = f"tg2d_adi_{G}x{G}_{S}steps"
         self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
                        "d": 0.1, "velocity_modes": 8, "mode": args.mode,
                        "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
-        self.kernel = {"blocked": "k_tg_xsweep_near (current block's double-float sums fused with the x sweep) + "
-                                  "k_far_gemm (tcgen05, exact bf16 slices)",
+        self.kernel = {"blocked": "k_hist_sum_df<2> (current block) + k_far_gemm (tcgen05, exact bf16 slices)",
                        "df64": "k_hist_sum_df<2>"}.get(args.mode, "k_hist_sum<2>")
 
     def solve_device(self):

@@ -8,20 +8,21 @@
 // has a power-of-two scale per weight row (2^Ew[m][c]) and per point
 // (2^Ed[c][p]); scaled values have |y| < 128 and are cut into four integer
 // slices y = a0 + a1/2^8 + a2/2^16 + a3/2^24 with |a_i| <= 128, which bf16
-// holds exactly.  Products a_i*b_j are exact in FP32 and so are the per-chunk
-// sums of each level l = i + j <= 3 (|sum| <= 4*64*2^14 = 2^22): the
-// tensor-core accumulation cannot round or truncate.  Per chunk the epilogue
-// combines the four level sums exactly (double-float with one
-// renormalisation), scales by 2^(Ew+Ed) and adds into a double-float running
-// sum.  The only approximation is the slicing (~2^-32 of the chunk maxima,
-// round to nearest, unbiased); the near layers of the block are summed
-// separately in double-float.
+// holds exactly.  Products a_i*b_j are exact in FP32 and so are the sums of
+// each level l = i + j <= 3 over a group of two chunks (|sum| <= 4*128*2^14 =
+// 2^23; both chunks of a group share their exponents): the tensor-core
+// accumulation cannot round or truncate.  Per group the epilogue combines the
+// four level sums exactly (double-float with one renormalisation), scales by
+// 2^(Ew+Ed) and adds into a double-float running sum.  The only approximation is the slicing (~2^-32 of the chunk maxima,
+// round to nearest, unbiased) relative to the group maxima; the near layers of
+// the block are summed separately in double-float.
 //
 // Data layout: K-major planes (point p holds its layers contiguously; one
 // 64-layer chunk = one 128-byte swizzle row), loaded by TMA with 128-byte
 // swizzle; exponents as int8 tables Ed[c][Ppad], Ew[c][128].
 //
-// CTA (320 threads, one per SM): warp 0 issues TMA loads into a 2-stage ring
+// Persistent CTAs (320 threads, one per SM, looping over 64-point tiles): warp
+// 0 issues TMA loads into a 2-stage ring
 // (96 KiB per stage: 4 weight tiles 128x64 + 4 history tiles 64x64 bf16), warp
 // 1 owns TMEM (512 columns; 2 buffers x 4 levels x 64 columns) and issues the
 // MMAs from one thread, warps 2-9 run the epilogue (two warps per TMEM lane
@@ -52,6 +53,9 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
 }  // namespace
+
+// Chunk groups (pairs of 64-layer chunks, see fh_slice_row_group).
+__host__ __device__ inline int fh_ngroups(int nchunks) { return (nchunks + 1) / 2; }
 
 // x = 2^E (a0 + a1/2^8 + a2/2^16 + a3/2^24) with integer |a_i| <= 128 given |x| < 2^(E+7).
 __device__ __forceinline__ void fh_slice4(double x, int E, __nv_bfloat16 (&b)[kSlices]) {
@@ -98,8 +102,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int *sh_err = reinterpret_cast<volatile int *>(gbars + 8 * (2 * kStages + 6));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long p0 = (long long)blockIdx.x * kBN;
   const int nchunks = K / kBK;
+  // persistent: this CTA owns tiles blockIdx.x, blockIdx.x + gridDim.x, ...;
+  // the stage ring and the accumulator buffers run on one chunk counter g
+  // across its tiles, so loads of the next tile overlap the current epilogue
+  const int ntiles = (int)(Ppad / kBN);
+  const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int total = my_tiles * nchunks;
+  const int ngroups = fh_ngroups(nchunks);  // accumulator buffers cycle per chunk group
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -128,9 +138,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int last_issued[kStages];
       for (int s = 0; s < kStages; ++s) last_issued[s] = -1;
-      for (int c = 0; c < nchunks; ++c) {
-        const int s = c % kStages;
-        if (c >= kStages && !fh_mbar_wait(empty(s), ((c / kStages) - 1) & 1)) {
+      for (int g = 0; g < total; ++g) {
+        const int tile = (int)blockIdx.x + (g / nchunks) * (int)gridDim.x;
+        const int c = g % nchunks;
+        const int s = g % kStages;
+        if (g >= kStages && !fh_mbar_wait(empty(s), ((g / kStages) - 1) & 1)) {
           ok = false;
           break;
         }
@@ -138,8 +150,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t sb = base + s * kStageBytes;
         for (int pl = 0; pl < kSlices; ++pl) fh_tma_load_3d(sb + pl * kTileA, &tmA, c * kBK, 0, pl, full(s));
         for (int pl = 0; pl < kSlices; ++pl)
-          fh_tma_load_3d(sb + kSlices * kTileA + pl * kTileB, &tmB, c * kBK, (int)p0, pl, full(s));
-        last_issued[s] = c;
+          fh_tma_load_3d(sb + kSlices * kTileA + pl * kTileB, &tmB, c * kBK, tile * kBN, pl, full(s));
+        last_issued[s] = g;
       }
       if (!ok) {
         *sh_err = 1;
@@ -150,35 +162,42 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = fh_idesc_bf16_f32(kBM, kBN);
-      for (int c = 0; c < nchunks; ++c) {
-        const int s = c % kStages, b = c & 1;
-        if (c >= 2 && !fh_mbar_wait(accempty(b), ((c >> 1) - 1) & 1)) {
+      int gc = 0;  // chunk counter (stage ring)
+      for (int gg = 0; gg < my_tiles * ngroups && ok; ++gg) {
+        const int G = gg % ngroups;
+        const int nc = min(2, nchunks - 2 * G);
+        const int b = gg & 1;
+        if (gg >= 2 && !fh_mbar_wait(accempty(b), ((gg >> 1) - 1) & 1)) {
           ok = false;
           break;
         }
-        if (!fh_mbar_wait(full(s), (c / kStages) & 1)) {
-          ok = false;
-          break;
-        }
-        fh_tc_fence_after();
-        const uint32_t sb = base + s * kStageBytes;
         const uint32_t lv0 = tmem + (uint32_t)(b * kLevels * kBN);
         uint32_t first[kLevels] = {0, 0, 0, 0};
-#pragma unroll
-        for (int kk = 0; kk < kBK / 16; ++kk) {
-          // level l = i + j collects the slice products a_i b_j (exact integers)
-          const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-          const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
-#pragma unroll
-          for (int q = 0; q < 10; ++q) {
-            const int l = ia[q] + ib[q];
-            const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileA + kk * 32);
-            const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileA + ib[q] * kTileB + kk * 32);
-            fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
-            first[l] = 1;
+        for (int cc = 0; cc < nc; ++cc, ++gc) {
+          const int s = gc % kStages;
+          if (!fh_mbar_wait(full(s), (gc / kStages) & 1)) {
+            ok = false;
+            break;
           }
+          fh_tc_fence_after();
+          const uint32_t sb = base + s * kStageBytes;
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; ++kk) {
+            // level l = i + j collects the slice products a_i b_j (exact integers)
+            const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+            const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+#pragma unroll
+            for (int q = 0; q < 10; ++q) {
+              const int l = ia[q] + ib[q];
+              const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileA + kk * 32);
+              const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileA + ib[q] * kTileB + kk * 32);
+              fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
+              first[l] = 1;
+            }
+          }
+          fh_mma_commit(empty(s));
         }
-        fh_mma_commit(empty(s));
+        if (!ok) break;
         fh_mma_commit(accfull(b));
       }
       fh_mma_commit(mmadone);
@@ -193,73 +212,70 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lanebase = (uint32_t)(32 * q) << 16;
     const int m = 32 * q + lane;
     const int col0 = 32 * half;
-    float HI[32], LO[32];
+    for (int tt = 0; tt < my_tiles && ok; ++tt) {
+      const long long p0 = (long long)((int)blockIdx.x + tt * (int)gridDim.x) * kBN;
+      float HI[32], LO[32];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) HI[i] = LO[i] = 0.f;
-    for (int c = 0; c < nchunks; ++c) {
-      const int b = c & 1;
-      if (!__all_sync(0xffffffffu, fh_mbar_wait(accfull(b), (c >> 1) & 1))) {
-        ok = false;
-        break;
-      }
-      fh_tc_fence_after();
-      const int ew = (int)Ew[(long long)c * kBM + m];
-      const int8_t *edc = Ed + (long long)c * Ppad + p0 + col0;
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        float L0[16], L1[16], L2[16], L3[16];
-        const uint32_t cb = tmem + lanebase + (uint32_t)(b * kLevels * kBN + col0 + 16 * t);
-        fh_tmem_ld16(cb, L0);
-        fh_tmem_ld16(cb + kBN, L1);
-        fh_tmem_ld16(cb + 2 * kBN, L2);
-        fh_tmem_ld16(cb + 3 * kBN, L3);
-        fh_tmem_wait_ld();
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          // T = L0 + L1/2^8 + L2/2^16 + L3/2^24 exactly as (th, tl):
-          // TwoSum of the first two levels, L2 joins the error term exactly,
-          // a fast two-sum renormalises, then L3 joins exactly.
-          const float x1 = L1[i] * 0.00390625f;
-          float th = L0[i] + x1;
-          const float bb = th - L0[i];
-          float tl = (L0[i] - (th - bb)) + (x1 - bb);
-          tl += L2[i] * 1.52587890625e-05f;
-          const float tr = th + tl;
-          tl = tl - (tr - th);
-          th = tr;
-          tl += L3[i] * 5.9604644775390625e-08f;
-          const float sc = fh_exp2i(ew + (int)edc[16 * t + i]);
-          const float vh = th * sc, vl = tl * sc;
-          // (HI, LO) += (vh, vl)
-          const int k = 16 * t + i;
-          const float s = HI[k] + vh;
-          const float bs = s - HI[k];
-          const float e = (HI[k] - (s - bs)) + (vh - bs);
-          HI[k] = s;
-          LO[k] += e + vl;
+      for (int i = 0; i < 32; ++i) HI[i] = LO[i] = 0.f;
+      for (int G = 0; G < ngroups; ++G) {
+        const int gg = tt * ngroups + G;
+        const int b = gg & 1;
+        // exponents of this group (loaded before the wait: they do not depend on it)
+        const int ew = (int)Ew[(long long)(2 * G) * kBM + m];
+        const uint4 *edv = reinterpret_cast<const uint4 *>(Ed + (long long)(2 * G) * Ppad + p0 + col0);
+        const uint4 ev0 = __ldg(edv), ev1 = __ldg(edv + 1);
+        const uint32_t ew32[8] = {ev0.x, ev0.y, ev0.z, ev0.w, ev1.x, ev1.y, ev1.z, ev1.w};
+        if (!__all_sync(0xffffffffu, fh_mbar_wait(accfull(b), (gg >> 1) & 1))) {
+          ok = false;
+          break;
         }
-      }
-      fh_tc_fence_before();
-      fh_mbar_arrive(accempty(b));
-    }
-    // every MMA has completed (the last accfull), so the stage ring is free:
-    // stage the 128 x 64 tile of (hi, lo) pairs and store it row by row
-    float2 *tile = reinterpret_cast<float2 *>(gbase);
-    constexpr int kPitch = kBN + 1;  // pairs per staged row: 130 words, lanes hit distinct banks
-    if (ok) {
+        fh_tc_fence_after();
 #pragma unroll
-      for (int k = 0; k < 32; ++k) tile[m * kPitch + col0 + k] = make_float2(HI[k], LO[k]);
+        for (int t = 0; t < 2; ++t) {
+          float L0[16], L1[16], L2[16], L3[16];
+          const uint32_t cb = tmem + lanebase + (uint32_t)(b * kLevels * kBN + col0 + 16 * t);
+          fh_tmem_ld16(cb, L0);
+          fh_tmem_ld16(cb + kBN, L1);
+          fh_tmem_ld16(cb + 2 * kBN, L2);
+          fh_tmem_ld16(cb + 3 * kBN, L3);
+          fh_tmem_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            // T = L0 + L1/2^8 + L2/2^16 + L3/2^24 (|L_l| <= 2^23) exactly as (th, tl):
+            // TwoSum of the first two levels, L2 joins the error term exactly,
+            // a fast two-sum renormalises, then L3 joins exactly.
+            const float x1 = L1[i] * 0.00390625f;
+            float th = L0[i] + x1;
+            const float bb = th - L0[i];
+            float tl = (L0[i] - (th - bb)) + (x1 - bb);
+            tl += L2[i] * 1.52587890625e-05f;
+            const float tr = th + tl;
+            tl = tl - (tr - th);
+            th = tr;
+            tl += L3[i] * 5.9604644775390625e-08f;
+            const int kk = 16 * t + i;
+            const float sc = fh_exp2i(ew + (int)(int8_t)(ew32[kk >> 2] >> (8 * (kk & 3))));
+            const float vh = th * sc, vl = tl * sc;
+            // (HI, LO) += (vh, vl)
+            const int k = 16 * t + i;
+            const float s2 = HI[k] + vh;
+            const float bs = s2 - HI[k];
+            const float e = (HI[k] - (s2 - bs)) + (vh - bs);
+            HI[k] = s2;
+            LO[k] += e + vl;
+          }
+        }
+        fh_tc_fence_before();
+        fh_mbar_arrive(accempty(b));
+      }
+      if (ok && nchunks > 0) {
+        // row m, 32 consecutive points: (hi, lo) pairs as 16-byte stores
+        float4 *o = reinterpret_cast<float4 *>(out + (long long)m * ldo + p0 + col0);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) o[k] = make_float4(HI[2 * k], LO[2 * k], HI[2 * k + 1], LO[2 * k + 1]);
+      }
     }
     if (!ok) *sh_err = 1;
-    fh_named_barrier(1, 32 * kEpiWarps);
-    if (!*sh_err && nchunks > 0) {
-      const int et = threadIdx.x - 64;  // 0..255
-      for (int r = et >> 5; r < kBM; r += kEpiWarps) {
-        float2 *o = out + (long long)r * ldo + p0;
-        for (int cc = lane; cc < kBN; cc += 32)
-          if (p0 + cc < P) o[cc] = tile[r * kPitch + cc];
-      }
-    }
   }
   fh_tc_fence_before();
   __syncthreads();
@@ -268,35 +284,36 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 1) fh_tmem_dealloc(tmem, kTmemCols);
 }
 
-// Weight planes of a TG block: row m = 2r + {0: x, 1: y} of step j0 + r,
-// A3[s][m][k] (K-major) and Ew[c][m]; one warp per (row, 64-layer chunk).
-__global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, double alpha, double beta,
-                              __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
-  const int c = blockIdx.x;
-  const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// Chunk groups: group G covers the 64-layer chunks 2G and 2G+1 (the last group
+// holds one chunk when the chunk count is odd).  All chunks of a group share
+// the row exponent Ew and the history exponent Ed, so the tensor cores can
+// accumulate a whole group (128 layers: level sums <= 4*128*2^14 = 2^23, still
+// exact in FP32) before the epilogue combines it.
+
+// One warp slices row m of group G: val(k) is the weight of layer k.
+template <class Val>
+__device__ __forceinline__ void fh_slice_row_group(const Val &val, int G, int nchunks, int m, int Kcap,
+                                                   __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
   const int lane = threadIdx.x & 31;
-  if (m >= kBM) return;
-  const double X = (double)(j0 + (m >> 1)) + ((m & 1) ? 1.0 : 0.5);
-  double w[2];
+  const int c0 = 2 * G, nc = min(2, nchunks - c0);
+  double w[4];
   double mx = 0.0;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int k = c * kBK + lane + 32 * h;
-    w[h] = 0.0;
-    if (k < K) {
-      const double s0 = (double)k + 0.0;
-      w[h] = Da * fh_psi_int(s0, s0 + 1.0, X, tau, alpha, beta);
-    }
+  for (int h = 0; h < 4; ++h) {
+    const int k = c0 * kBK + lane + 32 * h;
+    w[h] = h < 2 * nc ? val(k) : 0.0;
     mx = fmax(mx, fabs(w[h]));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   const int E = fh_chunk_exp(mx);
-  if (lane == 0) Ew[(long long)c * kBM + m] = (int8_t)E;
+  if (lane == 0)
+    for (int c = c0; c < c0 + nc; ++c) Ew[(long long)c * kBM + m] = (int8_t)E;
   const long long plane = (long long)kBM * Kcap;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int k = c * kBK + lane + 32 * h;
+  for (int h = 0; h < 4; ++h) {
+    if (h >= 2 * nc) break;
+    const int k = c0 * kBK + lane + 32 * h;
     __nv_bfloat16 bs[kSlices];
     fh_slice4(w[h], E, bs);
     const long long o = (long long)m * Kcap + k;
@@ -305,36 +322,25 @@ __global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, do
   }
 }
 
+// Weight planes of a TG block: row m = 2r + {0: x, 1: y} of step j0 + r,
+// A3[s][m][k] (K-major) and Ew[c][m]; one warp per (row, chunk group).
+__global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, double alpha, double beta,
+                              __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
+  const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= kBM) return;
+  const double X = (double)(j0 + (m >> 1)) + ((m & 1) ? 1.0 : 0.5);
+  auto val = [&](int k) { return k < K ? Da * fh_psi_int((double)k + 0.0, (double)k + 1.0, X, tau, alpha, beta) : 0.0; };
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
+}
+
 // Weight rows W[m*ldw + k], k < K, rows m >= mrows are zero (standalone
 // contraction, or a block of the per-solve weight table).
 __global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, int K, int Kcap, int mrows,
                                  __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
-  const int c = blockIdx.x;
   const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
   if (m >= kBM) return;
-  double w[2];
-  double mx = 0.0;
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int k = c * kBK + lane + 32 * h;
-    w[h] = (k < K && m < mrows) ? W[(long long)m * ldw + k] : 0.0;
-    mx = fmax(mx, fabs(w[h]));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int E = fh_chunk_exp(mx);
-  if (lane == 0) Ew[(long long)c * kBM + m] = (int8_t)E;
-  const long long plane = (long long)kBM * Kcap;
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int k = c * kBK + lane + 32 * h;
-    __nv_bfloat16 bs[kSlices];
-    fh_slice4(w[h], E, bs);
-    const long long o = (long long)m * Kcap + k;
-#pragma unroll
-    for (int i = 0; i < kSlices; ++i) A3[i * plane + o] = bs[i];
-  }
+  auto val = [&](int k) { return (k < K && m < mrows) ? W[(long long)m * ldw + k] : 0.0; };
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
 }
 
 // Slices of a double-float value (hi, lo) scaled by 2^-E, |hi + lo| < 2^(E+7):
@@ -365,23 +371,43 @@ __device__ __forceinline__ float fh_exp2f_int(int e) { return __int_as_float((e 
 // tile of each plane staged in shared memory (pitch 66: conflict-free) and
 // written as full 128-byte rows.  Chunks whose maximum is below 2^-100 are
 // scaled as if it were 2^-100 (their slices carry the value to 2^-132).
+// Per-point exponent E (frexp exponent q of the largest |value|, floored at
+// -100; E = q - 7) of a double-float chunk group.
+__device__ __forceinline__ int fh_point_exp(float mx) {
+  int q = -100;
+  if (mx >= 7.888609052210118e-31f) q = ((__float_as_int(mx) >> 23) & 0xff) - 126;  // 2^-100
+  return q - 7;
+}
+
+// Layers [kg0, kg0 + 64 NCH) of the double-float history (layer-major (hi, lo)
+// pairs, pitch ldd, P valid points), NCH = 1 or 2 chunks of one group, into
+// the K-major planes H3[s][p][k] and the per-point exponents Ed[c][p] (the same
+// for both chunks of a group).  64 points per CTA, 4 threads per point (16 NCH
+// layers each): coalesced pair loads, FP32 slicing in registers, the 64 x 64
+// bf16 tile of each plane and chunk staged in shared memory (pitch 66:
+// conflict-free) and written as full 128-byte rows.  Points whose maximum is
+// below 2^-100 are scaled as if it were 2^-100 (their slices carry the value
+// to 2^-132).
 constexpr int kCvPts = 64;
+constexpr int kCvPitch = kBK + 2;  // bf16 per staged row
+constexpr size_t kCvSmemPerChunk = sizeof(__nv_bfloat16) * kSlices * kCvPts * kCvPitch;
+template <int NCH>
 __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict__ D, long long ldd, long long P,
-                                                        long long Ppad, int k0, int Kcap,
+                                                        long long Ppad, int kg0, int Kcap,
                                                         __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
-  constexpr int kPitch = kBK + 2;  // bf16 per staged row
-  __shared__ __align__(16) __nv_bfloat16 out[kSlices][kCvPts * kPitch];
+  extern __shared__ __align__(16) __nv_bfloat16 cvout[];  // [NCH][kSlices][kCvPts * kCvPitch]
   __shared__ float qmax[4][kCvPts];
+  constexpr int kL = 16 * NCH;  // layers per thread
   const long long p0 = (long long)blockIdx.x * kCvPts;
   const int pt = threadIdx.x & (kCvPts - 1);
-  const int qh = threadIdx.x >> 6;  // layers qh*16 .. qh*16+15
+  const int qh = threadIdx.x >> 6;  // layers qh*kL .. qh*kL + kL - 1 of the group
   const long long p = p0 + pt;
-  float hi[16], lo[16];
+  float hi[kL], lo[kL];
   float mx = 0.f;
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
+  for (int i = 0; i < kL; ++i) {
     float2 v = make_float2(0.f, 0.f);
-    if (p < P) v = __ldcs(D + (long long)(k0 + qh * 16 + i) * ldd + p);
+    if (p < P) v = __ldcs(D + (long long)(kg0 + qh * kL + i) * ldd + p);
     hi[i] = v.x;
     lo[i] = v.y;
     mx = fmaxf(mx, fabsf(v.x));
@@ -389,84 +415,78 @@ __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict
   qmax[qh][pt] = mx;
   __syncthreads();
   mx = fmaxf(fmaxf(qmax[0][pt], qmax[1][pt]), fmaxf(qmax[2][pt], qmax[3][pt]));
-  // frexp exponent q of mx (mx < 2^q), floored at -100; E = q - 7
-  int q = -100;
-  if (mx >= 7.888609052210118e-31f) q = ((__float_as_int(mx) >> 23) & 0xff) - 126;  // 2^-100
-  const int E = q - 7;
-  if (qh == 0 && p < Ppad) Ed[(long long)(k0 / kBK) * Ppad + p] = (int8_t)E;
+  const int E = fh_point_exp(mx);
+  if (qh < NCH && p < Ppad) Ed[(long long)(kg0 / kBK + qh) * Ppad + p] = (int8_t)E;
   const float scale = fh_exp2f_int(-E);  // -E <= 107
 #pragma unroll
-  for (int i = 0; i < 16; i += 2) {
+  for (int i = 0; i < kL; i += 2) {
     __nv_bfloat16 s0[kSlices], s1[kSlices];
     fh_slice4_pair(hi[i], lo[i], scale, s0);
     fh_slice4_pair(hi[i + 1], lo[i + 1], scale, s1);
+    const int l = qh * kL + i;  // layer within the group
+    const int ch = l / kBK, kk = l % kBK;
 #pragma unroll
     for (int c = 0; c < kSlices; ++c) {
       __nv_bfloat162 w;
       w.x = s0[c];
       w.y = s1[c];
-      *reinterpret_cast<__nv_bfloat162 *>(&out[c][pt * kPitch + qh * 16 + i]) = w;
+      *reinterpret_cast<__nv_bfloat162 *>(
+          &cvout[((size_t)ch * kSlices + c) * kCvPts * kCvPitch + pt * kCvPitch + kk]) = w;
     }
   }
   __syncthreads();
-  // rows of 64 layers (128 B) per point and plane; a warp writes 4 rows per pass
+  // rows of 64 layers (128 B) per point, plane and chunk; a warp writes 4 rows per pass
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long plane = Ppad * (long long)Kcap;
-  for (int r = warp * 4 + (lane >> 3); r < kSlices * kCvPts; r += 8 * 4) {
-    const int c = r / kCvPts, row = r - c * kCvPts;
+  for (int r = warp * 4 + (lane >> 3); r < NCH * kSlices * kCvPts; r += 8 * 4) {
+    const int chc = r / kCvPts, row = r - chc * kCvPts;  // chc = chunk * kSlices + plane
+    const int ch = chc / kSlices, c = chc - ch * kSlices;
     const long long pr = p0 + row;
     if (pr >= Ppad) continue;
-    const uint32_t *src = reinterpret_cast<const uint32_t *>(&out[c][row * kPitch + (lane & 7) * 8]);
+    const uint32_t *src =
+        reinterpret_cast<const uint32_t *>(&cvout[(size_t)chc * kCvPts * kCvPitch + row * kCvPitch + (lane & 7) * 8]);
     uint4 v;
     v.x = src[0];
     v.y = src[1];
     v.z = src[2];
     v.w = src[3];
-    reinterpret_cast<uint4 *>(H3 + c * plane + pr * Kcap + k0)[lane & 7] = v;
+    reinterpret_cast<uint4 *>(H3 + c * plane + pr * Kcap + kg0 + ch * kBK)[lane & 7] = v;
   }
 }
 
-// Layers [k0, k0+64) of D (layer-major FP64, pitch ldd, P valid points) into
-// the K-major planes H3[s][p][k] and the exponents Ed[k0/64][p].  One thread
-// per point, the 64 values pass through a 64 KiB shared tile.
-__global__ void __launch_bounds__(128) k_blk_convert(const double *__restrict__ D, long long ldd, long long P,
-                                                     long long Ppad, int k0, int Kcap, int df,
-                                                     __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
-  extern __shared__ double tile[];  // [64][128]
-  const long long pb = (long long)blockIdx.x * 128;
+// FP64 history (standalone contraction): layers [kg0, kg0 + 64 nch) of D
+// (layer-major, pitch ldd) into the planes and per-point exponents, one thread
+// per point (64 points per CTA), the values through a shared tile.
+__global__ void __launch_bounds__(64) k_blk_convert(const double *__restrict__ D, long long ldd, long long P,
+                                                    long long Ppad, int kg0, int nch, int Kcap,
+                                                    __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
+  extern __shared__ double tile[];  // [64 nch][64]
   const int t = threadIdx.x;
-  const long long p = pb + t;
+  const long long p = (long long)blockIdx.x * 64 + t;
+  const int nl = kBK * nch;
   double mx = 0.0;
-  for (int k = 0; k < kBK; ++k) {
-    double v = 0.0;
-    if (p < P) {
-      if (df) {  // (hi, lo) FP32 pair storage
-        const float2 hl = __ldcs(reinterpret_cast<const float2 *>(D) + (long long)(k0 + k) * ldd + p);
-        v = (double)hl.x + (double)hl.y;
-      } else {
-        v = __ldcs(D + (long long)(k0 + k) * ldd + p);
-      }
-    }
-    tile[k * 128 + t] = v;
+  for (int k = 0; k < nl; ++k) {
+    const double v = p < P ? __ldcs(D + (long long)(kg0 + k) * ldd + p) : 0.0;
+    tile[k * 64 + t] = v;
     mx = fmax(mx, fabs(v));
   }
   const int E = fh_chunk_exp(mx);
-  if (p < Ppad) Ed[(long long)(k0 / kBK) * Ppad + p] = (int8_t)E;
-  const long long plane = Ppad * (long long)Kcap;
   if (p >= Ppad) return;
+  for (int c = 0; c < nch; ++c) Ed[(long long)(kg0 / kBK + c) * Ppad + p] = (int8_t)E;
+  const long long plane = Ppad * (long long)Kcap;
 #pragma unroll 1
-  for (int v = 0; v < kBK / 8; ++v) {
+  for (int v = 0; v < nl / 8; ++v) {
     __align__(16) __nv_bfloat16 c[kSlices][8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       __nv_bfloat16 bs[kSlices];
-      fh_slice4(tile[(v * 8 + i) * 128 + t], E, bs);
+      fh_slice4(tile[(v * 8 + i) * 64 + t], E, bs);
 #pragma unroll
       for (int q = 0; q < kSlices; ++q) c[q][i] = bs[q];
     }
 #pragma unroll
     for (int q = 0; q < kSlices; ++q)
-      reinterpret_cast<uint4 *>(H3 + q * plane + p * Kcap + k0)[v] = *reinterpret_cast<const uint4 *>(c[q]);
+      reinterpret_cast<uint4 *>(H3 + q * plane + p * Kcap + kg0)[v] = *reinterpret_cast<const uint4 *>(c[q]);
   }
 }
 
@@ -505,6 +525,7 @@ static int make_map(fh_ctx *ctx, CUtensorMap *map, void *base, unsigned long lon
 struct fh_blk {
   long long P = 0, Ppad = 0;
   int Kcap = 0;
+  int nsm = 1;  // SMs of the device: one persistent CTA each
   fh_dbuf H3, A3, Ed, Ew, err;
   CUtensorMap mapA, mapB;
 };
@@ -518,6 +539,7 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
   b.P = P;
   b.Ppad = fh_ceil_div(P, 128) * 128;
   b.Kcap = Kcap;
+  FH_CUDA_TRY(ctx, cudaDeviceGetAttribute(&b.nsm, cudaDevAttrMultiProcessorCount, ctx->device));
   int rc;
   if ((rc = fh_alloc(ctx, b.H3, sizeof(__nv_bfloat16) * kSlices * (size_t)b.Ppad * Kcap)) ||
       (rc = fh_alloc(ctx, b.A3, sizeof(__nv_bfloat16) * kSlices * (size_t)kBM * Kcap)) ||
@@ -530,23 +552,35 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
   if (!attr) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_far_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(sizeof(double) * kBK * 128)));
+                                          (int)(sizeof(double) * 2 * kBK * 64)));
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(2 * kCvSmemPerChunk)));
     attr = true;
   }
   return FH_OK;
 }
 
-// Converts layers [k0, k0+64) of the FP64 history into the planes and exponents.
+// Converts layers [k0, k0+64) of the history (FP64, or (hi, lo) pairs when df)
+// into the planes and exponents; chunks must be converted in order.  An odd
+// chunk completes the group (k0 - 64, k0): both chunks are (re)converted with
+// the group's per-point exponents.
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df) {
   FH_REQUIRE(ctx, k0 % kBK == 0 && k0 + kBK <= b.Kcap, FH_EINVAL, "blocked contraction: bad layer block %d", k0);
+  const int c = k0 / kBK;
+  const int kg0 = (c & 1) ? k0 - kBK : k0;
+  const int nch = (c & 1) ? 2 : 1;
   if (df) {
-    k_blk_convert_df<<<(unsigned)(b.Ppad / kCvPts), 256, 0, ctx->stream>>>(
-        reinterpret_cast<const float2 *>(D), ldd, b.P, b.Ppad, k0, b.Kcap, b.H3.as<__nv_bfloat16>(),
-        b.Ed.as<int8_t>());
+    const float2 *Dp = reinterpret_cast<const float2 *>(D);
+    if (nch == 2)
+      k_blk_convert_df<2><<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
+          Dp, ldd, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+    else
+      k_blk_convert_df<1><<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
+          Dp, ldd, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
     return fh_after_launch(ctx, "k_blk_convert_df");
   }
-  k_blk_convert<<<(unsigned)(b.Ppad / 128), 128, sizeof(double) * kBK * 128, ctx->stream>>>(
-      D, ldd, b.P, b.Ppad, k0, b.Kcap, df, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+  k_blk_convert<<<(unsigned)(b.Ppad / 64), 64, sizeof(double) * nch * kBK * 64, ctx->stream>>>(
+      D, ldd, b.P, b.Ppad, kg0, nch, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_convert");
 }
 
@@ -555,7 +589,7 @@ int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k
 // ldw, nsteps steps) the rows are taken from it instead of being recomputed.
 int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta,
                       const double *table, int ldw, int nsteps) {
-  dim3 g((unsigned)(j0 / kBK), kBM / 8);
+  dim3 g((unsigned)fh_ngroups(j0 / kBK), kBM / 8);
   if (table) {
     const int mrows = 2 * (nsteps - j0) < kBM ? 2 * (nsteps - j0) : kBM;
     k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(table + (long long)j0 * 2 * ldw, ldw, j0, b.Kcap, mrows,
@@ -571,7 +605,8 @@ int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, dou
 int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo) {
   FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
   fh_prof_mark(ctx, FH_PROF_GEMM, false);
-  k_far_gemm<<<(unsigned)(b.Ppad / kBN), kThreads, kSmemBytes, ctx->stream>>>(
+  const long long ntiles = b.Ppad / kBN;
+  k_far_gemm<<<(unsigned)(ntiles < b.nsm ? ntiles : b.nsm), kThreads, kSmemBytes, ctx->stream>>>(
       b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, b.err.as<int>());
   fh_prof_mark(ctx, FH_PROF_GEMM, true);
   return fh_after_launch(ctx, "k_far_gemm");
@@ -603,7 +638,7 @@ extern "C" int fh_history_contract_bf16(fh_ctx *ctx, int K, long long P, const d
   fh_blk b;
   int rc = fh_blk_init(ctx, b, P, K);
   if (rc) return rc;
-  dim3 g((unsigned)(K / kBK), kBM / 8);
+  dim3 g((unsigned)fh_ngroups(K / kBK), kBM / 8);
   k_blk_split_rows<<<g, 256, 0, ctx->stream>>>(W, ldw, K, K, kBM, b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
   if ((rc = fh_after_launch(ctx, "k_blk_split_rows"))) return rc;
   for (int k0 = 0; k0 < K; k0 += kBK)

@@ -122,20 +122,20 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
     sl += e + pl;
   };
   int k = 0;
-  for (; k + 4 <= nk; k += 4) {  // four layers (64 B per thread) in flight
-    float4 v[4];
+  for (; k + 8 <= nk; k += 8) {  // eight layers (128 B per thread) in flight
+    float4 v[8];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = __ldcs(d + u * ld4);
-    d += 4 * ld4;
+    for (int u = 0; u < 8; ++u) v[u] = __ldcs(d + u * ld4);
+    d += 8 * ld4;
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
       for (int m = 0; m < M; ++m) {
         const float2 w = wsf[m * kchunk + k + u];
         acc(w, v[u].x, v[u].y, ah[m][0], al[m][0]);
         acc(w, v[u].z, v[u].w, ah[m][1], al[m][1]);
       }
-    if ((k & 15) == 12) {
+    if ((k & 15) == 8) {
 #pragma unroll
       for (int m = 0; m < M; ++m)
 #pragma unroll

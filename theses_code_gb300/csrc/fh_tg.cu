@@ -265,152 +265,6 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
   }
 }
 
-// x half-step fused with the short history sum of the double-float modes
-// (layers [kstart, j) with j - kstart <= 64, plus the far-history pairs of the
-// blocked mode).  The CTA's four x lines are one contiguous range of 4 (sN+2)
-// points; phase A streams their history layers once and accumulates both the
-// x and the y sums in double-float (the y sums go to Sy for the y sweep), then
-// the x sweep proceeds as in k_tg_xsweep with the x sums from shared memory.
-static constexpr int kXNThreads = 512;
-static constexpr int kNearMax = 64;
-__global__ void __launch_bounds__(kXNThreads) k_tg_xsweep_near(
-    fh_tg_dev g, double *C, double *__restrict__ Ch, const float2 *__restrict__ D, int knear,
-    const double *__restrict__ Wx, const double *__restrict__ Wy, const float2 *__restrict__ farx,
-    const float2 *__restrict__ fary, double *__restrict__ Sy, const double *__restrict__ fax,
-    const double *__restrict__ gx, const double *__restrict__ alx, const double *__restrict__ pfx,
-    const double *__restrict__ pbx, const double *__restrict__ cw) {
-  extern __shared__ double sbuf[];
-  __shared__ float2 wsx[kNearMax], wsy[kNearMax];
-  const int warp = threadIdx.x >> 5;
-  const int line0 = 1 + blockIdx.x * kXLines;
-  const int N = g.sN;
-  const int L = tg_line_stride(N);
-  const int ld = g.ld;
-  double *Sx = sbuf + (size_t)kXLines * 5 * L;  // [4][ld]
-  if (threadIdx.x < knear) {
-    const double a = Wx[threadIdx.x], b = Wy[threadIdx.x];
-    const float ah = __double2float_rn(a), bh = __double2float_rn(b);
-    wsx[threadIdx.x] = make_float2(ah, __double2float_rn(a - (double)ah));
-    wsy[threadIdx.x] = make_float2(bh, __double2float_rn(b - (double)bh));
-  }
-  __syncthreads();
-  // ---- phase A: double-float history sums of the 4 rows (4 points per thread in flight)
-  const int nrows = min(kXLines, g.M - line0);
-  const int npts = nrows * ld;
-  const long long p0 = (long long)line0 * ld;
-  auto acc = [](const float2 w, const float2 d, float &sh, float &sl) {
-    const float ph = w.x * d.x;
-    float pl = fmaf(w.x, d.x, -ph);
-    pl = fmaf(w.x, d.y, pl);
-    pl = fmaf(w.y, d.x, pl);
-    const float t = sh + ph;
-    const float bb = t - sh;
-    const float e = (sh - (t - bb)) + (ph - bb);
-    sh = t;
-    sl += e + pl;
-  };
-  for (int base = 0; base < npts; base += kXNThreads * 4) {
-    float xh[4], xl[4], yh[4], yl[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int idx = base + threadIdx.x + e * kXNThreads;
-      xh[e] = xl[e] = yh[e] = yl[e] = 0.f;
-      if (idx < npts && farx) {
-        const float2 fx = farx[p0 + idx], fy = fary[p0 + idx];
-        xh[e] = fx.x;
-        xl[e] = fx.y;
-        yh[e] = fy.x;
-        yl[e] = fy.y;
-      }
-    }
-    auto renorm = [&]() {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {  // fast two-sum
-        float t = xh[e] + xl[e];
-        xl[e] = xl[e] - (t - xh[e]);
-        xh[e] = t;
-        t = yh[e] + yl[e];
-        yl[e] = yl[e] - (t - yh[e]);
-        yh[e] = t;
-      }
-    };
-    int k = 0;
-    for (; k + 4 <= knear; k += 4) {  // 4 layers x 4 points = 16 loads in flight
-      float2 d[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int idx = base + threadIdx.x + e * kXNThreads;
-          d[u][e] = idx < npts ? __ldcs(D + (long long)(k + u) * g.P + p0 + idx) : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float2 wx = wsx[k + u], wy = wsy[k + u];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          acc(wx, d[u][e], xh[e], xl[e]);
-          acc(wy, d[u][e], yh[e], yl[e]);
-        }
-      }
-      if (((k + 4) & 15) == 0) renorm();
-    }
-    for (; k < knear; ++k) {
-      const float2 wx = wsx[k], wy = wsy[k];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int idx = base + threadIdx.x + e * kXNThreads;
-        const float2 d = idx < npts ? __ldcs(D + (long long)k * g.P + p0 + idx) : make_float2(0.f, 0.f);
-        acc(wx, d, xh[e], xl[e]);
-        acc(wy, d, yh[e], yl[e]);
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int idx = base + threadIdx.x + e * kXNThreads;
-      if (idx < npts) {
-        Sx[idx] = (double)xh[e] + (double)xl[e];
-        Sy[p0 + idx] = (double)yh[e] + (double)yl[e];
-      }
-    }
-  }
-  __syncthreads();
-  // ---- phase B: stage the four lines' forward maps (x sums from shared memory)
-  const double kst = -g.st * (cw[0] + 0.0), S2 = g.S * 0.5, st = g.st;
-  for (int ln = 0; ln < nrows; ++ln) {
-    const int line = line0 + ln;
-    double *fa = sbuf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
-    const long long base = (long long)line * ld;
-    for (int i = 1 + threadIdx.x; i < N; i += kXNThreads) {
-      const long long id = base + i;
-      double om = kst * C[id];
-      om += S2;
-      om += st * Sx[ln * ld + i];
-      fa[fh_sk(i)] = fax[id];
-      fb[fh_sk(i)] = -gx[id] * om;
-      al[fh_sk(i)] = alx[id];
-      pf[fh_sk(i)] = pfx[id];
-      pb[fh_sk(i)] = pbx[id];
-    }
-    if (threadIdx.x == 0) pb[fh_sk(0)] = pbx[base];
-  }
-  __syncthreads();
-  if (warp < nrows) {
-    double *fa = sbuf + (size_t)warp * 5 * L;
-    fh_line_solve_prefix(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, 0.0, g.C1, fa + L, fa);
-  }
-  __syncthreads();
-  for (int ln = 0; ln < nrows; ++ln) {
-    const double *u = sbuf + (size_t)ln * 5 * L;
-    const long long base = (long long)(line0 + ln) * ld;
-    for (int i = threadIdx.x; i <= N + 1; i += kXNThreads) {
-      const double v = u[fh_sk(i)];
-      Ch[base + i] = v;
-      if (i == 0 || i >= N) C[base + i] = v;
-    }
-  }
-}
-
 // y half-step (fr_d_t_g_2d.cpp:2634-2648): four adjacent lines i per CTA so
 // that the strided column loads share 32-byte sectors; 128 threads stage each
 // line (kUnroll rows per thread in flight), warp w solves line w.  Reads the
@@ -569,30 +423,6 @@ static int tg_one_step(fh_tg_solver *s) {
   const float2 *far = nullptr;
   if (blocked && s->j0 > 0) far = s->far.as<float2>() + 2LL * (j - s->j0) * s->ldfar;
   int splits = 0, kchunk = 0;
-  const bool fused = s->df && knear <= kNearMax && (knear >= 1 || far);
-  if (fused) {
-    // short double-float history (and the far pairs) inside the x sweep;
-    // profiled as a history-sum launch
-    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-    const size_t smn = sizeof(double) * ((size_t)kXLines * 5 * tg_line_stride(g.sN) + (size_t)kXLines * g.ld);
-    k_tg_xsweep_near<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXNThreads, smn, ctx->stream>>>(
-        g, s->C.as<double>(), s->Ch.as<double>(),
-        reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P, knear, Wj + kstart,
-        Wj + ldw + kstart, far, far ? far + s->ldfar : nullptr, s->part.as<double>(), s->fax.as<double>(),
-        s->gx.as<double>(), s->alx.as<double>(), s->pfx.as<double>(), s->pbx.as<double>(), cwj);
-    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
-    if ((rc = fh_after_launch(ctx, "k_tg_xsweep_near"))) return rc;
-    fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-    const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
-    k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
-        g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (long long)j * g.P, s->part.as<double>(), 0,
-        1, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(), s->pby.as<double>(),
-        cwj, nullptr, 1);
-    fh_prof_mark(ctx, FH_PROF_SWEEP, true);
-    if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
-    s->tstep++;
-    return FH_OK;
-  }
   if (knear >= 1) {
     fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
     if (s->df)
@@ -634,21 +464,16 @@ static int tg_one_step(fh_tg_solver *s) {
 // lower it below what an earlier, larger one launches with).
 static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   static std::mutex mu;
-  static int cur_x[64], cur_y[64], cur_n[64];
+  static int cur_x[64], cur_y[64];
   const int smx = (int)(sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(sN));
-  const int smn = smx + (int)(sizeof(double) * kXLines * (size_t)(sN + 2));
   const int smy = (int)(sizeof(double) * 4 * 6 * (size_t)tg_line_stride(M));
-  FH_REQUIRE(ctx, smn <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL,
+  FH_REQUIRE(ctx, smx <= 200 * 1024 && smy <= 200 * 1024, FH_EINVAL,
              "fh_tg_create: grid too large for the sweeps (sN <= 1170, M <= 970)");
   FH_REQUIRE(ctx, ctx->device >= 0 && ctx->device < 64, FH_EINVAL, "fh_tg_create: device index");
   std::lock_guard<std::mutex> lk(mu);
   if (smx > cur_x[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
     cur_x[ctx->device] = smx;
-  }
-  if (smn > cur_n[ctx->device]) {
-    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep_near, cudaFuncAttributeMaxDynamicSharedMemorySize, smn));
-    cur_n[ctx->device] = smn;
   }
   if (smy > cur_y[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
