@@ -236,6 +236,13 @@ int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host);
 int fh_ab_set_c(fh_ab_solver *s, const double *C);
 /* Override the current-step coefficient Ii (default: the lag-1 weight). */
 int fh_ab_set_current_coef(fh_ab_solver *s, double Ii);
+/* History mode, before the first step: FH_AB_FP64 (default, FP64 sums) or
+ * FH_AB_BLOCKED (entries older than the current 128-step block contracted on
+ * the tensor cores with exact bf16 slices, the rest in FP64; ~2x the history
+ * memory).  No counterpart in the reference. */
+#define FH_AB_FP64 0
+#define FH_AB_BLOCKED 1
+int fh_ab_set_mode(fh_ab_solver *s, int mode);
 int fh_ab_step(fh_ab_solver *s, int nsteps);
 int fh_ab_get_c_host(fh_ab_solver *s, double *C_host);
 

@@ -171,9 +171,10 @@ class AB_solver {
   int step = 0;
   std::vector<double> C;
 
-  AB_solver(Context &ctx, int m_, int max_steps, double tau_, double alpha_)
+  AB_solver(Context &ctx, int m_, int max_steps, double tau_, double alpha_, int mode = FH_AB_FP64)
       : m(m_), tau(tau_), alpha(alpha_), C(size_t(m_) + 1, 0.0), ctx_(ctx) {
     ctx_.check(fh_ab_create(ctx_.get(), m, max_steps, tau, alpha, &s_));
+    if (mode != FH_AB_FP64) ctx_.check(fh_ab_set_mode(s_, mode));
   }
   ~AB_solver() {
     if (s_) fh_ab_destroy(s_);

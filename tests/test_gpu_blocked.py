@@ -67,3 +67,26 @@ def test_tg_blocked_mode_vs_fp64_oracle(ctx, sN, M, steps):
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     print(f"blocked {sN}x{M} {steps} steps: rel max-norm err {err:.3e}")
     assert err <= 1e-9, err
+
+
+@pytest.mark.parametrize("n", [300, 520])
+def test_ab_blocked_mode_vs_oracle(ctx, n):
+    """Atangana-Baleanu solve with the entries older than the current 128-step
+    block contracted on the tensor cores: relative max-norm <= 1e-9 vs the
+    FP64 oracle."""
+    from oracle import oracle as O
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_AB_BLOCKED
+    from theses_code_gb300.solvers import ABSolver
+    cfg, src, bl, br, C0 = workloads.ab_1d(m=256, alpha=0.6, tau=1e-3, seed=2)
+    s = ABSolver(ctx, cfg["m"], n, cfg["tau"], cfg["alpha"], FH_AB_BLOCKED)
+    s.set_source(src, bl, br)
+    s.set_c(C0)
+    s.calc_step(n)
+    w = O.ab_weights(n, cfg["tau"], cfg["alpha"])
+    srcs = np.repeat(src, n, axis=0)
+    ref, _ = O.ab_solve(cfg["m"], n, cfg["tau"], cfg["alpha"], w, srcs, np.zeros(n), np.zeros(n), C0)
+    got = s.get_c()
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    print(f"AB blocked {n} steps: rel max-norm err {err:.3e}")
+    assert err <= 1e-9, err

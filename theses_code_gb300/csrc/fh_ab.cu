@@ -10,6 +10,17 @@
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
 
+// blocked contraction helpers (fh_blocked.cu)
+struct fh_blk;
+fh_blk *fh_blk_new();
+void fh_blk_delete(fh_blk *b);
+int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
+int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
+int fh_blk_toeplitz_weights(fh_ctx *ctx, fh_blk &b, const double *w, int base, int K, int mrows);
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo);
+long long fh_blk_ppad(const fh_blk &b);
+static constexpr int kAbBlock = 128;  // steps per block: one weight row each
+
 struct fh_ab_solver {
   fh_ctx *ctx = nullptr;
   int m = 0, max_steps = 0, step = 0, nrows = 0, max_splits = 1024;
@@ -17,6 +28,14 @@ struct fh_ab_solver {
   double tau = 0, alpha = 0, A = 0, Bd = 0, Cc = 0;
   fh_dbuf w, ii, al, den, inv, sl, pf, pb, C, D, W, part, S, src, bl, br;
   fh_graph_cache graph;
+  int mode = FH_AB_FP64;
+  fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes of the history entries older than T0
+  fh_dbuf far;            // far rows ((hi, lo) pairs) of the steps T0+1 .. T0+128
+  long long ldfar = 0;
+  int T0 = 0;
+  ~fh_ab_solver() {
+    if (blk) fh_blk_delete(blk);
+  }
 };
 
 // al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
@@ -53,10 +72,10 @@ __global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__res
   }
 }
 
-// W[tt] = w[i - tt], tt = 0..i-2
-__global__ void k_ab_stepweights(int i, const double *__restrict__ w, double *__restrict__ W) {
-  const int tt = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tt < i - 1) W[tt] = w[i - tt];
+// W[t] = w[i - (k0 + t)] for the history entries k0 + t, t < n
+__global__ void k_ab_stepweights(int i, int k0, int n, const double *__restrict__ w, double *__restrict__ W) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) W[t] = w[i - k0 - t];
 }
 
 // One step of the tridiagonal solve (the line has m+1 nodes):
@@ -78,7 +97,8 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
                                                         const double *__restrict__ src,
                                                         const double *__restrict__ blp,
                                                         const double *__restrict__ brp, double *C,
-                                                        const double *__restrict__ S, double *__restrict__ Dnew,
+                                                        const double *__restrict__ S,
+                                                        const float2 *__restrict__ far, double *__restrict__ Dnew,
                                                         double tau) {
   extern __shared__ double sm[];
   const int ch = (m + 31) / 32;
@@ -89,7 +109,11 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
   const double ioma = 1.0 / oma, itau = 1.0 / tau;
   for (int j = threadIdx.x; j <= m; j += kAbThreads) {
     double r = fma(cI, C[j], src[j]);
-    if (S) r -= S[j] * ioma;  // MF_intF_simple returns ret/(1-a)
+    if (S || far) {  // MF_intF_simple returns ret/(1-a)
+      double sv = S ? S[j] : 0.0;
+      if (far) sv += (double)far[j].x + (double)far[j].y;
+      r -= sv * ioma;
+    }
     rb[sk(j)] = r * invg[j];
     sl[sk(j)] = slg[j];
     pf[sk(j)] = pfg[j];
@@ -142,24 +166,40 @@ static int ab_one_step(fh_ab_solver *s) {
   const int K = i - 1;        // history entries dC_0 .. dC_{i-2}
   const int row = (i - 1 < s->nrows - 1) ? i - 1 : s->nrows - 1;
   int rc;
+  if (s->blk && K > 0 && K % kAbBlock == 0) {
+    // new block: entries [K-128, K) into the slice planes, Toeplitz rows of the
+    // next 128 steps, far rows S_far[r] = sum_{tt<K} w[K+1+r-tt] dC_tt
+    if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock, 0)) ||
+        (rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock / 2, 0)))
+      return rc;
+    const int mrows = s->max_steps - K < kAbBlock ? s->max_steps - K : kAbBlock;
+    if ((rc = fh_blk_toeplitz_weights(ctx, *s->blk, s->w.as<double>(), K + 1, K, mrows))) return rc;
+    if ((rc = fh_blk_gemm(ctx, *s->blk, K, s->far.as<float2>(), s->ldfar))) return rc;
+    s->T0 = K;
+  }
+  const int k0 = s->blk ? s->T0 : 0;  // entries summed on the CUDA cores this step
+  const int kn = K - k0;
+  const float2 *far = (s->blk && s->T0 > 0) ? s->far.as<float2>() + (long long)(K - s->T0) * s->ldfar : nullptr;
   const double *S = nullptr;
-  if (K > 0) {
-    k_ab_stepweights<<<(unsigned)fh_ceil_div(K, 256), 256, 0, ctx->stream>>>(i, s->w.as<double>(), s->W.as<double>());
+  if (kn > 0) {
+    k_ab_stepweights<<<(unsigned)fh_ceil_div(kn, 256), 256, 0, ctx->stream>>>(i, k0, kn, s->w.as<double>(),
+                                                                             s->W.as<double>());
     if ((rc = fh_after_launch(ctx, "k_ab_stepweights"))) return rc;
     int splits, kchunk;
-    fh_hist_plan(s->P, K, s->max_splits, &splits, &kchunk);
-    if ((rc = fh_launch_hist_sum_partials(ctx, 1, K, s->P, s->W.as<double>(), s->max_steps + 1, s->D.as<double>(),
-                                          s->P, splits, kchunk, s->part.as<double>(), s->P)))
+    fh_hist_plan(s->P, kn, s->max_splits, &splits, &kchunk);
+    if ((rc = fh_launch_hist_sum_partials(ctx, 1, kn, s->P, s->W.as<double>(), s->max_steps + 1,
+                                          s->D.as<double>() + (long long)k0 * s->P, s->P, splits, kchunk,
+                                          s->part.as<double>(), s->P)))
       return rc;
     if ((rc = fh_launch_reduce_splits(ctx, splits, s->P, s->part.as<double>(), s->P, s->S.as<double>()))) return rc;
     S = s->S.as<double>();
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-  k_ab_line<<<1, kAbThreads, ab_line_smem(s->m), ctx->stream>>>(s->m, 1.0 - s->alpha, s->ii.as<double>(), s->al.as<double>(),
-                                          s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
-                                          s->pb.as<double>(), s->src.as<double>() + (long long)row * (s->m + 1),
-                                          s->bl.as<double>() + row, s->br.as<double>() + row, s->C.as<double>(), S,
-                                          s->D.as<double>() + (long long)s->step * s->P, s->tau);
+  k_ab_line<<<1, kAbThreads, ab_line_smem(s->m), ctx->stream>>>(
+      s->m, 1.0 - s->alpha, s->ii.as<double>(), s->al.as<double>(), s->inv.as<double>(), s->sl.as<double>(),
+      s->pf.as<double>(), s->pb.as<double>(), s->src.as<double>() + (long long)row * (s->m + 1),
+      s->bl.as<double>() + row, s->br.as<double>() + row, s->C.as<double>(), S, far,
+      s->D.as<double>() + (long long)s->step * s->P, s->tau);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_ab_line"))) return rc;
   s->step++;
@@ -254,6 +294,7 @@ int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host) {
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, sizeof(double) * (s->m + 1), cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->step = 0;
+  s->T0 = 0;
   return FH_OK;
 }
 
@@ -263,6 +304,7 @@ int fh_ab_set_c(fh_ab_solver *s, const double *C) {
   FH_REQUIRE(ctx, C, FH_EINVAL, "fh_ab_set_c: null pointer");
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, sizeof(double) * (s->m + 1), cudaMemcpyDeviceToDevice, ctx->stream));
   s->step = 0;
+  s->T0 = 0;
   return FH_OK;
 }
 
@@ -277,6 +319,34 @@ int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
                                         s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
                                         s->pb.as<double>());
   return fh_after_launch(ctx, "k_ab_factor");
+}
+
+int fh_ab_set_mode(fh_ab_solver *s, int mode) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, mode == FH_AB_FP64 || mode == FH_AB_BLOCKED, FH_EINVAL, "fh_ab_set_mode: unknown mode %d", mode);
+  FH_REQUIRE(ctx, s->step == 0, FH_EINVAL, "fh_ab_set_mode: only before the first step");
+  s->mode = mode;
+  if (mode == FH_AB_BLOCKED && !s->blk && s->max_steps > kAbBlock) {
+    s->blk = fh_blk_new();
+    const int kcap = (int)fh_ceil_div(s->max_steps, kAbBlock) * kAbBlock;
+    int rc = fh_blk_init(ctx, *s->blk, s->P, kcap);
+    if (!rc) {
+      s->ldfar = fh_blk_ppad(*s->blk);
+      rc = fh_alloc(ctx, s->far, sizeof(float2) * kAbBlock * (size_t)s->ldfar, false);
+    }
+    if (rc) {
+      fh_blk_delete(s->blk);
+      s->blk = nullptr;
+      return rc;
+    }
+  }
+  if (mode == FH_AB_FP64 && s->blk) {
+    fh_blk_delete(s->blk);
+    s->blk = nullptr;
+  }
+  s->graph.reset();
+  return FH_OK;
 }
 
 int fh_ab_step(fh_ab_solver *s, int nsteps) {

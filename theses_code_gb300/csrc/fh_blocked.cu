@@ -333,6 +333,17 @@ __global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, do
   fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
 }
 
+// Toeplitz weight rows (1D solvers with lag weights): row m = step T0 + 1 + m
+// weighs history entry k with w[base + m - k] (base = T0 + 1); rows m >= mrows
+// are zero.
+__global__ void k_blk_toeplitz_rows(const double *__restrict__ w, int base, int K, int Kcap, int mrows,
+                                    __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
+  const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= kBM) return;
+  auto val = [&](int k) { return (k < K && m < mrows) ? w[base + m - k] : 0.0; };
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
+}
+
 // Weight rows W[m*ldw + k], k < K, rows m >= mrows are zero (standalone
 // contraction, or a block of the per-solve weight table).
 __global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, int K, int Kcap, int mrows,
@@ -599,6 +610,15 @@ int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, dou
   k_blk_weights<<<g, 256, 0, ctx->stream>>>(j0, j0, b.Kcap, Da, tau, alpha, beta, b.A3.as<__nv_bfloat16>(),
                                            b.Ew.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_weights");
+}
+
+// Toeplitz weight planes for K history entries (k_blk_toeplitz_rows).
+int fh_blk_toeplitz_weights(fh_ctx *ctx, fh_blk &b, const double *w, int base, int K, int mrows) {
+  FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
+  dim3 g((unsigned)fh_ngroups(K / kBK), kBM / 8);
+  k_blk_toeplitz_rows<<<g, 256, 0, ctx->stream>>>(w, base, K, b.Kcap, mrows, b.A3.as<__nv_bfloat16>(),
+                                                  b.Ew.as<int8_t>());
+  return fh_after_launch(ctx, "k_blk_toeplitz_rows");
 }
 
 // S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p] as (hi, lo) pairs.

@@ -38,7 +38,7 @@ struct fh_h_batch {
   std::vector<fh_h_params> hp;
   std::vector<long long> off;
   std::vector<fh_h_tile> tiles;
-  fh_dbuf inst, tl, U, D, W, Lb, wc, part, Al, Bt, sA, sB, sR, sOm;
+  fh_dbuf inst, tl, U, D, W, Lb, ibt, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
 };
@@ -51,7 +51,8 @@ static constexpr int kTileThreads = 256;  // 512 nodes per tile
 // The reference's t = 0 term multiplies layer1 - layer1 (its layer pointer
 // starts at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
 __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
-                            int ldw, double *__restrict__ wc, const double *__restrict__ Lb) {
+                            int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
+                            const double *__restrict__ ibt) {
   const int b = blockIdx.y;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const fh_h_dev_inst I = inst[b];
@@ -61,6 +62,10 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
       w = 0.0;
     else if (I.weights == FH_W_L1)
       w = Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
+    else if (I.beta != 1.0)
+      w = fh_psi_int_tab((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta,
+                         ibt + (long long)b * 2 * kIbTerms, ibt + (long long)b * 2 * kIbTerms + kIbTerms) *
+          (1 - I.alpha);
     else
       w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
     W[(long long)b * ldw + t] = w;
@@ -71,6 +76,15 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
                 : fh_psi_int((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) *
                       (1 - I.alpha);
   }
+}
+
+// Incomplete-beta series coefficients of every psi instance (fh_ib_tables).
+__global__ void k_h_ibtab(const fh_h_dev_inst *__restrict__ inst, int n, double *__restrict__ ibt) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const fh_h_dev_inst I = inst[b];
+  if (I.weights != FH_W_PSI) return;
+  fh_ib_tables(1.0 / I.beta, 1.0 - I.alpha, ibt + (long long)b * 2 * kIbTerms, ibt + (long long)b * 2 * kIbTerms + kIbTerms);
 }
 
 // Lag table of the L1 instances: Lb[b][l] = (l+1)^(1-a) - l^(1-a) (mt_minimal.cpp:930),
@@ -268,7 +282,8 @@ static int h_one_step(fh_h_batch *B) {
   dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, 128), (unsigned)B->n);
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
   k_h_weights<<<gw, 128, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
-                                           B->max_weights, B->wc.as<double>(), B->Lb.as<double>());
+                                           B->max_weights, B->wc.as<double>(), B->Lb.as<double>(),
+                                           B->ibt.as<double>());
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
   if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
   int splits = 0, kchunk = 0;
@@ -361,6 +376,7 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
       (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, B->W, sizeof(double) * (size_t)ninst * B->max_weights)) ||
       (rc = fh_alloc(ctx, B->Lb, sizeof(double) * (size_t)ninst * B->max_weights, false)) ||
+      (rc = fh_alloc(ctx, B->ibt, sizeof(double) * 2 * kIbTerms * (size_t)ninst, false)) ||
       (rc = fh_alloc(ctx, B->wc, sizeof(double) * ninst)) ||
       (rc = fh_alloc(ctx, B->part, st * (size_t)B->max_splits, false))) {
     delete B;
@@ -376,6 +392,12 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
   k_h_lagtab<<<dim3((unsigned)fh_ceil_div(B->max_weights, 128), (unsigned)ninst), 128, 0, ctx->stream>>>(
       B->inst.as<fh_h_dev_inst>(), B->max_weights, B->Lb.as<double>(), B->max_weights);
   if ((rc = fh_after_launch(ctx, "k_h_lagtab"))) {
+    delete B;
+    return rc;
+  }
+  k_h_ibtab<<<(unsigned)fh_ceil_div(ninst, 128), 128, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), ninst,
+                                                                        B->ibt.as<double>());
+  if ((rc = fh_after_launch(ctx, "k_h_ibtab"))) {
     delete B;
     return rc;
   }

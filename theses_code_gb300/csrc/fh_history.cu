@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
                                                               int K, const double *__restrict__ W, int ldw,
                                                               int kchunk, double *__restrict__ part,
                                                               long long ldpart, const float2 *__restrict__ far,
-                                                              long long ldfar) {
+                                                              long long ldfar, int pair_out) {
   extern __shared__ float2 wsf[];  // [M][kchunk] (hi, lo)
   const int s = blockIdx.y;
   const int k0 = s * kchunk;
@@ -158,16 +158,25 @@ __global__ void __launch_bounds__(kHistThreads) k_hist_sum_df(const float2 *__re
   }
 #pragma unroll
   for (int m = 0; m < M; ++m) {
-    double2 o;
-    o.x = (double)ah[m][0] + (double)al[m][0];
-    o.y = (double)ah[m][1] + (double)al[m][1];
-    *reinterpret_cast<double2 *>(part + ((long long)s * M + m) * ldpart + p) = o;
+    if (pair_out) {  // renormalised (hi, lo) pairs for double-float consumers
+      float4 o;
+      o.x = ah[m][0] + al[m][0];
+      o.y = al[m][0] - (o.x - ah[m][0]);
+      o.z = ah[m][1] + al[m][1];
+      o.w = al[m][1] - (o.z - ah[m][1]);
+      *reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(part) + ((long long)s * M + m) * ldpart + p) = o;
+    } else {
+      double2 o;
+      o.x = (double)ah[m][0] + (double)al[m][0];
+      o.y = (double)ah[m][1] + (double)al[m][1];
+      *reinterpret_cast<double2 *>(part + ((long long)s * M + m) * ldpart + p) = o;
+    }
   }
 }
 
 int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                    const float2 *D, long long ldd, int splits, int kchunk, double *part,
-                                   long long ldpart, const float2 *far, long long ldfar) {
+                                   long long ldpart, const float2 *far, long long ldfar, int pair_out) {
   if (K <= 0 || P <= 0) return FH_OK;
   dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
   const size_t smem = sizeof(float2) * (size_t)M * (size_t)kchunk;
@@ -175,10 +184,10 @@ int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const
   fh_prof_mark(ctx, FH_PROF_HISTORY, false);
   if (M == 1)
     k_hist_sum_df<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
-                                                                  ldfar);
+                                                                  ldfar, pair_out);
   else
     k_hist_sum_df<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
-                                                                  ldfar);
+                                                                  ldfar, pair_out);
   fh_prof_mark(ctx, FH_PROF_HISTORY, true);
   return fh_after_launch(ctx, "k_hist_sum_df");
 }

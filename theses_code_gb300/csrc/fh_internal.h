@@ -69,6 +69,12 @@ struct fh_graph_cache {
       v.clear();
     }
   }
+  void reset() {  // forget the captured graph (the launch sequence changed)
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    nsteps = -1;
+    release_events();
+  }
   ~fh_graph_cache() {
     if (exec) cudaGraphExecDestroy(exec);
     release_events();
@@ -155,8 +161,9 @@ int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const do
 int fh_launch_reduce_splits(fh_ctx *ctx, int splits, long long P, const double *part, long long ldpart, double *S);
 // History stored as (hi, lo) FP32 pairs, double-float accumulation; split 0
 // starts from far[m*ldfar + p] (a (hi, lo) pair per point) when far != null.
+// The partial sums are doubles, or (hi, lo) pairs when pair_out.
 int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                                    const float2 *D, long long ldd, int splits, int kchunk, double *part,
-                                   long long ldpart, const float2 *far, long long ldfar);
+                                   long long ldpart, const float2 *far, long long ldfar, int pair_out);
 // Chooses the split count for a K x P history sum given a partial-buffer capacity.
 void fh_hist_plan(long long P, int K, int max_splits, int *splits, int *kchunk);

@@ -9,6 +9,7 @@
 // ~2N/32 + 10 dependent steps.
 #pragma once
 #include "fh_common.cuh"
+#include "fh_df.cuh"
 
 // Reverse exclusive scan: lane l receives G_{l+1} o G_{l+2} o ... o G_31
 // (identity for lane 31), i.e. the maps of all higher lanes applied first.
@@ -175,6 +176,49 @@ __device__ __forceinline__ void fh_line_solve_prefix(int N, const double *fa, co
   if (lane == 0) {
     u[fh_sk(N)] = uN;
     u[fh_sk(N + 1)] = uN;
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------------------
+// Double-float variant of fh_line_solve_prefix (arrays of (hi, lo) pairs,
+// fh_df.cuh arithmetic on the FP32 pipe); same chunking and scheme.
+__device__ __forceinline__ void fh_line_solve_prefix_df(int N, const float2 *fa, const float2 *fb, const float2 *al,
+                                                        const float2 *pf, const float2 *pb, fh_df al1, fh_df bt1,
+                                                        float2 *bt, float2 *u) {
+  const int lane = threadIdx.x & 31;
+  const int chf = fh_chunk_f(N);
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  fh_df b{0.f, 0.f};
+  for (int i = f0; i < f1; ++i) {
+    b = fh_df_fma(fh_df_from_pair(fa[fh_sk(i)]), b, fh_df_from_pair(fb[fh_sk(i)]));
+    bt[fh_sk(i)] = fh_df_pair(b);
+  }
+  const fh_daff Pf = fh_warp_exclusive_daff(f1 > f0 ? fh_daff{fh_df_from_pair(pf[fh_sk(f1 - 1)]), b}
+                                                    : fh_daff{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}});
+  const fh_df s = fh_df_fma(Pf.a, bt1, Pf.b);  // Bt[f0]
+  for (int i = f0; i < f1; ++i)
+    bt[fh_sk(i)] = fh_df_pair(fh_df_fma(fh_df_from_pair(pf[fh_sk(i)]), s, fh_df_from_pair(bt[fh_sk(i)])));
+  if (lane == 0) bt[fh_sk(0)] = fh_df_pair(bt1);
+  __syncwarp();
+  const fh_df alN = (N >= 2) ? fh_df_from_pair(al[fh_sk(N - 1)]) : al1;
+  const fh_df uN = fh_df_div(fh_df_from_pair(bt[fh_sk(N - 1)]), fh_df_sub(fh_df{1.f, 0.f}, alN));
+  const int chb = fh_chunk_b(N);
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  fh_df v{0.f, 0.f};
+  __syncwarp();  // u may alias fa: all forward reads are done
+  for (int i = b1 - 1; i >= b0; --i) {
+    v = fh_df_fma((i >= 1) ? fh_df_from_pair(al[fh_sk(i)]) : al1, v, fh_df_from_pair(bt[fh_sk(i)]));
+    u[fh_sk(i)] = fh_df_pair(v);
+  }
+  const fh_daff Pb = fh_warp_exclusive_daff_rev(b1 > b0 ? fh_daff{fh_df_from_pair(pb[fh_sk(b0)]), v}
+                                                        : fh_daff{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}});
+  const fh_df t = fh_df_fma(Pb.a, uN, Pb.b);  // u_{b1}
+  for (int i = b0; i < b1; ++i)
+    u[fh_sk(i)] = fh_df_pair(fh_df_fma(fh_df_from_pair(pb[fh_sk(i)]), t, fh_df_from_pair(u[fh_sk(i)])));
+  if (lane == 0) {
+    u[fh_sk(N)] = fh_df_pair(uN);
+    u[fh_sk(N + 1)] = fh_df_pair(uN);
   }
   __syncwarp();
 }

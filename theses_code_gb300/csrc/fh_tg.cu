@@ -59,6 +59,9 @@ struct fh_tg_solver {
   bool factor_fixed = false;
   int max_splits = 8;
   fh_dbuf C, Ch, V2, D, W, cw, part, alx, gx, fax, pfx, pbx, aly, gy, fay, pfy, pby, far;
+  // blocked mode: the sweeps run in double-float; fields and factor tables as (hi, lo) pairs
+  bool dfsweep = false;
+  fh_dbuf Cd, Chd, fax2, gx2, alx2, pfx2, pbx2, fay2, gy2, aly2, pfy2, pby2;
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
   fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
@@ -170,16 +173,18 @@ __global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ W
 // Shared-memory footprint of one staged line array: fh_sk(N+1)+1 doubles.
 __host__ __device__ inline int tg_line_stride(int N) { return (N + 2) + ((N + 2) >> 4) + 2; }
 
-static constexpr int kXLines = 4;       // x lines per CTA, one warp each
-static constexpr int kXThreads = 32 * kXLines;
+static constexpr int kXLines = 4;       // x lines per CTA, one solving warp each
+static constexpr int kXGroup = 128;     // threads staging / writing one line
+static constexpr int kXThreads = kXGroup * kXLines;
 static constexpr int kYThreads = 512;  // four adjacent y lines per CTA
 static constexpr int kUnroll = 4;      // equations staged per thread per round
 
-// x half-step (fr_d_t_g_2d.cpp:2577-2590): four lines j per CTA.  All threads
-// stage the four lines' forward maps into shared memory with independent,
-// coalesced loads, then warp w solves line w (the four solving warps sit on
-// the SM's four sub-partitions, so the FP64 work of the solves runs in
-// parallel), then all threads write the half-step field Ch.  The boundary
+// x half-step (fr_d_t_g_2d.cpp:2577-2590): four lines j per CTA.  A group of
+// 128 threads per line stages its forward maps into shared memory with
+// independent, coalesced loads (all four lines in one round trip), then warp
+// w solves line w (the four solving warps sit on the SM's four
+// sub-partitions, so the solves run in parallel), then the groups write the
+// half-step field Ch.  The boundary
 // nodes i = 0, N, N+1 are also written into C, which otherwise keeps the
 // full-step field.
 __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C, double *__restrict__ Ch,
@@ -197,16 +202,16 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
   const int N = g.sN;
   const int L = tg_line_stride(N);
   const double kst = -g.st * (cw[0] + 0.0), S2 = g.S * 0.5, st = g.st;
-  for (int ln = 0; ln < kXLines; ++ln) {
+  {
+    const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
     const int line = line0 + ln;
-    if (line >= g.M) break;
     double *fa = sbuf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
     const long long base = (long long)line * g.ld;
-    for (int r0 = 1; r0 < N; r0 += kXThreads * kUnroll) {
+    for (int r0 = 1; line < g.M && r0 < N; r0 += kXGroup * kUnroll) {
       double ts[kUnroll], c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
 #pragma unroll
       for (int e = 0; e < kUnroll; ++e) {
-        const int i = r0 + threadIdx.x + e * kXThreads;
+        const int i = r0 + tg + e * kXGroup;
         const long long id = base + (i < N ? i : 1);
         c[e] = C[id];
         a[e] = fax[id];
@@ -223,12 +228,12 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
       for (int s = 0; s < splits; ++s)
 #pragma unroll
         for (int e = 0; e < kUnroll; ++e) {
-          const int i = r0 + threadIdx.x + e * kXThreads;
+          const int i = r0 + tg + e * kXGroup;
           ts[e] += part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)];
         }
 #pragma unroll
       for (int e = 0; e < kUnroll; ++e) {
-        const int i = r0 + threadIdx.x + e * kXThreads;
+        const int i = r0 + tg + e * kXGroup;
         if (i < N) {
           double om = kst * c[e];
           om += S2;
@@ -242,22 +247,22 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
       }
     }
     // node 0 belongs to lane 0's backward chunk: its prefix product
-    if (threadIdx.x == 0) pb[fh_sk(0)] = pbx[base];
+    if (tg == 0 && line < g.M) pb[fh_sk(0)] = pbx[base];
   }
   __syncthreads();
-  if (line0 + warp < g.M) {
+  if (warp < kXLines && line0 + warp < g.M) {
     double *fa = sbuf + (size_t)warp * 5 * L;
     // bt scratch reuses pf's slots only after pf is consumed: use a separate
     // region, the fb array, which the forward walk overwrites in place
     fh_line_solve_prefix(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, 0.0, g.C1, fa + L, fa);
   }
   __syncthreads();
-  for (int ln = 0; ln < kXLines; ++ln) {
+  {
+    const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
     const int line = line0 + ln;
-    if (line >= g.M) break;
     const double *u = sbuf + (size_t)ln * 5 * L;
     const long long base = (long long)line * g.ld;
-    for (int i = threadIdx.x; i <= N + 1; i += kXThreads) {
+    for (int i = tg; line < g.M && i <= N + 1; i += kXGroup) {
       const double v = u[fh_sk(i)];
       Ch[base + i] = v;
       if (i == 0 || i >= N) C[base + i] = v;
@@ -359,6 +364,180 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
   }
 }
 
+// ---------------------------------------------------- double-float sweeps
+// Blocked mode runs both half steps in double-float arithmetic on the FP32
+// pipe (fh_df.cuh): fields, factor tables, history partial sums and far rows
+// are (hi, lo) FP32 pairs, so no FP64 instruction is left in the sweeps.  Same
+// structure as k_tg_xsweep / k_tg_ysweep.
+__global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 *Cd, float2 *__restrict__ Chd,
+                                                           const float2 *__restrict__ part, long long ldp,
+                                                           int splits, const float2 *__restrict__ fax,
+                                                           const float2 *__restrict__ gx,
+                                                           const float2 *__restrict__ alx,
+                                                           const float2 *__restrict__ pfx,
+                                                           const float2 *__restrict__ pbx,
+                                                           const double *__restrict__ cw,
+                                                           const float2 *__restrict__ far) {
+  extern __shared__ float2 sbf[];
+  const int warp = threadIdx.x >> 5;
+  const int line0 = 1 + blockIdx.x * kXLines;
+  const int N = g.sN;
+  const int L = tg_line_stride(N);
+  const fh_df kst = fh_df_from_double(-g.st * (cw[0] + 0.0)), S2 = fh_df_from_double(g.S * 0.5),
+              st = fh_df_from_double(g.st);
+  {
+    const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
+    const int line = line0 + ln;
+    float2 *fa = sbf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
+    const long long base = (long long)line * g.ld;
+    for (int r0 = 1; line < g.M && r0 < N; r0 += kXGroup * kUnroll) {
+      float2 c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
+      fh_df ts[kUnroll];
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = r0 + tg + e * kXGroup;
+        const long long id = base + (i < N ? i : 1);
+        c[e] = Cd[id];
+        a[e] = fax[id];
+        gi[e] = gx[id];
+        l[e] = alx[id];
+        qf[e] = pfx[id];
+        qb[e] = pbx[id];
+        ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+      }
+      for (int s = 0; s < splits; ++s)
+#pragma unroll
+        for (int e = 0; e < kUnroll; ++e) {
+          const int i = r0 + tg + e * kXGroup;
+          ts[e] = fh_df_add(ts[e], fh_df_from_pair(part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)]));
+        }
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = r0 + tg + e * kXGroup;
+        if (i < N) {
+          fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
+          om = fh_df_fma(st, ts[e], om);
+          fa[fh_sk(i)] = a[e];
+          fb[fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(gi[e]), om)));
+          al[fh_sk(i)] = l[e];
+          pf[fh_sk(i)] = qf[e];
+          pb[fh_sk(i)] = qb[e];
+        }
+      }
+    }
+    if (tg == 0 && line < g.M) pb[fh_sk(0)] = pbx[base];
+  }
+  __syncthreads();
+  if (warp < kXLines && line0 + warp < g.M) {
+    float2 *fa = sbf + (size_t)warp * 5 * L;
+    fh_line_solve_prefix_df(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, fh_df{0.f, 0.f},
+                            fh_df_from_double(g.C1), fa + L, fa);
+  }
+  __syncthreads();
+  {
+    const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
+    const int line = line0 + ln;
+    const float2 *u = sbf + (size_t)ln * 5 * L;
+    const long long base = (long long)line * g.ld;
+    for (int i = tg; line < g.M && i <= N + 1; i += kXGroup) {
+      const float2 v = u[fh_sk(i)];
+      Chd[base + i] = v;
+      if (i == 0 || i >= N) Cd[base + i] = v;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 *Cd, const float2 *__restrict__ Chd,
+                                                           float2 *__restrict__ Dj, const float2 *__restrict__ part,
+                                                           long long ldp, int splits,
+                                                           const float2 *__restrict__ fay,
+                                                           const float2 *__restrict__ gy,
+                                                           const float2 *__restrict__ aly,
+                                                           const float2 *__restrict__ pfy,
+                                                           const float2 *__restrict__ pby,
+                                                           const double *__restrict__ cw,
+                                                           const float2 *__restrict__ far) {
+  extern __shared__ float2 sbf[];
+  const int warp = threadIdx.x >> 5;
+  const int N = g.M;
+  const int L = tg_line_stride(N);
+  const int i0 = 1 + blockIdx.x * 4;
+  const fh_df kst = fh_df_from_double(-g.st * (cw[1] + 0.0)), kyh = fh_df_from_double(cw[2] + 0.0),
+              S2 = fh_df_from_double(g.S * 0.5), st = fh_df_from_double(g.st);
+  const int col = threadIdx.x & 3;
+  const int rg = threadIdx.x >> 2;  // row group 0..127
+  constexpr int kRows = kYThreads / 4;
+  const int line = i0 + col;
+  const bool live = line < g.sN;
+  float2 *fa = sbf + (size_t)col * 6 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L, *cf = pb + L;
+  for (int r0 = 1; r0 < N; r0 += kRows * kUnroll) {
+    float2 c[kUnroll], f[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
+    fh_df ts[kUnroll];
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int q = r0 + rg + e * kRows;
+      const long long id = (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld;
+      c[e] = Chd[id];
+      f[e] = Cd[id];
+      a[e] = fay[id];
+      gi[e] = gy[id];
+      l[e] = aly[id];
+      qf[e] = pfy[id];
+      qb[e] = pby[id];
+      ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+    }
+    for (int s = 0; s < splits; ++s)
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int q = r0 + rg + e * kRows;
+        ts[e] = fh_df_add(
+            ts[e], fh_df_from_pair(part[(long long)(2 * s + 1) * ldp + (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld]));
+      }
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int q = r0 + rg + e * kRows;
+      if (live && q < N) {
+        const fh_df cc = fh_df_from_pair(c[e]);
+        // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
+        const fh_df t = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), ts[e]);
+        fh_df om = fh_df_fma(kst, cc, S2);
+        om = fh_df_fma(st, t, om);
+        fa[fh_sk(q)] = a[e];
+        fb[fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(gi[e]), om)));
+        al[fh_sk(q)] = l[e];
+        pf[fh_sk(q)] = qf[e];
+        pb[fh_sk(q)] = qb[e];
+        cf[fh_sk(q)] = f[e];
+      }
+    }
+  }
+  if (live && rg == 0) pb[fh_sk(0)] = pby[line];  // node 0: lane 0's backward chunk
+  __syncthreads();
+  if (warp < 4 && i0 + warp < g.sN) {
+    float2 *wfa = sbf + (size_t)warp * 6 * L;
+    fh_line_solve_prefix_df(N, wfa, wfa + L, wfa + 2 * L, wfa + 3 * L, wfa + 4 * L, fh_df{1.f, 0.f},
+                            fh_df{0.f, 0.f}, wfa + L, wfa);
+  }
+  __syncthreads();
+  if (live) {
+    for (int q = rg; q <= N + 1; q += kRows) {
+      const long long id = line + (long long)q * g.ld;
+      const float2 u = fa[fh_sk(q)];
+      Cd[id] = u;
+      if (q >= 1 && q < N) Dj[id] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(cf[fh_sk(q)])));
+    }
+  }
+}
+
+__global__ void k_to_pairs(const double *__restrict__ x, float2 *__restrict__ y, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = fh_df_pair(fh_df_from_double(x[i]));
+}
+__global__ void k_from_pairs(const float2 *__restrict__ y, double *__restrict__ x, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = fh_df_to_double(fh_df_from_pair(y[i]));
+}
+
 // ------------------------------------------------------------------ host
 
 static constexpr int kWeightTableMaxSteps = 4096;  // 2 x 4096^2 doubles = 268 MB
@@ -374,7 +553,18 @@ static int tg_factor(fh_tg_solver *s, const double *cwj) {
   k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(
       g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(),
       s->pfy.as<double>(), s->pby.as<double>());
-  return fh_after_launch(ctx, "k_tg_factor(y)");
+  if ((rc = fh_after_launch(ctx, "k_tg_factor(y)"))) return rc;
+  if (s->dfsweep) {
+    const fh_dbuf *src[10] = {&s->fax, &s->gx, &s->alx, &s->pfx, &s->pbx, &s->fay, &s->gy, &s->aly, &s->pfy, &s->pby};
+    fh_dbuf *dst[10] = {&s->fax2, &s->gx2, &s->alx2, &s->pfx2, &s->pbx2,
+                        &s->fay2, &s->gy2, &s->aly2, &s->pfy2, &s->pby2};
+    for (int q = 0; q < 10; ++q) {
+      k_to_pairs<<<(unsigned)fh_ceil_div(g.P, 256), 256, 0, ctx->stream>>>(src[q]->as<double>(), dst[q]->as<float2>(),
+                                                                          g.P);
+      if ((rc = fh_after_launch(ctx, "k_to_pairs"))) return rc;
+    }
+  }
+  return FH_OK;
 }
 
 static int tg_one_step(fh_tg_solver *s) {
@@ -384,6 +574,10 @@ static int tg_one_step(fh_tg_solver *s) {
   const int ldw = s->max_steps;
   int rc;
   const bool blocked = s->blk != nullptr;
+  if (s->dfsweep && j == 0) {
+    k_to_pairs<<<(unsigned)fh_ceil_div(g.P, 256), 256, 0, ctx->stream>>>(s->C.as<double>(), s->Cd.as<float2>(), g.P);
+    if ((rc = fh_after_launch(ctx, "k_to_pairs"))) return rc;
+  }
   if (blocked && j > 0 && j % kTgBlock == 0) {
     // new block: planes for layers [j-64, j), weight planes for steps j..j+63,
     // far rows S_far[2r + {0,1}] = sum_{k<j} w_{j+r}(k) D[k] on the tensor cores
@@ -428,7 +622,8 @@ static int tg_one_step(fh_tg_solver *s) {
     if (s->df)
       rc = fh_launch_hist_sum_df_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                           reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P,
-                                          g.P, splits, kchunk, s->part.as<double>(), g.P, far, s->ldfar);
+                                          g.P, splits, kchunk, s->part.as<double>(), g.P, far, s->ldfar,
+                                          s->dfsweep ? 1 : 0);
     else
       rc = fh_launch_hist_sum_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                        s->D.as<double>() + (long long)kstart * g.P, g.P, splits, kchunk,
@@ -440,6 +635,23 @@ static int tg_one_step(fh_tg_solver *s) {
   if (far && !(knear >= 1 && s->df)) {
     farx = far;
     fary = far + s->ldfar;
+  }
+  if (s->dfsweep) {
+    fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+    const size_t smx = sizeof(float2) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
+    k_tg_xsweep_df<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXThreads, smx, ctx->stream>>>(
+        g, s->Cd.as<float2>(), s->Chd.as<float2>(), s->part.as<float2>(), g.P, splits, s->fax2.as<float2>(),
+        s->gx2.as<float2>(), s->alx2.as<float2>(), s->pfx2.as<float2>(), s->pbx2.as<float2>(), cwj, farx);
+    if ((rc = fh_after_launch(ctx, "k_tg_xsweep_df"))) return rc;
+    const size_t smy = sizeof(float2) * 4 * 6 * (size_t)tg_line_stride(g.M);
+    k_tg_ysweep_df<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
+        g, s->Cd.as<float2>(), s->Chd.as<float2>(), reinterpret_cast<float2 *>(s->D.as<double>()) + (long long)j * g.P,
+        s->part.as<float2>(), g.P, splits, s->fay2.as<float2>(), s->gy2.as<float2>(), s->aly2.as<float2>(),
+        s->pfy2.as<float2>(), s->pby2.as<float2>(), cwj, fary);
+    fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+    if ((rc = fh_after_launch(ctx, "k_tg_ysweep_df"))) return rc;
+    s->tstep++;
+    return FH_OK;
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
   const size_t smx = sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
@@ -462,6 +674,16 @@ static int tg_one_step(fh_tg_solver *s) {
 // a per-function attribute of the device, shared by every solver in the
 // process, so it only ever grows (a smaller solver created later must not
 // lower it below what an earlier, larger one launches with).
+// Double-float sweeps keep the field as pairs; the FP64 field C (returned by
+// fh_tg_field / fh_tg_get_c_host) is refreshed at the end of every step call.
+static int tg_publish(fh_tg_solver *s) {
+  if (!s->dfsweep || s->tstep == 0) return FH_OK;
+  fh_ctx *ctx = s->ctx;
+  k_from_pairs<<<(unsigned)fh_ceil_div(s->dv.P, 256), 256, 0, ctx->stream>>>(s->Cd.as<float2>(), s->C.as<double>(),
+                                                                            s->dv.P);
+  return fh_after_launch(ctx, "k_from_pairs");
+}
+
 static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   static std::mutex mu;
   static int cur_x[64], cur_y[64];
@@ -473,10 +695,12 @@ static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   std::lock_guard<std::mutex> lk(mu);
   if (smx > cur_x[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep_df, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
     cur_x[ctx->device] = smx;
   }
   if (smy > cur_y[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep_df, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
     cur_y[ctx->device] = smy;
   }
   return FH_OK;
@@ -537,6 +761,17 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
       (rc = fh_alloc(ctx, s->part, fld * 2 * (size_t)s->max_splits, false))) {
     delete s;
     return rc;
+  }
+  s->dfsweep = (mode == FH_TG_BLOCKED);
+  if (s->dfsweep) {
+    const size_t fp = sizeof(float2) * (size_t)g.P;
+    fh_dbuf *arr[12] = {&s->Cd, &s->Chd, &s->fax2, &s->gx2, &s->alx2, &s->pfx2,
+                        &s->pbx2, &s->fay2, &s->gy2, &s->aly2, &s->pfy2, &s->pby2};
+    for (auto *b : arr)
+      if ((rc = fh_alloc(ctx, *b, fp))) {
+        delete s;
+        return rc;
+      }
   }
   if (mode == FH_TG_BLOCKED && max_steps > kTgBlock) {
     s->blk = fh_blk_new();
@@ -602,7 +837,7 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
         int r = tg_one_step(s);
         if (r) return r;
       }
-      return (int)FH_OK;
+      return tg_publish(s);
     });
     if (rc) return rc;
     s->tstep = nsteps;
@@ -613,7 +848,7 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
     int rc = tg_one_step(s);
     if (rc) return rc;
   }
-  return FH_OK;
+  return tg_publish(s);
 }
 
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host) {

@@ -66,3 +66,56 @@ __device__ __forceinline__ double fh_psi_int(double x0, double x1, double X, dou
   const double T = X * tau;
   return pow(T, 1.0 - alpha * beta) / beta * diff;
 }
+
+// ---- tabulated series for many weights of one (alpha, beta) pair
+// Both incomplete-beta series above have coefficients that depend only on
+// (a, b) = (1/beta, 1-alpha); with them tabulated, a series is one Horner
+// polynomial of kIbTerms FMAs (their arguments stay <= 1/2, so 64 terms reach
+// 2^-64 of the leading term) instead of a loop with two divisions per term.
+constexpr int kIbTerms = 64;
+
+// Lc[j] = (1-b)_j / (j! (a+j)), Uc[j] = (1-a)_j / (j! (b+j)).
+__device__ __forceinline__ void fh_ib_tables(double a, double b, double *Lc, double *Uc) {
+  double c = 1.0, d = 1.0;
+  for (int j = 0; j < kIbTerms; ++j) {
+    Lc[j] = c / (a + (double)j);
+    Uc[j] = d / (b + (double)j);
+    c *= ((double)(j + 1) - b) / (double)(j + 1);
+    d *= ((double)(j + 1) - a) / (double)(j + 1);
+  }
+}
+
+__device__ __forceinline__ double fh_horner(const double *__restrict__ c, double y) {
+  double s = c[kIbTerms - 1];
+#pragma unroll 8
+  for (int j = kIbTerms - 2; j >= 0; --j) s = fma(s, y, c[j]);
+  return s;
+}
+
+// fh_psi_int for beta != 1 from the tables: B(y; a, b) = y^a Lc(y) with
+// y^a = x/X exactly (a = 1/beta, y = (x/X)^beta), upper tail c^b Uc(c).
+__device__ __forceinline__ double fh_psi_int_tab(double x0, double x1, double X, double tau, double alpha,
+                                                 double beta, const double *__restrict__ Lc,
+                                                 const double *__restrict__ Uc) {
+  const double a = 1.0 / beta, b = 1.0 - alpha;
+  const double r0 = x0 / X, r1 = x1 / X;
+  const double y0 = pow(r0, beta), y1 = pow(r1, beta);
+  auto lower = [&](double y, double r) { return y <= 0.0 ? 0.0 : r * fh_horner(Lc, y); };
+  auto upper = [&](double x) {
+    if (x >= X) return 0.0;
+    const double c = -expm1(beta * log1p((x - X) / X));
+    return c <= 0.0 ? 0.0 : pow(c, b) * fh_horner(Uc, c);
+  };
+  double diff;
+  if (y1 <= 0.5) {
+    diff = lower(y1, r1) - lower(y0, r0);
+  } else if (y0 > 0.5) {
+    diff = upper(x0) - upper(x1);
+  } else {
+    const double btot = exp(lgamma(a) + lgamma(b) - lgamma(a + b));
+    diff = (btot - upper(x1)) - lower(y0, r0);
+  }
+  const double T = X * tau;
+  return pow(T, 1.0 - alpha * beta) / beta * diff;
+}
+

@@ -133,13 +133,15 @@ class TGSolver:
 class ABSolver:
     """solve_and_check-style Atangana-Baleanu convection-diffusion solve."""
 
-    def __init__(self, ctx: Context, m: int, max_steps: int, tau: float, alpha: float):
+    def __init__(self, ctx: Context, m: int, max_steps: int, tau: float, alpha: float, mode: int = _lib.FH_AB_FP64):
         self.ctx = ctx
         self.m = m
         h = C.c_void_p()
         check(ctx.L.fh_ab_create(ctx.h, int(m), int(max_steps), float(tau), float(alpha), C.byref(h)), ctx.h)
         self.h = h
         ctx.adopt(self)
+        if mode != _lib.FH_AB_FP64:
+            check(ctx.L.fh_ab_set_mode(h, int(mode)), ctx.h)
 
     def close(self):
         if self.h and self.ctx.h:
