@@ -333,10 +333,13 @@ class AB1D(Workload):
     def __init__(self, ctx, args, dev, rank):
         import torch
         from theses_code_gb300 import workloads
+        from theses_code_gb300._lib import FH_AB_BLOCKED, FH_AB_FP64
         from theses_code_gb300.solvers import ABSolver
         S = args.solve_steps if args.solve_steps != 2000 else 20000
         cfg, src, bl, br, C0 = workloads.ab_1d(m=2048, alpha=0.6, tau=1e-4, seed=5 + rank)
-        self.solver = ABSolver(ctx, cfg["m"], S, cfg["tau"], cfg["alpha"])
+        self.cfg, self.src, self.bl, self.br = cfg, src, bl, br
+        self.mode = FH_AB_BLOCKED if args.mode == "blocked" else FH_AB_FP64
+        self.solver = ABSolver(ctx, cfg["m"], S, cfg["tau"], cfg["alpha"], self.mode)
         self.solver.set_source(src, bl, br)
         self.C_d = torch.as_tensor(C0, device=f"cuda:{dev}")
         self.C_h = torch.from_numpy(C0.copy()).pin_memory()
@@ -348,8 +351,42 @@ class AB1D(Workload):
         self.alg = {"history": self.alg_hist_bytes}
         self.name = f"ab1d_N2048_{S}steps"
         self.config = {"workload": self.name, "m": cfg["m"], "alpha": 0.6, "tau": 1e-4, "solve_steps": S,
-                       "source_modes": 16, "l2": "history %.0f MB" % (8 * 2050 * S / 1e6)}
-        self.kernel = "k_hist_sum<1>"
+                       "source_modes": 16, "mode": "blocked" if self.mode == FH_AB_BLOCKED else "fp64",
+                       "l2": "history %.0f MB" % (8 * 2050 * S / 1e6)}
+        self.kernel = "k_hist_sum<1>" + (" (current block) + k_far_gemm" if self.mode == FH_AB_BLOCKED else "")
+        if self.mode == FH_AB_BLOCKED:
+            # the FP64 sums cover only the entries of the current 128-step block; the
+            # tensor cores contract the older ones once per block (128 weight rows)
+            P, ppad = cfg["m"] + 1, -(-(cfg["m"] + 2) // 128) * 128
+            blocks = range(128, S, 128)
+            self.alg = {"history": sum(8.0 * ((i - 1) % 128) * P + 8.0 * P for i in range(2, S + 1)),
+                        "gemm_flops": sum(2.0 * 128 * t0 * P for t0 in blocks),
+                        "gemm_tc_flops": sum(10 * 2.0 * 128 * t0 * ppad for t0 in blocks),
+                        "gemm_bytes": sum(8.0 * t0 * ppad + 8.0 * 128 * ppad + 8.0 * 128 * t0 for t0 in blocks)}
+
+    def compare(self, ctx, stream, main_mode):
+        """One FP64-mode solve of the same inputs: relative max-norm difference."""
+        import torch
+        from theses_code_gb300._lib import FH_AB_FP64
+        from theses_code_gb300.solvers import ABSolver
+        self.solve_device()
+        got = self.solver.get_c()
+        sv = ABSolver(ctx, self.cfg["m"], self.S, self.cfg["tau"], self.cfg["alpha"], FH_AB_FP64)
+        sv.set_source(self.src, self.bl, self.br)
+        sv.set_c_device(self.C_d.data_ptr())
+        sv.calc_step(self.S)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sv.set_c_device(self.C_d.data_ptr())
+        e0.record(stream)
+        sv.calc_step(self.S)
+        e1.record(stream)
+        e1.synchronize()
+        ref = sv.get_c()
+        sv.close()
+        ms = e0.elapsed_time(e1)
+        err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+        return {main_mode: {"rel_err_vs_fp64": err}, "fp64": {"rel_err_vs_fp64": 0.0, "value": self.gps / (ms / 1e3),
+                                                             "ms_per_solve": ms}}
 
     def solve_device(self):
         self.solver.set_c_device(self.C_d.data_ptr())
@@ -462,7 +499,7 @@ def run_gb300(args):
         if n == 0 or ms <= 0:
             continue
         d = {"ms_per_solve": ms / K, "launches_per_solve": n / K, "share_of_solve": ms / tp_ms}
-        if name == "gemm":
+        if name == "gemm" and "gemm_tc_flops" in wl.alg:
             tc = wl.alg["gemm_tc_flops"] * K / (ms / 1e3) / 1e12
             d.update({"bound": "tensor", "achieved": tc, "peak": pk["bf16"], "unit": "TFLOP/s",
                       "frac": tc / pk["bf16"],
@@ -494,7 +531,8 @@ def run_gb300(args):
         "dtype": "f64", "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clk, "roofline": roofline, "kernels": kernels, "profiled_ms_per_step": tp_ms / args.steps,
     }
-    if args.config == "tg2d" and not args.no_compare and rank == 0:
+    if args.config in ("tg2d", "ab1d") and not args.no_compare and rank == 0 and \
+            (args.config == "tg2d" or args.mode == "blocked"):
         cmp = wl.compare(ctx, stream, args.mode)
         result["modes"] = cmp
         if "fp64" in cmp and "value" in cmp["fp64"]:

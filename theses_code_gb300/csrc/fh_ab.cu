@@ -38,6 +38,10 @@ struct fh_ab_solver {
   }
 };
 
+constexpr int kAbThreads = 256;
+constexpr int kAbSolveWarps = 4;  // the solve runs on four warps (one per SM sub-partition)
+constexpr int kAbSolveThreads = 32 * kAbSolveWarps;
+
 // al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
 // The matrix is fixed, so the step-independent parts of both recurrences are
 // tabulated here once: inv[j] = 1/den[j], the forward slope sl[j] = -A inv[j],
@@ -58,7 +62,7 @@ __global__ void k_ab_factor(int m, double A, double Bd, double Cc, double *__res
     inv[j] = 1.0 / d;
     sl[j] = -A * inv[j];
   }
-  const int ch = (m + 31) / 32;
+  const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
   double p = 1.0;
   for (int j = 1; j <= m; ++j) {
     p = ((j - 1) % ch == 0) ? sl[j] : p * sl[j];
@@ -82,12 +86,12 @@ __global__ void k_ab_stepweights(int i, int k0, int n, const double *__restrict_
 //   forward   bt[j] = (Rp_j - A bt[j-1]) / den_j = sl_j bt[j-1] + Rp_j inv_j
 //   backward  C[j]  = bt[j] - al[j] C[j+1],  C[m] = right boundary value
 // All threads stage the right parts and the tabulated coefficients into
-// shared memory with coalesced loads (skewed by i / chunk so that the 32
-// lanes' chunks fall on distinct banks), warp 0 walks its lanes' chunks from
-// a zero start and adds prefix * start value after a warp scan of the chunk
-// maps (fh_line_solve_prefix scheme), then all threads write C and the new
-// history entry.
-constexpr int kAbThreads = 256;
+// shared memory with coalesced loads (skewed by i / chunk so that the
+// threads' chunks fall on distinct banks), four warps (one per SM
+// sub-partition) walk their threads' chunks from a zero start and add
+// prefix * start value after a group scan of the chunk maps
+// (fh_line_solve_prefix scheme), then all threads write C and the new history
+// entry.
 __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const double *__restrict__ ii,
                                                         const double *__restrict__ alg,
                                                         const double *__restrict__ invg,
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
                                                         const float2 *__restrict__ far, double *__restrict__ Dnew,
                                                         double tau) {
   extern __shared__ double sm[];
-  const int ch = (m + 31) / 32;
+  const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
   const int Lm = m + 2 + m / ch + 1;
   double *rb = sm, *sl = rb + Lm, *pf = sl + Lm, *al = pf + Lm, *pb = al + Lm, *bt = pb + Lm, *cv = bt + Lm;
   auto sk = [ch](int j) { return j + j / ch; };
@@ -121,30 +125,33 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
     pb[sk(j)] = pbg[j];
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
+  __shared__ fh_aff scan_sm[kAbSolveWarps];
+  if (threadIdx.x < kAbSolveThreads) {
+    const int t = threadIdx.x;
     const double bl = blp[0], br = brp[0];
-    const int f0 = 1 + lane * ch, f1 = min(m + 1, f0 + ch);
+    const int f0 = 1 + t * ch, f1 = min(m + 1, f0 + ch);
     double b = 0.0;
     for (int j = f0; j < f1; ++j) {
       b = fma(sl[sk(j)], b, rb[sk(j)]);
       bt[sk(j)] = b;
     }
-    const fh_aff Pf = fh_warp_exclusive_affine(f1 > f0 ? fh_aff{pf[sk(f1 - 1)], b} : fh_aff{1.0, 0.0});
+    const fh_aff Pf =
+        fh_group_exclusive_affine<kAbSolveWarps>(f1 > f0 ? fh_aff{pf[sk(f1 - 1)], b} : fh_aff{1.0, 0.0}, scan_sm, 1);
     const double s0 = fma(Pf.a, bl, Pf.b);  // bt[f0 - 1]
     for (int j = f0; j < f1; ++j) bt[sk(j)] = fma(pf[sk(j)], s0, bt[sk(j)]);
-    if (lane == 0) bt[sk(0)] = bl;
-    __syncwarp();
-    const int b0 = lane * ch, b1 = min(m, b0 + ch);
+    if (t == 0) bt[sk(0)] = bl;
+    fh_group_bar(1, kAbSolveThreads);
+    const int b0 = t * ch, b1 = min(m, b0 + ch);
     double c = 0.0;
     for (int j = b1 - 1; j >= b0; --j) {
       c = fma(-al[sk(j)], c, bt[sk(j)]);
       cv[sk(j)] = c;
     }
-    const fh_aff Pb = fh_warp_exclusive_affine_rev(b1 > b0 ? fh_aff{pb[sk(b0)], c} : fh_aff{1.0, 0.0});
-    const double t = fma(Pb.a, br, Pb.b);  // C[b1]
-    for (int j = b0; j < b1; ++j) cv[sk(j)] = fma(pb[sk(j)], t, cv[sk(j)]);
-    if (lane == 0) cv[sk(m)] = br;
+    const fh_aff Pb = fh_group_exclusive_affine_rev<kAbSolveWarps>(b1 > b0 ? fh_aff{pb[sk(b0)], c} : fh_aff{1.0, 0.0},
+                                                                   scan_sm, 1);
+    const double tv = fma(Pb.a, br, Pb.b);  // C[b1]
+    for (int j = b0; j < b1; ++j) cv[sk(j)] = fma(pb[sk(j)], tv, cv[sk(j)]);
+    if (t == 0) cv[sk(m)] = br;
   }
   __syncthreads();
   for (int j = threadIdx.x; j <= m; j += kAbThreads) {
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
 }
 
 static size_t ab_line_smem(int m) {
-  const int ch = (m + 31) / 32;
+  const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
   return sizeof(double) * 7 * (size_t)(m + 2 + m / ch + 1);
 }
 

@@ -223,3 +223,64 @@ __device__ __forceinline__ void fh_line_solve_prefix_df(int N, const float2 *fa,
   __syncwarp();
 }
 
+// ------------------------------------------------------------------------
+// Group scans: NW warps (threads 0 .. 32 NW - 1 of the CTA) scan one chain
+// of 32 NW chunk maps; warp totals pass through shared memory sm[NW] and a
+// named barrier (id bar, the NW warps only).  The caller's threads must all
+// call with the same NW and bar.
+__device__ __forceinline__ void fh_group_bar(int bar, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+}
+
+// Thread t receives f_{t-1} o ... o f_0 (identity for thread 0).
+template <int NW>
+__device__ __forceinline__ fh_aff fh_group_exclusive_affine(fh_aff f, fh_aff *sm, int bar) {
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = threadIdx.x >> 5;
+  fh_aff g = f;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const double pa = __shfl_up_sync(0xffffffffu, g.a, d);
+    const double pb = __shfl_up_sync(0xffffffffu, g.b, d);
+    if (lane >= (unsigned)d) g = fh_aff_compose(g, fh_aff{pa, pb});
+  }
+  if (lane == 31u) sm[w] = g;
+  double ea = __shfl_up_sync(0xffffffffu, g.a, 1);
+  double eb = __shfl_up_sync(0xffffffffu, g.b, 1);
+  if (lane == 0u) {
+    ea = 1.0;
+    eb = 0.0;
+  }
+  fh_group_bar(bar, 32 * NW);
+  fh_aff P{1.0, 0.0};
+  for (int k = 0; k < w; ++k) P = fh_aff_compose(sm[k], P);
+  fh_group_bar(bar, 32 * NW);  // sm may be reused after this
+  return fh_aff_compose(fh_aff{ea, eb}, P);
+}
+
+// Thread t receives G_{t+1} o ... o G_{T-1} (identity for the last thread).
+template <int NW>
+__device__ __forceinline__ fh_aff fh_group_exclusive_affine_rev(fh_aff f, fh_aff *sm, int bar) {
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = threadIdx.x >> 5;
+  fh_aff g = f;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const double pa = __shfl_down_sync(0xffffffffu, g.a, d);
+    const double pb = __shfl_down_sync(0xffffffffu, g.b, d);
+    if (lane + d < 32u) g = fh_aff_compose(g, fh_aff{pa, pb});
+  }
+  if (lane == 0u) sm[w] = g;
+  double ea = __shfl_down_sync(0xffffffffu, g.a, 1);
+  double eb = __shfl_down_sync(0xffffffffu, g.b, 1);
+  if (lane == 31u) {
+    ea = 1.0;
+    eb = 0.0;
+  }
+  fh_group_bar(bar, 32 * NW);
+  fh_aff Q{1.0, 0.0};
+  for (int k = NW - 1; k > w; --k) Q = fh_aff_compose(sm[k], Q);
+  fh_group_bar(bar, 32 * NW);
+  return fh_aff_compose(fh_aff{ea, eb}, Q);
+}
+
