@@ -301,6 +301,7 @@ class H1D(Workload):
             S = args.solve_steps if args.solve_steps != 2000 else 500
             self.name = f"psi_batch_{args.instances}inst_{S}steps"
         self.solver = HSolverBatch(ctx, params, S + 1)
+        self.params, self.U0s = params, U0s
         flat = np.concatenate(U0s)
         self.U_d = torch.as_tensor(flat, device=f"cuda:{dev}")
         self.U_h = torch.from_numpy(flat).pin_memory()
@@ -316,6 +317,20 @@ class H1D(Workload):
                        "solve_steps": S, "state_doubles": seg,
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
         self.kernel = "k_hist_tiles"
+
+    def cpu_baseline(self):
+        """Oracle port of H_solver (serial) on a bounded sample of the instances,
+        the full step count."""
+        from oracle import oracle as O
+        sample = self.params[:1] if len(self.params) == 1 else self.params[:4]
+        t0 = time.perf_counter()
+        for p, u in zip(sample, self.U0s):
+            O.h_solve(p, u, self.S)
+        dt = time.perf_counter() - t0
+        pts = sum(p["N"] - 1 for p in sample)
+        return {"value": pts * self.S / dt, "unit": METRIC, "cores": 1, "kind": "port",
+                "sample": f"oracle H_solver port, {len(sample)} of {len(self.params)} instances, "
+                          f"{self.S} steps, {dt:.1f} s, 1 thread"}
 
     def solve_device(self):
         self.solver.set_u_device(self.U_d.data_ptr())
@@ -363,6 +378,20 @@ class AB1D(Workload):
                         "gemm_flops": sum(2.0 * 128 * t0 * P for t0 in blocks),
                         "gemm_tc_flops": sum(10 * 2.0 * 128 * t0 * ppad for t0 in blocks),
                         "gemm_bytes": sum(8.0 * t0 * ppad + 8.0 * 128 * ppad + 8.0 * 128 * t0 for t0 in blocks)}
+
+    def cpu_baseline(self):
+        """Oracle port of solve_and_check (serial) on the first 2000 of the steps
+        (shorter histories than the average step of the full solve: favours the CPU)."""
+        from oracle import oracle as O
+        n = min(self.S, 2000)
+        m = self.cfg["m"]
+        w = O.ab_weights(n, self.cfg["tau"], self.cfg["alpha"])
+        srcs = np.repeat(self.src, n, axis=0)
+        t0 = time.perf_counter()
+        O.ab_solve(m, n, self.cfg["tau"], self.cfg["alpha"], w, srcs, np.zeros(n), np.zeros(n), np.zeros(m + 1))
+        dt = time.perf_counter() - t0
+        return {"value": (m - 1) * n / dt, "unit": METRIC, "cores": 1, "kind": "port",
+                "sample": f"oracle solve_and_check port, m={m}, first {n} of {self.S} steps, {dt:.1f} s, 1 thread"}
 
     def compare(self, ctx, stream, main_mode):
         """One FP64-mode solve of the same inputs: relative max-norm difference."""
@@ -538,8 +567,8 @@ def run_gb300(args):
         if "fp64" in cmp and "value" in cmp["fp64"]:
             result["speedup_vs_plain_fp64"] = value / cmp["fp64"]["value"]
         result["rel_err_vs_fp64"] = cmp[args.mode]["rel_err_vs_fp64"]
-    if rank == 0 and not args.no_cpu_baseline and args.config == "tg2d":
-        result["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args) if args.config == "tg2d" else wl.cpu_baseline()
     if rank == 0:
         print(json.dumps(result))
     ctx.close()

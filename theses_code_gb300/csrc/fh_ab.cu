@@ -109,8 +109,15 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
   const int Lm = m + 2 + m / ch + 1;
   double *rb = sm, *sl = rb + Lm, *pf = sl + Lm, *al = pf + Lm, *pb = al + Lm, *bt = pb + Lm, *cv = bt + Lm;
   auto sk = [ch](int j) { return j + j / ch; };
-  const double cI = ii[0] / oma;  // Ii/(1-a)
-  const double ioma = 1.0 / oma, itau = 1.0 / tau;
+  // step constants computed once per CTA (FP64 divisions are scarce on this GPU)
+  __shared__ double cst[3];
+  if (threadIdx.x == 0) {
+    cst[0] = ii[0] / oma;  // Ii/(1-a)
+    cst[1] = 1.0 / oma;
+    cst[2] = 1.0 / tau;
+  }
+  __syncthreads();
+  const double cI = cst[0], ioma = cst[1], itau = cst[2];
   for (int j = threadIdx.x; j <= m; j += kAbThreads) {
     double r = fma(cI, C[j], src[j]);
     if (S || far) {  // MF_intF_simple returns ret/(1-a)

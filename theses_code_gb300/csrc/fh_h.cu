@@ -44,6 +44,7 @@ struct fh_h_batch {
 };
 
 static constexpr int kTileThreads = 256;  // 512 nodes per tile
+static constexpr int kHWeightThreads = 128;  // slots per weights CTA
 
 // ------------------------------------------------------------------ kernels
 
@@ -56,16 +57,51 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
   const int b = blockIdx.y;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const fh_h_dev_inst I = inst[b];
-  if (t < os - 1) {
+  if (I.weights == FH_W_PSI && I.beta != 1.0) {
+    // psi = t^beta: the weight of slot t is the difference of one incomplete-beta
+    // value at its two ends (fh_psi_int_tab); each node is evaluated once and
+    // shared with the neighbouring slot through shared memory
+    __shared__ double nv[kHWeightThreads + 1], sc[2];
+    __shared__ int nlow[kHWeightThreads + 1];
+    const double X = (double)(tstep + 1), a = 1.0 / I.beta, bb = 1.0 - I.alpha;
+    const double *Lc = ibt + (long long)b * 2 * kIbTerms, *Uc = Lc + kIbTerms;
+    const int t0 = blockIdx.x * blockDim.x;
+    for (int i = threadIdx.x; i <= (int)blockDim.x; i += blockDim.x) {
+      const int x = t0 + i;
+      if (x <= os - 1) {
+        const double r = (double)x / X, y = pow(r, I.beta);
+        if (y <= 0.5) {
+          nv[i] = y <= 0.0 ? 0.0 : r * fh_horner(Lc, y);
+          nlow[i] = 1;
+        } else {
+          const double c = -expm1(I.beta * log1p(((double)x - X) / X));
+          nv[i] = c <= 0.0 ? 0.0 : pow(c, bb) * fh_horner(Uc, c);
+          nlow[i] = 0;
+        }
+      }
+    }
+    if (threadIdx.x == 0) {
+      sc[0] = pow(X * I.tau, 1.0 - I.alpha * I.beta) / I.beta;
+      sc[1] = exp(lgamma(a) + lgamma(bb) - lgamma(a + bb));  // B(a, b)
+    }
+    __syncthreads();
+    if (t < os - 1) {
+      const int i = threadIdx.x;
+      double diff;
+      if (nlow[i] && nlow[i + 1])
+        diff = nv[i + 1] - nv[i];
+      else if (!nlow[i])
+        diff = nv[i] - nv[i + 1];
+      else
+        diff = (sc[1] - nv[i + 1]) - nv[i];
+      W[(long long)b * ldw + t] = t == 0 ? 0.0 : sc[0] * diff * (1 - I.alpha);
+    }
+  } else if (t < os - 1) {
     double w;
     if (t == 0)
       w = 0.0;
     else if (I.weights == FH_W_L1)
       w = Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
-    else if (I.beta != 1.0)
-      w = fh_psi_int_tab((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta,
-                         ibt + (long long)b * 2 * kIbTerms, ibt + (long long)b * 2 * kIbTerms + kIbTerms) *
-          (1 - I.alpha);
     else
       w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
     W[(long long)b * ldw + t] = w;
@@ -279,9 +315,9 @@ static int h_one_step(fh_h_batch *B) {
   const int os = B->nsaved;
   const int K = os >= 2 ? os - 1 : 0;
   int rc;
-  dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, 128), (unsigned)B->n);
+  dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, kHWeightThreads), (unsigned)B->n);
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
-  k_h_weights<<<gw, 128, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
+  k_h_weights<<<gw, kHWeightThreads, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
                                            B->max_weights, B->wc.as<double>(), B->Lb.as<double>(),
                                            B->ibt.as<double>());
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);

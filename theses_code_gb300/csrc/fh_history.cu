@@ -178,16 +178,18 @@ int fh_launch_hist_sum_df_partials(fh_ctx *ctx, int M, int K, long long P, const
                                    const float2 *D, long long ldd, int splits, int kchunk, double *part,
                                    long long ldpart, const float2 *far, long long ldfar, int pair_out) {
   if (K <= 0 || P <= 0) return FH_OK;
-  dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
+  // short sums are a single wave: smaller CTAs even out the load per SM
+  const int threads = K <= 64 ? kHistThreads / 2 : kHistThreads;
+  dim3 grid((unsigned)fh_ceil_div(P, 2LL * threads), (unsigned)splits);
   const size_t smem = sizeof(float2) * (size_t)M * (size_t)kchunk;
   FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large (%d layers)", kchunk);
   fh_prof_mark(ctx, FH_PROF_HISTORY, false);
   if (M == 1)
-    k_hist_sum_df<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
-                                                                  ldfar, pair_out);
+    k_hist_sum_df<1><<<grid, threads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far, ldfar,
+                                                             pair_out);
   else
-    k_hist_sum_df<2><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far,
-                                                                  ldfar, pair_out);
+    k_hist_sum_df<2><<<grid, threads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart, far, ldfar,
+                                                             pair_out);
   fh_prof_mark(ctx, FH_PROF_HISTORY, true);
   return fh_after_launch(ctx, "k_hist_sum_df");
 }

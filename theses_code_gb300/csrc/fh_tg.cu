@@ -383,55 +383,66 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 
   const int line0 = 1 + blockIdx.x * kXLines;
   const int N = g.sN;
   const int L = tg_line_stride(N);
-  const fh_df kst = fh_df_from_double(-g.st * (cw[0] + 0.0)), S2 = fh_df_from_double(g.S * 0.5),
-              st = fh_df_from_double(g.st);
-  {
-    const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
-    const int line = line0 + ln;
-    float2 *fa = sbf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
-    const long long base = (long long)line * g.ld;
-    for (int r0 = 1; line < g.M && r0 < N; r0 += kXGroup * kUnroll) {
-      float2 c[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
-      fh_df ts[kUnroll];
+  const int ln = threadIdx.x / kXGroup, tg = threadIdx.x % kXGroup;
+  const int line = line0 + ln;
+  const bool live = line < g.M;
+  float2 *fa = sbf + (size_t)ln * 5 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L;
+  const long long base = (long long)line * g.ld;
+  // factor tables first; the pivot factor waits in the fb slot until the
+  // right part is known
+  if (live) {
+    for (int i = 1 + tg; i < N; i += kXGroup) {
+      const long long id = base + i;
+      fa[fh_sk(i)] = fax[id];
+      fb[fh_sk(i)] = gx[id];
+      al[fh_sk(i)] = alx[id];
+      pf[fh_sk(i)] = pfx[id];
+      pb[fh_sk(i)] = pbx[id];
+    }
+    if (tg == 0) pb[fh_sk(0)] = pbx[base];
+  }
+  // step constants as double-float, split once per CTA (FP64 instructions are
+  // scarce on this GPU: one per thread would stall every warp at the start)
+  __shared__ float2 cst[4];
+  if (threadIdx.x == 0) {
+    cst[0] = fh_df_pair(fh_df_from_double(-g.st * (cw[0] + 0.0)));
+    cst[1] = fh_df_pair(fh_df_from_double(g.S * 0.5));
+    cst[2] = fh_df_pair(fh_df_from_double(g.st));
+    cst[3] = fh_df_pair(fh_df_from_double(g.C1));
+  }
+  __syncthreads();
+  const fh_df kst = fh_df_from_pair(cst[0]), S2 = fh_df_from_pair(cst[1]), st = fh_df_from_pair(cst[2]);
+  for (int r0 = 1; live && r0 < N; r0 += kXGroup * kUnroll) {
+    float2 c[kUnroll];
+    fh_df ts[kUnroll];
+#pragma unroll
+    for (int e = 0; e < kUnroll; ++e) {
+      const int i = r0 + tg + e * kXGroup;
+      const long long id = base + (i < N ? i : 1);
+      c[e] = Cd[id];
+      ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+    }
+    for (int s = 0; s < splits; ++s)
 #pragma unroll
       for (int e = 0; e < kUnroll; ++e) {
         const int i = r0 + tg + e * kXGroup;
-        const long long id = base + (i < N ? i : 1);
-        c[e] = Cd[id];
-        a[e] = fax[id];
-        gi[e] = gx[id];
-        l[e] = alx[id];
-        qf[e] = pfx[id];
-        qb[e] = pbx[id];
-        ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+        ts[e] = fh_df_add(ts[e], fh_df_from_pair(part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)]));
       }
-      for (int s = 0; s < splits; ++s)
 #pragma unroll
-        for (int e = 0; e < kUnroll; ++e) {
-          const int i = r0 + tg + e * kXGroup;
-          ts[e] = fh_df_add(ts[e], fh_df_from_pair(part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)]));
-        }
-#pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int i = r0 + tg + e * kXGroup;
-        if (i < N) {
-          fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
-          om = fh_df_fma(st, ts[e], om);
-          fa[fh_sk(i)] = a[e];
-          fb[fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(gi[e]), om)));
-          al[fh_sk(i)] = l[e];
-          pf[fh_sk(i)] = qf[e];
-          pb[fh_sk(i)] = qb[e];
-        }
+    for (int e = 0; e < kUnroll; ++e) {
+      const int i = r0 + tg + e * kXGroup;
+      if (i < N) {
+        fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
+        om = fh_df_fma(st, ts[e], om);
+        fb[fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(fb[fh_sk(i)]), om)));
       }
     }
-    if (tg == 0 && line < g.M) pb[fh_sk(0)] = pbx[base];
   }
   __syncthreads();
   if (warp < kXLines && line0 + warp < g.M) {
     float2 *fa = sbf + (size_t)warp * 5 * L;
     fh_line_solve_prefix_df(N, fa, fa + L, fa + 2 * L, fa + 3 * L, fa + 4 * L, fh_df{0.f, 0.f},
-                            fh_df_from_double(g.C1), fa + L, fa);
+                            fh_df_from_pair(cst[3]), fa + L, fa);
   }
   __syncthreads();
   {
@@ -462,51 +473,61 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
   const int N = g.M;
   const int L = tg_line_stride(N);
   const int i0 = 1 + blockIdx.x * 4;
-  const fh_df kst = fh_df_from_double(-g.st * (cw[1] + 0.0)), kyh = fh_df_from_double(cw[2] + 0.0),
-              S2 = fh_df_from_double(g.S * 0.5), st = fh_df_from_double(g.st);
   const int col = threadIdx.x & 3;
   const int rg = threadIdx.x >> 2;  // row group 0..127
   constexpr int kRows = kYThreads / 4;
   const int line = i0 + col;
   const bool live = line < g.sN;
   float2 *fa = sbf + (size_t)col * 6 * L, *fb = fa + L, *al = fb + L, *pf = al + L, *pb = pf + L, *cf = pb + L;
-  for (int r0 = 1; r0 < N; r0 += kRows * kUnroll) {
-    float2 c[kUnroll], f[kUnroll], a[kUnroll], gi[kUnroll], l[kUnroll], qf[kUnroll], qb[kUnroll];
+  // factor tables first; the pivot factor waits in the fb slot (see k_tg_xsweep_df)
+  if (live) {
+    for (int q = 1 + rg; q < N; q += kRows) {
+      const long long id = line + (long long)q * g.ld;
+      fa[fh_sk(q)] = fay[id];
+      fb[fh_sk(q)] = gy[id];
+      al[fh_sk(q)] = aly[id];
+      pf[fh_sk(q)] = pfy[id];
+      pb[fh_sk(q)] = pby[id];
+    }
+  }
+  __shared__ float2 cst[4];  // step constants, split once per CTA (see k_tg_xsweep_df)
+  if (threadIdx.x == 0) {
+    cst[0] = fh_df_pair(fh_df_from_double(-g.st * (cw[1] + 0.0)));
+    cst[1] = fh_df_pair(fh_df_from_double(cw[2] + 0.0));
+    cst[2] = fh_df_pair(fh_df_from_double(g.S * 0.5));
+    cst[3] = fh_df_pair(fh_df_from_double(g.st));
+  }
+  __syncthreads();
+  const fh_df kst = fh_df_from_pair(cst[0]), kyh = fh_df_from_pair(cst[1]), S2 = fh_df_from_pair(cst[2]),
+              st = fh_df_from_pair(cst[3]);
+  for (int r0 = 1; live && r0 < N; r0 += kRows * kUnroll) {
+    float2 c[kUnroll], f[kUnroll];
     fh_df ts[kUnroll];
 #pragma unroll
     for (int e = 0; e < kUnroll; ++e) {
       const int q = r0 + rg + e * kRows;
-      const long long id = (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld;
+      const long long id = line + (long long)(q < N ? q : 1) * g.ld;
       c[e] = Chd[id];
       f[e] = Cd[id];
-      a[e] = fay[id];
-      gi[e] = gy[id];
-      l[e] = aly[id];
-      qf[e] = pfy[id];
-      qb[e] = pby[id];
       ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
     }
     for (int s = 0; s < splits; ++s)
 #pragma unroll
       for (int e = 0; e < kUnroll; ++e) {
         const int q = r0 + rg + e * kRows;
-        ts[e] = fh_df_add(
-            ts[e], fh_df_from_pair(part[(long long)(2 * s + 1) * ldp + (live ? line : 1) + (long long)(q < N ? q : 1) * g.ld]));
+        ts[e] = fh_df_add(ts[e],
+                          fh_df_from_pair(part[(long long)(2 * s + 1) * ldp + line + (long long)(q < N ? q : 1) * g.ld]));
       }
 #pragma unroll
     for (int e = 0; e < kUnroll; ++e) {
       const int q = r0 + rg + e * kRows;
-      if (live && q < N) {
+      if (q < N) {
         const fh_df cc = fh_df_from_pair(c[e]);
         // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
         const fh_df t = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), ts[e]);
         fh_df om = fh_df_fma(kst, cc, S2);
         om = fh_df_fma(st, t, om);
-        fa[fh_sk(q)] = a[e];
-        fb[fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(gi[e]), om)));
-        al[fh_sk(q)] = l[e];
-        pf[fh_sk(q)] = qf[e];
-        pb[fh_sk(q)] = qb[e];
+        fb[fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(fb[fh_sk(q)]), om)));
         cf[fh_sk(q)] = f[e];
       }
     }
