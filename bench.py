@@ -300,7 +300,11 @@ class H1D(Workload):
             params, U0s = workloads.psi_batch(n=args.instances, seed=7 + rank)
             S = args.solve_steps if args.solve_steps != 2000 else 500
             self.name = f"psi_batch_{args.instances}inst_{S}steps"
-        self.solver = HSolverBatch(ctx, params, S + 1)
+        from theses_code_gb300._lib import FH_H_DF64, FH_H_FP64
+        # the batch keeps its history as double-float pairs (plain-path accuracy,
+        # HBM-bound sums) unless --mode fp64; the single cfg-1 instance stays FP64
+        self.hmode = FH_H_FP64 if (args.mode == "fp64" or kind == "caputo1d") else FH_H_DF64
+        self.solver = HSolverBatch(ctx, params, S + 1, self.hmode)
         self.params, self.U0s = params, U0s
         flat = np.concatenate(U0s)
         self.U_d = torch.as_tensor(flat, device=f"cuda:{dev}")
@@ -315,8 +319,9 @@ class H1D(Workload):
         self.alg = {"history": self.alg_hist_bytes}
         self.config = {"workload": self.name, "instances": len(params), "interior_points": npts,
                        "solve_steps": S, "state_doubles": seg,
+                       "history": "fp64" if self.hmode == FH_H_FP64 else "double-float pairs",
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
-        self.kernel = "k_hist_tiles"
+        self.kernel = "k_hist_tiles" if self.hmode == FH_H_FP64 else "k_hist_tiles_df"
 
     def cpu_baseline(self):
         """Oracle port of H_solver (serial) on a bounded sample of the instances,

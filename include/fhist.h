@@ -191,6 +191,13 @@ int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_h
 /* H_solver::calc_step repeated nsteps times (tstep starts at 1). */
 int fh_h_batch_step(fh_h_batch *b, int nsteps);
 int fh_h_batch_tstep(const fh_h_batch *b);
+/* History storage, before the first step: FH_H_FP64 (default) or FH_H_DF64
+ * ((hi, lo) FP32 pairs summed in double-float on the FP32 pipe, 2^-48
+ * relative storage precision; solution within 1e-12 of the FP64 path on the
+ * parity cases).  No counterpart in the reference. */
+#define FH_H_FP64 0
+#define FH_H_DF64 1
+int fh_h_batch_set_mode(fh_h_batch *b, int mode);
 
 /* ------------------------------------------------------ 2D TG_solver ADI */
 typedef struct {

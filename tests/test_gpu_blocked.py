@@ -90,3 +90,46 @@ def test_ab_blocked_mode_vs_oracle(ctx, n):
     err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     print(f"AB blocked {n} steps: rel max-norm err {err:.3e}")
     assert err <= 1e-9, err
+
+
+def test_full_size_modes_agree(ctx):
+    """The benchmark workload (512 x 512, 2000 steps) at full size: the blocked
+    and double-float modes against the plain FP64 path, which the oracle pins
+    at 1e-12 on the smaller parity cases (a size-independent cross-check)."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FH_TG_DF64, FH_TG_FP64
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(512, 512, alpha=0.7, tau=5e-4, d=0.1, seed=11)
+    out = {}
+    for mode in (FH_TG_FP64, FH_TG_DF64, FH_TG_BLOCKED):
+        s = TGSolver(ctx, p, 2000, mode)
+        s.set_state(V2, C0)
+        s.calc_step(2000)
+        out[mode] = s.get_c()
+        s.close()
+    ref = out[FH_TG_FP64]
+    den = np.max(np.abs(ref))
+    e_df = np.max(np.abs(out[FH_TG_DF64] - ref)) / den
+    e_blk = np.max(np.abs(out[FH_TG_BLOCKED] - ref)) / den
+    print(f"512^2 x 2000: df64 {e_df:.3e}, blocked {e_blk:.3e}")
+    assert np.isfinite(out[FH_TG_BLOCKED]).all()
+    assert e_df <= 1e-12 and e_blk <= 1e-9, (e_df, e_blk)
+
+
+def test_contract_large_vs_torch_fp64(ctx):
+    """Exact-slice contraction at a size beyond the CPU oracle's reach, against
+    torch's FP64 matmul on the GPU (2e-8 of sum |W||D|)."""
+    import torch
+    K, P = 1024, 300000
+    g = torch.Generator(device="cuda").manual_seed(5)
+    W = torch.rand((128, K), dtype=torch.float64, device="cuda", generator=g) * torch.exp(
+        -torch.arange(K, device="cuda", dtype=torch.float64) / 300.0)
+    D = torch.randn((K, P), dtype=torch.float64, device="cuda", generator=g) * 1e-3
+    S = torch.empty((128, P), dtype=torch.float64, device="cuda")
+    ctx.call("fh_history_contract_bf16", K, P, W.data_ptr(), K, D.data_ptr(), P, S.data_ptr(), P)
+    ctx.sync()
+    ref = W @ D
+    scale = W.abs() @ D.abs()
+    err = float(((S - ref).abs() / scale).max())
+    print(f"K={K} P={P} max rel err {err:.3e}")
+    assert err <= 2e-8, err

@@ -249,6 +249,27 @@ def test_h_solver_psi_batch_vs_oracle(ctx):
         assert relmax(g, ref) <= 1e-11, (p["alpha"], p["beta"])
 
 
+def test_h_solver_df64_history_vs_oracle(ctx):
+    """History stored as (hi, lo) FP32 pairs and summed in double-float: the
+    plain-path bounds still hold (1e-12 for L1, 1e-11 for the psi batch)."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_H_DF64
+    from theses_code_gb300.solvers import HSolverBatch
+    p, U0 = workloads.caputo_1d(200, 0.8, 1.0, 1e-3)
+    s = HSolverBatch(ctx, [p], 301, FH_H_DF64)
+    s.set_u([U0])
+    s.calc_step(300)
+    ref, _ = O.h_solve(p, U0, 300)
+    assert relmax(s.get_u()[0], ref) <= TOL_SOLVER
+    params, U0s = workloads.psi_batch(n=6, seed=3, Nmin=17, Nmax=90, tau=2e-3)
+    s = HSolverBatch(ctx, params, 61, FH_H_DF64)
+    s.set_u(U0s)
+    s.calc_step(60)
+    for q, u0, g in zip(params, U0s, s.get_u()):
+        ref, _ = O.h_solve(q, u0, 60)
+        assert relmax(g, ref) <= 1e-11, (q["alpha"], q["beta"])
+
+
 def test_h_solver_history_full_is_reported(ctx):
     from theses_code_gb300 import workloads
     from theses_code_gb300._lib import FhError
@@ -305,6 +326,20 @@ def test_tg_solvers_of_different_sizes_coexist(ctx):
     assert relmax(small.get_c(), ref) <= TOL_SOLVER
     big.close()
     small.close()
+
+
+def test_size_limits_are_reported(ctx):
+    """Sizes beyond what the staged sweeps and lines hold are refused with
+    FH_EINVAL instead of being launched."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FhError
+    from theses_code_gb300.solvers import ABSolver, TGSolver
+    p, _, _ = workloads.convection_2d(40, 40)
+    p["M"] = 2000
+    with pytest.raises(FhError):
+        TGSolver(ctx, p, 10)
+    with pytest.raises(FhError):
+        ABSolver(ctx, 4000, 10, 1e-3, 0.5)
 
 
 def test_tg_psi_beta_vs_oracle(ctx):

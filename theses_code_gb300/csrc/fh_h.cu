@@ -16,6 +16,7 @@
 #include "fh_internal.h"
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
+#include "fh_df.cuh"
 #include "fh_weights.cuh"
 
 struct fh_h_dev_inst {
@@ -41,6 +42,7 @@ struct fh_h_batch {
   fh_dbuf inst, tl, U, D, W, Lb, ibt, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
+  int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
 };
 
 static constexpr int kTileThreads = 256;  // 512 nodes per tile
@@ -178,8 +180,64 @@ __global__ void __launch_bounds__(kTileThreads) k_hist_tiles(const fh_h_tile *__
   *reinterpret_cast<double2 *>(part + (long long)s * ldpart + p) = o;
 }
 
+// Double-float history ((hi, lo) FP32 pairs): the same tile sum with the
+// weights split into pairs in shared memory and the sums carried in
+// double-float on the FP32 pipe (2^-48 storage precision, HBM-bound).
+__global__ void __launch_bounds__(kTileThreads) k_hist_tiles_df(const fh_h_tile *__restrict__ tiles,
+                                                                const fh_h_dev_inst *__restrict__ inst,
+                                                                const float2 *__restrict__ D, long long ldd, int K,
+                                                                const double *__restrict__ W, int ldw, int kchunk,
+                                                                double *__restrict__ part, long long ldpart) {
+  extern __shared__ float2 wsf2[];
+  const fh_h_tile T = tiles[blockIdx.x];
+  const int s = blockIdx.y;
+  const int k0 = s * kchunk;
+  const int nk = min(K, k0 + kchunk) - k0;
+  const double *wrow = W + (long long)T.inst * ldw + k0;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) wsf2[i] = fh_df_pair(fh_df_from_double(wrow[i]));
+  __syncthreads();
+  const int q = threadIdx.x * 2;
+  if (q >= T.len) return;
+  const long long p = inst[T.inst].off + T.start + q;
+  fh_df a0{0.f, 0.f}, a1{0.f, 0.f};
+  const float4 *d = reinterpret_cast<const float4 *>(D + (long long)k0 * ldd + p);
+  const long long ld4 = ldd / 2;
+  int k = 0;
+  for (; k + 4 <= nk; k += 4) {
+    float4 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = __ldcs(d + u * ld4);
+    d += 4 * ld4;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const fh_df w = fh_df_from_pair(wsf2[k + u]);
+      a0 = fh_df_fma(w, fh_df{v[u].x, v[u].y}, a0);
+      a1 = fh_df_fma(w, fh_df{v[u].z, v[u].w}, a1);
+    }
+  }
+  for (; k < nk; ++k) {
+    const float4 v = __ldcs(d);
+    d += ld4;
+    const fh_df w = fh_df_from_pair(wsf2[k]);
+    a0 = fh_df_fma(w, fh_df{v.x, v.y}, a0);
+    a1 = fh_df_fma(w, fh_df{v.z, v.w}, a1);
+  }
+  double2 o;
+  o.x = fh_df_to_double(a0);
+  o.y = fh_df_to_double(a1);
+  *reinterpret_cast<double2 *>(part + (long long)s * ldpart + p) = o;
+}
+
 __device__ __forceinline__ double fh_h_K(const fh_h_dev_inst &I, double u) {
   return I.kmodel == FH_K_CONST ? I.kc : I.kc * exp(I.kgam * u);
+}
+
+// New history entry: FP64, or a (hi, lo) FP32 pair in the double-float mode.
+__device__ __forceinline__ void fh_h_store_diff(double *D, long long i, double d, int dfstore) {
+  if (dfstore)
+    reinterpret_cast<float2 *>(D)[i] = fh_df_pair(fh_df_from_double(d));
+  else
+    D[i] = d;
 }
 
 // H_solver::U1 with one warp per instance (al1, Om1, bt1, bottom Dirichlet,
@@ -197,7 +255,8 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
                                                      double *__restrict__ Al, double *__restrict__ Bt,
                                                      double *__restrict__ sA, double *__restrict__ sB,
                                                      double *__restrict__ sR, double *__restrict__ sOm,
-                                                     double *__restrict__ Dnew, int append, int first) {
+                                                     double *__restrict__ Dnew, int append, int first,
+                                                     int dfstore) {
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (b >= n) return;  // whole warp
@@ -295,15 +354,15 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     un = Al[o + i + 1] * un + Bt[o + i + 1];
     const double old = u[i];
     u[i] = un;
-    if (append) Dnew[o + i] = un - old;
+    if (append) fh_h_store_diff(Dnew, o + i, un - old, dfstore);
   }
   if (lane == 0) {
     const double oldN = u[N], oldG = u[N + 1];
     u[N] = uN;
     u[N + 1] = uN;
     if (append) {
-      Dnew[o + N] = uN - oldN;
-      Dnew[o + N + 1] = uN - oldG;
+      fh_h_store_diff(Dnew, o + N, uN - oldN, dfstore);
+      fh_h_store_diff(Dnew, o + N + 1, uN - oldG, dfstore);
     }
   }
 }
@@ -330,9 +389,14 @@ static int h_one_step(fh_h_batch *B) {
     const size_t smem = sizeof(double) * (size_t)kchunk;
     FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
     fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-    k_hist_tiles<<<g, kTileThreads, smem, ctx->stream>>>(B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
-                                                         B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
-                                                         B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+    if (B->mode == FH_H_DF64)
+      k_hist_tiles_df<<<g, kTileThreads, smem, ctx->stream>>>(  // float2 weights: same bytes as FP64
+          B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), reinterpret_cast<const float2 *>(B->D.as<double>()),
+          B->Ptot, K, B->W.as<double>(), B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+    else
+      k_hist_tiles<<<g, kTileThreads, smem, ctx->stream>>>(B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
+                                                           B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
+                                                           B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
     fh_prof_mark(ctx, FH_PROF_HISTORY, true);
     if ((rc = fh_after_launch(ctx, "k_hist_tiles"))) return rc;
     if (splits > 2) {  // fold the partial sums into split 0 (in split order)
@@ -347,7 +411,7 @@ static int h_one_step(fh_h_batch *B) {
   k_h_line_warp<<<(unsigned)fh_ceil_div(B->n, 4), 128, 0, ctx->stream>>>(
       B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wc.as<double>(), B->part.as<double>(), B->Ptot,
       splits, B->Al.as<double>(), B->Bt.as<double>(), B->sA.as<double>(), B->sB.as<double>(), B->sR.as<double>(),
-      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0);
+      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0, B->mode == FH_H_DF64 ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_h_line_warp"))) return rc;
   B->nsaved++;
@@ -547,5 +611,15 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
 }
 
 int fh_h_batch_tstep(const fh_h_batch *b) { return b ? b->tstep : -1; }
+
+int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, mode == FH_H_FP64 || mode == FH_H_DF64, FH_EINVAL, "fh_h_batch_set_mode: unknown mode %d", mode);
+  FH_REQUIRE(ctx, b->nsaved == 0, FH_EINVAL, "fh_h_batch_set_mode: only before the first step");
+  b->mode = mode;
+  b->graph.reset();
+  return FH_OK;
+}
 
 }  // extern "C"

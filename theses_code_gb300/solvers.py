@@ -24,7 +24,7 @@ def _hptr(a: np.ndarray) -> int:
 class HSolverBatch:
     """A batch of H_solver instances advanced in lock step (calc_step)."""
 
-    def __init__(self, ctx: Context, params: list[dict], max_steps: int):
+    def __init__(self, ctx: Context, params: list[dict], max_steps: int, mode: int = _lib.FH_H_FP64):
         self.ctx = ctx
         self.params = [HParams(**p) for p in params]
         arr = (HParams * len(params))(*self.params)
@@ -32,6 +32,8 @@ class HSolverBatch:
         check(ctx.L.fh_h_batch_create(ctx.h, len(params), arr, int(max_steps), C.byref(h)), ctx.h)
         self.h = h
         ctx.adopt(self)
+        if mode != _lib.FH_H_FP64:
+            check(ctx.L.fh_h_batch_set_mode(h, int(mode)), ctx.h)
         self.sizes = [p.N + 2 for p in self.params]
         self.total = int(ctx.L.fh_h_batch_state_size(h))
 
