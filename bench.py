@@ -305,6 +305,7 @@ class H1D(Workload):
         # HBM-bound sums) unless --mode fp64; the single cfg-1 instance stays FP64
         self.hmode = FH_H_FP64 if (args.mode == "fp64" or kind == "caputo1d") else FH_H_DF64
         self.solver = HSolverBatch(ctx, params, S + 1, self.hmode)
+        self.tuned = self.solver.autotune() if kind == "psi_batch" else None
         self.params, self.U0s = params, U0s
         flat = np.concatenate(U0s)
         self.U_d = torch.as_tensor(flat, device=f"cuda:{dev}")
@@ -320,6 +321,7 @@ class H1D(Workload):
         self.config = {"workload": self.name, "instances": len(params), "interior_points": npts,
                        "solve_steps": S, "state_doubles": seg,
                        "history": "fp64" if self.hmode == FH_H_FP64 else "double-float pairs",
+                       "launch_shape": self.tuned,
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
         self.kernel = "k_hist_tiles" if self.hmode == FH_H_FP64 else "k_hist_tiles_df"
 

@@ -198,6 +198,12 @@ int fh_h_batch_tstep(const fh_h_batch *b);
 #define FH_H_FP64 0
 #define FH_H_DF64 1
 int fh_h_batch_set_mode(fh_h_batch *b, int mode);
+/* Launch-shape autotuner for the batch history sum: times the candidate tile
+ * CTAs (128/256/512 threads) x K-split caps (1/8/64) on the batch's buffers
+ * and keeps the fastest; *best_ms (optional) receives its time per launch.
+ * Not during a stream capture.  No counterpart in the reference. */
+int fh_h_batch_autotune(fh_h_batch *b, float *best_ms);
+int fh_h_batch_launch_shape(const fh_h_batch *b, int *tile_threads, int *split_cap);
 
 /* ------------------------------------------------------ 2D TG_solver ADI */
 typedef struct {

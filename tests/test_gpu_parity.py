@@ -270,6 +270,22 @@ def test_h_solver_df64_history_vs_oracle(ctx):
         assert relmax(g, ref) <= 1e-11, (q["alpha"], q["beta"])
 
 
+def test_h_batch_autotune_keeps_results(ctx):
+    """The launch-shape autotuner changes only how the history sum is tiled:
+    the batch still matches the oracle afterwards."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=40, seed=5, Nmin=17, Nmax=300, tau=2e-3)
+    s = HSolverBatch(ctx, params, 81)
+    shape = s.autotune()
+    assert shape["tile_threads"] in (128, 256, 512) and shape["split_cap"] in (1, 8, 64)
+    s.set_u(U0s)
+    s.calc_step(80)
+    for q, u0, g in list(zip(params, U0s, s.get_u()))[:5]:
+        ref, _ = O.h_solve(q, u0, 80)
+        assert relmax(g, ref) <= 1e-11
+
+
 def test_h_solver_history_full_is_reported(ctx):
     from theses_code_gb300 import workloads
     from theses_code_gb300._lib import FhError

@@ -86,6 +86,8 @@ _SIGS = {
     "fh_ab_step": (_i, [_vp, _i]),
     "fh_ab_set_mode": (_i, [_vp, _i]),
     "fh_h_batch_set_mode": (_i, [_vp, _i]),
+    "fh_h_batch_autotune": (_i, [_vp, C.POINTER(C.c_float)]),
+    "fh_h_batch_launch_shape": (_i, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fh_ab_get_c_host": (_i, [_vp, _dp]),
 }
 

@@ -35,17 +35,23 @@ struct fh_h_tile {
 struct fh_h_batch {
   fh_ctx *ctx = nullptr;
   int n = 0, max_steps = 0, tstep = 1, nsaved = 0, max_splits = 64, max_weights = 0;
+  // history-sum launch shape (fh_h_batch_autotune): threads per tile CTA (two
+  // nodes each) and the cap on K splits; one tile list per candidate shape
+  int tile_threads = 256, split_cap = 64;
+  std::vector<fh_h_tile> tiles_by[3];
+  fh_dbuf tl_by[3];
   long long Ptot = 0;
   std::vector<fh_h_params> hp;
   std::vector<long long> off;
-  std::vector<fh_h_tile> tiles;
-  fh_dbuf inst, tl, U, D, W, Lb, ibt, wc, part, Al, Bt, sA, sB, sR, sOm;
+  fh_dbuf inst, U, D, W, Lb, ibt, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
   int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
 };
 
-static constexpr int kTileThreads = 256;  // 512 nodes per tile
+static constexpr int kTileThreads = 512;  // largest tile CTA (1024 nodes)
+static constexpr int kTileShapes[3] = {128, 256, 512};  // candidate tile CTAs
+static inline int tile_shape_index(int threads) { return threads == 128 ? 0 : threads == 256 ? 1 : 2; }
 static constexpr int kHWeightThreads = 128;  // slots per weights CTA
 
 // ------------------------------------------------------------------ kernels
@@ -369,6 +375,20 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
 
 // ------------------------------------------------------------------- host
 
+// K splits of the batch history sum: enough CTAs for ~3 waves of 8 resident
+// CTAs on 152 SMs, at least 32 layers per split, at most `cap` splits.
+static void h_plan(size_t ntiles, int K, int cap, int *splits, int *kchunk) {
+  const long long target = 3LL * 152 * 8;
+  int s = (int)fh_ceil_div(target, (long long)(ntiles > 0 ? ntiles : 1));
+  if (s > cap) s = cap;
+  if (s > K / 32) s = K / 32;
+  if (s < 1) s = 1;
+  int kc = (int)fh_ceil_div(K, s);
+  kc = (int)fh_ceil_div(kc, 4) * 4;
+  *splits = (int)fh_ceil_div(K, kc);
+  *kchunk = kc;
+}
+
 static int h_one_step(fh_h_batch *B) {
   fh_ctx *ctx = B->ctx;
   const int os = B->nsaved;
@@ -383,18 +403,18 @@ static int h_one_step(fh_h_batch *B) {
   if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
   int splits = 0, kchunk = 0;
   if (K > 0) {
-    fh_hist_plan(B->Ptot, K, B->max_splits, &splits, &kchunk);
-    // tiles are per instance: keep the CTA count close to the generic plan
-    dim3 g((unsigned)B->tiles.size(), (unsigned)splits);
+    const int ti = tile_shape_index(B->tile_threads);
+    h_plan(B->tiles_by[ti].size(), K, B->split_cap, &splits, &kchunk);
+    dim3 g((unsigned)B->tiles_by[ti].size(), (unsigned)splits);
     const size_t smem = sizeof(double) * (size_t)kchunk;
     FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
     fh_prof_mark(ctx, FH_PROF_HISTORY, false);
     if (B->mode == FH_H_DF64)
-      k_hist_tiles_df<<<g, kTileThreads, smem, ctx->stream>>>(  // float2 weights: same bytes as FP64
-          B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), reinterpret_cast<const float2 *>(B->D.as<double>()),
+      k_hist_tiles_df<<<g, B->tile_threads, smem, ctx->stream>>>(  // float2 weights: same bytes as FP64
+          B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), reinterpret_cast<const float2 *>(B->D.as<double>()),
           B->Ptot, K, B->W.as<double>(), B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
     else
-      k_hist_tiles<<<g, kTileThreads, smem, ctx->stream>>>(B->tl.as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
+      k_hist_tiles<<<g, B->tile_threads, smem, ctx->stream>>>(B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
                                                            B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
                                                            B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
     fh_prof_mark(ctx, FH_PROF_HISTORY, true);
@@ -463,14 +483,19 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     I.u_right = p.u_right;
     B->off.push_back(off);
     const int seg = ((p.N + 2) + 1) & ~1;
-    for (int st = 0; st < seg; st += 2 * kTileThreads) B->tiles.push_back({b, st, seg - st < 2 * kTileThreads ? seg - st : 2 * kTileThreads});
+    for (int k = 0; k < 3; ++k) {
+      const int tn = 2 * kTileShapes[k];
+      for (int st = 0; st < seg; st += tn) B->tiles_by[k].push_back({b, st, seg - st < tn ? seg - st : tn});
+    }
     off += seg;
   }
   B->Ptot = off;
   int rc;
   const size_t st = sizeof(double) * (size_t)B->Ptot;
   if ((rc = fh_alloc(ctx, B->inst, sizeof(fh_h_dev_inst) * ninst, false)) ||
-      (rc = fh_alloc(ctx, B->tl, sizeof(fh_h_tile) * B->tiles.size(), false)) || (rc = fh_alloc(ctx, B->U, st)) ||
+      (rc = fh_alloc(ctx, B->tl_by[0], sizeof(fh_h_tile) * B->tiles_by[0].size(), false)) ||
+      (rc = fh_alloc(ctx, B->tl_by[1], sizeof(fh_h_tile) * B->tiles_by[1].size(), false)) ||
+      (rc = fh_alloc(ctx, B->tl_by[2], sizeof(fh_h_tile) * B->tiles_by[2].size(), false)) || (rc = fh_alloc(ctx, B->U, st)) ||
       (rc = fh_alloc(ctx, B->Al, st)) || (rc = fh_alloc(ctx, B->Bt, st)) || (rc = fh_alloc(ctx, B->sA, st)) ||
       (rc = fh_alloc(ctx, B->sB, st)) || (rc = fh_alloc(ctx, B->sR, st)) || (rc = fh_alloc(ctx, B->sOm, st)) ||
       (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
@@ -483,7 +508,10 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     return rc;
   }
   cudaError_t e1 = cudaMemcpyAsync(B->inst.p, di.data(), sizeof(fh_h_dev_inst) * ninst, cudaMemcpyHostToDevice, ctx->stream);
-  cudaError_t e2 = cudaMemcpyAsync(B->tl.p, B->tiles.data(), sizeof(fh_h_tile) * B->tiles.size(), cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e2 = cudaSuccess;
+  for (int k = 0; k < 3 && e2 == cudaSuccess; ++k)
+    e2 = cudaMemcpyAsync(B->tl_by[k].p, B->tiles_by[k].data(), sizeof(fh_h_tile) * B->tiles_by[k].size(),
+                         cudaMemcpyHostToDevice, ctx->stream);
   cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     delete B;
@@ -611,6 +639,76 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
 }
 
 int fh_h_batch_tstep(const fh_h_batch *b) { return b ? b->tstep : -1; }
+
+// Times the batch history sum for every candidate launch shape (tile CTA of
+// 128/256/512 threads, K split cap 1/8/64) at a probe depth of
+// min(max_steps - 1, 512) layers on the batch's own buffers (history contents
+// do not change the timing) and keeps the fastest.
+int fh_h_batch_autotune(fh_h_batch *b, float *best_ms) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, !ctx->capturing, FH_EINVAL, "fh_h_batch_autotune: not during a capture");
+  const int K = b->max_steps - 1 < 512 ? b->max_steps - 1 : 512;
+  if (K < 32) return FH_OK;
+  static const int caps[3] = {1, 8, 64};
+  cudaEvent_t e0, e1;
+  FH_CUDA_TRY(ctx, cudaEventCreate(&e0));
+  FH_CUDA_TRY(ctx, cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bt = b->tile_threads, bc = b->split_cap;
+  for (int ti = 0; ti < 3; ++ti)
+    for (int ci = 0; ci < 3; ++ci) {
+      int splits, kchunk;
+      h_plan(b->tiles_by[ti].size(), K, caps[ci] < b->max_splits ? caps[ci] : b->max_splits, &splits, &kchunk);
+      if ((size_t)kchunk * sizeof(double) > 48 * 1024) continue;
+      const dim3 g((unsigned)b->tiles_by[ti].size(), (unsigned)splits);
+      float ms = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {  // first repetition warms up
+        cudaEventRecord(e0, ctx->stream);
+        if (b->mode == FH_H_DF64)
+          k_hist_tiles_df<<<g, kTileShapes[ti], sizeof(double) * kchunk, ctx->stream>>>(
+              b->tl_by[ti].as<fh_h_tile>(), b->inst.as<fh_h_dev_inst>(),
+              reinterpret_cast<const float2 *>(b->D.as<double>()), b->Ptot, K, b->W.as<double>(), b->max_weights,
+              kchunk, b->part.as<double>(), b->Ptot);
+        else
+          k_hist_tiles<<<g, kTileShapes[ti], sizeof(double) * kchunk, ctx->stream>>>(
+              b->tl_by[ti].as<fh_h_tile>(), b->inst.as<fh_h_dev_inst>(), b->D.as<double>(), b->Ptot, K,
+              b->W.as<double>(), b->max_weights, kchunk, b->part.as<double>(), b->Ptot);
+        cudaEventRecord(e1, ctx->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return fh_set_error(ctx, FH_ECUDA, "fh_h_batch_autotune: %s", cudaGetErrorString(e));
+        }
+        if (rep > 0) {
+          float t = 0.f;
+          cudaEventElapsedTime(&t, e0, e1);
+          ms += t;
+        }
+      }
+      ctx->launches += 3;
+      if (ms < best) {
+        best = ms;
+        bt = kTileShapes[ti];
+        bc = caps[ci];
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tile_threads = bt;
+  b->split_cap = bc;
+  b->graph.reset();
+  if (best_ms) *best_ms = best / 2;
+  return FH_OK;
+}
+
+int fh_h_batch_launch_shape(const fh_h_batch *b, int *tile_threads, int *split_cap) {
+  if (!b) return FH_EINVAL;
+  if (tile_threads) *tile_threads = b->tile_threads;
+  if (split_cap) *split_cap = b->split_cap;
+  return FH_OK;
+}
 
 int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");

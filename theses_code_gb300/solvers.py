@@ -48,6 +48,15 @@ class HSolverBatch:
         except Exception:
             pass
 
+    def autotune(self) -> dict:
+        """Picks the history-sum launch shape by timing the candidates
+        (fh_h_batch_autotune); returns the chosen shape and its time."""
+        ms = C.c_float(0.0)
+        check(self.ctx.L.fh_h_batch_autotune(self.h, C.byref(ms)), self.ctx.h)
+        t, c = C.c_int(0), C.c_int(0)
+        check(self.ctx.L.fh_h_batch_launch_shape(self.h, C.byref(t), C.byref(c)), self.ctx.h)
+        return {"tile_threads": t.value, "split_cap": c.value, "ms_per_launch": ms.value}
+
     def set_u(self, U: np.ndarray | list):
         flat = np.ascontiguousarray(np.concatenate([np.asarray(u, dtype=np.float64) for u in U])
                                     if isinstance(U, list) else U, dtype=np.float64)
