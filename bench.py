@@ -214,11 +214,13 @@ class TG2D(Workload):
         # algorithmic work per solve, by kernel class (interior points; per point-step:
         # 8 B per history layer read, the far pair and the two sums written)
         if blocked:
-            # near part: the layers of the current 64-step block (double-float pairs,
-            # 8 B each), the far pairs read (16 B) and the two sums written (16 B)
+            # near part, once per 8-step sub-block j8 (k_tg_mid_df): the older layers
+            # of the current 64-step block (double-float pairs, 8 B each), the far
+            # pairs of the 8 steps read (128 B, from the second block on) and the 16
+            # mid rows written (128 B)
             self.alg = {
-                "history": sum(8.0 * (j % 64) * pint + (32.0 if j >= 64 else 16.0) * pint
-                               for j in range(1, S) if j % 64),
+                "history": sum(8.0 * (j8 % 64) * pint + (256.0 if j8 >= 64 else 128.0) * pint
+                               for j8 in range(8, S, 8) if j8 % 64),
                 # far contraction: FP64-equivalent flops 2*128*K*P per 64-step block; the
                 # tensor cores execute 10 bf16 slice products per FP64 product on Ppad columns
                 "gemm_flops": sum(2.0 * 128 * j0 * pint for j0 in range(64, S, 64)),
@@ -227,15 +229,17 @@ class TG2D(Workload):
             }
         else:
             self.alg = {"history": sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))}
-        # sweeps: x reads C, fa, g, al, one partial, writes Ch; y reads Ch, C, fa, g, al,
-        # one partial, writes C and the new history layer
-        self.alg["sweep"] = 112.0 * pint * S
+        # sweeps: x reads C, fa, g, al, one history row, writes Ch; y reads Ch, C, fa, g,
+        # al, one history row, writes C and the new history layer; in blocked mode each
+        # sweep also reads the j % 8 layers of the current sub-block
+        self.alg["sweep"] = sum((112.0 + (16.0 * (j % 8) if blocked else 0.0)) * pint for j in range(S))
         self.alg_hist_bytes = self.alg["history"]
         self.name = f"tg2d_adi_{G}x{G}_{S}steps"
         self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
                        "d": 0.1, "velocity_modes": 8, "mode": args.mode,
                        "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
-        self.kernel = {"blocked": "k_hist_sum_df<2> (current block) + k_far_gemm (tcgen05, exact bf16 slices)",
+        self.kernel = {"blocked": "k_tg_mid_df (8-step sub-blocks of the current block) + k_far_gemm (tcgen05, "
+                                  "exact bf16 slices)",
                        "df64": "k_hist_sum_df<2>"}.get(args.mode, "k_hist_sum<2>")
 
     def solve_device(self):
@@ -549,7 +553,7 @@ def run_gb300(args):
     traffic = None
     ratio = profile_traffic_ratio({"fp64": "k_hist_sum_fp64_tg512x300.md",
                                    "df64": "k_hist_sum_df_tg512.md",
-                                   "blocked": "k_hist_sum_df_tg512.md"}.get(getattr(args, "mode", ""), ""))
+                                   "blocked": "k_tg_mid_df_tg512.md"}.get(getattr(args, "mode", ""), ""))
     if args.config == "tg2d" and ratio is not None and kt["history"][1] > 0:
         traffic = ratio * wl.alg["history"] / (kt["history"][1] / K)  # dram bytes per mean launch
     roofline = {"bound": "hbm", "achieved": hist.get("achieved"), "peak": pk["hbm"], "unit": "GB/s",

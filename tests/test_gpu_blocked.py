@@ -133,3 +133,58 @@ def test_contract_large_vs_torch_fp64(ctx):
     err = float(((S - ref).abs() / scale).max())
     print(f"K={K} P={P} max rel err {err:.3e}")
     assert err <= 2e-8, err
+
+
+def _blocked_vs_fp64(ctx, p, V2, C0, calls):
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FH_TG_FP64
+    from theses_code_gb300.solvers import TGSolver
+    steps = sum(calls)
+    out = {}
+    for mode in (FH_TG_FP64, FH_TG_BLOCKED):
+        s = TGSolver(ctx, p, steps, mode)
+        s.set_state(V2, C0)
+        for n in (calls if mode == FH_TG_BLOCKED else [steps]):
+            s.calc_step(n)
+        out[mode] = s.get_c()
+        s.close()
+    ref = out[FH_TG_FP64]
+    return np.max(np.abs(out[FH_TG_BLOCKED] - ref)) / np.max(np.abs(ref)), out[FH_TG_BLOCKED]
+
+
+def test_tg_blocked_uneven_step_calls(ctx):
+    """Steps advanced in calls that start and end inside 8-step sub-blocks and
+    64-step blocks give the same field as one call over all steps."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(64, 48, alpha=0.7, tau=5e-4, d=0.1, seed=7, C1=0.2)
+    err, got = _blocked_vs_fp64(ctx, p, V2, C0, [1, 3, 7, 13, 50, 1, 62, 63])
+    one = TGSolver(ctx, p, 200, FH_TG_BLOCKED)
+    one.set_state(V2, C0)
+    one.calc_step(200)
+    whole = one.get_c()
+    diff = np.max(np.abs(got - whole)) / np.max(np.abs(whole))
+    print(f"uneven calls: vs one call {diff:.3e}, vs FP64 {err:.3e}")
+    assert diff <= 1e-13, diff
+    assert err <= 1e-9, err
+
+
+def test_tg_blocked_psi_beta(ctx):
+    """psi(t) = t^1.3 in blocked mode: the factorization changes every step, so
+    the per-step double-float sweeps run (with the sub-block history rows)."""
+    from theses_code_gb300 import workloads
+    p, V2, C0 = workloads.convection_2d(64, 48, alpha=0.6, tau=1e-3, d=0.1, seed=5, C1=0.1)
+    p["beta"] = 1.3
+    err, _ = _blocked_vs_fp64(ctx, p, V2, C0, [150])
+    print(f"blocked psi beta 1.3: {err:.3e}")
+    assert err <= 1e-9, err
+
+
+def test_tg_blocked_wide_grid(ctx):
+    """Lines longer than 513 nodes: the per-step double-float sweeps (the fused
+    sub-block kernel holds at most 513-node lines in shared memory)."""
+    from theses_code_gb300 import workloads
+    p, V2, C0 = workloads.convection_2d(600, 40, alpha=0.7, tau=5e-4, d=0.1, seed=9, C1=0.2)
+    err, _ = _blocked_vs_fp64(ctx, p, V2, C0, [130])
+    print(f"blocked 600x40: {err:.3e}")
+    assert err <= 1e-9, err

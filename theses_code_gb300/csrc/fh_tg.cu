@@ -22,11 +22,13 @@
 // the reference layout idx = i + j*(sN+2); the history holds one difference
 // layer per full step, D[k] = C^{k+1} - C^k (the half-step layers the
 // reference also stores are only read through Ch).
+#include <algorithm>
 #include <mutex>
 
 #include "fh_internal.h"
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
+#include "fh_sm100.cuh"
 #include "fh_weights.cuh"
 
 // blocked contraction helpers (fh_blocked.cu)
@@ -62,6 +64,10 @@ struct fh_tg_solver {
   // blocked mode: the sweeps run in double-float; fields and factor tables as (hi, lo) pairs
   bool dfsweep = false;
   fh_dbuf Cd, Chd, fax2, gx2, alx2, pfx2, pbx2, fay2, gy2, aly2, pfy2, pby2;
+  // fused sub-block sweeps (k_tg_sweeps_fused): grid-barrier counter, error flag
+  bool fused = false;
+  int fuse_blocks = 0;
+  fh_dbuf bar, derr;
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
   fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
@@ -366,18 +372,30 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
 
 // ---------------------------------------------------- double-float sweeps
 // Blocked mode runs both half steps in double-float arithmetic on the FP32
-// pipe (fh_df.cuh): fields, factor tables, history partial sums and far rows
-// are (hi, lo) FP32 pairs, so no FP64 instruction is left in the sweeps.  Same
+// pipe (fh_df.cuh): fields, factor tables, history sums and far rows are
+// (hi, lo) FP32 pairs, so no FP64 instruction is left in the sweeps.  Same
 // structure as k_tg_xsweep / k_tg_ysweep.
+//
+// History right part of step j at a point: one precomputed row rb (the mid
+// row of step j, or its far row, or the near sum) plus the newest nt <= 7
+// layers D[j8 .. j-1] of the current 8-step sub-block weighted by
+// w_j(j8 + t), which the sweeps sum themselves (k_tg_mid_df below).
+static constexpr int kSub = 8;  // steps per sub-block of the near history
+
+__device__ __forceinline__ void tg_tiny_weights(const double *__restrict__ wt, int nt, float2 *wsm) {
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + nt) wsm[threadIdx.x - 32] = fh_df_pair(fh_df_from_double(wt[threadIdx.x - 32]));
+}
+
 __global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 *Cd, float2 *__restrict__ Chd,
-                                                           const float2 *__restrict__ part, long long ldp,
-                                                           int splits, const float2 *__restrict__ fax,
+                                                           const float2 *__restrict__ rb,
+                                                           const float2 *__restrict__ tiny, int nt,
+                                                           const double *__restrict__ wt,
+                                                           const float2 *__restrict__ fax,
                                                            const float2 *__restrict__ gx,
                                                            const float2 *__restrict__ alx,
                                                            const float2 *__restrict__ pfx,
                                                            const float2 *__restrict__ pbx,
-                                                           const double *__restrict__ cw,
-                                                           const float2 *__restrict__ far) {
+                                                           const double *__restrict__ cw) {
   extern __shared__ float2 sbf[];
   const int warp = threadIdx.x >> 5;
   const int line0 = 1 + blockIdx.x * kXLines;
@@ -403,13 +421,14 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 
   }
   // step constants as double-float, split once per CTA (FP64 instructions are
   // scarce on this GPU: one per thread would stall every warp at the start)
-  __shared__ float2 cst[4];
+  __shared__ float2 cst[4], wsm[kSub];
   if (threadIdx.x == 0) {
     cst[0] = fh_df_pair(fh_df_from_double(-g.st * (cw[0] + 0.0)));
     cst[1] = fh_df_pair(fh_df_from_double(g.S * 0.5));
     cst[2] = fh_df_pair(fh_df_from_double(g.st));
     cst[3] = fh_df_pair(fh_df_from_double(g.C1));
   }
+  tg_tiny_weights(wt, nt, wsm);
   __syncthreads();
   const fh_df kst = fh_df_from_pair(cst[0]), S2 = fh_df_from_pair(cst[1]), st = fh_df_from_pair(cst[2]);
   for (int r0 = 1; live && r0 < N; r0 += kXGroup * kUnroll) {
@@ -420,13 +439,17 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 
       const int i = r0 + tg + e * kXGroup;
       const long long id = base + (i < N ? i : 1);
       c[e] = Cd[id];
-      ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+      ts[e] = rb ? fh_df_from_pair(rb[id]) : fh_df{0.f, 0.f};
     }
-    for (int s = 0; s < splits; ++s)
 #pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int i = r0 + tg + e * kXGroup;
-        ts[e] = fh_df_add(ts[e], fh_df_from_pair(part[(long long)(2 * s) * ldp + base + (i < N ? i : 1)]));
+    for (int t = 0; t < kSub - 1; ++t)
+      if (t < nt) {
+        const fh_df w = fh_df_from_pair(wsm[t]);
+#pragma unroll
+        for (int e = 0; e < kUnroll; ++e) {
+          const int i = r0 + tg + e * kXGroup;
+          ts[e] = fh_df_fma(w, fh_df_from_pair(tiny[(long long)t * g.P + base + (i < N ? i : 1)]), ts[e]);
+        }
       }
 #pragma unroll
     for (int e = 0; e < kUnroll; ++e) {
@@ -459,15 +482,15 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep_df(fh_tg_dev g, float2 
 }
 
 __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 *Cd, const float2 *__restrict__ Chd,
-                                                           float2 *__restrict__ Dj, const float2 *__restrict__ part,
-                                                           long long ldp, int splits,
+                                                           float2 *__restrict__ Dj, const float2 *__restrict__ rb,
+                                                           const float2 *__restrict__ tiny, int nt,
+                                                           const double *__restrict__ wt,
                                                            const float2 *__restrict__ fay,
                                                            const float2 *__restrict__ gy,
                                                            const float2 *__restrict__ aly,
                                                            const float2 *__restrict__ pfy,
                                                            const float2 *__restrict__ pby,
-                                                           const double *__restrict__ cw,
-                                                           const float2 *__restrict__ far) {
+                                                           const double *__restrict__ cw) {
   extern __shared__ float2 sbf[];
   const int warp = threadIdx.x >> 5;
   const int N = g.M;
@@ -490,13 +513,14 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
       pb[fh_sk(q)] = pby[id];
     }
   }
-  __shared__ float2 cst[4];  // step constants, split once per CTA (see k_tg_xsweep_df)
+  __shared__ float2 cst[4], wsm[kSub];  // step constants, split once per CTA (see k_tg_xsweep_df)
   if (threadIdx.x == 0) {
     cst[0] = fh_df_pair(fh_df_from_double(-g.st * (cw[1] + 0.0)));
     cst[1] = fh_df_pair(fh_df_from_double(cw[2] + 0.0));
     cst[2] = fh_df_pair(fh_df_from_double(g.S * 0.5));
     cst[3] = fh_df_pair(fh_df_from_double(g.st));
   }
+  tg_tiny_weights(wt, nt, wsm);
   __syncthreads();
   const fh_df kst = fh_df_from_pair(cst[0]), kyh = fh_df_from_pair(cst[1]), S2 = fh_df_from_pair(cst[2]),
               st = fh_df_from_pair(cst[3]);
@@ -509,14 +533,18 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
       const long long id = line + (long long)(q < N ? q : 1) * g.ld;
       c[e] = Chd[id];
       f[e] = Cd[id];
-      ts[e] = far ? fh_df_from_pair(far[id]) : fh_df{0.f, 0.f};
+      ts[e] = rb ? fh_df_from_pair(rb[id]) : fh_df{0.f, 0.f};
     }
-    for (int s = 0; s < splits; ++s)
 #pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int q = r0 + rg + e * kRows;
-        ts[e] = fh_df_add(ts[e],
-                          fh_df_from_pair(part[(long long)(2 * s + 1) * ldp + line + (long long)(q < N ? q : 1) * g.ld]));
+    for (int t = 0; t < kSub - 1; ++t)
+      if (t < nt) {
+        const fh_df w = fh_df_from_pair(wsm[t]);
+#pragma unroll
+        for (int e = 0; e < kUnroll; ++e) {
+          const int q = r0 + rg + e * kRows;
+          ts[e] = fh_df_fma(w, fh_df_from_pair(tiny[(long long)t * g.P + line + (long long)(q < N ? q : 1) * g.ld]),
+                            ts[e]);
+        }
       }
 #pragma unroll
     for (int e = 0; e < kUnroll; ++e) {
@@ -547,6 +575,352 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
       Cd[id] = u;
       if (q >= 1 && q < N) Dj[id] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(cf[fh_sk(q)])));
     }
+  }
+}
+
+// ------------------------------------------------ mid rows of the near history
+// At the start of sub-block j8 (j8 > j0, the block start) the layers
+// [j0, j8) of the block are summed once for all nr <= 8 steps of the
+// sub-block:  mid[2r + m][p] = far[2(j8 - j0 + r) + m][p]
+//                             + sum_{k in [j0, j8)} w_{j8+r}^m(k) D[k][p]
+// (m = 0 x weights, m = 1 y weights).  Each layer is read once per sub-block
+// instead of once per step; the per-step remainder (the nt <= 7 layers of the
+// sub-block itself) is summed in the sweeps.  Double-float products and
+// TwoSum accumulation as in k_hist_sum_df; two points per thread.
+static constexpr int kMidThreads = 128;
+static constexpr int kMidMaxK = kTgBlock - kSub;  // 56 layers at most
+
+__global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restrict__ D, long long P, int K,
+                                                          const double *__restrict__ W, int ldw, int nr,
+                                                          const float2 *__restrict__ far, long long ldfar,
+                                                          float2 *__restrict__ out, long long ldo) {
+  constexpr int R = 2 * kSub;
+  __shared__ float2 ws[R][kMidMaxK];
+  for (int i = threadIdx.x; i < R * K; i += blockDim.x) {
+    const int row = i / K, k = i - row * K;
+    const int r = row >> 1, m = row & 1;
+    const double w = r < nr ? W[(long long)r * 2 * ldw + (long long)m * ldw + k] : 0.0;
+    const float wh = __double2float_rn(w);
+    ws[row][k] = make_float2(wh, __double2float_rn(w - (double)wh));
+  }
+  __syncthreads();
+  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (p >= P) return;
+  float ah[R][2], al[R][2];
+#pragma unroll
+  for (int row = 0; row < R; ++row) {
+    if (far && (row >> 1) < nr) {
+      const float4 f = *reinterpret_cast<const float4 *>(far + (long long)row * ldfar + p);
+      ah[row][0] = f.x;
+      al[row][0] = f.y;
+      ah[row][1] = f.z;
+      al[row][1] = f.w;
+    } else {
+      ah[row][0] = ah[row][1] = al[row][0] = al[row][1] = 0.f;
+    }
+  }
+  auto acc = [](const float2 w, const float dh, const float dl, float &sh, float &sl) {
+    const float ph = w.x * dh;
+    float pl = fmaf(w.x, dh, -ph);
+    pl = fmaf(w.x, dl, pl);
+    pl = fmaf(w.y, dh, pl);
+    const float t = sh + ph;
+    const float bb = t - sh;
+    const float e = (sh - (t - bb)) + (ph - bb);
+    sh = t;
+    sl += e + pl;
+  };
+  const float4 *d = reinterpret_cast<const float4 *>(D + p);
+  const long long ld4 = P / 2;
+  int k = 0;
+  for (; k + 4 <= K; k += 4) {
+    float4 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = __ldcs(d + (long long)(k + u) * ld4);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int row = 0; row < R; ++row) {
+        const float2 w = ws[row][k + u];
+        acc(w, v[u].x, v[u].y, ah[row][0], al[row][0]);
+        acc(w, v[u].z, v[u].w, ah[row][1], al[row][1]);
+      }
+    if ((k & 15) == 12) {
+#pragma unroll
+      for (int row = 0; row < R; ++row)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {  // renormalise (fast two-sum, |ah| >= |al|)
+          const float t = ah[row][q] + al[row][q];
+          al[row][q] = al[row][q] - (t - ah[row][q]);
+          ah[row][q] = t;
+        }
+    }
+  }
+  for (; k < K; ++k) {
+    const float4 v = __ldcs(d + (long long)k * ld4);
+#pragma unroll
+    for (int row = 0; row < R; ++row) {
+      const float2 w = ws[row][k];
+      acc(w, v.x, v.y, ah[row][0], al[row][0]);
+      acc(w, v.z, v.w, ah[row][1], al[row][1]);
+    }
+  }
+#pragma unroll
+  for (int row = 0; row < R; ++row) {
+    if ((row >> 1) >= nr) continue;
+    float h[2], l[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      h[q] = ah[row][q] + al[row][q];
+      l[q] = al[row][q] - (h[q] - ah[row][q]);
+    }
+    *reinterpret_cast<float4 *>(out + (long long)row * ldo + p) = make_float4(h[0], l[0], h[1], l[1]);
+  }
+}
+
+// ------------------------------------------------ fused sub-block sweeps
+// One cooperative launch runs both half steps of up to kSub consecutive steps
+// of one sub-block.  Every CTA owns four x lines and four y columns and keeps
+// the fixed factor tables of both (fa, g, al, pf, pb per node; 210 KiB for a
+// 512 x 512 grid) in shared memory for the whole launch, so a step only
+// reads the field, its history row and the sub-block's layers.  The half
+// steps are separated by grid barriers (every CTA is resident: one CTA per
+// SM, launched cooperatively); data written by other CTAs within the launch
+// is read through L2 (ld.global.cg), never from L1.  Each barrier wait is
+// bounded by FH_WAIT_NS of %globaltimer: on expiry the CTA sets *err and
+// returns (the other CTAs then time out at their next barrier).
+// Arithmetic per node as in k_tg_xsweep_df / k_tg_ysweep_df.
+static constexpr int kFuseThreads = 512;
+static constexpr int kFuseMaxN = 1 + kXGroup * kUnroll;  // one staging round per line
+
+struct tg_fuse_args {
+  fh_tg_dev g;
+  float2 *Cd, *Chd, *D;  // D: history layers (pairs), layer k at D + k P
+  const float2 *fax, *gx, *alx, *pfx, *pbx, *fay, *gy, *aly, *pfy, *pby;
+  const double *W;       // per-solve weight table, row j at W + 2 j ldw
+  const double *cwall;   // current weights, 4 per step
+  const float2 *rb0;     // history row of step j8 + s: x at rb0 + s rb_step, y at + rb_xy (null: none)
+  long long rb_step, rb_xy;
+  int ldw, j8, s0, ns;   // steps j8 + s0 .. j8 + s0 + ns - 1
+  unsigned *bar;
+  int *err;
+};
+
+static size_t tg_fuse_smem(int sN, int M) {
+  return sizeof(float2) * 4 * 6 * ((size_t)tg_line_stride(sN) + tg_line_stride(M));
+}
+
+// Grid barrier number `target / gridDim.x` on a counter zeroed before the launch.
+__device__ __forceinline__ bool tg_grid_sync(unsigned *bar, unsigned target, int *err) {
+  __shared__ int gs_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const uint64_t deadline = fh_globaltimer() + FH_WAIT_NS;
+    int ok = 1;
+    for (;;) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      if (*(volatile int *)err || fh_globaltimer() > deadline) {
+        ok = 0;
+        atomicOr(err, 1);
+        break;
+      }
+      __nanosleep(32);
+    }
+    gs_ok = ok;
+  }
+  __syncthreads();
+  return gs_ok != 0;
+}
+
+__global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fuse_args a) {
+  extern __shared__ float2 sbf[];
+  __shared__ float2 cx[kSub][4], cy[kSub][4], wx[kSub][kSub], wy[kSub][kSub];
+  const fh_tg_dev &g = a.g;
+  const int Nx = g.sN, Ny = g.M;
+  const int Lx = tg_line_stride(Nx), Ly = tg_line_stride(Ny);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // x lines: 128 threads stage each line; arrays fa, g, al, pf, pb, bt
+  const int ln = tid >> 7, tg = tid & 127;
+  const int xline = 1 + blockIdx.x * 4 + ln;
+  const bool xlive = xline < g.M;
+  float2 *xa = sbf + (size_t)ln * 6 * Lx;
+  const long long xbase = (long long)xline * g.ld;
+  // y columns: four adjacent columns per row (32-byte segments)
+  float2 *ys = sbf + (size_t)4 * 6 * Lx;
+  const int col = tid & 3, rg = tid >> 2;
+  const int ycol = 1 + blockIdx.x * 4 + col;
+  const bool ylive = ycol < g.sN;
+  float2 *ya = ys + (size_t)col * 6 * Ly;
+  if (xlive) {
+    for (int i = 1 + tg; i < Nx; i += kXGroup) {
+      const long long id = xbase + i;
+      xa[fh_sk(i)] = a.fax[id];
+      xa[Lx + fh_sk(i)] = a.gx[id];
+      xa[2 * Lx + fh_sk(i)] = a.alx[id];
+      xa[3 * Lx + fh_sk(i)] = a.pfx[id];
+      xa[4 * Lx + fh_sk(i)] = a.pbx[id];
+    }
+    if (tg == 0) xa[4 * Lx + fh_sk(0)] = a.pbx[xbase];
+  }
+  if (ylive) {
+    for (int q = 1 + rg; q < Ny; q += kXGroup) {
+      const long long id = ycol + (long long)q * g.ld;
+      ya[fh_sk(q)] = a.fay[id];
+      ya[Ly + fh_sk(q)] = a.gy[id];
+      ya[2 * Ly + fh_sk(q)] = a.aly[id];
+      ya[3 * Ly + fh_sk(q)] = a.pfy[id];
+      ya[4 * Ly + fh_sk(q)] = a.pby[id];
+    }
+    if (rg == 0) ya[4 * Ly + fh_sk(0)] = a.pby[ycol];
+  }
+  // double-float step constants and sub-block weights of every step, one FP64
+  // conversion per thread
+  constexpr int kPer = 8 + 2 * kSub;
+  for (int v = tid; v < a.ns * kPer; v += blockDim.x) {
+    const int s = a.s0 + v / kPer, r = v % kPer;
+    const int j = a.j8 + s;
+    const double *cw = a.cwall + 4LL * j;
+    const double *Wj = a.W + (long long)j * 2 * a.ldw + a.j8;
+    double val;
+    float2 *dst;
+    if (r < 4) {
+      dst = &cx[s][r];
+      val = r == 0 ? -g.st * (cw[0] + 0.0) : r == 1 ? g.S * 0.5 : r == 2 ? g.st : g.C1;
+    } else if (r < 8) {
+      dst = &cy[s][r - 4];
+      val = r == 4 ? -g.st * (cw[1] + 0.0) : r == 5 ? cw[2] + 0.0 : r == 6 ? g.S * 0.5 : g.st;
+    } else if (r < 8 + kSub) {
+      dst = &wx[s][r - 8];
+      val = (r - 8) < s ? Wj[r - 8] : 0.0;
+    } else {
+      dst = &wy[s][r - 8 - kSub];
+      val = (r - 8 - kSub) < s ? Wj[a.ldw + (r - 8 - kSub)] : 0.0;
+    }
+    *dst = fh_df_pair(fh_df_from_double(val));
+  }
+  __syncthreads();
+  const unsigned nblk = gridDim.x;
+  unsigned nb = 0;
+  const float2 *tiny = a.D + (long long)a.j8 * g.P;
+  for (int s = a.s0; s < a.s0 + a.ns; ++s) {
+    const int j = a.j8 + s;
+    const float2 *rbx = a.rb0 ? a.rb0 + (long long)s * a.rb_step : nullptr;
+    const float2 *rby = rbx ? rbx + a.rb_xy : nullptr;
+    // ---- x half step (fr_d_t_g_2d.cpp:2577-2590)
+    if (xlive) {
+      const fh_df kst = fh_df_from_pair(cx[s][0]), S2 = fh_df_from_pair(cx[s][1]), st = fh_df_from_pair(cx[s][2]);
+      float2 c[kUnroll];
+      fh_df ts[kUnroll];
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = 1 + tg + e * kXGroup;
+        const long long id = xbase + (i < Nx ? i : 1);
+        c[e] = __ldcg(a.Cd + id);
+        ts[e] = rbx ? fh_df_from_pair(__ldcg(rbx + id)) : fh_df{0.f, 0.f};
+      }
+#pragma unroll
+      for (int t = 0; t < kSub - 1; ++t)
+        if (t < s) {
+          const fh_df w = fh_df_from_pair(wx[s][t]);
+#pragma unroll
+          for (int e = 0; e < kUnroll; ++e) {
+            const int i = 1 + tg + e * kXGroup;
+            ts[e] = fh_df_fma(w, fh_df_from_pair(__ldcg(tiny + (long long)t * g.P + xbase + (i < Nx ? i : 1))), ts[e]);
+          }
+        }
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int i = 1 + tg + e * kXGroup;
+        if (i < Nx) {
+          fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
+          om = fh_df_fma(st, ts[e], om);
+          xa[5 * Lx + fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(xa[Lx + fh_sk(i)]), om)));
+        }
+      }
+    }
+    __syncthreads();
+    if (warp < 4 && 1 + (int)blockIdx.x * 4 + warp < g.M) {
+      float2 *w = sbf + (size_t)warp * 6 * Lx;
+      fh_line_solve_prefix_df(Nx, w, w + 5 * Lx, w + 2 * Lx, w + 3 * Lx, w + 4 * Lx, fh_df{0.f, 0.f},
+                              fh_df_from_pair(cx[s][3]), w + 5 * Lx, w + 5 * Lx);
+    }
+    __syncthreads();
+    if (xlive)
+      for (int i = tg; i <= Nx + 1; i += kXGroup) {
+        const float2 v = xa[5 * Lx + fh_sk(i)];
+        a.Chd[xbase + i] = v;
+        if (i == 0 || i >= Nx) a.Cd[xbase + i] = v;
+      }
+    if (!tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
+    // ---- y half step (fr_d_t_g_2d.cpp:2591-2606); D[j] = new field - old field
+    float2 f[kUnroll];
+    if (ylive) {
+      const fh_df kst = fh_df_from_pair(cy[s][0]), kyh = fh_df_from_pair(cy[s][1]), S2 = fh_df_from_pair(cy[s][2]),
+                  st = fh_df_from_pair(cy[s][3]);
+      float2 c[kUnroll];
+      fh_df ts[kUnroll];
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int q = 1 + rg + e * kXGroup;
+        const long long id = ycol + (long long)(q < Ny ? q : 1) * g.ld;
+        c[e] = __ldcg(a.Chd + id);
+        f[e] = __ldcg(a.Cd + id);
+        ts[e] = rby ? fh_df_from_pair(__ldcg(rby + id)) : fh_df{0.f, 0.f};
+      }
+#pragma unroll
+      for (int t = 0; t < kSub - 1; ++t)
+        if (t < s) {
+          const fh_df w = fh_df_from_pair(wy[s][t]);
+#pragma unroll
+          for (int e = 0; e < kUnroll; ++e) {
+            const int q = 1 + rg + e * kXGroup;
+            ts[e] = fh_df_fma(w, fh_df_from_pair(__ldcg(tiny + (long long)t * g.P + ycol + (long long)(q < Ny ? q : 1) * g.ld)),
+                              ts[e]);
+          }
+        }
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int q = 1 + rg + e * kXGroup;
+        if (q < Ny) {
+          const fh_df cc = fh_df_from_pair(c[e]);
+          // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
+          const fh_df t = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), ts[e]);
+          fh_df om = fh_df_fma(kst, cc, S2);
+          om = fh_df_fma(st, t, om);
+          ya[5 * Ly + fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(ya[Ly + fh_sk(q)]), om)));
+        }
+      }
+    }
+    __syncthreads();
+    if (warp < 4 && 1 + (int)blockIdx.x * 4 + warp < g.sN) {
+      float2 *w = ys + (size_t)warp * 6 * Ly;
+      fh_line_solve_prefix_df(Ny, w, w + 5 * Ly, w + 2 * Ly, w + 3 * Ly, w + 4 * Ly, fh_df{1.f, 0.f},
+                              fh_df{0.f, 0.f}, w + 5 * Ly, w + 5 * Ly);
+    }
+    __syncthreads();
+    if (ylive) {
+      float2 *Dj = a.D + (long long)j * g.P;
+#pragma unroll
+      for (int e = 0; e < kUnroll; ++e) {
+        const int q = 1 + rg + e * kXGroup;
+        if (q < Ny) {
+          const long long id = ycol + (long long)q * g.ld;
+          const float2 u = ya[5 * Ly + fh_sk(q)];
+          a.Cd[id] = u;
+          Dj[id] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[e])));
+        }
+      }
+      if (rg == 0) {
+        a.Cd[ycol] = ya[5 * Ly + fh_sk(0)];
+        a.Cd[ycol + (long long)Ny * g.ld] = ya[5 * Ly + fh_sk(Ny)];
+        a.Cd[ycol + (long long)(Ny + 1) * g.ld] = ya[5 * Ly + fh_sk(Ny + 1)];
+      }
+    }
+    if (s + 1 < a.s0 + a.ns && !tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
   }
 }
 
@@ -588,7 +962,133 @@ static int tg_factor(fh_tg_solver *s, const double *cwj) {
   return FH_OK;
 }
 
-static int tg_one_step(fh_tg_solver *s) {
+// Step j of the double-float sweeps (blocked mode); the block-start work,
+// the weights and the factorization of step j are already enqueued.
+//   per-solve weight table: mid rows at each sub-block start (k_tg_mid_df),
+//     the sweeps add the sub-block's own layers [j8, j);
+//   per-step weight row (more steps than the table holds): one near sum over
+//     the block's layers [j0, j) per step, far row folded in.
+static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int max_n, int *done) {
+  fh_ctx *ctx = s->ctx;
+  const fh_tg_dev &g = s->dv;
+  const int j = s->tstep;
+  const int ldw = s->max_steps;
+  const int j0 = s->blk ? s->j0 : 0;
+  const float2 *D2 = reinterpret_cast<const float2 *>(s->D.as<double>());
+  float2 *part = s->part.as<float2>();
+  const float2 *farj = (s->blk && j0 > 0) ? s->far.as<float2>() + 2LL * (j - j0) * s->ldfar : nullptr;
+  const float2 *rbx = farj, *rby = farj ? farj + s->ldfar : nullptr;
+  const float2 *tiny = nullptr;
+  const double *wtx = nullptr, *wty = nullptr;
+  int nt = 0, rc;
+  if (s->wtab) {
+    const int j8 = (j / kSub) * kSub;  // >= j0: blocks are whole sub-blocks
+    if (j8 > j0) {
+      if (j == j8) {
+        const int nr = min(kSub, s->max_steps - j8);
+        fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+        k_tg_mid_df<<<(unsigned)fh_ceil_div(g.P, 2LL * kMidThreads), kMidThreads, 0, ctx->stream>>>(
+            D2 + (long long)j0 * g.P, g.P, j8 - j0, s->W.as<double>() + (long long)j8 * 2 * ldw + j0, ldw, nr,
+            farj, s->ldfar, part, g.P);
+        fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+        if ((rc = fh_after_launch(ctx, "k_tg_mid_df"))) return rc;
+      }
+      rbx = part + 2LL * (j - j8) * g.P;
+      rby = rbx + g.P;
+    }
+    if (s->fused) {
+      // steps j .. j + ns - 1 of this sub-block in one cooperative launch
+      const int ns = min(max_n, kSub - (j - j8));
+      tg_fuse_args fa;
+      fa.g = g;
+      fa.Cd = s->Cd.as<float2>();
+      fa.Chd = s->Chd.as<float2>();
+      fa.D = reinterpret_cast<float2 *>(s->D.as<double>());
+      fa.fax = s->fax2.as<float2>();
+      fa.gx = s->gx2.as<float2>();
+      fa.alx = s->alx2.as<float2>();
+      fa.pfx = s->pfx2.as<float2>();
+      fa.pbx = s->pbx2.as<float2>();
+      fa.fay = s->fay2.as<float2>();
+      fa.gy = s->gy2.as<float2>();
+      fa.aly = s->aly2.as<float2>();
+      fa.pfy = s->pfy2.as<float2>();
+      fa.pby = s->pby2.as<float2>();
+      fa.W = s->W.as<double>();
+      fa.cwall = s->cw.as<double>();
+      fa.ldw = ldw;
+      fa.j8 = j8;
+      fa.s0 = j - j8;
+      fa.ns = ns;
+      fa.bar = s->bar.as<unsigned>();
+      fa.err = s->derr.as<int>();
+      if (j8 > j0) {  // mid rows of the sub-block
+        fa.rb0 = part;
+        fa.rb_step = 2LL * g.P;
+        fa.rb_xy = g.P;
+      } else if (s->blk && j0 > 0) {  // far rows of the block
+        fa.rb0 = s->far.as<float2>() + 2LL * (j8 - j0) * s->ldfar;
+        fa.rb_step = 2LL * s->ldfar;
+        fa.rb_xy = s->ldfar;
+      } else {
+        fa.rb0 = nullptr;
+        fa.rb_step = fa.rb_xy = 0;
+      }
+      FH_CUDA_TRY(ctx, cudaMemsetAsync(s->bar.p, 0, sizeof(unsigned), ctx->stream));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)s->fuse_blocks);
+      cfg.blockDim = dim3(kFuseThreads);
+      cfg.dynamicSmemBytes = tg_fuse_smem(g.sN, g.M);
+      cfg.stream = ctx->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+      const cudaError_t e = cudaLaunchKernelEx(&cfg, k_tg_sweeps_fused, fa);
+      fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+      if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "k_tg_sweeps_fused: %s", cudaGetErrorString(e));
+      if ((rc = fh_after_launch(ctx, "k_tg_sweeps_fused"))) return rc;
+      s->tstep += ns;
+      *done = ns;
+      return FH_OK;
+    }
+    nt = j - j8;
+    tiny = D2 + (long long)j8 * g.P;
+    wtx = Wj + j8;
+    wty = Wj + ldw + j8;
+  } else if (j - j0 >= 1) {
+    // one split: the block holds at most 63 near layers
+    const int K = j - j0, kchunk = (int)fh_ceil_div(K, 4) * 4;
+    if ((rc = fh_launch_hist_sum_df_partials(ctx, 2, K, g.P, Wj + j0, ldw, D2 + (long long)j0 * g.P, g.P, 1, kchunk,
+                                             reinterpret_cast<double *>(part), g.P, farj, s->ldfar, 1)))
+      return rc;
+    rbx = part;
+    rby = part + g.P;
+  }
+  fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+  const size_t smx = sizeof(float2) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
+  k_tg_xsweep_df<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXThreads, smx, ctx->stream>>>(
+      g, s->Cd.as<float2>(), s->Chd.as<float2>(), rbx, tiny, nt, wtx, s->fax2.as<float2>(), s->gx2.as<float2>(),
+      s->alx2.as<float2>(), s->pfx2.as<float2>(), s->pbx2.as<float2>(), cwj);
+  if ((rc = fh_after_launch(ctx, "k_tg_xsweep_df"))) return rc;
+  const size_t smy = sizeof(float2) * 4 * 6 * (size_t)tg_line_stride(g.M);
+  k_tg_ysweep_df<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
+      g, s->Cd.as<float2>(), s->Chd.as<float2>(), reinterpret_cast<float2 *>(s->D.as<double>()) + (long long)j * g.P,
+      rby, tiny, nt, wty, s->fay2.as<float2>(), s->gy2.as<float2>(), s->aly2.as<float2>(), s->pfy2.as<float2>(),
+      s->pby2.as<float2>(), cwj);
+  fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+  if ((rc = fh_after_launch(ctx, "k_tg_ysweep_df"))) return rc;
+  s->tstep++;
+  *done = 1;
+  return FH_OK;
+}
+
+// Enqueues the next step (or, for the fused sweeps, up to max_n steps of the
+// current sub-block); *done receives the number of steps enqueued.
+static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
+  *done = 1;
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
   const int j = s->tstep;
@@ -634,6 +1134,7 @@ static int tg_one_step(fh_tg_solver *s) {
   const double *cwj = s->wtab ? s->cw.as<double>() + 4LL * j : s->cw.as<double>();
   if (!s->factor_fixed || j == 0)
     if ((rc = tg_factor(s, cwj))) return rc;
+  if (s->dfsweep) return tg_step_df(s, Wj, cwj, max_n, done);
   // far-history rows of this step ((hi, lo) pairs, x row 2r, y row 2r+1)
   const float2 *far = nullptr;
   if (blocked && s->j0 > 0) far = s->far.as<float2>() + 2LL * (j - s->j0) * s->ldfar;
@@ -643,8 +1144,7 @@ static int tg_one_step(fh_tg_solver *s) {
     if (s->df)
       rc = fh_launch_hist_sum_df_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                           reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kstart * g.P,
-                                          g.P, splits, kchunk, s->part.as<double>(), g.P, far, s->ldfar,
-                                          s->dfsweep ? 1 : 0);
+                                          g.P, splits, kchunk, s->part.as<double>(), g.P, far, s->ldfar, 0);
     else
       rc = fh_launch_hist_sum_partials(ctx, 2, knear, g.P, Wj + kstart, ldw,
                                        s->D.as<double>() + (long long)kstart * g.P, g.P, splits, kchunk,
@@ -656,23 +1156,6 @@ static int tg_one_step(fh_tg_solver *s) {
   if (far && !(knear >= 1 && s->df)) {
     farx = far;
     fary = far + s->ldfar;
-  }
-  if (s->dfsweep) {
-    fh_prof_mark(ctx, FH_PROF_SWEEP, false);
-    const size_t smx = sizeof(float2) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
-    k_tg_xsweep_df<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXThreads, smx, ctx->stream>>>(
-        g, s->Cd.as<float2>(), s->Chd.as<float2>(), s->part.as<float2>(), g.P, splits, s->fax2.as<float2>(),
-        s->gx2.as<float2>(), s->alx2.as<float2>(), s->pfx2.as<float2>(), s->pbx2.as<float2>(), cwj, farx);
-    if ((rc = fh_after_launch(ctx, "k_tg_xsweep_df"))) return rc;
-    const size_t smy = sizeof(float2) * 4 * 6 * (size_t)tg_line_stride(g.M);
-    k_tg_ysweep_df<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
-        g, s->Cd.as<float2>(), s->Chd.as<float2>(), reinterpret_cast<float2 *>(s->D.as<double>()) + (long long)j * g.P,
-        s->part.as<float2>(), g.P, splits, s->fay2.as<float2>(), s->gy2.as<float2>(), s->aly2.as<float2>(),
-        s->pfy2.as<float2>(), s->pby2.as<float2>(), cwj, fary);
-    fh_prof_mark(ctx, FH_PROF_SWEEP, true);
-    if ((rc = fh_after_launch(ctx, "k_tg_ysweep_df"))) return rc;
-    s->tstep++;
-    return FH_OK;
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
   const size_t smx = sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
@@ -718,6 +1201,15 @@ static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_xsweep_df, cudaFuncAttributeMaxDynamicSharedMemorySize, smx));
     cur_x[ctx->device] = smx;
+  }
+  // the fused sweeps hold both directions' tables; larger grids use the per-step kernels
+  if (sN <= kFuseMaxN && M <= kFuseMaxN) {
+    static int cur_f[64];
+    const int smf = (int)tg_fuse_smem(sN, M);
+    if (smf > cur_f[ctx->device] && smf <= 220 * 1024) {
+      FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_sweeps_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, smf));
+      cur_f[ctx->device] = smf;
+    }
   }
   if (smy > cur_y[ctx->device]) {
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_ysweep, cudaFuncAttributeMaxDynamicSharedMemorySize, smy));
@@ -793,6 +1285,23 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
         delete s;
         return rc;
       }
+    // fused sub-block sweeps: fixed factorization, per-solve weight table, both
+    // directions' tables in shared memory, one resident CTA per four lines
+    const int nblk = (int)std::max(fh_ceil_div(g.M - 1, 4), fh_ceil_div(g.sN - 1, 4));
+    int nsm = 0, per_sm = 0;
+    const size_t smf = tg_fuse_smem(g.sN, g.M);
+    if (s->factor_fixed && s->wtab && g.sN <= kFuseMaxN && g.M <= kFuseMaxN && smf <= 220 * 1024 &&
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tg_sweeps_fused, kFuseThreads, smf) == cudaSuccess &&
+        nblk <= nsm * per_sm) {
+      if ((rc = fh_alloc(ctx, s->bar, sizeof(unsigned))) || (rc = fh_alloc(ctx, s->derr, sizeof(int)))) {
+        delete s;
+        return rc;
+      }
+      s->fused = true;
+      s->fuse_blocks = nblk;
+    }
+    cudaGetLastError();
   }
   if (mode == FH_TG_BLOCKED && max_steps > kTgBlock) {
     s->blk = fh_blk_new();
@@ -825,6 +1334,7 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
   s->tstep = 0;
   s->j0 = 0;
   s->have_state = true;
@@ -838,6 +1348,7 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
+  if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->tstep = 0;
   s->j0 = 0;
@@ -854,8 +1365,8 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
              nsteps, s->max_steps);
   if (ctx->graphs && s->tstep == 0 && nsteps > 1) {
     int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
-      for (int n = 0; n < nsteps; ++n) {
-        int r = tg_one_step(s);
+      for (int n = 0, d = 1; n < nsteps; n += d) {
+        int r = tg_one_step(s, nsteps - n, &d);
         if (r) return r;
       }
       return tg_publish(s);
@@ -865,8 +1376,8 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
     s->j0 = (s->blk && nsteps > kTgBlock) ? ((nsteps - 1) / kTgBlock) * kTgBlock : 0;
     return FH_OK;
   }
-  for (int n = 0; n < nsteps; ++n) {
-    int rc = tg_one_step(s);
+  for (int n = 0, d = 1; n < nsteps; n += d) {
+    int rc = tg_one_step(s, nsteps - n, &d);
     if (rc) return rc;
   }
   return tg_publish(s);
@@ -879,6 +1390,11 @@ int fh_tg_get_c_host(fh_tg_solver *s, double *C_host) {
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(C_host, s->C.p, n, cudaMemcpyDeviceToHost, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (s->fused) {
+    int h = 0;
+    FH_CUDA_TRY(ctx, cudaMemcpy(&h, s->derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fh_set_error(ctx, FH_ETIMEOUT, "fused sweeps: a bounded grid barrier expired");
+  }
   return FH_OK;
 }
 
