@@ -690,8 +690,8 @@ __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restr
 // bounded by FH_WAIT_NS of %globaltimer: on expiry the CTA sets *err and
 // returns (the other CTAs then time out at their next barrier).
 // Arithmetic per node as in k_tg_xsweep_df / k_tg_ysweep_df.
-static constexpr int kFuseThreads = 512;
-static constexpr int kFuseMaxN = 1 + kXGroup * kUnroll;  // one staging round per line
+static constexpr int kFuseThreads = 384;
+static constexpr int kFuseMaxN = 513;  // lines of at most 513 nodes (64 workers x 8 nodes)
 
 struct tg_fuse_args {
   fh_tg_dev g;
@@ -710,64 +710,142 @@ static size_t tg_fuse_smem(int sN, int M) {
   return sizeof(float2) * 4 * 6 * ((size_t)tg_line_stride(sN) + tg_line_stride(M));
 }
 
-// Grid barrier number `target / gridDim.x` on a counter zeroed before the launch.
+// Grid barrier number `target / gridDim.x` on a counter zeroed before the
+// launch.  The last warp of the CTA (kBarWarp, never a solving warp) arrives
+// and polls as a whole, lane 0 loading and broadcasting the count; all other
+// single-lane work of the kernel also runs in that warp, so the solving warps
+// never run with split lanes (a solving warp whose lane 0 had done such work
+// ran the shuffle scans of its line solve three times slower).
+static constexpr int kBarWarp = kFuseThreads / 32 - 1;
+
 __device__ __forceinline__ bool tg_grid_sync(unsigned *bar, unsigned target, int *err) {
   __shared__ int gs_ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(bar, 1u);
+  if ((threadIdx.x >> 5) == kBarWarp) {
+    const unsigned lane = threadIdx.x & 31u;
+    if (lane == 0) {
+      __threadfence();
+      atomicAdd(bar, 1u);
+    }
+    __syncwarp();
     const uint64_t deadline = fh_globaltimer() + FH_WAIT_NS;
     int ok = 1;
     for (;;) {
-      unsigned v;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
-      if (v >= target) break;
-      if (*(volatile int *)err || fh_globaltimer() > deadline) {
+      int st = 0;
+      if (lane == 0) {
+        unsigned v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+        st = v >= target ? 1 : ((*(volatile int *)err || fh_globaltimer() > deadline) ? 2 : 0);
+      }
+      st = __shfl_sync(0xffffffffu, st, 0);
+      if (st == 1) break;
+      if (st == 2) {
         ok = 0;
-        atomicOr(err, 1);
+        if (lane == 0) atomicOr(err, 1);
         break;
       }
       __nanosleep(32);
     }
-    gs_ok = ok;
+    if (lane == 0) gs_ok = ok;
+    __syncwarp();
   }
   __syncthreads();
   return gs_ok != 0;
 }
 
+// Phase stamps of the fused sweeps for profiling builds (-DFH_TG_STAMPS):
+// %clock64 of every phase boundary of every step, taken by warp kBarWarp,
+// read with fh_tg_stamps_read.  Empty otherwise.
+#ifdef FH_TG_STAMPS
+__device__ long long g_tg_stamps[256 * kSub * 8];
+#define TG_STAMP(p)                                                                   \
+  if (warp == kBarWarp) {                                                             \
+    const long long c_ = clock64();                                                   \
+    if ((threadIdx.x & 31) == 0) g_tg_stamps[(blockIdx.x * kSub + s) * 8 + (p)] = c_; \
+    __syncwarp();                                                                     \
+  }
+extern "C" int fh_tg_stamps_read(long long *h) {
+  return (int)cudaMemcpyFromSymbol(h, g_tg_stamps, sizeof(g_tg_stamps));
+}
+#else
+#define TG_STAMP(p)
+#endif
+
+// Roles: warps 0-3 solve (warp w the x line / y column w of the CTA) and do
+// nothing else, so they never run with split lanes; warps 4-11 ("workers", 64
+// per line, eight nodes each) do all loads and stores.  384 threads leave 170
+// registers per thread for the workers' per-node history sums.  While one direction is
+// being solved the workers precompute the history sums of the other (every
+// load that does not depend on that solve), so after a grid barrier only the
+// new field and the newest layer remain to be read.
+static constexpr int kSolveWarps = 4;
+static constexpr int kWorkers = kFuseThreads - 32 * kSolveWarps;  // 256
+static constexpr int kWPerLine = kWorkers / 4;                   // 64
+static constexpr int kWPts = 8;                                  // nodes per worker and line
+static constexpr int kLayerBatch = 1;                            // sub-block layers per load round
+static_assert(kWPerLine * kWPts + 1 >= kFuseMaxN, "fused sweeps: worker nodes must cover a line");
+
+// x history part of step j8 + s of a worker's nodes without the newest layer:
+// row + sum_{t < s-1} w(t) D[j8 + t]
+__device__ __forceinline__ void tg_x_partial(const tg_fuse_args &a, int s, const float2 (*wx)[kSub],
+                                             const float2 *tiny, long long xbase, int wt, int Nx,
+                                             fh_df (&tsx)[kWPts]) {
+  const float2 *rbx = a.rb0 ? a.rb0 + (long long)s * a.rb_step : nullptr;
+#pragma unroll
+  for (int e = 0; e < kWPts; ++e) {
+    const int i = 1 + wt + e * kWPerLine;
+    tsx[e] = rbx ? fh_df_from_pair(__ldcg(rbx + xbase + (i < Nx ? i : 1))) : fh_df{0.f, 0.f};
+  }
+  for (int t0 = 0; t0 < s - 1; t0 += kLayerBatch) {  // kLayerBatch layers per round trip
+    float2 d[kLayerBatch][kWPts];
+#pragma unroll
+    for (int u = 0; u < kLayerBatch; ++u)
+      if (t0 + u < s - 1)
+#pragma unroll
+        for (int e = 0; e < kWPts; ++e) {
+          const int i = 1 + wt + e * kWPerLine;
+          d[u][e] = __ldcg(tiny + (long long)(t0 + u) * a.g.P + xbase + (i < Nx ? i : 1));
+        }
+#pragma unroll
+    for (int u = 0; u < kLayerBatch; ++u)
+      if (t0 + u < s - 1) {
+        const fh_df w = fh_df_from_pair(wx[s][t0 + u]);
+#pragma unroll
+        for (int e = 0; e < kWPts; ++e) tsx[e] = fh_df_fma(w, fh_df_from_pair(d[u][e]), tsx[e]);
+      }
+  }
+}
+
 __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fuse_args a) {
   extern __shared__ float2 sbf[];
+  // cx/cy: step constants; wx/wy[s][t]: weight of layer j8 + t in step j8 + s
   __shared__ float2 cx[kSub][4], cy[kSub][4], wx[kSub][kSub], wy[kSub][kSub];
   const fh_tg_dev &g = a.g;
   const int Nx = g.sN, Ny = g.M;
   const int Lx = tg_line_stride(Nx), Ly = tg_line_stride(Ny);
   const int tid = threadIdx.x, warp = tid >> 5;
-  // x lines: 128 threads stage each line; arrays fa, g, al, pf, pb, bt
-  const int ln = tid >> 7, tg = tid & 127;
-  const int xline = 1 + blockIdx.x * 4 + ln;
-  const bool xlive = xline < g.M;
-  float2 *xa = sbf + (size_t)ln * 6 * Lx;
-  const long long xbase = (long long)xline * g.ld;
-  // y columns: four adjacent columns per row (32-byte segments)
-  float2 *ys = sbf + (size_t)4 * 6 * Lx;
-  const int col = tid & 3, rg = tid >> 2;
-  const int ycol = 1 + blockIdx.x * 4 + col;
-  const bool ylive = ycol < g.sN;
-  float2 *ya = ys + (size_t)col * 6 * Ly;
-  if (xlive) {
-    for (int i = 1 + tg; i < Nx; i += kXGroup) {
-      const long long id = xbase + i;
+  float2 *xs = sbf;                          // x lines: fa, g, al, pf, pb, bt (stride Lx)
+  float2 *ys = sbf + (size_t)4 * 6 * Lx;     // y columns: the same (stride Ly)
+  // fixed factor tables, all threads: x nodes line by line, y nodes row by row
+  // (four adjacent columns per row)
+  for (int v = tid; v < 4 * (Nx - 1); v += blockDim.x) {
+    const int ln = v / (Nx - 1), i = 1 + v % (Nx - 1);
+    const int line = 1 + blockIdx.x * 4 + ln;
+    if (line < g.M) {
+      float2 *xa = xs + (size_t)ln * 6 * Lx;
+      const long long id = (long long)line * g.ld + i;
       xa[fh_sk(i)] = a.fax[id];
       xa[Lx + fh_sk(i)] = a.gx[id];
       xa[2 * Lx + fh_sk(i)] = a.alx[id];
       xa[3 * Lx + fh_sk(i)] = a.pfx[id];
       xa[4 * Lx + fh_sk(i)] = a.pbx[id];
     }
-    if (tg == 0) xa[4 * Lx + fh_sk(0)] = a.pbx[xbase];
   }
-  if (ylive) {
-    for (int q = 1 + rg; q < Ny; q += kXGroup) {
+  for (int v = tid; v < 4 * (Ny - 1); v += blockDim.x) {
+    const int col = v & 3, q = 1 + (v >> 2);
+    const int ycol = 1 + blockIdx.x * 4 + col;
+    if (ycol < g.sN) {
+      float2 *ya = ys + (size_t)col * 6 * Ly;
       const long long id = ycol + (long long)q * g.ld;
       ya[fh_sk(q)] = a.fay[id];
       ya[Ly + fh_sk(q)] = a.gy[id];
@@ -775,10 +853,12 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
       ya[3 * Ly + fh_sk(q)] = a.pfy[id];
       ya[4 * Ly + fh_sk(q)] = a.pby[id];
     }
-    if (rg == 0) ya[4 * Ly + fh_sk(0)] = a.pby[ycol];
   }
-  // double-float step constants and sub-block weights of every step, one FP64
-  // conversion per thread
+  if (tid < 4 && 1 + (int)blockIdx.x * 4 + tid < g.M)
+    xs[(size_t)tid * 6 * Lx + 4 * Lx + fh_sk(0)] = a.pbx[(long long)(1 + blockIdx.x * 4 + tid) * g.ld];
+  if (tid >= 32 && tid < 36 && 1 + (int)blockIdx.x * 4 + (tid - 32) < g.sN)
+    ys[(size_t)(tid - 32) * 6 * Ly + 4 * Ly + fh_sk(0)] = a.pby[1 + blockIdx.x * 4 + (tid - 32)];
+  // double-float step constants and sub-block weights, one FP64 conversion per thread
   constexpr int kPer = 8 + 2 * kSub;
   for (int v = tid; v < a.ns * kPer; v += blockDim.x) {
     const int s = a.s0 + v / kPer, r = v % kPer;
@@ -802,111 +882,157 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
     }
     *dst = fh_df_pair(fh_df_from_double(val));
   }
+  __syncwarp();
   __syncthreads();
+
+  const bool worker = warp >= kSolveWarps;
+  const int wk = tid - 32 * kSolveWarps;  // worker index (negative for the solving warps)
+  // worker's x nodes: line wl, i = 1 + wt + 96 e
+  const int wl = worker ? wk / kWPerLine : 0, wt = worker ? wk % kWPerLine : 0;
+  const int xline = 1 + blockIdx.x * 4 + wl;
+  const bool xlive = worker && xline < g.M;
+  const long long xbase = (long long)xline * g.ld;
+  float2 *xa = xs + (size_t)wl * 6 * Lx;
+  // worker's y nodes: column col, q = 1 + wr + 96 e (four adjacent columns per row)
+  const int col = worker ? (wk & 3) : 0, wr = worker ? (wk >> 2) : 0;
+  const int ycol = 1 + blockIdx.x * 4 + col;
+  const bool ylive = worker && ycol < g.sN;
+  float2 *ya = ys + (size_t)col * 6 * Ly;
+  const float2 *tiny = a.D + (long long)a.j8 * g.P;  // layers of the sub-block
   const unsigned nblk = gridDim.x;
   unsigned nb = 0;
-  const float2 *tiny = a.D + (long long)a.j8 * g.P;
+
+  fh_df tsx[kWPts], tsy[kWPts];  // history parts of the worker's x / y nodes
+  float2 f[kWPts];               // old field at the worker's y nodes
+  if (xlive) tg_x_partial(a, a.s0, wx, tiny, xbase, wt, Nx, tsx);
+
   for (int s = a.s0; s < a.s0 + a.ns; ++s) {
     const int j = a.j8 + s;
-    const float2 *rbx = a.rb0 ? a.rb0 + (long long)s * a.rb_step : nullptr;
-    const float2 *rby = rbx ? rbx + a.rb_xy : nullptr;
-    // ---- x half step (fr_d_t_g_2d.cpp:2577-2590)
+    TG_STAMP(0);
+    // ---- x half step (fr_d_t_g_2d.cpp:2577-2590): field and newest layer
     if (xlive) {
       const fh_df kst = fh_df_from_pair(cx[s][0]), S2 = fh_df_from_pair(cx[s][1]), st = fh_df_from_pair(cx[s][2]);
-      float2 c[kUnroll];
-      fh_df ts[kUnroll];
+      const float2 *lat = s >= 1 ? tiny + (long long)(s - 1) * g.P : nullptr;
+      float2 c[kWPts], d[kWPts];
 #pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int i = 1 + tg + e * kXGroup;
+      for (int e = 0; e < kWPts; ++e) {
+        const int i = 1 + wt + e * kWPerLine;
         const long long id = xbase + (i < Nx ? i : 1);
         c[e] = __ldcg(a.Cd + id);
-        ts[e] = rbx ? fh_df_from_pair(__ldcg(rbx + id)) : fh_df{0.f, 0.f};
+        d[e] = lat ? __ldcg(lat + id) : make_float2(0.f, 0.f);
       }
+      const fh_df wl_ = s >= 1 ? fh_df_from_pair(wx[s][s - 1]) : fh_df{0.f, 0.f};
 #pragma unroll
-      for (int t = 0; t < kSub - 1; ++t)
-        if (t < s) {
-          const fh_df w = fh_df_from_pair(wx[s][t]);
-#pragma unroll
-          for (int e = 0; e < kUnroll; ++e) {
-            const int i = 1 + tg + e * kXGroup;
-            ts[e] = fh_df_fma(w, fh_df_from_pair(__ldcg(tiny + (long long)t * g.P + xbase + (i < Nx ? i : 1))), ts[e]);
-          }
-        }
-#pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int i = 1 + tg + e * kXGroup;
+      for (int e = 0; e < kWPts; ++e) {
+        const int i = 1 + wt + e * kWPerLine;
         if (i < Nx) {
+          const fh_df ts = lat ? fh_df_fma(wl_, fh_df_from_pair(d[e]), tsx[e]) : tsx[e];
           fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
-          om = fh_df_fma(st, ts[e], om);
+          om = fh_df_fma(st, ts, om);
           xa[5 * Lx + fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(xa[Lx + fh_sk(i)]), om)));
         }
       }
     }
     __syncthreads();
-    if (warp < 4 && 1 + (int)blockIdx.x * 4 + warp < g.M) {
-      float2 *w = sbf + (size_t)warp * 6 * Lx;
-      fh_line_solve_prefix_df(Nx, w, w + 5 * Lx, w + 2 * Lx, w + 3 * Lx, w + 4 * Lx, fh_df{0.f, 0.f},
-                              fh_df_from_pair(cx[s][3]), w + 5 * Lx, w + 5 * Lx);
+    TG_STAMP(1);
+    if (!worker) {
+      if (1 + (int)blockIdx.x * 4 + warp < g.M) {
+        float2 *w = xs + (size_t)warp * 6 * Lx;
+        fh_line_solve_prefix_df(Nx, w, w + 5 * Lx, w + 2 * Lx, w + 3 * Lx, w + 4 * Lx, fh_df{0.f, 0.f},
+                                fh_df_from_pair(cx[s][3]), w + 5 * Lx, w + 5 * Lx);
+      }
+    } else if (ylive) {
+      // y history part of this step (all its layers are complete) and the old field
+      const float2 *rby = a.rb0 ? a.rb0 + (long long)s * a.rb_step + a.rb_xy : nullptr;
+#pragma unroll
+      for (int e = 0; e < kWPts; ++e) {
+        const int q = 1 + wr + e * kWPerLine;
+        const long long id = ycol + (long long)(q < Ny ? q : 1) * g.ld;
+        f[e] = __ldcg(a.Cd + id);
+        tsy[e] = rby ? fh_df_from_pair(__ldcg(rby + id)) : fh_df{0.f, 0.f};
+      }
+      for (int t0 = 0; t0 < s; t0 += kLayerBatch) {
+        float2 d[kLayerBatch][kWPts];
+#pragma unroll
+        for (int u = 0; u < kLayerBatch; ++u)
+          if (t0 + u < s)
+#pragma unroll
+            for (int e = 0; e < kWPts; ++e) {
+              const int q = 1 + wr + e * kWPerLine;
+              d[u][e] = __ldcg(tiny + (long long)(t0 + u) * g.P + ycol + (long long)(q < Ny ? q : 1) * g.ld);
+            }
+#pragma unroll
+        for (int u = 0; u < kLayerBatch; ++u)
+          if (t0 + u < s) {
+            const fh_df w = fh_df_from_pair(wy[s][t0 + u]);
+#pragma unroll
+            for (int e = 0; e < kWPts; ++e) tsy[e] = fh_df_fma(w, fh_df_from_pair(d[u][e]), tsy[e]);
+          }
+      }
     }
     __syncthreads();
-    if (xlive)
-      for (int i = tg; i <= Nx + 1; i += kXGroup) {
-        const float2 v = xa[5 * Lx + fh_sk(i)];
-        a.Chd[xbase + i] = v;
-        if (i == 0 || i >= Nx) a.Cd[xbase + i] = v;
+    TG_STAMP(2);
+    if (xlive) {
+#pragma unroll
+      for (int e = 0; e < kWPts; ++e) {
+        const int i = 1 + wt + e * kWPerLine;
+        if (i < Nx) a.Chd[xbase + i] = xa[5 * Lx + fh_sk(i)];
       }
+    }
+    if (warp == kBarWarp && (tid & 31) < 12) {  // nodes 0, Nx, Nx+1 of the four lines
+      const int l = (tid & 31) / 3, k = (tid & 31) % 3;
+      const int line = 1 + blockIdx.x * 4 + l;
+      if (line < g.M) {
+        const int i = k == 0 ? 0 : Nx - 1 + k;
+        const float2 v = xs[(size_t)l * 6 * Lx + 5 * Lx + fh_sk(i)];
+        a.Chd[(long long)line * g.ld + i] = v;
+        a.Cd[(long long)line * g.ld + i] = v;
+      }
+    }
+    __syncwarp();
     if (!tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
-    // ---- y half step (fr_d_t_g_2d.cpp:2591-2606); D[j] = new field - old field
-    float2 f[kUnroll];
+    TG_STAMP(3);
+    // ---- y half step (fr_d_t_g_2d.cpp:2591-2606): the half-step field
     if (ylive) {
       const fh_df kst = fh_df_from_pair(cy[s][0]), kyh = fh_df_from_pair(cy[s][1]), S2 = fh_df_from_pair(cy[s][2]),
                   st = fh_df_from_pair(cy[s][3]);
-      float2 c[kUnroll];
-      fh_df ts[kUnroll];
+      float2 c[kWPts];
 #pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int q = 1 + rg + e * kXGroup;
-        const long long id = ycol + (long long)(q < Ny ? q : 1) * g.ld;
-        c[e] = __ldcg(a.Chd + id);
-        f[e] = __ldcg(a.Cd + id);
-        ts[e] = rby ? fh_df_from_pair(__ldcg(rby + id)) : fh_df{0.f, 0.f};
+      for (int e = 0; e < kWPts; ++e) {
+        const int q = 1 + wr + e * kWPerLine;
+        c[e] = __ldcg(a.Chd + ycol + (long long)(q < Ny ? q : 1) * g.ld);
       }
 #pragma unroll
-      for (int t = 0; t < kSub - 1; ++t)
-        if (t < s) {
-          const fh_df w = fh_df_from_pair(wy[s][t]);
-#pragma unroll
-          for (int e = 0; e < kUnroll; ++e) {
-            const int q = 1 + rg + e * kXGroup;
-            ts[e] = fh_df_fma(w, fh_df_from_pair(__ldcg(tiny + (long long)t * g.P + ycol + (long long)(q < Ny ? q : 1) * g.ld)),
-                              ts[e]);
-          }
-        }
-#pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int q = 1 + rg + e * kXGroup;
+      for (int e = 0; e < kWPts; ++e) {
+        const int q = 1 + wr + e * kWPerLine;
         if (q < Ny) {
           const fh_df cc = fh_df_from_pair(c[e]);
           // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
-          const fh_df t = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), ts[e]);
+          const fh_df tt = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), tsy[e]);
           fh_df om = fh_df_fma(kst, cc, S2);
-          om = fh_df_fma(st, t, om);
+          om = fh_df_fma(st, tt, om);
           ya[5 * Ly + fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(ya[Ly + fh_sk(q)]), om)));
         }
       }
     }
     __syncthreads();
-    if (warp < 4 && 1 + (int)blockIdx.x * 4 + warp < g.sN) {
-      float2 *w = ys + (size_t)warp * 6 * Ly;
-      fh_line_solve_prefix_df(Ny, w, w + 5 * Ly, w + 2 * Ly, w + 3 * Ly, w + 4 * Ly, fh_df{1.f, 0.f},
-                              fh_df{0.f, 0.f}, w + 5 * Ly, w + 5 * Ly);
+    TG_STAMP(4);
+    if (!worker) {
+      if (1 + (int)blockIdx.x * 4 + warp < g.sN) {
+        float2 *w = ys + (size_t)warp * 6 * Ly;
+        fh_line_solve_prefix_df(Ny, w, w + 5 * Ly, w + 2 * Ly, w + 3 * Ly, w + 4 * Ly, fh_df{1.f, 0.f},
+                                fh_df{0.f, 0.f}, w + 5 * Ly, w + 5 * Ly);
+      }
+    } else if (xlive && s + 1 < a.s0 + a.ns) {
+      tg_x_partial(a, s + 1, wx, tiny, xbase, wt, Nx, tsx);  // layers up to j - 1 are complete
     }
     __syncthreads();
+    TG_STAMP(5);
     if (ylive) {
       float2 *Dj = a.D + (long long)j * g.P;
 #pragma unroll
-      for (int e = 0; e < kUnroll; ++e) {
-        const int q = 1 + rg + e * kXGroup;
+      for (int e = 0; e < kWPts; ++e) {
+        const int q = 1 + wr + e * kWPerLine;
         if (q < Ny) {
           const long long id = ycol + (long long)q * g.ld;
           const float2 u = ya[5 * Ly + fh_sk(q)];
@@ -914,13 +1040,15 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
           Dj[id] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[e])));
         }
       }
-      if (rg == 0) {
+      if (wr == kWPerLine - 1) {  // boundary nodes: lanes of warp kBarWarp
         a.Cd[ycol] = ya[5 * Ly + fh_sk(0)];
         a.Cd[ycol + (long long)Ny * g.ld] = ya[5 * Ly + fh_sk(Ny)];
         a.Cd[ycol + (long long)(Ny + 1) * g.ld] = ya[5 * Ly + fh_sk(Ny + 1)];
       }
     }
+    __syncwarp();
     if (s + 1 < a.s0 + a.ns && !tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
+    TG_STAMP(6);
   }
 }
 
