@@ -590,6 +590,8 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
 static constexpr int kMidThreads = 128;
 static constexpr int kMidMaxK = kTgBlock - kSub;  // 56 layers at most
 
+// PPT points per thread (consecutive), (hi, lo) loads of 8 PPT bytes.
+template <int PPT>
 __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restrict__ D, long long P, int K,
                                                           const double *__restrict__ W, int ldw, int nr,
                                                           const float2 *__restrict__ far, long long ldfar,
@@ -604,21 +606,21 @@ __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restr
     ws[row][k] = make_float2(wh, __double2float_rn(w - (double)wh));
   }
   __syncthreads();
-  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * PPT;
   if (p >= P) return;
-  float ah[R][2], al[R][2];
+  float ah[R][PPT], al[R][PPT];
 #pragma unroll
-  for (int row = 0; row < R; ++row) {
-    if (far && (row >> 1) < nr) {
-      const float4 f = *reinterpret_cast<const float4 *>(far + (long long)row * ldfar + p);
-      ah[row][0] = f.x;
-      al[row][0] = f.y;
-      ah[row][1] = f.z;
-      al[row][1] = f.w;
-    } else {
-      ah[row][0] = ah[row][1] = al[row][0] = al[row][1] = 0.f;
+  for (int row = 0; row < R; ++row)
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+      if (far && (row >> 1) < nr) {
+        const float2 f = far[(long long)row * ldfar + p + q];
+        ah[row][q] = f.x;
+        al[row][q] = f.y;
+      } else {
+        ah[row][q] = al[row][q] = 0.f;
+      }
     }
-  }
   auto acc = [](const float2 w, const float dh, const float dl, float &sh, float &sl) {
     const float ph = w.x * dh;
     float pl = fmaf(w.x, dh, -ph);
@@ -630,26 +632,27 @@ __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restr
     sh = t;
     sl += e + pl;
   };
-  const float4 *d = reinterpret_cast<const float4 *>(D + p);
-  const long long ld4 = P / 2;
+  const float2 *d = D + p;
   int k = 0;
   for (; k + 4 <= K; k += 4) {
-    float4 v[4];
+    float2 v[4][PPT];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = __ldcs(d + (long long)(k + u) * ld4);
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int q = 0; q < PPT; ++q) v[u][q] = __ldcs(d + (long long)(k + u) * P + q);
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int row = 0; row < R; ++row) {
         const float2 w = ws[row][k + u];
-        acc(w, v[u].x, v[u].y, ah[row][0], al[row][0]);
-        acc(w, v[u].z, v[u].w, ah[row][1], al[row][1]);
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) acc(w, v[u][q].x, v[u][q].y, ah[row][q], al[row][q]);
       }
     if ((k & 15) == 12) {
 #pragma unroll
       for (int row = 0; row < R; ++row)
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {  // renormalise (fast two-sum, |ah| >= |al|)
+        for (int q = 0; q < PPT; ++q) {  // renormalise (fast two-sum, |ah| >= |al|)
           const float t = ah[row][q] + al[row][q];
           al[row][q] = al[row][q] - (t - ah[row][q]);
           ah[row][q] = t;
@@ -657,26 +660,27 @@ __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restr
     }
   }
   for (; k < K; ++k) {
-    const float4 v = __ldcs(d + (long long)k * ld4);
+    float2 v[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) v[q] = __ldcs(d + (long long)k * P + q);
 #pragma unroll
     for (int row = 0; row < R; ++row) {
       const float2 w = ws[row][k];
-      acc(w, v.x, v.y, ah[row][0], al[row][0]);
-      acc(w, v.z, v.w, ah[row][1], al[row][1]);
+#pragma unroll
+      for (int q = 0; q < PPT; ++q) acc(w, v[q].x, v[q].y, ah[row][q], al[row][q]);
     }
   }
 #pragma unroll
   for (int row = 0; row < R; ++row) {
     if ((row >> 1) >= nr) continue;
-    float h[2], l[2];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      h[q] = ah[row][q] + al[row][q];
-      l[q] = al[row][q] - (h[q] - ah[row][q]);
+    for (int q = 0; q < PPT; ++q) {
+      const float h = ah[row][q] + al[row][q];
+      out[(long long)row * ldo + p + q] = make_float2(h, al[row][q] - (h - ah[row][q]));
     }
-    *reinterpret_cast<float4 *>(out + (long long)row * ldo + p) = make_float4(h[0], l[0], h[1], l[1]);
   }
 }
+static constexpr int kMidPPT = 1;  // points per thread of k_tg_mid_df
 
 // ------------------------------------------------ fused sub-block sweeps
 // One cooperative launch runs both half steps of up to kSub consecutive steps
@@ -1115,7 +1119,8 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       if (j == j8) {
         const int nr = min(kSub, s->max_steps - j8);
         fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-        k_tg_mid_df<<<(unsigned)fh_ceil_div(g.P, 2LL * kMidThreads), kMidThreads, 0, ctx->stream>>>(
+        k_tg_mid_df<kMidPPT><<<(unsigned)fh_ceil_div(g.P, (long long)kMidPPT * kMidThreads), kMidThreads, 0,
+                                ctx->stream>>>(
             D2 + (long long)j0 * g.P, g.P, j8 - j0, s->W.as<double>() + (long long)j8 * 2 * ldw + j0, ldw, nr,
             farj, s->ldfar, part, g.P);
         fh_prof_mark(ctx, FH_PROF_HISTORY, true);
