@@ -129,7 +129,7 @@ def peaks():
 def profile_traffic_ratio(name: str):
     """dram bytes / algorithmic bytes of an ncu capture summarised in profiles/<name>."""
     tp = os.path.join(REPO, "profiles", name)
-    if not os.path.exists(tp):
+    if not name or not os.path.isfile(tp):
         return None
     for line in open(tp):
         if line.startswith("traffic_ratio:"):
