@@ -69,7 +69,7 @@ def test_tg_blocked_mode_vs_fp64_oracle(ctx, sN, M, steps):
     assert err <= 1e-9, err
 
 
-@pytest.mark.parametrize("n", [300, 520])
+@pytest.mark.parametrize("n", [100, 300, 520])
 def test_ab_blocked_mode_vs_oracle(ctx, n):
     """Atangana-Baleanu solve with the entries older than the current 128-step
     block contracted on the tensor cores: relative max-norm <= 1e-9 vs the
@@ -188,3 +188,24 @@ def test_tg_blocked_wide_grid(ctx):
     err, _ = _blocked_vs_fp64(ctx, p, V2, C0, [130])
     print(f"blocked 600x40: {err:.3e}")
     assert err <= 1e-9, err
+
+
+def test_ab_blocked_uneven_step_calls(ctx):
+    """AB blocked mode advanced in calls that start and end inside 8-step
+    sub-blocks and 128-step blocks: the same field as one call over all steps."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_AB_BLOCKED
+    from theses_code_gb300.solvers import ABSolver
+    cfg, src, bl, br, C0 = workloads.ab_1d(m=256, alpha=0.6, tau=1e-3, seed=3)
+    out = []
+    for calls in ([1, 7, 13, 50, 100, 129], [300]):
+        s = ABSolver(ctx, cfg["m"], 300, cfg["tau"], cfg["alpha"], FH_AB_BLOCKED)
+        s.set_source(src, bl, br)
+        s.set_c(C0)
+        for n in calls:
+            s.calc_step(n)
+        out.append(s.get_c())
+        s.close()
+    diff = np.max(np.abs(out[0] - out[1])) / np.max(np.abs(out[1]))
+    print(f"AB uneven calls vs one call: {diff:.3e}")
+    assert diff <= 1e-13, diff

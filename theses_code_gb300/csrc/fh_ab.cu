@@ -33,6 +33,8 @@ struct fh_ab_solver {
   fh_dbuf far;            // far rows ((hi, lo) pairs) of the steps T0+1 .. T0+128
   long long ldfar = 0;
   int T0 = 0;
+  bool fused = false;     // blocked mode: 8-step launches of k_ab_line_fused
+  fh_dbuf mid;            // history rows of the current 8-step sub-block
   ~fh_ab_solver() {
     if (blk) fh_blk_delete(blk);
   }
@@ -169,12 +171,146 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
   }
 }
 
+// ------------------------------------------------ blocked mode: 8-step sub-blocks
+// The history of step i (entries tt < K = i - 1) splits into the far rows of
+// the current 128-step block (tt < T0, tensor cores), the sub-block rows
+// (T0 <= tt < K8, k_ab_mid, once per 8 steps) and the at most 7 entries of the
+// sub-block itself (K8 <= tt < K), which k_ab_line_fused adds while it runs
+// the 8 steps of the sub-block in one launch.
+static constexpr int kAbSub = 8;
+static constexpr int kAbFuseThreads = 512;
+
+// mid[r][j] = far row of step K8 + r + sum_{T0 <= tt < K8} w[K8 + r + 1 - tt] D[tt][j], r < nr
+__global__ void k_ab_mid(int m, long long P, int T0, int K8, int nr, const double *__restrict__ w,
+                         const double *__restrict__ D, const float2 *__restrict__ far, long long ldfar,
+                         double *__restrict__ mid) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (j > m || r >= nr) return;
+  const int i = K8 + r + 1;  // reference step index of row r
+  double acc = 0.0;
+  for (int tt = T0; tt < K8; ++tt) acc = fma(__ldg(w + i - tt), D[(long long)tt * P + j], acc);
+  if (far) {
+    const float2 f = far[(long long)(K8 + r - T0) * ldfar + j];
+    acc += (double)f.x + (double)f.y;
+  }
+  mid[(long long)r * P + j] = acc;
+}
+
+// Steps K8 + s0 .. K8 + s0 + ns - 1 of one sub-block in one CTA: the fixed
+// elimination tables and the field stay in shared memory for the whole
+// launch; per step the right parts (source row, sub-block row or far row, the
+// sub-block's own entries), the solve of k_ab_line (four warps) and the new
+// history entry.
+__global__ void __launch_bounds__(kAbFuseThreads, 1)
+    k_ab_line_fused(int m, double oma, const double *__restrict__ ii, const double *__restrict__ alg,
+                    const double *__restrict__ invg, const double *__restrict__ slg, const double *__restrict__ pfg,
+                    const double *__restrict__ pbg, const double *__restrict__ src, int nrows,
+                    const double *__restrict__ blp, const double *__restrict__ brp, double *C, double *D,
+                    long long P, const double *__restrict__ w, const double *__restrict__ mid,
+                    const float2 *__restrict__ far8, long long ldfar, int K8, int s0, int ns, double tau) {
+  extern __shared__ double sm[];
+  const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
+  const int Lm = m + 2 + m / ch + 1;
+  double *rb = sm, *sl = rb + Lm, *pf = sl + Lm, *al = pf + Lm, *pb = al + Lm, *bt = pb + Lm, *cv = bt + Lm,
+         *inv = cv + Lm, *Cs = inv + Lm;
+  auto sk = [ch](int j) { return j + j / ch; };
+  __shared__ double cst[3], wts[kAbSub][kAbSub];
+  for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
+    sl[sk(j)] = slg[j];
+    pf[sk(j)] = pfg[j];
+    al[sk(j)] = alg[j];
+    pb[sk(j)] = pbg[j];
+    inv[j] = invg[j];
+    Cs[j] = C[j];
+  }
+  // step constants (FP64 divisions are scarce on this GPU) and the weights of
+  // the sub-block's entries: wts[s][t] = w[(K8 + s + 1) - (K8 + t)]
+  if (threadIdx.x == 0) {
+    cst[0] = ii[0] / oma;  // Ii/(1-a)
+    cst[1] = 1.0 / oma;
+    cst[2] = 1.0 / tau;
+  }
+  if (threadIdx.x < kAbSub * kAbSub) {
+    const int ss = threadIdx.x / kAbSub, t = threadIdx.x % kAbSub;
+    wts[ss][t] = t < ss ? w[ss + 1 - t] : 0.0;
+  }
+  __syncthreads();
+  const double cI = cst[0], ioma = cst[1], itau = cst[2];
+  __shared__ fh_aff scan_sm[kAbSolveWarps];
+  for (int s = s0; s < s0 + ns; ++s) {
+    const int K = K8 + s;  // history entries of this step (reference step i = K + 1)
+    const int row = K < nrows - 1 ? K : nrows - 1;
+    const double *srow = src + (long long)row * (m + 1);
+    const double *mrow = mid ? mid + (long long)s * P : nullptr;
+    const float2 *frow = far8 ? far8 + (long long)s * ldfar : nullptr;
+    const bool hist = mrow || frow || s > 0;
+    for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
+      double r = fma(cI, Cs[j], srow[j]);
+      if (hist) {  // MF_intF_simple returns ret/(1-a)
+        double sv = mrow ? mrow[j] : 0.0;
+        if (frow) sv += (double)frow[j].x + (double)frow[j].y;
+        for (int t = 0; t < s; ++t) sv = fma(wts[s][t], __ldcg(D + (long long)(K8 + t) * P + j), sv);
+        r -= sv * ioma;
+      }
+      rb[sk(j)] = r * inv[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < kAbSolveThreads) {
+      const int t = threadIdx.x;
+      const double bl = blp[row], br = brp[row];
+      const int f0 = 1 + t * ch, f1 = min(m + 1, f0 + ch);
+      double b = 0.0;
+      for (int j = f0; j < f1; ++j) {
+        b = fma(sl[sk(j)], b, rb[sk(j)]);
+        bt[sk(j)] = b;
+      }
+      const fh_aff Pf = fh_group_exclusive_affine<kAbSolveWarps>(f1 > f0 ? fh_aff{pf[sk(f1 - 1)], b}
+                                                                         : fh_aff{1.0, 0.0},
+                                                                 scan_sm, 1);
+      const double s0v = fma(Pf.a, bl, Pf.b);  // bt[f0 - 1]
+      for (int j = f0; j < f1; ++j) bt[sk(j)] = fma(pf[sk(j)], s0v, bt[sk(j)]);
+      if (t == 0) bt[sk(0)] = bl;
+      fh_group_bar(1, kAbSolveThreads);
+      const int b0 = t * ch, b1 = min(m, b0 + ch);
+      double c = 0.0;
+      for (int j = b1 - 1; j >= b0; --j) {
+        c = fma(-al[sk(j)], c, bt[sk(j)]);
+        cv[sk(j)] = c;
+      }
+      const fh_aff Pb = fh_group_exclusive_affine_rev<kAbSolveWarps>(b1 > b0 ? fh_aff{pb[sk(b0)], c}
+                                                                             : fh_aff{1.0, 0.0},
+                                                                     scan_sm, 1);
+      const double tv = fma(Pb.a, br, Pb.b);  // C[b1]
+      for (int j = b0; j < b1; ++j) cv[sk(j)] = fma(pb[sk(j)], tv, cv[sk(j)]);
+      if (t == 0) cv[sk(m)] = br;
+    }
+    __syncthreads();
+    double *Dk = D + (long long)K * P;
+    for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
+      const double v = cv[sk(j)];
+      Dk[j] = (v - Cs[j]) * itau;
+      Cs[j] = v;
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) C[j] = Cs[j];
+}
+
+static size_t ab_fused_smem(int m) {
+  const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
+  return sizeof(double) * (8 * (size_t)(m + 2 + m / ch + 1) + (size_t)m + 1);
+}
+
 static size_t ab_line_smem(int m) {
   const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
   return sizeof(double) * 7 * (size_t)(m + 2 + m / ch + 1);
 }
 
-static int ab_one_step(fh_ab_solver *s) {
+static int ab_fused_steps(fh_ab_solver *s, int max_n, int *done);
+
+static int ab_one_step(fh_ab_solver *s, int max_n, int *done) {
+  *done = 1;
   fh_ctx *ctx = s->ctx;
   const int i = s->step + 1;  // reference step index (1-based)
   const int K = i - 1;        // history entries dC_0 .. dC_{i-2}
@@ -191,6 +327,7 @@ static int ab_one_step(fh_ab_solver *s) {
     if ((rc = fh_blk_gemm(ctx, *s->blk, K, s->far.as<float2>(), s->ldfar))) return rc;
     s->T0 = K;
   }
+  if (s->fused) return ab_fused_steps(s, max_n, done);
   const int k0 = s->blk ? s->T0 : 0;  // entries summed on the CUDA cores this step
   const int kn = K - k0;
   const float2 *far = (s->blk && s->T0 > 0) ? s->far.as<float2>() + (long long)(K - s->T0) * s->ldfar : nullptr;
@@ -220,6 +357,39 @@ static int ab_one_step(fh_ab_solver *s) {
   return FH_OK;
 }
 
+// Blocked mode: the block-start work of step K is already enqueued; runs up to
+// max_n steps of the current 8-step sub-block (k_ab_mid first at its start).
+static int ab_fused_steps(fh_ab_solver *s, int max_n, int *done) {
+  fh_ctx *ctx = s->ctx;
+  const int K = s->step;
+  const int T0 = s->blk ? s->T0 : 0;
+  const int K8 = (K / kAbSub) * kAbSub;  // >= T0: blocks are whole sub-blocks
+  int rc;
+  if (K == K8 && K8 > T0) {
+    const int nr = min(kAbSub, s->max_steps - K8);
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+    k_ab_mid<<<dim3((unsigned)fh_ceil_div(s->m + 1, 128), (unsigned)nr), 128, 0, ctx->stream>>>(
+        s->m, s->P, T0, K8, nr, s->w.as<double>(), s->D.as<double>(),
+        (s->blk && T0 > 0) ? s->far.as<float2>() : nullptr, s->ldfar, s->mid.as<double>());
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+    if ((rc = fh_after_launch(ctx, "k_ab_mid"))) return rc;
+  }
+  const double *mid = K8 > T0 ? s->mid.as<double>() : nullptr;
+  const float2 *far8 = (!mid && s->blk && T0 > 0) ? s->far.as<float2>() + (long long)(K8 - T0) * s->ldfar : nullptr;
+  const int ns = min(max_n, kAbSub - (K - K8));
+  fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+  k_ab_line_fused<<<1, kAbFuseThreads, ab_fused_smem(s->m), ctx->stream>>>(
+      s->m, 1.0 - s->alpha, s->ii.as<double>(), s->al.as<double>(), s->inv.as<double>(), s->sl.as<double>(),
+      s->pf.as<double>(), s->pb.as<double>(), s->src.as<double>(), s->nrows, s->bl.as<double>(),
+      s->br.as<double>(), s->C.as<double>(), s->D.as<double>(), s->P, s->w.as<double>(), mid, far8, s->ldfar, K8,
+      K - K8, ns, s->tau);
+  fh_prof_mark(ctx, FH_PROF_SWEEP, true);
+  if ((rc = fh_after_launch(ctx, "k_ab_line_fused"))) return rc;
+  s->step += ns;
+  *done = ns;
+  return FH_OK;
+}
+
 extern "C" {
 
 int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh_ab_solver **out) {
@@ -231,6 +401,7 @@ int fh_ab_create(fh_ctx *ctx, int m, int max_steps, double tau, double alpha, fh
     const size_t sm = ab_line_smem(m);
     FH_REQUIRE(ctx, sm <= 200 * 1024, FH_EINVAL, "fh_ab_create: m too large for the staged line (m <= 3500)");
     FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ab_line, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ab_line_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   }
   fh_ab_solver *s = new fh_ab_solver();
   s->ctx = ctx;
@@ -359,6 +530,12 @@ int fh_ab_set_mode(fh_ab_solver *s, int mode) {
     fh_blk_delete(s->blk);
     s->blk = nullptr;
   }
+  // 8-step launches when the tables and the field fit in shared memory
+  s->fused = mode == FH_AB_BLOCKED && ab_fused_smem(s->m) <= 200 * 1024;
+  if (s->fused && !s->mid.p) {
+    const int rc = fh_alloc(ctx, s->mid, sizeof(double) * kAbSub * (size_t)s->P);
+    if (rc) return rc;
+  }
   s->graph.reset();
   return FH_OK;
 }
@@ -370,8 +547,8 @@ int fh_ab_step(fh_ab_solver *s, int nsteps) {
   FH_REQUIRE(ctx, nsteps >= 0 && s->step + nsteps <= s->max_steps, FH_ENOMEM, "fh_ab_step: history full");
   if (ctx->graphs && s->step == 0 && nsteps > 1) {
     int rc = fh_graph_run(ctx, s->graph, nsteps, [&]() {
-      for (int n = 0; n < nsteps; ++n) {
-        int r = ab_one_step(s);
+      for (int n = 0, d = 1; n < nsteps; n += d) {
+        int r = ab_one_step(s, nsteps - n, &d);
         if (r) return r;
       }
       return (int)FH_OK;
@@ -380,8 +557,8 @@ int fh_ab_step(fh_ab_solver *s, int nsteps) {
     s->step = nsteps;
     return FH_OK;
   }
-  for (int n = 0; n < nsteps; ++n) {
-    int rc = ab_one_step(s);
+  for (int n = 0, d = 1; n < nsteps; n += d) {
+    int rc = ab_one_step(s, nsteps - n, &d);
     if (rc) return rc;
   }
   return FH_OK;
