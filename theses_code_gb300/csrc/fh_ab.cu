@@ -9,6 +9,7 @@
 #include "fh_internal.h"
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
+#include "fh_df.cuh"
 
 // blocked contraction helpers (fh_blocked.cu)
 struct fh_blk;
@@ -33,8 +34,12 @@ struct fh_ab_solver {
   fh_dbuf far;            // far rows ((hi, lo) pairs) of the steps T0+1 .. T0+128
   long long ldfar = 0;
   int T0 = 0;
-  bool fused = false;     // blocked mode: 8-step launches of k_ab_line_fused
-  fh_dbuf mid;            // history rows of the current 8-step sub-block
+  // blocked mode with the line in shared memory: 8-step launches of
+  // k_ab_line_fused in double-float; history entries, lag weights, source rows
+  // and elimination tables as (hi, lo) FP32 pairs
+  bool fused = false;
+  fh_dbuf mid;            // history rows of the current 8-step sub-block (pairs)
+  fh_dbuf w2, src2, tab2; // pairs: lag weights, source rows, tables sl, pf, -al, pb, inv
   ~fh_ab_solver() {
     if (blk) fh_blk_delete(blk);
   }
@@ -179,127 +184,225 @@ __global__ void __launch_bounds__(kAbThreads) k_ab_line(int m, double oma, const
 // the 8 steps of the sub-block in one launch.
 static constexpr int kAbSub = 8;
 static constexpr int kAbFuseThreads = 512;
+static constexpr int kAbFuseMaxNodes = 5;  // nodes per thread: m + 1 <= 2560
 
-// mid[r][j] = far row of step K8 + r + sum_{T0 <= tt < K8} w[K8 + r + 1 - tt] D[tt][j], r < nr
-__global__ void k_ab_mid(int m, long long P, int T0, int K8, int nr, const double *__restrict__ w,
-                         const double *__restrict__ D, const float2 *__restrict__ far, long long ldfar,
-                         double *__restrict__ mid) {
+// mid[r][j] = far row of step K8 + r + sum_{T0 <= tt < K8} w[K8 + r + 1 - tt] D[tt][j], r < nr,
+// in double-float (D and w as (hi, lo) pairs, TwoSum accumulation as in
+// k_hist_sum_df), one node and one row per thread.
+__global__ void k_ab_mid(int m, long long P, int T0, int K8, int nr, const float2 *__restrict__ w2,
+                         const float2 *__restrict__ D, const float2 *__restrict__ far, long long ldfar,
+                         float2 *__restrict__ mid) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
   if (j > m || r >= nr) return;
   const int i = K8 + r + 1;  // reference step index of row r
-  double acc = 0.0;
-  for (int tt = T0; tt < K8; ++tt) acc = fma(__ldg(w + i - tt), D[(long long)tt * P + j], acc);
-  if (far) {
-    const float2 f = far[(long long)(K8 + r - T0) * ldfar + j];
-    acc += (double)f.x + (double)f.y;
+  fh_df acc{0.f, 0.f};
+  if (far) acc = fh_df_from_pair(far[(long long)(K8 + r - T0) * ldfar + j]);
+  float sh = acc.h, sl = acc.l;
+  for (int tt = T0; tt < K8; ++tt) {
+    const float2 w = __ldg(w2 + i - tt);
+    const float2 d = D[(long long)tt * P + j];
+    const float ph = w.x * d.x;
+    float pl = fmaf(w.x, d.x, -ph);
+    pl = fmaf(w.x, d.y, pl);
+    pl = fmaf(w.y, d.x, pl);
+    const float t = sh + ph;
+    const float bb = t - sh;
+    const float e = (sh - (t - bb)) + (ph - bb);
+    sh = t;
+    sl += e + pl;
+    if ((tt & 15) == 15) {  // renormalise
+      const float u = sh + sl;
+      sl = sl - (u - sh);
+      sh = u;
+    }
   }
-  mid[(long long)r * P + j] = acc;
+  const float h = sh + sl;
+  mid[(long long)r * P + j] = make_float2(h, sl - (h - sh));
 }
 
-// Steps K8 + s0 .. K8 + s0 + ns - 1 of one sub-block in one CTA: the fixed
-// elimination tables and the field stay in shared memory for the whole
-// launch; per step the right parts (source row, sub-block row or far row, the
-// sub-block's own entries), the solve of k_ab_line (four warps) and the new
-// history entry.
+// Steps K8 + s0 .. K8 + s0 + ns - 1 of one sub-block in one CTA, in
+// double-float: the elimination tables and the field stay in shared memory
+// for the whole launch; per step the right parts (source row, sub-block row or
+// far row, the sub-block's own entries), the solve of k_ab_line (four warps,
+// double-float group scans) and the new history entry dC/tau.  FP64 only
+// converts the field at the start and the end of the launch.  Every thread
+// keeps the right-part loads of all its nodes (j = tid + 512 k) in flight at
+// once, the sub-block's entries two per round trip.
 __global__ void __launch_bounds__(kAbFuseThreads, 1)
-    k_ab_line_fused(int m, double oma, const double *__restrict__ ii, const double *__restrict__ alg,
-                    const double *__restrict__ invg, const double *__restrict__ slg, const double *__restrict__ pfg,
-                    const double *__restrict__ pbg, const double *__restrict__ src, int nrows,
-                    const double *__restrict__ blp, const double *__restrict__ brp, double *C, double *D,
-                    long long P, const double *__restrict__ w, const double *__restrict__ mid,
-                    const float2 *__restrict__ far8, long long ldfar, int K8, int s0, int ns, double tau) {
-  extern __shared__ double sm[];
+    k_ab_line_fused(int m, double oma, const double *__restrict__ ii, const float2 *__restrict__ tab,
+                    long long ldt, const float2 *__restrict__ src2, int nrows, const double *__restrict__ blp,
+                    const double *__restrict__ brp, double *C, float2 *D, long long P,
+                    const float2 *__restrict__ w2, const float2 *__restrict__ mid, const float2 *__restrict__ far8,
+                    long long ldfar, int K8, int s0, int ns, double tau) {
+  constexpr int NMAX = kAbFuseMaxNodes;  // nodes per thread
+  extern __shared__ float2 smf[];
   const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
   const int Lm = m + 2 + m / ch + 1;
-  double *rb = sm, *sl = rb + Lm, *pf = sl + Lm, *al = pf + Lm, *pb = al + Lm, *bt = pb + Lm, *cv = bt + Lm,
+  float2 *rb = smf, *sl = rb + Lm, *pf = sl + Lm, *nal = pf + Lm, *pb = nal + Lm, *bt = pb + Lm, *cv = bt + Lm,
          *inv = cv + Lm, *Cs = inv + Lm;
   auto sk = [ch](int j) { return j + j / ch; };
-  __shared__ double cst[3], wts[kAbSub][kAbSub];
+  __shared__ float2 cst[3], wts[kAbSub][kAbSub], bnd[kAbSub][2];
   for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
-    sl[sk(j)] = slg[j];
-    pf[sk(j)] = pfg[j];
-    al[sk(j)] = alg[j];
-    pb[sk(j)] = pbg[j];
-    inv[j] = invg[j];
-    Cs[j] = C[j];
+    sl[sk(j)] = tab[j];
+    pf[sk(j)] = tab[ldt + j];
+    nal[sk(j)] = tab[2 * ldt + j];
+    pb[sk(j)] = tab[3 * ldt + j];
+    inv[j] = tab[4 * ldt + j];
+    Cs[j] = fh_df_pair(fh_df_from_double(C[j]));
   }
-  // step constants (FP64 divisions are scarce on this GPU) and the weights of
-  // the sub-block's entries: wts[s][t] = w[(K8 + s + 1) - (K8 + t)]
-  if (threadIdx.x == 0) {
-    cst[0] = ii[0] / oma;  // Ii/(1-a)
-    cst[1] = 1.0 / oma;
-    cst[2] = 1.0 / tau;
+  // step constants (one FP64 conversion per thread), the weights of the
+  // sub-block's entries wts[s][t] = w[(K8 + s + 1) - (K8 + t)] and the
+  // boundary values of every step
+  if (threadIdx.x == 0) cst[0] = fh_df_pair(fh_df_from_double(ii[0] / oma));  // Ii/(1-a)
+  if (threadIdx.x == 1) cst[1] = fh_df_pair(fh_df_from_double(-1.0 / oma));
+  if (threadIdx.x == 2) cst[2] = fh_df_pair(fh_df_from_double(1.0 / tau));
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + kAbSub * kAbSub) {
+    const int v = threadIdx.x - 32, ss = v / kAbSub, t = v % kAbSub;
+    wts[ss][t] = t < ss ? w2[ss + 1 - t] : make_float2(0.f, 0.f);
   }
-  if (threadIdx.x < kAbSub * kAbSub) {
-    const int ss = threadIdx.x / kAbSub, t = threadIdx.x % kAbSub;
-    wts[ss][t] = t < ss ? w[ss + 1 - t] : 0.0;
+  if (threadIdx.x >= 128 && threadIdx.x < 128 + 2 * kAbSub) {
+    const int v = threadIdx.x - 128, ss = v >> 1;
+    if (ss >= s0 && ss < s0 + ns) {
+      const int K = K8 + ss, row = K < nrows - 1 ? K : nrows - 1;
+      bnd[ss][v & 1] = fh_df_pair(fh_df_from_double((v & 1) ? brp[row] : blp[row]));
+    }
   }
   __syncthreads();
-  const double cI = cst[0], ioma = cst[1], itau = cst[2];
-  __shared__ fh_aff scan_sm[kAbSolveWarps];
+  const fh_df cI = fh_df_from_pair(cst[0]), nioma = fh_df_from_pair(cst[1]), itau = fh_df_from_pair(cst[2]);
+  const fh_daff I{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  __shared__ fh_daff scan_sm[kAbSolveWarps];
   for (int s = s0; s < s0 + ns; ++s) {
     const int K = K8 + s;  // history entries of this step (reference step i = K + 1)
     const int row = K < nrows - 1 ? K : nrows - 1;
-    const double *srow = src + (long long)row * (m + 1);
-    const double *mrow = mid ? mid + (long long)s * P : nullptr;
+    const float2 *srow = src2 + (long long)row * (m + 1);
+    const float2 *mrow = mid ? mid + (long long)s * P : nullptr;
     const float2 *frow = far8 ? far8 + (long long)s * ldfar : nullptr;
     const bool hist = mrow || frow || s > 0;
-    for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
-      double r = fma(cI, Cs[j], srow[j]);
-      if (hist) {  // MF_intF_simple returns ret/(1-a)
-        double sv = mrow ? mrow[j] : 0.0;
-        if (frow) sv += (double)frow[j].x + (double)frow[j].y;
-        for (int t = 0; t < s; ++t) sv = fma(wts[s][t], __ldcg(D + (long long)(K8 + t) * P + j), sv);
-        r -= sv * ioma;
+    {
+      // right parts: all of the thread's loads in flight together
+      float2 sr[NMAX], hv[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        const int j = threadIdx.x + k * kAbFuseThreads;
+        if (j <= m) {
+          sr[k] = srow[j];
+          hv[k] = mrow ? mrow[j] : (frow ? frow[j] : make_float2(0.f, 0.f));
+        }
       }
-      rb[sk(j)] = r * inv[j];
+      fh_df hs[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) hs[k] = fh_df_from_pair(hv[k]);
+      if (mrow && frow) {
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+          const int j = threadIdx.x + k * kAbFuseThreads;
+          if (j <= m) hs[k] = fh_df_add(fh_df_from_pair(mrow[j]), fh_df_from_pair(frow[j]));
+        }
+      }
+      for (int t0 = 0; t0 < s; t0 += 2) {  // the sub-block's own entries, two per round trip
+        float2 d[2][NMAX];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int k = 0; k < NMAX; ++k) {
+            const int j = threadIdx.x + k * kAbFuseThreads;
+            if (t0 + u < s && j <= m) d[u][k] = __ldcg(D + (long long)(K8 + t0 + u) * P + j);
+          }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (t0 + u < s) {
+            const fh_df w = fh_df_from_pair(wts[s][t0 + u]);
+#pragma unroll
+            for (int k = 0; k < NMAX; ++k) hs[k] = fh_df_fma(w, fh_df_from_pair(d[u][k]), hs[k]);
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        const int j = threadIdx.x + k * kAbFuseThreads;
+        if (j <= m) {
+          fh_df r = fh_df_fma(cI, fh_df_from_pair(Cs[j]), fh_df_from_pair(sr[k]));
+          if (hist) r = fh_df_fma(nioma, hs[k], r);  // MF_intF_simple returns ret/(1-a)
+          rb[sk(j)] = fh_df_pair(fh_df_mul(r, fh_df_from_pair(inv[j])));
+        }
+      }
     }
     __syncthreads();
     if (threadIdx.x < kAbSolveThreads) {
       const int t = threadIdx.x;
-      const double bl = blp[row], br = brp[row];
+      const fh_df bl = fh_df_from_pair(bnd[s][0]), br = fh_df_from_pair(bnd[s][1]);
       const int f0 = 1 + t * ch, f1 = min(m + 1, f0 + ch);
-      double b = 0.0;
+      fh_df b{0.f, 0.f};
       for (int j = f0; j < f1; ++j) {
-        b = fma(sl[sk(j)], b, rb[sk(j)]);
-        bt[sk(j)] = b;
+        b = fh_df_fma(fh_df_from_pair(sl[sk(j)]), b, fh_df_from_pair(rb[sk(j)]));
+        bt[sk(j)] = fh_df_pair(b);
       }
-      const fh_aff Pf = fh_group_exclusive_affine<kAbSolveWarps>(f1 > f0 ? fh_aff{pf[sk(f1 - 1)], b}
-                                                                         : fh_aff{1.0, 0.0},
-                                                                 scan_sm, 1);
-      const double s0v = fma(Pf.a, bl, Pf.b);  // bt[f0 - 1]
-      for (int j = f0; j < f1; ++j) bt[sk(j)] = fma(pf[sk(j)], s0v, bt[sk(j)]);
-      if (t == 0) bt[sk(0)] = bl;
+      const fh_daff Pf = fh_group_exclusive_daff<kAbSolveWarps>(
+          f1 > f0 ? fh_daff{fh_df_from_pair(pf[sk(f1 - 1)]), b} : I, scan_sm, 1);
+      const fh_df s0v = fh_df_fma(Pf.a, bl, Pf.b);  // bt[f0 - 1]
+      for (int j = f0; j < f1; ++j)
+        bt[sk(j)] = fh_df_pair(fh_df_fma(fh_df_from_pair(pf[sk(j)]), s0v, fh_df_from_pair(bt[sk(j)])));
+      if (t == 0) bt[sk(0)] = fh_df_pair(bl);
       fh_group_bar(1, kAbSolveThreads);
       const int b0 = t * ch, b1 = min(m, b0 + ch);
-      double c = 0.0;
+      fh_df c{0.f, 0.f};
       for (int j = b1 - 1; j >= b0; --j) {
-        c = fma(-al[sk(j)], c, bt[sk(j)]);
-        cv[sk(j)] = c;
+        c = fh_df_fma(fh_df_from_pair(nal[sk(j)]), c, fh_df_from_pair(bt[sk(j)]));
+        cv[sk(j)] = fh_df_pair(c);
       }
-      const fh_aff Pb = fh_group_exclusive_affine_rev<kAbSolveWarps>(b1 > b0 ? fh_aff{pb[sk(b0)], c}
-                                                                             : fh_aff{1.0, 0.0},
-                                                                     scan_sm, 1);
-      const double tv = fma(Pb.a, br, Pb.b);  // C[b1]
-      for (int j = b0; j < b1; ++j) cv[sk(j)] = fma(pb[sk(j)], tv, cv[sk(j)]);
-      if (t == 0) cv[sk(m)] = br;
+      const fh_daff Pb = fh_group_exclusive_daff_rev<kAbSolveWarps>(
+          b1 > b0 ? fh_daff{fh_df_from_pair(pb[sk(b0)]), c} : I, scan_sm, 1);
+      const fh_df tv = fh_df_fma(Pb.a, br, Pb.b);  // C[b1]
+      for (int j = b0; j < b1; ++j)
+        cv[sk(j)] = fh_df_pair(fh_df_fma(fh_df_from_pair(pb[sk(j)]), tv, fh_df_from_pair(cv[sk(j)])));
+      if (t == 0) cv[sk(m)] = fh_df_pair(br);
     }
     __syncthreads();
-    double *Dk = D + (long long)K * P;
+    float2 *Dk = D + (long long)K * P;
     for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) {
-      const double v = cv[sk(j)];
-      Dk[j] = (v - Cs[j]) * itau;
-      Cs[j] = v;
+      const fh_df v = fh_df_from_pair(cv[sk(j)]);
+      Dk[j] = fh_df_pair(fh_df_mul(fh_df_sub(v, fh_df_from_pair(Cs[j])), itau));
+      Cs[j] = fh_df_pair(v);
     }
     __syncthreads();
   }
-  for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) C[j] = Cs[j];
+  for (int j = threadIdx.x; j <= m; j += kAbFuseThreads) C[j] = fh_df_to_double(fh_df_from_pair(Cs[j]));
+}
+
+// (hi, lo) pairs of n doubles; neg: of their negatives
+__global__ void k_ab_pairs(const double *__restrict__ x, float2 *__restrict__ y, long long n, int neg) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = fh_df_pair(fh_df_from_double(neg ? -x[i] : x[i]));
 }
 
 static size_t ab_fused_smem(int m) {
   const int ch = (m + kAbSolveThreads - 1) / kAbSolveThreads;
-  return sizeof(double) * (8 * (size_t)(m + 2 + m / ch + 1) + (size_t)m + 1);
+  return sizeof(float2) * (8 * (size_t)(m + 2 + m / ch + 1) + (size_t)m + 1);
+}
+
+// Pair copies for the double-float launches: elimination tables (after every
+// factorization), lag weights, source rows.
+static int ab_pairs(fh_ctx *ctx, const double *x, float2 *y, long long n, int neg) {
+  k_ab_pairs<<<(unsigned)fh_ceil_div(n, 256), 256, 0, ctx->stream>>>(x, y, n, neg);
+  return fh_after_launch(ctx, "k_ab_pairs");
+}
+static int ab_table_pairs(fh_ab_solver *s) {
+  if (!s->fused) return FH_OK;
+  const long long n = s->m + 1;
+  float2 *t = s->tab2.as<float2>();
+  int rc;
+  if ((rc = ab_pairs(s->ctx, s->sl.as<double>(), t, n, 0)) || (rc = ab_pairs(s->ctx, s->pf.as<double>(), t + s->P, n, 0)) ||
+      (rc = ab_pairs(s->ctx, s->al.as<double>(), t + 2 * s->P, n, 1)) ||
+      (rc = ab_pairs(s->ctx, s->pb.as<double>(), t + 3 * s->P, n, 0)) ||
+      (rc = ab_pairs(s->ctx, s->inv.as<double>(), t + 4 * s->P, n, 0)))
+    return rc;
+  return FH_OK;
+}
+static int ab_src_pairs(fh_ab_solver *s) {
+  if (!s->fused || s->nrows < 1) return FH_OK;
+  int rc = fh_alloc(s->ctx, s->src2, sizeof(float2) * (size_t)s->nrows * (s->m + 1), false);
+  if (rc) return rc;
+  return ab_pairs(s->ctx, s->src.as<double>(), s->src2.as<float2>(), (long long)s->nrows * (s->m + 1), 0);
 }
 
 static size_t ab_line_smem(int m) {
@@ -319,8 +422,9 @@ static int ab_one_step(fh_ab_solver *s, int max_n, int *done) {
   if (s->blk && K > 0 && K % kAbBlock == 0) {
     // new block: entries [K-128, K) into the slice planes, Toeplitz rows of the
     // next 128 steps, far rows S_far[r] = sum_{tt<K} w[K+1+r-tt] dC_tt
-    if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock, 0)) ||
-        (rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock / 2, 0)))
+    const int dfh = s->fused ? 1 : 0;  // fused launches store the entries as (hi, lo) pairs
+    if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock, dfh)) ||
+        (rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), s->P, K - kAbBlock / 2, dfh)))
       return rc;
     const int mrows = s->max_steps - K < kAbBlock ? s->max_steps - K : kAbBlock;
     if ((rc = fh_blk_toeplitz_weights(ctx, *s->blk, s->w.as<double>(), K + 1, K, mrows))) return rc;
@@ -369,20 +473,19 @@ static int ab_fused_steps(fh_ab_solver *s, int max_n, int *done) {
     const int nr = min(kAbSub, s->max_steps - K8);
     fh_prof_mark(ctx, FH_PROF_HISTORY, false);
     k_ab_mid<<<dim3((unsigned)fh_ceil_div(s->m + 1, 128), (unsigned)nr), 128, 0, ctx->stream>>>(
-        s->m, s->P, T0, K8, nr, s->w.as<double>(), s->D.as<double>(),
-        (s->blk && T0 > 0) ? s->far.as<float2>() : nullptr, s->ldfar, s->mid.as<double>());
+        s->m, s->P, T0, K8, nr, s->w2.as<float2>(), reinterpret_cast<const float2 *>(s->D.as<double>()),
+        (s->blk && T0 > 0) ? s->far.as<float2>() : nullptr, s->ldfar, s->mid.as<float2>());
     fh_prof_mark(ctx, FH_PROF_HISTORY, true);
     if ((rc = fh_after_launch(ctx, "k_ab_mid"))) return rc;
   }
-  const double *mid = K8 > T0 ? s->mid.as<double>() : nullptr;
+  const float2 *mid = K8 > T0 ? s->mid.as<float2>() : nullptr;
   const float2 *far8 = (!mid && s->blk && T0 > 0) ? s->far.as<float2>() + (long long)(K8 - T0) * s->ldfar : nullptr;
   const int ns = min(max_n, kAbSub - (K - K8));
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
   k_ab_line_fused<<<1, kAbFuseThreads, ab_fused_smem(s->m), ctx->stream>>>(
-      s->m, 1.0 - s->alpha, s->ii.as<double>(), s->al.as<double>(), s->inv.as<double>(), s->sl.as<double>(),
-      s->pf.as<double>(), s->pb.as<double>(), s->src.as<double>(), s->nrows, s->bl.as<double>(),
-      s->br.as<double>(), s->C.as<double>(), s->D.as<double>(), s->P, s->w.as<double>(), mid, far8, s->ldfar, K8,
-      K - K8, ns, s->tau);
+      s->m, 1.0 - s->alpha, s->ii.as<double>(), s->tab2.as<float2>(), s->P, s->src2.as<float2>(), s->nrows,
+      s->bl.as<double>(), s->br.as<double>(), s->C.as<double>(), reinterpret_cast<float2 *>(s->D.as<double>()),
+      s->P, s->w2.as<float2>(), mid, far8, s->ldfar, K8, K - K8, ns, s->tau);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_ab_line_fused"))) return rc;
   s->step += ns;
@@ -467,8 +570,9 @@ int fh_ab_set_source_host(fh_ab_solver *s, int nrows, const double *src_host, co
                                    cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->bl.p, bl_host, sizeof(double) * nrows, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->br.p, br_host, sizeof(double) * nrows, cudaMemcpyHostToDevice, ctx->stream));
-  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->nrows = nrows;
+  if ((rc = ab_src_pairs(s))) return rc;
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return FH_OK;
 }
 
@@ -503,7 +607,8 @@ int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
   k_ab_factor<<<1, 1, 0, ctx->stream>>>(s->m, s->A, s->Bd, s->Cc, s->al.as<double>(), s->den.as<double>(),
                                         s->inv.as<double>(), s->sl.as<double>(), s->pf.as<double>(),
                                         s->pb.as<double>());
-  return fh_after_launch(ctx, "k_ab_factor");
+  const int rc = fh_after_launch(ctx, "k_ab_factor");
+  return rc ? rc : ab_table_pairs(s);
 }
 
 int fh_ab_set_mode(fh_ab_solver *s, int mode) {
@@ -531,10 +636,17 @@ int fh_ab_set_mode(fh_ab_solver *s, int mode) {
     s->blk = nullptr;
   }
   // 8-step launches when the tables and the field fit in shared memory
-  s->fused = mode == FH_AB_BLOCKED && ab_fused_smem(s->m) <= 200 * 1024;
-  if (s->fused && !s->mid.p) {
-    const int rc = fh_alloc(ctx, s->mid, sizeof(double) * kAbSub * (size_t)s->P);
-    if (rc) return rc;
+  s->fused = mode == FH_AB_BLOCKED && ab_fused_smem(s->m) <= 200 * 1024 &&
+             s->m + 1 <= kAbFuseThreads * kAbFuseMaxNodes;
+  if (s->fused) {
+    int rc;
+    if (!s->mid.p && (rc = fh_alloc(ctx, s->mid, sizeof(float2) * kAbSub * (size_t)s->P))) return rc;
+    if (!s->tab2.p && (rc = fh_alloc(ctx, s->tab2, sizeof(float2) * 5 * (size_t)s->P))) return rc;
+    if (!s->w2.p) {
+      if ((rc = fh_alloc(ctx, s->w2, sizeof(float2) * (size_t)(s->max_steps + 2)))) return rc;
+      if ((rc = ab_pairs(ctx, s->w.as<double>(), s->w2.as<float2>(), s->max_steps + 2, 0))) return rc;
+    }
+    if ((rc = ab_table_pairs(s)) || (rc = ab_src_pairs(s))) return rc;
   }
   s->graph.reset();
   return FH_OK;

@@ -284,3 +284,47 @@ __device__ __forceinline__ fh_aff fh_group_exclusive_affine_rev(fh_aff f, fh_aff
   return fh_aff_compose(fh_aff{ea, eb}, Q);
 }
 
+
+// ------------------------------------------------------------------------
+// Double-float group scans: NW warps (threads 0 .. 32 NW - 1 of the CTA) scan
+// one chain of 32 NW chunk maps in double-float; warp totals pass through
+// shared memory sm[NW] and the named barrier bar (NW warps only).
+template <int NW>
+__device__ __forceinline__ fh_daff fh_group_exclusive_daff(fh_daff f, fh_daff *sm, int bar) {
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = threadIdx.x >> 5;
+  fh_daff g = f;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const fh_daff p{fh_df_shfl_up(g.a, d), fh_df_shfl_up(g.b, d)};
+    if (lane >= (unsigned)d) g = fh_daff_compose(g, p);
+  }
+  if (lane == 31u) sm[w] = g;
+  fh_daff e{fh_df_shfl_up(g.a, 1), fh_df_shfl_up(g.b, 1)};
+  if (lane == 0u) e = fh_daff{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  fh_group_bar(bar, 32 * NW);
+  fh_daff P{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  for (int k = 0; k < w; ++k) P = fh_daff_compose(sm[k], P);
+  fh_group_bar(bar, 32 * NW);  // sm may be reused after this
+  return fh_daff_compose(e, P);
+}
+
+template <int NW>
+__device__ __forceinline__ fh_daff fh_group_exclusive_daff_rev(fh_daff f, fh_daff *sm, int bar) {
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = threadIdx.x >> 5;
+  fh_daff g = f;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const fh_daff p{fh_df_shfl_down(g.a, d), fh_df_shfl_down(g.b, d)};
+    if (lane + d < 32u) g = fh_daff_compose(g, p);
+  }
+  if (lane == 0u) sm[w] = g;
+  fh_daff e{fh_df_shfl_down(g.a, 1), fh_df_shfl_down(g.b, 1)};
+  if (lane == 31u) e = fh_daff{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  fh_group_bar(bar, 32 * NW);
+  fh_daff Q{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  for (int k = NW - 1; k > w; --k) Q = fh_daff_compose(sm[k], Q);
+  fh_group_bar(bar, 32 * NW);
+  return fh_daff_compose(e, Q);
+}
