@@ -85,7 +85,8 @@ __device__ __forceinline__ float fh_exp2i(int e) {
 __global__ void __launch_bounds__(kThreads, 1)
     k_far_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, long long P,
                const int8_t *__restrict__ Ew, const int8_t *__restrict__ Ed, long long Ppad,
-               float2 *__restrict__ out, long long ldo, int *__restrict__ err) {
+               float2 *__restrict__ out, long long ldo, int splits, float2 *__restrict__ part,
+               int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   const uint32_t raw = fh_smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -103,13 +104,26 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunks = K / kBK;
-  // persistent: this CTA owns tiles blockIdx.x, blockIdx.x + gridDim.x, ...;
-  // the stage ring and the accumulator buffers run on one chunk counter g
-  // across its tiles, so loads of the next tile overlap the current epilogue
+  // persistent: this CTA owns the work items blockIdx.x, blockIdx.x +
+  // gridDim.x, ...; item v = (tile v / splits, group range v % splits): with
+  // few tiles (narrow lines) the chunk groups of a tile are split across CTAs
+  // (split-K; the partial rows go to part[sp] and k_blk_reduce_splits adds
+  // them in split order).  The stage ring and the accumulator buffers run on
+  // counters across the items, so loads of the next item overlap the current
+  // epilogue.
   const int ntiles = (int)(Ppad / kBN);
-  const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  const int total = my_tiles * nchunks;
   const int ngroups = fh_ngroups(nchunks);  // accumulator buffers cycle per chunk group
+  const int gps = (ngroups + splits - 1) / splits;  // groups per split
+  const int nitems = ntiles * splits;
+  const int my_items = (int)blockIdx.x < nitems ? (nitems - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  // item k of this CTA: tile, first and last group
+  auto item = [&](int k, int &tile, int &sp, int &G0, int &G1) {
+    const int v = (int)blockIdx.x + k * (int)gridDim.x;
+    tile = v / splits;
+    sp = v % splits;
+    G0 = min(ngroups, sp * gps);
+    G1 = min(ngroups, G0 + gps);
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -138,20 +152,24 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int last_issued[kStages];
       for (int s = 0; s < kStages; ++s) last_issued[s] = -1;
-      for (int g = 0; g < total; ++g) {
-        const int tile = (int)blockIdx.x + (g / nchunks) * (int)gridDim.x;
-        const int c = g % nchunks;
-        const int s = g % kStages;
-        if (g >= kStages && !fh_mbar_wait(empty(s), ((g / kStages) - 1) & 1)) {
-          ok = false;
-          break;
+      int g = 0;  // stage counter
+      for (int k = 0; k < my_items && ok; ++k) {
+        int tile, sp, G0, G1;
+        item(k, tile, sp, G0, G1);
+        const int c1 = min(nchunks, 2 * G1);
+        for (int c = 2 * G0; c < c1; ++c, ++g) {
+          const int s = g % kStages;
+          if (g >= kStages && !fh_mbar_wait(empty(s), ((g / kStages) - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          fh_mbar_arrive_expect_tx(full(s), kStageBytes);
+          const uint32_t sb = base + s * kStageBytes;
+          for (int pl = 0; pl < kSlices; ++pl) fh_tma_load_3d(sb + pl * kTileA, &tmA, c * kBK, 0, pl, full(s));
+          for (int pl = 0; pl < kSlices; ++pl)
+            fh_tma_load_3d(sb + kSlices * kTileA + pl * kTileB, &tmB, c * kBK, tile * kBN, pl, full(s));
+          last_issued[s] = g;
         }
-        fh_mbar_arrive_expect_tx(full(s), kStageBytes);
-        const uint32_t sb = base + s * kStageBytes;
-        for (int pl = 0; pl < kSlices; ++pl) fh_tma_load_3d(sb + pl * kTileA, &tmA, c * kBK, 0, pl, full(s));
-        for (int pl = 0; pl < kSlices; ++pl)
-          fh_tma_load_3d(sb + kSlices * kTileA + pl * kTileB, &tmB, c * kBK, tile * kBN, pl, full(s));
-        last_issued[s] = g;
       }
       if (!ok) {
         *sh_err = 1;
@@ -163,8 +181,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       const uint32_t idesc = fh_idesc_bf16_f32(kBM, kBN);
       int gc = 0;  // chunk counter (stage ring)
-      for (int gg = 0; gg < my_tiles * ngroups && ok; ++gg) {
-        const int G = gg % ngroups;
+      int gg = 0;  // group counter (accumulator buffers)
+      for (int k = 0; k < my_items && ok; ++k) {
+       int tile, sp, G0, G1;
+       item(k, tile, sp, G0, G1);
+       for (int G = G0; G < G1 && ok; ++G, ++gg) {
         const int nc = min(2, nchunks - 2 * G);
         const int b = gg & 1;
         if (gg >= 2 && !fh_mbar_wait(accempty(b), ((gg >> 1) - 1) & 1)) {
@@ -199,6 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!ok) break;
         fh_mma_commit(accfull(b));
+       }
       }
       fh_mma_commit(mmadone);
       if (!fh_mbar_wait(mmadone, 0)) ok = false;
@@ -212,13 +234,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lanebase = (uint32_t)(32 * q) << 16;
     const int m = 32 * q + lane;
     const int col0 = 32 * half;
-    for (int tt = 0; tt < my_tiles && ok; ++tt) {
-      const long long p0 = (long long)((int)blockIdx.x + tt * (int)gridDim.x) * kBN;
+    int gg = 0;  // group counter (accumulator buffers)
+    for (int k = 0; k < my_items && ok; ++k) {
+      int tile, sp, G0, G1;
+      item(k, tile, sp, G0, G1);
+      const long long p0 = (long long)tile * kBN;
       float HI[32], LO[32];
 #pragma unroll
       for (int i = 0; i < 32; ++i) HI[i] = LO[i] = 0.f;
-      for (int G = 0; G < ngroups; ++G) {
-        const int gg = tt * ngroups + G;
+      for (int G = G0; G < G1; ++G, ++gg) {
         const int b = gg & 1;
         // exponents of this group (loaded before the wait: they do not depend on it)
         const int ew = (int)Ew[(long long)(2 * G) * kBM + m];
@@ -270,7 +294,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (ok && nchunks > 0) {
         // row m, 32 consecutive points: (hi, lo) pairs as 16-byte stores
-        float4 *o = reinterpret_cast<float4 *>(out + (long long)m * ldo + p0 + col0);
+        float4 *o = reinterpret_cast<float4 *>(
+            (splits > 1 ? part + ((long long)sp * kBM + m) * Ppad : out + (long long)m * ldo) + p0 + col0);
 #pragma unroll
         for (int k = 0; k < 16; ++k) o[k] = make_float4(HI[2 * k], LO[2 * k], HI[2 * k + 1], LO[2 * k + 1]);
       }
@@ -538,6 +563,8 @@ struct fh_blk {
   int Kcap = 0;
   int nsm = 1;  // SMs of the device: one persistent CTA each
   fh_dbuf H3, A3, Ed, Ew, err;
+  fh_dbuf part;        // split-K partial rows (narrow lines: fewer tiles than SMs)
+  int max_splits = 1;
   CUtensorMap mapA, mapB;
 };
 
@@ -556,6 +583,12 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
       (rc = fh_alloc(ctx, b.A3, sizeof(__nv_bfloat16) * kSlices * (size_t)kBM * Kcap)) ||
       (rc = fh_alloc(ctx, b.Ed, (size_t)b.Ppad * (Kcap / kBK))) ||
       (rc = fh_alloc(ctx, b.Ew, (size_t)kBM * (Kcap / kBK))) || (rc = fh_alloc(ctx, b.err, sizeof(int))))
+    return rc;
+  const long long ntiles = b.Ppad / kBN;
+  b.max_splits = ntiles < b.nsm ? (int)(b.nsm / ntiles) : 1;
+  if (b.max_splits > 8) b.max_splits = 8;
+  if (b.max_splits > 1 &&
+      (rc = fh_alloc(ctx, b.part, sizeof(float2) * (size_t)b.max_splits * kBM * (size_t)b.Ppad, false)))
     return rc;
   if ((rc = make_map(ctx, &b.mapA, b.A3.p, (unsigned long long)Kcap, kBM, kBM))) return rc;
   if ((rc = make_map(ctx, &b.mapB, b.H3.p, (unsigned long long)Kcap, (unsigned long long)b.Ppad, kBN))) return rc;
@@ -621,15 +654,46 @@ int fh_blk_toeplitz_weights(fh_ctx *ctx, fh_blk &b, const double *w, int base, i
   return fh_after_launch(ctx, "k_blk_toeplitz_rows");
 }
 
+// out[m][p] = sum_sp part[sp][m][p] in split order (double-float adds)
+__global__ void k_blk_reduce_splits(const float2 *__restrict__ part, int splits, long long Ppad,
+                                    float2 *__restrict__ out, long long ldo) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y;
+  if (p >= Ppad) return;
+  float2 v = part[(long long)m * Ppad + p];
+  float h = v.x, l = v.y;
+  for (int sp = 1; sp < splits; ++sp) {
+    const float2 u = part[((long long)sp * kBM + m) * Ppad + p];
+    const float t = h + u.x, bb = t - h;
+    const float e = (h - (t - bb)) + (u.x - bb);
+    l += e + u.y;
+    h = t;
+  }
+  const float t = h + l;
+  out[(long long)m * ldo + p] = make_float2(t, l - (t - h));
+}
+
 // S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p] as (hi, lo) pairs.
+// Narrow lines (fewer 64-point tiles than SMs) split the chunk groups of each
+// tile across CTAs and add the partial rows afterwards.
 int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo) {
   FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
   fh_prof_mark(ctx, FH_PROF_GEMM, false);
   const long long ntiles = b.Ppad / kBN;
-  k_far_gemm<<<(unsigned)(ntiles < b.nsm ? ntiles : b.nsm), kThreads, kSmemBytes, ctx->stream>>>(
-      b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, b.err.as<int>());
+  const int ngroups = fh_ngroups(K / kBK);
+  const int splits = b.max_splits < ngroups ? b.max_splits : ngroups;
+  const long long items = ntiles * splits;
+  k_far_gemm<<<(unsigned)(items < b.nsm ? items : b.nsm), kThreads, kSmemBytes, ctx->stream>>>(
+      b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, splits,
+      b.part.as<float2>(), b.err.as<int>());
+  int rc = fh_after_launch(ctx, "k_far_gemm");
+  if (!rc && splits > 1) {
+    k_blk_reduce_splits<<<dim3((unsigned)fh_ceil_div(b.Ppad, 256), kBM), 256, 0, ctx->stream>>>(
+        b.part.as<float2>(), splits, b.Ppad, out, ldo);
+    rc = fh_after_launch(ctx, "k_blk_reduce_splits");
+  }
   fh_prof_mark(ctx, FH_PROF_GEMM, true);
-  return fh_after_launch(ctx, "k_far_gemm");
+  return rc;
 }
 
 __global__ void k_pairs_to_double(const float2 *__restrict__ in, long long ldi, long long P, double *__restrict__ out,
