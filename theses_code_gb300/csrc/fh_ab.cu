@@ -46,7 +46,7 @@ struct fh_ab_solver {
 };
 
 constexpr int kAbThreads = 256;
-constexpr int kAbSolveWarps = 4;  // the solve runs on four warps (one per SM sub-partition)
+constexpr int kAbSolveWarps = 8;  // the solve runs on eight warps (two per SM sub-partition), 8-equation chunks
 constexpr int kAbSolveThreads = 32 * kAbSolveWarps;
 
 // al[j] = Cc/(Bd - A al[j-1]), den[j] = Bd - A al[j-1], al[0] = 0 (MF_int_series.cpp:933-940).
@@ -94,8 +94,8 @@ __global__ void k_ab_stepweights(int i, int k0, int n, const double *__restrict_
 //   backward  C[j]  = bt[j] - al[j] C[j+1],  C[m] = right boundary value
 // All threads stage the right parts and the tabulated coefficients into
 // shared memory with coalesced loads (skewed by i / chunk so that the
-// threads' chunks fall on distinct banks), four warps (one per SM
-// sub-partition) walk their threads' chunks from a zero start and add
+// threads' chunks fall on distinct banks), kAbSolveWarps warps walk their
+// threads' chunks from a zero start and add
 // prefix * start value after a group scan of the chunk maps
 // (fh_line_solve_prefix scheme), then all threads write C and the new history
 // entry.
@@ -224,8 +224,9 @@ __global__ void k_ab_mid(int m, long long P, int T0, int K8, int nr, const float
 // Steps K8 + s0 .. K8 + s0 + ns - 1 of one sub-block in one CTA, in
 // double-float: the elimination tables and the field stay in shared memory
 // for the whole launch; per step the right parts (source row, sub-block row or
-// far row, the sub-block's own entries), the solve of k_ab_line (four warps,
-// double-float group scans) and the new history entry dC/tau.  FP64 only
+// far row, the sub-block's own entries), the solve of k_ab_line
+// (kAbSolveWarps warps, double-float group scans) and the new history entry
+// dC/tau.  FP64 only
 // converts the field at the start and the end of the launch.  Every thread
 // keeps the right-part loads of all its nodes (j = tid + 512 k) in flight at
 // once, the sub-block's entries two per round trip.
