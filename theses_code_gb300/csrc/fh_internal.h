@@ -114,7 +114,7 @@ int fh_graph_run(fh_ctx *ctx, fh_graph_cache &gc, int nsteps, Body body) {
       gc.release_events();
       return fh_set_error(ctx, FH_ECUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
     }
-    e = cudaGraphInstantiate(&gc.exec, graph, 0);
+    e = cudaGraphInstantiate(&gc.exec, graph, cudaGraphInstantiateFlagUseNodePriority);  // launch priorities hold
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       gc.exec = nullptr;

@@ -68,6 +68,16 @@ struct fh_tg_solver {
   bool fused = false;
   int fuse_blocks = 0;
   fh_dbuf bar, derr;
+  // Near rows of sub-block j8 + 8 over the layers [j0, j8) ("old" rows) are
+  // summed on the low-priority stream hs while the sweeps of sub-block j8 run
+  // (on the SMs they leave free); at the start of sub-block j8 + 8 only its
+  // last 8 layers are added to them.  Two buffers by sub-block parity.
+  cudaStream_t hs = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_old = nullptr;
+  fh_dbuf mold;
+  int old_pending = -1;  // sub-block whose old rows are enqueued on hs, not yet waited for
+  int old_ready = -1;    // sub-block whose old rows are complete in mold
+  int hs_hi = 0;         // greatest stream priority of the device (for the sweeps)
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
   fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
@@ -75,6 +85,12 @@ struct fh_tg_solver {
   fh_graph_cache graph;
   ~fh_tg_solver() {
     if (blk) fh_blk_delete(blk);
+    if (hs) {
+      cudaStreamSynchronize(hs);
+      cudaStreamDestroy(hs);
+    }
+    if (ev_main) cudaEventDestroy(ev_main);
+    if (ev_old) cudaEventDestroy(ev_old);
   }
 };
 
@@ -1100,6 +1116,29 @@ static int tg_factor(fh_tg_solver *s, const double *cwj) {
 //     the sweeps add the sub-block's own layers [j8, j);
 //   per-step weight row (more steps than the table holds): one near sum over
 //     the block's layers [j0, j) per step, far row folded in.
+// The context stream waits for the old rows still pending on hs.
+static int tg_join_old(fh_tg_solver *s) {
+  if (s->old_pending < 0) return FH_OK;
+  FH_CUDA_TRY(s->ctx, cudaStreamWaitEvent(s->ctx->stream, s->ev_old, 0));
+  s->old_ready = s->old_pending;
+  s->old_pending = -1;
+  return FH_OK;
+}
+
+// Near rows of sub-block jb (steps jb .. jb + 7) over the layers [kb, ke), on
+// top of the rows base (stride lbase between steps' x rows, y row at + lbase/2
+// for the sub-block buffers, far rows otherwise), into out (16 rows of P).
+static int tg_mid(fh_tg_solver *s, cudaStream_t st, int jb, int kb, int ke, const float2 *base, long long ldbase,
+                  float2 *out) {
+  const fh_tg_dev &g = s->dv;
+  const int ldw = s->max_steps;
+  const int nr = min(kSub, s->max_steps - jb);
+  k_tg_mid_df<kMidPPT><<<(unsigned)fh_ceil_div(g.P, (long long)kMidPPT * kMidThreads), kMidThreads, 0, st>>>(
+      reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kb * g.P, g.P, ke - kb,
+      s->W.as<double>() + (long long)jb * 2 * ldw + kb, ldw, nr, base, ldbase, out, g.P);
+  return fh_after_launch(s->ctx, "k_tg_mid_df");
+}
+
 static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int max_n, int *done) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
@@ -1117,14 +1156,17 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
     const int j8 = (j / kSub) * kSub;  // >= j0: blocks are whole sub-blocks
     if (j8 > j0) {
       if (j == j8) {
-        const int nr = min(kSub, s->max_steps - j8);
         fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-        k_tg_mid_df<kMidPPT><<<(unsigned)fh_ceil_div(g.P, (long long)kMidPPT * kMidThreads), kMidThreads, 0,
-                                ctx->stream>>>(
-            D2 + (long long)j0 * g.P, g.P, j8 - j0, s->W.as<double>() + (long long)j8 * 2 * ldw + j0, ldw, nr,
-            farj, s->ldfar, part, g.P);
+        if (s->old_pending == j8 && (rc = tg_join_old(s))) return rc;
+        if (s->fused && s->old_ready == j8) {
+          // old rows [j0, j8 - 8) are done: add the last 8 layers
+          rc = tg_mid(s, ctx->stream, j8, j8 - kSub, j8, s->mold.as<float2>() + (long long)((j8 / kSub) & 1) * 16 * g.P,
+                      g.P, part);
+        } else {
+          rc = tg_mid(s, ctx->stream, j8, j0, j8, farj, s->ldfar, part);
+        }
         fh_prof_mark(ctx, FH_PROF_HISTORY, true);
-        if ((rc = fh_after_launch(ctx, "k_tg_mid_df"))) return rc;
+        if (rc) return rc;
       }
       rbx = part + 2LL * (j - j8) * g.P;
       rby = rbx + g.P;
@@ -1173,16 +1215,34 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       cfg.blockDim = dim3(kFuseThreads);
       cfg.dynamicSmemBytes = tg_fuse_smem(g.sN, g.M);
       cfg.stream = ctx->stream;
-      cudaLaunchAttribute at[1];
+      cudaLaunchAttribute at[2];
       at[0].id = cudaLaunchAttributeCooperative;
       at[0].val.cooperative = 1;
+      at[1].id = cudaLaunchAttributePriority;  // ahead of the old rows on hs
+      at[1].val.priority = s->hs_hi;
       cfg.attrs = at;
-      cfg.numAttrs = 1;
+      cfg.numAttrs = 2;
+      // old rows of sub-block j8 + 8 (layers [j0, j8), complete before this
+      // launch) on hs, beside the sweeps of this sub-block
+      const int jn = j8 + kSub;
+      const bool old_next = s->hs && j == j8 && j8 > j0 && jn < s->max_steps && (jn - j0) < kTgBlock;
+      if (old_next) {
+        FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_main, ctx->stream));
+        FH_CUDA_TRY(ctx, cudaStreamWaitEvent(s->hs, s->ev_main, 0));
+      }
       fh_prof_mark(ctx, FH_PROF_SWEEP, false);
       const cudaError_t e = cudaLaunchKernelEx(&cfg, k_tg_sweeps_fused, fa);
       fh_prof_mark(ctx, FH_PROF_SWEEP, true);
       if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "k_tg_sweeps_fused: %s", cudaGetErrorString(e));
       if ((rc = fh_after_launch(ctx, "k_tg_sweeps_fused"))) return rc;
+      if (old_next) {
+        const float2 *farn = (s->blk && j0 > 0) ? s->far.as<float2>() + 2LL * (jn - j0) * s->ldfar : nullptr;
+        if ((rc = tg_mid(s, s->hs, jn, j0, j8, farn, s->ldfar,
+                         s->mold.as<float2>() + (long long)((jn / kSub) & 1) * 16 * g.P)))
+          return rc;
+        FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_old, s->hs));
+        s->old_pending = jn;
+      }
       s->tstep += ns;
       *done = ns;
       return FH_OK;
@@ -1314,7 +1374,8 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
 // Double-float sweeps keep the field as pairs; the FP64 field C (returned by
 // fh_tg_field / fh_tg_get_c_host) is refreshed at the end of every step call.
 static int tg_publish(fh_tg_solver *s) {
-  if (!s->dfsweep || s->tstep == 0) return FH_OK;
+  int rc = tg_join_old(s);  // nothing of the call is left on hs
+  if (rc || !s->dfsweep || s->tstep == 0) return rc;
   fh_ctx *ctx = s->ctx;
   k_from_pairs<<<(unsigned)fh_ceil_div(s->dv.P, 256), 256, 0, ctx->stream>>>(s->Cd.as<float2>(), s->C.as<double>(),
                                                                             s->dv.P);
@@ -1433,6 +1494,20 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
       }
       s->fused = true;
       s->fuse_blocks = nblk;
+      int lo = 0, hi = 0;
+      cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+      if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->hs, cudaStreamNonBlocking, lo);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_old, cudaEventDisableTiming);
+      if (e != cudaSuccess) {
+        delete s;
+        return fh_set_error(ctx, FH_ECUDA, "fh_tg_create: history stream: %s", cudaGetErrorString(e));
+      }
+      s->hs_hi = hi;
+      if ((rc = fh_alloc(ctx, s->mold, sizeof(float2) * 2 * 16 * (size_t)g.P, false))) {
+        delete s;
+        return rc;
+      }
     }
     cudaGetLastError();
   }
@@ -1464,6 +1539,11 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_state: null solver");
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, V2 && C, FH_EINVAL, "fh_tg_set_state: null pointer");
+  {
+    const int rc0 = tg_join_old(s);
+    if (rc0) return rc0;
+    s->old_ready = -1;
+  }
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1478,6 +1558,11 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_state_host: null solver");
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, V2_host && C_host, FH_EINVAL, "fh_tg_set_state_host: null pointer");
+  {
+    const int rc0 = tg_join_old(s);
+    if (rc0) return rc0;
+    s->old_ready = -1;
+  }
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
