@@ -1085,15 +1085,19 @@ __global__ void k_from_pairs(const float2 *__restrict__ y, double *__restrict__ 
 
 static constexpr int kWeightTableMaxSteps = 4096;  // 2 x 4096^2 doubles = 268 MB
 
+// One line per thread, serial FP64 recurrences with divisions: few threads per
+// CTA spread the lines over many SMs (their FP64 units are the limit).
+static constexpr int kFactorThreads = 8;
+
 static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, 64), 64, 0, ctx->stream>>>(
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
       g, 0, s->V2.as<double>(), cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(),
       s->pfx.as<double>(), s->pbx.as<double>());
   int rc = fh_after_launch(ctx, "k_tg_factor(x)");
   if (rc) return rc;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, 64), 64, 0, ctx->stream>>>(
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
       g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(),
       s->pfy.as<double>(), s->pby.as<double>());
   if ((rc = fh_after_launch(ctx, "k_tg_factor(y)"))) return rc;
