@@ -750,12 +750,13 @@ __device__ __forceinline__ bool tg_grid_sync(unsigned *bar, unsigned target, int
     __syncwarp();
     const uint64_t deadline = fh_globaltimer() + FH_WAIT_NS;
     int ok = 1;
-    for (;;) {
+    for (unsigned it = 0;; ++it) {
       int st = 0;
       if (lane == 0) {
         unsigned v;
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
-        st = v >= target ? 1 : ((*(volatile int *)err || fh_globaltimer() > deadline) ? 2 : 0);
+        // the deadline and the error flag are checked every 64 polls
+        st = v >= target ? 1 : (((it & 63u) == 63u && (*(volatile int *)err || fh_globaltimer() > deadline)) ? 2 : 0);
       }
       st = __shfl_sync(0xffffffffu, st, 0);
       if (st == 1) break;
@@ -764,7 +765,7 @@ __device__ __forceinline__ bool tg_grid_sync(unsigned *bar, unsigned target, int
         if (lane == 0) atomicOr(err, 1);
         break;
       }
-      __nanosleep(32);
+      if (it >= 2048u) __nanosleep(64);  // tight polling first: a barrier usually completes within ~2 us
     }
     if (lane == 0) gs_ok = ok;
     __syncwarp();
