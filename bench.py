@@ -337,6 +337,8 @@ class H1D(Workload):
                        "launch_shape": self.tuned,
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
         self.kernel = "k_hist_tiles" if self.hmode == FH_H_FP64 else "k_hist_tiles_df"
+        if kind == "psi_batch" and self.hmode == FH_H_DF64:
+            self.class_profiles = {"history": "k_hist_tiles_df_psi1024.md"}
 
     def cpu_baseline(self):
         """Oracle port of H_solver (serial) on a bounded sample of the instances,

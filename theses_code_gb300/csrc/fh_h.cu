@@ -43,7 +43,7 @@ struct fh_h_batch {
   long long Ptot = 0;
   std::vector<fh_h_params> hp;
   std::vector<long long> off;
-  fh_dbuf inst, U, D, W, Lb, ibt, wc, part, Al, Bt, sA, sB, sR, sOm;
+  fh_dbuf inst, U, D, W, Lb, ibt, lgt, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
   int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
@@ -52,59 +52,78 @@ struct fh_h_batch {
 static constexpr int kTileThreads = 512;  // largest tile CTA (1024 nodes)
 static constexpr int kTileShapes[3] = {128, 256, 512};  // candidate tile CTAs
 static inline int tile_shape_index(int threads) { return threads == 128 ? 0 : threads == 256 ? 1 : 2; }
-static constexpr int kHWeightThreads = 128;  // slots per weights CTA
+static constexpr int kHWeightThreads = 128;                 // nodes per weights CTA
+static constexpr int kHWeightSlots = kHWeightThreads - 1;  // slots per weights CTA
+// per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | 2^(-1/beta)
+static constexpr int kIbStride = 2 * kIbTerms + 2;
 
 // ------------------------------------------------------------------ kernels
 
 // Row b of W: the weights of instance b for the history slots t = 0..os-2.
 // The reference's t = 0 term multiplies layer1 - layer1 (its layer pointer
 // starts at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
+// CTA (x, b) owns slots x*127 .. x*127+126 of instance b.
 __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
                             int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
-                            const double *__restrict__ ibt) {
+                            const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX) {
   const int b = blockIdx.y;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * kHWeightSlots + threadIdx.x;  // node index; slot index below kHWeightSlots
   const fh_h_dev_inst I = inst[b];
   if (I.weights == FH_W_PSI && I.beta != 1.0) {
     // psi = t^beta: the weight of slot t is the difference of one incomplete-beta
-    // value at its two ends (fh_psi_int_tab); each node is evaluated once and
-    // shared with the neighbouring slot through shared memory
-    __shared__ double nv[kHWeightThreads + 1], sc[2];
-    __shared__ int nlow[kHWeightThreads + 1];
-    const double X = (double)(tstep + 1), a = 1.0 / I.beta, bb = 1.0 - I.alpha;
-    const double *Lc = ibt + (long long)b * 2 * kIbTerms, *Uc = Lc + kIbTerms;
-    const int t0 = blockIdx.x * blockDim.x;
-    for (int i = threadIdx.x; i <= (int)blockDim.x; i += blockDim.x) {
-      const int x = t0 + i;
-      if (x <= os - 1) {
-        const double r = (double)x / X, y = pow(r, I.beta);
-        if (y <= 0.5) {
-          nv[i] = y <= 0.0 ? 0.0 : r * fh_horner(Lc, y);
-          nlow[i] = 1;
-        } else {
-          const double c = -expm1(I.beta * log1p(((double)x - X) / X));
-          nv[i] = c <= 0.0 ? 0.0 : pow(c, bb) * fh_horner(Uc, c);
-          nlow[i] = 0;
+    // value at its two ends (fh_psi_int_tab).  One node per thread, shared with
+    // the neighbouring slot through shared memory: node i < os sits at x = i,
+    // node os at x = tstep, the lower end of the current slot [tstep, tstep+1]
+    // whose upper end x = X has value 0 in the upper form.
+    __shared__ double nv[kHWeightThreads], sc;
+    __shared__ int nlow[kHWeightThreads];
+    const double X = (double)(tstep + 1), bb = 1.0 - I.alpha;
+    const double *Lc = ibt + (long long)b * kIbStride, *Uc = Lc + kIbTerms;
+    const int k = threadIdx.x;
+    if (i <= os) {
+      const int xi = i < os ? i : tstep;
+      if (xi == 0) {
+        nv[k] = 0.0;
+        nlow[k] = 1;
+      } else {
+        // t = beta log(x/X) as a double-double from the table of log(x)
+        // (|log X| > |log x|, so the head difference is a fast two-sum)
+        const double2 lx = lgt[xi], lX = lgt[tstep + 1];
+        const double sh = lx.x - lX.x;
+        const double sl = (lx.x - (sh + lX.x)) + (lx.y - lX.y);
+        const double th = I.beta * sh;
+        const double tl = fma(I.beta, sh, -th) + I.beta * sl;
+        const double r = (double)xi * invX;
+        if (r <= Lc[2 * kIbTerms + 1]) {  // y = r^beta <= 1/2: lower series in y
+          const double ey = exp(th);
+          const double y = fma(ey, tl, ey);
+          nv[k] = r * fh_horner_n(Lc, y, fh_ib_nterms(y));
+          nlow[k] = 1;
+        } else {  // upper tail in c = 1 - y = -expm1(t)
+          const double em = expm1(th);
+          const double c = -fma(em + 1.0, tl, em);
+          nv[k] = c <= 0.0 ? 0.0 : pow(c, bb) * fh_horner_n(Uc, c, fh_ib_nterms(c));
+          nlow[k] = 0;
         }
       }
     }
-    if (threadIdx.x == 0) {
-      sc[0] = pow(X * I.tau, 1.0 - I.alpha * I.beta) / I.beta;
-      sc[1] = exp(lgamma(a) + lgamma(bb) - lgamma(a + bb));  // B(a, b)
-    }
+    if (k == kHWeightThreads - 1) sc = pow(X * I.tau, 1.0 - I.alpha * I.beta) / I.beta;
     __syncthreads();
-    if (t < os - 1) {
-      const int i = threadIdx.x;
+    if (k < kHWeightSlots && i < os - 1) {
       double diff;
-      if (nlow[i] && nlow[i + 1])
-        diff = nv[i + 1] - nv[i];
-      else if (!nlow[i])
-        diff = nv[i] - nv[i + 1];
+      if (nlow[k] && nlow[k + 1])
+        diff = nv[k + 1] - nv[k];
+      else if (!nlow[k])
+        diff = nv[k] - nv[k + 1];
       else
-        diff = (sc[1] - nv[i + 1]) - nv[i];
-      W[(long long)b * ldw + t] = t == 0 ? 0.0 : sc[0] * diff * (1 - I.alpha);
+        diff = (Lc[2 * kIbTerms] - nv[k + 1]) - nv[k];
+      W[(long long)b * ldw + i] = i == 0 ? 0.0 : sc * diff * (1 - I.alpha);
     }
-  } else if (t < os - 1) {
+    if (i == os && k < kHWeightSlots) wc[b] = sc * (nlow[k] ? Lc[2 * kIbTerms] - nv[k] : nv[k]) * (1 - I.alpha);
+    return;
+  }
+  const int t = i;
+  if (threadIdx.x < kHWeightSlots && t < os - 1) {
     double w;
     if (t == 0)
       w = 0.0;
@@ -114,7 +133,7 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
       w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
     W[(long long)b * ldw + t] = w;
   }
-  if (t == 0) {
+  if (i == 0) {
     wc[b] = (I.weights == FH_W_L1)
                 ? 1.0
                 : fh_psi_int((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) *
@@ -128,7 +147,11 @@ __global__ void k_h_ibtab(const fh_h_dev_inst *__restrict__ inst, int n, double 
   if (b >= n) return;
   const fh_h_dev_inst I = inst[b];
   if (I.weights != FH_W_PSI) return;
-  fh_ib_tables(1.0 / I.beta, 1.0 - I.alpha, ibt + (long long)b * 2 * kIbTerms, ibt + (long long)b * 2 * kIbTerms + kIbTerms);
+  const double a = 1.0 / I.beta, bb = 1.0 - I.alpha;
+  double *row = ibt + (long long)b * kIbStride;
+  fh_ib_tables(a, bb, row, row + kIbTerms);
+  row[2 * kIbTerms] = exp(lgamma(a) + lgamma(bb) - lgamma(a + bb));  // B(a, b)
+  row[2 * kIbTerms + 1] = pow(0.5, a);                               // y <= 1/2 <=> x/X <= 2^(-1/beta)
 }
 
 // Lag table of the L1 instances: Lb[b][l] = (l+1)^(1-a) - l^(1-a) (mt_minimal.cpp:930),
@@ -252,8 +275,8 @@ __device__ __forceinline__ void fh_h_store_diff(double *D, long long i, double d
 //   Al[i+1] = B_i / (R_i - A_i Al[i])            Moebius maps (matrix scan)
 //   Bt[i+1] = (Al[i+1]/B_i)(A_i Bt[i] - Om_i)    affine maps
 //   u_i     = Al[i+1] u_{i+1} + Bt[i+1]           affine maps, reverse order
-// after which every lane re-walks its chunk with the reference's arithmetic
-// from the scanned start value.  The coefficients are kept in the scratch
+// after which every lane re-walks its chunk from the scanned start value with
+// one reciprocal per equation (Al[i+1] = B_i g, g = 1 / (R_i - A_i Al[i])).  The coefficients are kept in the scratch
 // arrays sA, sB, sR (reused for Al[i+1]/B_i) and sOm at the equation's node.
 __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__restrict__ inst, int n,
                                                      double *__restrict__ U, const double *__restrict__ wc,
@@ -271,6 +294,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
   double *u = U + o;
   const int N = I.N;
   const double DaW = I.Da * wc[b];
+  const double idL = 1.0 / I.dL;
   // ---- pass 1: coefficients of equations i in [f0, f1), chunk Moebius map
   const int chf = (N - 1 + 31) / 32;
   const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
@@ -283,7 +307,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
       const double B = I.Dg * Kp * I.cinv;
       const double R = I.cinv * (Kp + Km) * I.Dg + DaW;
       double om = -DaW * u[i];
-      if (I.gravity) om += (Kc - Km) / I.dL;
+      if (I.gravity) om += (Kc - Km) * idL;
       double ts = 0.0;
       for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + o + i];
       om += I.Da * ts;
@@ -329,8 +353,8 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     double alv = (lane == 0) ? I.al_left : fma(PT.m00, I.al_left, PT.m01) / fma(PT.m10, I.al_left, PT.m11);
     for (int i = f0; i < f1; ++i) {
       const double A = sA[o + i], B = sB[o + i], R = sR[o + i], om = sOm[o + i];
-      const double aln = B / (R - A * alv);
-      const double gq = aln / B;
+      const double gq = 1.0 / (R - A * alv);  // Al[i+1] / B_i
+      const double aln = B * gq;
       Al[o + i + 1] = aln;
       sR[o + i] = gq;
       F = fh_aff_compose(fh_aff{gq * A, -(gq * om)}, F);
@@ -394,11 +418,12 @@ static int h_one_step(fh_h_batch *B) {
   const int os = B->nsaved;
   const int K = os >= 2 ? os - 1 : 0;
   int rc;
-  dim3 gw((unsigned)fh_ceil_div(K > 0 ? K : 1, kHWeightThreads), (unsigned)B->n);
+  FH_REQUIRE(ctx, B->tstep + 1 < B->max_steps + 2, FH_EINVAL, "h_one_step: step %d beyond the log table", B->tstep);
+  dim3 gw((unsigned)(os / kHWeightSlots + 1), (unsigned)B->n);  // nodes 0..os
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
   k_h_weights<<<gw, kHWeightThreads, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
                                            B->max_weights, B->wc.as<double>(), B->Lb.as<double>(),
-                                           B->ibt.as<double>());
+                                           B->ibt.as<double>(), B->lgt.as<double2>(), 1.0 / (double)(B->tstep + 1));
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
   if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
   int splits = 0, kchunk = 0;
@@ -501,13 +526,25 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
       (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
       (rc = fh_alloc(ctx, B->W, sizeof(double) * (size_t)ninst * B->max_weights)) ||
       (rc = fh_alloc(ctx, B->Lb, sizeof(double) * (size_t)ninst * B->max_weights, false)) ||
-      (rc = fh_alloc(ctx, B->ibt, sizeof(double) * 2 * kIbTerms * (size_t)ninst, false)) ||
+      (rc = fh_alloc(ctx, B->ibt, sizeof(double) * kIbStride * (size_t)ninst, false)) ||
+      (rc = fh_alloc(ctx, B->lgt, sizeof(double2) * (size_t)(max_steps + 2), false)) ||
       (rc = fh_alloc(ctx, B->wc, sizeof(double) * ninst)) ||
       (rc = fh_alloc(ctx, B->part, st * (size_t)B->max_splits, false))) {
     delete B;
     return rc;
   }
+  // log(x) as (head, tail) doubles for x = 0..max_steps+1: the psi weights form
+  // beta log(x/X) from it as a double-double; long double carries the tail
+  std::vector<double2> lg((size_t)max_steps + 2);
+  lg[0] = make_double2(0.0, 0.0);
+  for (int x = 1; x < max_steps + 2; ++x) {
+    const long double l = logl((long double)x);
+    const double h = (double)l;
+    lg[x] = make_double2(h, (double)(l - (long double)h));
+  }
   cudaError_t e1 = cudaMemcpyAsync(B->inst.p, di.data(), sizeof(fh_h_dev_inst) * ninst, cudaMemcpyHostToDevice, ctx->stream);
+  if (e1 == cudaSuccess)
+    e1 = cudaMemcpyAsync(B->lgt.p, lg.data(), sizeof(double2) * lg.size(), cudaMemcpyHostToDevice, ctx->stream);
   cudaError_t e2 = cudaSuccess;
   for (int k = 0; k < 3 && e2 == cudaSuccess; ++k)
     e2 = cudaMemcpyAsync(B->tl_by[k].p, B->tiles_by[k].data(), sizeof(fh_h_tile) * B->tiles_by[k].size(),

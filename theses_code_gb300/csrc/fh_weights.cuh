@@ -85,6 +85,23 @@ __device__ __forceinline__ void fh_ib_tables(double a, double b, double *Lc, dou
   }
 }
 
+// Terms of a tabulated series at argument y in (0, 1/2] for a tail below
+// 2^-61 of its sum: both coefficient sequences are bounded by their first
+// term (|(1-a)_j / j!| <= 1 for 0 < a <= 2), so the tail after n terms is at
+// most 2 y^n of the sum.  FP32 log2 with two terms of margin.
+__device__ __forceinline__ int fh_ib_nterms(double y) {
+  const int n = (int)(62.0f / -__log2f((float)y)) + 2;
+  return n < kIbTerms ? n : kIbTerms;
+}
+
+// Horner over the first n coefficients.
+__device__ __forceinline__ double fh_horner_n(const double *__restrict__ c, double y, int n) {
+  double s = c[n - 1];
+#pragma unroll 4
+  for (int j = n - 2; j >= 0; --j) s = fma(s, y, c[j]);
+  return s;
+}
+
 __device__ __forceinline__ double fh_horner(const double *__restrict__ c, double y) {
   double s = c[kIbTerms - 1];
 #pragma unroll 8
