@@ -249,6 +249,28 @@ def test_h_solver_psi_batch_vs_oracle(ctx):
         assert relmax(g, ref) <= 1e-11, (p["alpha"], p["beta"])
 
 
+def test_h_solver_psi_long_run_vs_oracle(ctx):
+    """600 steps of two psi instances (the weights' cancellation grows with the
+    step number): one call (captured graph, next-step weights on the side
+    stream) and uneven calls (no graph, the first step of each call computes
+    its own weights) both match the oracle to the plain-path bound."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=2, seed=3, Nmin=17, Nmax=40, tau=2e-3)
+    steps = 600
+    a = HSolverBatch(ctx, params, steps + 1)
+    a.set_u(U0s)
+    a.calc_step(steps)
+    b = HSolverBatch(ctx, params, steps + 1)
+    b.set_u(U0s)
+    for n in (1, 250, 349):
+        b.calc_step(n)
+    for p, U0, ga, gb in zip(params, U0s, a.get_u(), b.get_u()):
+        ref, _ = O.h_solve(p, U0, steps)
+        assert relmax(ga, ref) <= TOL_SOLVER, (p["alpha"], p["beta"])
+        assert relmax(gb, ga) <= 1e-14
+
+
 def test_h_solver_df64_history_vs_oracle(ctx):
     """History stored as (hi, lo) FP32 pairs and summed in double-float: the
     plain-path bounds still hold (1e-12 for L1, 1e-11 for the psi batch)."""

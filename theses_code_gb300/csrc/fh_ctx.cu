@@ -33,8 +33,9 @@ int fh_alloc(fh_ctx *ctx, fh_dbuf &b, size_t bytes, bool zero) {
   return FH_OK;
 }
 
-void fh_prof_mark(fh_ctx *ctx, int kind, bool stop) {
+void fh_prof_mark(fh_ctx *ctx, int kind, bool stop, cudaStream_t stream) {
   if (!ctx->prof) return;
+  if (!stream) stream = ctx->stream;
   if (ctx->capturing) {
     // inside a capture: a fresh event per mark, recorded as a graph node
     std::vector<cudaEvent_t> &v = ctx->capturing->pev[kind];
@@ -45,7 +46,7 @@ void fh_prof_mark(fh_ctx *ctx, int kind, bool stop) {
       return;
     }
     v.push_back(e);
-    cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(e, stream, cudaEventRecordExternal);
     return;
   }
   fh_prof_kind &k = ctx->pk[kind];
@@ -58,7 +59,7 @@ void fh_prof_mark(fh_ctx *ctx, int kind, bool stop) {
     k.ev.push_back(e);
   }
   if (!stop && (k.used & 1)) return;  // unbalanced start: ignore
-  cudaEventRecord(k.ev[k.used++], ctx->stream);
+  cudaEventRecord(k.ev[k.used++], stream);
 }
 
 static void prof_collect(fh_ctx *ctx, int kind) {

@@ -47,6 +47,19 @@ struct fh_h_batch {
   fh_graph_cache graph;
   bool use_graph = true;
   int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
+  // weights of the next step on hs (h_one_step): two buffer pairs of W and
+  // wc, selected by the parity of the step; w_ready = step whose weights
+  // are pending on hs behind ev_w
+  cudaStream_t hs = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_w = nullptr;
+  int w_ready = -1;
+  double *Wp(int par) const { return W.as<double>() + (long long)par * n * max_weights; }
+  double *wcp(int par) const { return wc.as<double>() + (long long)par * n; }
+  ~fh_h_batch() {
+    if (hs) cudaStreamDestroy(hs);
+    if (ev_main) cudaEventDestroy(ev_main);
+    if (ev_w) cudaEventDestroy(ev_w);
+  }
 };
 
 static constexpr int kTileThreads = 512;  // largest tile CTA (1024 nodes)
@@ -413,37 +426,67 @@ static void h_plan(size_t ntiles, int K, int cap, int *splits, int *kchunk) {
   *kchunk = kc;
 }
 
-static int h_one_step(fh_h_batch *B) {
+// History sum over K layers with the weights W into part (tile shape ti).
+static int h_hist(fh_h_batch *B, int ti, int K, int splits, int kchunk, const double *W, cudaStream_t st) {
+  fh_ctx *ctx = B->ctx;
+  const dim3 g((unsigned)B->tiles_by[ti].size(), (unsigned)splits);
+  const size_t smem = sizeof(double) * (size_t)kchunk;
+  FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
+  if (B->mode == FH_H_DF64)
+    k_hist_tiles_df<<<g, kTileShapes[ti], smem, st>>>(  // float2 weights: same bytes as FP64
+        B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), reinterpret_cast<const float2 *>(B->D.as<double>()),
+        B->Ptot, K, W, B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+  else
+    k_hist_tiles<<<g, kTileShapes[ti], smem, st>>>(B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
+                                                   B->D.as<double>(), B->Ptot, K, W, B->max_weights, kchunk,
+                                                   B->part.as<double>(), B->Ptot);
+  return fh_after_launch(ctx, "k_hist_tiles");
+}
+
+// Weights of step `tstep` (os saved layers) into the buffer pair `par`.
+static int h_weights(fh_h_batch *B, int tstep, int os, int par, cudaStream_t st) {
+  fh_ctx *ctx = B->ctx;
+  FH_REQUIRE(ctx, tstep + 1 < B->max_steps + 2, FH_EINVAL, "h_weights: step %d beyond the log table", tstep);
+  dim3 gw((unsigned)(os / kHWeightSlots + 1), (unsigned)B->n);  // nodes 0..os
+  fh_prof_mark(ctx, FH_PROF_WEIGHTS, false, st);
+  k_h_weights<<<gw, kHWeightThreads, 0, st>>>(B->inst.as<fh_h_dev_inst>(), B->n, tstep, os, B->Wp(par), B->max_weights,
+                                              B->wcp(par), B->Lb.as<double>(), B->ibt.as<double>(),
+                                              B->lgt.as<double2>(), 1.0 / (double)(tstep + 1));
+  fh_prof_mark(ctx, FH_PROF_WEIGHTS, true, st);
+  return fh_after_launch(ctx, "k_h_weights");
+}
+
+// One step.  The weights depend on the step number only, so with `next` the
+// weights of the following step are computed on the side stream hs (high
+// priority, FP64-pipe-bound) beside this step's history sum (HBM-bound) and
+// line solves, into the other buffer pair; the following call waits for them.
+static int h_one_step(fh_h_batch *B, bool next) {
   fh_ctx *ctx = B->ctx;
   const int os = B->nsaved;
   const int K = os >= 2 ? os - 1 : 0;
+  const int par = B->tstep & 1;
   int rc;
-  FH_REQUIRE(ctx, B->tstep + 1 < B->max_steps + 2, FH_EINVAL, "h_one_step: step %d beyond the log table", B->tstep);
-  dim3 gw((unsigned)(os / kHWeightSlots + 1), (unsigned)B->n);  // nodes 0..os
-  fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
-  k_h_weights<<<gw, kHWeightThreads, 0, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->n, B->tstep, os, B->W.as<double>(),
-                                           B->max_weights, B->wc.as<double>(), B->Lb.as<double>(),
-                                           B->ibt.as<double>(), B->lgt.as<double2>(), 1.0 / (double)(B->tstep + 1));
-  fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
-  if ((rc = fh_after_launch(ctx, "k_h_weights"))) return rc;
+  if (B->w_ready == B->tstep) {
+    FH_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, B->ev_w, 0));
+  } else if ((rc = h_weights(B, B->tstep, os, par, ctx->stream))) {
+    return rc;
+  }
+  B->w_ready = -1;
+  if (next && B->hs) {
+    FH_CUDA_TRY(ctx, cudaEventRecord(B->ev_main, ctx->stream));
+    FH_CUDA_TRY(ctx, cudaStreamWaitEvent(B->hs, B->ev_main, 0));
+    if ((rc = h_weights(B, B->tstep + 1, os + 1, par ^ 1, B->hs))) return rc;
+    FH_CUDA_TRY(ctx, cudaEventRecord(B->ev_w, B->hs));
+    B->w_ready = B->tstep + 1;
+  }
   int splits = 0, kchunk = 0;
   if (K > 0) {
     const int ti = tile_shape_index(B->tile_threads);
     h_plan(B->tiles_by[ti].size(), K, B->split_cap, &splits, &kchunk);
-    dim3 g((unsigned)B->tiles_by[ti].size(), (unsigned)splits);
-    const size_t smem = sizeof(double) * (size_t)kchunk;
-    FH_REQUIRE(ctx, smem <= 48 * 1024, FH_EINVAL, "history chunk too large");
     fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-    if (B->mode == FH_H_DF64)
-      k_hist_tiles_df<<<g, B->tile_threads, smem, ctx->stream>>>(  // float2 weights: same bytes as FP64
-          B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), reinterpret_cast<const float2 *>(B->D.as<double>()),
-          B->Ptot, K, B->W.as<double>(), B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
-    else
-      k_hist_tiles<<<g, B->tile_threads, smem, ctx->stream>>>(B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(),
-                                                           B->D.as<double>(), B->Ptot, K, B->W.as<double>(),
-                                                           B->max_weights, kchunk, B->part.as<double>(), B->Ptot);
+    rc = h_hist(B, ti, K, splits, kchunk, B->Wp(par), ctx->stream);
     fh_prof_mark(ctx, FH_PROF_HISTORY, true);
-    if ((rc = fh_after_launch(ctx, "k_hist_tiles"))) return rc;
+    if (rc) return rc;
     if (splits > 2) {  // fold the partial sums into split 0 (in split order)
       if ((rc = fh_launch_reduce_splits(ctx, splits, B->Ptot, B->part.as<double>(), B->Ptot, B->part.as<double>())))
         return rc;
@@ -454,7 +497,7 @@ static int h_one_step(fh_h_batch *B) {
   double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
   k_h_line_warp<<<(unsigned)fh_ceil_div(B->n, 4), 128, 0, ctx->stream>>>(
-      B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wc.as<double>(), B->part.as<double>(), B->Ptot,
+      B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wcp(par), B->part.as<double>(), B->Ptot,
       splits, B->Al.as<double>(), B->Bt.as<double>(), B->sA.as<double>(), B->sB.as<double>(), B->sR.as<double>(),
       B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0, B->mode == FH_H_DF64 ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
@@ -524,14 +567,25 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
       (rc = fh_alloc(ctx, B->Al, st)) || (rc = fh_alloc(ctx, B->Bt, st)) || (rc = fh_alloc(ctx, B->sA, st)) ||
       (rc = fh_alloc(ctx, B->sB, st)) || (rc = fh_alloc(ctx, B->sR, st)) || (rc = fh_alloc(ctx, B->sOm, st)) ||
       (rc = fh_alloc(ctx, B->D, st * (size_t)max_steps)) ||
-      (rc = fh_alloc(ctx, B->W, sizeof(double) * (size_t)ninst * B->max_weights)) ||
+      (rc = fh_alloc(ctx, B->W, sizeof(double) * 2 * (size_t)ninst * B->max_weights)) ||
       (rc = fh_alloc(ctx, B->Lb, sizeof(double) * (size_t)ninst * B->max_weights, false)) ||
       (rc = fh_alloc(ctx, B->ibt, sizeof(double) * kIbStride * (size_t)ninst, false)) ||
       (rc = fh_alloc(ctx, B->lgt, sizeof(double2) * (size_t)(max_steps + 2), false)) ||
-      (rc = fh_alloc(ctx, B->wc, sizeof(double) * ninst)) ||
+      (rc = fh_alloc(ctx, B->wc, sizeof(double) * 2 * (size_t)ninst)) ||
       (rc = fh_alloc(ctx, B->part, st * (size_t)B->max_splits, false))) {
     delete B;
     return rc;
+  }
+  {
+    int plo = 0, phi = 0;
+    cudaError_t es = cudaDeviceGetStreamPriorityRange(&plo, &phi);
+    if (es == cudaSuccess) es = cudaStreamCreateWithPriority(&B->hs, cudaStreamNonBlocking, phi);
+    if (es == cudaSuccess) es = cudaEventCreateWithFlags(&B->ev_main, cudaEventDisableTiming);
+    if (es == cudaSuccess) es = cudaEventCreateWithFlags(&B->ev_w, cudaEventDisableTiming);
+    if (es != cudaSuccess) {
+      delete B;
+      return fh_set_error(ctx, FH_ECUDA, "fh_h_batch_create: weights stream: %s", cudaGetErrorString(es));
+    }
   }
   // log(x) as (head, tail) doubles for x = 0..max_steps+1: the psi weights form
   // beta log(x/X) from it as a double-double; long double carries the tail
@@ -656,9 +710,10 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
              b->nsaved, nsteps, b->max_steps);
   if (b->use_graph && ctx->graphs && b->nsaved == 0 && nsteps > 1) {
     // whole solve from the initial state: capture once, replay afterwards
+    b->w_ready = -1;
     int rc = fh_graph_run(ctx, b->graph, nsteps, [&]() {
       for (int i = 0; i < nsteps; ++i) {
-        int r = h_one_step(b);
+        int r = h_one_step(b, i + 1 < nsteps);
         if (r) return r;
       }
       return (int)FH_OK;
@@ -668,8 +723,9 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
     b->nsaved = nsteps;
     return FH_OK;
   }
+  b->w_ready = -1;
   for (int i = 0; i < nsteps; ++i) {
-    int rc = h_one_step(b);
+    int rc = h_one_step(b, i + 1 < nsteps);
     if (rc) return rc;
   }
   return FH_OK;
@@ -698,19 +754,15 @@ int fh_h_batch_autotune(fh_h_batch *b, float *best_ms) {
       int splits, kchunk;
       h_plan(b->tiles_by[ti].size(), K, caps[ci] < b->max_splits ? caps[ci] : b->max_splits, &splits, &kchunk);
       if ((size_t)kchunk * sizeof(double) > 48 * 1024) continue;
-      const dim3 g((unsigned)b->tiles_by[ti].size(), (unsigned)splits);
       float ms = 0.f;
       for (int rep = 0; rep < 3; ++rep) {  // first repetition warms up
         cudaEventRecord(e0, ctx->stream);
-        if (b->mode == FH_H_DF64)
-          k_hist_tiles_df<<<g, kTileShapes[ti], sizeof(double) * kchunk, ctx->stream>>>(
-              b->tl_by[ti].as<fh_h_tile>(), b->inst.as<fh_h_dev_inst>(),
-              reinterpret_cast<const float2 *>(b->D.as<double>()), b->Ptot, K, b->W.as<double>(), b->max_weights,
-              kchunk, b->part.as<double>(), b->Ptot);
-        else
-          k_hist_tiles<<<g, kTileShapes[ti], sizeof(double) * kchunk, ctx->stream>>>(
-              b->tl_by[ti].as<fh_h_tile>(), b->inst.as<fh_h_dev_inst>(), b->D.as<double>(), b->Ptot, K,
-              b->W.as<double>(), b->max_weights, kchunk, b->part.as<double>(), b->Ptot);
+        int rc = h_hist(b, ti, K, splits, kchunk, b->W.as<double>(), ctx->stream);
+        if (rc) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return rc;
+        }
         cudaEventRecord(e1, ctx->stream);
         cudaError_t e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) {
@@ -724,7 +776,6 @@ int fh_h_batch_autotune(fh_h_batch *b, float *best_ms) {
           ms += t;
         }
       }
-      ctx->launches += 3;
       if (ms < best) {
         best = ms;
         bt = kTileShapes[ti];

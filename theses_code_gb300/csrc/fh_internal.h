@@ -30,8 +30,9 @@ struct fh_ctx {
   char err[512] = {0};
 };
 
-// Records the start (stop = false) or stop event of a timed launch of `kind`.
-void fh_prof_mark(fh_ctx *ctx, int kind, bool stop);
+// Records the start (stop = false) or stop event of a timed launch of `kind`
+// on `stream` (the context stream when null).
+void fh_prof_mark(fh_ctx *ctx, int kind, bool stop, cudaStream_t stream = nullptr);
 
 int fh_set_error(const fh_ctx *ctx, int code, const char *fmt, ...);
 
