@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -62,6 +63,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--dt-eps", type=float, default=0.0,
+                    help="tg2d: restricted summing (the reference's dt_alg 2) with this weight cut; 0 = full history")
     return ap.parse_args()
 
 
@@ -198,7 +201,9 @@ class TG2D(Workload):
         p, V2, C0 = workloads.convection_2d(G, G, alpha=0.7, tau=5e-4, d=0.1, seed=11 + rank)
         self.modes = {"blocked": FH_TG_BLOCKED, "df64": FH_TG_DF64, "fp64": FH_TG_FP64}
         self.p = p
-        self.solver = TGSolver(ctx, p, S, self.modes[args.mode])
+        self.dt_eps = args.dt_eps
+        self.S = S
+        self.solver = self.new_solver(ctx, args.mode)
         self.V2_d = torch.as_tensor(V2, device=f"cuda:{dev}").contiguous()
         self.C0_d = torch.as_tensor(C0, device=f"cuda:{dev}").contiguous()
         P = V2.size
@@ -228,16 +233,22 @@ class TG2D(Workload):
                 "gemm_bytes": sum(8.0 * j0 * ppad + 8.0 * 128 * ppad + 8.0 * 128 * j0 for j0 in range(64, S, 64)),
             }
         else:
-            self.alg = {"history": sum(8.0 * j * pint + 16.0 * pint for j in range(1, S))}
+            # restricted summing: only the layer pairs whose weight reaches dt_eps
+            lag = self.restricted_lag(p, args.dt_eps, S) if args.dt_eps > 0 else S
+            self.alg = {"history": sum(8.0 * min(j, lag) * pint + 16.0 * pint for j in range(1, S))}
         # sweeps: x reads C, fa, g, al, one history row, writes Ch; y reads Ch, C, fa, g,
         # al, one history row, writes C and the new history layer; in blocked mode each
         # sweep also reads the j % 8 layers of the current sub-block
         self.alg["sweep"] = sum((112.0 + (16.0 * (j % 8) if blocked else 0.0)) * pint for j in range(S))
         self.alg_hist_bytes = self.alg["history"]
-        self.name = f"tg2d_adi_{G}x{G}_{S}steps"
+        self.name = f"tg2d_adi_{G}x{G}_{S}steps" + (f"_restricted{args.dt_eps:g}" if args.dt_eps > 0 else "")
         self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
                        "d": 0.1, "velocity_modes": 8, "mode": args.mode,
                        "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
+        if args.dt_eps > 0:
+            self.config["dt_alg"] = 2
+            self.config["dt_eps"] = args.dt_eps
+            self.config["restricted_lag"] = self.restricted_lag(p, args.dt_eps, S)
         if blocked:
             self.class_kernels = {"history": "k_tg_mid_df (near history rows of each 8-step sub-block)",
                                   "sweep": "k_tg_sweeps_fused (cooperative, 8 steps of x and y sweeps per launch)",
@@ -262,6 +273,23 @@ class TG2D(Workload):
         L.fh_tg_get_c_host(h, self.out_h.data_ptr())
         return self.out_h.numpy()
 
+    def new_solver(self, ctx, mode):
+        from theses_code_gb300.solvers import TGSolver
+        sv = TGSolver(ctx, self.p, self.S, self.modes[mode])
+        if self.dt_eps > 0:
+            sv.set_restricted(self.dt_eps)
+        return sv
+
+    @staticmethod
+    def restricted_lag(p, eps, S):
+        """Layer pairs with an x or y weight >= eps (psi = t: Toeplitz in the lag)."""
+        a = p["alpha"]
+        f = p["tau"] ** (1.0 - a) / (math.gamma(1.0 - a) * (1.0 - a))
+        for d in range(1, S + 1):
+            if all(f * ((d + ja) ** (1.0 - a) - (d + ja - 1.0) ** (1.0 - a)) < eps for ja in (0.5, 1.0)):
+                return d - 1
+        return S
+
     def compare(self, ctx, stream, main_mode):
         """One solve of the same inputs by every other mode (CUDA-event timed on the
         context stream, graphs on); relative max-norm differences to the FP64 path."""
@@ -273,7 +301,7 @@ class TG2D(Workload):
         for m in ("fp64", "df64", "blocked"):
             if m == main_mode:
                 continue
-            sv = TGSolver(ctx, self.p, self.S, self.modes[m])
+            sv = self.new_solver(ctx, m)
             sv.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
             sv.calc_step(self.S)  # first call captures the graph
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -227,6 +227,15 @@ int fh_tg_destroy(fh_tg_solver *s);
 int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C_host);
 /* Device-pointer variant (inputs already resident in HBM). */
 int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C);
+/* Restricted summing, TG_solver_ with dt_alg 2 (replaces the Om1 loop
+ * fr_d_t_g_2d.cpp:3356-3380 and the kb precalculation 3101-3232 with dt_alg
+ * 2): every history sum runs from the newest layer pair back and stops at the
+ * first weight below dt_eps (weights include Da).  dt_eps = 0 restores the
+ * full history (dt_alg 0).  Only before the first step of a solve (after
+ * fh_tg_create or fh_tg_set_state).  With psi = t the sums read only the
+ * layers within the lag where the weights fall below dt_eps; the history
+ * store keeps every layer. */
+int fh_tg_set_restricted(fh_tg_solver *s, double dt_eps);
 /* TG_solver::calc_step repeated nsteps times. */
 int fh_tg_step(fh_tg_solver *s, int nsteps);
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);

@@ -245,7 +245,10 @@ static void tg_line(const fho_tg_params *p, const double *V2, double *C, const d
     Om[i] += p->S * 0.5;
     double ts = 0.0;
     if (2 * j + 1 + dir >= 3)
-      for (int k = j - 1; k >= 0; --k) ts += wk[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
+      for (int k = j - 1; k >= 0; --k) {
+        if (p->dt_alg == 2 && fabs(wk[k]) < p->dt_eps) break; /* restricted summing (3364-3380) */
+        ts += wk[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
+      }
     /* y half-step term with the reference's operand order old[size-2]-old[size-1] (3479-3481) */
     if (dir == 1) ts += (kyh + 0.0) * (work[(size_t)j * P + id] - C[id]);
     Om[i] += st * ts;

@@ -33,7 +33,8 @@ class HParams(C.Structure):
 class TGParams(C.Structure):
     _fields_ = [("sN", C.c_int), ("M", C.c_int), ("tau", C.c_double), ("alpha", C.c_double),
                 ("beta", C.c_double), ("sigma", C.c_double), ("d", C.c_double), ("C1", C.c_double),
-                ("S", C.c_double), ("dL", C.c_double), ("dLx", C.c_double)]
+                ("S", C.c_double), ("dL", C.c_double), ("dLx", C.c_double), ("dt_alg", C.c_int),
+                ("dt_eps", C.c_double)]
 
 
 def build() -> str:

@@ -1,10 +1,11 @@
 // Harness around the reference 2D ADI solver TG_solver_<0,1,0>
 // (fr_d_t_g_2d.cpp:2037-4052): psi(t) = t (Caputo-Gerasimov), fixed diffusion
-// coefficient, dt_alg 0 (full history), int_alg 1 (_kb_row weights, exact for
-// psi = t), no mass exchange.  V2 (|v|^2) and the initial field are injected
-// after construction.  Test infrastructure only.
+// coefficient, dt_alg 0 (full history) or 2 (restricted summing with dt_eps),
+// int_alg 1 (_kb_row weights, exact for psi = t), no mass exchange.  V2 (|v|^2)
+// and the initial field are injected after construction.  Test infrastructure
+// only.
 //
-// argv: sN M tau alpha d C1 S steps
+// argv: sN M tau alpha d C1 S steps [dt_alg dt_eps]
 // stdin: (sN+2)*(M+2) values of V2 then (sN+2)*(M+2) initial values
 // stdout: "geom dL dLx sigma" then "c <values>" after the last step.
 #define main reference_main
@@ -22,7 +23,8 @@ int main(int argc, char **argv) {
   double c1 = atof(argv[6]), s_ = atof(argv[7]);
   int steps = atoi(argv[8]);
   int_alg = 1;
-  dt_alg = 0;
+  dt_alg = argc >= 11 ? atoi(argv[9]) : 0;
+  if (argc >= 11) dt_eps = atof(argv[10]);
   massN = 0;
   testing = 0;
   use_ocl = 0;

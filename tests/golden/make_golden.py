@@ -89,6 +89,14 @@ def main():
     dump("tg_adi.json", {"sN": sN, "M": M, "tau": 5e-3, "alpha": 0.7, "d": 0.1, "C1": 0.3, "S": 0.05,
                          "steps": 12, "dL": dL, "dLx": dLx, "sigma": sigma, "V2": list(V2),
                          "C0": list(C0), "C": res["c"][0]})
+    # the same problem with restricted summing (dt_alg 2): 40 steps, the sums
+    # stop at the first weight below 0.012 (about 12 layers back)
+    res = parse(run("tg", args[:7] + [40, 2, 0.012], list(V2) + list(C0)))
+    dump("tg_adi_restricted.json", {"sN": sN, "M": M, "tau": 5e-3, "alpha": 0.7, "d": 0.1, "C1": 0.3, "S": 0.05,
+                                    "steps": 40, "dt_alg": 2, "dt_eps": 0.012, "dL": dL, "dLx": dLx,
+                                    "sigma": sigma, "V2": list(V2), "C0": list(C0), "C": res["c"][0]})
+    res = parse(run("tg", args[:7] + [40], list(V2) + list(C0)))
+    dump("tg_adi_40.json", {"C": res["c"][0]})
     # Atangana-Baleanu: Mittag-Leffler values, lag weights, solve_and_check error
     ml = []
     for (a, b, z) in [(0.5, 1.0, -0.7), (0.8, 1.0, -1.2), (0.6, 2.0, -0.9), (0.9, 5.0, -0.5),

@@ -345,6 +345,66 @@ def test_tg_vs_oracle(ctx, sN, M, steps, mode):
     assert relmax(s.get_c(), ref) <= TOL_SOLVER
 
 
+@pytest.mark.parametrize("mode", [0, 2])  # FH_TG_FP64, FH_TG_DF64
+def test_tg_restricted_reference_golden(ctx, mode):
+    """Restricted summing (dt_alg 2, dt_eps 0.012) against the reference run."""
+    from theses_code_gb300.solvers import TGSolver
+    g = json.load(open(os.path.join(G, "tg_adi_restricted.json")))
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+             C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+    s = TGSolver(ctx, p, g["steps"], mode)
+    s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+    s.set_restricted(g["dt_eps"])
+    s.calc_step(g["steps"])
+    assert relmax(s.get_c(), g["C"]) <= TOL_SOLVER
+
+
+@pytest.mark.parametrize("mode,tol", [(0, TOL_SOLVER), (2, TOL_SOLVER), (1, 1e-9)])  # FP64, DF64, blocked
+def test_tg_restricted_vs_oracle(ctx, mode, tol):
+    """150 steps with the sums cut about 32 layer pairs back (psi = t: the
+    sums read only those layers); the blocked mode also zeroes the cut
+    weights of its tensor-core rows.  A second solve with dt_eps = 0 is the
+    full history again."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 40, alpha=0.7, tau=5e-4, d=0.1, seed=9, C1=0.2, S=0.01)
+    steps, eps = 150, 0.003
+    s = TGSolver(ctx, p, steps, mode)
+    s.set_state(V2, C0)
+    s.set_restricted(eps)
+    s.calc_step(steps)
+    ref, _ = O.tg_solve(dict(p, dt_alg=2, dt_eps=eps), V2, C0, steps)
+    full, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(full, ref) > 1e-4
+    assert relmax(s.get_c(), ref) <= tol
+    s.set_state(V2, C0)
+    s.set_restricted(0.0)
+    s.calc_step(steps)
+    assert relmax(s.get_c(), full) <= tol
+
+
+def test_tg_restricted_psi_beta_vs_oracle(ctx):
+    """psi = t^1.3 (weights not Toeplitz: every stored layer pair is visited,
+    the cut ones with weight 0)."""
+    import math
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 33, alpha=0.6, tau=1e-3, seed=4, C1=0.1)
+    p["beta"] = 1.3
+    steps = 60
+    Da = 1.0 / math.gamma(1.0 - p["alpha"])
+    w = [Da * O.psi_int(k, k + 1.0, steps - 0.5, p["tau"], p["alpha"], 1.3) for k in (39, 40)]
+    eps = 0.5 * (w[0] + w[1])  # between the weights 20 and 19 layer pairs back at the last step
+    s = TGSolver(ctx, p, steps)
+    s.set_state(V2, C0)
+    s.set_restricted(eps)
+    s.calc_step(steps)
+    ref, _ = O.tg_solve(dict(p, dt_alg=2, dt_eps=eps), V2, C0, steps)
+    full, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(full, ref) > 1e-6
+    assert relmax(s.get_c(), ref) <= 1e-11
+
+
 def test_tg_solvers_of_different_sizes_coexist(ctx):
     """A smaller solver created after a larger one must not break the larger
     one's sweeps (their shared-memory needs differ)."""

@@ -52,6 +52,21 @@ def test_tg_adi_matches_reference():
     assert relmax(C, g["C"]) <= 1e-13
 
 
+def test_tg_adi_restricted_matches_reference():
+    """dt_alg 2 (restricted summing, dt_eps 0.012): the sums stop about 12
+    layer pairs back; the result moves far from the full-history run."""
+    g = load("tg_adi_restricted.json")
+    full = load("tg_adi_40.json")
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"],
+             d=g["d"], C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"], dt_alg=2, dt_eps=g["dt_eps"])
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), g["steps"])
+    assert relmax(C, g["C"]) <= 1e-13
+    assert relmax(np.array(full["C"]), g["C"]) > 0.05
+    p["dt_alg"] = 0
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), g["steps"])
+    assert relmax(C, full["C"]) <= 1e-13
+
+
 def test_psi_weights_match_reference_series():
     """calc_int (mt_psi_caputo.cpp:720-741) at eps 1e-15 against the converged
     incomplete-beta value.  The reference series does not converge on the very

@@ -349,12 +349,15 @@ __device__ __forceinline__ void fh_slice_row_group(const Val &val, int G, int nc
 
 // Weight planes of a TG block: row m = 2r + {0: x, 1: y} of step j0 + r,
 // A3[s][m][k] (K-major) and Ew[c][m]; one warp per (row, chunk group).
-__global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, double alpha, double beta,
+__global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, double alpha, double beta, double cut,
                               __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
   const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (m >= kBM) return;
   const double X = (double)(j0 + (m >> 1)) + ((m & 1) ? 1.0 : 0.5);
-  auto val = [&](int k) { return k < K ? Da * fh_psi_int((double)k + 0.0, (double)k + 1.0, X, tau, alpha, beta) : 0.0; };
+  auto val = [&](int k) {  // weights below `cut` are 0 (restricted summing)
+    const double w = k < K ? Da * fh_psi_int((double)k + 0.0, (double)k + 1.0, X, tau, alpha, beta) : 0.0;
+    return fabs(w) < cut ? 0.0 : w;
+  };
   fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
 }
 
@@ -631,7 +634,7 @@ int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k
 // Weight planes of the TG block starting at step j0 (K = j0 history layers).
 // With a weight table (row 2j: x weights of step j, row 2j+1: y weights, pitch
 // ldw, nsteps steps) the rows are taken from it instead of being recomputed.
-int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta,
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta, double cut,
                       const double *table, int ldw, int nsteps) {
   dim3 g((unsigned)fh_ngroups(j0 / kBK), kBM / 8);
   if (table) {
@@ -640,7 +643,7 @@ int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, dou
                                                  b.A3.as<__nv_bfloat16>(), b.Ew.as<int8_t>());
     return fh_after_launch(ctx, "k_blk_split_rows");
   }
-  k_blk_weights<<<g, 256, 0, ctx->stream>>>(j0, j0, b.Kcap, Da, tau, alpha, beta, b.A3.as<__nv_bfloat16>(),
+  k_blk_weights<<<g, 256, 0, ctx->stream>>>(j0, j0, b.Kcap, Da, tau, alpha, beta, cut, b.A3.as<__nv_bfloat16>(),
                                            b.Ew.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_weights");
 }

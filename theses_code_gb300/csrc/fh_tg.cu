@@ -37,7 +37,7 @@ fh_blk *fh_blk_new();
 void fh_blk_delete(fh_blk *b);
 int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
-int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta,
+int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta, double cut,
                       const double *table, int ldw, int nsteps);
 int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo);
 long long fh_blk_ppad(const fh_blk &b);
@@ -47,7 +47,15 @@ struct fh_tg_dev {
   int sN, M, ld;
   long long P;
   double tau, alpha, beta, Da, st, d, C1, S, dL, dLx;
+  double hcut;  // restricted summing: history weights below hcut are 0 (0: full history)
 };
+
+// History weight w with restricted summing (dt_alg 2, fr_d_t_g_2d.cpp:3356-3380):
+// the reference's sums run from the newest layer pair back and stop at the
+// first weight below dt_eps.  The weights fall monotonically with the lag
+// (psi increasing), so zeroing every weight below dt_eps drops exactly the
+// layers the reference leaves out.
+__device__ __forceinline__ double tg_hw(const fh_tg_dev &g, double w) { return fabs(w) < g.hcut ? 0.0 : w; }
 
 struct fh_tg_solver {
   fh_ctx *ctx = nullptr;
@@ -83,6 +91,9 @@ struct fh_tg_solver {
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
   long long ldfar = 0;
   fh_graph_cache graph;
+  // restricted summing with psi = t: every history weight of a lag beyond
+  // rs_lag is below the cut (-1: unknown or full history)
+  int rs_lag = -1;
   ~fh_tg_solver() {
     if (blk) fh_blk_delete(blk);
     if (hs) {
@@ -103,8 +114,8 @@ __global__ void k_tg_weights(fh_tg_dev g, int j, int kstart, double *__restrict_
   const int k = kstart + blockIdx.x * blockDim.x + threadIdx.x;
   if (k < j) {
     const double s0 = (double)k + 0.0;
-    W[k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta);
-    W[ldw + k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta);
+    W[k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta));
+    W[ldw + k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta));
   }
   if (k == kstart) {
     const double jj = (double)j;
@@ -181,8 +192,8 @@ __global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ W
   double *W = Wall + (long long)j * 2 * ldw;
   if (k < j) {
     const double s0 = (double)k + 0.0;
-    W[k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta);
-    W[ldw + k] = g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta);
+    W[k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta));
+    W[ldw + k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta));
   }
   if (k == 0) {
     const double jj = (double)j;
@@ -1302,14 +1313,18 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
     // far rows S_far[2r + {0,1}] = sum_{k<j} w_{j+r}(k) D[k] on the tensor cores
     fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
     if ((rc = fh_blk_convert(ctx, *s->blk, s->D.as<double>(), g.P, j - kTgBlock, s->df ? 1 : 0))) return rc;
-    if ((rc = fh_blk_tg_weights(ctx, *s->blk, j, g.Da, g.tau, g.alpha, g.beta, s->wtab ? s->W.as<double>() : nullptr,
+    if ((rc = fh_blk_tg_weights(ctx, *s->blk, j, g.Da, g.tau, g.alpha, g.beta, g.hcut,
+                                s->wtab ? s->W.as<double>() : nullptr,
                                 s->max_steps, s->max_steps)))
       return rc;
     fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
     if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<float2>(), s->ldfar))) return rc;
     s->j0 = j;
   }
-  const int kstart = blocked ? s->j0 : 0;  // history layers summed in FP64 this step
+  // history layers summed in FP64 this step: the current block in blocked
+  // mode; with restricted summing and psi = t, the layers within the cut lag
+  int kstart = blocked ? s->j0 : 0;
+  if (!blocked && s->rs_lag >= 0 && j > s->rs_lag) kstart = j - s->rs_lag;
   const int knear = j - kstart;
   const double *Wj;
   if (s->wtab) {
@@ -1537,6 +1552,35 @@ int fh_tg_destroy(fh_tg_solver *s) {
   if (!s) return FH_OK;
   if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
   delete s;
+  return FH_OK;
+}
+
+// Closed-form psi = t weight of the lag-d layer pair (interval [j-d, j-d+1])
+// at time j + ja, ja = 0.5 (x sums) or 1 (y sums), without Da tau^(1-a)/(1-a).
+static double tg_lag_weight(double d, double ja, double a) {
+  return pow(d + ja, 1.0 - a) - pow(d + ja - 1.0, 1.0 - a);
+}
+
+int fh_tg_set_restricted(fh_tg_solver *s, double dt_eps) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_restricted: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, dt_eps >= 0.0 && dt_eps < 1e300, FH_EINVAL, "fh_tg_set_restricted: dt_eps = %g", dt_eps);
+  FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_restricted: only before the first step of a solve");
+  s->dv.hcut = dt_eps;
+  s->rs_lag = -1;
+  if (dt_eps > 0.0 && s->p.beta == 1.0) {
+    // first lag whose x and y weights are both below dt_eps (1 - 1e-9) (the
+    // device weights there are certainly cut: they differ from these by ulps);
+    // all longer lags have smaller weights, so the sums may start at j - rs_lag
+    const double a = s->p.alpha, f = s->dv.Da * pow(s->p.tau, 1.0 - a) / (1.0 - a);
+    const double cut = dt_eps * (1.0 - 1e-9);
+    for (int d = 1; d <= s->max_steps; ++d)
+      if (f * tg_lag_weight(d, 0.5, a) < cut && f * tg_lag_weight(d, 1.0, a) < cut) {
+        s->rs_lag = d;
+        break;
+      }
+  }
+  s->graph.reset();
   return FH_OK;
 }
 

@@ -124,6 +124,11 @@ class TGSolver:
     def set_state_device(self, V2_ptr: int, C_ptr: int):
         check(self.ctx.L.fh_tg_set_state(self.h, C.c_void_p(V2_ptr), C.c_void_p(C_ptr)), self.ctx.h)
 
+    def set_restricted(self, dt_eps: float):
+        """Restricted summing (the reference's dt_alg 2): each history sum stops
+        at the first weight below dt_eps, newest layer first; 0 = full history."""
+        check(self.ctx.L.fh_tg_set_restricted(self.h, float(dt_eps)), self.ctx.h)
+
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_tg_step(self.h, int(n)), self.ctx.h)
 
