@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--dt-eps", type=float, default=0.0,
                     help="tg2d: restricted summing (the reference's dt_alg 2) with this weight cut; 0 = full history")
+    ap.add_argument("--series", type=int, default=0,
+                    help="tg2d: series expansion of the history (the reference's dt_alg 3) with this many terms")
     return ap.parse_args()
 
 
@@ -202,6 +204,7 @@ class TG2D(Workload):
         self.modes = {"blocked": FH_TG_BLOCKED, "df64": FH_TG_DF64, "fp64": FH_TG_FP64}
         self.p = p
         self.dt_eps = args.dt_eps
+        self.series = args.series
         self.S = S
         self.solver = self.new_solver(ctx, args.mode)
         self.V2_d = torch.as_tensor(V2, device=f"cuda:{dev}").contiguous()
@@ -236,15 +239,22 @@ class TG2D(Workload):
             # restricted summing: only the layer pairs whose weight reaches dt_eps
             lag = self.restricted_lag(p, args.dt_eps, S) if args.dt_eps > 0 else S
             self.alg = {"history": sum(8.0 * min(j, lag) * pint + 16.0 * pint for j in range(1, S))}
+            if args.series:
+                # series accumulators: newest pair read, J accumulators read and written, two sums written
+                self.alg = {"history": (S - 1) * (16.0 * args.series + 24.0) * pint}
         # sweeps: x reads C, fa, g, al, one history row, writes Ch; y reads Ch, C, fa, g,
         # al, one history row, writes C and the new history layer; in blocked mode each
         # sweep also reads the j % 8 layers of the current sub-block
         self.alg["sweep"] = sum((112.0 + (16.0 * (j % 8) if blocked else 0.0)) * pint for j in range(S))
         self.alg_hist_bytes = self.alg["history"]
-        self.name = f"tg2d_adi_{G}x{G}_{S}steps" + (f"_restricted{args.dt_eps:g}" if args.dt_eps > 0 else "")
+        self.name = (f"tg2d_adi_{G}x{G}_{S}steps" + (f"_restricted{args.dt_eps:g}" if args.dt_eps > 0 else "")
+                     + (f"_series{args.series}" if args.series else ""))
         self.config = {"workload": self.name, "grid": [G, G], "solve_steps": S, "alpha": 0.7, "tau": 5e-4,
                        "d": 0.1, "velocity_modes": 8, "mode": args.mode,
                        "l2": "inputs larger than L2 (history up to %.1f GB per solve)" % (S * P * 8 / 1e9)}
+        if args.series:
+            self.config["dt_alg"] = 3
+            self.config["series_terms"] = args.series
         if args.dt_eps > 0:
             self.config["dt_alg"] = 2
             self.config["dt_eps"] = args.dt_eps
@@ -278,6 +288,8 @@ class TG2D(Workload):
         sv = TGSolver(ctx, self.p, self.S, self.modes[mode])
         if self.dt_eps > 0:
             sv.set_restricted(self.dt_eps)
+        if self.series and mode != "blocked":
+            sv.set_series(self.series)
         return sv
 
     @staticmethod
@@ -298,7 +310,7 @@ class TG2D(Workload):
         self.solve_device()
         res = {main_mode: self.solver.get_c()}
         times = {}
-        for m in ("fp64", "df64", "blocked"):
+        for m in ("fp64", "df64") + (() if self.series else ("blocked",)):
             if m == main_mode:
                 continue
             sv = self.new_solver(ctx, m)

@@ -236,6 +236,14 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C);
  * layers within the lag where the weights fall below dt_eps; the history
  * store keeps every layer. */
 int fh_tg_set_restricted(fh_tg_solver *s, double dt_eps);
+/* Series expansion of the history sums, TG_solver_ with dt_alg 3 and
+ * dt_eps = nterms (replaces the Om1 series branch fr_d_t_g_2d.cpp:3384-3429
+ * with _kb_row2 2965-3040 and _kb_row2_fixed_coefs 3041-3057): per node
+ * nterms accumulators of the binomial series of (t_n - s)^(-alpha) replace
+ * the stored layers (memory nterms + 1 layers instead of max_steps).
+ * psi = t, FH_TG_FP64 or FH_TG_DF64 only; nterms = 0 restores the full
+ * history; 1..256.  Only before the first step of a solve. */
+int fh_tg_set_series(fh_tg_solver *s, int nterms);
 /* TG_solver::calc_step repeated nsteps times. */
 int fh_tg_step(fh_tg_solver *s, int nsteps);
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);

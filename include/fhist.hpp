@@ -88,6 +88,8 @@ class TG_solver {
   // dt_alg 2 with dt_eps (restricted summing), or dt_alg 0 with dt_eps = 0;
   // before the first step of a solve
   void set_restricted(double dt_eps) { ctx_.check(fh_tg_set_restricted(s_, dt_eps)); }
+  // dt_alg 3 with dt_eps = nterms (series expansion, psi = t), 0 = full history
+  void set_series(int nterms) { ctx_.check(fh_tg_set_series(s_, nterms)); }
   // TG_solver::calc_step (fr_d_t_g_2d.cpp:2552): x half step, y half step
   void calc_step() { calc_steps(1); }
   void calc_steps(int n) {

@@ -225,7 +225,8 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
 
 /* One x line (dir 0, line jj) or y line (dir 1, line ii) of TG_solver::calc_step. */
 static void tg_line(const fho_tg_params *p, const double *V2, double *C, const double *work, int j, int dir, int line,
-                    double kcur, double kyh, const double *wk, double *A, double *B, double *R, double *Om, double *u) {
+                    double kcur, double kyh, const double *wk, const double *hs, double *A, double *B, double *R,
+                    double *Om, double *u) {
   const int sN = p->sN, M = p->M, ld = sN + 2;
   const size_t P = (size_t)(sN + 2) * (M + 2);
   const double st = p->sigma / p->tau;
@@ -244,7 +245,9 @@ static void tg_line(const fho_tg_params *p, const double *V2, double *C, const d
     Om[i] = -st * (kcur + 0.0) * C[id];
     Om[i] += p->S * 0.5;
     double ts = 0.0;
-    if (2 * j + 1 + dir >= 3)
+    if (hs) /* dt_alg 3: the series value of this step */
+      ts = hs[id];
+    else if (2 * j + 1 + dir >= 3)
       for (int k = j - 1; k >= 0; --k) {
         if (p->dt_alg == 2 && fabs(wk[k]) < p->dt_eps) break; /* restricted summing (3364-3380) */
         ts += wk[k] * (work[(size_t)(k + 1) * P + id] - work[(size_t)k * P + id]);
@@ -260,6 +263,45 @@ static void tg_line(const fho_tg_params *p, const double *V2, double *C, const d
     C[dir == 0 ? (size_t)i + (size_t)line * ld : (size_t)line + (size_t)i * ld] = u[i];
 }
 
+/* dt_alg 3, psi = t (fr_d_t_g_2d.cpp:3384-3429 with _kb_row2 2965-3040 and
+ * _kb_row2_fixed_coefs 3041-3057, dt_eps = J terms): per point the series
+ * accumulators H[n] = sum_t int_{t tau}^{(t+1) tau} s^n ds (C^{t+1} - C^t)
+ * gain the newest layer pair each step (the x and y sums of the reference
+ * keep two equal copies), and the history sum at time gtj is
+ * Da sum_n (alpha)_n / n! gtj^(-alpha-n) H[n], cut at the first non-finite
+ * coefficient. */
+static void tg_series_add(const fho_tg_params *p, int J, int j, size_t P, const double *dnew, const double *dold,
+                          double *H) {
+  const double t0 = p->tau * (double)(j - 1), t1 = p->tau * (double)j; /* interval j-1 */
+  double v6 = t0 / t1, mult = t1;
+  for (int n = 0; n < J; ++n) {
+    double v3;
+    if (n == 0) {
+      v3 = (t1 - t0) / t1;
+    } else {
+      v6 *= t0 / t1;
+      v3 = 0.0 + 1.0 * ((1.0 / (n + 1.0)) * (1 - v6)); /* inv_g_der(t1, 1, t1) = 1 for psi = t */
+    }
+    const double c = mult * v3;
+    for (size_t id = 0; id < P; ++id) H[(size_t)n * P + id] += c * (dnew[id] - dold[id]);
+    mult *= t1;
+  }
+}
+
+static void tg_series_eval(const fho_tg_params *p, int J, double gtj, size_t P, const double *H, double Da,
+                           double *out) {
+  const double a = p->alpha;
+  for (size_t id = 0; id < P; ++id) out[id] = 0.0;
+  double v1 = pow(gtj, -a), i = 0.0;
+  for (int n = 0; n < J; ++n) {
+    for (size_t id = 0; id < P; ++id) out[id] += v1 * H[(size_t)n * P + id];
+    i += 1.0;
+    v1 *= -(-a - i + 1.0) / (i * gtj);
+    if (!isfinite(v1)) break;
+  }
+  for (size_t id = 0; id < P; ++id) out[id] = Da * out[id];
+}
+
 int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work) {
   const int sN = p->sN, M = p->M;
   const size_t P = (size_t)(sN + 2) * (M + 2);
@@ -269,12 +311,25 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
   double *wx = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
   double *wy = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
   if (!wx || !wy) return 1;
+  const int J = p->dt_alg == 3 ? (int)p->dt_eps : 0;
+  if (p->dt_alg == 3 && (J < 1 || p->beta != 1.0)) return 2;
+  double *H = J ? (double *)calloc((size_t)J * P, sizeof(double)) : NULL;
+  double *hx = J ? (double *)malloc(sizeof(double) * P) : NULL, *hy = J ? (double *)malloc(sizeof(double) * P) : NULL;
+  if (J && (!H || !hx || !hy)) return 1;
   memcpy(work, C, sizeof(double) * P); /* full-step layer 0 (TG_solver::initial) */
 #define KB(s, ja, sa, l) (Da * fho_psi_int((double)(s) + (sa), (double)(s) + (sa) + (l), (double)j + (ja), p->tau, a, p->beta))
   for (int j = 0; j < steps; ++j) {
     /* weights of TG_solver_::kb (fr_d_t_g_2d.cpp:3059-3239), dt_alg 0 */
     const double kx = KB(j, 0.5, 0.0, 0.5), ky = KB(j, 1.0, 0.5, 0.5), kyh = KB(j, 1.0, 0.0, 0.5);
     for (int k = 0; k < j; ++k) { wx[k] = KB(k, 0.5, 0.0, 1.0); wy[k] = KB(k, 1.0, 0.0, 1.0); }
+    const double *hsx = NULL, *hsy = NULL;
+    if (J && j >= 1) {
+      tg_series_add(p, J, j, P, work + (size_t)j * P, work + (size_t)(j - 1) * P, H);
+      tg_series_eval(p, J, p->tau * ((double)j + 0.5), P, H, Da, hx);
+      tg_series_eval(p, J, p->tau * ((double)j + 1.0), P, H, Da, hy);
+      hsx = hx;
+      hsy = hy;
+    }
     /* x half-step: lines jj = 1..M-1 (fr_d_t_g_2d.cpp:2577-2590); y half-step: lines
      * ii = 1..sN-1 (2634-2648).  Lines are independent, so they run in parallel. */
     for (int dir = 0; dir < 2; ++dir) {
@@ -286,14 +341,15 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
         double *u = (double *)malloc(sizeof(double) * nmax);
 #pragma omp for schedule(static)
         for (int line = 1; line < nlines; ++line)
-          tg_line(p, V2, C, work, j, dir, line, dir == 0 ? kx : ky, kyh, dir == 0 ? wx : wy, A, B, R, Om, u);
+          tg_line(p, V2, C, work, j, dir, line, dir == 0 ? kx : ky, kyh, dir == 0 ? wx : wy, dir == 0 ? hsx : hsy,
+                  A, B, R, Om, u);
         free(A); free(B); free(R); free(Om); free(u);
       }
     }
     memcpy(work + (size_t)(j + 1) * P, C, sizeof(double) * P);
   }
 #undef KB
-  free(wx); free(wy);
+  free(wx); free(wy); free(H); free(hx); free(hy);
   return 0;
 }
 

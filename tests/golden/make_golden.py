@@ -97,6 +97,9 @@ def main():
                                     "sigma": sigma, "V2": list(V2), "C0": list(C0), "C": res["c"][0]})
     res = parse(run("tg", args[:7] + [40], list(V2) + list(C0)))
     dump("tg_adi_40.json", {"C": res["c"][0]})
+    # series expansion (dt_alg 3, psi = t): 12 terms, 40 steps
+    res = parse(run("tg", args[:7] + [40, 3, 12], list(V2) + list(C0)))
+    dump("tg_adi_series.json", {"steps": 40, "dt_alg": 3, "dt_eps": 12, "C": res["c"][0]})
     # Atangana-Baleanu: Mittag-Leffler values, lag weights, solve_and_check error
     ml = []
     for (a, b, z) in [(0.5, 1.0, -0.7), (0.8, 1.0, -1.2), (0.6, 2.0, -0.9), (0.9, 5.0, -0.5),

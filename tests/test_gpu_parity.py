@@ -405,6 +405,67 @@ def test_tg_restricted_psi_beta_vs_oracle(ctx):
     assert relmax(s.get_c(), ref) <= 1e-11
 
 
+@pytest.mark.parametrize("mode", [0, 2])  # FH_TG_FP64, FH_TG_DF64
+def test_tg_series_reference_golden(ctx, mode):
+    """Series expansion (dt_alg 3, 12 terms) against the reference run."""
+    from theses_code_gb300.solvers import TGSolver
+    g = json.load(open(os.path.join(G, "tg_adi_restricted.json")))
+    sr = json.load(open(os.path.join(G, "tg_adi_series.json")))
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+             C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+    s = TGSolver(ctx, p, sr["steps"], mode)
+    s.set_series(sr["dt_eps"])
+    s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+    s.calc_step(sr["steps"])
+    assert relmax(s.get_c(), sr["C"]) <= TOL_SOLVER
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_tg_series_vs_oracle(ctx, mode):
+    """40 x 40, 150 steps, 20 terms: captured-graph solve, a second solve from
+    the same state (the accumulators restart), uneven calls, and back to the
+    full history with 0 terms."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 40, alpha=0.7, tau=5e-4, d=0.1, seed=9, C1=0.2, S=0.01)
+    steps, J = 150, 20
+    ref, _ = O.tg_solve(dict(p, dt_alg=3, dt_eps=J), V2, C0, steps)
+    full, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(full, ref) > 1e-4
+    s = TGSolver(ctx, p, steps, mode)
+    s.set_series(J)
+    for calls in ((steps,), (steps,), (1, 60, 89)):
+        s.set_state(V2, C0)
+        for n in calls:
+            s.calc_step(n)
+        assert relmax(s.get_c(), ref) <= TOL_SOLVER, calls
+    s.set_state(V2, C0)
+    s.set_series(0)
+    s.calc_step(steps)
+    assert relmax(s.get_c(), full) <= TOL_SOLVER
+
+
+def test_tg_series_limits(ctx):
+    """The series needs psi = t and a plain mode; bad term counts are refused."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FhError
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 40, alpha=0.7, tau=5e-4, d=0.1, seed=9)
+    with pytest.raises(FhError):
+        TGSolver(ctx, p, 100, FH_TG_BLOCKED).set_series(10)
+    s = TGSolver(ctx, dict(p, beta=1.3), 10)
+    with pytest.raises(FhError):
+        s.set_series(10)
+    s = TGSolver(ctx, p, 10)
+    for bad in (-1, 257):
+        with pytest.raises(FhError):
+            s.set_series(bad)
+    s.set_state(V2, C0)
+    s.calc_step(1)
+    with pytest.raises(FhError):  # only before the first step
+        s.set_series(5)
+
+
 def test_tg_solvers_of_different_sizes_coexist(ctx):
     """A smaller solver created after a larger one must not break the larger
     one's sweeps (their shared-memory needs differ)."""

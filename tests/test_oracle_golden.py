@@ -67,6 +67,18 @@ def test_tg_adi_restricted_matches_reference():
     assert relmax(C, full["C"]) <= 1e-13
 
 
+def test_tg_adi_series_matches_reference():
+    """dt_alg 3 (series expansion, 12 terms, psi = t) against the reference run."""
+    g = load("tg_adi_restricted.json")  # the same problem
+    sr = load("tg_adi_series.json")
+    full = load("tg_adi_40.json")
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"],
+             d=g["d"], C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"], dt_alg=3, dt_eps=sr["dt_eps"])
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), sr["steps"])
+    assert relmax(C, sr["C"]) <= 1e-13
+    assert relmax(np.array(full["C"]), sr["C"]) > 0.01
+
+
 def test_psi_weights_match_reference_series():
     """calc_int (mt_psi_caputo.cpp:720-741) at eps 1e-15 against the converged
     incomplete-beta value.  The reference series does not converge on the very

@@ -23,6 +23,8 @@
 // layer per full step, D[k] = C^{k+1} - C^k (the half-step layers the
 // reference also stores are only read through Ch).
 #include <algorithm>
+#include <cmath>
+#include <vector>
 #include <mutex>
 
 #include "fh_internal.h"
@@ -94,6 +96,11 @@ struct fh_tg_solver {
   // restricted summing with psi = t: every history weight of a lag beyond
   // rs_lag is below the cut (-1: unknown or full history)
   int rs_lag = -1;
+  // series expansion (dt_alg 3): ser_J terms, accumulators H[n][p], per-step
+  // coefficient rows ser_tab[j] = c[J] | ex[J] | ey[J]; the history store
+  // keeps only the newest layer pair
+  int ser_J = 0;
+  fh_dbuf H, ser_tab;
   ~fh_tg_solver() {
     if (blk) fh_blk_delete(blk);
     if (hs) {
@@ -201,6 +208,42 @@ __global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ W
     cwall[4 * j + 1] = g.Da * fh_psi_int(jj + 0.5, jj + 0.5 + 0.5, jj + 1.0, g.tau, g.alpha, g.beta);
     cwall[4 * j + 2] = g.Da * fh_psi_int(jj + 0.0, jj + 0.0 + 0.5, jj + 1.0, g.tau, g.alpha, g.beta);
   }
+}
+
+// Series expansion of the history sums (dt_alg 3, psi = t; fr_d_t_g_2d.cpp:
+// 3384-3429): per point the accumulators gain the newest layer pair,
+// H[n] += c[n] (C^j - C^(j-1)) (one FMA: FP64-pipe-bound kernel), and the
+// x and y sums are Da sum_n e[n] H[n] with the per-step coefficients
+// e[n] = (alpha)_n / n! gtj^(-alpha-n) of the two half-step times (zero after
+// the reference's cut at the first non-finite one).  Writes the sums where
+// the sweeps read one K split (part[0][p], part[1][p]).  One point per
+// thread; the step's coefficient row staged in shared memory.
+static constexpr int kSerMaxTerms = 256;
+__global__ void __launch_bounds__(256) k_tg_series(const double *__restrict__ Dn, int df, double *__restrict__ H, int J,
+                                                   long long P, const double *__restrict__ tab, double Da,
+                                                   double *__restrict__ part) {
+  __shared__ double ct[3 * kSerMaxTerms];
+  for (int i = threadIdx.x; i < 3 * J; i += blockDim.x) ct[i] = tab[i];
+  __syncthreads();
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double d;
+  if (df) {
+    const float2 v = reinterpret_cast<const float2 *>(Dn)[p];
+    d = (double)v.x + (double)v.y;
+  } else {
+    d = Dn[p];
+  }
+  double sx = 0.0, sy = 0.0;
+  double *h = H + p;
+  for (int n = 0; n < J; ++n, h += P) {
+    const double v = fma(ct[n], d, *h);
+    *h = v;
+    sx = fma(ct[J + n], v, sx);
+    sy = fma(ct[2 * J + n], v, sy);
+  }
+  part[p] = Da * sx;
+  part[P + p] = Da * sy;
 }
 
 // Shared-memory footprint of one staged line array: fh_sk(N+1)+1 doubles.
@@ -1325,6 +1368,7 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   // mode; with restricted summing and psi = t, the layers within the cut lag
   int kstart = blocked ? s->j0 : 0;
   if (!blocked && s->rs_lag >= 0 && j > s->rs_lag) kstart = j - s->rs_lag;
+  if (s->ser_J) kstart = j;  // series expansion: no layer sums
   const int knear = j - kstart;
   const double *Wj;
   if (s->wtab) {
@@ -1352,6 +1396,15 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   const float2 *far = nullptr;
   if (blocked && s->j0 > 0) far = s->far.as<float2>() + 2LL * (j - s->j0) * s->ldfar;
   int splits = 0, kchunk = 0;
+  if (s->ser_J && j >= 1) {
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+    k_tg_series<<<(unsigned)fh_ceil_div(g.P, 256), 256, 0, ctx->stream>>>(
+        s->D.as<double>(), s->df ? 1 : 0, s->H.as<double>(), s->ser_J, g.P,
+        s->ser_tab.as<double>() + 3LL * s->ser_J * j, g.Da, s->part.as<double>());
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+    if ((rc = fh_after_launch(ctx, "k_tg_series"))) return rc;
+    splits = 1;
+  }
   if (knear >= 1) {
     fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
     if (s->df)
@@ -1378,7 +1431,8 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
   const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
   k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
-      g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (long long)j * g.P, s->part.as<double>(), g.P,
+      g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (s->ser_J ? 0LL : (long long)j * g.P),
+      s->part.as<double>(), g.P,
       splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(),
       s->pby.as<double>(), cwj, fary, s->df ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
@@ -1584,6 +1638,73 @@ int fh_tg_set_restricted(fh_tg_solver *s, double dt_eps) {
   return FH_OK;
 }
 
+int fh_tg_set_series(fh_tg_solver *s, int nterms) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_series: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, nterms >= 0 && nterms <= kSerMaxTerms, FH_EINVAL, "fh_tg_set_series: nterms = %d (0..%d)", nterms,
+             kSerMaxTerms);
+  FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_series: only before the first step of a solve");
+  FH_REQUIRE(ctx, nterms == 0 || (s->p.beta == 1.0 && s->mode != FH_TG_BLOCKED), FH_EINVAL,
+             "fh_tg_set_series: psi = t and the FP64 or DF64 mode only");
+  const fh_tg_dev &g = s->dv;
+  int rc;
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->H.release();
+  s->ser_tab.release();
+  s->D.release();
+  s->ser_J = 0;
+  s->graph.reset();
+  // the history store: every layer pair, or only the newest for the series
+  if ((rc = fh_alloc(ctx, s->D, sizeof(double) * (size_t)g.P * (nterms ? 1 : (size_t)s->max_steps)))) return rc;
+  if (nterms == 0) return FH_OK;
+  // coefficient rows of every step j >= 1 (fr_d_t_g_2d.cpp _kb_row2 2965-3040
+  // for psi = t, where the inner integral is exact after one term, and
+  // _kb_row2_fixed_coefs 3041-3057), in the reference's arithmetic
+  const int J = nterms;
+  std::vector<double> tab((size_t)s->max_steps * 3 * J, 0.0);
+  const double tau = s->p.tau, a = s->p.alpha;
+  for (int j = 1; j < s->max_steps; ++j) {
+    double *c = tab.data() + (size_t)j * 3 * J, *ex = c + J, *ey = c + 2 * J;
+    const double t0 = tau * (double)(j - 1), t1 = tau * (double)j;
+    double v6 = t0 / t1, mult = t1;
+    for (int n = 0; n < J; ++n) {
+      double v3;
+      if (n == 0) {
+        v3 = (t1 - t0) / t1;
+      } else {
+        v6 *= t0 / t1;
+        v3 = 0.0 + 1.0 * ((1.0 / (n + 1.0)) * (1 - v6));
+      }
+      c[n] = mult * v3;
+      mult *= t1;
+    }
+    for (int m = 0; m < 2; ++m) {
+      double *e = m ? ey : ex;
+      const double gtj = tau * ((double)j + (m ? 1.0 : 0.5));
+      double v1 = pow(gtj, -a), i = 0.0;
+      for (int n = 0; n < J; ++n) {
+        e[n] = v1;
+        i += 1.0;
+        v1 *= -(-a - i + 1.0) / (i * gtj);
+        if (!std::isfinite(v1)) break;  // the remaining coefficients stay 0
+      }
+    }
+  }
+  if ((rc = fh_alloc(ctx, s->H, sizeof(double) * (size_t)J * (size_t)g.P)) ||
+      (rc = fh_alloc(ctx, s->ser_tab, sizeof(double) * tab.size(), false)))
+    return rc;
+  FH_CUDA_TRY(ctx, cudaMemcpy(s->ser_tab.p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+  s->ser_J = J;
+  return FH_OK;
+}
+
+// Zero series accumulators at the start of a solve.
+static int tg_series_reset(fh_tg_solver *s) {
+  if (!s->ser_J) return FH_OK;
+  FH_CUDA_TRY(s->ctx, cudaMemsetAsync(s->H.p, 0, s->H.bytes, s->ctx->stream));
+  return FH_OK;
+}
+
 int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_state: null solver");
   fh_ctx *ctx = s->ctx;
@@ -1597,6 +1718,7 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
   if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (int rc = tg_series_reset(s)) return rc;
   s->tstep = 0;
   s->j0 = 0;
   s->have_state = true;
@@ -1616,6 +1738,7 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
   if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (int rc = tg_series_reset(s)) return rc;
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->tstep = 0;
   s->j0 = 0;

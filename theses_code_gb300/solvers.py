@@ -129,6 +129,12 @@ class TGSolver:
         at the first weight below dt_eps, newest layer first; 0 = full history."""
         check(self.ctx.L.fh_tg_set_restricted(self.h, float(dt_eps)), self.ctx.h)
 
+    def set_series(self, nterms: int):
+        """Series expansion of the history sums (the reference's dt_alg 3 with
+        dt_eps = nterms, psi = t): nterms accumulators per node replace the
+        stored layers; 0 = full history."""
+        check(self.ctx.L.fh_tg_set_series(self.h, int(nterms)), self.ctx.h)
+
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_tg_step(self.h, int(n)), self.ctx.h)
 
