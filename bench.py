@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--dt-eps", type=float, default=0.0,
                     help="tg2d: restricted summing (the reference's dt_alg 2) with this weight cut; 0 = full history")
+    ap.add_argument("--gamma-min", type=float, default=1.0,
+                    help="psi_batch: space-derivative orders drawn from U[gamma_min, 1) (< 1: fractional in z)")
     ap.add_argument("--series", type=int, default=0,
                     help="tg2d: series expansion of the history (the reference's dt_alg 3) with this many terms")
     return ap.parse_args()
@@ -358,6 +360,13 @@ class H1D(Workload):
         # HBM-bound sums) unless --mode fp64; the single cfg-1 instance stays FP64
         self.hmode = FH_H_FP64 if (args.mode == "fp64" or kind == "caputo1d") else FH_H_DF64
         self.solver = HSolverBatch(ctx, params, S + 1, self.hmode)
+        self.gammas = None
+        if kind == "psi_batch" and args.gamma_min < 1.0:
+            # space-fractional derivative in z: seeded orders, nodes capped at 2048
+            rng = np.random.default_rng(17 + rank)
+            self.gammas = rng.uniform(args.gamma_min, 1.0, size=len(params))
+            self.solver.set_space_order(self.gammas)
+            self.name += f"_gamma{args.gamma_min:g}"
         self.tuned = self.solver.autotune() if kind == "psi_batch" else None
         self.params, self.U0s = params, U0s
         flat = np.concatenate(U0s)
@@ -386,8 +395,9 @@ class H1D(Workload):
         from oracle import oracle as O
         sample = self.params[:1] if len(self.params) == 1 else self.params[:4]
         t0 = time.perf_counter()
-        for p, u in zip(sample, self.U0s):
-            O.h_solve(p, u, self.S)
+        gam = self.gammas if self.gammas is not None else [1.0] * len(sample)
+        for p, u, gm in zip(sample, self.U0s, gam):
+            O.h_solve(dict(p, gamma=float(gm)), u, self.S)
         dt = time.perf_counter() - t0
         pts = sum(p["N"] - 1 for p in sample)
         return {"value": pts * self.S / dt, "unit": METRIC, "cores": 1, "kind": "port",

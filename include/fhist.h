@@ -190,6 +190,15 @@ int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host);
 int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_host);
 /* H_solver::calc_step repeated nsteps times (tstep starts at 1). */
 int fh_h_batch_step(fh_h_batch *b, int nsteps);
+/* Space-fractional Caputo derivative in z, H_solver with gamma < 1 (the
+ * calc_v term of Om1, mt_minimal.cpp:228-271,879-905 and
+ * mt_psi_caputo.cpp:749-777,1293-1313, with Dg and the kb(gamma, i-1, i, i)
+ * factor of A_, B, R, mt_psi_caputo.cpp:1164-1181, mt_minimal.cpp:744-749):
+ * gamma_host[i] in (0, 1] per instance, 1 = classical second derivative (the
+ * default).  Instances with gamma < 1 need N <= 2048.  Only before the first
+ * step.  The nonlocal sum costs O(N^2) FP64 FMAs per instance and step, as in
+ * the reference. */
+int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host);
 int fh_h_batch_tstep(const fh_h_batch *b);
 /* History storage, before the first step: FH_H_FP64 (default) or FH_H_DF64
  * ((hi, lo) FP32 pairs summed in double-float on the FP32 pipe, 2^-48

@@ -140,6 +140,8 @@ class H_solver_batch {
     ctx_.check(fh_h_batch_step(b_, n));
     tstep = fh_h_batch_tstep(b_);
   }
+  // space-derivative order per instance (gamma < 1: fractional in z), before the first step
+  void set_space_order(const std::vector<double> &gamma) { ctx_.check(fh_h_batch_set_space_order(b_, gamma.data())); }
   void get() { ctx_.check(fh_h_batch_get_u_host(b_, U.data())); }
 
  private:

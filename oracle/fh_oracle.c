@@ -161,10 +161,43 @@ void fho_thomas(int N, const double *A, const double *R, const double *B, const 
 
 /* ------------------------------------------------------- 1D H_solver path */
 
+/* The space-fractional part of H_solver::Om1 (gamma < 1): V_i = calc_v of the
+ * first differences F_j = U_{j+1} - U_j, j = 0..i-1 (mt_minimal.cpp:228-271,
+ * mt_psi_caputo.cpp:749-777 with with_zero = 1): mt_minimal weighs F_j by
+ * (i-j+1)^A - (i-j)^A, mt_psi_caputo by A kb_space[i][j-1] (j >= 1) or
+ * A kb_space[i+1][0] (j = 0), kb_space[a][t0] = calc_int(gamma, t0, t0+1, a,
+ * dL, 0) (1461-1472; psi = x in space), A = 1 - gamma.  V_0 = 0. */
+static void h_space_v(const fho_h_params *p, int N, double dL, const double *U, double *F, double *V) {
+  const double A = 1.0 - p->gamma;
+  for (int i = 1; i < N; ++i) F[i] = U[i + 1] - U[i];
+  F[0] = U[1] - U[0];
+  V[0] = 0.0;
+  for (int i = 1; i < N; ++i) {
+    double v = 0.0;
+    for (int j = 0; j <= i - 1; ++j) {
+      double kv;
+      if (p->weights == FHO_W_L1)
+        kv = pow((double)i - (double)j + 1, A) - pow((double)i - (double)j, A);
+      else if (j != 0)
+        kv = A * fho_psi_int(j - 1, j, i, dL, p->gamma, 1.0);
+      else
+        kv = A * fho_psi_int(0, 1, i + 1, dL, p->gamma, 1.0);
+      v += kv * F[j];
+    }
+    V[i] = v;
+  }
+}
+
 int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
+  if (!(p->gamma > 0.0 && p->gamma <= 1.0)) return 2; /* gamma in (0, 1] */
   const int N = p->N, ld = N + 2;
   const double dL = p->L / N;
-  const double Dg = pow(dL, -2.0); /* pow(dL,-1-gamma)/Gamma(2-gamma), gamma = 1 */
+  const int frac = p->gamma != 1.0;
+  /* reset_D: mt_minimal.cpp:744-749 Dg = dL^(-1-gamma)/Gamma(2-gamma);
+   * mt_psi_caputo.cpp:1176-1181 Dg = dL^-2/Gamma(2-gamma) with the factor
+   * kb(gamma, i-1, i, i) (1-gamma) in A_, B, R (1164-1175) */
+  const double Dg = !frac ? pow(dL, -2.0)
+                          : (p->weights == FHO_W_L1 ? pow(dL, -1.0 - p->gamma) : pow(dL, -2.0)) / tgamma(2.0 - p->gamma);
   const double a = p->alpha;
   /* reset_D: mt_minimal.cpp:744-749 (tau^-a) / mt_psi_caputo.cpp:1176-1181 (tau^-1) */
   const double Da = (p->weights == FHO_W_L1) ? pow(p->tau, -a) / tgamma(2.0 - a)
@@ -175,7 +208,8 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
   double *Rc = (double *)malloc(sizeof(double) * ld);
   double *Om = (double *)malloc(sizeof(double) * ld);
   double *w = (double *)malloc(sizeof(double) * (size_t)(steps + 2));
-  if (!K || !Ac || !Bc || !Rc || !Om || !w) return 1;
+  double *F = (double *)malloc(sizeof(double) * ld), *V = (double *)malloc(sizeof(double) * ld);
+  if (!K || !Ac || !Bc || !Rc || !Om || !w || !F || !V) return 1;
   int nsaved = 0;
   for (int tstep = 1; tstep <= steps; ++tstep) {
     const int os = nsaved;
@@ -190,11 +224,21 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
       for (int t = 0; t < os - 1; ++t) w[t] = fho_psi_int(t, t + 1, tstep + 1, p->tau, a, p->beta) * (1 - a);
     }
     for (int i = 0; i <= N; ++i) K[i] = (p->kmodel == FHO_K_CONST) ? p->kc : p->kc * exp(p->kgam * U[i]);
+    if (frac) h_space_v(p, N, dL, U, F, V);
     for (int i = 1; i < N; ++i) {
+      const double kbf = (frac && p->weights == FHO_W_PSI) ? fho_psi_int(i - 1, i, i, dL, p->gamma, 1.0) : 1.0;
+      const double g1 = frac ? 1.0 - p->gamma : 1.0;
       Ac[i] = Dg * K[i - 1] * p->cinv;
       Bc[i] = Dg * K[i + 1] * p->cinv;
-      Rc[i] = p->cinv * (K[i + 1] + K[i - 1]) * Dg + Da * wc;
+      Rc[i] = p->cinv * (K[i + 1] + K[i - 1]) * Dg;
+      if (frac && p->weights == FHO_W_PSI) {
+        Ac[i] = Ac[i] * kbf * g1;
+        Bc[i] = Bc[i] * kbf * g1;
+        Rc[i] = Rc[i] * kbf * g1;
+      }
+      Rc[i] += Da * wc;
       Om[i] = -Da * wc * U[i];
+      if (frac) Om[i] = -Dg * p->cinv * (K[i] * V[i] - K[i - 1] * V[i - 1]) - Da * wc * U[i];
       if (p->gravity) Om[i] += (K[i] - K[i - 1]) / dL; /* (KK(p)-KK(p-1))/dL, mt_minimal.cpp:904 */
       double ts = 0.0;
       if (os >= 2) {
@@ -217,7 +261,7 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
     memcpy(hist + (size_t)os * ld, U, sizeof(double) * ld);
     nsaved++;
   }
-  free(K); free(Ac); free(Bc); free(Rc); free(Om); free(w);
+  free(K); free(Ac); free(Bc); free(Rc); free(Om); free(w); free(F); free(V);
   return 0;
 }
 

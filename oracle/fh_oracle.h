@@ -72,6 +72,7 @@ typedef struct {
   int gravity;    /* add (K(i)-K(i-1))/dL to the right part                       */
   double al_left, bt_left; /* u_0 = al_left*u_1 + bt_left                         */
   double u_right; /* Dirichlet value at node N                                    */
+  double gamma;   /* space-derivative order (1: classical second derivative)      */
 } fho_h_params;
 
 /* Runs `steps` calls of H_solver::calc_step (tstep starting at 1) on U (N+2 values,

@@ -7,7 +7,8 @@
 // inv_dw_dh = 20, k_form 0 (KK = k), rp_form 0, no irrigation, bottom_cond 1
 // (Dirichlet Hbottom), flags 4 (day/night coefficient 1).
 //
-// argv: BS NB L tau alpha k steps Hbottom [func_in_kernel func_power_t eps]
+// argv: BS NB L tau alpha k steps Hbottom [func_in_kernel func_power_t eps [gamma]]
+// (gamma < 1: the space-fractional Caputo derivative in z, calc_v non-zero)
 // stdin: N+1 initial values U[0..N]
 // stdout: "uc <value>" then "u <N+2 values>" after the last step.
 #ifndef REF_TU
@@ -40,7 +41,8 @@ int main(int argc, char **argv) {
   F = new double[N + 2];
   BVK = new double[BS];
   flags = 4;
-  H_solver s(0, 2, 1, 1, tau_, alpha_, 1.0, NULL, 0, Lz, 0.5, hb);
+  const double gam = argc >= 13 ? atof(argv[12]) : 1.0;
+  H_solver s(0, 2, 1, 1, tau_, alpha_, gam, NULL, 0, Lz, 0.5, hb);
   s.k = kk;
   for (int i = 0; i <= N; ++i)
     if (scanf("%lf", &s.U[i]) != 1) return 3;

@@ -56,7 +56,7 @@ static int h_case(fhist::Context &ctx, int weights, double beta, const char *nam
   s.set_state();
   for (int t = 0; t < steps; ++t) s.calc_step();
   s.get();
-  fho_h_params q = {N, 1.0, 1e-3, 0.8, weights, beta, FHO_K_CONST, 1.0, 0.0, 1.0, 0, 0.0, 0.0, 0.0};
+  fho_h_params q = {N, 1.0, 1e-3, 0.8, weights, beta, FHO_K_CONST, 1.0, 0.0, 1.0, 0, 0.0, 0.0, 0.0, 1.0};
   std::vector<double> hist(size_t(steps) * (N + 2));
   if (fho_h_solve(&q, ref.data(), steps, hist.data())) return 1;
   return report(name, relmax(s.U, ref), 1e-12);

@@ -67,6 +67,10 @@ def main():
     # 1D H_solver, psi = t^0.7 (func_in_kernel 3) with the series converged (eps 1e-15)
     h_solver_case("h_psi", "h_psi_t07.json", 5, 2, 3.0, 600.0, 0.75, 1e-4, 24, -20.0, (3, 0.7, 1e-15))
     h_solver_case("h_psi", "h_psi_t15.json", 5, 2, 3.0, 600.0, 0.6, 1e-4, 24, -20.0, (3, 1.5, 1e-15))
+    # space-fractional derivative in z (gamma < 1, calc_v non-zero)
+    h_solver_case("h_minimal", "h_minimal_space.json", 10, 2, 3.0, 600.0, 0.8, 1e-4, 40, -20.0, (0, 1.0, 1e-15, 0.7))
+    h_solver_case("h_psi", "h_psi_space.json", 10, 2, 3.0, 600.0, 0.8, 1e-4, 40, -20.0, (0, 1.0, 1e-15, 0.75))
+    h_solver_case("h_psi", "h_psi_t07_space.json", 5, 2, 3.0, 600.0, 0.75, 1e-4, 24, -20.0, (3, 0.7, 1e-15, 0.6))
     # psi-Caputo weights from the reference series (calc_int, mt_psi_caputo.cpp:720-741)
     wres = {}
     for (alpha, beta) in [(0.7, 0.6), (0.6, 1.5), (0.9, 2.0), (0.55, 0.8)]:

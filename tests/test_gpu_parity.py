@@ -221,6 +221,64 @@ def test_h_solver_reference_golden(ctx, name, weights, beta):
     assert np.array_equal(u[0], u[1])
 
 
+@pytest.mark.parametrize("name,weights,beta", [("h_minimal_space.json", 0, 1.0), ("h_psi_space.json", 1, 1.0),
+                                               ("h_psi_t07_space.json", 1, 0.7)])
+def test_h_solver_space_fractional_reference_golden(ctx, name, weights, beta):
+    """gamma < 1 (the calc_v term) against the reference runs; the second
+    instance of the batch stays classical (gamma = 1)."""
+    from theses_code_gb300.solvers import HSolverBatch
+    g = json.load(open(os.path.join(G, name)))
+    N = g["N"]
+    p = dict(N=N, L=g["L"], tau=g["tau"], alpha=g["alpha"], weights=weights, beta=beta, kmodel=0,
+             kc=g["k"], kgam=0.0, cinv=20.0, gravity=1, al_left=1.0, bt_left=-g["uc"], u_right=g["Hbottom"])
+    U0 = np.zeros(N + 2)
+    U0[:N + 1] = g["U0"]
+    s = HSolverBatch(ctx, [p, p], g["steps"] + 1)
+    s.set_space_order([g["extra"][3], 1.0])
+    s.set_u([U0, U0])
+    s.calc_step(g["steps"])
+    u = s.get_u()
+    assert relmax(u[0], g["U"]) <= TOL_SOLVER
+    ref1, _ = O.h_solve(p, U0, g["steps"])
+    assert relmax(u[1], ref1) <= TOL_SOLVER
+
+
+@pytest.mark.parametrize("mode", [0, 1])  # FH_H_FP64, FH_H_DF64
+def test_h_solver_space_fractional_batch_vs_oracle(ctx, mode):
+    """Ragged psi batch (D(u) = D0 exp(gamma u)) with mixed space orders."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=6, seed=3, Nmin=17, Nmax=300, tau=2e-3)
+    gam = [0.55, 1.0, 0.8, 0.95, 1.0, 0.65]
+    steps = 60
+    s = HSolverBatch(ctx, params, steps + 1, mode)
+    s.set_space_order(gam)
+    s.set_u(U0s)
+    s.calc_step(steps)
+    for p, U0, gm, got in zip(params, U0s, gam, s.get_u()):
+        ref, _ = O.h_solve(dict(p, gamma=gm), U0, steps)
+        assert relmax(got, ref) <= 1e-11, (p["alpha"], p["beta"], gm)
+
+
+def test_h_solver_space_order_limits(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FhError
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=2, seed=3, Nmin=17, Nmax=40, tau=2e-3)
+    s = HSolverBatch(ctx, params, 5)
+    for bad in ([0.0, 1.0], [1.2, 1.0], [float("nan"), 1.0]):
+        with pytest.raises(FhError):
+            s.set_space_order(bad)
+    big = dict(params[0], N=3000)
+    with pytest.raises(FhError):
+        HSolverBatch(ctx, [big], 5).set_space_order([0.7])
+    s.set_space_order([0.7, 1.0])
+    s.set_u(U0s)
+    s.calc_step(1)
+    with pytest.raises(FhError):  # only before the first step
+        s.set_space_order([1.0, 1.0])
+
+
 def test_h_solver_caputo_1d_vs_oracle(ctx):
     from theses_code_gb300 import workloads
     from theses_code_gb300.solvers import HSolverBatch

@@ -24,6 +24,26 @@ def relmax(a, b):
 
 
 @pytest.mark.parametrize("name,weights,beta", [
+    ("h_minimal_space.json", O.W_L1, 1.0),   # gamma 0.7: space-fractional derivative in z
+    ("h_psi_space.json", O.W_PSI, 1.0),      # gamma 0.75
+    ("h_psi_t07_space.json", O.W_PSI, 0.7),  # gamma 0.6, psi = t^0.7
+])
+def test_h_solver_space_fractional_matches_reference(name, weights, beta):
+    g = load(name)
+    N = g["N"]
+    p = dict(N=N, L=g["L"], tau=g["tau"], alpha=g["alpha"], weights=weights, beta=beta,
+             kmodel=O.K_CONST, kc=g["k"], kgam=0.0, cinv=20.0, gravity=1, al_left=1.0,
+             bt_left=-g["uc"], u_right=g["Hbottom"], gamma=g["extra"][3])
+    U0 = np.zeros(N + 2)
+    U0[:N + 1] = g["U0"]
+    U, _ = O.h_solve(p, U0, g["steps"])
+    assert relmax(U, g["U"]) <= 1e-13
+    # the nonlocal term matters: the classical run is far from the reference's
+    U1, _ = O.h_solve(dict(p, gamma=1.0), U0, g["steps"])
+    assert relmax(U1, g["U"]) > 1e-4
+
+
+@pytest.mark.parametrize("name,weights,beta", [
     ("h_minimal_l1.json", O.W_L1, 1.0),   # mt_minimal.cpp H_solver
     ("h_psi_t.json", O.W_PSI, 1.0),       # mt_psi_caputo.cpp H_solver, psi = t
     ("h_psi_t07.json", O.W_PSI, 0.7),     # psi = t^0.7, reference series at eps 1e-15

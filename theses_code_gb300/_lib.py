@@ -75,6 +75,7 @@ _SIGS = {
     "fh_tg_set_state": (_i, [_vp, _dp, _dp]),
     "fh_tg_step": (_i, [_vp, _i]),
     "fh_tg_set_restricted": (_i, [_vp, C.c_double]),
+    "fh_h_batch_set_space_order": (_i, [_vp, _dp]),
     "fh_tg_set_series": (_i, [_vp, _i]),
     "fh_tg_get_c_host": (_i, [_vp, _dp]),
     "fh_tg_field": (_vp, [_vp]),

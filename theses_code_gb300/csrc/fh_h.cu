@@ -24,6 +24,10 @@ struct fh_h_dev_inst {
   int fixed;  // coefficients independent of u and of the step: factor once
   long long off;  // segment start in the concatenated state
   double dL, Dg, Da, tau, alpha, beta, kc, kgam, cinv, al_left, bt_left, u_right;
+  // space-fractional derivative in z (fh_h_batch_set_space_order): order
+  // spg, spA = 1 - spg (0: classical second derivative), kbf = the
+  // mt_psi_caputo factor kb(gamma, i-1, i, i) of A, B, R
+  double spg, spA, kbf;
 };
 
 struct fh_h_tile {
@@ -47,6 +51,12 @@ struct fh_h_batch {
   fh_graph_cache graph;
   bool use_graph = true;
   int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
+  std::vector<fh_h_dev_inst> di;  // host copy of inst
+  // space-fractional instances: Toeplitz weights wsp and the sums sV per
+  // node (state layout), shared memory of k_h_space_v
+  bool space = false;
+  size_t space_smem = 0;
+  fh_dbuf wsp, sV;
   // weights of the next step on hs (h_one_step): two buffer pairs of W and
   // wc, selected by the parity of the step; w_ready = step whose weights
   // are pending on hs behind ev_w
@@ -65,6 +75,7 @@ struct fh_h_batch {
 static constexpr int kTileThreads = 512;  // largest tile CTA (1024 nodes)
 static constexpr int kTileShapes[3] = {128, 256, 512};  // candidate tile CTAs
 static inline int tile_shape_index(int threads) { return threads == 128 ? 0 : threads == 256 ? 1 : 2; }
+static constexpr int kSpaceMaxN = 2048;  // nodes of a space-fractional instance (shared-memory sums)
 static constexpr int kHWeightThreads = 128;                 // nodes per weights CTA
 static constexpr int kHWeightSlots = kHWeightThreads - 1;  // slots per weights CTA
 // per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | 2^(-1/beta)
@@ -270,6 +281,53 @@ __global__ void __launch_bounds__(kTileThreads) k_hist_tiles_df(const fh_h_tile 
   *reinterpret_cast<double2 *>(part + (long long)s * ldpart + p) = o;
 }
 
+// Space-fractional Caputo derivative in z (gamma < 1): H_solver::Om1 adds
+// -Dg/(dw/dh) (K_i V_i - K_{i-1} V_{i-1}) with V_i = sum_{j<i} w_{i-j} F_j over
+// the first differences F_j = u_{j+1} - u_j of the current state
+// (calc_v, mt_minimal.cpp:228-271, mt_psi_caputo.cpp:749-777, with_zero 1).
+// The weights depend on i - j only: mt_minimal (m+1)^A - m^A, mt_psi_caputo
+// A kb_space of one interval at distance m+1 (1461-1472; psi = x in space;
+// the reference tabulates kb_space[i][j-1], equal up to rounding).
+// wsp[off + m], m = 1..N-1, per instance.
+__global__ void k_h_spw(const fh_h_dev_inst *__restrict__ inst, double *__restrict__ wsp) {
+  const fh_h_dev_inst I = inst[blockIdx.y];
+  if (I.spA == 0.0) return;
+  for (int m = 1 + blockIdx.x * blockDim.x + threadIdx.x; m < I.N; m += gridDim.x * blockDim.x)
+    wsp[I.off + m] = I.weights == FH_W_L1
+                         ? pow((double)m + 1, I.spA) - pow((double)m, I.spA)
+                         : I.spA * fh_psi_int(0.0, 1.0, (double)m + 1.0, I.dL, I.spg, 1.0);
+}
+
+// V_i of one instance per CTA (F and the weights in shared memory), i =
+// 1..N-1; V_0 = 0.  O(N^2) FP64 FMAs per instance and step, as the reference
+// (FP64-pipe-bound; a double-float form on the FP32 pipe ran 3.4x faster but
+// the flux difference K_i V_i - K_{i-1} V_{i-1} amplified its 2^-48 products
+// to 1e-10 of the solution at N ~ 1000).  Rows go to threads in snake order
+// (t, 2T-1-t, 2T+t, ...) so that every thread sums about as many terms.
+__global__ void __launch_bounds__(256) k_h_space_v(const fh_h_dev_inst *__restrict__ inst, const double *__restrict__ U,
+                                                   const double *__restrict__ wsp, double *__restrict__ V) {
+  extern __shared__ double spm[];
+  const fh_h_dev_inst I = inst[blockIdx.x];
+  if (I.spA == 0.0) return;
+  const int N = I.N;
+  const double *u = U + I.off;
+  double *F = spm, *w = spm + N;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    F[j] = u[j + 1] - u[j];
+    w[j] = wsp[I.off + j];
+  }
+  __syncthreads();
+  const int T = blockDim.x;
+  for (int r = 0; r * T < N - 1; ++r) {
+    const int i = 1 + r * T + ((r & 1) ? T - 1 - (int)threadIdx.x : (int)threadIdx.x);
+    if (i >= N) continue;
+    double v = 0.0;
+    for (int j = 0; j < i; ++j) v = fma(w[i - j], F[j], v);
+    V[I.off + i] = v;
+  }
+  if (threadIdx.x == 0) V[I.off] = 0.0;
+}
+
 __device__ __forceinline__ double fh_h_K(const fh_h_dev_inst &I, double u) {
   return I.kmodel == FH_K_CONST ? I.kc : I.kc * exp(I.kgam * u);
 }
@@ -298,7 +356,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
                                                      double *__restrict__ sA, double *__restrict__ sB,
                                                      double *__restrict__ sR, double *__restrict__ sOm,
                                                      double *__restrict__ Dnew, int append, int first,
-                                                     int dfstore) {
+                                                     int dfstore, const double *__restrict__ sV) {
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (b >= n) return;  // whole warp
@@ -316,10 +374,19 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     double Km = fh_h_K(I, u[f0 - 1]), Kc = fh_h_K(I, u[f0]);
     for (int i = f0; i < f1; ++i) {
       const double Kp = fh_h_K(I, u[i + 1]);
-      const double A = I.Dg * Km * I.cinv;
-      const double B = I.Dg * Kp * I.cinv;
-      const double R = I.cinv * (Kp + Km) * I.Dg + DaW;
+      double A = I.Dg * Km * I.cinv;
+      double B = I.Dg * Kp * I.cinv;
+      double R = I.cinv * (Kp + Km) * I.Dg;
       double om = -DaW * u[i];
+      if (I.spA != 0.0) {  // space-fractional derivative (k_h_space_v)
+        if (I.weights == FH_W_PSI) {
+          A = A * I.kbf * I.spA;
+          B = B * I.kbf * I.spA;
+          R = R * I.kbf * I.spA;
+        }
+        om = -I.Dg * I.cinv * (Kc * sV[o + i] - Km * sV[o + i - 1]) - DaW * u[i];
+      }
+      R += DaW;
       if (I.gravity) om += (Kc - Km) * idL;
       double ts = 0.0;
       for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + o + i];
@@ -493,13 +560,18 @@ static int h_one_step(fh_h_batch *B, bool next) {
       splits = 1;
     }
   }
+  fh_prof_mark(ctx, FH_PROF_SWEEP, false);  // right parts (incl. the space-fractional sums) and line solves
+  if (B->space) {
+    k_h_space_v<<<(unsigned)B->n, 256, B->space_smem, ctx->stream>>>(B->inst.as<fh_h_dev_inst>(), B->U.as<double>(),
+                                                                   B->wsp.as<double>(), B->sV.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_h_space_v"))) return rc;
+  }
   const int append = os >= 1;
   double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
-  fh_prof_mark(ctx, FH_PROF_SWEEP, false);
   k_h_line_warp<<<(unsigned)fh_ceil_div(B->n, 4), 128, 0, ctx->stream>>>(
       B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wcp(par), B->part.as<double>(), B->Ptot,
       splits, B->Al.as<double>(), B->Bt.as<double>(), B->sA.as<double>(), B->sB.as<double>(), B->sR.as<double>(),
-      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0, B->mode == FH_H_DF64 ? 1 : 0);
+      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0, B->mode == FH_H_DF64 ? 1 : 0, B->sV.as<double>());
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_h_line_warp"))) return rc;
   B->nsaved++;
@@ -549,6 +621,9 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     I.al_left = p.al_left;
     I.bt_left = p.bt_left;
     I.u_right = p.u_right;
+    I.spg = 1.0;
+    I.spA = 0.0;
+    I.kbf = 1.0;
     B->off.push_back(off);
     const int seg = ((p.N + 2) + 1) & ~1;
     for (int k = 0; k < 3; ++k) {
@@ -596,6 +671,7 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     const double h = (double)l;
     lg[x] = make_double2(h, (double)(l - (long double)h));
   }
+  B->di = di;
   cudaError_t e1 = cudaMemcpyAsync(B->inst.p, di.data(), sizeof(fh_h_dev_inst) * ninst, cudaMemcpyHostToDevice, ctx->stream);
   if (e1 == cudaSuccess)
     e1 = cudaMemcpyAsync(B->lgt.p, lg.data(), sizeof(double2) * lg.size(), cudaMemcpyHostToDevice, ctx->stream);
@@ -732,6 +808,58 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
 }
 
 int fh_h_batch_tstep(const fh_h_batch *b) { return b ? b->tstep : -1; }
+
+int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, gamma_host, FH_EINVAL, "fh_h_batch_set_space_order: null pointer");
+  FH_REQUIRE(ctx, b->nsaved == 0, FH_EINVAL, "fh_h_batch_set_space_order: only before the first step");
+  int maxN = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const double g = gamma_host[i];
+    FH_REQUIRE(ctx, g > 0.0 && g <= 1.0, FH_EINVAL, "fh_h_batch_set_space_order: gamma[%d] = %g not in (0, 1]", i, g);
+    FH_REQUIRE(ctx, g == 1.0 || b->hp[i].N <= kSpaceMaxN, FH_EINVAL,
+               "fh_h_batch_set_space_order: instance %d: N = %d > %d with gamma < 1", i, b->hp[i].N, kSpaceMaxN);
+    if (g != 1.0 && b->hp[i].N > maxN) maxN = b->hp[i].N;
+  }
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < b->n; ++i) {
+    fh_h_dev_inst &I = b->di[i];
+    const double g = gamma_host[i];
+    I.spg = g;
+    I.spA = g == 1.0 ? 0.0 : 1.0 - g;
+    if (g == 1.0) {
+      I.Dg = pow(I.dL, -2.0);
+      I.kbf = 1.0;
+    } else {
+      // reset_D: mt_minimal.cpp:744-749 dL^(-1-gamma)/Gamma(2-gamma),
+      // mt_psi_caputo.cpp:1176-1181 dL^-2/Gamma(2-gamma)
+      I.Dg = (I.weights == FH_W_L1 ? pow(I.dL, -1.0 - g) : pow(I.dL, -2.0)) / tgamma(2.0 - g);
+      // kb(gamma, i-1, i, i, dL) of one interval at distance 1 (psi = x)
+      const double gtj = I.dL, v = (gtj / gtj) * pow(gtj, 1.0 - g);
+      const double v4 = pow(fabs(1.0 - 0.0 / gtj), 1.0 - g), v3 = pow(fabs(1.0 - gtj / gtj), 1.0 - g);
+      I.kbf = (-(v3 - v4) / (1.0 - g)) * v;
+    }
+  }
+  b->space = maxN > 0;
+  b->space_smem = sizeof(double) * 2 * (size_t)maxN;
+  b->wsp.release();
+  b->sV.release();
+  int rc;
+  if (b->space && ((rc = fh_alloc(ctx, b->wsp, sizeof(double) * (size_t)b->Ptot)) ||
+                   (rc = fh_alloc(ctx, b->sV, sizeof(double) * (size_t)b->Ptot))))
+    return rc;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(b->inst.p, b->di.data(), sizeof(fh_h_dev_inst) * b->n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  if (b->space) {
+    k_h_spw<<<dim3((unsigned)fh_ceil_div(maxN, 128), (unsigned)b->n), 128, 0, ctx->stream>>>(
+        b->inst.as<fh_h_dev_inst>(), b->wsp.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_h_spw"))) return rc;
+  }
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  b->graph.reset();
+  return FH_OK;
+}
 
 // Times the batch history sum for every candidate launch shape (tile CTA of
 // 128/256/512 threads, K split cap 1/8/64) at a probe depth of

@@ -57,6 +57,13 @@ class HSolverBatch:
         check(self.ctx.L.fh_h_batch_launch_shape(self.h, C.byref(t), C.byref(c)), self.ctx.h)
         return {"tile_threads": t.value, "split_cap": c.value, "ms_per_launch": ms.value}
 
+    def set_space_order(self, gamma):
+        """Space-derivative order per instance (the reference's gamma; < 1 adds the
+        space-fractional Caputo term in z), before the first step."""
+        g = np.ascontiguousarray(np.asarray(gamma, dtype=np.float64).reshape(-1))
+        assert g.size == len(self.params)
+        check(self.ctx.L.fh_h_batch_set_space_order(self.h, _hptr(g)), self.ctx.h)
+
     def set_u(self, U: np.ndarray | list):
         flat = np.ascontiguousarray(np.concatenate([np.asarray(u, dtype=np.float64) for u in U])
                                     if isinstance(U, list) else U, dtype=np.float64)
