@@ -329,6 +329,27 @@ def test_h_solver_psi_long_run_vs_oracle(ctx):
         assert relmax(gb, ga) <= 1e-14
 
 
+def test_h_solver_warp_and_cta_line_paths(ctx):
+    """Batches of 152 instances or more solve one instance per warp, smaller
+    ones one instance per CTA: both match the oracle, and each other."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = workloads.psi_batch(n=160, seed=11, Nmin=17, Nmax=60, tau=2e-3)
+    steps = 40
+    big = HSolverBatch(ctx, params, steps + 1)   # warp per instance
+    big.set_u(U0s)
+    big.calc_step(steps)
+    small = HSolverBatch(ctx, params[:8], steps + 1)  # CTA per instance
+    small.set_u(U0s[:8])
+    small.calc_step(steps)
+    gb, gs = big.get_u(), small.get_u()
+    for k in (0, 3, 7, 159):
+        ref, _ = O.h_solve(params[k], U0s[k], steps)
+        assert relmax(gb[k], ref) <= 1e-11, k
+    for k in range(8):
+        assert relmax(gs[k], gb[k]) <= 1e-13, k
+
+
 def test_h_solver_df64_history_vs_oracle(ctx):
     """History stored as (hi, lo) FP32 pairs and summed in double-float: the
     plain-path bounds still hold (1e-12 for L1, 1e-11 for the psi batch)."""

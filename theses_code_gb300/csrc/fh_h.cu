@@ -75,6 +75,7 @@ struct fh_h_batch {
 static constexpr int kTileThreads = 512;  // largest tile CTA (1024 nodes)
 static constexpr int kTileShapes[3] = {128, 256, 512};  // candidate tile CTAs
 static inline int tile_shape_index(int threads) { return threads == 128 ? 0 : threads == 256 ? 1 : 2; }
+static constexpr int kLineCtaMaxInst = 152;  // batches below this many instances solve one CTA per instance
 static constexpr int kSpaceMaxN = 2048;  // nodes of a space-fractional instance (shared-memory sums)
 static constexpr int kHWeightThreads = 128;                 // nodes per weights CTA
 static constexpr int kHWeightSlots = kHWeightThreads - 1;  // slots per weights CTA
@@ -349,25 +350,43 @@ __device__ __forceinline__ void fh_h_store_diff(double *D, long long i, double d
 // after which every lane re-walks its chunk from the scanned start value with
 // one reciprocal per equation (Al[i+1] = B_i g, g = 1 / (R_i - A_i Al[i])).  The coefficients are kept in the scratch
 // arrays sA, sB, sR (reused for Al[i+1]/B_i) and sOm at the equation's node.
-__global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__restrict__ inst, int n,
-                                                     double *__restrict__ U, const double *__restrict__ wc,
-                                                     const double *__restrict__ part, long long ldpart, int splits,
-                                                     double *__restrict__ Al, double *__restrict__ Bt,
-                                                     double *__restrict__ sA, double *__restrict__ sB,
-                                                     double *__restrict__ sR, double *__restrict__ sOm,
-                                                     double *__restrict__ Dnew, int append, int first,
-                                                     int dfstore, const double *__restrict__ sV) {
-  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (b >= n) return;  // whole warp
-  const fh_h_dev_inst I = inst[b];
+// Scans and syncs of one instance's group of threads: one warp (NW = 1) or
+// the whole CTA (NW warps, named barrier 1).
+template <int NW>
+struct HGroup {
+  static __device__ __forceinline__ fh_mob mob(fh_mob f, fh_mob *sm) { return fh_group_exclusive_mob<NW>(f, sm, 1); }
+  static __device__ __forceinline__ fh_aff aff(fh_aff f, fh_aff *sm) { return fh_group_exclusive_affine<NW>(f, sm, 1); }
+  static __device__ __forceinline__ fh_aff aff_rev(fh_aff f, fh_aff *sm) {
+    return fh_group_exclusive_affine_rev<NW>(f, sm, 1);
+  }
+  static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+template <>
+struct HGroup<1> {
+  static __device__ __forceinline__ fh_mob mob(fh_mob f, fh_mob *) { return fh_warp_exclusive_mob(f); }
+  static __device__ __forceinline__ fh_aff aff(fh_aff f, fh_aff *) { return fh_warp_exclusive_affine(f); }
+  static __device__ __forceinline__ fh_aff aff_rev(fh_aff f, fh_aff *) { return fh_warp_exclusive_affine_rev(f); }
+  static __device__ __forceinline__ void sync() { __syncwarp(); }
+};
+
+// One instance by a group of 32 NW threads; `lane` is the thread's index in
+// the group (its chunk of consecutive equations).
+template <int NW, bool SPACE>
+__device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, double *__restrict__ U,
+                                       const double *__restrict__ wc, const double *__restrict__ part,
+                                       long long ldpart, int splits, double *__restrict__ Al,
+                                       double *__restrict__ Bt, double *__restrict__ sA, double *__restrict__ sB,
+                                       double *__restrict__ sR, double *__restrict__ sOm, double *__restrict__ Dnew,
+                                       int append, int first, int dfstore, const double *__restrict__ sV,
+                                       fh_mob *smm, fh_aff *sma) {
+  constexpr int TG = 32 * NW;
   const long long o = I.off;
   double *u = U + o;
   const int N = I.N;
   const double DaW = I.Da * wc[b];
   const double idL = 1.0 / I.dL;
   // ---- pass 1: coefficients of equations i in [f0, f1), chunk Moebius map
-  const int chf = (N - 1 + 31) / 32;
+  const int chf = (N - 1 + TG - 1) / TG;
   const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
   fh_mob T{1.0, 0.0, 0.0, 1.0};
   if (f0 < f1) {
@@ -378,7 +397,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
       double B = I.Dg * Kp * I.cinv;
       double R = I.cinv * (Kp + Km) * I.Dg;
       double om = -DaW * u[i];
-      if (I.spA != 0.0) {  // space-fractional derivative (k_h_space_v)
+      if (SPACE && I.spA != 0.0) {  // space-fractional derivative (k_h_space_v)
         if (I.weights == FH_W_PSI) {
           A = A * I.kbf * I.spA;
           B = B * I.kbf * I.spA;
@@ -410,7 +429,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     // constant coefficients: Al[i+1] and Al[i+1]/B_i are computed once,
     // serially in the reference order, and kept (Al, sR) for later steps
     if (first) {
-      __syncwarp();
+      HGroup<NW>::sync();
       if (lane == 0) {
         double a = I.al_left;
         Al[o + 1] = a;
@@ -421,7 +440,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
           sR[o + i] = a / B;
         }
       }
-      __syncwarp();
+      HGroup<NW>::sync();
     }
     for (int i = f0; i < f1; ++i) {
       const double gq = sR[o + i];
@@ -429,7 +448,7 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     }
   } else {
     // ---- Al: Moebius scan, re-walk with the reference arithmetic, chunk affine map of Bt
-    const fh_mob PT = fh_warp_exclusive_mob(T);
+    const fh_mob PT = HGroup<NW>::mob(T, smm);
     double alv = (lane == 0) ? I.al_left : fma(PT.m00, I.al_left, PT.m01) / fma(PT.m10, I.al_left, PT.m11);
     for (int i = f0; i < f1; ++i) {
       const double A = sA[o + i], B = sB[o + i], R = sR[o + i], om = sOm[o + i];
@@ -443,21 +462,21 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
     if (lane == 0) Al[o + 1] = I.al_left;
   }
   // ---- Bt: scan, re-walk Bt[i+1] = (Al[i+1]/B)(A Bt[i] - Om)
-  const fh_aff PF = fh_warp_exclusive_affine(F);
+  const fh_aff PF = HGroup<NW>::aff(F, sma);
   double btv = (lane == 0) ? I.bt_left : fma(PF.a, I.bt_left, PF.b);
   for (int i = f0; i < f1; ++i) {
     btv = sR[o + i] * (sA[o + i] * btv - sOm[o + i]);
     Bt[o + i + 1] = btv;
   }
   if (lane == 0) Bt[o + 1] = I.bt_left;
-  __syncwarp();
+  HGroup<NW>::sync();
   // ---- back substitution u_i = Al[i+1] u_{i+1} + Bt[i+1], i = N-1..0; u_N = u_right
   const double uN = I.u_right;
-  const int chb = (N + 31) / 32;
+  const int chb = (N + TG - 1) / TG;
   const int b0 = lane * chb, b1 = min(N, b0 + chb);
   fh_aff G{1.0, 0.0};
   for (int i = b1 - 1; i >= b0; --i) G = fh_aff_compose(fh_aff{Al[o + i + 1], Bt[o + i + 1]}, G);
-  const fh_aff PG = fh_warp_exclusive_affine_rev(G);
+  const fh_aff PG = HGroup<NW>::aff_rev(G, sma);
   double un = fma(PG.a, uN, PG.b);  // u at node b1
   // every lane reads the old values of its own nodes before writing them
   for (int i = b1 - 1; i >= b0; --i) {
@@ -475,6 +494,40 @@ __global__ void __launch_bounds__(128) k_h_line_warp(const fh_h_dev_inst *__rest
       fh_h_store_diff(Dnew, o + N + 1, uN - oldG, dfstore);
     }
   }
+}
+
+// SPACE: the batch has space-fractional instances (a separate instantiation
+// keeps the registers of the classical path).
+// Seven resident CTAs per SM (registers <= 73) keep 4096 instances (1024
+// CTAs) in one wave on 152 SMs.
+template <bool SPACE>
+__global__ void __launch_bounds__(128, 7) k_h_line_warp(const fh_h_dev_inst *__restrict__ inst, int n,
+                                                     double *__restrict__ U, const double *__restrict__ wc,
+                                                     const double *__restrict__ part, long long ldpart, int splits,
+                                                     double *__restrict__ Al, double *__restrict__ Bt,
+                                                     double *__restrict__ sA, double *__restrict__ sB,
+                                                     double *__restrict__ sR, double *__restrict__ sOm,
+                                                     double *__restrict__ Dnew, int append, int first,
+                                                     int dfstore, const double *__restrict__ sV) {
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (b >= n) return;  // whole warp
+  h_line<1, SPACE>(inst[b], b, threadIdx.x & 31, U, wc, part, ldpart, splits, Al, Bt, sA, sB, sR, sOm, Dnew, append,
+                   first, dfstore, sV, nullptr, nullptr);
+}
+
+// Small batches (fewer instances than SMs): one CTA of kLineCtaWarps warps per
+// instance, so that each thread walks ~N/256 equations instead of ~N/32.
+static constexpr int kLineCtaWarps = 8;
+template <bool SPACE>
+__global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
+    const fh_h_dev_inst *__restrict__ inst, double *__restrict__ U, const double *__restrict__ wc,
+    const double *__restrict__ part, long long ldpart, int splits, double *__restrict__ Al, double *__restrict__ Bt,
+    double *__restrict__ sA, double *__restrict__ sB, double *__restrict__ sR, double *__restrict__ sOm,
+    double *__restrict__ Dnew, int append, int first, int dfstore, const double *__restrict__ sV) {
+  __shared__ fh_mob smm[kLineCtaWarps];
+  __shared__ fh_aff sma[kLineCtaWarps];
+  h_line<kLineCtaWarps, SPACE>(inst[blockIdx.x], blockIdx.x, threadIdx.x, U, wc, part, ldpart, splits, Al, Bt, sA, sB,
+                               sR, sOm, Dnew, append, first, dfstore, sV, smm, sma);
 }
 
 // ------------------------------------------------------------------- host
@@ -568,10 +621,29 @@ static int h_one_step(fh_h_batch *B, bool next) {
   }
   const int append = os >= 1;
   double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
-  k_h_line_warp<<<(unsigned)fh_ceil_div(B->n, 4), 128, 0, ctx->stream>>>(
-      B->inst.as<fh_h_dev_inst>(), B->n, B->U.as<double>(), B->wcp(par), B->part.as<double>(), B->Ptot,
-      splits, B->Al.as<double>(), B->Bt.as<double>(), B->sA.as<double>(), B->sB.as<double>(), B->sR.as<double>(),
-      B->sOm.as<double>(), Dnew, append, os == 0 ? 1 : 0, B->mode == FH_H_DF64 ? 1 : 0, B->sV.as<double>());
+  {
+    const int fst = os == 0 ? 1 : 0, dfs = B->mode == FH_H_DF64 ? 1 : 0;
+    const dim3 gc((unsigned)B->n), gw((unsigned)fh_ceil_div(B->n, 4));
+    const fh_h_dev_inst *in = B->inst.as<fh_h_dev_inst>();
+    double *Al = B->Al.as<double>(), *Bt = B->Bt.as<double>(), *sA = B->sA.as<double>(), *sB = B->sB.as<double>();
+    double *sR = B->sR.as<double>(), *sOm = B->sOm.as<double>(), *U = B->U.as<double>();
+    const double *part = B->part.as<double>(), *wcp = B->wcp(par), *sV = B->sV.as<double>();
+    if (B->n < kLineCtaMaxInst) {
+      if (B->space)
+        k_h_line_cta<true><<<gc, 32 * kLineCtaWarps, 0, ctx->stream>>>(in, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB,
+                                                                      sR, sOm, Dnew, append, fst, dfs, sV);
+      else
+        k_h_line_cta<false><<<gc, 32 * kLineCtaWarps, 0, ctx->stream>>>(in, U, wcp, part, B->Ptot, splits, Al, Bt, sA,
+                                                                       sB, sR, sOm, Dnew, append, fst, dfs, sV);
+    } else {
+      if (B->space)
+        k_h_line_warp<true><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB, sR, sOm,
+                                                         Dnew, append, fst, dfs, sV);
+      else
+        k_h_line_warp<false><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB, sR,
+                                                          sOm, Dnew, append, fst, dfs, sV);
+    }
+  }
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_h_line_warp"))) return rc;
   B->nsaved++;

@@ -285,6 +285,36 @@ __device__ __forceinline__ fh_aff fh_group_exclusive_affine_rev(fh_aff f, fh_aff
 }
 
 
+// Moebius maps (FP64, rescaled by powers of two): thread t receives
+// f_{t-1} o ... o f_0 (identity for thread 0).
+template <int NW>
+__device__ __forceinline__ fh_mob fh_group_exclusive_mob(fh_mob f, fh_mob *sm, int bar) {
+  const unsigned lane = threadIdx.x & 31u;
+  const int w = threadIdx.x >> 5;
+  fh_mob g = fh_mob_normalise(f);
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    fh_mob p;
+    p.m00 = __shfl_up_sync(0xffffffffu, g.m00, d);
+    p.m01 = __shfl_up_sync(0xffffffffu, g.m01, d);
+    p.m10 = __shfl_up_sync(0xffffffffu, g.m10, d);
+    p.m11 = __shfl_up_sync(0xffffffffu, g.m11, d);
+    if (lane >= (unsigned)d) g = fh_mob_normalise(fh_mob_compose(g, p));
+  }
+  if (lane == 31u) sm[w] = g;
+  fh_mob e;
+  e.m00 = __shfl_up_sync(0xffffffffu, g.m00, 1);
+  e.m01 = __shfl_up_sync(0xffffffffu, g.m01, 1);
+  e.m10 = __shfl_up_sync(0xffffffffu, g.m10, 1);
+  e.m11 = __shfl_up_sync(0xffffffffu, g.m11, 1);
+  if (lane == 0u) e = fh_mob{1.0, 0.0, 0.0, 1.0};
+  fh_group_bar(bar, 32 * NW);
+  fh_mob P{1.0, 0.0, 0.0, 1.0};
+  for (int k = 0; k < w; ++k) P = fh_mob_normalise(fh_mob_compose(sm[k], P));
+  fh_group_bar(bar, 32 * NW);  // sm may be reused after this
+  return fh_mob_normalise(fh_mob_compose(e, P));
+}
+
 // ------------------------------------------------------------------------
 // Double-float group scans: NW warps (threads 0 .. 32 NW - 1 of the CTA) scan
 // one chain of 32 NW chunk maps in double-float; warp totals pass through
