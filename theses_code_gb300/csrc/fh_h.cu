@@ -607,7 +607,10 @@ static int h_one_step(fh_h_batch *B, bool next) {
     rc = h_hist(B, ti, K, splits, kchunk, B->Wp(par), ctx->stream);
     fh_prof_mark(ctx, FH_PROF_HISTORY, true);
     if (rc) return rc;
-    if (splits > 2) {  // fold the partial sums into split 0 (in split order)
+    // fold the partial sums into split 0 (in split order) for the warp-per-
+    // instance lines; the CTA-per-instance lines of small batches read all
+    // splits themselves (one launch less per step)
+    if (splits > 2 && B->n >= kLineCtaMaxInst) {
       if ((rc = fh_launch_reduce_splits(ctx, splits, B->Ptot, B->part.as<double>(), B->Ptot, B->part.as<double>())))
         return rc;
       splits = 1;
