@@ -11,6 +11,7 @@
 // stores layer differences d_t = layer[t+1] - layer[t] at slot t for the
 // concatenated state (layer-major), so the history loads coalesce across
 // neighbouring nodes and instances.
+#include <utility>
 #include <vector>
 
 #include "fh_internal.h"
@@ -898,6 +899,16 @@ int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host) {
     if (g != 1.0 && b->hp[i].N > maxN) maxN = b->hp[i].N;
   }
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // new buffers first: on failure the batch keeps its previous configuration
+  fh_dbuf nw, nv;
+  int rc;
+  if (maxN > 0 && ((rc = fh_alloc(ctx, nw, sizeof(double) * (size_t)b->Ptot)) ||
+                   (rc = fh_alloc(ctx, nv, sizeof(double) * (size_t)b->Ptot))))
+    return rc;
+  std::swap(b->wsp.p, nw.p);
+  std::swap(b->wsp.bytes, nw.bytes);
+  std::swap(b->sV.p, nv.p);
+  std::swap(b->sV.bytes, nv.bytes);
   for (int i = 0; i < b->n; ++i) {
     fh_h_dev_inst &I = b->di[i];
     const double g = gamma_host[i];
@@ -918,12 +929,6 @@ int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host) {
   }
   b->space = maxN > 0;
   b->space_smem = sizeof(double) * 2 * (size_t)maxN;
-  b->wsp.release();
-  b->sV.release();
-  int rc;
-  if (b->space && ((rc = fh_alloc(ctx, b->wsp, sizeof(double) * (size_t)b->Ptot)) ||
-                   (rc = fh_alloc(ctx, b->sV, sizeof(double) * (size_t)b->Ptot))))
-    return rc;
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(b->inst.p, b->di.data(), sizeof(fh_h_dev_inst) * b->n, cudaMemcpyHostToDevice,
                                    ctx->stream));
   if (b->space) {

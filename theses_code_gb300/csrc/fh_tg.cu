@@ -1649,14 +1649,22 @@ int fh_tg_set_series(fh_tg_solver *s, int nterms) {
   const fh_tg_dev &g = s->dv;
   int rc;
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  s->H.release();
-  s->ser_tab.release();
-  s->D.release();
-  s->ser_J = 0;
-  s->graph.reset();
+  // new buffers first: on failure the solver keeps its previous configuration
+  fh_dbuf nD, nH, ntab;
   // the history store: every layer pair, or only the newest for the series
-  if ((rc = fh_alloc(ctx, s->D, sizeof(double) * (size_t)g.P * (nterms ? 1 : (size_t)s->max_steps)))) return rc;
-  if (nterms == 0) return FH_OK;
+  if ((rc = fh_alloc(ctx, nD, sizeof(double) * (size_t)g.P * (nterms ? 1 : (size_t)s->max_steps)))) return rc;
+  auto adopt = [](fh_dbuf &dst, fh_dbuf &src) {
+    std::swap(dst.p, src.p);
+    std::swap(dst.bytes, src.bytes);
+  };
+  s->graph.reset();
+  if (nterms == 0) {
+    adopt(s->D, nD);
+    s->H.release();
+    s->ser_tab.release();
+    s->ser_J = 0;
+    return FH_OK;
+  }
   // coefficient rows of every step j >= 1 (fr_d_t_g_2d.cpp _kb_row2 2965-3040
   // for psi = t, where the inner integral is exact after one term, and
   // _kb_row2_fixed_coefs 3041-3057), in the reference's arithmetic
@@ -1690,10 +1698,13 @@ int fh_tg_set_series(fh_tg_solver *s, int nterms) {
       }
     }
   }
-  if ((rc = fh_alloc(ctx, s->H, sizeof(double) * (size_t)J * (size_t)g.P)) ||
-      (rc = fh_alloc(ctx, s->ser_tab, sizeof(double) * tab.size(), false)))
+  if ((rc = fh_alloc(ctx, nH, sizeof(double) * (size_t)J * (size_t)g.P)) ||
+      (rc = fh_alloc(ctx, ntab, sizeof(double) * tab.size(), false)))
     return rc;
-  FH_CUDA_TRY(ctx, cudaMemcpy(s->ser_tab.p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+  FH_CUDA_TRY(ctx, cudaMemcpy(ntab.p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+  adopt(s->D, nD);
+  adopt(s->H, nH);
+  adopt(s->ser_tab, ntab);
   s->ser_J = J;
   return FH_OK;
 }
