@@ -462,6 +462,23 @@ def test_tg_restricted_vs_oracle(ctx, mode, tol):
     assert relmax(s.get_c(), full) <= tol
 
 
+def test_tg_restricted_blocked_skips_old_groups(ctx):
+    """Blocked mode, 400 steps, cut ~100 layer pairs back: from step 256 on the
+    tensor-core contraction starts at the first 128-layer group with a
+    non-zero weight."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(40, 40, alpha=0.7, tau=5e-4, d=0.1, seed=9, C1=0.2, S=0.01)
+    steps, eps = 400, 1.4e-3
+    s = TGSolver(ctx, p, steps, FH_TG_BLOCKED)
+    s.set_state(V2, C0)
+    s.set_restricted(eps)
+    s.calc_step(steps)
+    ref, _ = O.tg_solve(dict(p, dt_alg=2, dt_eps=eps), V2, C0, steps)
+    assert relmax(s.get_c(), ref) <= 1e-9
+
+
 def test_tg_restricted_psi_beta_vs_oracle(ctx):
     """psi = t^1.3 (weights not Toeplitz: every stored layer pair is visited,
     the cut ones with weight 0)."""

@@ -18,7 +18,7 @@ void fh_blk_delete(fh_blk *b);
 int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
 int fh_blk_toeplitz_weights(fh_ctx *ctx, fh_blk &b, const double *w, int base, int K, int mrows);
-int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo);
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo, int gbeg = 0);
 long long fh_blk_ppad(const fh_blk &b);
 static constexpr int kAbBlock = 128;  // steps per block: one weight row each
 

@@ -85,7 +85,7 @@ __device__ __forceinline__ float fh_exp2i(int e) {
 __global__ void __launch_bounds__(kThreads, 1)
     k_far_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, long long P,
                const int8_t *__restrict__ Ew, const int8_t *__restrict__ Ed, long long Ppad,
-               float2 *__restrict__ out, long long ldo, int splits, float2 *__restrict__ part,
+               float2 *__restrict__ out, long long ldo, int splits, int gbeg, float2 *__restrict__ part,
                int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   const uint32_t raw = fh_smem_u32(smem_raw);
@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   // epilogue.
   const int ntiles = (int)(Ppad / kBN);
   const int ngroups = fh_ngroups(nchunks);  // accumulator buffers cycle per chunk group
-  const int gps = (ngroups + splits - 1) / splits;  // groups per split
+  // groups [gbeg, ngroups) are contracted (the older ones have zero weights)
+  const int gps = (ngroups - gbeg + splits - 1) / splits;  // groups per split
   const int nitems = ntiles * splits;
   const int my_items = (int)blockIdx.x < nitems ? (nitems - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   // item k of this CTA: tile, first and last group
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int v = (int)blockIdx.x + k * (int)gridDim.x;
     tile = v / splits;
     sp = v % splits;
-    G0 = min(ngroups, sp * gps);
+    G0 = min(ngroups, gbeg + sp * gps);
     G1 = min(ngroups, G0 + gps);
   };
 
@@ -679,15 +680,17 @@ __global__ void k_blk_reduce_splits(const float2 *__restrict__ part, int splits,
 // S_far = A3 (128 x K) * planes (K x P) -> out[m*ldo + p] as (hi, lo) pairs.
 // Narrow lines (fewer 64-point tiles than SMs) split the chunk groups of each
 // tile across CTAs and add the partial rows afterwards.
-int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo) {
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo, int gbeg) {
   FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "blocked contraction: K=%d", K);
   fh_prof_mark(ctx, FH_PROF_GEMM, false);
   const long long ntiles = b.Ppad / kBN;
   const int ngroups = fh_ngroups(K / kBK);
-  const int splits = b.max_splits < ngroups ? b.max_splits : ngroups;
+  if (gbeg < 0) gbeg = 0;
+  if (gbeg > ngroups - 1) gbeg = ngroups - 1;  // at least one group: every output row is written
+  const int splits = b.max_splits < ngroups - gbeg ? b.max_splits : ngroups - gbeg;
   const long long items = ntiles * splits;
   k_far_gemm<<<(unsigned)(items < b.nsm ? items : b.nsm), kThreads, kSmemBytes, ctx->stream>>>(
-      b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, splits,
+      b.mapA, b.mapB, K, b.P, b.Ew.as<int8_t>(), b.Ed.as<int8_t>(), b.Ppad, out, ldo, splits, gbeg,
       b.part.as<float2>(), b.err.as<int>());
   int rc = fh_after_launch(ctx, "k_far_gemm");
   if (!rc && splits > 1) {
@@ -732,7 +735,7 @@ extern "C" int fh_history_contract_bf16(fh_ctx *ctx, int K, long long P, const d
     if ((rc = fh_blk_convert(ctx, b, D, ldd, k0, 0))) return rc;
   fh_dbuf pairs;
   if ((rc = fh_alloc(ctx, pairs, sizeof(float2) * (size_t)kBM * b.Ppad, false))) return rc;
-  if ((rc = fh_blk_gemm(ctx, b, K, pairs.as<float2>(), b.Ppad))) return rc;
+  if ((rc = fh_blk_gemm(ctx, b, K, pairs.as<float2>(), b.Ppad, 0))) return rc;
   k_pairs_to_double<<<dim3((unsigned)fh_ceil_div(P, 256), kBM), 256, 0, ctx->stream>>>(pairs.as<float2>(), b.Ppad, P,
                                                                                       S, ldS);
   if ((rc = fh_after_launch(ctx, "k_pairs_to_double"))) return rc;

@@ -41,7 +41,7 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
 int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta, double cut,
                       const double *table, int ldw, int nsteps);
-int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo);
+int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo, int gbeg = 0);
 long long fh_blk_ppad(const fh_blk &b);
 static constexpr int kTgBlock = 64;  // steps per block (128 weight rows)
 
@@ -1361,7 +1361,10 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
                                 s->max_steps, s->max_steps)))
       return rc;
     fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
-    if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<float2>(), s->ldfar))) return rc;
+    // restricted summing with psi = t: the layers older than j - rs_lag have
+    // zero weight for every step of the block; their chunk groups are skipped
+    const int gbeg = s->rs_lag >= 0 && j > s->rs_lag ? (j - s->rs_lag) / (2 * 64) : 0;
+    if ((rc = fh_blk_gemm(ctx, *s->blk, j, s->far.as<float2>(), s->ldfar, gbeg))) return rc;
     s->j0 = j;
   }
   // history layers summed in FP64 this step: the current block in blocked
