@@ -483,11 +483,25 @@ class AB1D(Workload):
         e1.record(stream)
         e1.synchronize()
         ref = sv.get_c()
-        sv.close()
         ms = e0.elapsed_time(e1)
         err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
-        return {main_mode: {"rel_err_vs_fp64": err}, "fp64": {"rel_err_vs_fp64": 0.0, "value": self.gps / (ms / 1e3),
-                                                             "ms_per_solve": ms}}
+        # error at every output step (ten checkpoints along the solve)
+        every = max(1, self.S // 10)
+        per_step = []
+        self.solver.set_c_device(self.C_d.data_ptr())
+        sv.set_c_device(self.C_d.data_ptr())
+        done = 0
+        while done < self.S:
+            n = min(every, self.S - done)
+            self.solver.calc_step(n)
+            sv.calc_step(n)
+            done += n
+            a, b = self.solver.get_c(), sv.get_c()
+            per_step.append(float(np.max(np.abs(a - b)) / np.max(np.abs(b))))
+        sv.close()
+        return {main_mode: {"rel_err_vs_fp64": err, "rel_err_per_output_step": {"every": every, "max": max(per_step),
+                                                                                "values": per_step}},
+                "fp64": {"rel_err_vs_fp64": 0.0, "value": self.gps / (ms / 1e3), "ms_per_solve": ms}}
 
     def solve_device(self):
         self.solver.set_c_device(self.C_d.data_ptr())
