@@ -1,0 +1,52 @@
+"""Steepest-descent fitting (mt_psi_caputo.cpp:1892-1953) over the batched 1D
+solver: the GPU driver follows the oracle driver's iterates."""
+import numpy as np
+import pytest
+
+from theses_code_gb300 import fit, workloads
+
+
+def _problem():
+    from oracle import oracle as O
+    params, U0s = workloads.psi_batch(n=1, seed=3, Nmin=40, Nmax=40, tau=2e-3)
+    base = dict(params[0], u_right=0.0)
+    U0 = -np.asarray(U0s[0])  # pressure heads <= 0 (solve_and_test clamps v to <= 0)
+    truth = dict(base, alpha=0.7, kc=0.4)
+    tau, t_end = base["tau"], 0.1
+    tts = fit._schedule(tau, t_end)
+    _, hist = O.h_solve(truth, U0, len(tts))
+    dL = base["L"] / base["N"]
+    values = []
+    for T in (0.021, 0.05, 0.0731, 0.099):
+        s = int(T / tau)
+        before = U0 if s == 0 else hist[s - 1]
+        k1 = (T - tts[s]) / tau
+        for Z in (0.13, 0.42, 0.77):
+            v = (1 - k1) * fit._interp_z(before, dL, Z, base["N"] - 1) + k1 * fit._interp_z(hist[s], dL, Z, base["N"])
+            values.append((T, Z, min(0.0, v)))
+    return base, truth, U0, t_end, values
+
+
+def test_oracle_driver_reduces_misfit():
+    base, truth, U0, t_end, values = _problem()
+    run = fit.oracle_runner()
+    assert run([truth], U0, base["tau"], t_end, values)[0] < 1e-20
+    v_base = run([base], U0, base["tau"], t_end, values)[0]
+    p, v, it, ns = fit.steepest_descent(run, base, ["alpha", "kc"], U0, t_end, values, vmax=[0.01, 0.01],
+                                        eps=1e-9, max_iter=6)
+    assert v < 0.01 * v_base and it >= 1 and ns >= 1 + 3 * it and (ns - 1) % 3 == 0
+
+
+@pytest.mark.gpu
+def test_gpu_driver_matches_oracle_driver():
+    from theses_code_gb300._lib import Context
+    ctx = Context(0)
+    base, truth, U0, t_end, values = _problem()
+    kw = dict(vmax=[0.01, 0.01], eps=1e-9, max_iter=6)
+    pc, vc, itc, nc = fit.steepest_descent(fit.oracle_runner(), base, ["alpha", "kc"], U0, t_end, values, **kw)
+    pg, vg, itg, ng = fit.steepest_descent(fit.gpu_runner(ctx), base, ["alpha", "kc"], U0, t_end, values, **kw)
+    assert (itg, ng) == (itc, nc)
+    for k in ("alpha", "kc"):
+        assert abs(pg[k] - pc[k]) <= 1e-9 * abs(pc[k]), k
+    assert abs(vg - vc) <= 1e-8 * vc + 1e-20
+    ctx.close()

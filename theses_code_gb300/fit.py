@@ -1,0 +1,169 @@
+"""Parameter fitting over the batched 1D solver.
+
+The reference fits its H_solver parameters to measured pressure heads by
+steepest descent and PSO (mt_psi_caputo.cpp:1750-1953): every candidate
+parameter set is one full solve scored by ``solve_and_test``.  Here the
+candidates of one round (the base point and one forward-difference
+perturbation per fitted parameter) run as instances of one
+``HSolverBatch``, so a gradient costs one batched solve instead of
+``1 + len(keys)`` serial ones.
+
+``misfit`` restates ``solve_and_test`` with metric 0
+(mt_psi_caputo.cpp:1762-1812): at each measurement (T, Z, F) the solution is
+interpolated linearly in depth before and after the step whose interval
+[tt, tt + tau) holds T, then linearly in time, clamped to <= 0, and
+(F - v)^2 is summed; a non-finite solution scores 1e300.  ``steepest_descent``
+restates mt_psi_caputo.cpp:1892-1953 (step halving on failure, stop below
+``eps`` or after ``max_iter`` rounds).
+
+The same functions run on the CPU oracle when ``solve`` is the oracle's
+``h_solve`` wrapper (``oracle_runner``); that is how the tests check them.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+BIG = 1e300
+
+
+def _schedule(tau: float, t_end: float):
+    """Start times tt of the reference's loop ``for (tt = 0; tt <= t; tt += tau)``."""
+    tts, tt = [], 0.0
+    while tt <= t_end:
+        tts.append(tt)
+        tt += tau
+    return tts
+
+
+def _interp_z(U: np.ndarray, dL: float, z: float, jmax: int):
+    for j in range(jmax):
+        if dL * j < z <= dL * (j + 1):
+            k2 = (z - dL * j) / dL
+            return (1 - k2) * U[j] + k2 * U[j + 1]
+    return None
+
+
+def _score(before: list, after: list, tts, tau, dL, N, values) -> float:
+    """Metric-0 misfit from the states before/after each step (lists indexed by step)."""
+    err = 0.0
+    for s, tt in enumerate(tts):
+        for (T, Z, F) in values:
+            if not (T >= tt and T < tt + tau):
+                continue
+            vb = _interp_z(before[s], dL, Z, N - 1)
+            va = _interp_z(after[s], dL, Z, N)
+            if va is None:
+                continue
+            k1 = (T - tt) / tau
+            v = (1 - k1) * (vb if vb is not None else 0.0) + k1 * va
+            if v > 0.0:
+                v = 0.0
+            err += (F - v) * (F - v)
+        if not np.isfinite(after[s][0]):
+            return BIG
+    return err
+
+
+def gpu_runner(ctx, mode: int | None = None):
+    """Scores a list of parameter sets as one batch on the GPU."""
+    from .solvers import HSolverBatch
+    from . import _lib
+
+    def run(params_list, U0, tau, t_end, values):
+        tts = _schedule(tau, t_end)
+        steps = len(tts)
+        b = HSolverBatch(ctx, params_list, steps + 1, _lib.FH_H_FP64 if mode is None else mode)
+        b.set_u([U0] * len(params_list))
+        # steps whose interval holds a measurement: states before and after them
+        need = {s for s, tt in enumerate(tts) for (T, _, _) in values if T >= tt and T < tt + tau}
+        before = [[None] * steps for _ in params_list]
+        after = [[None] * steps for _ in params_list]
+        done = 0
+        for s in sorted(need):
+            if s > done:
+                b.calc_step(s - done)
+                done = s
+            cur = b.get_u()
+            b.calc_step(1)
+            done += 1
+            nxt = b.get_u()
+            for k in range(len(params_list)):
+                before[k][s], after[k][s] = cur[k], nxt[k]
+        if done < steps:
+            b.calc_step(steps - done)
+        last = b.get_u()
+        b.close()
+        out = []
+        for k, p in enumerate(params_list):
+            N, dL = p["N"], p["L"] / p["N"]
+            for s in range(steps):  # steps without measurements only need finiteness
+                if after[k][s] is None:
+                    after[k][s] = last[k] if s == steps - 1 else np.zeros(1)
+            out.append(_score(before[k], after[k], tts, tau, dL, N, values))
+            if not np.all(np.isfinite(last[k])):
+                out[-1] = BIG
+        return out
+
+    return run
+
+
+def oracle_runner():
+    """The same scoring on the CPU oracle (test infrastructure)."""
+    from oracle import oracle as O
+
+    def run(params_list, U0, tau, t_end, values):
+        tts = _schedule(tau, t_end)
+        steps = len(tts)
+        out = []
+        for p in params_list:
+            U, hist = O.h_solve(p, U0, steps)
+            before = [U0] + [hist[s] for s in range(steps - 1)]
+            after = [hist[s] for s in range(steps)]
+            N, dL = p["N"], p["L"] / p["N"]
+            sc = _score(before, after, tts, tau, dL, N, values)
+            out.append(BIG if not np.all(np.isfinite(U)) else sc)
+        return out
+
+    return run
+
+
+def steepest_descent(run, base: dict, keys: list[str], U0: np.ndarray, t_end: float, values,
+                     vmax: list[float] | None = None, eps: float = 1e-6, max_iter: int = 20):
+    """Fits base[keys] (mt_psi_caputo.cpp:1892-1953).  Returns (params, misfit,
+    rounds, solves)."""
+    tau = base["tau"]
+    vmax = vmax or [0.0] * len(keys)
+    p = dict(base)
+    solves = 1
+    v0 = run([p], U0, tau, t_end, values)[0]
+    if v0 == BIG:
+        return p, v0, 0, solves
+    step, it = 1.0, 0
+    while True:
+        sts = [step * (vm if vm != 0 else 1.0) for vm in vmax]
+        cands = []
+        for k, st in zip(keys, sts):
+            q = dict(p)
+            q[k] = p[k] + st
+            cands.append(q)
+        vs = run(cands, U0, tau, t_end, values)  # all perturbations in one batch
+        solves += len(cands)
+        grad = [(v - v0) / st for v, st in zip(vs, sts)]
+        sp = dict(p)
+        for k, g in zip(keys, grad):
+            p[k] = p[k] - step * g
+        vnew = run([p], U0, tau, t_end, values)[0]
+        solves += 1
+        if vnew >= v0:
+            p = sp
+            step /= 2.0
+            if step < eps:
+                break
+        else:
+            if abs(vnew - v0) < eps:
+                return p, vnew, it + 1, solves
+            v0 = vnew
+        if it > max_iter:
+            break
+        it += 1
+    return p, v0, it, solves
