@@ -50,3 +50,30 @@ def test_gpu_driver_matches_oracle_driver():
         assert abs(pg[k] - pc[k]) <= 1e-9 * abs(pc[k]), k
     assert abs(vg - vc) <= 1e-8 * vc + 1e-20
     ctx.close()
+
+
+def test_oracle_pso_reduces_misfit():
+    base, truth, U0, t_end, values = _problem()
+    run = fit.oracle_runner()
+    v_base = run([base], U0, base["tau"], t_end, values)[0]
+    p, v, it, ns = fit.pso(run, base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end, values, n=8,
+                           max_iter=4, seed=1)
+    assert v < 0.2 * v_base and ns == 8 * (it + 1)
+    # an out-of-range candidate scores 1e300 instead of failing the batch
+    assert run([dict(base, alpha=1.2), base], U0, base["tau"], t_end, values)[0] == fit.BIG
+
+
+@pytest.mark.gpu
+def test_gpu_pso_matches_oracle_pso():
+    from theses_code_gb300._lib import Context
+    ctx = Context(0)
+    base, truth, U0, t_end, values = _problem()
+    kw = dict(n=8, max_iter=4, seed=1)
+    b = [(0.55, 0.9), (0.2, 0.9)]
+    pc, vc, itc, nc = fit.pso(fit.oracle_runner(), base, ["alpha", "kc"], b, U0, t_end, values, **kw)
+    pg, vg, itg, ng = fit.pso(fit.gpu_runner(ctx), base, ["alpha", "kc"], b, U0, t_end, values, **kw)
+    assert (itg, ng) == (itc, nc)
+    for k in ("alpha", "kc"):
+        assert abs(pg[k] - pc[k]) <= 1e-9 * abs(pc[k]), k
+    assert abs(vg - vc) <= 1e-8 * vc + 1e-20
+    ctx.close()

@@ -1,23 +1,23 @@
 """Parameter fitting over the batched 1D solver.
 
 The reference fits its H_solver parameters to measured pressure heads by
-steepest descent and PSO (mt_psi_caputo.cpp:1750-1953): every candidate
+steepest descent and PSO (mt_psi_caputo.cpp:1750-2240): every candidate
 parameter set is one full solve scored by ``solve_and_test``.  Here the
-candidates of one round (the base point and one forward-difference
-perturbation per fitted parameter) run as instances of one
-``HSolverBatch``, so a gradient costs one batched solve instead of
-``1 + len(keys)`` serial ones.
+candidates of one round (the forward-difference perturbations of a gradient,
+or a whole swarm) run as instances of one ``HSolverBatch`` (``gpu_runner``),
+so a round costs one batched solve instead of one solve per candidate.
 
-``misfit`` restates ``solve_and_test`` with metric 0
+``_score`` restates ``solve_and_test`` with metric 0
 (mt_psi_caputo.cpp:1762-1812): at each measurement (T, Z, F) the solution is
 interpolated linearly in depth before and after the step whose interval
 [tt, tt + tau) holds T, then linearly in time, clamped to <= 0, and
 (F - v)^2 is summed; a non-finite solution scores 1e300.  ``steepest_descent``
 restates mt_psi_caputo.cpp:1892-1953 (step halving on failure, stop below
-``eps`` or after ``max_iter`` rounds).
+``eps`` or after ``max_iter`` rounds); ``pso`` the swarm update of 2183-2223
+in synchronous form.
 
-The same functions run on the CPU oracle when ``solve`` is the oracle's
-``h_solve`` wrapper (``oracle_runner``); that is how the tests check them.
+``oracle_runner`` scores the same candidates on the CPU oracle (test
+infrastructure); the tests run both drivers on both runners.
 """
 from __future__ import annotations
 
@@ -64,11 +64,31 @@ def _score(before: list, after: list, tts, tau, dL, N, values) -> float:
     return err
 
 
+def _valid(p: dict) -> bool:
+    """The parameter checks of fh_h_batch_create (a candidate outside them,
+    e.g. alpha >= 1 after a PSO move, scores 1e300 instead of failing the
+    batch)."""
+    return (p["N"] >= 2 and p["L"] > 0 and p["tau"] > 0 and 0 < p["alpha"] < 1
+            and (p["weights"] == 0 or p["beta"] > 0) and np.isfinite(p["kc"]) and np.isfinite(p["kgam"]))
+
+
+def _only_valid(run):
+    def wrapped(params_list, U0, tau, t_end, values):
+        ok = [k for k, p in enumerate(params_list) if _valid(p)]
+        out = [BIG] * len(params_list)
+        if ok:
+            for k, v in zip(ok, run([params_list[k] for k in ok], U0, tau, t_end, values)):
+                out[k] = v
+        return out
+    return wrapped
+
+
 def gpu_runner(ctx, mode: int | None = None):
     """Scores a list of parameter sets as one batch on the GPU."""
     from .solvers import HSolverBatch
     from . import _lib
 
+    @_only_valid
     def run(params_list, U0, tau, t_end, values):
         tts = _schedule(tau, t_end)
         steps = len(tts)
@@ -111,6 +131,7 @@ def oracle_runner():
     """The same scoring on the CPU oracle (test infrastructure)."""
     from oracle import oracle as O
 
+    @_only_valid
     def run(params_list, U0, tau, t_end, values):
         tts = _schedule(tau, t_end)
         steps = len(tts)
@@ -167,3 +188,46 @@ def steepest_descent(run, base: dict, keys: list[str], U0: np.ndarray, t_end: fl
             break
         it += 1
     return p, v0, it, solves
+
+
+def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0: np.ndarray, t_end: float, values,
+        n: int = 16, omega: float = 0.7, fi_p: float = 1.4, fi_g: float = 1.4, eps: float = 1e-8,
+        max_iter: int = 10, seed: int = 0):
+    """Particle swarm over base[keys] (the update of mt_psi_caputo.cpp:2183-2223:
+    v = omega v + fi_p rp (p_best - x) + fi_g rg (g_best - x), x += v, random
+    numbers in steps of 1e-4; stop when the worst particle is within eps of
+    the best).  Synchronous: every particle of an iteration moves with the
+    global best of the previous iteration and the swarm is scored as one batch
+    (the reference scores particles one by one and lets later ones see the
+    best found earlier in the same iteration).  Returns (params, misfit,
+    iterations, solves)."""
+    rng = np.random.default_rng(seed)
+    rnd = lambda: int(rng.integers(0, 10000)) / 10000.0  # noqa: E731
+    tau = base["tau"]
+    size = len(keys)
+    x = [[lo + (hi - lo) * rnd() for (lo, hi) in bounds] for _ in range(n)]
+    v = [[0.0] * size for _ in range(n)]
+    cand = lambda xi: dict(base, **dict(zip(keys, xi)))  # noqa: E731
+    f = run([cand(xi) for xi in x], U0, tau, t_end, values)
+    solves = n
+    pb, pf = [xi[:] for xi in x], list(f)
+    g = int(np.argmin(f))
+    gb, gf = x[g][:], f[g]
+    it = 0
+    for it in range(1, max_iter + 1):
+        for i in range(n):
+            for j in range(size):
+                rp, rg = rnd(), rnd()
+                v[i][j] = omega * v[i][j] + fi_p * rp * (pb[i][j] - x[i][j]) + fi_g * rg * (gb[j] - x[i][j])
+            for j in range(size):
+                x[i][j] += v[i][j]
+        f = run([cand(xi) for xi in x], U0, tau, t_end, values)  # the swarm in one batch
+        solves += n
+        for i in range(n):
+            if f[i] < pf[i]:
+                pb[i], pf[i] = x[i][:], f[i]
+            if f[i] < gf:
+                gb, gf = x[i][:], f[i]
+        if max(f) - gf < eps:
+            break
+    return cand(gb), gf, it, solves
