@@ -77,3 +77,37 @@ def test_gpu_pso_matches_oracle_pso():
         assert abs(pg[k] - pc[k]) <= 1e-9 * abs(pc[k]), k
     assert abs(vg - vc) <= 1e-8 * vc + 1e-20
     ctx.close()
+
+
+def test_fit_input_file_round_trip(tmp_path):
+    """The reference's fit_input.txt layout (mt_minimal.cpp:1955-2043): heads
+    scaled by Hmult, the initial profile interpolated and extrapolated as in
+    mt_psi_caputo.cpp:1700-1733, and a fit driven from the file."""
+    from theses_code_gb300 import fit_input as FI
+    base, truth, U0, t_end, values = _problem()
+    lines = ["1 %d 3 1 0 0 0 0 1.0" % len(values), "8 0.7 1.4 1.4 1e-8 4"]
+    lines += ["%r %r %r" % (float(T), float(Z), float(F) / FI.HMULT) for (T, Z, F) in values]
+    lines += ["0.2 -0.03", "0.5 -0.01", "0.9 -0.02"]  # initial heads / Hmult
+    lines += ["0.05 0.5 -0.01"]  # one check value
+    lines += ["0.7 0.4"]  # fixed parameter values
+    path = tmp_path / "fit_input.txt"
+    path.write_text("\n".join(lines) + "\n")
+    inp = FI.read_fit_input(str(path))
+    assert inp["pso"]["n"] == 8 and inp["pso"]["max_iter"] == 4 and inp["param_values"] == [0.7, 0.4]
+    assert np.allclose([v[2] for v in inp["values"]], [v[2] for v in values], rtol=1e-15)
+    assert inp["check"][0][2] == pytest.approx(-0.1)
+    U = FI.initial_profile(inp["init_Z"], inp["init_F"], 10, 0.1)
+    assert U[0] == pytest.approx(-0.3 - 0.2 * (-0.1 - -0.3) / 0.3)      # extrapolated above the first depth
+    assert U[3] == pytest.approx(-0.3 + (0.1 / 0.3) * 0.2)              # between 0.2 and 0.5
+    assert U[10] == pytest.approx(-0.2 + 0.1 * (-0.2 - -0.1) / 0.4)     # extrapolated below the last
+    U0f, t_endf, vals = FI.fit_problem(inp, base)
+    run = fit.oracle_runner()
+    v0 = run([base], U0f, base["tau"], t_endf, vals)[0]
+    p, v, it, ns = fit.steepest_descent(run, base, ["alpha", "kc"], U0f, t_endf, vals, vmax=[0.01, 0.01],
+                                        eps=1e-9, max_iter=3)
+    assert v < v0
+    lines[0] = "1 %d 3 1 1 0 0 0 1.0" % len(values)  # one precipitation record: not modelled
+    lines.insert(2 + len(values) + 3, "0.01 1e-7")
+    path.write_text("\n".join(lines) + "\n")
+    with pytest.raises(NotImplementedError):
+        FI.fit_problem(FI.read_fit_input(str(path)), base)
