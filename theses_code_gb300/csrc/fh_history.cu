@@ -8,7 +8,7 @@
 // scheduling (no atomics).
 //
 // Cost model: every element of D is read once per step and used in M FMAs.
-// On GB300 the FP64 pipe, not HBM, bounds this loop once M >= 1 (see DESIGN.md).
+// On GB300 the FP64 pipe, not HBM, bounds this loop once M >= 1.
 #include "fh_internal.h"
 #include "fh_common.cuh"
 
