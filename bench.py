@@ -336,6 +336,22 @@ class TG2D(Workload):
                 d["value"] = self.gps / (times[m] / 1e3)
                 d["ms_per_solve"] = times[m]
             out[m] = d
+        if main_mode != "fp64":
+            # the main mode against FP64 at ten output steps along the solve
+            every = max(1, self.S // 10)
+            ref_sv = self.new_solver(ctx, "fp64")
+            ref_sv.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
+            self.solver.set_state_device(self.V2_d.data_ptr(), self.C0_d.data_ptr())
+            per_step, done = [], 0
+            while done < self.S:
+                n = min(every, self.S - done)
+                ref_sv.calc_step(n)
+                self.solver.calc_step(n)
+                done += n
+                a, b = self.solver.get_c(), ref_sv.get_c()
+                per_step.append(float(np.max(np.abs(a - b)) / np.max(np.abs(b))))
+            ref_sv.close()
+            out[main_mode]["rel_err_per_output_step"] = {"every": every, "max": max(per_step), "values": per_step}
         return out
 
 
@@ -658,6 +674,8 @@ def run_gb300(args):
         if "fp64" in cmp and "value" in cmp["fp64"]:
             result["speedup_vs_plain_fp64"] = value / cmp["fp64"]["value"]
         result["rel_err_vs_fp64"] = cmp[args.mode]["rel_err_vs_fp64"]
+        if "rel_err_per_output_step" in cmp[args.mode]:
+            result["rel_err_max_over_output_steps"] = cmp[args.mode]["rel_err_per_output_step"]["max"]
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args) if args.config == "tg2d" else wl.cpu_baseline()
     if rank == 0:
