@@ -80,8 +80,9 @@ static constexpr int kLineCtaMaxInst = 152;  // batches below this many instance
 static constexpr int kSpaceMaxN = 2048;  // nodes of a space-fractional instance (shared-memory sums)
 static constexpr int kHWeightThreads = 128;                 // nodes per weights CTA
 static constexpr int kHWeightSlots = kHWeightThreads - 1;  // slots per weights CTA
-// per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | 2^(-1/beta)
-static constexpr int kIbStride = 2 * kIbTerms + 2;
+// per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | 2^(-1/beta) |
+// log tau | 1/beta
+static constexpr int kIbStride = 2 * kIbTerms + 4;
 
 // ------------------------------------------------------------------ kernels
 
@@ -133,7 +134,9 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
         }
       }
     }
-    if (k == kHWeightThreads - 1) sc = pow(X * I.tau, 1.0 - I.alpha * I.beta) / I.beta;
+    // (X tau)^(1 - alpha beta) / beta with log X from the table: one exp
+    if (k == kHWeightThreads - 1)
+      sc = exp((1.0 - I.alpha * I.beta) * (lgt[tstep + 1].x + Lc[2 * kIbTerms + 2])) * Lc[2 * kIbTerms + 3];
     __syncthreads();
     if (k < kHWeightSlots && i < os - 1) {
       double diff;
@@ -178,6 +181,8 @@ __global__ void k_h_ibtab(const fh_h_dev_inst *__restrict__ inst, int n, double 
   fh_ib_tables(a, bb, row, row + kIbTerms);
   row[2 * kIbTerms] = exp(lgamma(a) + lgamma(bb) - lgamma(a + bb));  // B(a, b)
   row[2 * kIbTerms + 1] = pow(0.5, a);                               // y <= 1/2 <=> x/X <= 2^(-1/beta)
+  row[2 * kIbTerms + 2] = log(I.tau);
+  row[2 * kIbTerms + 3] = a;                                          // 1/beta
 }
 
 // Lag table of the L1 instances: Lb[b][l] = (l+1)^(1-a) - l^(1-a) (mt_minimal.cpp:930),
