@@ -17,8 +17,13 @@ throughput and every result's relative max-norm difference to the FP64 path
 
 Other configurations (not the default line): caputo1d (1D L1, N=200, 1000
 steps), psi_batch (4096 ragged psi-Caputo instances, sample of the 5000-step
-solve), ab1d (Atangana-Baleanu, N=2048, 20000 steps), serve (Poisson stream of
-mixed solves, p50/p99 latency).
+solve; --solve-steps 5000 for the whole solve), ab1d (Atangana-Baleanu,
+N=2048, 20000 steps), serve (Poisson stream of mixed solves, p50/p99
+latency).  The reference's approximate history schemes on the 2D workload:
+--dt-eps E (restricted summing, dt_alg 2) and --series J (series expansion,
+dt_alg 3); --gamma-min G gives psi_batch space-fractional orders in [G, 1).
+Blocked modes also report their error against the FP64 path at ten output
+steps.
 
 --impl reference times the CPU implementation of the same path (the oracle
 port of the reference solver, all host threads) on a bounded sample and prints
