@@ -111,3 +111,20 @@ def test_fit_input_file_round_trip(tmp_path):
     path.write_text("\n".join(lines) + "\n")
     with pytest.raises(NotImplementedError):
         FI.fit_problem(FI.read_fit_input(str(path)), base)
+
+
+def test_misfit_metrics():
+    """solve_and_test's metrics 0, 1 and 2 (mt_psi_caputo.cpp:1790-1803) on
+    hand-made states: one step, two measurements."""
+    before = [np.array([-1.0, -2.0, -3.0])]
+    after = [np.array([-1.0, -2.0, -4.0])]
+    tts, tau, dL, N = [0.0], 1.0, 1.0, 2
+    values = [(0.5, 0.5, -1.0), (0.25, 1.5, -3.0)]
+    # point 1: z 0.5 -> (-1.5 before, -1.5 after) -> -1.5; point 2: z 1.5 ->
+    # before (j < N-1: none) 0, after -3.0; k1 0.25 -> -0.75
+    v1, v2 = -1.5, 0.75 * 0.0 + 0.25 * -3.0
+    e0 = fit._score(before, after, tts, tau, dL, N, values, 0)
+    assert e0 == pytest.approx((-1.0 - v1) ** 2 + (-3.0 - v2) ** 2)
+    r1, r2 = abs((-1.0 - v1) / -1.0), abs((-3.0 - v2) / -3.0)
+    assert fit._score(before, after, tts, tau, dL, N, values, 1) == pytest.approx(max(r1, r2))
+    assert fit._score(before, after, tts, tau, dL, N, values, 2) == pytest.approx(r1 + r2 if r2 > r1 else r1)

@@ -43,8 +43,12 @@ def _interp_z(U: np.ndarray, dL: float, z: float, jmax: int):
     return None
 
 
-def _score(before: list, after: list, tts, tau, dL, N, values) -> float:
-    """Metric-0 misfit from the states before/after each step (lists indexed by step)."""
+def _score(before: list, after: list, tts, tau, dL, N, values, metric: int = 0) -> float:
+    """Misfit from the states before/after each step (lists indexed by step).
+    metric 0: sum of squared differences; 1: largest relative difference;
+    2: relative differences added when one exceeds the running value (the
+    reference's rule, mt_psi_caputo.cpp:1790-1803); F = 0 points are skipped
+    by metrics 1 and 2."""
     err = 0.0
     for s, tt in enumerate(tts):
         for (T, Z, F) in values:
@@ -58,7 +62,12 @@ def _score(before: list, after: list, tts, tau, dL, N, values) -> float:
             v = (1 - k1) * (vb if vb is not None else 0.0) + k1 * va
             if v > 0.0:
                 v = 0.0
-            err += (F - v) * (F - v)
+            if metric == 0:
+                err += (F - v) * (F - v)
+            elif F != 0:
+                rel = abs((F - v) / F)
+                if rel > err:
+                    err = rel if metric == 1 else err + rel
         if not np.isfinite(after[s][0]):
             return BIG
     return err
@@ -83,7 +92,7 @@ def _only_valid(run):
     return wrapped
 
 
-def gpu_runner(ctx, mode: int | None = None):
+def gpu_runner(ctx, mode: int | None = None, metric: int = 0):
     """Scores a list of parameter sets as one batch on the GPU."""
     from .solvers import HSolverBatch
     from . import _lib
@@ -119,7 +128,7 @@ def gpu_runner(ctx, mode: int | None = None):
             for s in range(steps):  # steps without measurements only need finiteness
                 if after[k][s] is None:
                     after[k][s] = last[k] if s == steps - 1 else np.zeros(1)
-            out.append(_score(before[k], after[k], tts, tau, dL, N, values))
+            out.append(_score(before[k], after[k], tts, tau, dL, N, values, metric))
             if not np.all(np.isfinite(last[k])):
                 out[-1] = BIG
         return out
@@ -127,7 +136,7 @@ def gpu_runner(ctx, mode: int | None = None):
     return run
 
 
-def oracle_runner():
+def oracle_runner(metric: int = 0):
     """The same scoring on the CPU oracle (test infrastructure)."""
     from oracle import oracle as O
 
@@ -141,7 +150,7 @@ def oracle_runner():
             before = [U0] + [hist[s] for s in range(steps - 1)]
             after = [hist[s] for s in range(steps)]
             N, dL = p["N"], p["L"] / p["N"]
-            sc = _score(before, after, tts, tau, dL, N, values)
+            sc = _score(before, after, tts, tau, dL, N, values, metric)
             out.append(BIG if not np.all(np.isfinite(U)) else sc)
         return out
 
