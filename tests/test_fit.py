@@ -128,3 +128,13 @@ def test_misfit_metrics():
     r1, r2 = abs((-1.0 - v1) / -1.0), abs((-3.0 - v2) / -3.0)
     assert fit._score(before, after, tts, tau, dL, N, values, 1) == pytest.approx(max(r1, r2))
     assert fit._score(before, after, tts, tau, dL, N, values, 2) == pytest.approx(r1 + r2 if r2 > r1 else r1)
+
+
+def test_oracle_adaptive_pso_runs():
+    """The adaptive schedule (omega and per-coordinate fi) on the oracle."""
+    base, truth, U0, t_end, values = _problem()
+    run = fit.oracle_runner()
+    v_base = run([base], U0, base["tau"], t_end, values)[0]
+    p, v, it, ns = fit.pso(run, base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end, values, n=8,
+                           max_iter=4, seed=1, adaptive=True)
+    assert v < v_base and ns == 8 * (it + 1) and 0.0 < p["alpha"] < 1.0

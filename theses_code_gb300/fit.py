@@ -201,14 +201,19 @@ def steepest_descent(run, base: dict, keys: list[str], U0: np.ndarray, t_end: fl
 
 def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0: np.ndarray, t_end: float, values,
         n: int = 16, omega: float = 0.7, fi_p: float = 1.4, fi_g: float = 1.4, eps: float = 1e-8,
-        max_iter: int = 10, seed: int = 0):
+        max_iter: int = 10, seed: int = 0, adaptive: bool = False):
     """Particle swarm over base[keys] (the update of mt_psi_caputo.cpp:2183-2223:
     v = omega v + fi_p rp (p_best - x) + fi_g rg (g_best - x), x += v, random
     numbers in steps of 1e-4; stop when the worst particle is within eps of
     the best).  Synchronous: every particle of an iteration moves with the
     global best of the previous iteration and the swarm is scored as one batch
     (the reference scores particles one by one and lets later ones see the
-    best found earlier in the same iteration).  Returns (params, misfit,
+    best found earlier in the same iteration).  ``adaptive`` applies the
+    reference's adaptive schedule (mt_psi_caputo.cpp:2093-2179): omega starts
+    at 1 and is divided or multiplied by its initial value as the mean
+    velocity runs above or below v0 exp(-(2(it+1)/(max_iter-it))^2), and
+    per-coordinate fi_p, fi_g follow the velocity spread against the initial
+    population's range (clamped to [0, 2]).  Returns (params, misfit,
     iterations, solves)."""
     rng = np.random.default_rng(seed)
     rnd = lambda: int(rng.integers(0, 10000)) / 10000.0  # noqa: E731
@@ -222,12 +227,37 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
     pb, pf = [xi[:] for xi in x], list(f)
     g = int(np.argmin(f))
     gb, gf = x[g][:], f[g]
+    fp, fg = [fi_p] * size, [fi_g] * size
+    clamp = lambda a: min(2.0, max(0.0, a))  # noqa: E731
+    if adaptive:
+        xa = np.asarray(x)
+        v0 = float(np.sqrt(np.sum(xa * xa))) / n  # the reference measures positions here
+        v0v = np.sqrt(np.sum(xa * xa, axis=0)) / n
+        vmax = [(xa[:, j].max() - xa[:, j].min()) / fi_g for j in range(size)]
+        vmax = [vm if vm != 0.0 else 1.0 / fi_g for vm in vmax]
+        ad_p, ad_c = omega, fi_p
+        omega = 1.0
+        fp = [clamp(ad_c * v0v[j] / vmax[j]) for j in range(size)]
+        fg = [clamp(ad_c * (1 - v0v[j] / vmax[j])) for j in range(size)]
     it = 0
     for it in range(1, max_iter + 1):
+        if adaptive:
+            q = np.float32(2 * it) / np.float32(max_iter - (it - 1))  # float arithmetic, as the reference
+            ve = v0 * float(np.exp(-float(q * q)))
+            va = np.asarray(v)
+            vavg = float(np.sqrt(np.sum(va * va))) / n
+            vavgc = np.sqrt(np.sum(va * va, axis=0)) / n
+            if vavg > ve:
+                omega /= ad_p
+            if vavg < ve:
+                omega *= ad_p
+            omega = clamp(omega)
+            fp = [clamp(ad_c * vavgc[j] / vmax[j]) for j in range(size)]
+            fg = [clamp(ad_c * (1 - vavgc[j] / vmax[j])) for j in range(size)]
         for i in range(n):
             for j in range(size):
                 rp, rg = rnd(), rnd()
-                v[i][j] = omega * v[i][j] + fi_p * rp * (pb[i][j] - x[i][j]) + fi_g * rg * (gb[j] - x[i][j])
+                v[i][j] = omega * v[i][j] + fp[j] * rp * (pb[i][j] - x[i][j]) + fg[j] * rg * (gb[j] - x[i][j])
             for j in range(size):
                 x[i][j] += v[i][j]
         f = run([cand(xi) for xi in x], U0, tau, t_end, values)  # the swarm in one batch
