@@ -138,3 +138,16 @@ def test_oracle_adaptive_pso_runs():
     p, v, it, ns = fit.pso(run, base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end, values, n=8,
                            max_iter=4, seed=1, adaptive=True)
     assert v < v_base and ns == 8 * (it + 1) and 0.0 < p["alpha"] < 1.0
+
+
+def test_oracle_pso_restarts():
+    """With restart_prox = 1 and omega 0.5 about half the moves restart: the
+    swarm takes another path than without restarts (same random stream)."""
+    base, truth, U0, t_end, values = _problem()
+    run = fit.oracle_runner()
+    kw = dict(n=8, omega=0.5, max_iter=2, seed=3)
+    b = [(0.55, 0.9), (0.2, 0.9)]
+    p1, v1, _, _ = fit.pso(run, base, ["alpha", "kc"], b, U0, t_end, values, restart_prox=1.0, **kw)
+    p0, v0, _, _ = fit.pso(run, base, ["alpha", "kc"], b, U0, t_end, values, restart_prox=0.0, **kw)
+    assert v1 < fit.BIG and v0 < fit.BIG
+    assert (p1["alpha"], p1["kc"]) != (p0["alpha"], p0["kc"])

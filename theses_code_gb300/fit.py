@@ -201,7 +201,7 @@ def steepest_descent(run, base: dict, keys: list[str], U0: np.ndarray, t_end: fl
 
 def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0: np.ndarray, t_end: float, values,
         n: int = 16, omega: float = 0.7, fi_p: float = 1.4, fi_g: float = 1.4, eps: float = 1e-8,
-        max_iter: int = 10, seed: int = 0, adaptive: bool = False):
+        max_iter: int = 10, seed: int = 0, adaptive: bool = False, restart_prox: float = 0.0):
     """Particle swarm over base[keys] (the update of mt_psi_caputo.cpp:2183-2223:
     v = omega v + fi_p rp (p_best - x) + fi_g rg (g_best - x), x += v, random
     numbers in steps of 1e-4; stop when the worst particle is within eps of
@@ -213,8 +213,10 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
     at 1 and is divided or multiplied by its initial value as the mean
     velocity runs above or below v0 exp(-(2(it+1)/(max_iter-it))^2), and
     per-coordinate fi_p, fi_g follow the velocity spread against the initial
-    population's range (clamped to [0, 2]).  Returns (params, misfit,
-    iterations, solves)."""
+    population's range (clamped to [0, 2]).  After each move a particle
+    restarts at a random position with probability (1 - omega) restart_prox
+    when omega < 1 (2203-2209; off by default as in the reference).  Returns
+    (params, misfit, iterations, solves)."""
     rng = np.random.default_rng(seed)
     rnd = lambda: int(rng.integers(0, 10000)) / 10000.0  # noqa: E731
     tau = base["tau"]
@@ -260,6 +262,8 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
                 v[i][j] = omega * v[i][j] + fp[j] * rp * (pb[i][j] - x[i][j]) + fg[j] * rg * (gb[j] - x[i][j])
             for j in range(size):
                 x[i][j] += v[i][j]
+            if rnd() < ((1.0 - omega) if omega < 1.0 else 0.0) * restart_prox:
+                x[i] = [lo + (hi - lo) * rnd() for (lo, hi) in bounds]
         f = run([cand(xi) for xi in x], U0, tau, t_end, values)  # the swarm in one batch
         solves += n
         for i in range(n):
