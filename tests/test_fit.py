@@ -151,3 +151,18 @@ def test_oracle_pso_restarts():
     p0, v0, _, _ = fit.pso(run, base, ["alpha", "kc"], b, U0, t_end, values, restart_prox=0.0, **kw)
     assert v1 < fit.BIG and v0 < fit.BIG
     assert (p1["alpha"], p1["kc"]) != (p0["alpha"], p0["kc"])
+
+
+def test_pso_log_lines():
+    """The reference's PSO log layout (mt_psi_caputo.cpp:2056-2244)."""
+    import io
+    base, truth, U0, t_end, values = _problem()
+    buf = io.StringIO()
+    p, v, it, ns = fit.pso(fit.oracle_runner(), base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end,
+                           values, n=4, max_iter=2, seed=2, log=buf)
+    lines = buf.getvalue().splitlines()
+    assert [l.split(" - ")[0] for l in lines[:4]] == ["#initial %d" % i for i in range(4)]
+    assert lines[4].startswith("#initial best: ") and len(lines[4].split()) == 2 + 3
+    assert len(lines) == 5 + it and lines[5].startswith("0 avg ")
+    last = lines[-1].split("best: ")[1].split()
+    assert float(last[0]) == pytest.approx(v, rel=1e-5) and float(last[1]) == pytest.approx(p["alpha"], rel=1e-5)

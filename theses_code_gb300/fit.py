@@ -201,7 +201,7 @@ def steepest_descent(run, base: dict, keys: list[str], U0: np.ndarray, t_end: fl
 
 def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0: np.ndarray, t_end: float, values,
         n: int = 16, omega: float = 0.7, fi_p: float = 1.4, fi_g: float = 1.4, eps: float = 1e-8,
-        max_iter: int = 10, seed: int = 0, adaptive: bool = False, restart_prox: float = 0.0):
+        max_iter: int = 10, seed: int = 0, adaptive: bool = False, restart_prox: float = 0.0, log=None):
     """Particle swarm over base[keys] (the update of mt_psi_caputo.cpp:2183-2223:
     v = omega v + fi_p rp (p_best - x) + fi_g rg (g_best - x), x += v, random
     numbers in steps of 1e-4; stop when the worst particle is within eps of
@@ -215,8 +215,11 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
     per-coordinate fi_p, fi_g follow the velocity spread against the initial
     population's range (clamped to [0, 2]).  After each move a particle
     restarts at a random position with probability (1 - omega) restart_prox
-    when omega < 1 (2203-2209; off by default as in the reference).  Returns
-    (params, misfit, iterations, solves)."""
+    when omega < 1 (2203-2209; off by default as in the reference).  The
+    search also stops once the best misfit is at most eps (2250).  ``log``
+    (a text file) receives the reference's log lines (2056-2244):
+    "#initial i - f", "#initial best: f x...", then per iteration
+    "it avg A best: f x...".  Returns (params, misfit, iterations, solves)."""
     rng = np.random.default_rng(seed)
     rnd = lambda: int(rng.integers(0, 10000)) / 10000.0  # noqa: E731
     tau = base["tau"]
@@ -229,6 +232,10 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
     pb, pf = [xi[:] for xi in x], list(f)
     g = int(np.argmin(f))
     gb, gf = x[g][:], f[g]
+    if log is not None:
+        for i in range(n):
+            log.write("#initial %d - %g\n" % (i, f[i]))
+        log.write("#initial best: " + "".join("%2.2g " % z for z in [gf] + gb) + "\n")
     fp, fg = [fi_p] * size, [fi_g] * size
     clamp = lambda a: min(2.0, max(0.0, a))  # noqa: E731
     if adaptive:
@@ -271,6 +278,8 @@ def pso(run, base: dict, keys: list[str], bounds: list[tuple[float, float]], U0:
                 pb[i], pf[i] = x[i][:], f[i]
             if f[i] < gf:
                 gb, gf = x[i][:], f[i]
-        if max(f) - gf < eps:
+        if log is not None:
+            log.write("%d avg %g best: " % (it - 1, sum(f) / n) + "".join("%g " % z for z in [gf] + gb) + "\n")
+        if max(f) - gf < eps or gf <= eps:
             break
     return cand(gb), gf, it, solves
