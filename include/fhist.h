@@ -96,7 +96,11 @@ int fh_mittag_leffler(fh_ctx *ctx, int n, double a, double b, const double *z, d
  * Replaces the history loops of H_solver::Om1 (mt_psi_caputo.cpp:1315-1342),
  * TG_solver_::Om1 (fr_d_t_g_2d.cpp:3340-3490), H_solver::time_summing
  * (irrigation_fractional.cpp:4099-4177) and the GPU Sum kernels
- * (irrigation_fractional.cpp:1224-1495).  P and ldd must be even, D 16-byte aligned. */
+ * (irrigation_fractional.cpp:1224-1495).  P and ldd must be even, D 16-byte aligned.
+ * Asynchronous on the context stream; its split partials live in a workspace
+ * the context keeps, which a call grows (allocating, after synchronising the
+ * stream) only when it needs more than earlier calls did, so repeated calls of
+ * one size neither allocate nor synchronise. */
 int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                    const double *D, long long ldd, double *S, long long ldS);
 
@@ -116,19 +120,24 @@ int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, cons
 int fh_history_contract_bf16(fh_ctx *ctx, int K, long long P, const double *W, int ldw,
                                const double *D, long long ldd, double *S, long long ldS);
 
-/* Allocation-free variant of fh_history_sum (same arguments, same result).
- * No counterpart in the reference.  For callers that cannot call cudaMalloc
- * when they need the sum: applications that hand all device memory to their
- * own pool or admit work against a fixed memory budget, and step loops where
- * a cudaMalloc/cudaFree pair would synchronise the device.  The split-K partial
- * sums go to a fixed array of FH_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) that
- * every GPU loading the library reserves until the process exits; the call
- * never allocates.  Limit: M*P <= FH_NOALLOC_SCRATCH_DOUBLES, else FH_ERANGE.
- * The first call on a device looks up the array's device address (and loads
- * the library's device code there): make that first call before any stream
- * capture.  All calls on a device share the array and it keeps the last
- * call's partials; calls whose GPU work overlaps (other streams or contexts
- * on the same device) race on it and must be serialised by the caller. */
+/* Allocation-free variant of fh_history_sum: same arguments, and the same
+ * sums within FP64 rounding (when M*P > FH_NOALLOC_SCRATCH_DOUBLES/16 the fixed
+ * array holds fewer split partials than fh_history_sum plans, so the layers are
+ * grouped into fewer, longer splits and the partials are added in another
+ * order).  No counterpart in the reference.  For callers that cannot call
+ * cudaMalloc when they need the sum: applications that hand all device memory
+ * to their own pool or admit work against a fixed memory budget, and step
+ * loops where a cudaMalloc/cudaFree pair would synchronise the device.  The
+ * split-K partial sums go to a fixed array of FH_NOALLOC_SCRATCH_DOUBLES
+ * doubles (16 MiB) that every GPU loading the library reserves until the
+ * process exits; the call never allocates.  Limit: M*P <=
+ * FH_NOALLOC_SCRATCH_DOUBLES, else FH_ERANGE; K has no limit (a split of any
+ * length stages its weights in pieces).  The first call on a device looks up
+ * the array's device address (and loads the library's device code there):
+ * make that first call before any stream capture.  All calls on a device share
+ * the array and it keeps the last call's partials; calls whose GPU work
+ * overlaps (other streams or contexts on the same device) race on it and must
+ * be serialised by the caller. */
 #define FH_NOALLOC_SCRATCH_DOUBLES 2097152LL
 int fh_history_sum_noalloc(fh_ctx *ctx, int M, int K, long long P, const double *W, int ldw,
                            const double *D, long long ldd, double *S, long long ldS);
@@ -139,7 +148,8 @@ int fh_history_sum_noalloc(fh_ctx *ctx, int M, int K, long long P, const double 
  * u_N = Bt_N/(1-Al_N) (right_mode 1); u_{N+1} = u_N.  System s uses entries
  * [s*lds, s*lds + N] of A, R, B, Om and [s*ldu, s*ldu + N+1] of u.
  * Replaces H_solver::al1/bt1/U1 (mt_minimal.cpp:829-858, 942-1031) and
- * TG_solver::U1 (fr_d_t_g_2d.cpp:2523-2551). */
+ * TG_solver::U1 (fr_d_t_g_2d.cpp:2523-2551).  Asynchronous on the context
+ * stream, with Al in the context's workspace (as fh_history_sum). */
 int fh_tridiag_batched(fh_ctx *ctx, int nsys, int N, const double *A, const double *R,
                        const double *B, const double *Om, long long lds, const double *al1,
                        const double *bt1, int right_mode, const double *u_right, double *u,
@@ -275,6 +285,13 @@ int fh_ab_set_c_host(fh_ab_solver *s, const double *C_host);
 int fh_ab_set_c(fh_ab_solver *s, const double *C);
 /* Override the current-step coefficient Ii (default: the lag-1 weight). */
 int fh_ab_set_current_coef(fh_ab_solver *s, double Ii);
+/* Replace the history weights of lags 1..n (w_host[l-1] = weight of lag l,
+ * before the first step) by a caller's table: the I_cache of MF_intF_simple
+ * (MF_int_series.cpp:614-718), whose entries MF_int_choice (523-530) takes
+ * from the integral-representation quadrature MF_intFv (469-521) once
+ * (a/(1-a)) (lag tau)^a >= 1, where that quadrature is a few percent from
+ * the converged series the library evaluates by default. */
+int fh_ab_set_lag_weights_host(fh_ab_solver *s, int n, const double *w_host);
 /* History mode, before the first step: FH_AB_FP64 (default, FP64 sums) or
  * FH_AB_BLOCKED (entries older than the current 128-step block contracted on
  * the tensor cores with exact bf16 slices, the rest in FP64; ~2x the history

@@ -194,6 +194,10 @@ class AB_solver {
     ctx_.check(fh_ab_set_source_host(s_, nrows, src, bl, br));
   }
   void set_current_coef(double Ii) { ctx_.check(fh_ab_set_current_coef(s_, Ii)); }
+  // the reference's lag-weight cache (MF_intF_simple I_cache), lags 1..n
+  void set_lag_weights(const std::vector<double> &w) {
+    ctx_.check(fh_ab_set_lag_weights_host(s_, (int)w.size(), w.data()));
+  }
   void set_state() {
     ctx_.check(fh_ab_set_c_host(s_, C.data()));
     step = 0;

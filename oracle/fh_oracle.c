@@ -14,34 +14,44 @@
 
 /* ------------------------------------------------------------------ weights */
 
-/* y^a * sum_j (1-b)_j y^j / (j! (a+j))  -- lower incomplete beta B(y; a, b). */
-static long double ib_lower(long double y, long double a, long double b) {
-  if (y <= 0.0L) return 0.0L;
-  long double s = 0.0L, c = 1.0L, yj = 1.0L;
+/* psi = t^beta interval weights (beta != 1), long double:
+ *   int_{x0 tau}^{x1 tau} (T^beta - s^beta)^(-alpha) ds = T^(1-alpha beta)/beta [B(y1) - B(y0)],
+ *   T = X tau, y = (x/X)^beta, B(y) = B(y; a, b) the lower incomplete beta, a = 1/beta, b = 1-alpha.
+ * The difference of the two incomplete-beta values is evaluated directly, from
+ * divided differences of its series, so that no leading digits cancel late in
+ * a solve:
+ *   lower side: B(y) = r P(y), r = x/X, P(y) = sum_j (1-b)_j y^j / (j! (a+j));
+ *               B(y1) - B(y0) = (r1 - r0) P(y0) + r1 (y1 - y0) P[y0, y1]
+ *   upper side: B(1) - B(y) = U(c) = c^b Q(c), c = 1 - y, Q(c) = sum_j (1-a)_j c^j / (j! (b+j));
+ *               U(c0) - U(c1) = (c0^b - c1^b) Q(c1) + c0^b (c0 - c1) Q[c1, c0]
+ * (P[u, v] = (P(v) - P(u)) / (v - u)).  This is the converged value of the
+ * integral that H_solver::calc_int / _kb_row (mt_psi_caputo.cpp:497-564,
+ * 720-741) sums as a series to global_eps. */
+
+/* S = sum_j c_j z0^j, D = sum_j c_j h_{j-1}(z0, z1) with c_j = (p)_j / (j! (q+j)),
+ * h_{j-1} = sum_{i<j} z0^i z1^(j-1-i) (so that D = the divided difference). */
+static void ib_series_dd(long double p, long double q, long double z0, long double z1, long double *S,
+                         long double *D) {
+  long double s = 0.0L, d = 0.0L, c = 1.0L, pw = 1.0L, h = 0.0L;
   for (int j = 0; j < 4000; ++j) {
-    long double t = c * yj / (a + (long double)j);
-    s += t;
-    if (fabsl(t) <= 1e-24L * fabsl(s)) break;
-    c *= ((long double)(j + 1) - b) / (long double)(j + 1);
-    yj *= y;
+    const long double cj = c / (q + (long double)j);
+    const long double ts = cj * pw, td = cj * h;
+    s += ts;
+    d += td;
+    if (j > 2 && fabsl(ts) <= 1e-24L * fabsl(s) && fabsl(td) <= 1e-24L * fabsl(d)) break;
+    h = z1 * h + pw;
+    pw *= z0;
+    c *= ((long double)j + p) / (long double)(j + 1);
     if (c == 0.0L) break;
   }
-  return powl(y, a) * s;
+  *S = s;
+  *D = d;
 }
 
-/* Upper tail B(1;a,b) - B(y;a,b) written in c = 1-y:  c^b sum_j (1-a)_j c^j/(j!(b+j)). */
-static long double ib_upper(long double c, long double a, long double b) {
-  if (c <= 0.0L) return 0.0L;
-  long double s = 0.0L, d = 1.0L, cj = 1.0L;
-  for (int j = 0; j < 4000; ++j) {
-    long double t = d * cj / (b + (long double)j);
-    s += t;
-    if (fabsl(t) <= 1e-24L * fabsl(s)) break;
-    d *= ((long double)(j + 1) - a) / (long double)(j + 1);
-    cj *= c;
-    if (d == 0.0L) break;
-  }
-  return powl(c, b) * s;
+static long double ib_series(long double p, long double q, long double z) {
+  long double S, D;
+  ib_series_dd(p, q, z, z, &S, &D);
+  return S;
 }
 
 double fho_psi_int(double x0, double x1, double X, double tau, double alpha, double beta) {
@@ -58,22 +68,38 @@ double fho_psi_int(double x0, double x1, double X, double tau, double alpha, dou
     sum += v2 * v;
     return sum;
   }
-  /* int_{t0}^{t1} (T^b - s^b)^(-a) ds = T^(1-a b)/b * [B(y1; 1/b, 1-a) - B(y0; 1/b, 1-a)],
-   * y = (s/T)^beta; complements 1-y taken through expm1/log1p. */
-  long double a = 1.0L / (long double)beta, b = 1.0L - (long double)alpha;
-  long double Xl = (long double)X;
-  long double y0 = powl((long double)x0 / Xl, (long double)beta);
-  long double y1 = powl((long double)x1 / Xl, (long double)beta);
-  long double c0 = (x0 >= X) ? 0.0L : -expm1l((long double)beta * log1pl(((long double)x0 - Xl) / Xl));
-  long double c1 = (x1 >= X) ? 0.0L : -expm1l((long double)beta * log1pl(((long double)x1 - Xl) / Xl));
+  const long double a = 1.0L / (long double)beta, b = 1.0L - (long double)alpha, be = (long double)beta;
+  const long double Xl = X, r0 = (long double)x0 / Xl, r1 = (long double)x1 / Xl;
+  const int zero0 = !(x0 > 0.0), top = !(x1 < X);
+  /* beta log(x/X) and beta log(x1/x0); y1 - y0 without cancellation */
+  const long double t1 = top ? 0.0L : be * log1pl(((long double)x1 - Xl) / Xl);
+  const long double t0 = zero0 ? 0.0L : be * log1pl(((long double)x0 - Xl) / Xl);
+  const long double td = zero0 ? 0.0L : be * log1pl(((long double)x1 - (long double)x0) / (long double)x0);
+  const long double y1 = top ? 1.0L : expl(t1), y0 = zero0 ? 0.0L : expl(t0);
+  const long double dy = zero0 ? y1 : y0 * expm1l(td);
   long double diff;
-  if (y1 <= 0.5L) {
-    diff = ib_lower(y1, a, b) - ib_lower(y0, a, b);
-  } else if (y0 > 0.5L) {
-    diff = ib_upper(c0, a, b) - ib_upper(c1, a, b);
+  if (y1 <= 0.55L) {
+    long double S, D;
+    ib_series_dd(1.0L - b, a, y0, y1, &S, &D);
+    const long double dr = ((long double)x1 - (long double)x0) / Xl; /* not r1 - r0 */
+    diff = zero0 ? r1 * ib_series(1.0L - b, a, y1) : dr * S + r1 * dy * D;
+  } else if (y0 >= 0.45L) {
+    const long double c1 = top ? 0.0L : -expm1l(t1), c0 = c1 + dy;
+    if (c1 <= 0.0L) {
+      diff = powl(c0, b) * ib_series(1.0L - a, b, c0);
+    } else {
+      long double S, D;
+      ib_series_dd(1.0L - a, b, c1, c0, &S, &D);
+      const long double c1b = powl(c1, b), dcb = c1b * expm1l(b * log1pl(dy / c1));
+      diff = dcb * S + (c1b + dcb) * dy * D;
+    }
   } else {
-    long double btot = expl(lgammal(a) + lgammal(b) - lgammal(a + b));
-    diff = (btot - ib_upper(c1, a, b)) - ib_lower(y0, a, b);
+    /* the interval spans both sides (X of a few steps) */
+    const long double btot = expl(lgammal(a) + lgammal(b) - lgammal(a + b));
+    const long double c1 = top ? 0.0L : -expm1l(t1);
+    const long double up = c1 <= 0.0L ? 0.0L : powl(c1, b) * ib_series(1.0L - a, b, c1);
+    const long double lo = zero0 ? 0.0L : r0 * ib_series(1.0L - b, a, y0);
+    diff = (btot - up) - lo;
   }
   long double T = Xl * (long double)tau;
   long double pre = powl(T, 1.0L - (long double)alpha * (long double)beta) / (long double)beta;
@@ -188,6 +214,15 @@ static void h_space_v(const fho_h_params *p, int N, double dL, const double *U, 
   }
 }
 
+/* +1 or -1 from a hash of (i, t): the sign pattern of fho_h_params.pert. */
+static double pert_sign(unsigned i, unsigned t) {
+  unsigned long long h = (i + 1ULL) * 0x9E3779B97F4A7C15ULL ^ (t + 1ULL) * 0xC2B2AE3D27D4EB4FULL;
+  h ^= h >> 29;
+  h *= 0xBF58476D1CE4E5B9ULL;
+  h ^= h >> 32;
+  return (h & 1ULL) ? 1.0 : -1.0;
+}
+
 int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
   if (!(p->gamma > 0.0 && p->gamma <= 1.0)) return 2; /* gamma in (0, 1] */
   const int N = p->N, ld = N + 2;
@@ -224,6 +259,10 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
       for (int t = 0; t < os - 1; ++t) w[t] = fho_psi_int(t, t + 1, tstep + 1, p->tau, a, p->beta) * (1 - a);
     }
     for (int i = 0; i <= N; ++i) K[i] = (p->kmodel == FHO_K_CONST) ? p->kc : p->kc * exp(p->kgam * U[i]);
+    if (p->pert != 0.0) {
+      for (int i = 0; i <= N; ++i) K[i] *= 1.0 + p->pert * pert_sign((unsigned)i, (unsigned)tstep);
+      for (int t = 0; t < os - 1; ++t) w[t] *= 1.0 + p->pert * pert_sign((unsigned)t + 100000u, (unsigned)tstep);
+    }
     if (frac) h_space_v(p, N, dL, U, F, V);
     for (int i = 1; i < N; ++i) {
       const double kbf = (frac && p->weights == FHO_W_PSI) ? fho_psi_int(i - 1, i, i, dL, p->gamma, 1.0) : 1.0;

@@ -73,6 +73,10 @@ typedef struct {
   double al_left, bt_left; /* u_0 = al_left*u_1 + bt_left                         */
   double u_right; /* Dirichlet value at node N                                    */
   double gamma;   /* space-derivative order (1: classical second derivative)      */
+  double pert;    /* 0 for the reference's arithmetic; e > 0 multiplies every K_i and
+                   * every history weight by 1 +- e (signs from a fixed hash of the
+                   * node or slot and the step): the run measures how far rounding-
+                   * level differences (another libm's exp or pow) move the solution */
 } fho_h_params;
 
 /* Runs `steps` calls of H_solver::calc_step (tstep starting at 1) on U (N+2 values,

@@ -27,7 +27,7 @@ class HParams(C.Structure):
                 ("weights", C.c_int), ("beta", C.c_double), ("kmodel", C.c_int),
                 ("kc", C.c_double), ("kgam", C.c_double), ("cinv", C.c_double),
                 ("gravity", C.c_int), ("al_left", C.c_double), ("bt_left", C.c_double),
-                ("u_right", C.c_double), ("gamma", C.c_double)]
+                ("u_right", C.c_double), ("gamma", C.c_double), ("pert", C.c_double)]
 
 
 class TGParams(C.Structure):
@@ -125,7 +125,7 @@ def thomas(A, R, B, Om, al1, bt1, right_mode, u_right, u) -> np.ndarray:
 
 def h_solve(params: dict, U0: np.ndarray, steps: int):
     """Returns (U, hist) after `steps` H_solver::calc_step calls."""
-    p = HParams(**{"gamma": 1.0, **params})  # gamma = 1: classical second derivative in z
+    p = HParams(**{"gamma": 1.0, "pert": 0.0, **params})  # gamma = 1: classical second derivative in z
     U = np.ascontiguousarray(U0, dtype=np.float64).copy()
     assert U.shape[0] == p.N + 2
     hist = np.zeros((max(steps, 1), p.N + 2))

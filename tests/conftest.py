@@ -27,3 +27,18 @@ def pytest_collection_modifyitems(config, items):
     for it in items:
         if "gpu" in it.keywords:
             it.add_marker(skip)
+
+
+def torch_ordered_context(device: int = 0):
+    """A library Context whose raw entry-point calls start after the work torch
+    has queued: the tests make their device buffers on torch's stream, and the
+    library runs on a stream of its own."""
+    import torch
+    from theses_code_gb300._lib import Context
+
+    class TorchOrdered(Context):
+        def call(self, name, *args):
+            torch.cuda.synchronize()
+            return super().call(name, *args)
+
+    return TorchOrdered(device)

@@ -112,10 +112,17 @@ def main():
         ml.append([a, b, z, r["ml"][0][0]])
     r = parse(run("ab", ["abw", 0.5, 0.01, 50]))
     abw = [[int(l), v] for l, v in r["abw"]]
-    ii = parse(run("ab", ["ii", 0.5, 0.5 / 50]))["ii"][0][0]
-    r = parse(run("ab", ["solve", 0.5, 0.5, 50, 10]))
+    # solve_and_check (full history, simple 1): error and the field of the last step
+    solves = []
+    for (a, T, n, m) in [(0.5, 0.5, 50, 10), (0.6, 1.0, 200, 64)]:
+        ii = parse(run("ab", ["ii", a, T / n]))["ii"][0][0]
+        r = parse(run("ab", ["field", a, T, n, m]))
+        c = [v for _, v in sorted((int(j), v) for j, v in r["c"])]
+        assert len(c) == m + 1
+        lag = [v for _, v in sorted((int(L), v) for L, v in parse(run("ab", ["ablag", a, T / n, n]))["ablag"])]
+        solves.append({"alpha": a, "T": T, "n": n, "m": m, "ii": ii, "err": r["err"][0][0], "C": c, "lagw": lag})
     dump("ab.json", {"ml": ml, "abw": {"alpha": 0.5, "tau": 0.01, "n": 50, "w": abw},
-                     "solve": {"alpha": 0.5, "T": 0.5, "n": 50, "m": 10, "ii": ii, "err": r["err"][0][0]}})
+                     "solve": solves[0], "solve2": solves[1]})
 
 
 if __name__ == "__main__":

@@ -6,6 +6,27 @@ import pytest
 from theses_code_gb300 import fit, workloads
 
 
+def oracle_runner(metric: int = 0):
+    """fit.gpu_runner's scoring with every candidate solved by the CPU oracle."""
+    from oracle import oracle as O
+
+    @fit._only_valid
+    def run(params_list, U0, tau, t_end, values):
+        tts = fit._schedule(tau, t_end)
+        steps = len(tts)
+        out = []
+        for p in params_list:
+            U, hist = O.h_solve(p, U0, steps)
+            before = [U0] + [hist[s] for s in range(steps - 1)]
+            after = [hist[s] for s in range(steps)]
+            N, dL = p["N"], p["L"] / p["N"]
+            sc = fit._score(before, after, tts, tau, dL, N, values, metric)
+            out.append(fit.BIG if not np.all(np.isfinite(U)) else sc)
+        return out
+
+    return run
+
+
 def _problem():
     from oracle import oracle as O
     params, U0s = workloads.psi_batch(n=1, seed=3, Nmin=40, Nmax=40, tau=2e-3)
@@ -29,7 +50,7 @@ def _problem():
 
 def test_oracle_driver_reduces_misfit():
     base, truth, U0, t_end, values = _problem()
-    run = fit.oracle_runner()
+    run = oracle_runner()
     assert run([truth], U0, base["tau"], t_end, values)[0] < 1e-20
     v_base = run([base], U0, base["tau"], t_end, values)[0]
     p, v, it, ns = fit.steepest_descent(run, base, ["alpha", "kc"], U0, t_end, values, vmax=[0.01, 0.01],
@@ -43,7 +64,7 @@ def test_gpu_driver_matches_oracle_driver():
     ctx = Context(0)
     base, truth, U0, t_end, values = _problem()
     kw = dict(vmax=[0.01, 0.01], eps=1e-9, max_iter=6)
-    pc, vc, itc, nc = fit.steepest_descent(fit.oracle_runner(), base, ["alpha", "kc"], U0, t_end, values, **kw)
+    pc, vc, itc, nc = fit.steepest_descent(oracle_runner(), base, ["alpha", "kc"], U0, t_end, values, **kw)
     pg, vg, itg, ng = fit.steepest_descent(fit.gpu_runner(ctx), base, ["alpha", "kc"], U0, t_end, values, **kw)
     assert (itg, ng) == (itc, nc)
     for k in ("alpha", "kc"):
@@ -54,7 +75,7 @@ def test_gpu_driver_matches_oracle_driver():
 
 def test_oracle_pso_reduces_misfit():
     base, truth, U0, t_end, values = _problem()
-    run = fit.oracle_runner()
+    run = oracle_runner()
     v_base = run([base], U0, base["tau"], t_end, values)[0]
     p, v, it, ns = fit.pso(run, base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end, values, n=8,
                            max_iter=4, seed=1)
@@ -70,7 +91,7 @@ def test_gpu_pso_matches_oracle_pso():
     base, truth, U0, t_end, values = _problem()
     kw = dict(n=8, max_iter=4, seed=1)
     b = [(0.55, 0.9), (0.2, 0.9)]
-    pc, vc, itc, nc = fit.pso(fit.oracle_runner(), base, ["alpha", "kc"], b, U0, t_end, values, **kw)
+    pc, vc, itc, nc = fit.pso(oracle_runner(), base, ["alpha", "kc"], b, U0, t_end, values, **kw)
     pg, vg, itg, ng = fit.pso(fit.gpu_runner(ctx), base, ["alpha", "kc"], b, U0, t_end, values, **kw)
     assert (itg, ng) == (itc, nc)
     for k in ("alpha", "kc"):
@@ -101,7 +122,7 @@ def test_fit_input_file_round_trip(tmp_path):
     assert U[3] == pytest.approx(-0.3 + (0.1 / 0.3) * 0.2)              # between 0.2 and 0.5
     assert U[10] == pytest.approx(-0.2 + 0.1 * (-0.2 - -0.1) / 0.4)     # extrapolated below the last
     U0f, t_endf, vals = FI.fit_problem(inp, base)
-    run = fit.oracle_runner()
+    run = oracle_runner()
     v0 = run([base], U0f, base["tau"], t_endf, vals)[0]
     p, v, it, ns = fit.steepest_descent(run, base, ["alpha", "kc"], U0f, t_endf, vals, vmax=[0.01, 0.01],
                                         eps=1e-9, max_iter=3)
@@ -133,7 +154,7 @@ def test_misfit_metrics():
 def test_oracle_adaptive_pso_runs():
     """The adaptive schedule (omega and per-coordinate fi) on the oracle."""
     base, truth, U0, t_end, values = _problem()
-    run = fit.oracle_runner()
+    run = oracle_runner()
     v_base = run([base], U0, base["tau"], t_end, values)[0]
     p, v, it, ns = fit.pso(run, base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end, values, n=8,
                            max_iter=4, seed=1, adaptive=True)
@@ -144,7 +165,7 @@ def test_oracle_pso_restarts():
     """With restart_prox = 1 and omega 0.5 about half the moves restart: the
     swarm takes another path than without restarts (same random stream)."""
     base, truth, U0, t_end, values = _problem()
-    run = fit.oracle_runner()
+    run = oracle_runner()
     kw = dict(n=8, omega=0.5, max_iter=2, seed=3)
     b = [(0.55, 0.9), (0.2, 0.9)]
     p1, v1, _, _ = fit.pso(run, base, ["alpha", "kc"], b, U0, t_end, values, restart_prox=1.0, **kw)
@@ -158,7 +179,7 @@ def test_pso_log_lines():
     import io
     base, truth, U0, t_end, values = _problem()
     buf = io.StringIO()
-    p, v, it, ns = fit.pso(fit.oracle_runner(), base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end,
+    p, v, it, ns = fit.pso(oracle_runner(), base, ["alpha", "kc"], [(0.55, 0.9), (0.2, 0.9)], U0, t_end,
                            values, n=4, max_iter=2, seed=2, log=buf)
     lines = buf.getvalue().splitlines()
     assert [l.split(" - ")[0] for l in lines[:4]] == ["#initial %d" % i for i in range(4)]

@@ -13,8 +13,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def ctx():
-    from theses_code_gb300._lib import Context
-    c = Context(0)
+    from conftest import torch_ordered_context
+    c = torch_ordered_context(0)
     yield c
     c.close()
 

@@ -1,0 +1,135 @@
+"""GPU parity at the benchmark configurations' own sizes: each solver path
+against the CPU oracle on the workloads the benchmark times (same generators,
+same seeds), with enough steps that the history carries hundreds to thousands
+of layers.
+
+  config 1: 1D Caputo L1, N = 200, the full 1000 steps
+  config 2: 2D ADI 512 x 512, 200 steps, FP64 / double-float / blocked
+  config 3: 4096 ragged psi-Caputo instances (D(u) = D0 exp(gamma u)),
+            500 steps; 16 sampled instances incl. the largest N vs the oracle
+  config 4: 1D Atangana-Baleanu, N = 2048, 2000 steps, FP64 / blocked
+
+The oracle runs in a pool of spawned processes where it would take minutes
+serially (the pool starts before the first GPU call of its test)."""
+import concurrent.futures as cf
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O
+
+TOL_SOLVER = 1e-12   # plain FP64 path (and double-float storage) vs the oracle
+TOL_MIXED = 1e-9     # mixed-precision tensor-core history vs the oracle
+
+
+def relmax(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from theses_code_gb300._lib import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _h_oracle(args):
+    p, U0, steps = args
+    from oracle import oracle as Oc
+    return Oc.h_solve(p, U0, steps)[0]
+
+
+def _pool(n):
+    return cf.ProcessPoolExecutor(max_workers=max(1, min(n, os.cpu_count() or 1)),
+                                  mp_context=mp.get_context("spawn"))
+
+
+def test_config1_full_run(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    p, U0 = workloads.caputo_1d(200, 0.8, 1.0, 1e-3)
+    steps = 1000
+    s = HSolverBatch(ctx, [p], steps + 1)
+    s.set_u([U0])
+    s.calc_step(steps)
+    ref, _ = O.h_solve(p, U0, steps)
+    assert relmax(s.get_u()[0], ref) <= TOL_SOLVER
+    s.close()
+
+
+def test_config2_512_grid(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FH_TG_DF64, FH_TG_FP64
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(512, 512, alpha=0.7, tau=5e-4, d=0.1, seed=11)
+    steps = 200
+    ref, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(ref, C0.reshape(-1)) > 1e-3  # the plume moved
+    for mode, tol in ((FH_TG_FP64, TOL_SOLVER), (FH_TG_DF64, TOL_SOLVER), (FH_TG_BLOCKED, TOL_MIXED)):
+        s = TGSolver(ctx, p, steps, mode)
+        s.set_state(V2, C0)
+        s.calc_step(steps)
+        assert relmax(s.get_c(), ref) <= tol, mode
+        s.close()
+
+
+def test_config3_4096_instances():
+    """Each sampled instance within 1e-12 of the oracle, or, where the instance
+    itself is that sensitive, within twice the distance by which the oracle
+    moves when every K_i = D0 exp(gamma u_i) and every history weight is
+    perturbed by one part in 2^53 (the size of the differences between two
+    libm's exp and pow, which the GPU and the CPU cannot avoid)."""
+    from theses_code_gb300 import workloads
+    params, U0s = workloads.psi_batch(n=4096, seed=7)
+    steps = 500
+    idx = sorted(set(int(k) for k in np.random.default_rng(1).choice(4096, 15, replace=False))
+                 | {int(np.argmax([q["N"] for q in params]))})
+    assert len(idx) == 16
+    jobs = [(params[k], U0s[k], steps) for k in idx] + [(dict(params[k], pert=2.0 ** -53), U0s[k], steps) for k in idx]
+    # the oracle pool starts before the first GPU call of this test
+    with _pool(len(jobs)) as ex:
+        fut = ex.map(_h_oracle, jobs)
+        from theses_code_gb300._lib import Context
+        from theses_code_gb300.solvers import HSolverBatch
+        c = Context(0)
+        s = HSolverBatch(c, params, steps + 1)
+        s.set_u(U0s)
+        s.calc_step(steps)
+        got = s.get_u()
+        s.close()
+        c.close()
+        res = list(fut)
+    refs, perts = res[:len(idx)], res[len(idx):]
+    report = {}
+    for k, r, q in zip(idx, refs, perts):
+        err, sens = relmax(got[k], r), relmax(q, r)
+        report[k] = (err, sens)
+        assert err <= max(TOL_SOLVER, 2.0 * sens), (k, err, sens)
+    print("config 3 (err, sensitivity):", report)
+    # most instances are not that sensitive: those meet 1e-12 outright
+    assert sum(e <= TOL_SOLVER for e, _ in report.values()) >= 14, report
+
+
+def test_config4_2048_line(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_AB_BLOCKED, FH_AB_FP64
+    from theses_code_gb300.solvers import ABSolver
+    cfg, src, bl, br, C0 = workloads.ab_1d(m=2048, alpha=0.6, tau=1e-4, seed=5)
+    n = 2000
+    w = O.ab_weights(n, cfg["tau"], cfg["alpha"])
+    srcs = np.repeat(src, n, axis=0)
+    ref, _ = O.ab_solve(cfg["m"], n, cfg["tau"], cfg["alpha"], w, srcs, np.zeros(n), np.zeros(n), C0)
+    for mode, tol in ((FH_AB_FP64, TOL_SOLVER), (FH_AB_BLOCKED, TOL_MIXED)):
+        s = ABSolver(ctx, cfg["m"], n, cfg["tau"], cfg["alpha"], mode)
+        s.set_source(src, bl, br)
+        s.set_c(C0)
+        s.calc_step(n)
+        assert relmax(s.get_c(), ref) <= tol, mode
+        s.close()

@@ -116,6 +116,28 @@ def test_psi_weights_match_reference_series():
                 assert abs(o - val) <= 1e-9 * abs(val), (key, a, t0, o, val)
 
 
+def test_psi_weights_match_incomplete_beta():
+    """The oracle's psi = t^beta weights against mpmath's incomplete beta
+    function at 40 digits, T^(1-a b)/b * betainc(1/b, 1-a, y0, y1), over early,
+    middle and late intervals of long solves (where the difference of the two
+    incomplete-beta values loses log10(X) digits if it is formed directly)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(3)
+    for alpha, beta in [(0.6, 0.5), (0.8, 2.0), (0.55, 1.37), (0.9, 0.75), (0.5, 2.0), (0.7, 1.3)]:
+        for X, tau in [(2.0, 1e-3), (7.0, 1e-3), (60.5, 1e-3), (500.5, 5e-4), (5001.0, 1e-3)]:
+            ks = {0, 1, int(X) - 2, int(X) - 1} | {int(k) for k in rng.integers(0, int(X - 1), 6)}
+            for k in sorted(ks):
+                x0, x1 = float(k), min(k + 1.0, X)
+                if not 0.0 <= x0 < X:
+                    continue
+                Xm, b = mp.mpf(X), mp.mpf(beta)
+                ref = (Xm * tau) ** (1 - mp.mpf(alpha) * b) / b * mp.betainc(
+                    1 / b, 1 - mp.mpf(alpha), (mp.mpf(x0) / Xm) ** b, (mp.mpf(x1) / Xm) ** b)
+                got = O.psi_int(x0, x1, X, tau, alpha, beta)
+                assert abs(got - float(ref)) <= 4e-16 * abs(float(ref)), (alpha, beta, X, k)
+
+
 def test_psi_t_is_l1():
     """For psi = t the psi-Caputo weight is the L1 coefficient times tau^(1-a)/(1-a)."""
     for alpha in (0.3, 0.7, 0.95):
@@ -144,17 +166,30 @@ def test_ab_lag_weights_match_reference():
             assert abs(O.ab_int(lag, v["tau"], v["alpha"]) - val) <= 1e-12 * abs(val)
 
 
-def test_ab_solve_matches_reference():
-    s = load("ab.json")["solve"]
+@pytest.mark.parametrize("key", ["solve", "solve2"])
+def test_ab_solve_matches_reference(key):
+    """solve_and_check (full history) with the reference's own current-step
+    coefficient and lag-weight cache (MF_intF_simple's I_cache: the converged
+    series while (a/(1-a)) (lag tau)^a < 1, the MF_intFv quadrature beyond, up
+    to 1e-5 from the series): the field of the last step and the mean-squared
+    error."""
+    s = load("ab.json")[key]
     m, n, a = s["m"], s["n"], s["alpha"]
     tau = s["T"] / n
-    w = O.ab_weights(n, tau, a)
+    w = np.zeros(n + 1)
+    w[1:] = s["lagw"]
     w[0] = s["ii"]
+    conv = O.ab_weights(n, tau, a)  # the converged series: equal where the reference sums the series
+    for L in range(2, n + 1):
+        if (a / (1 - a)) * (L * tau) ** a < 1.0:
+            assert abs(conv[L] - w[L]) <= 1e-13 * abs(w[L]), L
     lam = -a / (1 - a)
     src = np.array([[(24.0 / (1 - a)) * (i * tau) ** 4 * O.mittag_leffler(a, 5.0, lam * (i * tau) ** a)
                      for _ in range(m + 1)] for i in range(1, n + 1)])
     ex = np.array([[(i * tau) ** 4 for _ in range(m + 1)] for i in range(1, n + 1)])
-    _, err = O.ab_solve(m, n, tau, a, w, src, ex[:, 0].copy(), ex[:, -1].copy(), np.zeros(m + 1), ex)
+    c, err = O.ab_solve(m, n, tau, a, w, src, ex[:, 0].copy(), ex[:, -1].copy(), np.zeros(m + 1), ex)
+    ref = np.array(s["C"])
+    assert np.max(np.abs(c - ref)) <= 1e-13 * np.max(np.abs(ref))
     assert abs(err - s["err"]) <= 1e-12 * s["err"]
 
 

@@ -86,6 +86,7 @@ _SIGS = {
     "fh_ab_set_c_host": (_i, [_vp, _dp]),
     "fh_ab_set_c": (_i, [_vp, _dp]),
     "fh_ab_set_current_coef": (_i, [_vp, _d]),
+    "fh_ab_set_lag_weights_host": (_i, [_vp, _i, _dp]),
     "fh_ab_step": (_i, [_vp, _i]),
     "fh_ab_set_mode": (_i, [_vp, _i]),
     "fh_h_batch_set_mode": (_i, [_vp, _i]),

@@ -6,6 +6,8 @@
 // history stores dC_t/tau = (C^{t+1}-C^t)/tau per node.  The matrix is the same
 // every step, so its elimination coefficients are built once and every step
 // runs the two affine recurrences with one warp (see fh_linescan.cuh).
+#include <cmath>
+
 #include "fh_internal.h"
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
@@ -610,6 +612,23 @@ int fh_ab_set_current_coef(fh_ab_solver *s, double Ii) {
                                         s->pb.as<double>());
   const int rc = fh_after_launch(ctx, "k_ab_factor");
   return rc ? rc : ab_table_pairs(s);
+}
+
+int fh_ab_set_lag_weights_host(fh_ab_solver *s, int n, const double *w_host) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, w_host && n >= 1 && n <= s->max_steps + 1, FH_EINVAL,
+             "fh_ab_set_lag_weights_host: need 1 <= n <= max_steps + 1 and a table");
+  FH_REQUIRE(ctx, s->step == 0, FH_EINVAL, "fh_ab_set_lag_weights_host: only before the first step");
+  for (int l = 0; l < n; ++l)
+    FH_REQUIRE(ctx, std::isfinite(w_host[l]), FH_ENONFINITE, "fh_ab_set_lag_weights_host: weight of lag %d", l + 1);
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->w.as<double>() + 1, w_host, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  int rc;
+  if (s->w2.p && (rc = ab_pairs(ctx, s->w.as<double>(), s->w2.as<float2>(), s->max_steps + 2, 0))) return rc;
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  s->graph.reset();
+  return FH_OK;
 }
 
 int fh_ab_set_mode(fh_ab_solver *s, int mode) {

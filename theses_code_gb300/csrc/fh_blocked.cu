@@ -596,15 +596,12 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
     return rc;
   if ((rc = make_map(ctx, &b.mapA, b.A3.p, (unsigned long long)Kcap, kBM, kBM))) return rc;
   if ((rc = make_map(ctx, &b.mapB, b.H3.p, (unsigned long long)Kcap, (unsigned long long)b.Ppad, kBN))) return rc;
-  static bool attr = false;
-  if (!attr) {
-    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_far_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
-    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(sizeof(double) * 2 * kBK * 64)));
-    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(2 * kCvSmemPerChunk)));
-    attr = true;
-  }
+  // shared-memory opt-ins on this context's device (per device, so on every init)
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_far_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(double) * 2 * kBK * 64)));
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(2 * kCvSmemPerChunk)));
   return FH_OK;
 }
 

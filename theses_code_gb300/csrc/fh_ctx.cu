@@ -19,6 +19,16 @@ int fh_after_launch(fh_ctx *ctx, const char *what) {
   return FH_OK;
 }
 
+int fh_ctx_work(fh_ctx *ctx, size_t bytes, void **out) {
+  if (ctx->work.bytes < bytes) {
+    FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // earlier calls may still use the old buffer
+    const int rc = fh_alloc(ctx, ctx->work, bytes + bytes / 4, false);
+    if (rc) return rc;
+  }
+  *out = ctx->work.p;
+  return FH_OK;
+}
+
 int fh_alloc(fh_ctx *ctx, fh_dbuf &b, size_t bytes, bool zero) {
   b.release();
   if (bytes == 0) bytes = 16;

@@ -52,6 +52,9 @@ struct fh_h_batch {
   fh_graph_cache graph;
   bool use_graph = true;
   int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
+  // Al of the variable-coefficient instances serially in the reference order
+  // (h_alpha_serial); varcoef: the batch has such instances
+  bool serial_al = true, varcoef = false;
   std::vector<fh_h_dev_inst> di;  // host copy of inst
   // space-fractional instances: Toeplitz weights wsp and the sums sV per
   // node (state layout), shared memory of k_h_space_v
@@ -78,97 +81,82 @@ static constexpr int kTileShapes[3] = {128, 256, 512};  // candidate tile CTAs
 static inline int tile_shape_index(int threads) { return threads == 128 ? 0 : threads == 256 ? 1 : 2; }
 static constexpr int kLineCtaMaxInst = 152;  // batches below this many instances solve one CTA per instance
 static constexpr int kSpaceMaxN = 2048;  // nodes of a space-fractional instance (shared-memory sums)
-static constexpr int kHWeightThreads = 128;                 // nodes per weights CTA
-static constexpr int kHWeightSlots = kHWeightThreads - 1;  // slots per weights CTA
-// per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | 2^(-1/beta) |
+static constexpr int kHWeightThreads = 128;                 // slots per weights CTA
+// per psi instance: Lc[kIbTerms] | Uc[kIbTerms] | B(a, b) | kIbLowMax^(1/beta) |
 // log tau | 1/beta
 static constexpr int kIbStride = 2 * kIbTerms + 4;
 
 // ------------------------------------------------------------------ kernels
 
-// Row b of W: the weights of instance b for the history slots t = 0..os-2.
-// The reference's t = 0 term multiplies layer1 - layer1 (its layer pointer
-// starts at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
-// CTA (x, b) owns slots x*127 .. x*127+126 of instance b.
+// Row b of W: the weights of instance b for the history slots t = 0..os-2,
+// and wc[b], the weight of the current slot [tstep, tstep + 1].  The
+// reference's t = 0 term multiplies layer1 - layer1 (its layer pointer starts
+// at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
+// Thread i of CTA (x, b) owns slot i = x*128 + threadIdx.x; i = max(os - 1, 0)
+// is the current slot.
 __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
                             int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
                             const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX) {
   const int b = blockIdx.y;
-  const int i = blockIdx.x * kHWeightSlots + threadIdx.x;  // node index; slot index below kHWeightSlots
+  const int i = blockIdx.x * kHWeightThreads + threadIdx.x;
+  const int nh = os > 1 ? os - 1 : 0;  // history slots
+  if (i > nh) return;
   const fh_h_dev_inst I = inst[b];
+  const bool cur = i == nh;
   if (I.weights == FH_W_PSI && I.beta != 1.0) {
-    // psi = t^beta: the weight of slot t is the difference of one incomplete-beta
-    // value at its two ends (fh_psi_int_tab).  One node per thread, shared with
-    // the neighbouring slot through shared memory: node i < os sits at x = i,
-    // node os at x = tstep, the lower end of the current slot [tstep, tstep+1]
-    // whose upper end x = X has value 0 in the upper form.
-    __shared__ double nv[kHWeightThreads], sc;
-    __shared__ int nlow[kHWeightThreads];
-    const double X = (double)(tstep + 1), bb = 1.0 - I.alpha;
+    // psi = t^beta: the interval [x0, x0 + 1] in the divided-difference form of
+    // fh_ib_diff, with the per-instance series tables and the logs as
+    // double-doubles from the table of log(x)
+    if (i == 0 && !cur) {
+      W[(long long)b * ldw] = 0.0;
+      return;
+    }
     const double *Lc = ibt + (long long)b * kIbStride, *Uc = Lc + kIbTerms;
-    const int k = threadIdx.x;
-    if (i <= os) {
-      const int xi = i < os ? i : tstep;
-      if (xi == 0) {
-        nv[k] = 0.0;
-        nlow[k] = 1;
-      } else {
-        // t = beta log(x/X) as a double-double from the table of log(x)
-        // (|log X| > |log x|, so the head difference is a fast two-sum)
-        const double2 lx = lgt[xi], lX = lgt[tstep + 1];
-        const double sh = lx.x - lX.x;
-        const double sl = (lx.x - (sh + lX.x)) + (lx.y - lX.y);
-        const double th = I.beta * sh;
-        const double tl = fma(I.beta, sh, -th) + I.beta * sl;
-        const double r = (double)xi * invX;
-        if (r <= Lc[2 * kIbTerms + 1]) {  // y = r^beta <= 1/2: lower series in y
-          const double ey = exp(th);
-          const double y = fma(ey, tl, ey);
-          nv[k] = r * fh_horner_n(Lc, y, fh_ib_nterms(y));
-          nlow[k] = 1;
-        } else {  // upper tail in c = 1 - y = -expm1(t)
-          const double em = expm1(th);
-          const double c = -fma(em + 1.0, tl, em);
-          // c^(1-alpha) as exp((1-alpha) log c): |(1-alpha) log c| < 5 here, so
-          // the exponent carries ~5e-16 absolute error (pow: ~1e-16) at less
-          // than half of pow's FP64 instructions
-          nv[k] = c <= 0.0 ? 0.0 : exp(bb * log(c)) * fh_horner_n(Uc, c, fh_ib_nterms(c));
-          nlow[k] = 0;
-        }
-      }
-    }
+    const int X = tstep + 1, x0 = cur ? tstep : i, x1 = x0 + 1;
+    // p - q as a double-double for log values 0 <= p <= q (fast two-sum)
+    auto dd_sub = [](double2 p, double2 q, double &h, double &l) {
+      h = p.x - q.x;
+      l = (p.x - (h + q.x)) + (p.y - q.y);
+    };
+    const double2 lX = lgt[X], l0 = lgt[x0], l1 = lgt[x1];
+    fh_ib_slot q;
+    q.zero0 = x0 == 0;
+    q.top = x1 == X;
+    q.r0 = (double)x0 * invX;
+    q.r1 = (double)x1 * invX;
+    q.dr = invX;
+    dd_sub(l1, lX, q.l1h, q.l1l);  // log(x1/X)
+    dd_sub(l0, lX, q.l0h, q.l0l);  // log(x0/X)
+    dd_sub(l0, l1, q.ldh, q.ldl);  // log(x0/x1) = -log(x1/x0)
+    q.ldh = -q.ldh;
+    q.ldl = -q.ldl;
+    const double bb = 1.0 - I.alpha;
+    const double diff = fh_ib_diff(q, I.beta, bb, Lc[2 * kIbTerms + 1], [&] { return Lc[2 * kIbTerms]; },
+                                   fh_ib_coef_tab{Lc}, fh_ib_coef_tab{Uc});
     // (X tau)^(1 - alpha beta) / beta with log X from the table: one exp
-    if (k == kHWeightThreads - 1)
-      sc = exp((1.0 - I.alpha * I.beta) * (lgt[tstep + 1].x + Lc[2 * kIbTerms + 2])) * Lc[2 * kIbTerms + 3];
-    __syncthreads();
-    if (k < kHWeightSlots && i < os - 1) {
-      double diff;
-      if (nlow[k] && nlow[k + 1])
-        diff = nv[k + 1] - nv[k];
-      else if (!nlow[k])
-        diff = nv[k] - nv[k + 1];
-      else
-        diff = (Lc[2 * kIbTerms] - nv[k + 1]) - nv[k];
-      W[(long long)b * ldw + i] = i == 0 ? 0.0 : sc * diff * (1 - I.alpha);
-    }
-    if (i == os && k < kHWeightSlots) wc[b] = sc * (nlow[k] ? Lc[2 * kIbTerms] - nv[k] : nv[k]) * (1 - I.alpha);
+    const double sc = exp((1.0 - I.alpha * I.beta) * (lX.x + Lc[2 * kIbTerms + 2])) * Lc[2 * kIbTerms + 3];
+    const double w = sc * diff * (1 - I.alpha);
+    if (cur)
+      wc[b] = w;
+    else
+      W[(long long)b * ldw + i] = w;
     return;
   }
   const int t = i;
-  if (threadIdx.x < kHWeightSlots && t < os - 1) {
+  if (!cur) {
     double w;
     if (t == 0)
       w = 0.0;
     else if (I.weights == FH_W_L1)
       w = Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
     else
-      w = fh_psi_int((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) * (1 - I.alpha);
+      w = fh_psi_int_t((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha) * (1 - I.alpha);
     W[(long long)b * ldw + t] = w;
   }
-  if (i == 0) {
+  else {
     wc[b] = (I.weights == FH_W_L1)
                 ? 1.0
-                : fh_psi_int((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha, I.beta) *
+                : fh_psi_int_t((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha) *
                       (1 - I.alpha);
   }
 }
@@ -183,7 +171,7 @@ __global__ void k_h_ibtab(const fh_h_dev_inst *__restrict__ inst, int n, double 
   double *row = ibt + (long long)b * kIbStride;
   fh_ib_tables(a, bb, row, row + kIbTerms);
   row[2 * kIbTerms] = exp(lgamma(a) + lgamma(bb) - lgamma(a + bb));  // B(a, b)
-  row[2 * kIbTerms + 1] = pow(0.5, a);                               // y <= 1/2 <=> x/X <= 2^(-1/beta)
+  row[2 * kIbTerms + 1] = pow(kIbLowMax, a);                         // y <= kIbLowMax <=> x/X <= this
   row[2 * kIbTerms + 2] = log(I.tau);
   row[2 * kIbTerms + 3] = a;                                          // 1/beta
 }
@@ -305,7 +293,7 @@ __global__ void k_h_spw(const fh_h_dev_inst *__restrict__ inst, double *__restri
   for (int m = 1 + blockIdx.x * blockDim.x + threadIdx.x; m < I.N; m += gridDim.x * blockDim.x)
     wsp[I.off + m] = I.weights == FH_W_L1
                          ? pow((double)m + 1, I.spA) - pow((double)m, I.spA)
-                         : I.spA * fh_psi_int(0.0, 1.0, (double)m + 1.0, I.dL, I.spg, 1.0);
+                         : I.spA * fh_psi_int_t(0.0, 1.0, (double)m + 1.0, I.dL, I.spg);
 }
 
 // V_i of one instance per CTA (F and the weights in shared memory), i =
@@ -378,27 +366,68 @@ struct HGroup<1> {
   static __device__ __forceinline__ void sync() { __syncwarp(); }
 };
 
+// Parts of the line solve one launch runs: everything (kLineAll), the
+// coefficients and right parts only (kLineCoef), or the sweeps from an Al
+// already in memory (kLineSolve; k_h_alpha_lanes writes it in between).
+enum { kLineAll = 0, kLineCoef = 1, kLineSolve = 2 };
+
+// Al[i+1] = B_i / (R_i - A_i Al[i]) for i = 1..N-1 from Al[1], serially in the
+// order and arithmetic of H_solver::al1 (mt_psi_caputo.cpp:1262-1292,
+// mt_minimal.cpp:829-858): the product, the difference and the quotient are
+// each rounded once (no contraction), so the factors are those of the
+// reference for the same coefficients.  The Thomas factors of a diffusion line
+// are a weakly contracting recurrence: any re-association of it (a parallel
+// scan) changes every factor by a few ulps, and over hundreds of steps of a
+// 1000-node line those changes grew to 1e-10 of the solution.
+__device__ __forceinline__ void h_alpha_serial(int N, double al_left, const double *__restrict__ A,
+                                               const double *__restrict__ B, const double *__restrict__ R,
+                                               double *__restrict__ Al) {
+  double a = al_left;
+  Al[1] = a;
+  int i = 1;
+  for (; i + 4 <= N; i += 4) {  // coefficient loads ahead of the dependent chain
+    double Aq[4], Bq[4], Rq[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      Aq[k] = A[i + k];
+      Bq[k] = B[i + k];
+      Rq[k] = R[i + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a = __ddiv_rn(Bq[k], __dsub_rn(Rq[k], __dmul_rn(Aq[k], a)));
+      Al[i + k + 1] = a;
+    }
+  }
+  for (; i < N; ++i) {
+    a = __ddiv_rn(B[i], __dsub_rn(R[i], __dmul_rn(A[i], a)));
+    Al[i + 1] = a;
+  }
+}
+
 // One instance by a group of 32 NW threads; `lane` is the thread's index in
-// the group (its chunk of consecutive equations).
-template <int NW, bool SPACE>
+// the group (its chunk of consecutive equations).  serial: Al of the
+// variable-coefficient instances serially (h_alpha_serial, by lane 0 in
+// kLineAll launches); otherwise by the Moebius scan (kLineAll only).
+template <int NW, bool SPACE, int PH>
 __device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, double *__restrict__ U,
                                        const double *__restrict__ wc, const double *__restrict__ part,
                                        long long ldpart, int splits, double *__restrict__ Al,
                                        double *__restrict__ Bt, double *__restrict__ sA, double *__restrict__ sB,
                                        double *__restrict__ sR, double *__restrict__ sOm, double *__restrict__ Dnew,
                                        int append, int first, int dfstore, const double *__restrict__ sV,
-                                       fh_mob *smm, fh_aff *sma) {
+                                       fh_mob *smm, fh_aff *sma, int serial) {
   constexpr int TG = 32 * NW;
   const long long o = I.off;
   double *u = U + o;
   const int N = I.N;
   const double DaW = I.Da * wc[b];
-  const double idL = 1.0 / I.dL;
-  // ---- pass 1: coefficients of equations i in [f0, f1), chunk Moebius map
+  // ---- pass 1: coefficients of equations i in [f0, f1), chunk Moebius map;
+  // the products and sums in the reference's order, each rounded once
   const int chf = (N - 1 + TG - 1) / TG;
   const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
   fh_mob T{1.0, 0.0, 0.0, 1.0};
-  if (f0 < f1) {
+  if (PH != kLineSolve && f0 < f1) {
     double Km = fh_h_K(I, u[f0 - 1]), Kc = fh_h_K(I, u[f0]);
     for (int i = f0; i < f1; ++i) {
       const double Kp = fh_h_K(I, u[i + 1]);
@@ -412,20 +441,21 @@ __device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, 
           B = B * I.kbf * I.spA;
           R = R * I.kbf * I.spA;
         }
-        om = -I.Dg * I.cinv * (Kc * sV[o + i] - Km * sV[o + i - 1]) - DaW * u[i];
+        const double flux = __dsub_rn(__dmul_rn(Kc, sV[o + i]), __dmul_rn(Km, sV[o + i - 1]));
+        om = __dsub_rn(-I.Dg * I.cinv * flux, DaW * u[i]);
       }
-      R += DaW;
-      if (I.gravity) om += (Kc - Km) * idL;
+      R = __dadd_rn(R, DaW);
+      if (I.gravity) om = __dadd_rn(om, __ddiv_rn(Kc - Km, I.dL));
       double ts = 0.0;
       for (int s = 0; s < splits; ++s) ts += part[(long long)s * ldpart + o + i];
-      om += I.Da * ts;
+      om = __dadd_rn(om, __dmul_rn(I.Da, ts));
       sOm[o + i] = om;
       if (!I.fixed || first) {
         sA[o + i] = A;
         sB[o + i] = B;
         sR[o + i] = R;
       }
-      if (!I.fixed) {
+      if (!I.fixed && !serial) {
         T = fh_mob_compose(fh_mob{0.0, B, -A, R}, T);
         if (((i - f0) & 7) == 7) T = fh_mob_normalise(T);
       }
@@ -433,24 +463,20 @@ __device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, 
       Kc = Kp;
     }
   }
+  if (PH == kLineCoef) return;
   fh_aff F{1.0, 0.0};
-  if (I.fixed) {
-    // constant coefficients: Al[i+1] and Al[i+1]/B_i are computed once,
-    // serially in the reference order, and kept (Al, sR) for later steps
-    if (first) {
+  if (I.fixed || serial) {
+    // Al serially in the reference order (h_alpha_serial): once for constant
+    // coefficients (kept for later steps), every step otherwise; then
+    // sR[i] = Al[i+1] / B_i, the reference's factor of the Bt recurrence
+    const bool need = I.fixed ? first : PH == kLineAll;
+    if (need) {
       HGroup<NW>::sync();
-      if (lane == 0) {
-        double a = I.al_left;
-        Al[o + 1] = a;
-        for (int i = 1; i < N; ++i) {
-          const double B = sB[o + i];
-          a = B / (sR[o + i] - sA[o + i] * a);
-          Al[o + i + 1] = a;
-          sR[o + i] = a / B;
-        }
-      }
+      if (lane == 0) h_alpha_serial(N, I.al_left, sA + o, sB + o, sR + o, Al + o);
       HGroup<NW>::sync();
     }
+    if (!I.fixed || first)
+      for (int i = f0; i < f1; ++i) sR[o + i] = __ddiv_rn(Al[o + i + 1], sB[o + i]);
     for (int i = f0; i < f1; ++i) {
       const double gq = sR[o + i];
       F = fh_aff_compose(fh_aff{gq * sA[o + i], -(gq * sOm[o + i])}, F);
@@ -506,10 +532,11 @@ __device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, 
 }
 
 // SPACE: the batch has space-fractional instances (a separate instantiation
-// keeps the registers of the classical path).
-// Seven resident CTAs per SM (registers <= 73) keep 4096 instances (1024
-// CTAs) in one wave on 152 SMs.
-template <bool SPACE>
+// keeps the registers of the classical path).  PH: the part of the line solve
+// (kLineAll with the Moebius scan for Al, or kLineCoef / kLineSolve around
+// k_h_alpha_lanes).  Seven resident CTAs per SM (registers <= 73) keep 4096
+// instances (1024 CTAs) in one wave on 152 SMs.
+template <bool SPACE, int PH>
 __global__ void __launch_bounds__(128, 7) k_h_line_warp(const fh_h_dev_inst *__restrict__ inst, int n,
                                                      double *__restrict__ U, const double *__restrict__ wc,
                                                      const double *__restrict__ part, long long ldpart, int splits,
@@ -520,23 +547,38 @@ __global__ void __launch_bounds__(128, 7) k_h_line_warp(const fh_h_dev_inst *__r
                                                      int dfstore, const double *__restrict__ sV) {
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (b >= n) return;  // whole warp
-  h_line<1, SPACE>(inst[b], b, threadIdx.x & 31, U, wc, part, ldpart, splits, Al, Bt, sA, sB, sR, sOm, Dnew, append,
-                   first, dfstore, sV, nullptr, nullptr);
+  h_line<1, SPACE, PH>(inst[b], b, threadIdx.x & 31, U, wc, part, ldpart, splits, Al, Bt, sA, sB, sR, sOm, Dnew,
+                       append, first, dfstore, sV, nullptr, nullptr, PH != kLineAll);
+}
+
+// Al of every variable-coefficient instance (h_alpha_serial), one lane per
+// instance: the chain is FP64 latency (~650 cycles per equation on GB300), so
+// 32 instances share each warp instruction, and one warp per CTA spreads the
+// chains over the SMs.
+__global__ void __launch_bounds__(32) k_h_alpha_lanes(const fh_h_dev_inst *__restrict__ inst, int n,
+                                                      const double *__restrict__ sA, const double *__restrict__ sB,
+                                                      const double *__restrict__ sR, double *__restrict__ Al) {
+  const int b = blockIdx.x * 32 + threadIdx.x;
+  if (b >= n) return;
+  const fh_h_dev_inst I = inst[b];
+  if (I.fixed) return;
+  h_alpha_serial(I.N, I.al_left, sA + I.off, sB + I.off, sR + I.off, Al + I.off);
 }
 
 // Small batches (fewer instances than SMs): one CTA of kLineCtaWarps warps per
-// instance, so that each thread walks ~N/256 equations instead of ~N/32.
+// instance, so that each thread walks ~N/256 equations instead of ~N/32; Al
+// serially by thread 0 (serial != 0) or by the Moebius scan.
 static constexpr int kLineCtaWarps = 8;
 template <bool SPACE>
 __global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
     const fh_h_dev_inst *__restrict__ inst, double *__restrict__ U, const double *__restrict__ wc,
     const double *__restrict__ part, long long ldpart, int splits, double *__restrict__ Al, double *__restrict__ Bt,
     double *__restrict__ sA, double *__restrict__ sB, double *__restrict__ sR, double *__restrict__ sOm,
-    double *__restrict__ Dnew, int append, int first, int dfstore, const double *__restrict__ sV) {
+    double *__restrict__ Dnew, int append, int first, int dfstore, const double *__restrict__ sV, int serial) {
   __shared__ fh_mob smm[kLineCtaWarps];
   __shared__ fh_aff sma[kLineCtaWarps];
-  h_line<kLineCtaWarps, SPACE>(inst[blockIdx.x], blockIdx.x, threadIdx.x, U, wc, part, ldpart, splits, Al, Bt, sA, sB,
-                               sR, sOm, Dnew, append, first, dfstore, sV, smm, sma);
+  h_line<kLineCtaWarps, SPACE, kLineAll>(inst[blockIdx.x], blockIdx.x, threadIdx.x, U, wc, part, ldpart, splits, Al,
+                                         Bt, sA, sB, sR, sOm, Dnew, append, first, dfstore, sV, smm, sma, serial);
 }
 
 // ------------------------------------------------------------------- host
@@ -583,7 +625,7 @@ static int h_hist(fh_h_batch *B, int ti, int K, int splits, int kchunk, const do
 static int h_weights(fh_h_batch *B, int tstep, int os, int par, cudaStream_t st) {
   fh_ctx *ctx = B->ctx;
   FH_REQUIRE(ctx, tstep + 1 < B->max_steps + 2, FH_EINVAL, "h_weights: step %d beyond the log table", tstep);
-  dim3 gw((unsigned)(os / kHWeightSlots + 1), (unsigned)B->n);  // nodes 0..os
+  dim3 gw((unsigned)((os > 1 ? os - 1 : 0) / kHWeightThreads + 1), (unsigned)B->n);  // history slots + current
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, false, st);
   k_h_weights<<<gw, kHWeightThreads, 0, st>>>(B->inst.as<fh_h_dev_inst>(), B->n, tstep, os, B->Wp(par), B->max_weights,
                                               B->wcp(par), B->Lb.as<double>(), B->ibt.as<double>(),
@@ -650,20 +692,38 @@ static int h_one_step(fh_h_batch *B, bool next) {
     double *Al = B->Al.as<double>(), *Bt = B->Bt.as<double>(), *sA = B->sA.as<double>(), *sB = B->sB.as<double>();
     double *sR = B->sR.as<double>(), *sOm = B->sOm.as<double>(), *U = B->U.as<double>();
     const double *part = B->part.as<double>(), *wcp = B->wcp(par), *sV = B->sV.as<double>();
+    const int serial = B->serial_al ? 1 : 0;
     if (B->n < kLineCtaMaxInst) {
       if (B->space)
         k_h_line_cta<true><<<gc, 32 * kLineCtaWarps, 0, ctx->stream>>>(in, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB,
-                                                                      sR, sOm, Dnew, append, fst, dfs, sV);
+                                                                      sR, sOm, Dnew, append, fst, dfs, sV, serial);
       else
         k_h_line_cta<false><<<gc, 32 * kLineCtaWarps, 0, ctx->stream>>>(in, U, wcp, part, B->Ptot, splits, Al, Bt, sA,
-                                                                       sB, sR, sOm, Dnew, append, fst, dfs, sV);
-    } else {
+                                                                       sB, sR, sOm, Dnew, append, fst, dfs, sV, serial);
+    } else if (!serial || !B->varcoef) {
       if (B->space)
-        k_h_line_warp<true><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB, sR, sOm,
-                                                         Dnew, append, fst, dfs, sV);
+        k_h_line_warp<true, kLineAll><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt, sA,
+                                                                   sB, sR, sOm, Dnew, append, fst, dfs, sV);
       else
-        k_h_line_warp<false><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt, sA, sB, sR,
-                                                          sOm, Dnew, append, fst, dfs, sV);
+        k_h_line_warp<false, kLineAll><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt,
+                                                                    sA, sB, sR, sOm, Dnew, append, fst, dfs, sV);
+    } else {
+      // coefficients, serial Al one lane per instance, sweeps
+      if (B->space)
+        k_h_line_warp<true, kLineCoef><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt,
+                                                                    sA, sB, sR, sOm, Dnew, append, fst, dfs, sV);
+      else
+        k_h_line_warp<false, kLineCoef><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt,
+                                                                     sA, sB, sR, sOm, Dnew, append, fst, dfs, sV);
+      if ((rc = fh_after_launch(ctx, "k_h_line_warp"))) return rc;
+      k_h_alpha_lanes<<<(unsigned)fh_ceil_div(B->n, 32), 32, 0, ctx->stream>>>(in, B->n, sA, sB, sR, Al);
+      if ((rc = fh_after_launch(ctx, "k_h_alpha_lanes"))) return rc;
+      if (B->space)
+        k_h_line_warp<true, kLineSolve><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al, Bt,
+                                                                     sA, sB, sR, sOm, Dnew, append, fst, dfs, sV);
+      else
+        k_h_line_warp<false, kLineSolve><<<gw, 128, 0, ctx->stream>>>(in, B->n, U, wcp, part, B->Ptot, splits, Al,
+                                                                      Bt, sA, sB, sR, sOm, Dnew, append, fst, dfs, sV);
     }
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
@@ -701,6 +761,7 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     I.kmodel = p.kmodel;
     I.gravity = p.gravity;
     I.fixed = (p.kmodel == FH_K_CONST) && (p.weights == FH_W_L1 || p.beta == 1.0);
+    if (!I.fixed) B->varcoef = true;
     I.off = off;
     I.dL = p.L / p.N;
     I.Dg = pow(I.dL, -2.0);

@@ -14,54 +14,67 @@
 
 static constexpr int kHistThreads = 256;
 
+// Weights of at most kHistStage layers per row are staged in shared memory at
+// a time (32 KiB for M = 2): a split of any length walks its layers in
+// stages, in order, so the sum is the same as with one stage and the kernel
+// never needs more than the default 48 KiB of dynamic shared memory.
+static constexpr int kHistStage = 2048;
+
 template <int M>
 __global__ void __launch_bounds__(kHistThreads) k_hist_sum(const double *__restrict__ D, long long ldd, long long P,
                                                            int K, const double *__restrict__ W, int ldw, int kchunk,
                                                            double *__restrict__ part, long long ldpart) {
-  extern __shared__ double ws[];  // [M][kchunk]
+  extern __shared__ double ws[];  // [M][min(kchunk, kHistStage)]
   const int s = blockIdx.y;
   const int k0 = s * kchunk;
   const int nk = min(K, k0 + kchunk) - k0;
-  for (int i = threadIdx.x; i < M * nk; i += blockDim.x) {
-    const int m = i / nk, k = i - m * nk;
-    ws[m * kchunk + k] = W[(long long)m * ldw + k0 + k];
-  }
-  __syncthreads();
+  const int ldws = min(kchunk, kHistStage);
   const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
-  if (p >= P) return;
+  const bool live = p < P;
   double acc0[M], acc1[M];
 #pragma unroll
   for (int m = 0; m < M; ++m) acc0[m] = acc1[m] = 0.0;
-  const double *d = D + (long long)k0 * ldd + p;
-  int k = 0;
-  for (; k + 4 <= nk; k += 4) {
-    const double2 v0 = fh_ld_stream2(d);
-    const double2 v1 = fh_ld_stream2(d + ldd);
-    const double2 v2 = fh_ld_stream2(d + 2 * ldd);
-    const double2 v3 = fh_ld_stream2(d + 3 * ldd);
-    d += 4 * ldd;
+  const double *d = D + (long long)k0 * ldd + (live ? p : 0);
+  for (int kb = 0; kb < nk; kb += ldws) {
+    const int ns = min(ldws, nk - kb);
+    if (kb > 0) __syncthreads();  // every thread is done with the previous stage
+    for (int i = threadIdx.x; i < M * ns; i += blockDim.x) {
+      const int m = i / ns, k = i - m * ns;
+      ws[m * ldws + k] = W[(long long)m * ldw + k0 + kb + k];
+    }
+    __syncthreads();
+    if (!live) continue;
+    int k = 0;
+    for (; k + 4 <= ns; k += 4) {
+      const double2 v0 = fh_ld_stream2(d);
+      const double2 v1 = fh_ld_stream2(d + ldd);
+      const double2 v2 = fh_ld_stream2(d + 2 * ldd);
+      const double2 v3 = fh_ld_stream2(d + 3 * ldd);
+      d += 4 * ldd;
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-      const double *wm = ws + m * kchunk + k;
-      acc0[m] = fma(wm[0], v0.x, acc0[m]);
-      acc1[m] = fma(wm[0], v0.y, acc1[m]);
-      acc0[m] = fma(wm[1], v1.x, acc0[m]);
-      acc1[m] = fma(wm[1], v1.y, acc1[m]);
-      acc0[m] = fma(wm[2], v2.x, acc0[m]);
-      acc1[m] = fma(wm[2], v2.y, acc1[m]);
-      acc0[m] = fma(wm[3], v3.x, acc0[m]);
-      acc1[m] = fma(wm[3], v3.y, acc1[m]);
+      for (int m = 0; m < M; ++m) {
+        const double *wm = ws + m * ldws + k;
+        acc0[m] = fma(wm[0], v0.x, acc0[m]);
+        acc1[m] = fma(wm[0], v0.y, acc1[m]);
+        acc0[m] = fma(wm[1], v1.x, acc0[m]);
+        acc1[m] = fma(wm[1], v1.y, acc1[m]);
+        acc0[m] = fma(wm[2], v2.x, acc0[m]);
+        acc1[m] = fma(wm[2], v2.y, acc1[m]);
+        acc0[m] = fma(wm[3], v3.x, acc0[m]);
+        acc1[m] = fma(wm[3], v3.y, acc1[m]);
+      }
+    }
+    for (; k < ns; ++k) {
+      const double2 v = fh_ld_stream2(d);
+      d += ldd;
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+        acc0[m] = fma(ws[m * ldws + k], v.x, acc0[m]);
+        acc1[m] = fma(ws[m * ldws + k], v.y, acc1[m]);
+      }
     }
   }
-  for (; k < nk; ++k) {
-    const double2 v = fh_ld_stream2(d);
-    d += ldd;
-#pragma unroll
-    for (int m = 0; m < M; ++m) {
-      acc0[m] = fma(ws[m * kchunk + k], v.x, acc0[m]);
-      acc1[m] = fma(ws[m * kchunk + k], v.y, acc1[m]);
-    }
-  }
+  if (!live) return;
 #pragma unroll
   for (int m = 0; m < M; ++m) {
     double2 o;
@@ -274,17 +287,8 @@ int fh_launch_hist_sum_partials(fh_ctx *ctx, int M, int K, long long P, const do
                                 long long ldd, int splits, int kchunk, double *part, long long ldpart) {
   if (K <= 0 || P <= 0) return FH_OK;
   dim3 grid((unsigned)fh_ceil_div(P, 2LL * kHistThreads), (unsigned)splits);
-  const size_t smem = sizeof(double) * (size_t)M * (size_t)kchunk;
-  if (smem > 48 * 1024) {
-    // large chunks: opt in to more dynamic shared memory once per kernel
-    static bool attr_set[3] = {false, false, false};
-    if (!attr_set[M]) {
-      if (M == 1) cudaFuncSetAttribute(k_hist_sum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      else cudaFuncSetAttribute(k_hist_sum<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_set[M] = true;
-    }
-    FH_REQUIRE(ctx, smem <= 200 * 1024, FH_EINVAL, "history chunk too large (%d layers)", kchunk);
-  }
+  FH_REQUIRE(ctx, kchunk >= 1, FH_EINVAL, "history chunk of %d layers", kchunk);
+  const size_t smem = sizeof(double) * (size_t)M * (size_t)(kchunk < kHistStage ? kchunk : kHistStage);
   fh_prof_mark(ctx, FH_PROF_HISTORY, false);
   if (M == 1)
     k_hist_sum<1><<<grid, kHistThreads, smem, ctx->stream>>>(D, ldd, P, K, W, ldw, kchunk, part, ldpart);
@@ -312,15 +316,15 @@ int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int 
   }
   int splits, kchunk;
   fh_hist_plan(P, K, 16, &splits, &kchunk);
-  fh_dbuf part;
-  int rc = fh_alloc(ctx, part, sizeof(double) * (size_t)splits * M * (size_t)P, false);
+  // the split partials in the context's workspace: allocated (with a
+  // synchronisation) only when a call needs more than earlier calls did
+  void *work = nullptr;
+  int rc = fh_ctx_work(ctx, sizeof(double) * (size_t)splits * M * (size_t)P, &work);
   if (rc) return rc;
-  if ((rc = fh_launch_hist_sum_partials(ctx, M, K, P, W, ldw, D, ldd, splits, kchunk, part.as<double>(), P)))
-    return rc;
-  k_hist_reduce<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(M, splits, P, part.as<double>(), P, S, ldS);
-  if ((rc = fh_after_launch(ctx, "k_hist_reduce"))) return rc;
-  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // before the scratch buffer is released
-  return FH_OK;
+  double *part = static_cast<double *>(work);
+  if ((rc = fh_launch_hist_sum_partials(ctx, M, K, P, W, ldw, D, ldd, splits, kchunk, part, P))) return rc;
+  k_hist_reduce<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(M, splits, P, part, P, S, ldS);
+  return fh_after_launch(ctx, "k_hist_reduce");
 }
 
 int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H, long long ldh,

@@ -18,6 +18,20 @@ struct fh_prof_kind {
 
 struct fh_graph_cache;
 
+// Device allocation owned by an object; freed in its destructor.
+struct fh_dbuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~fh_dbuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
 struct fh_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -27,8 +41,15 @@ struct fh_ctx {
   bool graphs = true;  // whole solves from the initial state replay a captured graph
   fh_prof_kind pk[FH_PROF_KINDS];
   fh_graph_cache *capturing = nullptr;  // graph being captured (profiling marks become graph nodes)
+  fh_dbuf work;  // scratch of the stateless entry points (fh_ctx_work)
   char err[512] = {0};
 };
+
+// Scratch of at least `bytes` for work enqueued on ctx->stream: the context's
+// buffer, grown when too small (the stream is synchronised before the old
+// buffer is freed), so repeated calls of one size neither allocate nor
+// synchronise.
+int fh_ctx_work(fh_ctx *ctx, size_t bytes, void **out);
 
 // Records the start (stop = false) or stop event of a timed launch of `kind`
 // on `stream` (the context stream when null).
@@ -135,20 +156,6 @@ int fh_graph_run(fh_ctx *ctx, fh_graph_cache &gc, int nsteps, Body body) {
   }
   return FH_OK;
 }
-
-// Device allocation owned by an object; freed in its destructor.
-struct fh_dbuf {
-  void *p = nullptr;
-  size_t bytes = 0;
-  ~fh_dbuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  template <class T>
-  T *as() const { return static_cast<T *>(p); }
-};
 
 int fh_alloc(fh_ctx *ctx, fh_dbuf &b, size_t bytes, bool zero = true);
 

@@ -108,14 +108,14 @@ int fh_tridiag_batched(fh_ctx *ctx, int nsys, int N, const double *A, const doub
   if (nsys == 0) return FH_OK;
   FH_REQUIRE(ctx, A && R && B && Om && al1 && bt1 && u && (right_mode == 1 || u_right), FH_EINVAL,
              "fh_tridiag_batched: null pointer");
-  fh_dbuf al;
-  int rc = fh_alloc(ctx, al, sizeof(double) * (size_t)nsys * (size_t)(N + 1), false);
+  // Al in the context's workspace: allocated (with a synchronisation) only
+  // when a call needs more than earlier calls did
+  void *al = nullptr;
+  int rc = fh_ctx_work(ctx, sizeof(double) * (size_t)nsys * (size_t)(N + 1), &al);
   if (rc) return rc;
   k_tridiag_batched<<<(unsigned)fh_ceil_div(nsys, 128), 128, 0, ctx->stream>>>(
-      nsys, N, A, R, B, Om, lds, al1, bt1, right_mode, u_right, u, ldu, al.as<double>());
-  if ((rc = fh_after_launch(ctx, "k_tridiag_batched"))) return rc;
-  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return FH_OK;
+      nsys, N, A, R, B, Om, lds, al1, bt1, right_mode, u_right, u, ldu, static_cast<double *>(al));
+  return fh_after_launch(ctx, "k_tridiag_batched");
 }
 
 int fh_pcr_solver(fh_ctx *ctx, const double *a, const double *b, const double *c, const double *d, double *x, int n,
@@ -126,11 +126,8 @@ int fh_pcr_solver(fh_ctx *ctx, const double *a, const double *b, const double *c
   FH_REQUIRE(ctx, a && b && c && d && x, FH_EINVAL, "fh_pcr_solver: null pointer");
   const int threads = n < 256 ? ((n + 31) / 32) * 32 : 256;
   const size_t smem = sizeof(double) * 4 * (size_t)n;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    attr = true;
-  }
+  if (smem > 48 * 1024)  // opt-in on this context's device
+    FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
   k_pcr<<<(unsigned)nsys, threads, smem, ctx->stream>>>(a, b, c, d, x, n);
   return fh_after_launch(ctx, "k_pcr");
 }

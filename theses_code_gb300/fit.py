@@ -16,8 +16,9 @@ restates mt_psi_caputo.cpp:1892-1953 (step halving on failure, stop below
 ``eps`` or after ``max_iter`` rounds); ``pso`` the swarm update of 2183-2223
 in synchronous form.
 
-``oracle_runner`` scores the same candidates on the CPU oracle (test
-infrastructure); the tests run both drivers on both runners.
+A runner is any callable that scores a list of candidate parameter sets;
+the tests also score the same candidates on the CPU oracle and check that
+both drivers take the same rounds on either runner.
 """
 from __future__ import annotations
 
@@ -131,27 +132,6 @@ def gpu_runner(ctx, mode: int | None = None, metric: int = 0):
             out.append(_score(before[k], after[k], tts, tau, dL, N, values, metric))
             if not np.all(np.isfinite(last[k])):
                 out[-1] = BIG
-        return out
-
-    return run
-
-
-def oracle_runner(metric: int = 0):
-    """The same scoring on the CPU oracle (test infrastructure)."""
-    from oracle import oracle as O
-
-    @_only_valid
-    def run(params_list, U0, tau, t_end, values):
-        tts = _schedule(tau, t_end)
-        steps = len(tts)
-        out = []
-        for p in params_list:
-            U, hist = O.h_solve(p, U0, steps)
-            before = [U0] + [hist[s] for s in range(steps - 1)]
-            after = [hist[s] for s in range(steps)]
-            N, dL = p["N"], p["L"] / p["N"]
-            sc = _score(before, after, tts, tau, dL, N, values, metric)
-            out.append(BIG if not np.all(np.isfinite(U)) else sc)
         return out
 
     return run

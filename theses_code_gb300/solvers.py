@@ -200,6 +200,11 @@ class ABSolver:
     def set_current_coef(self, Ii: float):
         check(self.ctx.L.fh_ab_set_current_coef(self.h, float(Ii)), self.ctx.h)
 
+    def set_lag_weights(self, w):
+        """History weights of lags 1..len(w) (the reference's I_cache), before the first step."""
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(-1))
+        check(self.ctx.L.fh_ab_set_lag_weights_host(self.h, int(w.size), _hptr(w)), self.ctx.h)
+
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_ab_step(self.h, int(n)), self.ctx.h)
 
