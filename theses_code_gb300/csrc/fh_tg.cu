@@ -754,23 +754,43 @@ static constexpr int kMidPPT = 1;  // points per thread of k_tg_mid_df
 
 // ------------------------------------------------ fused sub-block sweeps
 // One cooperative launch runs both half steps of up to kSub consecutive steps
-// of one sub-block.  Every CTA owns four x lines and four y columns and keeps
-// the fixed factor tables of both (fa, g, al, pf, pb per node; 210 KiB for a
-// 512 x 512 grid) in shared memory for the whole launch, so a step only
-// reads the field, its history row and the sub-block's layers.  The half
+// of one sub-block.  Every CTA owns four x lines and four y columns; the
+// fixed factor tables of both (fa, al in the solve layout, g in the node
+// layout; 96 KiB) stay in shared memory for the whole launch.  The half
 // steps are separated by grid barriers (every CTA is resident: one CTA per
 // SM, launched cooperatively); data written by other CTAs within the launch
 // is read through L2 (ld.global.cg), never from L1.  Each barrier wait is
 // bounded by FH_WAIT_NS of %globaltimer: on expiry the CTA sets *err and
 // returns (the other CTAs then time out at their next barrier).
-// Arithmetic per node as in k_tg_xsweep_df / k_tg_ysweep_df.
-static constexpr int kFuseThreads = 384;
-static constexpr int kFuseMaxN = 513;  // lines of at most 513 nodes (64 workers x 8 nodes)
+//
+// Two thread mappings per half step:
+//  * node mapping (coalesced global traffic): thread tid holds node 1 + tid of
+//    each x line (k = line), or row 1 + tid/4 + 128 k of column tid % 4 (the
+//    four columns of a row are adjacent in memory); it loads the fields and
+//    history layers, keeps the history partial sums of its nodes in
+//    registers, forms the right parts -g om and stores the results;
+//  * solve mapping: the 128 threads of group l (warps 4l..4l+3) solve line l,
+//    thread t the equations 1 + 4t .. 4 + 4t, exchanging right parts and
+//    solutions with the node mapping through shared memory.
+// The grid barriers are split: a CTA arrives when its results are stored and
+// computes the history partial sums of the next half step (one round trip of
+// loads) before it waits, so those loads overlap the barrier.  Arithmetic per
+// node as in
+// k_tg_xsweep_df / k_tg_ysweep_df (double-float).
+static constexpr int kFuseGroup = 128;                        // threads per line (four warps)
+static constexpr int kFuseEq = 4;                             // equations per solving thread
+static constexpr int kFuseLines = 4;                          // x lines and y columns per CTA
+static constexpr int kFuseThreads = kFuseGroup * kFuseLines;  // 512
+static constexpr int kFuseMaxN = kFuseGroup * kFuseEq + 1;    // lines of at most 513 nodes
+static constexpr int kFuseSE = kFuseGroup + 4;                // solve-layout stride of one equation slot
+static constexpr int kFuseSL = kFuseEq * kFuseSE;             // solve-layout slots per line
+static constexpr int kFuseNL = kFuseMaxN - 1;                 // node-layout slots per line (nodes 1..512)
+static constexpr int kBarWarp = kFuseThreads / 32 - 1;
 
 struct tg_fuse_args {
   fh_tg_dev g;
   float2 *Cd, *Chd, *D;  // D: history layers (pairs), layer k at D + k P
-  const float2 *fax, *gx, *alx, *pfx, *pbx, *fay, *gy, *aly, *pfy, *pby;
+  const float2 *fax, *gx, *alx, *fay, *gy, *aly;
   const double *W;       // per-solve weight table, row j at W + 2 j ldw
   const double *cwall;   // current weights, 4 per step
   const float2 *rb0;     // history row of step j8 + s: x at rb0 + s rb_step, y at + rb_xy (null: none)
@@ -780,28 +800,28 @@ struct tg_fuse_args {
   int *err;
 };
 
-static size_t tg_fuse_smem(int sN, int M) {
-  return sizeof(float2) * 4 * 6 * ((size_t)tg_line_stride(sN) + tg_line_stride(M));
+// dynamic shared memory: fa, al (solve layout) and g (node layout) of both
+// directions, and the right-part / solution exchange of four lines
+static constexpr size_t kFuseSmem =
+    sizeof(float2) * (2 * 2 * kFuseLines * (size_t)kFuseSL + 2 * kFuseLines * (size_t)kFuseNL + kFuseLines * (size_t)kFuseSL);
+
+// solve-layout slot of equation i (1 <= i <= 512): thread (i-1)/4, entry (i-1)%4
+__device__ __forceinline__ int tg_fslot(int i) { return ((i - 1) & 3) * kFuseSE + ((i - 1) >> 2); }
+
+__device__ __forceinline__ void tg_grid_arrive(unsigned *bar) {
+  __syncthreads();  // every store of the CTA precedes the release
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+  }
 }
 
-// Grid barrier number `target / gridDim.x` on a counter zeroed before the
-// launch.  The last warp of the CTA (kBarWarp, never a solving warp) arrives
-// and polls as a whole, lane 0 loading and broadcasting the count; all other
-// single-lane work of the kernel also runs in that warp, so the solving warps
-// never run with split lanes (a solving warp whose lane 0 had done such work
-// ran the shuffle scans of its line solve three times slower).
-static constexpr int kBarWarp = kFuseThreads / 32 - 1;
-
-__device__ __forceinline__ bool tg_grid_sync(unsigned *bar, unsigned target, int *err) {
+// Waits until the barrier counter reaches `target` (warp kBarWarp polls, lane 0
+// loading and broadcasting the count); false (and *err set) on expiry.
+__device__ __forceinline__ bool tg_grid_wait(const unsigned *bar, unsigned target, int *err) {
   __shared__ int gs_ok;
-  __syncthreads();
   if ((threadIdx.x >> 5) == kBarWarp) {
     const unsigned lane = threadIdx.x & 31u;
-    if (lane == 0) {
-      __threadfence();
-      atomicAdd(bar, 1u);
-    }
-    __syncwarp();
     const uint64_t deadline = fh_globaltimer() + FH_WAIT_NS;
     int ok = 1;
     for (unsigned it = 0;; ++it) {
@@ -846,48 +866,107 @@ extern "C" int fh_tg_stamps_read(long long *h) {
 #define TG_STAMP(p)
 #endif
 
-// Roles: warps 0-3 solve (warp w the x line / y column w of the CTA) and do
-// nothing else, so they never run with split lanes; warps 4-11 ("workers", 64
-// per line, eight nodes each) do all loads and stores.  384 threads leave 170
-// registers per thread for the workers' per-node history sums.  While one direction is
-// being solved the workers precompute the history sums of the other (every
-// load that does not depend on that solve), so after a grid barrier only the
-// new field and the newest layer remain to be read.
-static constexpr int kSolveWarps = 4;
-static constexpr int kWorkers = kFuseThreads - 32 * kSolveWarps;  // 256
-static constexpr int kWPerLine = kWorkers / 4;                   // 64
-static constexpr int kWPts = 8;                                  // nodes per worker and line
-static constexpr int kLayerBatch = 1;                            // sub-block layers per load round
-static_assert(kWPerLine * kWPts + 1 >= kFuseMaxN, "fused sweeps: worker nodes must cover a line");
-
-// x history part of step j8 + s of a worker's nodes without the newest layer:
-// row + sum_{t < s-1} w(t) D[j8 + t]
-__device__ __forceinline__ void tg_x_partial(const tg_fuse_args &a, int s, const float2 (*wx)[kSub],
-                                             const float2 *tiny, long long xbase, int wt, int Nx,
-                                             fh_df (&tsx)[kWPts]) {
-  const float2 *rbx = a.rb0 ? a.rb0 + (long long)s * a.rb_step : nullptr;
+// Exclusive scan of the chunk maps of one line's 128 threads (four warps,
+// named barrier `bar`, warp totals in sm[4]): forward, thread t receives
+// f_{t-1} o ... o f_0; reverse, G_{t+1} o ... o G_127.
+template <bool REV>
+__device__ __forceinline__ fh_daff tg_group_scan(fh_daff f, fh_daff *sm, int bar, int w4) {
+  const unsigned lane = threadIdx.x & 31u;
+  fh_daff g = f;
 #pragma unroll
-  for (int e = 0; e < kWPts; ++e) {
-    const int i = 1 + wt + e * kWPerLine;
-    tsx[e] = rbx ? fh_df_from_pair(__ldcg(rbx + xbase + (i < Nx ? i : 1))) : fh_df{0.f, 0.f};
+  for (int d = 1; d < 32; d <<= 1) {
+    if (!REV) {
+      const fh_daff p{fh_df_shfl_up(g.a, d), fh_df_shfl_up(g.b, d)};
+      if (lane >= (unsigned)d) g = fh_daff_compose(g, p);
+    } else {
+      const fh_daff p{fh_df_shfl_down(g.a, d), fh_df_shfl_down(g.b, d)};
+      if (lane + d < 32u) g = fh_daff_compose(g, p);
+    }
   }
-  for (int t0 = 0; t0 < s - 1; t0 += kLayerBatch) {  // kLayerBatch layers per round trip
-    float2 d[kLayerBatch][kWPts];
+  const fh_daff id{fh_df{1.f, 0.f}, fh_df{0.f, 0.f}};
+  fh_daff e;
+  if (!REV) {
+    if (lane == 31u) sm[w4] = g;
+    e = fh_daff{fh_df_shfl_up(g.a, 1), fh_df_shfl_up(g.b, 1)};
+    if (lane == 0u) e = id;
+  } else {
+    if (lane == 0u) sm[w4] = g;
+    e = fh_daff{fh_df_shfl_down(g.a, 1), fh_df_shfl_down(g.b, 1)};
+    if (lane == 31u) e = id;
+  }
+  fh_group_bar(bar, kFuseGroup);
+  fh_daff P = id;
+  if (!REV)
+    for (int k = 0; k < w4; ++k) P = fh_daff_compose(sm[k], P);
+  else
+    for (int k = 3; k > w4; --k) P = fh_daff_compose(sm[k], P);
+  fh_group_bar(bar, kFuseGroup);  // sm may be reused after this
+  return fh_daff_compose(e, P);
+}
+
+// One line of N nodes by the 128 threads of its group: Thomas in the
+// reference form from the fixed factors, u_i = al_i u_{i+1} + bt_i with
+// bt_i = fa_i bt_{i-1} + fb_i, bt_0 = bt1, al_0 = al1, u_N = u_{N+1} =
+// bt_{N-1} / (1 - al_{N-1}).  Each thread walks its four equations from zero
+// (keeping the prefix slope products), the chunk maps are scanned across the
+// group, and the start value finishes each chunk.  fb (solve layout) is
+// replaced by u; ub receives u_0 and u_N.
+__device__ __forceinline__ void tg_group_solve(int N, const float2 *fa, const float2 *al, float2 *xch, float2 *ub,
+                                               fh_df al1, fh_df bt1, fh_daff *sm, fh_df *uNs, int bar, int t, int w4) {
+  const fh_df one{1.f, 0.f}, zero{0.f, 0.f};
+  fh_df B[kFuseEq], P[kFuseEq];
+  fh_df b = zero, p = one;
 #pragma unroll
-    for (int u = 0; u < kLayerBatch; ++u)
-      if (t0 + u < s - 1)
+  for (int e = 0; e < kFuseEq; ++e) {
+    const int i = 1 + kFuseEq * t + e;
+    if (i < N) {
+      const int sl = e * kFuseSE + t;
+      const fh_df f = fh_df_from_pair(fa[sl]);
+      b = fh_df_fma(f, b, fh_df_from_pair(xch[sl]));
+      p = fh_df_mul(p, f);
+    }
+    B[e] = b;
+    P[e] = p;
+  }
+  const fh_daff Pf = tg_group_scan<false>(fh_daff{p, b}, sm, bar, w4);
+  const fh_df s = fh_df_fma(Pf.a, bt1, Pf.b);  // bt at equation 4t (bt1 for t = 0)
+  fh_df bt[kFuseEq];
 #pragma unroll
-        for (int e = 0; e < kWPts; ++e) {
-          const int i = 1 + wt + e * kWPerLine;
-          d[u][e] = __ldcg(tiny + (long long)(t0 + u) * a.g.P + xbase + (i < Nx ? i : 1));
-        }
+  for (int e = 0; e < kFuseEq; ++e) bt[e] = fh_df_fma(P[e], s, B[e]);
+  // u_N from the thread of equation N - 1
+  {
+    const int e = (N - 2) - kFuseEq * t;
+    if (e >= 0 && e < kFuseEq) {
+      const fh_df aN = fh_df_from_pair(al[e * kFuseSE + t]);
+      *uNs = fh_df_div(bt[e], fh_df_sub(one, aN));
+    }
+  }
+  fh_group_bar(bar, kFuseGroup);
+  const fh_df uN = *uNs;
+  fh_df V[kFuseEq], Q[kFuseEq];
+  fh_df v = zero, q = one;
 #pragma unroll
-    for (int u = 0; u < kLayerBatch; ++u)
-      if (t0 + u < s - 1) {
-        const fh_df w = fh_df_from_pair(wx[s][t0 + u]);
+  for (int e = kFuseEq - 1; e >= 0; --e) {
+    const int i = 1 + kFuseEq * t + e;
+    if (i < N) {
+      const fh_df a = fh_df_from_pair(al[e * kFuseSE + t]);
+      v = fh_df_fma(a, v, bt[e]);
+      q = fh_df_mul(q, a);
+    }
+    V[e] = v;
+    Q[e] = q;
+  }
+  const fh_daff Pb = tg_group_scan<true>(fh_daff{q, v}, sm, bar, w4);
+  const fh_df u1 = fh_df_fma(Pb.a, uN, Pb.b);  // u at equation 4t + 5 (u_N past the last chunk)
 #pragma unroll
-        for (int e = 0; e < kWPts; ++e) tsx[e] = fh_df_fma(w, fh_df_from_pair(d[u][e]), tsx[e]);
-      }
+  for (int e = 0; e < kFuseEq; ++e) {
+    const int i = 1 + kFuseEq * t + e;
+    if (i < N) xch[e * kFuseSE + t] = fh_df_pair(fh_df_fma(Q[e], u1, V[e]));
+  }
+  if (t == 0) {
+    const fh_df u0 = fh_df_fma(al1, fh_df_fma(Q[0], u1, V[0]), bt1);
+    ub[0] = fh_df_pair(u0);
+    ub[1] = fh_df_pair(uN);
   }
 }
 
@@ -895,44 +974,38 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
   extern __shared__ float2 sbf[];
   // cx/cy: step constants; wx/wy[s][t]: weight of layer j8 + t in step j8 + s
   __shared__ float2 cx[kSub][4], cy[kSub][4], wx[kSub][kSub], wy[kSub][kSub];
+  __shared__ fh_daff scan_sm[kFuseLines][4];
+  __shared__ fh_df uN_sm[kFuseLines];
+  __shared__ float2 ub_sm[kFuseLines][2];
   const fh_tg_dev &g = a.g;
   const int Nx = g.sN, Ny = g.M;
-  const int Lx = tg_line_stride(Nx), Ly = tg_line_stride(Ny);
   const int tid = threadIdx.x, warp = tid >> 5;
-  float2 *xs = sbf;                          // x lines: fa, g, al, pf, pb, bt (stride Lx)
-  float2 *ys = sbf + (size_t)4 * 6 * Lx;     // y columns: the same (stride Ly)
-  // fixed factor tables, all threads: x nodes line by line, y nodes row by row
-  // (four adjacent columns per row)
-  for (int v = tid; v < 4 * (Nx - 1); v += blockDim.x) {
-    const int ln = v / (Nx - 1), i = 1 + v % (Nx - 1);
-    const int line = 1 + blockIdx.x * 4 + ln;
-    if (line < g.M) {
-      float2 *xa = xs + (size_t)ln * 6 * Lx;
-      const long long id = (long long)line * g.ld + i;
-      xa[fh_sk(i)] = a.fax[id];
-      xa[Lx + fh_sk(i)] = a.gx[id];
-      xa[2 * Lx + fh_sk(i)] = a.alx[id];
-      xa[3 * Lx + fh_sk(i)] = a.pfx[id];
-      xa[4 * Lx + fh_sk(i)] = a.pbx[id];
+  float2 *fa_x = sbf, *al_x = fa_x + kFuseLines * kFuseSL;  // solve layout, [line][slot]
+  float2 *fa_y = al_x + kFuseLines * kFuseSL, *al_y = fa_y + kFuseLines * kFuseSL;
+  float2 *g_x = al_y + kFuseLines * kFuseSL, *g_y = g_x + kFuseLines * kFuseNL;  // node layout, [line][i-1]
+  float2 *xch = g_y + kFuseLines * kFuseNL;  // [line][slot]: -g om, then u
+  // lines line0 .. line0 + 3 (rows j of the x sweep, columns i of the y sweep),
+  // aligned to four so that a row of the CTA's columns is one 32-byte sector;
+  // line 0 (a boundary) is not solved
+  const int line0 = kFuseLines * blockIdx.x;
+  auto xl_ok = [&](int l) { return line0 + l >= 1 && line0 + l < g.M; };
+  auto yl_ok = [&](int l) { return line0 + l >= 1 && line0 + l < g.sN; };
+  // fixed factor tables
+  for (int v = tid; v < kFuseLines * kFuseNL; v += blockDim.x) {
+    const int l = v / kFuseNL, i = 1 + v % kFuseNL;
+    if (xl_ok(l) && i < Nx) {
+      const long long id = (long long)(line0 + l) * g.ld + i;
+      fa_x[l * kFuseSL + tg_fslot(i)] = a.fax[id];
+      al_x[l * kFuseSL + tg_fslot(i)] = a.alx[id];
+      g_x[l * kFuseNL + i - 1] = a.gx[id];
+    }
+    if (yl_ok(l) && i < Ny) {
+      const long long id = line0 + l + (long long)i * g.ld;
+      fa_y[l * kFuseSL + tg_fslot(i)] = a.fay[id];
+      al_y[l * kFuseSL + tg_fslot(i)] = a.aly[id];
+      g_y[l * kFuseNL + i - 1] = a.gy[id];
     }
   }
-  for (int v = tid; v < 4 * (Ny - 1); v += blockDim.x) {
-    const int col = v & 3, q = 1 + (v >> 2);
-    const int ycol = 1 + blockIdx.x * 4 + col;
-    if (ycol < g.sN) {
-      float2 *ya = ys + (size_t)col * 6 * Ly;
-      const long long id = ycol + (long long)q * g.ld;
-      ya[fh_sk(q)] = a.fay[id];
-      ya[Ly + fh_sk(q)] = a.gy[id];
-      ya[2 * Ly + fh_sk(q)] = a.aly[id];
-      ya[3 * Ly + fh_sk(q)] = a.pfy[id];
-      ya[4 * Ly + fh_sk(q)] = a.pby[id];
-    }
-  }
-  if (tid < 4 && 1 + (int)blockIdx.x * 4 + tid < g.M)
-    xs[(size_t)tid * 6 * Lx + 4 * Lx + fh_sk(0)] = a.pbx[(long long)(1 + blockIdx.x * 4 + tid) * g.ld];
-  if (tid >= 32 && tid < 36 && 1 + (int)blockIdx.x * 4 + (tid - 32) < g.sN)
-    ys[(size_t)(tid - 32) * 6 * Ly + 4 * Ly + fh_sk(0)] = a.pby[1 + blockIdx.x * 4 + (tid - 32)];
   // double-float step constants and sub-block weights, one FP64 conversion per thread
   constexpr int kPer = 8 + 2 * kSub;
   for (int v = tid; v < a.ns * kPer; v += blockDim.x) {
@@ -957,172 +1030,183 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
     }
     *dst = fh_df_pair(fh_df_from_double(val));
   }
-  __syncwarp();
   __syncthreads();
 
-  const bool worker = warp >= kSolveWarps;
-  const int wk = tid - 32 * kSolveWarps;  // worker index (negative for the solving warps)
-  // worker's x nodes: line wl, i = 1 + wt + 96 e
-  const int wl = worker ? wk / kWPerLine : 0, wt = worker ? wk % kWPerLine : 0;
-  const int xline = 1 + blockIdx.x * 4 + wl;
-  const bool xlive = worker && xline < g.M;
-  const long long xbase = (long long)xline * g.ld;
-  float2 *xa = xs + (size_t)wl * 6 * Lx;
-  // worker's y nodes: column col, q = 1 + wr + 96 e (four adjacent columns per row)
-  const int col = worker ? (wk & 3) : 0, wr = worker ? (wk >> 2) : 0;
-  const int ycol = 1 + blockIdx.x * 4 + col;
-  const bool ylive = worker && ycol < g.sN;
-  float2 *ya = ys + (size_t)col * 6 * Ly;
+  // node mapping: x node 1 + tid of line k; y row 1 + tid/4 + 128 k of column tid % 4
+  const int xi = 1 + tid;
+  const int yc = tid & 3, yq0 = 1 + (tid >> 2);
+  const bool ycol_live = yl_ok(yc);
+  auto xlive = [&](int k) { return xl_ok(k) && xi < Nx; };
+  auto xid = [&](int k) { return (long long)(line0 + k) * g.ld + xi; };
+  auto yq = [&](int k) { return yq0 + 128 * k; };
+  auto ylive = [&](int k) { return ycol_live && yq(k) < Ny; };
+  auto yid = [&](int k) { return (long long)(line0 + yc) + (long long)yq(k) * g.ld; };
+  // solve mapping
+  const int grp = tid / kFuseGroup, gt = tid % kFuseGroup, w4 = gt >> 5;
   const float2 *tiny = a.D + (long long)a.j8 * g.P;  // layers of the sub-block
   const unsigned nblk = gridDim.x;
   unsigned nb = 0;
 
-  fh_df tsx[kWPts], tsy[kWPts];  // history parts of the worker's x / y nodes
-  float2 f[kWPts];               // old field at the worker's y nodes
-  if (xlive) tg_x_partial(a, a.s0, wx, tiny, xbase, wt, Nx, tsx);
+  fh_df tsx[kFuseLines], tsy[kFuseLines];  // history parts of the thread's x / y nodes
+  float2 f[kFuseLines];                    // old field at the thread's y nodes
+  // x history part of step s without its newest layer: row + sum_{t < s-1} w(t) D[j8 + t]
+  // history part of step s at the thread's x nodes without the newest layer,
+  // row + sum_{t < s-1} w(t) D[j8 + t], and at its y nodes, row + sum_{t < s}
+  // w(t) D[j8 + t], with the old field there: every load of a part is issued
+  // at once (*_load), then summed (*_sum).
+  auto x_load = [&](int s, float2 (&r)[kFuseLines], float2 (&d)[kSub - 1][kFuseLines]) {
+    const float2 *rbx = a.rb0 ? a.rb0 + (long long)s * a.rb_step : nullptr;
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) r[k] = (rbx && xlive(k)) ? __ldcg(rbx + xid(k)) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int t = 0; t < kSub - 1; ++t)
+#pragma unroll
+      for (int k = 0; k < kFuseLines; ++k)
+        d[t][k] = (t < s - 1 && xlive(k)) ? __ldcg(tiny + (long long)t * g.P + xid(k)) : make_float2(0.f, 0.f);
+  };
+  auto x_sum = [&](int s, const float2 (&r)[kFuseLines], const float2 (&d)[kSub - 1][kFuseLines]) {
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) tsx[k] = fh_df_from_pair(r[k]);
+#pragma unroll
+    for (int t = 0; t < kSub - 1; ++t)
+      if (t < s - 1) {
+        const fh_df w = fh_df_from_pair(wx[s][t]);
+#pragma unroll
+        for (int k = 0; k < kFuseLines; ++k) tsx[k] = fh_df_fma(w, fh_df_from_pair(d[t][k]), tsx[k]);
+      }
+  };
+  auto y_load = [&](int s, float2 (&r)[kFuseLines], float2 (&d)[kSub - 1][kFuseLines]) {
+    const float2 *rby = a.rb0 ? a.rb0 + (long long)s * a.rb_step + a.rb_xy : nullptr;
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) {
+      f[k] = ylive(k) ? __ldcg(a.Cd + yid(k)) : make_float2(0.f, 0.f);
+      r[k] = (rby && ylive(k)) ? __ldcg(rby + yid(k)) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int t = 0; t < kSub - 1; ++t)
+#pragma unroll
+      for (int k = 0; k < kFuseLines; ++k)
+        d[t][k] = (t < s && ylive(k)) ? __ldcg(tiny + (long long)t * g.P + yid(k)) : make_float2(0.f, 0.f);
+  };
+  auto y_sum = [&](int s, const float2 (&r)[kFuseLines], const float2 (&d)[kSub - 1][kFuseLines]) {
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) tsy[k] = fh_df_from_pair(r[k]);
+#pragma unroll
+    for (int t = 0; t < kSub - 1; ++t)
+      if (t < s) {
+        const fh_df w = fh_df_from_pair(wy[s][t]);
+#pragma unroll
+        for (int k = 0; k < kFuseLines; ++k) tsy[k] = fh_df_fma(w, fh_df_from_pair(d[t][k]), tsy[k]);
+      }
+  };
+  {
+    float2 r[kFuseLines], d[kSub - 1][kFuseLines];
+    x_load(a.s0, r, d);
+    x_sum(a.s0, r, d);
+  }
 
   for (int s = a.s0; s < a.s0 + a.ns; ++s) {
     const int j = a.j8 + s;
     TG_STAMP(0);
     // ---- x half step (fr_d_t_g_2d.cpp:2577-2590): field and newest layer
-    if (xlive) {
+    {
       const fh_df kst = fh_df_from_pair(cx[s][0]), S2 = fh_df_from_pair(cx[s][1]), st = fh_df_from_pair(cx[s][2]);
       const float2 *lat = s >= 1 ? tiny + (long long)(s - 1) * g.P : nullptr;
-      float2 c[kWPts], d[kWPts];
-#pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int i = 1 + wt + e * kWPerLine;
-        const long long id = xbase + (i < Nx ? i : 1);
-        c[e] = __ldcg(a.Cd + id);
-        d[e] = lat ? __ldcg(lat + id) : make_float2(0.f, 0.f);
-      }
       const fh_df wl_ = s >= 1 ? fh_df_from_pair(wx[s][s - 1]) : fh_df{0.f, 0.f};
+      float2 c[kFuseLines], d[kFuseLines];
 #pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int i = 1 + wt + e * kWPerLine;
-        if (i < Nx) {
-          const fh_df ts = lat ? fh_df_fma(wl_, fh_df_from_pair(d[e]), tsx[e]) : tsx[e];
-          fh_df om = fh_df_fma(kst, fh_df_from_pair(c[e]), S2);
-          om = fh_df_fma(st, ts, om);
-          xa[5 * Lx + fh_sk(i)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(xa[Lx + fh_sk(i)]), om)));
-        }
+      for (int k = 0; k < kFuseLines; ++k) {
+        c[k] = xlive(k) ? __ldcg(a.Cd + xid(k)) : make_float2(0.f, 0.f);
+        d[k] = (lat && xlive(k)) ? __ldcg(lat + xid(k)) : make_float2(0.f, 0.f);
       }
+#pragma unroll
+      for (int k = 0; k < kFuseLines; ++k)
+        if (xlive(k)) {
+          const fh_df ts = lat ? fh_df_fma(wl_, fh_df_from_pair(d[k]), tsx[k]) : tsx[k];
+          fh_df om = fh_df_fma(kst, fh_df_from_pair(c[k]), S2);
+          om = fh_df_fma(st, ts, om);
+          xch[k * kFuseSL + tg_fslot(xi)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(g_x[k * kFuseNL + xi - 1]), om)));
+        }
     }
     __syncthreads();
     TG_STAMP(1);
-    if (!worker) {
-      if (1 + (int)blockIdx.x * 4 + warp < g.M) {
-        float2 *w = xs + (size_t)warp * 6 * Lx;
-        fh_line_solve_prefix_df(Nx, w, w + 5 * Lx, w + 2 * Lx, w + 3 * Lx, w + 4 * Lx, fh_df{0.f, 0.f},
-                                fh_df_from_pair(cx[s][3]), w + 5 * Lx, w + 5 * Lx);
-      }
-    } else if (ylive) {
-      // y history part of this step (all its layers are complete) and the old field
-      const float2 *rby = a.rb0 ? a.rb0 + (long long)s * a.rb_step + a.rb_xy : nullptr;
-#pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int q = 1 + wr + e * kWPerLine;
-        const long long id = ycol + (long long)(q < Ny ? q : 1) * g.ld;
-        f[e] = __ldcg(a.Cd + id);
-        tsy[e] = rby ? fh_df_from_pair(__ldcg(rby + id)) : fh_df{0.f, 0.f};
-      }
-      for (int t0 = 0; t0 < s; t0 += kLayerBatch) {
-        float2 d[kLayerBatch][kWPts];
-#pragma unroll
-        for (int u = 0; u < kLayerBatch; ++u)
-          if (t0 + u < s)
-#pragma unroll
-            for (int e = 0; e < kWPts; ++e) {
-              const int q = 1 + wr + e * kWPerLine;
-              d[u][e] = __ldcg(tiny + (long long)(t0 + u) * g.P + ycol + (long long)(q < Ny ? q : 1) * g.ld);
-            }
-#pragma unroll
-        for (int u = 0; u < kLayerBatch; ++u)
-          if (t0 + u < s) {
-            const fh_df w = fh_df_from_pair(wy[s][t0 + u]);
-#pragma unroll
-            for (int e = 0; e < kWPts; ++e) tsy[e] = fh_df_fma(w, fh_df_from_pair(d[u][e]), tsy[e]);
-          }
-      }
-    }
+    if (xl_ok(grp))
+      tg_group_solve(Nx, fa_x + grp * kFuseSL, al_x + grp * kFuseSL, xch + grp * kFuseSL, ub_sm[grp], fh_df{0.f, 0.f},
+                     fh_df_from_pair(cx[s][3]), scan_sm[grp], &uN_sm[grp], 1 + grp, gt, w4);
     __syncthreads();
     TG_STAMP(2);
-    if (xlive) {
 #pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int i = 1 + wt + e * kWPerLine;
-        if (i < Nx) a.Chd[xbase + i] = xa[5 * Lx + fh_sk(i)];
+    for (int k = 0; k < kFuseLines; ++k)
+      if (xlive(k)) a.Chd[xid(k)] = xch[k * kFuseSL + tg_fslot(xi)];
+    if (tid < 3 * kFuseLines) {  // nodes 0, Nx, Nx + 1 of the four lines: Ch and C
+      const int l = tid / 3, k = tid % 3;
+      if (xl_ok(l)) {
+        const float2 v = ub_sm[l][k == 0 ? 0 : 1];
+        const long long id = (long long)(line0 + l) * g.ld + (k == 0 ? 0 : Nx - 1 + k);
+        a.Chd[id] = v;
+        a.Cd[id] = v;
       }
     }
-    if (warp == kBarWarp && (tid & 31) < 12) {  // nodes 0, Nx, Nx+1 of the four lines
-      const int l = (tid & 31) / 3, k = (tid & 31) % 3;
-      const int line = 1 + blockIdx.x * 4 + l;
-      if (line < g.M) {
-        const int i = k == 0 ? 0 : Nx - 1 + k;
-        const float2 v = xs[(size_t)l * 6 * Lx + 5 * Lx + fh_sk(i)];
-        a.Chd[(long long)line * g.ld + i] = v;
-        a.Cd[(long long)line * g.ld + i] = v;
-      }
+    tg_grid_arrive(a.bar);
+    {  // the y history part overlaps the barrier (its layers are complete)
+      float2 r[kFuseLines], d[kSub - 1][kFuseLines];
+      y_load(s, r, d);
+      y_sum(s, r, d);
     }
-    __syncwarp();
-    if (!tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
+    if (!tg_grid_wait(a.bar, ++nb * nblk, a.err)) return;
     TG_STAMP(3);
     // ---- y half step (fr_d_t_g_2d.cpp:2591-2606): the half-step field
-    if (ylive) {
+    {
       const fh_df kst = fh_df_from_pair(cy[s][0]), kyh = fh_df_from_pair(cy[s][1]), S2 = fh_df_from_pair(cy[s][2]),
                   st = fh_df_from_pair(cy[s][3]);
-      float2 c[kWPts];
+      float2 c[kFuseLines];
 #pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int q = 1 + wr + e * kWPerLine;
-        c[e] = __ldcg(a.Chd + ycol + (long long)(q < Ny ? q : 1) * g.ld);
-      }
+      for (int k = 0; k < kFuseLines; ++k) c[k] = ylive(k) ? __ldcg(a.Chd + yid(k)) : make_float2(0.f, 0.f);
 #pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int q = 1 + wr + e * kWPerLine;
-        if (q < Ny) {
-          const fh_df cc = fh_df_from_pair(c[e]);
+      for (int k = 0; k < kFuseLines; ++k)
+        if (ylive(k)) {
+          const fh_df cc = fh_df_from_pair(c[k]);
           // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
-          const fh_df tt = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[e]), cc), tsy[e]);
+          const fh_df tt = fh_df_fma(kyh, fh_df_sub(fh_df_from_pair(f[k]), cc), tsy[k]);
           fh_df om = fh_df_fma(kst, cc, S2);
           om = fh_df_fma(st, tt, om);
-          ya[5 * Ly + fh_sk(q)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(ya[Ly + fh_sk(q)]), om)));
+          xch[yc * kFuseSL + tg_fslot(yq(k))] =
+              fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(g_y[yc * kFuseNL + yq(k) - 1]), om)));
         }
-      }
     }
     __syncthreads();
     TG_STAMP(4);
-    if (!worker) {
-      if (1 + (int)blockIdx.x * 4 + warp < g.sN) {
-        float2 *w = ys + (size_t)warp * 6 * Ly;
-        fh_line_solve_prefix_df(Ny, w, w + 5 * Ly, w + 2 * Ly, w + 3 * Ly, w + 4 * Ly, fh_df{1.f, 0.f},
-                                fh_df{0.f, 0.f}, w + 5 * Ly, w + 5 * Ly);
-      }
-    } else if (xlive && s + 1 < a.s0 + a.ns) {
-      tg_x_partial(a, s + 1, wx, tiny, xbase, wt, Nx, tsx);  // layers up to j - 1 are complete
-    }
+    if (yl_ok(grp))
+      tg_group_solve(Ny, fa_y + grp * kFuseSL, al_y + grp * kFuseSL, xch + grp * kFuseSL, ub_sm[grp], fh_df{1.f, 0.f},
+                     fh_df{0.f, 0.f}, scan_sm[grp], &uN_sm[grp], 1 + grp, gt, w4);
     __syncthreads();
     TG_STAMP(5);
-    if (ylive) {
+    {
       float2 *Dj = a.D + (long long)j * g.P;
 #pragma unroll
-      for (int e = 0; e < kWPts; ++e) {
-        const int q = 1 + wr + e * kWPerLine;
-        if (q < Ny) {
-          const long long id = ycol + (long long)q * g.ld;
-          const float2 u = ya[5 * Ly + fh_sk(q)];
-          a.Cd[id] = u;
-          Dj[id] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[e])));
+      for (int k = 0; k < kFuseLines; ++k)
+        if (ylive(k)) {
+          const float2 u = xch[yc * kFuseSL + tg_fslot(yq(k))];
+          a.Cd[yid(k)] = u;
+          Dj[yid(k)] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[k])));
+        }
+      if (tid < 3 * kFuseLines) {  // rows 0, Ny, Ny + 1 of the four columns: C only
+        const int l = tid / 3, k = tid % 3;
+        if (yl_ok(l)) {
+          const long long id = (long long)(line0 + l) + (long long)(k == 0 ? 0 : Ny - 1 + k) * g.ld;
+          a.Cd[id] = ub_sm[l][k == 0 ? 0 : 1];
         }
       }
-      if (wr == kWPerLine - 1) {  // boundary nodes: lanes of warp kBarWarp
-        a.Cd[ycol] = ya[5 * Ly + fh_sk(0)];
-        a.Cd[ycol + (long long)Ny * g.ld] = ya[5 * Ly + fh_sk(Ny)];
-        a.Cd[ycol + (long long)(Ny + 1) * g.ld] = ya[5 * Ly + fh_sk(Ny + 1)];
-      }
     }
-    __syncwarp();
-    if (s + 1 < a.s0 + a.ns && !tg_grid_sync(a.bar, ++nb * nblk, a.err)) return;
+    if (s + 1 < a.s0 + a.ns) {
+      tg_grid_arrive(a.bar);
+      {  // the x history part of the next step overlaps the barrier (layers up to j - 1 are complete)
+        float2 r[kFuseLines], d[kSub - 1][kFuseLines];
+        x_load(s + 1, r, d);
+        x_sum(s + 1, r, d);
+      }
+      if (!tg_grid_wait(a.bar, ++nb * nblk, a.err)) return;
+    }
     TG_STAMP(6);
   }
 }
@@ -1241,13 +1325,9 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       fa.fax = s->fax2.as<float2>();
       fa.gx = s->gx2.as<float2>();
       fa.alx = s->alx2.as<float2>();
-      fa.pfx = s->pfx2.as<float2>();
-      fa.pbx = s->pbx2.as<float2>();
       fa.fay = s->fay2.as<float2>();
       fa.gy = s->gy2.as<float2>();
       fa.aly = s->aly2.as<float2>();
-      fa.pfy = s->pfy2.as<float2>();
-      fa.pby = s->pby2.as<float2>();
       fa.W = s->W.as<double>();
       fa.cwall = s->cw.as<double>();
       fa.ldw = ldw;
@@ -1272,7 +1352,7 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)s->fuse_blocks);
       cfg.blockDim = dim3(kFuseThreads);
-      cfg.dynamicSmemBytes = tg_fuse_smem(g.sN, g.M);
+      cfg.dynamicSmemBytes = kFuseSmem;
       cfg.stream = ctx->stream;
       cudaLaunchAttribute at[2];
       at[0].id = cudaLaunchAttributeCooperative;
@@ -1476,7 +1556,7 @@ static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   // the fused sweeps hold both directions' tables; larger grids use the per-step kernels
   if (sN <= kFuseMaxN && M <= kFuseMaxN) {
     static int cur_f[64];
-    const int smf = (int)tg_fuse_smem(sN, M);
+    const int smf = (int)kFuseSmem;
     if (smf > cur_f[ctx->device] && smf <= 220 * 1024) {
       FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tg_sweeps_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, smf));
       cur_f[ctx->device] = smf;
@@ -1558,9 +1638,9 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
       }
     // fused sub-block sweeps: fixed factorization, per-solve weight table, both
     // directions' tables in shared memory, one resident CTA per four lines
-    const int nblk = (int)std::max(fh_ceil_div(g.M - 1, 4), fh_ceil_div(g.sN - 1, 4));
+    const int nblk = std::max((g.M - 1) / kFuseLines + 1, (g.sN - 1) / kFuseLines + 1);  // lines 4b .. 4b + 3
     int nsm = 0, per_sm = 0;
-    const size_t smf = tg_fuse_smem(g.sN, g.M);
+    const size_t smf = kFuseSmem;
     if (s->factor_fixed && s->wtab && g.sN <= kFuseMaxN && g.M <= kFuseMaxN && smf <= 220 * 1024 &&
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device) == cudaSuccess &&
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tg_sweeps_fused, kFuseThreads, smf) == cudaSuccess &&
