@@ -376,10 +376,12 @@ class H1D(Workload):
             params, U0s = workloads.psi_batch(n=args.instances, seed=7 + rank)
             S = args.solve_steps if args.solve_steps != 2000 else 500
             self.name = f"psi_batch_{args.instances}inst_{S}steps"
-        from theses_code_gb300._lib import FH_H_DF64, FH_H_FP64
-        # the batch keeps its history as double-float pairs (plain-path accuracy,
-        # HBM-bound sums) unless --mode fp64; the single cfg-1 instance stays FP64
-        self.hmode = FH_H_FP64 if (args.mode == "fp64" or kind == "caputo1d") else FH_H_DF64
+        from theses_code_gb300._lib import FH_H_BLOCKED, FH_H_DF64, FH_H_FP64
+        # psi batch: --mode blocked (default; far history on the tensor cores),
+        # df64 (double-float history pairs) or fp64; the single cfg-1 instance stays FP64
+        self.hmodes = {"fp64": FH_H_FP64, "df64": FH_H_DF64, "blocked": FH_H_BLOCKED}
+        self.hmode = FH_H_FP64 if kind == "caputo1d" else self.hmodes[args.mode]
+        self.params_all, self.S_all = params, S
         self.solver = HSolverBatch(ctx, params, S + 1, self.hmode)
         self.gammas = None
         if kind == "psi_batch" and args.gamma_min < 1.0:
@@ -388,7 +390,7 @@ class H1D(Workload):
             self.gammas = rng.uniform(args.gamma_min, 1.0, size=len(params))
             self.solver.set_space_order(self.gammas)
             self.name += f"_gamma{args.gamma_min:g}"
-        self.tuned = self.solver.autotune() if kind == "psi_batch" else None
+        self.tuned = self.solver.autotune() if (kind == "psi_batch" and self.hmode != FH_H_BLOCKED) else None
         self.params, self.U0s = params, U0s
         flat = np.concatenate(U0s)
         self.U_d = torch.as_tensor(flat, device=f"cuda:{dev}")
@@ -399,16 +401,37 @@ class H1D(Workload):
         self.gps = float(npts) * S
         self.h2d = self.d2h = flat.size * 8
         seg = sum(((p["N"] + 2) + 1) & ~1 for p in params)
-        self.alg_hist_bytes = sum(8.0 * max(os_ - 1, 0) * npts + 8.0 * npts for os_ in range(S))
-        self.alg = {"history": self.alg_hist_bytes}
+        if self.hmode == FH_H_BLOCKED:
+            # per step: the near slots of the current 64-step block (8 B per value),
+            # the far pair (8 B) read and the sum written (8 B); per block start K:
+            # the far contraction, 2*64*K FP64-equivalent flops per point (10 bf16
+            # slice products each, executed on the 128-point tiles)
+            tpts = sum(-(-(p["N"] + 2) // 128) * 128 for p in params)
+            ks = [k for k in range(64, S, 64)]
+            self.alg_hist_bytes = sum(8.0 * (max(os_ - 1, 0) % 64) * npts + 24.0 * npts for os_ in range(S))
+            self.alg = {"history": self.alg_hist_bytes,
+                        "gemm_flops": sum(2.0 * 64 * k * npts for k in ks),
+                        "gemm_tc_flops": sum(10 * 2.0 * 64 * k * tpts for k in ks),
+                        "gemm_bytes": sum(8.0 * k * tpts + 8.0 * 64 * len(params) * k + 8.0 * 64 * npts for k in ks)}
+        else:
+            self.alg_hist_bytes = sum(8.0 * max(os_ - 1, 0) * npts + 8.0 * npts for os_ in range(S))
+            self.alg = {"history": self.alg_hist_bytes}
         self.config = {"workload": self.name, "instances": len(params), "interior_points": npts,
                        "solve_steps": S, "state_doubles": seg,
-                       "history": "fp64" if self.hmode == FH_H_FP64 else "double-float pairs",
+                       "history": {FH_H_FP64: "fp64", FH_H_DF64: "double-float pairs",
+                                   FH_H_BLOCKED: "blocked: far slots on the tensor cores (exact bf16 slices), "
+                                                 "current 64-step block in double-float"}[self.hmode],
                        "launch_shape": self.tuned,
                        "l2": "inputs larger than L2" if 8 * seg * S > 129e6 else "history fits in L2"}
-        self.kernel = "k_hist_tiles" if self.hmode == FH_H_FP64 else "k_hist_tiles_df"
+        self.kernel = {FH_H_FP64: "k_hist_tiles", FH_H_DF64: "k_hist_tiles_df",
+                       FH_H_BLOCKED: "k_h_near_df + k_hb_gemm (tcgen05, exact bf16 slices)"}[self.hmode]
         if kind == "psi_batch" and self.hmode == FH_H_DF64:
             self.class_profiles = {"history": "k_hist_tiles_df_psi1024.md"}
+        if self.hmode == FH_H_BLOCKED:
+            self.class_kernels = {"history": "k_h_near_df (current block in double-float)",
+                                  "gemm": "k_hb_gemm (tcgen05, exact bf16 slices, per-instance weight rows)",
+                                  "weights": "k_h_weights (near slots) + k_hb_weights (far weight planes)"}
+        self.ctx_ = ctx
 
     def cpu_baseline(self):
         """Oracle port of H_solver (serial) on a bounded sample of the instances,
@@ -428,6 +451,59 @@ class H1D(Workload):
     def solve_device(self):
         self.solver.set_u_device(self.U_d.data_ptr())
         self.solver.calc_step(self.S)
+
+    def compare(self, ctx, stream, main_mode):
+        """One solve of the same batch by the other history modes (CUDA-event
+        timed, graphs on); per-instance relative max-norm differences to the
+        FP64 path (the largest over the instances), and the main mode's at ten
+        output steps."""
+        import torch
+        from theses_code_gb300.solvers import HSolverBatch
+
+        def relmax_inst(a, b):
+            return max(float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300)) for x, y in zip(a, b))
+
+        self.solve_device()
+        res = {main_mode: self.solver.get_u()}
+        times = {}
+        for m in ("fp64", "df64", "blocked"):
+            if m == main_mode:
+                continue
+            sv = HSolverBatch(ctx, self.params_all, self.S + 1, self.hmodes[m])
+            sv.set_u_device(self.U_d.data_ptr())
+            sv.calc_step(self.S)  # first call captures the graph
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sv.set_u_device(self.U_d.data_ptr())
+            e0.record(stream)
+            sv.calc_step(self.S)
+            e1.record(stream)
+            e1.synchronize()
+            times[m] = e0.elapsed_time(e1)
+            res[m] = sv.get_u()
+            sv.close()
+        ref = res["fp64"]
+        out = {}
+        for m, u in res.items():
+            d = {"rel_err_vs_fp64": relmax_inst(u, ref)}
+            if m in times:
+                d["value"] = self.gps / (times[m] / 1e3)
+                d["ms_per_solve"] = times[m]
+            out[m] = d
+        if main_mode != "fp64":
+            every = max(1, self.S // 10)
+            ref_sv = HSolverBatch(ctx, self.params_all, self.S + 1, self.hmodes["fp64"])
+            ref_sv.set_u_device(self.U_d.data_ptr())
+            self.solver.set_u_device(self.U_d.data_ptr())
+            per_step, done = [], 0
+            while done < self.S:
+                n = min(every, self.S - done)
+                ref_sv.calc_step(n)
+                self.solver.calc_step(n)
+                done += n
+                per_step.append(relmax_inst(self.solver.get_u(), ref_sv.get_u()))
+            ref_sv.close()
+            out[main_mode]["rel_err_per_output_step"] = {"every": every, "max": max(per_step), "values": per_step}
+        return out
 
     def solve_host(self):
         L, h = self.solver.ctx.L, self.solver.h
@@ -672,7 +748,7 @@ def run_gb300(args):
         "dtype": "f64", "data": "synthetic", "config": cfg, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clk, "roofline": roofline, "kernels": kernels, "profiled_ms_per_step": tp_ms / args.steps,
     }
-    if args.config in ("tg2d", "ab1d") and not args.no_compare and rank == 0 and \
+    if args.config in ("tg2d", "ab1d", "psi_batch") and not args.no_compare and rank == 0 and \
             (args.config == "tg2d" or args.mode == "blocked"):
         cmp = wl.compare(ctx, stream, args.mode)
         result["modes"] = cmp

@@ -210,12 +210,21 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps);
  * the reference. */
 int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host);
 int fh_h_batch_tstep(const fh_h_batch *b);
-/* History storage, before the first step: FH_H_FP64 (default) or FH_H_DF64
+/* History storage, before the first step: FH_H_FP64 (default), FH_H_DF64
  * ((hi, lo) FP32 pairs summed in double-float on the FP32 pipe, 2^-48
  * relative storage precision; solution within 1e-12 of the FP64 path on the
- * parity cases).  No counterpart in the reference. */
+ * parity cases) or FH_H_BLOCKED: per block of 64 steps, the history slots
+ * older than the block are contracted once for all 64 steps on the tensor
+ * cores (exact bf16 slices with per-point and per-row power-of-two scales,
+ * tcgen05, one 128-point tile of one instance against that instance's 64
+ * weight rows), the block's own slots are summed per step in double-float
+ * from a 128-layer ring; line solves and weights stay FP64; the history costs
+ * 8 bytes per value (slice planes) and the full FP64 history is not kept.
+ * Bound 1e-9 relative against the FP64 oracle.  No counterpart in the
+ * reference. */
 #define FH_H_FP64 0
 #define FH_H_DF64 1
+#define FH_H_BLOCKED 2
 int fh_h_batch_set_mode(fh_h_batch *b, int mode);
 /* Launch-shape autotuner for the batch history sum: times the candidate tile
  * CTAs (128/256/512 threads) x K-split caps (1/8/64) on the batch's buffers

@@ -117,6 +117,31 @@ def test_config3_4096_instances():
     assert sum(e <= TOL_SOLVER for e, _ in report.values()) >= 14, report
 
 
+def test_config3_blocked_mode():
+    """The 4096-instance batch in the blocked history mode (tensor-core far
+    history) against the oracle at the mixed-precision bound, 500 steps."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_H_BLOCKED
+    params, U0s = workloads.psi_batch(n=4096, seed=7)
+    steps = 500
+    idx = sorted(set(int(k) for k in np.random.default_rng(2).choice(4096, 15, replace=False))
+                 | {int(np.argmax([q["N"] for q in params]))})
+    with _pool(len(idx)) as ex:
+        fut = ex.map(_h_oracle, [(params[k], U0s[k], steps) for k in idx])
+        from theses_code_gb300._lib import Context
+        from theses_code_gb300.solvers import HSolverBatch
+        c = Context(0)
+        s = HSolverBatch(c, params, steps + 1, FH_H_BLOCKED)
+        s.set_u(U0s)
+        s.calc_step(steps)
+        got = s.get_u()
+        s.close()
+        c.close()
+        refs = list(fut)
+    errs = {k: relmax(got[k], r) for k, r in zip(idx, refs)}
+    assert max(errs.values()) <= TOL_MIXED, errs
+
+
 def test_config4_2048_line(ctx):
     from theses_code_gb300 import workloads
     from theses_code_gb300._lib import FH_AB_BLOCKED, FH_AB_FP64

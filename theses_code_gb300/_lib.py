@@ -16,7 +16,7 @@ FH_W_L1, FH_W_PSI = 0, 1
 FH_K_CONST, FH_K_EXP = 0, 1
 FH_TG_FP64, FH_TG_BLOCKED, FH_TG_DF64 = 0, 1, 2
 FH_AB_FP64, FH_AB_BLOCKED = 0, 1
-FH_H_FP64, FH_H_DF64 = 0, 1
+FH_H_FP64, FH_H_DF64, FH_H_BLOCKED = 0, 1, 2
 FH_PROF_HISTORY, FH_PROF_SWEEP, FH_PROF_WEIGHTS, FH_PROF_GEMM = 0, 1, 2, 3
 FH_NOALLOC_SCRATCH_DOUBLES = 2097152
 

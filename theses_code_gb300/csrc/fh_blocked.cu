@@ -30,12 +30,15 @@
 // deadline; on expiry the kernel records FH_ETIMEOUT, waits (bounded) for its
 // own copies and MMAs, frees TMEM and returns.
 #include <cuda.h>
+
+#include <vector>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include "fh_common.cuh"
 #include "fh_internal.h"
 #include "fh_sm100.cuh"
+#include "fh_slices.cuh"
 #include "fh_weights.cuh"
 
 namespace {
@@ -45,7 +48,7 @@ constexpr int kBK = 64;   // layers per chunk / pipeline stage (one 128-byte row
 constexpr int kStages = 2;
 constexpr uint32_t kTileA = kBM * kBK * 2;          // 16 KiB
 constexpr uint32_t kTileB = kBN * kBK * 2;          // 8 KiB
-constexpr int kSlices = 4;
+constexpr int kSlices = kSlcN;
 constexpr int kLevels = kSlices;                     // levels l = i + j <= 3
 constexpr uint32_t kStageBytes = kSlices * (kTileA + kTileB);  // 96 KiB
 constexpr int kEpiWarps = 8;
@@ -53,28 +56,6 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
 }  // namespace
-
-// Chunk groups (pairs of 64-layer chunks, see fh_slice_row_group).
-__host__ __device__ inline int fh_ngroups(int nchunks) { return (nchunks + 1) / 2; }
-
-// x = 2^E (a0 + a1/2^8 + a2/2^16 + a3/2^24) with integer |a_i| <= 128 given |x| < 2^(E+7).
-__device__ __forceinline__ void fh_slice4(double x, int E, __nv_bfloat16 (&b)[kSlices]) {
-  double r = ldexp(x, -E);
-#pragma unroll
-  for (int i = 0; i < kSlices; ++i) {
-    const double a = rint(r);
-    b[i] = __double2bfloat16(a);
-    r = (r - a) * 256.0;
-  }
-}
-
-// Exponent E with max|x| < 2^(E+7); 0 for an all-zero chunk.
-__device__ __forceinline__ int fh_chunk_exp(double mx) {
-  if (!(mx > 0.0)) return 0;
-  int q;
-  frexp(mx, &q);  // mx = f 2^q, f in [0.5, 1)
-  return q - 7;
-}
 
 __device__ __forceinline__ float fh_exp2i(int e) {
   // 2^e as float (0 below the normal range; e stays far below the overflow range here)
@@ -310,43 +291,234 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 1) fh_tmem_dealloc(tmem, kTmemCols);
 }
 
+// ----------------------------------------------------------------------------
+// Batched form (1D instances of a batch, each with its own weights): the far
+// history of the next 64 steps of every instance,
+//   far[n][p] = sum_{k<K} W_inst(p)[n][k] * H[k][p],   n < 64,
+// with the roles of the operands swapped against k_far_gemm: A = 128
+// consecutive history points of one instance (K-major planes H3[s][p][k]),
+// B = that instance's 64 weight rows (planes W3[s][inst*64 + n][k]), so the
+// TMEM accumulator holds 128 points (lanes) x 64 steps (columns) x 4 levels,
+// double-buffered (512 columns).  The tiles come from a list (first point,
+// instance, valid points); a tile may reach into the next instance's points,
+// whose results are not stored.  Exponents: Ed[c][p] per point, Ew[c][row]
+// per weight row.  Same pipeline, exactness argument and bounded waits as
+// k_far_gemm.
+struct fh_hb_tile {
+  long long p0;  // first point (concatenated point index)
+  int inst;      // instance: weight rows inst*64 .. inst*64 + 63
+  int np;        // valid points of the instance in this tile (<= 128)
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_hb_gemm(const __grid_constant__ CUtensorMap tmH, const __grid_constant__ CUtensorMap tmW, int K,
+              const fh_hb_tile *__restrict__ tiles, int ntiles, const int8_t *__restrict__ Ew, long long R,
+              const int8_t *__restrict__ Ed, long long Ppad, float2 *__restrict__ far, long long ldf,
+              int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  const uint32_t raw = fh_smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t *gbase = smem_raw + (base - raw);
+  const uint32_t bars = base + kStages * kStageBytes;
+  uint8_t *gbars = gbase + kStages * kStageBytes;
+  auto full = [&](int s) { return bars + 8u * s; };
+  auto empty = [&](int s) { return bars + 8u * (kStages + s); };
+  auto accfull = [&](int b) { return bars + 8u * (2 * kStages + b); };
+  auto accempty = [&](int b) { return bars + 8u * (2 * kStages + 2 + b); };
+  const uint32_t mmadone = bars + 8u * (2 * kStages + 4);
+  const uint32_t tslot = bars + 8u * (2 * kStages + 5);
+  volatile uint32_t *tslot_g = reinterpret_cast<volatile uint32_t *>(gbars + 8 * (2 * kStages + 5));
+  volatile int *sh_err = reinterpret_cast<volatile int *>(gbars + 8 * (2 * kStages + 6));
+  constexpr uint32_t kTileH = 128 * kBK * 2;  // 128 points x 64 layers bf16
+  constexpr uint32_t kTileW = kBN * kBK * 2;  // 64 rows x 64 layers bf16
+  static_assert(kSlices * (kTileH + kTileW) == kStageBytes, "stage layout");
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunks = K / kBK;
+  const int ngroups = fh_ngroups(nchunks);
+  const int my_items = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      fh_mbar_init(full(s), 1);
+      fh_mbar_init(empty(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      fh_mbar_init(accfull(b), 1);
+      fh_mbar_init(accempty(b), 32 * kEpiWarps);
+    }
+    fh_mbar_init(mmadone, 1);
+    *sh_err = 0;
+    fh_fence_mbar_init();
+  }
+  if (warp == 1) {
+    fh_tmem_alloc(tslot, kTmemCols);
+    fh_tmem_relinquish();
+  }
+  fh_tc_fence_before();
+  __syncthreads();
+  fh_tc_fence_after();
+  const uint32_t tmem = *tslot_g;
+  bool ok = true;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int last_issued[kStages];
+      for (int s = 0; s < kStages; ++s) last_issued[s] = -1;
+      int g = 0;  // stage counter
+      for (int k = 0; k < my_items && ok; ++k) {
+        const fh_hb_tile T = tiles[(int)blockIdx.x + k * (int)gridDim.x];
+        for (int c = 0; c < nchunks; ++c, ++g) {
+          const int s = g % kStages;
+          if (g >= kStages && !fh_mbar_wait(empty(s), ((g / kStages) - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          fh_mbar_arrive_expect_tx(full(s), kStageBytes);
+          const uint32_t sb = base + s * kStageBytes;
+          for (int pl = 0; pl < kSlices; ++pl)
+            fh_tma_load_3d(sb + pl * kTileH, &tmH, c * kBK, (int)T.p0, pl, full(s));
+          for (int pl = 0; pl < kSlices; ++pl)
+            fh_tma_load_3d(sb + kSlices * kTileH + pl * kTileW, &tmW, c * kBK, T.inst * kBN, pl, full(s));
+          last_issued[s] = g;
+        }
+      }
+      if (!ok) {
+        *sh_err = 1;
+        for (int s = 0; s < kStages; ++s)
+          if (last_issued[s] >= 0) fh_mbar_wait(full(s), (last_issued[s] / kStages) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = fh_idesc_bf16_f32(128, kBN);
+      int gc = 0;  // chunk counter (stage ring)
+      int gg = 0;  // group counter (accumulator buffers)
+      for (int k = 0; k < my_items && ok; ++k) {
+        for (int G = 0; G < ngroups && ok; ++G, ++gg) {
+          const int nc = min(2, nchunks - 2 * G);
+          const int b = gg & 1;
+          if (gg >= 2 && !fh_mbar_wait(accempty(b), ((gg >> 1) - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t lv0 = tmem + (uint32_t)(b * kLevels * kBN);
+          uint32_t first[kLevels] = {0, 0, 0, 0};
+          for (int cc = 0; cc < nc; ++cc, ++gc) {
+            const int s = gc % kStages;
+            if (!fh_mbar_wait(full(s), (gc / kStages) & 1)) {
+              ok = false;
+              break;
+            }
+            fh_tc_fence_after();
+            const uint32_t sb = base + s * kStageBytes;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+              const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+              const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+#pragma unroll
+              for (int q = 0; q < 10; ++q) {
+                const int l = ia[q] + ib[q];
+                const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileH + kk * 32);
+                const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileH + ib[q] * kTileW + kk * 32);
+                fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
+                first[l] = 1;
+              }
+            }
+            fh_mma_commit(empty(s));
+          }
+          if (!ok) break;
+          fh_mma_commit(accfull(b));
+        }
+      }
+      fh_mma_commit(mmadone);
+      if (!fh_mbar_wait(mmadone, 0)) ok = false;
+      if (!ok) *sh_err = 1;
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4)..+31 (points), the two warps
+    // of a lane quarter split the 64 columns (steps)
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const uint32_t lanebase = (uint32_t)(32 * q) << 16;
+    const int col0 = 32 * half;
+    int gg = 0;
+    for (int k = 0; k < my_items && ok; ++k) {
+      const fh_hb_tile T = tiles[(int)blockIdx.x + k * (int)gridDim.x];
+      const int pt = 32 * q + lane;
+      const long long p = T.p0 + pt;
+      const long long row0 = (long long)T.inst * kBN + col0;
+      float HI[32], LO[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) HI[i] = LO[i] = 0.f;
+      for (int G = 0; G < ngroups; ++G, ++gg) {
+        const int b = gg & 1;
+        // exponents of this group (loaded before the wait: they do not depend on it)
+        const int ed = p < Ppad ? (int)Ed[(long long)(2 * G) * Ppad + p] : 0;
+        const uint4 *ewv = reinterpret_cast<const uint4 *>(Ew + (long long)(2 * G) * R + row0);
+        const uint4 ev0 = __ldg(ewv), ev1 = __ldg(ewv + 1);
+        const uint32_t ew32[8] = {ev0.x, ev0.y, ev0.z, ev0.w, ev1.x, ev1.y, ev1.z, ev1.w};
+        if (!__all_sync(0xffffffffu, fh_mbar_wait(accfull(b), (gg >> 1) & 1))) {
+          ok = false;
+          break;
+        }
+        fh_tc_fence_after();
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          float L0[16], L1[16], L2[16], L3[16];
+          const uint32_t cb = tmem + lanebase + (uint32_t)(b * kLevels * kBN + col0 + 16 * t);
+          fh_tmem_ld16(cb, L0);
+          fh_tmem_ld16(cb + kBN, L1);
+          fh_tmem_ld16(cb + 2 * kBN, L2);
+          fh_tmem_ld16(cb + 3 * kBN, L3);
+          fh_tmem_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            // T = L0 + L1/2^8 + L2/2^16 + L3/2^24 exactly as (th, tl) (see k_far_gemm)
+            const float x1 = L1[i] * 0.00390625f;
+            float th = L0[i] + x1;
+            const float bb = th - L0[i];
+            float tl = (L0[i] - (th - bb)) + (x1 - bb);
+            tl += L2[i] * 1.52587890625e-05f;
+            const float tr = th + tl;
+            tl = tl - (tr - th);
+            th = tr;
+            tl += L3[i] * 5.9604644775390625e-08f;
+            const int kk = 16 * t + i;
+            const float sc = fh_exp2i(ed + (int)(int8_t)(ew32[kk >> 2] >> (8 * (kk & 3))));
+            const float vh = th * sc, vl = tl * sc;
+            const float s2 = HI[kk] + vh;
+            const float bs = s2 - HI[kk];
+            const float e = (HI[kk] - (s2 - bs)) + (vh - bs);
+            HI[kk] = s2;
+            LO[kk] += e + vl;
+          }
+        }
+        fh_tc_fence_before();
+        fh_mbar_arrive(accempty(b));
+      }
+      if (ok && nchunks > 0 && pt < T.np) {
+#pragma unroll
+        for (int kk = 0; kk < 32; ++kk) {
+          const float h = HI[kk] + LO[kk];
+          far[(long long)(col0 + kk) * ldf + p] = make_float2(h, LO[kk] - (h - HI[kk]));
+        }
+      }
+    }
+    if (!ok) *sh_err = 1;
+  }
+  fh_tc_fence_before();
+  __syncthreads();
+  fh_tc_fence_after();
+  if (threadIdx.x == 0 && *sh_err) atomicOr(err, 1);
+  if (warp == 1) fh_tmem_dealloc(tmem, kTmemCols);
+}
+
 // Chunk groups: group G covers the 64-layer chunks 2G and 2G+1 (the last group
 // holds one chunk when the chunk count is odd).  All chunks of a group share
 // the row exponent Ew and the history exponent Ed, so the tensor cores can
 // accumulate a whole group (128 layers: level sums <= 4*128*2^14 = 2^23, still
-// exact in FP32) before the epilogue combines it.
-
-// One warp slices row m of group G: val(k) is the weight of layer k.
-template <class Val>
-__device__ __forceinline__ void fh_slice_row_group(const Val &val, int G, int nchunks, int m, int Kcap,
-                                                   __nv_bfloat16 *__restrict__ A3, int8_t *__restrict__ Ew) {
-  const int lane = threadIdx.x & 31;
-  const int c0 = 2 * G, nc = min(2, nchunks - c0);
-  double w[4];
-  double mx = 0.0;
-#pragma unroll
-  for (int h = 0; h < 4; ++h) {
-    const int k = c0 * kBK + lane + 32 * h;
-    w[h] = h < 2 * nc ? val(k) : 0.0;
-    mx = fmax(mx, fabs(w[h]));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int E = fh_chunk_exp(mx);
-  if (lane == 0)
-    for (int c = c0; c < c0 + nc; ++c) Ew[(long long)c * kBM + m] = (int8_t)E;
-  const long long plane = (long long)kBM * Kcap;
-#pragma unroll
-  for (int h = 0; h < 4; ++h) {
-    if (h >= 2 * nc) break;
-    const int k = c0 * kBK + lane + 32 * h;
-    __nv_bfloat16 bs[kSlices];
-    fh_slice4(w[h], E, bs);
-    const long long o = (long long)m * Kcap + k;
-#pragma unroll
-    for (int i = 0; i < kSlices; ++i) A3[i * plane + o] = bs[i];
-  }
-}
+// exact in FP32) before the epilogue combines it (fh_slices.cuh).
 
 // Weight planes of a TG block: row m = 2r + {0: x, 1: y} of step j0 + r,
 // A3[s][m][k] (K-major) and Ew[c][m]; one warp per (row, chunk group).
@@ -359,7 +531,7 @@ __global__ void k_blk_weights(int j0, int K, int Kcap, double Da, double tau, do
     const double w = k < K ? Da * fh_psi_int((double)k + 0.0, (double)k + 1.0, X, tau, alpha, beta) : 0.0;
     return fabs(w) < cut ? 0.0 : w;
   };
-  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, kBM, Kcap, A3, Ew);
 }
 
 // Toeplitz weight rows (1D solvers with lag weights): row m = step T0 + 1 + m
@@ -370,7 +542,7 @@ __global__ void k_blk_toeplitz_rows(const double *__restrict__ w, int base, int 
   const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (m >= kBM) return;
   auto val = [&](int k) { return (k < K && m < mrows) ? w[base + m - k] : 0.0; };
-  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, kBM, Kcap, A3, Ew);
 }
 
 // Weight rows W[m*ldw + k], k < K, rows m >= mrows are zero (standalone
@@ -380,7 +552,7 @@ __global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, in
   const int m = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (m >= kBM) return;
   auto val = [&](int k) { return (k < K && m < mrows) ? W[(long long)m * ldw + k] : 0.0; };
-  fh_slice_row_group(val, blockIdx.x, K / kBK, m, Kcap, A3, Ew);
+  fh_slice_row_group(val, blockIdx.x, K / kBK, m, kBM, Kcap, A3, Ew);
 }
 
 // Slices of a double-float value (hi, lo) scaled by 2^-E, |hi + lo| < 2^(E+7):
@@ -432,7 +604,7 @@ constexpr int kCvPts = 64;
 constexpr int kCvPitch = kBK + 2;  // bf16 per staged row
 constexpr size_t kCvSmemPerChunk = sizeof(__nv_bfloat16) * kSlices * kCvPts * kCvPitch;
 template <int NCH>
-__global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict__ D, long long ldd, long long P,
+__global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict__ D, long long ldd, int kd0, long long P,
                                                         long long Ppad, int kg0, int Kcap,
                                                         __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
   extern __shared__ __align__(16) __nv_bfloat16 cvout[];  // [NCH][kSlices][kCvPts * kCvPitch]
@@ -447,7 +619,7 @@ __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict
 #pragma unroll
   for (int i = 0; i < kL; ++i) {
     float2 v = make_float2(0.f, 0.f);
-    if (p < P) v = __ldcs(D + (long long)(kg0 + qh * kL + i) * ldd + p);
+    if (p < P) v = __ldcs(D + (long long)(kg0 - kd0 + qh * kL + i) * ldd + p);
     hi[i] = v.x;
     lo[i] = v.y;
     mx = fmaxf(mx, fabsf(v.x));
@@ -618,10 +790,10 @@ int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k
     const float2 *Dp = reinterpret_cast<const float2 *>(D);
     if (nch == 2)
       k_blk_convert_df<2><<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
-          Dp, ldd, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+          Dp, ldd, 0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
     else
       k_blk_convert_df<1><<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
-          Dp, ldd, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+          Dp, ldd, 0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
     return fh_after_launch(ctx, "k_blk_convert_df");
   }
   k_blk_convert<<<(unsigned)(b.Ppad / 64), 64, sizeof(double) * nch * kBK * 64, ctx->stream>>>(
@@ -697,6 +869,97 @@ int fh_blk_gemm(fh_ctx *ctx, fh_blk &b, int K, float2 *out, long long ldo, int g
   }
   fh_prof_mark(ctx, FH_PROF_GEMM, true);
   return rc;
+}
+
+// ------------------------------------------------------------ batched form
+// Planes, exponents, weight planes, tile list and tensor maps of the batched
+// far contraction (k_hb_gemm).  History planes H3[s][Ppad][Kcap] over the
+// concatenated points; weight planes W3[s][R][Kcap], R = 64 rows per instance.
+struct fh_hblk {
+  long long P = 0, Ppad = 0, R = 0;
+  int Kcap = 0, ntiles = 0, nsm = 1;
+  fh_dbuf H3, Ed, W3, Ew, tiles, err;
+  CUtensorMap mapH, mapW;
+};
+
+fh_hblk *fh_hblk_new() { return new fh_hblk(); }
+void fh_hblk_delete(fh_hblk *b) { delete b; }
+__nv_bfloat16 *fh_hblk_wplanes(fh_hblk &b) { return b.W3.as<__nv_bfloat16>(); }
+int8_t *fh_hblk_wexp(fh_hblk &b) { return b.Ew.as<int8_t>(); }
+int fh_hblk_kcap(const fh_hblk &b) { return b.Kcap; }
+
+// tiles: (first point, instance, valid points) of every 128-point tile
+int fh_hblk_init(fh_ctx *ctx, fh_hblk &b, long long P, int Kcap, int ninst, const long long *tile_p0,
+                 const int *tile_inst, const int *tile_np, int ntiles) {
+  FH_REQUIRE(ctx, Kcap % kBK == 0 && Kcap > 0 && ninst > 0 && ntiles > 0, FH_EINVAL, "batched contraction: sizes");
+  b.P = P;
+  b.Ppad = fh_ceil_div(P + 128, 128) * 128;  // a tile starting at any point stays inside
+  b.R = (long long)ninst * kBN;
+  b.Kcap = Kcap;
+  b.ntiles = ntiles;
+  FH_CUDA_TRY(ctx, cudaDeviceGetAttribute(&b.nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  int rc;
+  if ((rc = fh_alloc(ctx, b.H3, sizeof(__nv_bfloat16) * kSlices * (size_t)b.Ppad * Kcap)) ||
+      (rc = fh_alloc(ctx, b.Ed, (size_t)b.Ppad * (Kcap / kBK))) ||
+      (rc = fh_alloc(ctx, b.W3, sizeof(__nv_bfloat16) * kSlices * (size_t)b.R * Kcap)) ||
+      (rc = fh_alloc(ctx, b.Ew, (size_t)b.R * (Kcap / kBK))) ||
+      (rc = fh_alloc(ctx, b.tiles, sizeof(fh_hb_tile) * (size_t)ntiles, false)) ||
+      (rc = fh_alloc(ctx, b.err, sizeof(int))))
+    return rc;
+  std::vector<fh_hb_tile> t((size_t)ntiles);
+  for (int i = 0; i < ntiles; ++i) {
+    FH_REQUIRE(ctx, tile_p0[i] >= 0 && tile_p0[i] < P && tile_np[i] >= 1 && tile_np[i] <= 128 && tile_inst[i] >= 0 &&
+                        tile_inst[i] < ninst,
+               FH_EINVAL, "batched contraction: tile %d", i);
+    t[(size_t)i] = fh_hb_tile{tile_p0[i], tile_inst[i], tile_np[i]};
+  }
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(b.tiles.p, t.data(), sizeof(fh_hb_tile) * t.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // t is a local buffer
+  if ((rc = make_map(ctx, &b.mapH, b.H3.p, (unsigned long long)Kcap, (unsigned long long)b.Ppad, 128))) return rc;
+  if ((rc = make_map(ctx, &b.mapW, b.W3.p, (unsigned long long)Kcap, (unsigned long long)b.R, kBN))) return rc;
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_hb_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(2 * kCvSmemPerChunk)));
+  return FH_OK;
+}
+
+// Converts history chunk c (layers [64c, 64c + 64)) held in a ring of
+// (hi, lo) pairs (ring row r = layer r mod 128, pitch ldd); an odd chunk
+// completes its group and both chunks are (re)converted with the group's
+// per-point exponents, so the ring must still hold the even partner.
+int fh_hblk_convert(fh_ctx *ctx, fh_hblk &b, const float2 *ring, long long ldd, int c) {
+  FH_REQUIRE(ctx, c >= 0 && (c + 1) * kBK <= b.Kcap, FH_EINVAL, "batched contraction: chunk %d", c);
+  const int kg0 = ((c & 1) ? c - 1 : c) * kBK;
+  const int kd0 = (kg0 / 128) * 128;  // layer held in ring row 0
+  if (c & 1)
+    k_blk_convert_df<2><<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
+        ring, ldd, kd0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+  else
+    k_blk_convert_df<1><<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
+        ring, ldd, kd0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+  return fh_after_launch(ctx, "k_blk_convert_df");
+}
+
+// far[n*ldf + p] = sum_{k<K} W3[inst(p)*64 + n][k] H[k][p] as (hi, lo) pairs,
+// for the valid points of every tile.
+int fh_hblk_gemm(fh_ctx *ctx, fh_hblk &b, int K, float2 *far, long long ldf) {
+  FH_REQUIRE(ctx, K % kBK == 0 && K > 0 && K <= b.Kcap, FH_EINVAL, "batched contraction: K=%d", K);
+  fh_prof_mark(ctx, FH_PROF_GEMM, false);
+  k_hb_gemm<<<(unsigned)(b.ntiles < b.nsm ? b.ntiles : b.nsm), kThreads, kSmemBytes, ctx->stream>>>(
+      b.mapH, b.mapW, K, b.tiles.as<fh_hb_tile>(), b.ntiles, b.Ew.as<int8_t>(), b.R, b.Ed.as<int8_t>(), b.Ppad, far,
+      ldf, b.err.as<int>());
+  const int rc = fh_after_launch(ctx, "k_hb_gemm");
+  fh_prof_mark(ctx, FH_PROF_GEMM, true);
+  return rc;
+}
+
+int fh_hblk_check(fh_ctx *ctx, fh_hblk &b) {
+  int h = 0;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(&h, b.err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) return fh_set_error(ctx, FH_ETIMEOUT, "batched contraction: a bounded wait expired");
+  return FH_OK;
 }
 
 __global__ void k_pairs_to_double(const float2 *__restrict__ in, long long ldi, long long P, double *__restrict__ out,

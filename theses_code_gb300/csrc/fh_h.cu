@@ -18,7 +18,21 @@
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
 #include "fh_df.cuh"
+#include "fh_slices.cuh"
 #include "fh_weights.cuh"
+
+// batched far contraction on the tensor cores (fh_blocked.cu)
+struct fh_hblk;
+fh_hblk *fh_hblk_new();
+void fh_hblk_delete(fh_hblk *b);
+int fh_hblk_init(fh_ctx *ctx, fh_hblk &b, long long P, int Kcap, int ninst, const long long *tile_p0,
+                 const int *tile_inst, const int *tile_np, int ntiles);
+int fh_hblk_convert(fh_ctx *ctx, fh_hblk &b, const float2 *ring, long long ldd, int c);
+int fh_hblk_gemm(fh_ctx *ctx, fh_hblk &b, int K, float2 *far, long long ldf);
+int fh_hblk_check(fh_ctx *ctx, fh_hblk &b);
+__nv_bfloat16 *fh_hblk_wplanes(fh_hblk &b);
+int8_t *fh_hblk_wexp(fh_hblk &b);
+int fh_hblk_kcap(const fh_hblk &b);
 
 struct fh_h_dev_inst {
   int N, weights, kmodel, gravity;
@@ -51,7 +65,7 @@ struct fh_h_batch {
   fh_dbuf inst, U, D, W, Lb, ibt, lgt, wc, part, Al, Bt, sA, sB, sR, sOm;
   fh_graph_cache graph;
   bool use_graph = true;
-  int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs
+  int mode = FH_H_FP64;  // FH_H_DF64: history as (hi, lo) FP32 pairs; FH_H_BLOCKED: below
   // Al of the variable-coefficient instances serially in the reference order
   // (h_alpha_serial); varcoef: the batch has such instances
   bool serial_al = true, varcoef = false;
@@ -67,9 +81,16 @@ struct fh_h_batch {
   cudaStream_t hs = nullptr;
   cudaEvent_t ev_main = nullptr, ev_w = nullptr;
   int w_ready = -1;
+  // FH_H_BLOCKED: history slots older than the current 64-step block in bf16
+  // slice planes (hb), contracted once per block for its 64 steps into far
+  // rows; the slots of the last two chunks as (hi, lo) pairs in a 128-layer
+  // ring (slot t in row t mod 128)
+  fh_hblk *hb = nullptr;
+  fh_dbuf ring, far;
   double *Wp(int par) const { return W.as<double>() + (long long)par * n * max_weights; }
   double *wcp(int par) const { return wc.as<double>() + (long long)par * n; }
   ~fh_h_batch() {
+    if (hb) fh_hblk_delete(hb);
     if (hs) cudaStreamDestroy(hs);
     if (ev_main) cudaEventDestroy(ev_main);
     if (ev_w) cudaEventDestroy(ev_w);
@@ -92,13 +113,13 @@ static constexpr int kIbStride = 2 * kIbTerms + 4;
 // and wc[b], the weight of the current slot [tstep, tstep + 1].  The
 // reference's t = 0 term multiplies layer1 - layer1 (its layer pointer starts
 // at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
-// Thread i of CTA (x, b) owns slot i = x*128 + threadIdx.x; i = max(os - 1, 0)
-// is the current slot.
-__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, double *__restrict__ W,
-                            int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
+// Thread i of CTA (x, b) owns slot i = t_lo + x*128 + threadIdx.x (slots below
+// t_lo are not computed); i = max(os - 1, 0) is the current slot.
+__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, int t_lo,
+                            double *__restrict__ W, int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
                             const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX) {
   const int b = blockIdx.y;
-  const int i = blockIdx.x * kHWeightThreads + threadIdx.x;
+  const int i = t_lo + blockIdx.x * kHWeightThreads + threadIdx.x;
   const int nh = os > 1 ? os - 1 : 0;  // history slots
   if (i > nh) return;
   const fh_h_dev_inst I = inst[b];
@@ -581,6 +602,160 @@ __global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
                                          Bt, sA, sB, sR, sOm, Dnew, append, first, dfstore, sV, smm, sma, serial);
 }
 
+// ---------------------------------------------------- blocked history mode
+// psi = t^beta node value F(x) = B(y(x); 1/beta, 1-alpha) at X (lower series
+// r P(y), flag low = 1) or its upper tail U(c) = c^b Q(c) (low = 0), from the
+// per-instance tables and the log table: one exp or expm1 + log + exp and one
+// Horner polynomial per node.  A slot weight is the difference of its two
+// nodes; the difference loses ~log10(X) digits, which is far below the 2^-32
+// of the bf16 slices the blocked contraction uses these weights at.
+__device__ __forceinline__ void h_psi_node(const fh_h_dev_inst &I, const double *__restrict__ Lc,
+                                           const double2 *__restrict__ lgt, int x, int X, double invX, double &v,
+                                           int &low) {
+  if (x <= 0) {
+    v = 0.0;
+    low = 1;
+    return;
+  }
+  if (x >= X) {  // c = 0
+    v = 0.0;
+    low = 0;
+    return;
+  }
+  const double *Uc = Lc + kIbTerms;
+  const double2 lx = lgt[x], lX = lgt[X];
+  const double sh = lx.x - lX.x;
+  const double sl = (lx.x - (sh + lX.x)) + (lx.y - lX.y);
+  const double th = I.beta * sh;
+  const double tl = fma(I.beta, sh, -th) + I.beta * sl;
+  const double r = (double)x * invX;
+  if (r <= Lc[2 * kIbTerms + 1]) {  // y <= kIbLowMax: lower series in y
+    const double ey = exp(th);
+    const double y = fma(ey, tl, ey);
+    v = r * fh_series(fh_ib_coef_tab{Lc}, fh_ib_nterms(y), y);
+    low = 1;
+  } else {  // upper tail in c = 1 - y
+    const double em = expm1(th);
+    const double c = -fma(em + 1.0, tl, em);
+    v = c <= 0.0 ? 0.0 : exp((1.0 - I.alpha) * log(c)) * fh_series(fh_ib_coef_tab{Uc}, fh_ib_nterms(c), c);
+    low = 0;
+  }
+}
+
+// Weight planes of the block whose first step has K = 64 blk history slots:
+// row m = 64 inst + r is step tstep = K + r + 2 (X = K + r + 3) of instance
+// inst, weighing the slots t < K (slot 0: weight 0, as in k_h_weights); rows
+// past the last step are zero.  One warp per (row, chunk group), sliced into
+// W3/Ew (fh_slices.cuh).
+__global__ void k_hb_weights(const fh_h_dev_inst *__restrict__ inst, int K, int max_steps,
+                             const double *__restrict__ Lb, int ldw, const double *__restrict__ ibt,
+                             const double2 *__restrict__ lgt, long long R, int Kcap, __nv_bfloat16 *__restrict__ W3,
+                             int8_t *__restrict__ Ew) {
+  const long long m = (long long)blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= R) return;  // whole warp
+  const int lane = threadIdx.x & 31;
+  const int b = (int)(m / kSlcK), r = (int)(m % kSlcK);
+  const fh_h_dev_inst I = inst[b];
+  const int G = blockIdx.x, nchunks = K / kSlcK;
+  const int tstep = K + r + 2, X = tstep + 1, os = K + r + 1;
+  const bool live = tstep <= max_steps;
+  double w[4];
+  const int k0 = 2 * G * kSlcK + lane;
+  if (I.weights == FH_W_L1) {
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int k = k0 + 32 * h;
+      w[h] = (live && k >= 1 && k < K) ? Lb[(long long)b * ldw + (os - k - 1)] : 0.0;
+    }
+  } else if (I.beta == 1.0) {
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int k = k0 + 32 * h;
+      w[h] = (live && k >= 1 && k < K)
+                 ? fh_psi_int_t((double)k, (double)k + 1.0, (double)X, I.tau, I.alpha) * (1 - I.alpha)
+                 : 0.0;
+    }
+  } else {
+    const double *Lc = ibt + (long long)b * kIbStride;
+    const double invX = 1.0 / (double)X;
+    double v[5];
+    int lo[5];
+    // nodes k0 + 32 h (h < 4) and, for lane 31, the upper node 128 G + 128 of
+    // the group's last slot
+#pragma unroll
+    for (int h = 0; h < 5; ++h) {
+      v[h] = 0.0;
+      lo[h] = 1;
+      if (live && (h < 4 || lane == 31))
+        h_psi_node(I, Lc, lgt, h < 4 ? k0 + 32 * h : 2 * G * kSlcK + 128, X, invX, v[h], lo[h]);
+    }
+    const double sc = live ? exp((1.0 - I.alpha * I.beta) * (lgt[X].x + Lc[2 * kIbTerms + 2])) *
+                                 Lc[2 * kIbTerms + 3] * (1 - I.alpha)
+                           : 0.0;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      // upper node of slot k = k0 + 32 h: node k + 1 (the next lane, or lane 0 of the next h)
+      double v1 = __shfl_down_sync(0xffffffffu, v[h], 1);
+      int l1 = __shfl_down_sync(0xffffffffu, lo[h], 1);
+      const double vn = __shfl_sync(0xffffffffu, v[h + 1], 0);
+      const int ln = __shfl_sync(0xffffffffu, lo[h + 1], 0);
+      if (lane == 31) {
+        v1 = h < 3 ? vn : v[4];
+        l1 = h < 3 ? ln : lo[4];
+      }
+      const int k = k0 + 32 * h;
+      double diff;
+      if (lo[h] && l1)
+        diff = v1 - v[h];
+      else if (!lo[h])
+        diff = v[h] - v1;
+      else
+        diff = (Lc[2 * kIbTerms] - v1) - v[h];
+      w[h] = (live && k >= 1 && k < K) ? sc * diff : 0.0;
+    }
+  }
+  fh_slice_group_values(w, G, nchunks, m, R, Kcap, W3, Ew);
+}
+
+// History sum of the blocked mode at one step: part[p] = far[p] + sum over
+// the near slots t in [t_lo, K) of W[inst][t] * ring[t mod 128][p], in
+// double-float (the far row holds the contraction of the older slots; null
+// before the first block has one), two points per thread over the
+// per-instance tiles; written as FP64 for the line kernels.
+__global__ void __launch_bounds__(kTileThreads) k_h_near_df(const fh_h_tile *__restrict__ tiles,
+                                                            const fh_h_dev_inst *__restrict__ inst,
+                                                            const float2 *__restrict__ ring, long long ldr, int t_lo,
+                                                            int K, const double *__restrict__ W, int ldw,
+                                                            const float2 *__restrict__ far,
+                                                            double *__restrict__ part) {
+  __shared__ float2 wsf2[kSlcK];
+  const fh_h_tile T = tiles[blockIdx.x];
+  const int nk = K - t_lo;  // < 64
+  const double *wrow = W + (long long)T.inst * ldw + t_lo;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) wsf2[i] = fh_df_pair(fh_df_from_double(wrow[i]));
+  __syncthreads();
+  const int q = threadIdx.x * 2;
+  if (q >= T.len) return;
+  const long long p = inst[T.inst].off + T.start + q;
+  fh_df a0{0.f, 0.f}, a1{0.f, 0.f};
+  if (far) {
+    const float4 f = *reinterpret_cast<const float4 *>(far + p);
+    a0 = fh_df{f.x, f.y};
+    a1 = fh_df{f.z, f.w};
+  }
+  for (int k = 0; k < nk; ++k) {
+    const int t = t_lo + k;
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(ring + (long long)(t & 127) * ldr + p));
+    const fh_df w = fh_df_from_pair(wsf2[k]);
+    a0 = fh_df_fma(w, fh_df{v.x, v.y}, a0);
+    a1 = fh_df_fma(w, fh_df{v.z, v.w}, a1);
+  }
+  double2 o;
+  o.x = fh_df_to_double(a0);
+  o.y = fh_df_to_double(a1);
+  *reinterpret_cast<double2 *>(part + p) = o;
+}
+
 // ------------------------------------------------------------------- host
 
 // K splits of the batch history sum: enough CTAs for ~3 waves of 8 resident
@@ -621,14 +796,17 @@ static int h_hist(fh_h_batch *B, int ti, int K, int splits, int kchunk, const do
   return fh_after_launch(ctx, "k_hist_tiles");
 }
 
-// Weights of step `tstep` (os saved layers) into the buffer pair `par`.
-static int h_weights(fh_h_batch *B, int tstep, int os, int par, cudaStream_t st) {
+// Weights of step `tstep` (os saved layers) into the buffer pair `par`: the
+// history slots from t_lo on and the current weight.
+static int h_weights(fh_h_batch *B, int tstep, int os, int par, cudaStream_t st, int t_lo = 0) {
   fh_ctx *ctx = B->ctx;
   FH_REQUIRE(ctx, tstep + 1 < B->max_steps + 2, FH_EINVAL, "h_weights: step %d beyond the log table", tstep);
-  dim3 gw((unsigned)((os > 1 ? os - 1 : 0) / kHWeightThreads + 1), (unsigned)B->n);  // history slots + current
+  const int nh = os > 1 ? os - 1 : 0;
+  if (t_lo > nh) t_lo = nh;
+  dim3 gw((unsigned)((nh - t_lo) / kHWeightThreads + 1), (unsigned)B->n);  // slots t_lo .. nh
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, false, st);
-  k_h_weights<<<gw, kHWeightThreads, 0, st>>>(B->inst.as<fh_h_dev_inst>(), B->n, tstep, os, B->Wp(par), B->max_weights,
-                                              B->wcp(par), B->Lb.as<double>(), B->ibt.as<double>(),
+  k_h_weights<<<gw, kHWeightThreads, 0, st>>>(B->inst.as<fh_h_dev_inst>(), B->n, tstep, os, t_lo, B->Wp(par),
+                                              B->max_weights, B->wcp(par), B->Lb.as<double>(), B->ibt.as<double>(),
                                               B->lgt.as<double2>(), 1.0 / (double)(tstep + 1));
   fh_prof_mark(ctx, FH_PROF_WEIGHTS, true, st);
   return fh_after_launch(ctx, "k_h_weights");
@@ -643,10 +821,14 @@ static int h_one_step(fh_h_batch *B, bool next) {
   const int os = B->nsaved;
   const int K = os >= 2 ? os - 1 : 0;
   const int par = B->tstep & 1;
+  const bool blk = B->mode == FH_H_BLOCKED;
+  // blocked mode: slots below t_lo (whole 64-slot chunks) are in the far rows
+  auto near_lo = [&](int k) { return blk ? (k / kSlcK) * kSlcK : 0; };
+  const int t_lo = near_lo(K);
   int rc;
   if (B->w_ready == B->tstep) {
     FH_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, B->ev_w, 0));
-  } else if ((rc = h_weights(B, B->tstep, os, par, ctx->stream))) {
+  } else if ((rc = h_weights(B, B->tstep, os, par, ctx->stream, t_lo))) {
     return rc;
   }
   B->w_ready = -1;
@@ -656,12 +838,38 @@ static int h_one_step(fh_h_batch *B, bool next) {
   if (next && B->hs && B->n < kLineCtaMaxInst) {
     FH_CUDA_TRY(ctx, cudaEventRecord(B->ev_main, ctx->stream));
     FH_CUDA_TRY(ctx, cudaStreamWaitEvent(B->hs, B->ev_main, 0));
-    if ((rc = h_weights(B, B->tstep + 1, os + 1, par ^ 1, B->hs))) return rc;
+    if ((rc = h_weights(B, B->tstep + 1, os + 1, par ^ 1, B->hs, near_lo(os + 1 >= 2 ? os : 0)))) return rc;
     FH_CUDA_TRY(ctx, cudaEventRecord(B->ev_w, B->hs));
     B->w_ready = B->tstep + 1;
   }
   int splits = 0, kchunk = 0;
-  if (K > 0) {
+  if (blk) {
+    float2 *ring = B->ring.as<float2>(), *far = B->far.as<float2>();
+    if (K >= kSlcK && K == t_lo) {
+      // first step of a block: the chunk just completed into the planes, the
+      // weight planes of the block's 64 steps, and their far rows
+      fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+      rc = fh_hblk_convert(ctx, *B->hb, ring, B->Ptot, K / kSlcK - 1);
+      fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+      if (rc) return rc;
+      fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
+      const long long R = (long long)B->n * kSlcK;
+      k_hb_weights<<<dim3((unsigned)fh_ngroups(K / kSlcK), (unsigned)fh_ceil_div(R, 8)), 256, 0, ctx->stream>>>(
+          B->inst.as<fh_h_dev_inst>(), K, B->max_steps, B->Lb.as<double>(), B->max_weights, B->ibt.as<double>(),
+          B->lgt.as<double2>(), R, fh_hblk_kcap(*B->hb), fh_hblk_wplanes(*B->hb), fh_hblk_wexp(*B->hb));
+      fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
+      if ((rc = fh_after_launch(ctx, "k_hb_weights"))) return rc;
+      if ((rc = fh_hblk_gemm(ctx, *B->hb, K, far, B->Ptot))) return rc;
+    }
+    const int ti = tile_shape_index(B->tile_threads);
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+    k_h_near_df<<<(unsigned)B->tiles_by[ti].size(), kTileShapes[ti], 0, ctx->stream>>>(
+        B->tl_by[ti].as<fh_h_tile>(), B->inst.as<fh_h_dev_inst>(), ring, B->Ptot, t_lo, K, B->Wp(par),
+        B->max_weights, t_lo >= kSlcK ? far + (long long)(K - t_lo) * B->Ptot : nullptr, B->part.as<double>());
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+    if ((rc = fh_after_launch(ctx, "k_h_near_df"))) return rc;
+    splits = 1;
+  } else if (K > 0) {
     const int ti = tile_shape_index(B->tile_threads);
     h_plan(B->tiles_by[ti].size(), K, B->split_cap, &splits, &kchunk);
     fh_prof_mark(ctx, FH_PROF_HISTORY, false);
@@ -684,9 +892,11 @@ static int h_one_step(fh_h_batch *B, bool next) {
     if ((rc = fh_after_launch(ctx, "k_h_space_v"))) return rc;
   }
   const int append = os >= 1;
-  double *Dnew = append ? B->D.as<double>() + (long long)(os - 1) * B->Ptot : nullptr;
+  double *Dnew = !append ? nullptr
+                 : blk   ? reinterpret_cast<double *>(B->ring.as<float2>() + (long long)((os - 1) & 127) * B->Ptot)
+                         : B->D.as<double>() + (long long)(os - 1) * B->Ptot;
   {
-    const int fst = os == 0 ? 1 : 0, dfs = B->mode == FH_H_DF64 ? 1 : 0;
+    const int fst = os == 0 ? 1 : 0, dfs = (B->mode == FH_H_DF64 || blk) ? 1 : 0;
     const dim3 gc((unsigned)B->n), gw((unsigned)fh_ceil_div(B->n, 4));
     const fh_h_dev_inst *in = B->inst.as<fh_h_dev_inst>();
     double *Al = B->Al.as<double>(), *Bt = B->Bt.as<double>(), *sA = B->sA.as<double>(), *sB = B->sB.as<double>();
@@ -1028,6 +1238,7 @@ int fh_h_batch_autotune(fh_h_batch *b, float *best_ms) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
   fh_ctx *ctx = b->ctx;
   FH_REQUIRE(ctx, !ctx->capturing, FH_EINVAL, "fh_h_batch_autotune: not during a capture");
+  FH_REQUIRE(ctx, b->mode != FH_H_BLOCKED, FH_EINVAL, "fh_h_batch_autotune: the blocked mode has no split history sum");
   const int K = b->max_steps - 1 < 512 ? b->max_steps - 1 : 512;
   if (K < 32) return FH_OK;
   static const int caps[3] = {1, 8, 64};
@@ -1088,8 +1299,42 @@ int fh_h_batch_launch_shape(const fh_h_batch *b, int *tile_threads, int *split_c
 int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
   fh_ctx *ctx = b->ctx;
-  FH_REQUIRE(ctx, mode == FH_H_FP64 || mode == FH_H_DF64, FH_EINVAL, "fh_h_batch_set_mode: unknown mode %d", mode);
+  FH_REQUIRE(ctx, mode == FH_H_FP64 || mode == FH_H_DF64 || mode == FH_H_BLOCKED, FH_EINVAL,
+             "fh_h_batch_set_mode: unknown mode %d", mode);
   FH_REQUIRE(ctx, b->nsaved == 0, FH_EINVAL, "fh_h_batch_set_mode: only before the first step");
+  int rc;
+  if (mode == FH_H_BLOCKED && !b->hb) {
+    // 128-point tiles of every instance's segment
+    std::vector<long long> tp0;
+    std::vector<int> tin, tnp;
+    for (int i = 0; i < b->n; ++i) {
+      const int seg = b->hp[i].N + 2;
+      for (int k = 0; k < seg; k += 128) {
+        tp0.push_back(b->off[i] + k);
+        tin.push_back(i);
+        tnp.push_back(seg - k < 128 ? seg - k : 128);
+      }
+    }
+    const int kcap = (int)fh_ceil_div(b->max_steps, kSlcK) * kSlcK;
+    b->hb = fh_hblk_new();
+    if ((rc = fh_hblk_init(ctx, *b->hb, b->Ptot, kcap, b->n, tp0.data(), tin.data(), tnp.data(), (int)tp0.size())) ||
+        (rc = fh_alloc(ctx, b->ring, sizeof(float2) * 128 * (size_t)b->Ptot)) ||
+        (rc = fh_alloc(ctx, b->far, sizeof(float2) * kSlcK * (size_t)b->Ptot, false))) {
+      fh_hblk_delete(b->hb);
+      b->hb = nullptr;
+      b->ring.release();
+      b->far.release();
+      return rc;
+    }
+    b->D.release();  // the full-precision history is not kept in this mode
+  }
+  if (mode != FH_H_BLOCKED && b->hb) {
+    fh_hblk_delete(b->hb);
+    b->hb = nullptr;
+    b->ring.release();
+    b->far.release();
+    if ((rc = fh_alloc(ctx, b->D, sizeof(double) * (size_t)b->Ptot * (size_t)b->max_steps))) return rc;
+  }
   b->mode = mode;
   b->graph.reset();
   return FH_OK;
