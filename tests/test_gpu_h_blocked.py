@@ -52,7 +52,9 @@ def test_blocked_psi_batch_vs_oracle(ctx):
 
 def test_blocked_mixed_weight_kinds(ctx):
     """L1, psi = t and psi = t^beta instances (constant and variable
-    coefficients) in one blocked batch."""
+    coefficients) in one blocked batch, long enough (300 steps) that the
+    oldest chunk group of the psi instances is interpolated across the block
+    at 256 slots while the L1 instance's is evaluated per step."""
     from theses_code_gb300 import workloads
     from theses_code_gb300._lib import FH_H_BLOCKED
     from theses_code_gb300.solvers import HSolverBatch
@@ -61,7 +63,7 @@ def test_blocked_mixed_weight_kinds(ctx):
     pt = dict(params[0], beta=1.0)
     allp = [p1, pt] + params
     allu = [u1, U0s[0]] + U0s
-    steps = 200
+    steps = 300
     s = HSolverBatch(ctx, allp, steps + 1, FH_H_BLOCKED)
     s.set_u(allu)
     s.calc_step(steps)

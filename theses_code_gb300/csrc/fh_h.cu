@@ -86,7 +86,8 @@ struct fh_h_batch {
   // rows; the slots of the last two chunks as (hi, lo) pairs in a 128-layer
   // ring (slot t in row t mod 128)
   fh_hblk *hb = nullptr;
-  fh_dbuf ring, far;
+  fh_dbuf ring, far, cheb;  // cheb: interpolation tables of k_hb_wcheb
+  bool has_l1 = false;      // some instance has L1 weights (k_hb_weights covers every group)
   double *Wp(int par) const { return W.as<double>() + (long long)par * n * max_weights; }
   double *wcp(int par) const { return wc.as<double>() + (long long)par * n; }
   ~fh_h_batch() {
@@ -609,26 +610,15 @@ __global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
 // Horner polynomial per node.  A slot weight is the difference of its two
 // nodes; the difference loses ~log10(X) digits, which is far below the 2^-32
 // of the bf16 slices the blocked contraction uses these weights at.
-__device__ __forceinline__ void h_psi_node(const fh_h_dev_inst &I, const double *__restrict__ Lc,
-                                           const double2 *__restrict__ lgt, int x, int X, double invX, double &v,
-                                           int &low) {
-  if (x <= 0) {
-    v = 0.0;
-    low = 1;
-    return;
-  }
-  if (x >= X) {  // c = 0
-    v = 0.0;
-    low = 0;
-    return;
-  }
+// h_psi_node_at: the same at a real X (0 < x < X) given log x and log X as
+// double-doubles and r = x/X.
+__device__ __forceinline__ void h_psi_node_at(const fh_h_dev_inst &I, const double *__restrict__ Lc, double2 lx,
+                                              double2 lX, double r, double &v, int &low) {
   const double *Uc = Lc + kIbTerms;
-  const double2 lx = lgt[x], lX = lgt[X];
   const double sh = lx.x - lX.x;
   const double sl = (lx.x - (sh + lX.x)) + (lx.y - lX.y);
   const double th = I.beta * sh;
   const double tl = fma(I.beta, sh, -th) + I.beta * sl;
-  const double r = (double)x * invX;
   if (r <= Lc[2 * kIbTerms + 1]) {  // y <= kIbLowMax: lower series in y
     const double ey = exp(th);
     const double y = fma(ey, tl, ey);
@@ -642,12 +632,165 @@ __device__ __forceinline__ void h_psi_node(const fh_h_dev_inst &I, const double 
   }
 }
 
+__device__ __forceinline__ void h_psi_node(const fh_h_dev_inst &I, const double *__restrict__ Lc,
+                                           const double2 *__restrict__ lgt, int x, int X, double invX, double &v,
+                                           int &low) {
+  if (x <= 0) {
+    v = 0.0;
+    low = 1;
+    return;
+  }
+  if (x >= X) {  // c = 0
+    v = 0.0;
+    low = 0;
+    return;
+  }
+  h_psi_node_at(I, Lc, lgt[x], lgt[X], (double)x * invX, v, low);
+}
+
+// Far slots by interpolation across the block's steps.  For a fixed slot
+// [t, t + 1] the weight w(X) over the block's X in [K + 3, K + 66] is
+// analytic off the branch points X = t, t + 1, so within the Bernstein
+// ellipse of the interval with parameter rho = D + sqrt(D^2 - 1),
+// D = 1 + 2 d / 63, d = K + 2 - t the distance of the nearer branch point:
+// the interpolant at m first-kind Chebyshev points is within ~rho^-m of w
+// (Trefethen, Approximation Theory and Approximation Practice, ch. 8).  A
+// chunk group takes the order of its last slot for kHbChebBits bits (2^-38,
+// far below the 2^-31 of the group's bf16 slices); groups that would need
+// more than kHbChebMax points are evaluated exactly per step.
+constexpr int kHbChebMax = 16;
+constexpr double kHbChebBits = 38.0;
+constexpr int kHbGroupSlots = 2 * kSlcK;  // slots of a chunk group
+__host__ __device__ inline int hb_cheb_order(int d) {
+  const double D = 1.0 + 2.0 * (double)d / 63.0;
+  const double rho = D + sqrt(D * D - 1.0);
+  return (int)ceil(kHbChebBits * 0.6931471805599453 / log(rho)) + 1;
+}
+// Leading chunk groups of the block at K that are interpolated.
+static int hb_cheb_groups(int K) {
+  const int ng = fh_ngroups(K / kSlcK);
+  int g = 0;
+  while (g < ng - 1 && hb_cheb_order(K + 2 - (g * kHbGroupSlots + kHbGroupSlots - 1)) <= kHbChebMax) ++g;
+  return g;
+}
+// Interpolation tables for m = 1..kHbChebMax points: block m holds the
+// Lagrange basis L[r][j] at the block's steps r < 64 (x_r = -1 + 2 r / 63;
+// row stride kHbChebMax) and, in row 64, the X offsets 31.5 (1 + x_j) of the
+// points x_j = cos((2 j + 1) pi / (2 m)) from K + 3.
+static constexpr size_t kHbChebBlock = (size_t)(kSlcK + 1) * kHbChebMax;
+static void hb_cheb_table(std::vector<double> &t) {
+  t.assign((kHbChebMax + 1) * kHbChebBlock, 0.0);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int m = 1; m <= kHbChebMax; ++m) {
+    double *T = t.data() + (size_t)m * kHbChebBlock;
+    long double xj[kHbChebMax];
+    for (int j = 0; j < m; ++j) {
+      xj[j] = cosl((long double)(2 * j + 1) * pi / (long double)(2 * m));
+      T[kSlcK * kHbChebMax + j] = (double)(31.5L * (1.0L + xj[j]));
+    }
+    for (int r = 0; r < kSlcK; ++r) {
+      const long double x = -1.0L + 2.0L * (long double)r / 63.0L;
+      for (int j = 0; j < m; ++j) {
+        long double l = 1.0L;
+        for (int i = 0; i < m; ++i)
+          if (i != j) l *= (x - xj[i]) / (xj[j] - xj[i]);
+        T[r * kHbChebMax + j] = (double)l;
+      }
+    }
+  }
+}
+
+// Weight planes of the interpolated chunk groups G < gridDim.x of the psi
+// instances (one CTA per (group, instance)): the group's 129 node values at
+// each of the m points X_j (h_psi_node_at; psi = t: (1 - x/X)^(1 - alpha)),
+// the 128 slot weights at each X_j, then per step r of the block the
+// interpolated weights sum_j L[r][j] w_j, sliced into W3/Ew as k_hb_weights
+// does.  Rows past the last step are zero.
+__global__ void __launch_bounds__(256) k_hb_wcheb(const fh_h_dev_inst *__restrict__ inst, int K, int max_steps,
+                                                  const double *__restrict__ ibt, const double2 *__restrict__ lgt,
+                                                  const double *__restrict__ cheb, long long R, int Kcap,
+                                                  __nv_bfloat16 *__restrict__ W3, int8_t *__restrict__ Ew) {
+  __shared__ double sv[kHbChebMax][kHbGroupSlots + 1];
+  __shared__ double sw[kHbChebMax][kHbGroupSlots];
+  __shared__ double sL[kSlcK * kHbChebMax];
+  __shared__ double sX[kHbChebMax][3];  // log X_j, 1/X_j, scale of X_j
+  __shared__ unsigned char slo[kHbChebMax][kHbGroupSlots + 1];
+  const int b = blockIdx.y, G = blockIdx.x;
+  const fh_h_dev_inst I = inst[b];
+  if (I.weights != FH_W_PSI) return;  // whole CTA
+  const int x0 = G * kHbGroupSlots;
+  const int m = min(hb_cheb_order(K + 2 - (x0 + kHbGroupSlots - 1)), kHbChebMax);
+  const double *tab = cheb + (size_t)m * kHbChebBlock;
+  for (int i = threadIdx.x; i < kSlcK * kHbChebMax; i += blockDim.x) sL[i] = tab[i];
+  const double *Lc = ibt + (long long)b * kIbStride;
+  const bool psi_t = I.beta == 1.0;
+  if (threadIdx.x < m) {
+    const int j = threadIdx.x;
+    const double X = (double)(K + 3) + tab[kSlcK * kHbChebMax + j];
+    const double lX = log(X);
+    sX[j][0] = lX;
+    sX[j][1] = 1.0 / X;
+    // (X tau)^(1 - alpha beta) (1 - alpha) / beta; psi = t: (X tau)^(1 - alpha)
+    sX[j][2] = psi_t ? exp((1.0 - I.alpha) * (lX + Lc[2 * kIbTerms + 2]))
+                     : exp((1.0 - I.alpha * I.beta) * (lX + Lc[2 * kIbTerms + 2])) * Lc[2 * kIbTerms + 3] *
+                           (1.0 - I.alpha);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m * (kHbGroupSlots + 1); i += blockDim.x) {
+    const int j = i / (kHbGroupSlots + 1), k = i - j * (kHbGroupSlots + 1);
+    const int x = x0 + k;  // x < K + 3 <= X_j
+    double v;
+    int lo;
+    if (psi_t) {
+      v = exp((1.0 - I.alpha) * log1p(-(double)x * sX[j][1]));
+      lo = 0;
+    } else if (x == 0) {
+      v = 0.0;
+      lo = 1;
+    } else {
+      h_psi_node_at(I, Lc, lgt[x], make_double2(sX[j][0], 0.0), (double)x * sX[j][1], v, lo);
+    }
+    sv[j][k] = v;
+    slo[j][k] = (unsigned char)lo;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m * kHbGroupSlots; i += blockDim.x) {
+    const int j = i / kHbGroupSlots, k = i - j * kHbGroupSlots;
+    const double v0 = sv[j][k], v1 = sv[j][k + 1];
+    const int l0 = slo[j][k], l1 = slo[j][k + 1];
+    double diff;
+    if (l0 && l1)
+      diff = v1 - v0;
+    else if (!l0)
+      diff = v0 - v1;
+    else
+      diff = (Lc[2 * kIbTerms] - v1) - v0;
+    sw[j][k] = x0 + k >= 1 ? sX[j][2] * diff : 0.0;  // slot 0 weighs nothing
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunks = K / kSlcK;
+  for (int r = warp; r < kSlcK; r += blockDim.x >> 5) {
+    double w[4] = {0.0, 0.0, 0.0, 0.0};
+    if (K + r + 2 <= max_steps) {
+      const double *Lr = sL + r * kHbChebMax;
+      for (int j = 0; j < m; ++j) {
+        const double l = Lr[j];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) w[h] = fma(l, sw[j][lane + 32 * h], w[h]);
+      }
+    }
+    fh_slice_group_values(w, G, nchunks, (long long)b * kSlcK + r, R, Kcap, W3, Ew);
+  }
+}
+
 // Weight planes of the block whose first step has K = 64 blk history slots:
 // row m = 64 inst + r is step tstep = K + r + 2 (X = K + r + 3) of instance
 // inst, weighing the slots t < K (slot 0: weight 0, as in k_h_weights); rows
-// past the last step are zero.  One warp per (row, chunk group), sliced into
-// W3/Ew (fh_slices.cuh).
-__global__ void k_hb_weights(const fh_h_dev_inst *__restrict__ inst, int K, int max_steps,
+// past the last step are zero.  One warp per (row, chunk group G >= G0), sliced
+// into W3/Ew (fh_slices.cuh); the groups below gcheb of the psi instances are
+// k_hb_wcheb's.
+__global__ void k_hb_weights(const fh_h_dev_inst *__restrict__ inst, int K, int max_steps, int G0, int gcheb,
                              const double *__restrict__ Lb, int ldw, const double *__restrict__ ibt,
                              const double2 *__restrict__ lgt, long long R, int Kcap, __nv_bfloat16 *__restrict__ W3,
                              int8_t *__restrict__ Ew) {
@@ -656,7 +799,8 @@ __global__ void k_hb_weights(const fh_h_dev_inst *__restrict__ inst, int K, int 
   const int lane = threadIdx.x & 31;
   const int b = (int)(m / kSlcK), r = (int)(m % kSlcK);
   const fh_h_dev_inst I = inst[b];
-  const int G = blockIdx.x, nchunks = K / kSlcK;
+  const int G = G0 + blockIdx.x, nchunks = K / kSlcK;
+  if (I.weights == FH_W_PSI && G < gcheb) return;  // interpolated (k_hb_wcheb); whole warp
   const int tstep = K + r + 2, X = tstep + 1, os = K + r + 1;
   const bool live = tstep <= max_steps;
   double w[4];
@@ -854,9 +998,17 @@ static int h_one_step(fh_h_batch *B, bool next) {
       if (rc) return rc;
       fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
       const long long R = (long long)B->n * kSlcK;
-      k_hb_weights<<<dim3((unsigned)fh_ngroups(K / kSlcK), (unsigned)fh_ceil_div(R, 8)), 256, 0, ctx->stream>>>(
-          B->inst.as<fh_h_dev_inst>(), K, B->max_steps, B->Lb.as<double>(), B->max_weights, B->ibt.as<double>(),
-          B->lgt.as<double2>(), R, fh_hblk_kcap(*B->hb), fh_hblk_wplanes(*B->hb), fh_hblk_wexp(*B->hb));
+      const int ng = fh_ngroups(K / kSlcK), gcheb = hb_cheb_groups(K), G0 = B->has_l1 ? 0 : gcheb;
+      if (gcheb > 0) {
+        k_hb_wcheb<<<dim3((unsigned)gcheb, (unsigned)B->n), 256, 0, ctx->stream>>>(
+            B->inst.as<fh_h_dev_inst>(), K, B->max_steps, B->ibt.as<double>(), B->lgt.as<double2>(),
+            B->cheb.as<double>(), R, fh_hblk_kcap(*B->hb), fh_hblk_wplanes(*B->hb), fh_hblk_wexp(*B->hb));
+        if ((rc = fh_after_launch(ctx, "k_hb_wcheb"))) return rc;
+      }
+      k_hb_weights<<<dim3((unsigned)(ng - G0), (unsigned)fh_ceil_div(R, 8)), 256, 0, ctx->stream>>>(
+          B->inst.as<fh_h_dev_inst>(), K, B->max_steps, G0, gcheb, B->Lb.as<double>(), B->max_weights,
+          B->ibt.as<double>(), B->lgt.as<double2>(), R, fh_hblk_kcap(*B->hb), fh_hblk_wplanes(*B->hb),
+          fh_hblk_wexp(*B->hb));
       fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
       if ((rc = fh_after_launch(ctx, "k_hb_weights"))) return rc;
       if ((rc = fh_hblk_gemm(ctx, *B->hb, K, far, B->Ptot))) return rc;
@@ -972,6 +1124,7 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
     I.gravity = p.gravity;
     I.fixed = (p.kmodel == FH_K_CONST) && (p.weights == FH_W_L1 || p.beta == 1.0);
     if (!I.fixed) B->varcoef = true;
+    if (I.weights == FH_W_L1) B->has_l1 = true;
     I.off = off;
     I.dL = p.L / p.N;
     I.Dg = pow(I.dL, -2.0);
@@ -1304,6 +1457,9 @@ int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
   FH_REQUIRE(ctx, b->nsaved == 0, FH_EINVAL, "fh_h_batch_set_mode: only before the first step");
   int rc;
   if (mode == FH_H_BLOCKED && !b->hb) {
+    // the weight-plane grids have n (interpolated groups) and 8 n rows
+    FH_REQUIRE(ctx, (long long)b->n * 8 <= 65535, FH_EINVAL,
+               "fh_h_batch_set_mode: the blocked mode takes at most 8191 instances (%d)", b->n);
     // 128-point tiles of every instance's segment
     std::vector<long long> tp0;
     std::vector<int> tin, tnp;
@@ -1316,14 +1472,21 @@ int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
       }
     }
     const int kcap = (int)fh_ceil_div(b->max_steps, kSlcK) * kSlcK;
+    std::vector<double> ct;
+    hb_cheb_table(ct);
     b->hb = fh_hblk_new();
     if ((rc = fh_hblk_init(ctx, *b->hb, b->Ptot, kcap, b->n, tp0.data(), tin.data(), tnp.data(), (int)tp0.size())) ||
         (rc = fh_alloc(ctx, b->ring, sizeof(float2) * 128 * (size_t)b->Ptot)) ||
-        (rc = fh_alloc(ctx, b->far, sizeof(float2) * kSlcK * (size_t)b->Ptot, false))) {
+        (rc = fh_alloc(ctx, b->far, sizeof(float2) * kSlcK * (size_t)b->Ptot, false)) ||
+        (rc = fh_alloc(ctx, b->cheb, sizeof(double) * ct.size(), false)) ||
+        (rc = cudaMemcpy(b->cheb.p, ct.data(), sizeof(double) * ct.size(), cudaMemcpyHostToDevice) != cudaSuccess
+                  ? fh_set_error(ctx, FH_ECUDA, "fh_h_batch_set_mode: upload of the interpolation tables failed")
+                  : FH_OK)) {
       fh_hblk_delete(b->hb);
       b->hb = nullptr;
       b->ring.release();
       b->far.release();
+      b->cheb.release();
       return rc;
     }
     b->D.release();  // the full-precision history is not kept in this mode
@@ -1333,6 +1496,7 @@ int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
     b->hb = nullptr;
     b->ring.release();
     b->far.release();
+    b->cheb.release();
     if ((rc = fh_alloc(ctx, b->D, sizeof(double) * (size_t)b->Ptot * (size_t)b->max_steps))) return rc;
   }
   b->mode = mode;
