@@ -147,17 +147,21 @@ def test_history_sum_rejects_odd_and_misaligned(ctx, torch_mod):
         ctx.call("fh_history_sum", 3, 2, 4, W.data_ptr(), 2, D.data_ptr(), 4, S.data_ptr(), 4)
 
 
-def test_history_sum_layers(ctx, torch_mod):
+@pytest.mark.parametrize("K,P,ldh", [(41, 333, 333), (0, 17, 17), (5000, 700, 704), (129, 100000, 100000)])
+def test_history_sum_layers(ctx, torch_mod, K, P, ldh):
+    """One split (few layers or many points) and K splits added in split
+    order (few points, long history), strided layers."""
     torch = torch_mod
     rng = np.random.default_rng(3)
-    K, P = 41, 333
-    H = rng.normal(size=(K + 1, P))
-    w = rng.uniform(size=K)
-    S = torch.zeros(P, dtype=torch.float64, device="cuda")
+    H = rng.normal(size=(K + 1, ldh))
+    w = rng.uniform(size=max(K, 1))
+    S = torch.full((P,), 7.0, dtype=torch.float64, device="cuda")
     wd, Hd = dev(torch, w), dev(torch, H)  # keep the device buffers alive until the kernel ran
-    ctx.call("fh_history_sum_layers", K, P, wd.data_ptr(), Hd.data_ptr(), P, S.data_ptr())
+    ctx.call("fh_history_sum_layers", K, P, wd.data_ptr(), Hd.data_ptr(), ldh, S.data_ptr())
     ctx.sync()
-    assert relmax(S.cpu().numpy(), O.history_sum_layers(H, w)) < 1e-13
+    ref = O.history_sum_layers(H[:, :P], w[:K]) if K > 0 else np.zeros(P)
+    got = S.cpu().numpy()
+    assert (np.max(np.abs(got)) == 0.0) if K == 0 else relmax(got, ref) < 1e-13
 
 
 # ------------------------------------------------------------- tridiagonal

@@ -220,18 +220,21 @@ __global__ void k_hist_reduce(int M, int splits, long long P, const double *__re
 }
 
 // Layer form: S[p] = sum_t w[t] * (H[(t+1) ldh + p] - H[t ldh + p]) (reference Sum kernel semantics).
+// Split y sums the layers [y kchunk, (y + 1) kchunk) into part[y][p]
+// (coalesced over p; the split's first difference reads its lower layer).
 __global__ void k_hist_sum_layers(int K, long long P, const double *__restrict__ w, const double *__restrict__ H,
-                                  long long ldh, double *__restrict__ S) {
+                                  long long ldh, int kchunk, double *__restrict__ part, long long ldpart) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
+  const int t0 = blockIdx.y * kchunk, t1 = min(K, t0 + kchunk);
   double acc = 0.0;
-  double prev = H[p];
-  for (int t = 0; t < K; ++t) {
+  double prev = t0 < t1 ? H[(long long)t0 * ldh + p] : 0.0;
+  for (int t = t0; t < t1; ++t) {
     const double cur = __ldcs(H + (long long)(t + 1) * ldh + p);
     acc = fma(__ldg(w + t), cur - prev, acc);
     prev = cur;
   }
-  S[p] = acc;
+  part[(long long)blockIdx.y * ldpart + p] = acc;
 }
 
 // S[p] = sum_s part[s][p] in split order: 8 warps take every 8th split for 32
@@ -333,8 +336,27 @@ int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, cons
   FH_REQUIRE(ctx, K >= 0 && P >= 0 && ldh >= P, FH_EINVAL, "fh_history_sum_layers: bad sizes");
   if (P == 0) return FH_OK;
   FH_REQUIRE(ctx, S && H && (K == 0 || w), FH_EINVAL, "fh_history_sum_layers: null pointer");
-  k_hist_sum_layers<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(K, P, w, H, ldh, S);
-  return fh_after_launch(ctx, "k_hist_sum_layers");
+  // K splits when the points alone give too few CTAs: ~3 waves of 8 resident
+  // CTAs on 152 SMs, at least 64 layers per split, at most 64 splits; the
+  // splits' partial sums are added in split order
+  const long long nb = fh_ceil_div(P, 256);
+  long long s = fh_ceil_div(3LL * 152 * 8, nb);
+  if (s > K / 64) s = K / 64;
+  if (s > 64) s = 64;
+  if (s < 1) s = 1;
+  const int kchunk = (int)fh_ceil_div((long long)(K > 0 ? K : 1), s);
+  const int splits = (int)fh_ceil_div((long long)(K > 0 ? K : 1), (long long)kchunk);
+  double *part = S;
+  if (splits > 1) {
+    void *work = nullptr;
+    int rc = fh_ctx_work(ctx, sizeof(double) * (size_t)splits * (size_t)P, &work);
+    if (rc) return rc;
+    part = static_cast<double *>(work);
+  }
+  k_hist_sum_layers<<<dim3((unsigned)nb, (unsigned)splits), 256, 0, ctx->stream>>>(K, P, w, H, ldh, kchunk, part, P);
+  int rc = fh_after_launch(ctx, "k_hist_sum_layers");
+  if (rc || splits == 1) return rc;
+  return fh_launch_reduce_splits(ctx, splits, P, part, P, S);
 }
 
 }  // extern "C"
