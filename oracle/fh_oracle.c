@@ -385,6 +385,272 @@ static void tg_series_eval(const fho_tg_params *p, int J, double gtj, size_t P, 
   for (size_t id = 0; id < P; ++id) out[id] = Da * out[id];
 }
 
+/* dt_alg 4, psi = t: two-series approximation of the history sums
+ * (fr_d_t_g_2d.cpp:246-745, used by TG_solver_::Om1 3438-3469).  Per point
+ * the sum S(x) = sum_r g(x, r) F[r], g(x, r) = (x - r + a)^A - (x - r + b)^A,
+ * A = 1 - alpha, F[r] = C^r - C^(r-1) (the full-step differences H42), is
+ * carried by
+ *   "ia" approximations   sum_k c_k x^(A-k)       valid for x >= min
+ *     (binomial series of g in 1/x; fr_d_t_g_2d.cpp:265-333), and
+ *   "ibk" approximations  sum_k c_k (x - b)^k     valid for min <= x <= max
+ *     (Taylor series of g around b; 351-471),
+ * whose coefficients are linear in F.  calc_va (477-745) evaluates the sum at
+ * x = block + 1 from the approximations plus the newest term directly, then
+ * folds F[block + 1] into them, creating, splitting and retiring
+ * approximations so that each stays within approx_eps = 1e-7 of its share.
+ * The ranges depend on A, a, b and the block only, not on F.  Integer time
+ * grid (Ts = NULL), one layer per block (bs = 1), as the solver calls it. */
+#define TA_AK 10
+#define TA_MAXAK 20
+static const double ta_approx_eps = 1e-7, ta_eps = 1e-9;
+
+typedef struct {
+  double min;
+  int nterms;
+  double c[TA_MAXAK];
+} ta_ia;
+typedef struct {
+  double min, max, b;
+  int nterms, old;
+  double c[TA_MAXAK];
+} ta_ibk;
+typedef struct {
+  ta_ia *ia;
+  ta_ibk *ibk;
+  int nia, cia, nibk, cibk;
+} ta_set;
+
+/* prod_{i=1}^{n-1} (A - i + 1) / i in the reference's order */
+static double ta_ak(double A, int n) {
+  double ak = 1;
+  for (int i = 1; i < n; i++) ak *= (A - i + 1) / i;
+  return ak;
+}
+
+/* ia_mini (fr_d_t_g_2d.cpp:255-266) */
+static double ta_ia_mini(double A, double r, int nterms, double a, double b) {
+  const double ak = ta_ak(A, nterms);
+  return pow(fabs(ak * (pow(a - r, (double)nterms) - pow(b - r, (double)nterms)) / ta_approx_eps),
+             1.0 / (nterms - A));
+}
+
+/* ibk_i2 (fr_d_t_g_2d.cpp:337-371), Ts = NULL, step = -1 */
+static double ta_ibk_i2(double A, double r, double b, int nterms, double a, double c) {
+  const double ak = ta_ak(A, nterms);
+  if (fabs(b - r) < 1e-10) return pow(fabs(ta_approx_eps / ak), 1.0 / nterms);
+  const double p1 = pow((a + b - r), A) / pow((a + b - r), nterms);
+  const double p2 = pow((c + b - r), A) / pow((c + b - r), nterms);
+  return pow(fabs(ta_approx_eps / (ak * (p1 - p2))), 1.0 / nterms);
+}
+
+/* ia_approximation(A, rmin, rmax, F, NULL, cmin, nt, a, b) (285-314) */
+static ta_ia ta_ia_make(double A, double rmin, double rmax, const double *F, double cmin, int nt, double a,
+                        double b) {
+  ta_ia q;
+  double ak = 1;
+  q.c[0] = 0;
+  for (int i = 1; i < nt; i++) {
+    ak *= (A - i + 1) / i;
+    double krk = 0.0;
+    for (int j = (int)rmin; j < rmax; j++) krk += F[j] * (pow(a - (double)j, (double)i) - pow(b - (double)j, (double)i));
+    q.c[i] = ak * krk;
+  }
+  for (int i = nt; i < TA_MAXAK; i++) q.c[i] = 0.0;
+  q.min = cmin != -1 ? cmin : ceil(ta_ia_mini(A, rmax, nt, a, b));
+  if (!isfinite(q.min)) q.min = rmax;
+  q.nterms = nt;
+  return q;
+}
+
+static double ta_ia_calc(const ta_ia *q, double A, double x) {
+  double ret = 0.0;
+  for (int i = 0; i < q->nterms; i++) ret += q->c[i] * pow(x, A - (double)i);
+  return ret;
+}
+
+/* ibk_approximation(A, rmin, rmax, F, NULL, b, i2, nt, a, _b) (401-436) */
+static ta_ibk ta_ibk_make(double A, double rmin, double rmax, const double *F, double b, double i2, int nt,
+                          double a, double _b) {
+  ta_ibk q;
+  double ak = 1;
+  q.b = b;
+  for (int i = 0; i < nt; i++) {
+    if (i != 0) ak *= (A - i + 1) / i;
+    double krk = 0.0;
+    for (int j = (int)rmin; j < rmax; j++)
+      krk += F[j] * (pow(a + b - (double)j, A - (double)i) - pow(_b + b - (double)j, A - (double)i));
+    q.c[i] = ak * krk;
+  }
+  for (int i = nt; i < TA_MAXAK; i++) q.c[i] = 0.0;
+  q.min = i2 != -1 ? i2 : b - floor(ta_ibk_i2(A, rmax, b, nt, a, _b));
+  q.max = b;
+  q.nterms = nt;
+  q.old = 0;
+  return q;
+}
+
+static double ta_ibk_calc(const ta_ibk *q, double x) {
+  double ret = 0.0, xbk = 1;
+  for (int i = 0; i < q->nterms; i++) {
+    ret += q->c[i] * xbk;
+    xbk *= (x - q->b);
+  }
+  return ret;
+}
+
+static void ta_push_ibk(ta_set *S, ta_ibk q) {
+  if (S->nibk == S->cibk) {
+    S->cibk = S->cibk ? 2 * S->cibk : 16;
+    S->ibk = (ta_ibk *)realloc(S->ibk, sizeof(ta_ibk) * (size_t)S->cibk);
+  }
+  S->ibk[S->nibk++] = q;
+}
+static void ta_push_ia(ta_set *S, ta_ia q) {
+  if (S->nia == S->cia) {
+    S->cia = S->cia ? 2 * S->cia : 4;
+    S->ia = (ta_ia *)realloc(S->ia, sizeof(ta_ia) * (size_t)S->cia);
+  }
+  S->ia[S->nia++] = q;
+}
+static void ta_erase_ibk(ta_set *S, int j) {
+  memmove(S->ibk + j, S->ibk + j + 1, sizeof(ta_ibk) * (size_t)(S->nibk - j - 1));
+  S->nibk--;
+}
+
+/* A series of short approximations of the current layer covering [rr, upto]:
+ * centres b found by the fixed point b = rr + i2(r, b) + 1 (the loops of
+ * steps 2, 3 and 5 of calc_va); r2 is the r argument of ibk_i2. */
+static double ta_series(ta_set *S, double A, int block, const double *F, double rr, double r2, double upto,
+                        int cap, double a, double _b, int cmp_ceil) {
+  double bb0 = rr, bb = rr;
+  do {
+    bb = rr + 1;
+    do {
+      bb0 = bb;
+      bb = rr + ta_ibk_i2(A, r2, bb, TA_AK, a, _b) + 1;
+    } while ((bb - bb0) > ta_eps);
+    if (!isfinite(bb)) {
+      bb = bb0;
+      if (!isfinite(bb)) bb = rr;
+    }
+    ta_ibk q = ta_ibk_make(A, block + 1, block + 2, F, floor(bb), rr, TA_AK, a, _b);
+    rr = floor(bb) + 1;
+    if (cap && floor(bb) > upto) q.max = upto;
+    ta_push_ibk(S, q);
+  } while (floor(bb) < (cmp_ceil ? ceil(upto) : upto));
+  return rr;
+}
+
+/* calc_va(A, 1, block, F, &V, NULL, ias, ibks, a, _b) (fr_d_t_g_2d.cpp:477-745) */
+static double ta_calc_va(ta_set *S, double A, int block, const double *F, double a, double _b) {
+  const double rmax = (double)(block + 2);
+  const int rmaxidx = block + 2;
+  double V = 0.0;
+  if (A == 0.0) return V;
+  {
+    const int i = block + 1;
+    const double ii = i;
+    for (int j = 0; j < S->nia; j++)
+      if (ii >= S->ia[j].min) V += ta_ia_calc(&S->ia[j], A, ii);
+    for (int j = 0; j < S->nibk; j++)
+      if ((ii >= S->ibk[j].min) && (ii <= S->ibk[j].max)) V += ta_ibk_calc(&S->ibk[j], ii);
+    double v = 0.0;
+    for (int j = block + 1; j <= i; j++) v += (pow((double)i - (double)j + a, A) - pow((double)i - (double)j + _b, A)) * F[j];
+    V += v;
+  }
+  /* 1) retire short approximations that end before rmax */
+  for (int j = 0; j < S->nibk; j++)
+    if (S->ibk[j].max < rmax) {
+      ta_erase_ibk(S, j);
+      j--;
+    }
+  /* 2) fold the layer into the short approximations ahead of it; split those
+   * the new layer's series cannot cover with MAXAK terms */
+  int ss = S->nibk;
+  for (int j = 0; j < ss; j++)
+    if (S->ibk[j].min >= rmax && S->ibk[j].old == 0) {
+      int spl = 0;
+      ta_ibk i2;
+      ta_ibk bibk = ta_ibk_make(A, block + 1, block + 2, F, S->ibk[j].b, -1.0, TA_AK, a, _b);
+      if (bibk.min > S->ibk[j].min) {
+        int t;
+        for (t = TA_AK; t < TA_MAXAK; t++)
+          if ((S->ibk[j].b - ta_ibk_i2(A, rmaxidx, S->ibk[j].b, t, a, _b)) < S->ibk[j].min) break;
+        if (t == TA_MAXAK)
+          spl = 1;
+        else
+          bibk = ta_ibk_make(A, block + 1, block + 2, F, S->ibk[j].b, -1.0, t, a, _b);
+        if (spl) i2 = S->ibk[j];
+      }
+      for (int i = 0; i < bibk.nterms; i++) S->ibk[j].c[i] += bibk.c[i];
+      if (S->ibk[j].nterms < bibk.nterms) S->ibk[j].nterms = bibk.nterms;
+      if (spl && bibk.min > S->ibk[j].min) {
+        i2.max = ceil(bibk.min);
+        S->ibk[j].min = i2.max + 1;
+        i2.old = 1;
+        if (S->ibk[j].min > S->ibk[j].max) {
+          i2.max = S->ibk[j].max;
+          ta_erase_ibk(S, j);
+          j--;
+          ss--;
+        }
+        ta_push_ibk(S, i2);
+        ta_series(S, A, block, F, i2.min, i2.min, i2.max, 1, a, _b, 0);
+      }
+    }
+  /* 3) new short approximations of this layer for the range of the newest
+   * approximation that straddles rmax */
+  double bm1 = -1;
+  for (int j = 0; j < S->nibk; j++)
+    if (S->ibk[j].max >= rmax && S->ibk[j].min < rmax && S->ibk[j].max > bm1 && S->ibk[j].old == 0) {
+      bm1 = S->ibk[j].max;
+      S->ibk[j].old = 1;
+    }
+  if (bm1 != -1) {
+    for (int j = 0; j < S->nibk; j++)
+      if (S->ibk[j].max < bm1) S->ibk[j].old = 1;
+    ta_series(S, A, block, F, rmax, rmaxidx, bm1, 1, a, _b, 0);
+  }
+  /* 4) the long approximation of this layer joins the newest one when it is
+   * valid from an earlier point */
+  ta_ia bia = ta_ia_make(A, block + 1, block + 2, F, -1, TA_AK, a, _b);
+  if (S->nia && bia.min < S->ia[S->nia - 1].min) {
+    ta_ia *last = &S->ia[S->nia - 1];
+    for (int i = 0; i < bia.nterms; i++) last->c[i] += bia.c[i];
+    if (last->nterms < bia.nterms) last->nterms = bia.nterms;
+    return V;
+  }
+  /* 5) otherwise short approximations bridge to its minimum and it is added */
+  bm1 = rmax;
+  for (int j = 0; j < S->nibk; j++)
+    if ((S->ibk[j].max + 1) > bm1) bm1 = S->ibk[j].max + 1;
+  bia.min = ta_series(S, A, block, F, bm1, rmaxidx, bia.min, 0, a, _b, 1);
+  ta_push_ia(S, bia);
+  return V;
+}
+
+static void ta_free(ta_set *S) {
+  free(S->ia);
+  free(S->ibk);
+  memset(S, 0, sizeof(*S));
+}
+
+int fho_tg_two_series_counts(double alpha, int steps, double a, double b, int *nia, int *nibk) {
+  ta_set S;
+  memset(&S, 0, sizeof(S));
+  double *F = (double *)calloc((size_t)steps + 2, sizeof(double));
+  if (!F) return 1;
+  for (int r = 0; r < steps + 2; ++r) F[r] = 1.0;
+  for (int blk = 0; blk < steps; ++blk) {
+    ta_calc_va(&S, 1.0 - alpha, blk, F, a, b);
+    nia[blk] = S.nia;
+    nibk[blk] = S.nibk;
+  }
+  ta_free(&S);
+  free(F);
+  return 0;
+}
+
 int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work) {
   const int sN = p->sN, M = p->M;
   const size_t P = (size_t)(sN + 2) * (M + 2);
@@ -396,9 +662,22 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
   if (!wx || !wy) return 1;
   const int J = p->dt_alg == 3 ? (int)p->dt_eps : 0;
   if (p->dt_alg == 3 && (J < 1 || p->beta != 1.0)) return 2;
+  if (p->dt_alg == 4 && p->beta != 1.0) return 2;
+  /* dt_alg 4: per point the approximations of the x and y sums (Happ1 with
+   * offsets (1.5, 0.5), Happ2 with (2, 1); fr_d_t_g_2d.cpp:3444-3462) */
+  ta_set *tax = NULL, *tay = NULL;
+  double *F4 = NULL;
+  if (p->dt_alg == 4) {
+    tax = (ta_set *)calloc(P, sizeof(ta_set));
+    tay = (ta_set *)calloc(P, sizeof(ta_set));
+    F4 = (double *)calloc((size_t)(steps + 2) * P, sizeof(double));
+    if (!tax || !tay || !F4) return 1;
+  }
   double *H = J ? (double *)calloc((size_t)J * P, sizeof(double)) : NULL;
-  double *hx = J ? (double *)malloc(sizeof(double) * P) : NULL, *hy = J ? (double *)malloc(sizeof(double) * P) : NULL;
-  if (J && (!H || !hx || !hy)) return 1;
+  const int hs_on = J || p->dt_alg == 4;
+  double *hx = hs_on ? (double *)malloc(sizeof(double) * P) : NULL, *hy = hs_on ? (double *)malloc(sizeof(double) * P) : NULL;
+  if (hs_on && (!hx || !hy)) return 1;
+  if (J && !H) return 1;
   memcpy(work, C, sizeof(double) * P); /* full-step layer 0 (TG_solver::initial) */
 #define KB(s, ja, sa, l) (Da * fho_psi_int((double)(s) + (sa), (double)(s) + (sa) + (l), (double)j + (ja), p->tau, a, p->beta))
   for (int j = 0; j < steps; ++j) {
@@ -410,6 +689,19 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
       tg_series_add(p, J, j, P, work + (size_t)j * P, work + (size_t)(j - 1) * P, H);
       tg_series_eval(p, J, p->tau * ((double)j + 0.5), P, H, Da, hx);
       tg_series_eval(p, J, p->tau * ((double)j + 1.0), P, H, Da, hy);
+      hsx = hx;
+      hsy = hy;
+    }
+    if (p->dt_alg == 4 && j >= 1) {
+      /* F4[id][r] = C^r - C^(r-1) for the newest r = j; both sums at x = j */
+      const double A = 1.0 - a, sc = Da * (pow(p->tau, 1.0 - a) / (1.0 - a));
+#pragma omp parallel for schedule(static)
+      for (size_t id = 0; id < P; ++id) {
+        double *Fi = F4 + id * (size_t)(steps + 2);
+        Fi[j] = work[(size_t)j * P + id] - work[(size_t)(j - 1) * P + id];
+        hx[id] = ta_calc_va(&tax[id], A, j - 1, Fi, 1.5, 0.5) * sc;
+        hy[id] = ta_calc_va(&tay[id], A, j - 1, Fi, 2.0, 1.0) * sc;
+      }
       hsx = hx;
       hsy = hy;
     }
@@ -433,6 +725,12 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
   }
 #undef KB
   free(wx); free(wy); free(H); free(hx); free(hy);
+  if (tax)
+    for (size_t id = 0; id < P; ++id) {
+      ta_free(&tax[id]);
+      ta_free(&tay[id]);
+    }
+  free(tax); free(tay); free(F4);
   return 0;
 }
 

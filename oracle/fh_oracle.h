@@ -95,7 +95,8 @@ typedef struct {
   double C1;          /* x-sweep Dirichlet value at i = 0                   */
   double S;           /* constant source _S                                 */
   double dL, dLx;     /* steps in i (x-sweep) and j (y-sweep)               */
-  int dt_alg;         /* 0 full history, 2 restricted summing, 3 series      */
+  int dt_alg;         /* 0 full history, 2 restricted summing, 3 series,
+                         4 two-series approximation (psi = t)               */
   double dt_eps;      /* dt_alg 2: the sums stop at the first |weight| < eps;
                          dt_alg 3 (psi = t): number of series terms          */
 } fho_tg_params;
@@ -104,12 +105,17 @@ typedef struct {
  * dt_alg 0 or 2 (restricted summing: each history sum runs from the newest
  * layer pair back and stops at the first weight below dt_eps,
  * fr_d_t_g_2d.cpp:3356-3380) or 3 (series expansion, psi = t, dt_eps terms,
- * fr_d_t_g_2d.cpp:3384-3429), int_alg 1, massN 0, testing 0.  Returns 2 for
- * dt_alg 3 with psi != t or dt_eps < 1.  C is updated in place; V2 is |v|^2
+ * fr_d_t_g_2d.cpp:3384-3429) or 4 (two-series approximation, psi = t,
+ * fr_d_t_g_2d.cpp:246-745 and 3438-3469), int_alg 1, massN 0, testing 0.
+ * Returns 2 for dt_alg 3 or 4 with psi != t or dt_alg 3 with dt_eps < 1.  C is updated in place; V2 is |v|^2
  * per node.  work must hold (steps+1) full layers (the full-step layers; the
  * reference's half-step layers are never read by the dt_alg 0 sums except the
  * newest, which is C itself during the y sweep).  Returns 0 on success. */
 int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps, double *work);
+
+/* dt_alg 4 bookkeeping alone: the numbers of long (ia) and short (ibk)
+ * approximations per point after each of `steps` layers (offsets a, b). */
+int fho_tg_two_series_counts(double alpha, int steps, double a, double b, int *nia, int *nibk);
 
 /* ------------------------------------------- 1D Atangana-Baleanu solve path */
 

@@ -104,6 +104,13 @@ def main():
     # series expansion (dt_alg 3, psi = t): 12 terms, 40 steps
     res = parse(run("tg", args[:7] + [40, 3, 12], list(V2) + list(C0)))
     dump("tg_adi_series.json", {"steps": 40, "dt_alg": 3, "dt_eps": 12, "C": res["c"][0]})
+    # two-series approximation (dt_alg 4, psi = t): 150 steps at alpha 0.7 and
+    # 300 steps at alpha 0.9 (tens of long and short approximations per point)
+    two = {}
+    for alpha, steps in ((0.7, 150), (0.9, 300)):
+        a4 = [sN, M, 5e-3, alpha, 0.1, 0.3, 0.05, steps, 4, 1e-8]
+        two[f"{alpha}_{steps}"] = {"alpha": alpha, "steps": steps, "C": parse(run("tg", a4, list(V2) + list(C0)))["c"][0]}
+    dump("tg_adi_two_series.json", two)
     # Atangana-Baleanu: Mittag-Leffler values, lag weights, solve_and_check error
     ml = []
     for (a, b, z) in [(0.5, 1.0, -0.7), (0.8, 1.0, -1.2), (0.6, 2.0, -0.9), (0.9, 5.0, -0.5),

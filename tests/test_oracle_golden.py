@@ -99,6 +99,37 @@ def test_tg_adi_series_matches_reference():
     assert relmax(np.array(full["C"]), sr["C"]) > 0.01
 
 
+@pytest.mark.parametrize("key", ["0.7_150", "0.9_300"])
+def test_tg_adi_two_series_matches_reference(key):
+    """dt_alg 4 (two-series approximation of the history sums, psi = t):
+    the per-point long and short approximations are rebuilt from the same
+    F-independent ranges, so the oracle meets the reference run bit for bit,
+    while the approximation itself stays ~1e-7 from the full-history run."""
+    g = load("tg_adi_restricted.json")  # the same problem
+    r = load("tg_adi_two_series.json")[key]
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=r["alpha"], beta=1.0, sigma=g["sigma"],
+             d=g["d"], C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"], dt_alg=4, dt_eps=1e-8)
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), r["steps"])
+    assert relmax(C, r["C"]) <= 1e-14
+    full, _ = O.tg_solve(dict(p, dt_alg=0), np.array(g["V2"]), np.array(g["C0"]), r["steps"])
+    assert 1e-9 < relmax(full, r["C"]) < 1e-5
+
+
+def test_two_series_bookkeeping_counts():
+    """The approximation sets stay small: after 2000 layers tens of long and
+    short approximations per point and direction, growing slower than the
+    layer count."""
+    import ctypes as C
+    n = 2000
+    for a, b in ((1.5, 0.5), (2.0, 1.0)):
+        nia = np.zeros(n, dtype=np.int32)
+        nibk = np.zeros(n, dtype=np.int32)
+        assert O.lib().fho_tg_two_series_counts(C.c_double(0.7), n, C.c_double(a), C.c_double(b),
+                                                nia.ctypes.data_as(C.c_void_p), nibk.ctypes.data_as(C.c_void_p)) == 0
+        assert 10 <= nia[-1] <= 40 and 10 <= nibk[-1] <= 100
+        assert nia[999] <= nia[-1] < 2 * nia[999] and nibk.max() < 100
+
+
 def test_psi_weights_match_reference_series():
     """calc_int (mt_psi_caputo.cpp:720-741) at eps 1e-15 against the converged
     incomplete-beta value.  The reference series does not converge on the very
