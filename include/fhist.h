@@ -272,6 +272,31 @@ int fh_tg_set_restricted(fh_tg_solver *s, double dt_eps);
  * psi = t, FH_TG_FP64 or FH_TG_DF64 only; nterms = 0 restores the full
  * history; 1..256.  Only before the first step of a solve. */
 int fh_tg_set_series(fh_tg_solver *s, int nterms);
+/* Two-series approximation of the history sums, TG_solver_ with dt_alg 4
+ * (replaces the Om1 branch fr_d_t_g_2d.cpp:3438-3469 with calc_va and the
+ * ia / ibk approximations 246-745): per node long (powers of t) and short
+ * (Taylor) series whose coefficients absorb each new layer difference, each
+ * within approx_eps = 1e-7 of its share of the sum.  The approximation
+ * bookkeeping does not depend on the field and is planned on the host for
+ * every step up to max_steps when enabled; the device keeps the coefficients
+ * per node (tens of approximations of up to 20 terms per direction) and the
+ * newest layer only.  psi = t, FH_TG_FP64 or FH_TG_DF64, no series expansion
+ * at the same time; enable = 0 restores the full history.  Only before the
+ * first step of a solve. */
+int fh_tg_set_two_series(fh_tg_solver *s, int enable);
+/* The host bookkeeping of fh_tg_set_two_series for inspection (no device
+ * work, no reference counterpart): per step j = 1 .. max_steps - 1 and
+ * direction d (0: x sums, 1: y sums) spans[4 (2 j + d) + 0..2] = {first item,
+ * first update item, end}; an item is 4 ints {kind | terms << 8, slot,
+ * source slot, coefficient offset}, kind 0 evaluate (basis values at the
+ * offset), 1 copy the source slot, 2 / 3 add to a long / short slot and 4 / 5
+ * initialise one with the newest layer's coefficients ak[k] (F g[k]) (ak at
+ * the offset, g after them; long slots keep c[0] = 0).  nslots[2]: slots per
+ * point and direction; dterm[2]: the newest layer's weight.  Call with null
+ * items / coef / spans to obtain *n_items and *n_coef, then with buffers of
+ * those sizes (spans: 8 (max_steps + 1) ints). */
+int fh_tg_two_series_plan(double alpha, int max_steps, int *nslots, double *dterm, int *n_items, int *items,
+                          int *n_coef, double *coef, int *spans);
 /* TG_solver::calc_step repeated nsteps times. */
 int fh_tg_step(fh_tg_solver *s, int nsteps);
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);

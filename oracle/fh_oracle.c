@@ -635,6 +635,25 @@ static void ta_free(ta_set *S) {
   memset(S, 0, sizeof(*S));
 }
 
+int fho_two_series_sums(double alpha, int nsteps, int P, const double *F, double *Vx, double *Vy) {
+  for (int p = 0; p < P; ++p) {
+    ta_set sx, sy;
+    memset(&sx, 0, sizeof(sx));
+    memset(&sy, 0, sizeof(sy));
+    double *Fi = (double *)malloc(sizeof(double) * (size_t)(nsteps + 1));
+    if (!Fi) return 1;
+    for (int r = 0; r <= nsteps; ++r) Fi[r] = F[(size_t)r * P + p];
+    for (int j = 1; j <= nsteps; ++j) {
+      Vx[(size_t)j * P + p] = ta_calc_va(&sx, 1.0 - alpha, j - 1, Fi, 1.5, 0.5);
+      Vy[(size_t)j * P + p] = ta_calc_va(&sy, 1.0 - alpha, j - 1, Fi, 2.0, 1.0);
+    }
+    free(Fi);
+    ta_free(&sx);
+    ta_free(&sy);
+  }
+  return 0;
+}
+
 int fho_tg_two_series_counts(double alpha, int steps, double a, double b, int *nia, int *nibk) {
   ta_set S;
   memset(&S, 0, sizeof(S));

@@ -117,6 +117,12 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
  * approximations per point after each of `steps` layers (offsets a, b). */
 int fho_tg_two_series_counts(double alpha, int steps, double a, double b, int *nia, int *nibk);
 
+/* dt_alg 4 sums alone for given layer differences F[r][p] (r = 0..nsteps,
+ * F[0] unused): Vx[j][p], Vy[j][p] (j = 1..nsteps) = calc_va of block j - 1
+ * with the x (1.5, 0.5) and y (2, 1) offsets, before the factor
+ * Da tau^(1-alpha) / (1-alpha). */
+int fho_two_series_sums(double alpha, int nsteps, int P, const double *F, double *Vx, double *Vy);
+
 /* ------------------------------------------- 1D Atangana-Baleanu solve path */
 
 /* solve_and_check (MF_int_series.cpp:875-958) with simple=1, quad=0:

@@ -658,3 +658,76 @@ def test_ab_vs_oracle(ctx):
     srcs = np.repeat(src, n, axis=0)
     ref, _ = O.ab_solve(cfg["m"], n, cfg["tau"], cfg["alpha"], w, srcs, np.zeros(n), np.zeros(n), C0)
     assert relmax(s.get_c(), ref) <= TOL_SOLVER
+
+
+@pytest.mark.parametrize("mode_name", ["FH_TG_FP64", "FH_TG_DF64"])
+def test_tg_two_series_vs_reference_and_oracle(ctx, mode_name):
+    """dt_alg 4 (two-series approximation, psi = t) through the library:
+    against the reference's own run (golden) and the oracle, and ~1e-7 away
+    from the full-history solve (the approximation is the reference's)."""
+    from theses_code_gb300 import _lib
+    from theses_code_gb300.solvers import TGSolver
+    g = json.load(open(os.path.join(G, "tg_adi_restricted.json")))
+    for key in ("0.7_150", "0.9_300"):
+        r = json.load(open(os.path.join(G, "tg_adi_two_series.json")))[key]
+        p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=r["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+                 C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+        s = TGSolver(ctx, p, r["steps"] + 1, getattr(_lib, mode_name))
+        s.set_two_series(True)
+        s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+        s.calc_step(r["steps"])
+        got = s.get_c()
+        assert relmax(got, r["C"]) <= TOL_SOLVER, (key, relmax(got, r["C"]))
+        ref, _ = O.tg_solve(dict(p, dt_alg=4, dt_eps=1e-8), np.array(g["V2"]), np.array(g["C0"]), r["steps"])
+        assert relmax(got, ref) <= TOL_SOLVER
+        s.close()
+
+
+def test_tg_two_series_larger_grid(ctx):
+    """dt_alg 4 on a 48 x 40 grid over 300 steps (tens of approximations per
+    node) against the oracle, in uneven step calls after a captured solve."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(48, 40, alpha=0.6, tau=1e-3, d=0.1, seed=4, C1=0.2)
+    steps = 300
+    ref, _ = O.tg_solve(dict(p, dt_alg=4, dt_eps=1e-8), V2, C0, steps)
+    full, _ = O.tg_solve(p, V2, C0, steps)
+    assert 1e-10 < relmax(ref, full) < 1e-4  # the approximation is in play
+    s = TGSolver(ctx, p, steps + 1)
+    s.set_two_series(True)
+    s.set_state(V2, C0)
+    s.calc_step(steps)
+    assert relmax(s.get_c(), ref) <= TOL_SOLVER
+    s.set_state(V2, C0)
+    for n in (1, 150, 149):
+        s.calc_step(n)
+    assert relmax(s.get_c(), ref) <= TOL_SOLVER
+    s.close()
+
+
+def test_tg_two_series_limits(ctx):
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FhError
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(24, 20, alpha=0.6, tau=1e-3, d=0.1, seed=4)
+    s = TGSolver(ctx, p, 20)
+    s.set_series(8)
+    with pytest.raises(FhError):
+        s.set_two_series(True)  # not with the single-series expansion
+    s.set_series(0)
+    s.set_two_series(True)
+    with pytest.raises(FhError):
+        s.set_series(8)
+    s.set_state(V2, C0)
+    s.calc_step(3)
+    with pytest.raises(FhError):
+        s.set_two_series(False)  # only before the first step
+    s.close()
+    b = TGSolver(ctx, p, 20, FH_TG_BLOCKED)
+    with pytest.raises(FhError):
+        b.set_two_series(True)
+    b.close()
+    q = TGSolver(ctx, dict(p, beta=1.3), 20)
+    with pytest.raises(FhError):
+        q.set_two_series(True)
+    q.close()

@@ -32,6 +32,7 @@
 #include "fh_linescan.cuh"
 #include "fh_sm100.cuh"
 #include "fh_weights.cuh"
+#include "fh_two_series.h"
 
 // blocked contraction helpers (fh_blocked.cu)
 struct fh_blk;
@@ -101,7 +102,12 @@ struct fh_tg_solver {
   // keeps only the newest layer pair
   int ser_J = 0;
   fh_dbuf H, ser_tab;
+  // two-series approximation (dt_alg 4): planned tables and coefficient
+  // slots; the history store keeps only the newest layer pair
+  fh_ta *two = nullptr;
+  bool one_layer() const { return ser_J || two; }
   ~fh_tg_solver() {
+    if (two) fh_ta_delete(two);
     if (blk) fh_blk_delete(blk);
     if (hs) {
       cudaStreamSynchronize(hs);
@@ -1451,7 +1457,7 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   // mode; with restricted summing and psi = t, the layers within the cut lag
   int kstart = blocked ? s->j0 : 0;
   if (!blocked && s->rs_lag >= 0 && j > s->rs_lag) kstart = j - s->rs_lag;
-  if (s->ser_J) kstart = j;  // series expansion: no layer sums
+  if (s->one_layer()) kstart = j;  // series expansions: no layer sums
   const int knear = j - kstart;
   const double *Wj;
   if (s->wtab) {
@@ -1488,6 +1494,15 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
     if ((rc = fh_after_launch(ctx, "k_tg_series"))) return rc;
     splits = 1;
   }
+  if (s->two && j >= 1) {
+    fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+    const double a = s->p.alpha;
+    rc = fh_ta_step(ctx, s->two, j, s->D.as<double>(), s->df ? 1 : 0, g.P, g.Da * (pow(g.tau, 1.0 - a) / (1.0 - a)),
+                    s->part.as<double>(), ctx->stream);
+    fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+    if (rc) return rc;
+    splits = 1;
+  }
   if (knear >= 1) {
     fh_hist_plan(g.P, knear, s->max_splits, &splits, &kchunk);
     if (s->df)
@@ -1514,7 +1529,7 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
   const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
   k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
-      g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (s->ser_J ? 0LL : (long long)j * g.P),
+      g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (s->one_layer() ? 0LL : (long long)j * g.P),
       s->part.as<double>(), g.P,
       splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(),
       s->pby.as<double>(), cwj, fary, s->df ? 1 : 0);
@@ -1729,6 +1744,7 @@ int fh_tg_set_series(fh_tg_solver *s, int nterms) {
   FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_series: only before the first step of a solve");
   FH_REQUIRE(ctx, nterms == 0 || (s->p.beta == 1.0 && s->mode != FH_TG_BLOCKED), FH_EINVAL,
              "fh_tg_set_series: psi = t and the FP64 or DF64 mode only");
+  FH_REQUIRE(ctx, nterms == 0 || !s->two, FH_EINVAL, "fh_tg_set_series: the two-series approximation is enabled");
   const fh_tg_dev &g = s->dv;
   int rc;
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1789,6 +1805,31 @@ int fh_tg_set_series(fh_tg_solver *s, int nterms) {
   adopt(s->H, nH);
   adopt(s->ser_tab, ntab);
   s->ser_J = J;
+  return FH_OK;
+}
+
+int fh_tg_set_two_series(fh_tg_solver *s, int enable) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_two_series: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_two_series: only before the first step of a solve");
+  FH_REQUIRE(ctx, !enable || (s->p.beta == 1.0 && s->mode != FH_TG_BLOCKED), FH_EINVAL,
+             "fh_tg_set_two_series: psi = t and the FP64 or DF64 mode only");
+  FH_REQUIRE(ctx, !enable || !s->ser_J, FH_EINVAL, "fh_tg_set_two_series: the series expansion is enabled");
+  FH_REQUIRE(ctx, s->p.alpha > 0.0 && s->p.alpha < 1.0, FH_EINVAL, "fh_tg_set_two_series: alpha = %g",
+             s->p.alpha);
+  const fh_tg_dev &g = s->dv;
+  int rc;
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // new buffers first: on failure the solver keeps its previous configuration
+  fh_dbuf nD;
+  if ((rc = fh_alloc(ctx, nD, sizeof(double) * (size_t)g.P * (enable ? 1 : (size_t)s->max_steps)))) return rc;
+  fh_ta *t = nullptr;
+  if (enable && (rc = fh_ta_create(ctx, s->p.alpha, s->max_steps, g.P, &t))) return rc;
+  std::swap(s->D.p, nD.p);
+  std::swap(s->D.bytes, nD.bytes);
+  if (s->two) fh_ta_delete(s->two);
+  s->two = t;
+  s->graph.reset();
   return FH_OK;
 }
 

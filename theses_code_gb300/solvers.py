@@ -142,6 +142,12 @@ class TGSolver:
         stored layers; 0 = full history."""
         check(self.ctx.L.fh_tg_set_series(self.h, int(nterms)), self.ctx.h)
 
+    def set_two_series(self, enable: bool = True):
+        """Two-series approximation of the history sums (the reference's
+        dt_alg 4, psi = t): per node long and short series absorb each new
+        layer difference; only the newest layer is stored."""
+        check(self.ctx.L.fh_tg_set_two_series(self.h, int(bool(enable))), self.ctx.h)
+
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_tg_step(self.h, int(n)), self.ctx.h)
 
