@@ -777,7 +777,7 @@ def run_serve(args):
     torch.cuda.set_device(0)
     reqs = serve.make_mix(args.requests, rate=args.rate, seed=3, mode_2d=FH_TG_BLOCKED)
     warm = serve.make_mix(6, rate=args.rate, seed=101, max_2d=64, steps=(100, 200), nrange=(64, 256))
-    srv = serve.Server(args.budget_gb * 1e9, chunk=250, max_cohort=512, max_active=16)
+    srv = serve.Server(args.budget_gb * 1e9, chunk=250, max_pool=512, max_active=16)
     srv.run(warm)
     clocks = ClockSampler(0)
     clocks.start()

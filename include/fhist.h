@@ -192,9 +192,24 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
 int fh_h_batch_destroy(fh_h_batch *b);
 /* Total number of doubles of the concatenated state (sum of N_i + 2). */
 long long fh_h_batch_state_size(const fh_h_batch *b);
+/* Device bytes the batch holds (history, tables, work buffers); -1 for null.
+ * No reference counterpart (serving admission). */
+long long fh_h_batch_device_bytes(const fh_h_batch *b);
 /* Concatenated per-instance U arrays (N_i + 2 each, instance order); resets tstep to 1. */
 int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host);
 int fh_h_batch_set_u(fh_h_batch *b, const double *U);
+/* Continuous batching: instance i starts a new solve (parameters p, initial
+ * state U0_host of p->N + 2 values) between two steps of the batch, while
+ * the other instances go on.  Its steps count from 1 again, its history
+ * starts empty (the earlier occupant's history slots are never read), and
+ * its result after n further batch steps equals a fresh solve of n steps
+ * within rounding (the history sums split at the batch's slot boundaries).
+ * p->N may not exceed the node count the instance was created with (rounded
+ * up to even); the occupant runs until the batch's max_steps is reached.
+ * FP64 and DF64 history modes, no space-fractional instances in the batch.
+ * Whole-batch state setters put every instance back on the batch clock.
+ * No reference counterpart (the reference runs one solve per object). */
+int fh_h_batch_restart(fh_h_batch *b, int i, const fh_h_params *p, const double *U0_host);
 int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host);
 /* U of instances [first, first+count) only (concatenated), synchronising the stream. */
 int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_host);
@@ -301,6 +316,9 @@ int fh_tg_two_series_plan(double alpha, int max_steps, int *nslots, double *dter
 int fh_tg_step(fh_tg_solver *s, int nsteps);
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);
 /* Device pointer to the current field ((sN+2)*(M+2) doubles, owned by the solver). */
+/* Device bytes the solver holds (history, tables, work buffers); -1 for
+ * null.  No reference counterpart (serving admission). */
+long long fh_tg_device_bytes(const fh_tg_solver *s);
 const double *fh_tg_field(const fh_tg_solver *s);
 int fh_tg_tstep(const fh_tg_solver *s);
 

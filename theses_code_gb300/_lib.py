@@ -63,9 +63,12 @@ _SIGS = {
     "fh_h_batch_create": (_i, [_vp, _i, C.POINTER(HParams), _i, C.POINTER(_vp)]),
     "fh_h_batch_destroy": (_i, [_vp]),
     "fh_h_batch_state_size": (_ll, [_vp]),
+    "fh_h_batch_device_bytes": (_ll, [_vp]),
+    "fh_tg_device_bytes": (_ll, [_vp]),
     "fh_h_batch_set_u_host": (_i, [_vp, _dp]),
     "fh_h_batch_get_u_host": (_i, [_vp, _dp]),
     "fh_h_batch_set_u": (_i, [_vp, _dp]),
+    "fh_h_batch_restart": (_i, [_vp, _i, C.POINTER(HParams), _dp]),
     "fh_h_batch_get_u_range_host": (_i, [_vp, _i, _i, _dp]),
     "fh_h_batch_step": (_i, [_vp, _i]),
     "fh_h_batch_tstep": (_i, [_vp]),

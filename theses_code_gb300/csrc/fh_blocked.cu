@@ -746,6 +746,9 @@ struct fh_blk {
 
 fh_blk *fh_blk_new() { return new fh_blk(); }
 void fh_blk_delete(fh_blk *b) { delete b; }
+size_t fh_blk_bytes(const fh_blk &b) {
+  return b.H3.bytes + b.A3.bytes + b.Ed.bytes + b.Ew.bytes + b.err.bytes + b.part.bytes;
+}
 long long fh_blk_ppad(const fh_blk &b) { return b.Ppad; }
 
 int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
@@ -887,6 +890,9 @@ void fh_hblk_delete(fh_hblk *b) { delete b; }
 __nv_bfloat16 *fh_hblk_wplanes(fh_hblk &b) { return b.W3.as<__nv_bfloat16>(); }
 int8_t *fh_hblk_wexp(fh_hblk &b) { return b.Ew.as<int8_t>(); }
 int fh_hblk_kcap(const fh_hblk &b) { return b.Kcap; }
+size_t fh_hblk_bytes(const fh_hblk &b) {
+  return b.H3.bytes + b.Ed.bytes + b.W3.bytes + b.Ew.bytes + b.tiles.bytes + b.err.bytes;
+}
 
 // tiles: (first point, instance, valid points) of every 128-point tile
 int fh_hblk_init(fh_ctx *ctx, fh_hblk &b, long long P, int Kcap, int ninst, const long long *tile_p0,

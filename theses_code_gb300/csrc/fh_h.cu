@@ -33,10 +33,15 @@ int fh_hblk_check(fh_ctx *ctx, fh_hblk &b);
 __nv_bfloat16 *fh_hblk_wplanes(fh_hblk &b);
 int8_t *fh_hblk_wexp(fh_hblk &b);
 int fh_hblk_kcap(const fh_hblk &b);
+size_t fh_hblk_bytes(const fh_hblk &b);
 
 struct fh_h_dev_inst {
   int N, weights, kmodel, gravity;
   int fixed;  // coefficients independent of u and of the step: factor once
+  // the instance's own clock (fh_h_batch_restart): its step is tstep - tb and
+  // its saved-layer count nsaved - ob; history slots below ob belong to an
+  // earlier occupant and are never read
+  int tb, ob;
   long long off;  // segment start in the concatenated state
   double dL, Dg, Da, tau, alpha, beta, kc, kgam, cinv, al_left, bt_left, u_right;
   // space-fractional derivative in z (fh_h_batch_set_space_order): order
@@ -70,6 +75,7 @@ struct fh_h_batch {
   // (h_alpha_serial); varcoef: the batch has such instances
   bool serial_al = true, varcoef = false;
   std::vector<fh_h_dev_inst> di;  // host copy of inst
+  std::vector<int> cap;           // nodes a restarted occupant of each instance may have (segment - 2)
   // space-fractional instances: Toeplitz weights wsp and the sums sV per
   // node (state layout), shared memory of k_h_space_v
   bool space = false;
@@ -116,14 +122,18 @@ static constexpr int kIbStride = 2 * kIbTerms + 4;
 // at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
 // Thread i of CTA (x, b) owns slot i = t_lo + x*128 + threadIdx.x (slots below
 // t_lo are not computed); i = max(os - 1, 0) is the current slot.
-__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep, int os, int t_lo,
-                            double *__restrict__ W, int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
-                            const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX) {
+__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep_g, int os_g, int t_lo,
+                            double *__restrict__ W_g, int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
+                            const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX_g) {
   const int b = blockIdx.y;
+  const fh_h_dev_inst I = inst[b];
+  // the instance's own step and slot numbers; its slot i is column I.ob + i
+  const int tstep = tstep_g - I.tb, os = os_g - I.ob;
+  double *W = W_g + I.ob;
+  const double invX = I.tb == 0 ? invX_g : 1.0 / (double)(tstep + 1);
   const int i = t_lo + blockIdx.x * kHWeightThreads + threadIdx.x;
   const int nh = os > 1 ? os - 1 : 0;  // history slots
   if (i > nh) return;
-  const fh_h_dev_inst I = inst[b];
   const bool cur = i == nh;
   if (I.weights == FH_W_PSI && I.beta != 1.0) {
     // psi = t^beta: the interval [x0, x0 + 1] in the divided-difference form of
@@ -224,10 +234,11 @@ __global__ void __launch_bounds__(kTileThreads) k_hist_tiles(const fh_h_tile *__
   __syncthreads();
   const int q = threadIdx.x * 2;
   if (q >= T.len) return;
-  const long long p = inst[T.inst].off + T.start + q;
+  const fh_h_dev_inst &I = inst[T.inst];
+  const long long p = I.off + T.start + q;
   double a0 = 0.0, a1 = 0.0;
-  const double *d = D + (long long)k0 * ldd + p;
-  int k = 0;
+  int k = max(0, I.ob - k0);  // slots of the instance's current occupant only
+  const double *d = D + (long long)(k0 + k) * ldd + p;
   for (; k + 4 <= nk; k += 4) {
     const double2 v0 = fh_ld_stream2(d), v1 = fh_ld_stream2(d + ldd);
     const double2 v2 = fh_ld_stream2(d + 2 * ldd), v3 = fh_ld_stream2(d + 3 * ldd);
@@ -271,11 +282,12 @@ __global__ void __launch_bounds__(kTileThreads) k_hist_tiles_df(const fh_h_tile 
   __syncthreads();
   const int q = threadIdx.x * 2;
   if (q >= T.len) return;
-  const long long p = inst[T.inst].off + T.start + q;
+  const fh_h_dev_inst &I = inst[T.inst];
+  const long long p = I.off + T.start + q;
   fh_df a0{0.f, 0.f}, a1{0.f, 0.f};
-  const float4 *d = reinterpret_cast<const float4 *>(D + (long long)k0 * ldd + p);
+  int k = max(0, I.ob - k0);  // slots of the instance's current occupant only
+  const float4 *d = reinterpret_cast<const float4 *>(D + (long long)(k0 + k) * ldd + p);
   const long long ld4 = ldd / 2;
-  int k = 0;
   for (; k + 4 <= nk; k += 4) {
     float4 v[4];
 #pragma unroll
@@ -437,9 +449,10 @@ __device__ __forceinline__ void h_line(const fh_h_dev_inst &I, int b, int lane, 
                                        long long ldpart, int splits, double *__restrict__ Al,
                                        double *__restrict__ Bt, double *__restrict__ sA, double *__restrict__ sB,
                                        double *__restrict__ sR, double *__restrict__ sOm, double *__restrict__ Dnew,
-                                       int append, int first, int dfstore, const double *__restrict__ sV,
+                                       int append, int os, int dfstore, const double *__restrict__ sV,
                                        fh_mob *smm, fh_aff *sma, int serial) {
   constexpr int TG = 32 * NW;
+  const bool first = os == I.ob;  // the instance's first step (saved-layer count os)
   const long long o = I.off;
   double *u = U + o;
   const int N = I.N;
@@ -565,12 +578,12 @@ __global__ void __launch_bounds__(128, 7) k_h_line_warp(const fh_h_dev_inst *__r
                                                      double *__restrict__ Al, double *__restrict__ Bt,
                                                      double *__restrict__ sA, double *__restrict__ sB,
                                                      double *__restrict__ sR, double *__restrict__ sOm,
-                                                     double *__restrict__ Dnew, int append, int first,
+                                                     double *__restrict__ Dnew, int append, int os,
                                                      int dfstore, const double *__restrict__ sV) {
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (b >= n) return;  // whole warp
   h_line<1, SPACE, PH>(inst[b], b, threadIdx.x & 31, U, wc, part, ldpart, splits, Al, Bt, sA, sB, sR, sOm, Dnew,
-                       append, first, dfstore, sV, nullptr, nullptr, PH != kLineAll);
+                       append, os, dfstore, sV, nullptr, nullptr, PH != kLineAll);
 }
 
 // Al of every variable-coefficient instance (h_alpha_serial), one lane per
@@ -596,11 +609,11 @@ __global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
     const fh_h_dev_inst *__restrict__ inst, double *__restrict__ U, const double *__restrict__ wc,
     const double *__restrict__ part, long long ldpart, int splits, double *__restrict__ Al, double *__restrict__ Bt,
     double *__restrict__ sA, double *__restrict__ sB, double *__restrict__ sR, double *__restrict__ sOm,
-    double *__restrict__ Dnew, int append, int first, int dfstore, const double *__restrict__ sV, int serial) {
+    double *__restrict__ Dnew, int append, int os, int dfstore, const double *__restrict__ sV, int serial) {
   __shared__ fh_mob smm[kLineCtaWarps];
   __shared__ fh_aff sma[kLineCtaWarps];
   h_line<kLineCtaWarps, SPACE, kLineAll>(inst[blockIdx.x], blockIdx.x, threadIdx.x, U, wc, part, ldpart, splits, Al,
-                                         Bt, sA, sB, sR, sOm, Dnew, append, first, dfstore, sV, smm, sma, serial);
+                                         Bt, sA, sB, sR, sOm, Dnew, append, os, dfstore, sV, smm, sma, serial);
 }
 
 // ---------------------------------------------------- blocked history mode
@@ -1048,7 +1061,7 @@ static int h_one_step(fh_h_batch *B, bool next) {
                  : blk   ? reinterpret_cast<double *>(B->ring.as<float2>() + (long long)((os - 1) & 127) * B->Ptot)
                          : B->D.as<double>() + (long long)(os - 1) * B->Ptot;
   {
-    const int fst = os == 0 ? 1 : 0, dfs = (B->mode == FH_H_DF64 || blk) ? 1 : 0;
+    const int fst = os, dfs = (B->mode == FH_H_DF64 || blk) ? 1 : 0;  // first step per instance: os == its base
     const dim3 gc((unsigned)B->n), gw((unsigned)fh_ceil_div(B->n, 4));
     const fh_h_dev_inst *in = B->inst.as<fh_h_dev_inst>();
     double *Al = B->Al.as<double>(), *Bt = B->Bt.as<double>(), *sA = B->sA.as<double>(), *sB = B->sB.as<double>();
@@ -1095,6 +1108,56 @@ static int h_one_step(fh_h_batch *B, bool next) {
   return FH_OK;
 }
 
+// A new solve of the whole batch: every instance on the batch's clock again.
+static int h_reset_clocks(fh_h_batch *b) {
+  bool any = false;
+  for (auto &I : b->di)
+    if (I.tb || I.ob) {
+      I.tb = I.ob = 0;
+      any = true;
+    }
+  if (!any) return FH_OK;
+  FH_CUDA_TRY(b->ctx, cudaMemcpyAsync(b->inst.p, b->di.data(), sizeof(fh_h_dev_inst) * b->n, cudaMemcpyHostToDevice,
+                                      b->ctx->stream));
+  FH_CUDA_TRY(b->ctx, cudaStreamSynchronize(b->ctx->stream));
+  b->w_ready = -1;
+  b->graph.reset();
+  return FH_OK;
+}
+
+static bool h_params_ok(const fh_h_params &p) {
+  return p.N >= 2 && p.N <= (1 << 20) && p.L > 0 && p.tau > 0 && p.alpha > 0 && p.alpha < 1 &&
+         (p.weights == FH_W_L1 || p.weights == FH_W_PSI) && (p.kmodel == FH_K_CONST || p.kmodel == FH_K_EXP) &&
+         (p.weights == FH_W_L1 || p.beta > 0);
+}
+
+// Device record of one instance (segment at `off`, own clock at zero).
+static void h_fill_inst(const fh_h_params &p, long long off, fh_h_dev_inst &I) {
+  I.N = p.N;
+  I.weights = p.weights;
+  I.kmodel = p.kmodel;
+  I.gravity = p.gravity;
+  I.fixed = (p.kmodel == FH_K_CONST) && (p.weights == FH_W_L1 || p.beta == 1.0);
+  I.tb = 0;
+  I.ob = 0;
+  I.off = off;
+  I.dL = p.L / p.N;
+  I.Dg = pow(I.dL, -2.0);
+  I.Da = p.weights == FH_W_L1 ? pow(p.tau, -p.alpha) / tgamma(2.0 - p.alpha) : pow(p.tau, -1.0) / tgamma(2.0 - p.alpha);
+  I.tau = p.tau;
+  I.alpha = p.alpha;
+  I.beta = p.beta;
+  I.kc = p.kc;
+  I.kgam = p.kgam;
+  I.cinv = p.cinv;
+  I.al_left = p.al_left;
+  I.bt_left = p.bt_left;
+  I.u_right = p.u_right;
+  I.spg = 1.0;
+  I.spA = 0.0;
+  I.kbf = 1.0;
+}
+
 extern "C" {
 
 int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, int max_steps, fh_h_batch **out) {
@@ -1111,39 +1174,17 @@ int fh_h_batch_create(fh_ctx *ctx, int ninst, const fh_h_params *params_host, in
   long long off = 0;
   for (int b = 0; b < ninst; ++b) {
     const fh_h_params &p = params_host[b];
-    if (!(p.N >= 2 && p.N <= (1 << 20) && p.L > 0 && p.tau > 0 && p.alpha > 0 && p.alpha < 1 &&
-          (p.weights == FH_W_L1 || p.weights == FH_W_PSI) && (p.kmodel == FH_K_CONST || p.kmodel == FH_K_EXP) &&
-          (p.weights == FH_W_L1 || p.beta > 0))) {
+    if (!h_params_ok(p)) {
       delete B;
       return fh_set_error(ctx, FH_EINVAL, "fh_h_batch_create: bad parameters for instance %d", b);
     }
     fh_h_dev_inst &I = di[b];
-    I.N = p.N;
-    I.weights = p.weights;
-    I.kmodel = p.kmodel;
-    I.gravity = p.gravity;
-    I.fixed = (p.kmodel == FH_K_CONST) && (p.weights == FH_W_L1 || p.beta == 1.0);
+    h_fill_inst(p, off, I);
     if (!I.fixed) B->varcoef = true;
     if (I.weights == FH_W_L1) B->has_l1 = true;
-    I.off = off;
-    I.dL = p.L / p.N;
-    I.Dg = pow(I.dL, -2.0);
-    I.Da = p.weights == FH_W_L1 ? pow(p.tau, -p.alpha) / tgamma(2.0 - p.alpha)
-                                : pow(p.tau, -1.0) / tgamma(2.0 - p.alpha);
-    I.tau = p.tau;
-    I.alpha = p.alpha;
-    I.beta = p.beta;
-    I.kc = p.kc;
-    I.kgam = p.kgam;
-    I.cinv = p.cinv;
-    I.al_left = p.al_left;
-    I.bt_left = p.bt_left;
-    I.u_right = p.u_right;
-    I.spg = 1.0;
-    I.spA = 0.0;
-    I.kbf = 1.0;
     B->off.push_back(off);
     const int seg = ((p.N + 2) + 1) & ~1;
+    B->cap.push_back(seg - 2);
     for (int k = 0; k < 3; ++k) {
       const int tn = 2 * kTileShapes[k];
       for (int st = 0; st < seg; st += tn) B->tiles_by[k].push_back({b, st, seg - st < tn ? seg - st : tn});
@@ -1225,6 +1266,17 @@ int fh_h_batch_destroy(fh_h_batch *b) {
   return FH_OK;
 }
 
+long long fh_h_batch_device_bytes(const fh_h_batch *b) {
+  if (!b) return -1;
+  const fh_dbuf *bufs[] = {&b->inst, &b->U, &b->D, &b->W, &b->Lb, &b->ibt, &b->lgt, &b->wc, &b->part, &b->Al,
+                           &b->Bt, &b->sA, &b->sB, &b->sR, &b->sOm, &b->wsp, &b->sV, &b->ring, &b->far, &b->cheb,
+                           &b->tl_by[0], &b->tl_by[1], &b->tl_by[2]};
+  size_t s = 0;
+  for (const fh_dbuf *d : bufs) s += d->bytes;
+  if (b->hb) s += fh_hblk_bytes(*b->hb);
+  return (long long)s;
+}
+
 long long fh_h_batch_state_size(const fh_h_batch *b) {
   if (!b) return -1;
   long long s = 0;
@@ -1246,6 +1298,43 @@ int fh_h_batch_set_u_host(fh_h_batch *b, const double *U_host) {
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   b->tstep = 1;
   b->nsaved = 0;
+  return h_reset_clocks(b);
+}
+
+int fh_h_batch_restart(fh_h_batch *b, int i, const fh_h_params *p, const double *U0_host) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  fh_ctx *ctx = b->ctx;
+  FH_REQUIRE(ctx, p && U0_host && i >= 0 && i < b->n, FH_EINVAL, "fh_h_batch_restart: bad arguments");
+  FH_REQUIRE(ctx, h_params_ok(*p), FH_EINVAL, "fh_h_batch_restart: bad parameters");
+  FH_REQUIRE(ctx, p->N <= b->cap[i], FH_EINVAL, "fh_h_batch_restart: N = %d above the instance's %d nodes", p->N,
+             b->cap[i]);
+  FH_REQUIRE(ctx, b->mode != FH_H_BLOCKED && !b->space, FH_EINVAL,
+             "fh_h_batch_restart: FP64 or DF64 history, no space-fractional instances");
+  FH_REQUIRE(ctx, b->nsaved + 1 < b->max_steps, FH_ENOMEM, "fh_h_batch_restart: no history slots left (%d of %d)",
+             b->nsaved, b->max_steps);
+  fh_h_dev_inst I;
+  h_fill_inst(*p, b->off[i], I);
+  I.tb = b->tstep - 1;  // the occupant's first step is its step 1
+  I.ob = b->nsaved;
+  b->di[i] = I;
+  b->hp[i] = *p;
+  if (!I.fixed) b->varcoef = true;
+  if (I.weights == FH_W_L1) b->has_l1 = true;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(b->U.as<double>() + b->off[i], U0_host, sizeof(double) * ((size_t)p->N + 2),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+  fh_h_dev_inst *di = b->inst.as<fh_h_dev_inst>() + i;
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(di, &b->di[i], sizeof(fh_h_dev_inst), cudaMemcpyHostToDevice, ctx->stream));
+  // the occupant's lag and series tables
+  k_h_lagtab<<<dim3((unsigned)fh_ceil_div(b->max_weights, 128), 1), 128, 0, ctx->stream>>>(
+      di, b->max_weights, b->Lb.as<double>() + (long long)i * b->max_weights, b->max_weights);
+  int rc = fh_after_launch(ctx, "k_h_lagtab");
+  if (rc) return rc;
+  k_h_ibtab<<<1, 32, 0, ctx->stream>>>(di, 1, b->ibt.as<double>() + (long long)i * kIbStride);
+  if ((rc = fh_after_launch(ctx, "k_h_ibtab"))) return rc;
+  // the host copy of the initial state and the records are read before return
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  b->w_ready = -1;  // weights prepared ahead used the previous occupant's clock
+  b->graph.reset();
   return FH_OK;
 }
 
@@ -1262,7 +1351,7 @@ int fh_h_batch_set_u(fh_h_batch *b, const double *U) {
   }
   b->tstep = 1;
   b->nsaved = 0;
-  return FH_OK;
+  return h_reset_clocks(b);
 }
 
 int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host) {

@@ -38,6 +38,7 @@
 struct fh_blk;
 fh_blk *fh_blk_new();
 void fh_blk_delete(fh_blk *b);
+size_t fh_blk_bytes(const fh_blk &b);
 int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap);
 int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k0, int df);
 int fh_blk_tg_weights(fh_ctx *ctx, fh_blk &b, int j0, double Da, double tau, double alpha, double beta, double cut,
@@ -985,7 +986,8 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
   __shared__ float2 ub_sm[kFuseLines][2];
   const fh_tg_dev &g = a.g;
   const int Nx = g.sN, Ny = g.M;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x;
+  [[maybe_unused]] const int warp = tid >> 5;  // read by the phase stamps of profiling builds
   float2 *fa_x = sbf, *al_x = fa_x + kFuseLines * kFuseSL;  // solve layout, [line][slot]
   float2 *fa_y = al_x + kFuseLines * kFuseSL, *al_y = fa_y + kFuseLines * kFuseSL;
   float2 *g_x = al_y + kFuseLines * kFuseSL, *g_y = g_x + kFuseLines * kFuseNL;  // node layout, [line][i-1]
@@ -1921,6 +1923,20 @@ int fh_tg_get_c_host(fh_tg_solver *s, double *C_host) {
     if (h) return fh_set_error(ctx, FH_ETIMEOUT, "fused sweeps: a bounded grid barrier expired");
   }
   return FH_OK;
+}
+
+long long fh_tg_device_bytes(const fh_tg_solver *s) {
+  if (!s) return -1;
+  const fh_dbuf *bufs[] = {&s->C,    &s->Ch,   &s->V2,   &s->D,    &s->W,    &s->cw,   &s->part, &s->alx,
+                           &s->gx,   &s->fax,  &s->pfx,  &s->pbx,  &s->aly,  &s->gy,   &s->fay,  &s->pfy,
+                           &s->pby,  &s->far,  &s->Cd,   &s->Chd,  &s->fax2, &s->gx2,  &s->alx2, &s->pfx2,
+                           &s->pbx2, &s->fay2, &s->gy2,  &s->aly2, &s->pfy2, &s->pby2, &s->bar,  &s->derr,
+                           &s->mold, &s->H,    &s->ser_tab};
+  size_t n = 0;
+  for (const fh_dbuf *d : bufs) n += d->bytes;
+  if (s->blk) n += fh_blk_bytes(*s->blk);
+  if (s->two) n += fh_ta_bytes(s->two);
+  return (long long)n;
 }
 
 const double *fh_tg_field(const fh_tg_solver *s) { return s ? s->C.as<double>() : nullptr; }

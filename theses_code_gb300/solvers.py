@@ -73,6 +73,18 @@ class HSolverBatch:
     def set_u_device(self, ptr: int):
         check(self.ctx.L.fh_h_batch_set_u(self.h, C.c_void_p(ptr)), self.ctx.h)
 
+    def restart(self, i: int, params: dict, U0: np.ndarray):
+        """Instance i starts a new solve (continuous batching): its own steps
+        count from 1 and its history starts empty while the others go on;
+        params["N"] may not exceed the instance's node count at creation."""
+        hp = HParams(**params)
+        u = np.ascontiguousarray(U0, dtype=np.float64)
+        assert u.size == hp.N + 2
+        check(self.ctx.L.fh_h_batch_restart(self.h, int(i), C.byref(hp), _hptr(u)), self.ctx.h)
+        self.params[i] = hp
+        self.sizes[i] = hp.N + 2
+        self.total = int(self.ctx.L.fh_h_batch_state_size(self.h))
+
     def get_u(self) -> list[np.ndarray]:
         out = np.empty(self.total)
         check(self.ctx.L.fh_h_batch_get_u_host(self.h, _hptr(out)), self.ctx.h)
@@ -94,6 +106,10 @@ class HSolverBatch:
 
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_h_batch_step(self.h, int(n)), self.ctx.h)
+
+    def device_bytes(self) -> int:
+        """Device memory the batch holds."""
+        return int(self.ctx.L.fh_h_batch_device_bytes(self.h))
 
     @property
     def tstep(self) -> int:
@@ -150,6 +166,10 @@ class TGSolver:
 
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_tg_step(self.h, int(n)), self.ctx.h)
+
+    def device_bytes(self) -> int:
+        """Device memory the solver holds."""
+        return int(self.ctx.L.fh_tg_device_bytes(self.h))
 
     def get_c(self) -> np.ndarray:
         out = np.empty(self.shape[0] * self.shape[1])
