@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--config", default="tg2d", choices=["tg2d", "caputo1d", "psi_batch", "ab1d", "serve"])
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=2000.0)
-    ap.add_argument("--budget-gb", type=float, default=64.0)
+    ap.add_argument("--budget-gb", type=float, default=160.0)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--dt-eps", type=float, default=0.0,
                     help="tg2d: restricted summing (the reference's dt_alg 2) with this weight cut; 0 = full history")
@@ -769,33 +769,48 @@ def run_gb300(args):
 
 def run_serve(args):
     """Poisson stream of mixed 1D/2D solves through theses_code_gb300.serve:
-    admission by history memory, cohorts of 1D requests, 2D requests on their
-    own streams (blocked history).  Reports solves/s and p50/p99 latency."""
+    admission by the device bytes each solver allocates, 1D requests in slot
+    pools that running requests' successors join, 2D requests on their own
+    streams (blocked history).  The capacity (solves/s with every request
+    present at once) is the value; the same mix then arrives as a Poisson
+    stream at 50 % and 90 % of that rate, and p50/p99 latency are reported
+    for each load, so they measure the scheduler rather than a queue."""
     import torch
     from theses_code_gb300 import serve
     from theses_code_gb300._lib import FH_TG_BLOCKED
     torch.cuda.set_device(0)
-    reqs = serve.make_mix(args.requests, rate=args.rate, seed=3, mode_2d=FH_TG_BLOCKED)
-    warm = serve.make_mix(6, rate=args.rate, seed=101, max_2d=64, steps=(100, 200), nrange=(64, 256))
     srv = serve.Server(args.budget_gb * 1e9, chunk=250, max_pool=512, max_active=16)
+    warm = serve.make_mix(6, rate=args.rate, seed=101, max_2d=64, steps=(100, 200), nrange=(64, 256))
     srv.run(warm)
     clocks = ClockSampler(0)
     clocks.start()
-    done, st = srv.run(reqs, realtime=True)
+    reqs = serve.make_mix(args.requests, rate=args.rate, seed=3, mode_2d=FH_TG_BLOCKED)
+    done, st = srv.run(reqs, realtime=False)
+    cap = st["solves_per_s"]
+    loads = {}
+    for frac in (0.5, 0.9):
+        rq = serve.make_mix(args.requests, rate=frac * cap, seed=3, mode_2d=FH_TG_BLOCKED)
+        _, sl = srv.run(rq, realtime=True)
+        loads[f"{int(frac * 100)}pct"] = {"offered_per_s": frac * cap, "solves_per_s": sl["solves_per_s"],
+                                         "p50_s": sl["p50_s"], "p99_s": sl["p99_s"],
+                                         "joined_running_pools": sl["joined_running_pools"],
+                                         "peak_device_gb": sl["peak_device_bytes"] / 1e9}
     clk = clocks.stop()
     gps = 0.0
     for r in reqs:
         pts = (r.params["N"] - 1) if r.kind == "1d" else r.params["sN"] * r.params["M"]
         gps += pts * r.steps
-    res = {"metric": "solves/s", "value": st["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+    res = {"metric": "solves/s", "value": cap, "unit": "solves/s", "n_gpus": 1,
            "steps": len(done), "warmup": len(warm), "ms_per_step": 1e3 * st["wall_s"] / max(len(done), 1),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"serve_poisson_{args.requests}req", "rate_per_s": args.rate,
+           "config": {"workload": f"serve_poisson_{args.requests}req",
                       "mix": "60% 1D (L1/psi-Caputo, N 64-2048), 40% 2D (64^2-512^2, blocked history)",
-                      "steps": [500, 5000], "budget_gb": args.budget_gb},
-           "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"]},
+                      "steps": [500, 5000], "budget_gb": args.budget_gb,
+                      "capacity_run": "every request present at t = 0"},
+           "latency": loads,
            "grid_point_steps_per_s": gps / st["wall_s"], "clocks": clk,
-           "scheduler": {k: st[k] for k in ("peak_active_solvers", "scheduler_passes", "wall_s")}}
+           "scheduler": {k: st[k] for k in ("peak_active_solvers", "scheduler_passes", "wall_s",
+                                            "joined_running_pools", "peak_device_bytes")}}
     print(json.dumps(res))
 
 

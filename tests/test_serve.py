@@ -64,6 +64,9 @@ def test_requests_join_running_pools():
     _check(reqs, done)
 
 
+SLACK = 2 << 20  # the estimates' allowance for allocation granularity
+
+
 def test_byte_estimates_bound_the_allocations():
     from theses_code_gb300 import _lib, serve, workloads
     from theses_code_gb300._lib import Context
@@ -72,14 +75,14 @@ def test_byte_estimates_bound_the_allocations():
     for caps, steps in (([64, 128, 2048], 500), ([40] * 10, 70), ([1024], 5000)):
         s = HSolverBatch(ctx, [dict(workloads.caputo_1d(c - 1)[0]) for c in caps], steps)
         got, est = s.device_bytes(), serve.pool_bytes(caps, steps)
-        assert 0.7 * est <= got <= est, (caps, steps, got, est)
+        assert 0.7 * (est - SLACK) <= got <= est, (caps, steps, got, est)
         s.close()
     for g, steps, mode in ((64, 500, _lib.FH_TG_FP64), (200, 300, _lib.FH_TG_BLOCKED), (96, 60, _lib.FH_TG_BLOCKED),
                            (128, 5000, _lib.FH_TG_FP64)):
         p, V2, C0 = workloads.convection_2d(g, g, alpha=0.7, tau=5e-4, d=0.1, seed=1)
         s = TGSolver(ctx, p, steps, mode)
         got, est = s.device_bytes(), serve.tg_bytes(g, g, steps, mode)
-        assert 0.7 * est <= got <= est, (g, steps, mode, got, est)
+        assert 0.7 * (est - SLACK) <= got <= est, (g, steps, mode, got, est)
         s.close()
     ctx.close()
 

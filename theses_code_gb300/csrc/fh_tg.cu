@@ -807,10 +807,18 @@ struct tg_fuse_args {
   int *err;
 };
 
+// Per-thread shared-memory state of the y mapping ([slot][k][thread], each
+// thread reads only its own entries): the sub-block layers it produced in
+// this launch (ycache, the first kYCache of them) and the history row of the
+// current step's y sums, prefetched by cp.async at the start of the step
+// (ypre).  The field at its y nodes stays in registers across the steps.
+static constexpr int kYCache = 5;
 // dynamic shared memory: fa, al (solve layout) and g (node layout) of both
-// directions, and the right-part / solution exchange of four lines
+// directions, the right-part / solution exchange of four lines, then
+// ycache, ypre
 static constexpr size_t kFuseSmem =
-    sizeof(float2) * (2 * 2 * kFuseLines * (size_t)kFuseSL + 2 * kFuseLines * (size_t)kFuseNL + kFuseLines * (size_t)kFuseSL);
+    sizeof(float2) * (2 * 2 * kFuseLines * (size_t)kFuseSL + 2 * kFuseLines * (size_t)kFuseNL +
+                      kFuseLines * (size_t)kFuseSL + (size_t)(kYCache + 1) * kFuseLines * kFuseThreads);
 
 // solve-layout slot of equation i (1 <= i <= 512): thread (i-1)/4, entry (i-1)%4
 __device__ __forceinline__ int tg_fslot(int i) { return ((i - 1) & 3) * kFuseSE + ((i - 1) >> 2); }
@@ -859,11 +867,12 @@ __device__ __forceinline__ bool tg_grid_wait(const unsigned *bar, unsigned targe
 // %clock64 of every phase boundary of every step, taken by warp kBarWarp,
 // read with fh_tg_stamps_read.  Empty otherwise.
 #ifdef FH_TG_STAMPS
-__device__ long long g_tg_stamps[256 * kSub * 8];
+constexpr int kTgStamps = 12;  // stamps per step
+__device__ long long g_tg_stamps[256 * kSub * kTgStamps];
 #define TG_STAMP(p)                                                                   \
   if (warp == kBarWarp) {                                                             \
     const long long c_ = clock64();                                                   \
-    if ((threadIdx.x & 31) == 0) g_tg_stamps[(blockIdx.x * kSub + s) * 8 + (p)] = c_; \
+    if ((threadIdx.x & 31) == 0) g_tg_stamps[(blockIdx.x * kSub + s) * kTgStamps + (p)] = c_; \
     __syncwarp();                                                                     \
   }
 extern "C" int fh_tg_stamps_read(long long *h) {
@@ -991,7 +1000,10 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
   float2 *fa_x = sbf, *al_x = fa_x + kFuseLines * kFuseSL;  // solve layout, [line][slot]
   float2 *fa_y = al_x + kFuseLines * kFuseSL, *al_y = fa_y + kFuseLines * kFuseSL;
   float2 *g_x = al_y + kFuseLines * kFuseSL, *g_y = g_x + kFuseLines * kFuseNL;  // node layout, [line][i-1]
-  float2 *xch = g_y + kFuseLines * kFuseNL;  // [line][slot]: -g om, then u
+  float2 *xch = g_y + kFuseLines * kFuseNL;       // [line][slot]: -g om, then u
+  float2 *ycache = xch + kFuseLines * kFuseSL;    // [layer][k][thread]
+  float2 *ypre = ycache + kYCache * kFuseLines * kFuseThreads;
+  auto ys = [&](float2 *base, int k) -> float2 & { return base[k * kFuseThreads + tid]; };
   // lines line0 .. line0 + 3 (rows j of the x sweep, columns i of the y sweep),
   // aligned to four so that a row of the CTA's columns is one 32-byte sector;
   // line 0 (a boundary) is not solved
@@ -1083,18 +1095,35 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
         for (int k = 0; k < kFuseLines; ++k) tsx[k] = fh_df_fma(w, fh_df_from_pair(d[t][k]), tsx[k]);
       }
   };
+  // the y sums read the field and the layers this thread produced from
+  // shared memory, older layers from L2, and the prefetched history row
   auto y_load = [&](int s, float2 (&r)[kFuseLines], float2 (&d)[kSub - 1][kFuseLines]) {
-    const float2 *rby = a.rb0 ? a.rb0 + (long long)s * a.rb_step + a.rb_xy : nullptr;
-#pragma unroll
-    for (int k = 0; k < kFuseLines; ++k) {
-      f[k] = ylive(k) ? __ldcg(a.Cd + yid(k)) : make_float2(0.f, 0.f);
-      r[k] = (rby && ylive(k)) ? __ldcg(rby + yid(k)) : make_float2(0.f, 0.f);
-    }
 #pragma unroll
     for (int t = 0; t < kSub - 1; ++t)
 #pragma unroll
-      for (int k = 0; k < kFuseLines; ++k)
-        d[t][k] = (t < s && ylive(k)) ? __ldcg(tiny + (long long)t * g.P + yid(k)) : make_float2(0.f, 0.f);
+      for (int k = 0; k < kFuseLines; ++k) {
+        const int c = t - a.s0;
+        d[t][k] = (t >= s || !ylive(k))     ? make_float2(0.f, 0.f)
+                  : (c >= 0 && c < kYCache) ? ys(ycache + c * kFuseLines * kFuseThreads, k)
+                                            : __ldcg(tiny + (long long)t * g.P + yid(k));
+      }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) r[k] = ys(ypre, k);
+  };
+  // history row of the step's y sums into ypre (asynchronous; zero without rows)
+  auto y_prefetch = [&](int s) {
+    const float2 *rby = a.rb0 ? a.rb0 + (long long)s * a.rb_step + a.rb_xy : nullptr;
+#pragma unroll
+    for (int k = 0; k < kFuseLines; ++k) {
+      if (rby && ylive(k)) {
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&ys(ypre, k));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(rby + yid(k)) : "memory");
+      } else {
+        ys(ypre, k) = make_float2(0.f, 0.f);
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
   auto y_sum = [&](int s, const float2 (&r)[kFuseLines], const float2 (&d)[kSub - 1][kFuseLines]) {
 #pragma unroll
@@ -1107,6 +1136,8 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
         for (int k = 0; k < kFuseLines; ++k) tsy[k] = fh_df_fma(w, fh_df_from_pair(d[t][k]), tsy[k]);
       }
   };
+#pragma unroll
+  for (int k = 0; k < kFuseLines; ++k) f[k] = ylive(k) ? __ldcg(a.Cd + yid(k)) : make_float2(0.f, 0.f);
   {
     float2 r[kFuseLines], d[kSub - 1][kFuseLines];
     x_load(a.s0, r, d);
@@ -1136,6 +1167,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
           xch[k * kFuseSL + tg_fslot(xi)] = fh_df_pair(fh_df_neg(fh_df_mul(fh_df_from_pair(g_x[k * kFuseNL + xi - 1]), om)));
         }
     }
+    y_prefetch(s);  // after the x loads: the copies run under the x solve
     __syncthreads();
     TG_STAMP(1);
     if (xl_ok(grp))
@@ -1156,11 +1188,13 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
       }
     }
     tg_grid_arrive(a.bar);
+    TG_STAMP(7);
     {  // the y history part overlaps the barrier (its layers are complete)
       float2 r[kFuseLines], d[kSub - 1][kFuseLines];
       y_load(s, r, d);
       y_sum(s, r, d);
     }
+    TG_STAMP(8);
     if (!tg_grid_wait(a.bar, ++nb * nblk, a.err)) return;
     TG_STAMP(3);
     // ---- y half step (fr_d_t_g_2d.cpp:2591-2606): the half-step field
@@ -1191,12 +1225,16 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
     TG_STAMP(5);
     {
       float2 *Dj = a.D + (long long)j * g.P;
+      const int c = s - a.s0;  // this launch's layer index (cached below kYCache)
 #pragma unroll
       for (int k = 0; k < kFuseLines; ++k)
         if (ylive(k)) {
           const float2 u = xch[yc * kFuseSL + tg_fslot(yq(k))];
+          const float2 dn = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[k])));
           a.Cd[yid(k)] = u;
-          Dj[yid(k)] = fh_df_pair(fh_df_sub(fh_df_from_pair(u), fh_df_from_pair(f[k])));
+          Dj[yid(k)] = dn;
+          f[k] = u;  // the old field of the next step
+          if (c < kYCache) ys(ycache + c * kFuseLines * kFuseThreads, k) = dn;
         }
       if (tid < 3 * kFuseLines) {  // rows 0, Ny, Ny + 1 of the four columns: C only
         const int l = tid / 3, k = tid % 3;
@@ -1208,11 +1246,13 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
     }
     if (s + 1 < a.s0 + a.ns) {
       tg_grid_arrive(a.bar);
+      TG_STAMP(9);
       {  // the x history part of the next step overlaps the barrier (layers up to j - 1 are complete)
         float2 r[kFuseLines], d[kSub - 1][kFuseLines];
         x_load(s + 1, r, d);
         x_sum(s + 1, r, d);
       }
+      TG_STAMP(10);
       if (!tg_grid_wait(a.bar, ++nb * nblk, a.err)) return;
     }
     TG_STAMP(6);

@@ -65,8 +65,12 @@ def tg_bytes(sN: int, M: int, steps: int, mode: int) -> int:
         if steps > 64:
             Ppad = -(-P // 128) * 128
             Kcap = -(-steps // 64) * 64
-            b += 8 * Ppad * Kcap + 8 * 128 * Kcap + Ppad * (Kcap // 64) + 128 * (Kcap // 64) + 8192 * Ppad
-            b += 1024 * Ppad + 8
+            b += 8 * Ppad * Kcap + 8 * 128 * Kcap + Ppad * (Kcap // 64) + 128 * (Kcap // 64) + 1024 * Ppad + 8
+            # split-K partial rows when the 64-point tiles are fewer than the
+            # SMs (at most 8 splits; 160 SMs bounds the device's 152)
+            ntiles = Ppad // 64
+            if ntiles < 160:
+                b += 8 * min(8, 160 // ntiles) * 128 * Ppad
     return int(b) + 2 * _MIB
 
 
@@ -252,8 +256,10 @@ class Server:
                 #    slot that holds one request may not hold the one before it)
                 rest = []
                 for r in waiting:
-                    pool = next((a for a in active if isinstance(a, _Pool1D) and a.fits(r) >= 0), None)
-                    if r.kind == "1d" and pool is not None:
+                    pool = None
+                    if r.kind == "1d":
+                        pool = next((a for a in active if isinstance(a, _Pool1D) and a.fits(r) >= 0), None)
+                    if pool is not None:
                         pool.place(r)
                         joined += 1
                     else:
