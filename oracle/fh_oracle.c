@@ -307,26 +307,39 @@ int fho_h_solve(const fho_h_params *p, double *U, int steps, double *hist) {
 /* --------------------------------------------------- 2D TG_solver ADI path */
 
 /* One x line (dir 0, line jj) or y line (dir 1, line ii) of TG_solver::calc_step. */
+/* D of TG_solver_::D (fr_d_t_g_2d.cpp:2787-2800): d, or with fixed_d = 0 and
+ * kform 0 lambda |v| (ka[0] / k) at the node. */
+static double tg_D(const fho_tg_params *p, const double *V2, size_t id) {
+  if (p->fixed_d) return p->d;
+  const double v = sqrt(V2[id]);
+  const double k_ = p->ka0 / p->kk;
+  return p->lambda * v * k_;
+}
+
 static void tg_line(const fho_tg_params *p, const double *V2, double *C, const double *work, int j, int dir, int line,
-                    double kcur, double kyh, const double *wk, const double *hs, double *A, double *B, double *R,
-                    double *Om, double *u) {
+                    double kcur, double kyh, const double *wk, const double *hs, const double *Nn, const double *Np,
+                    double *A, double *B, double *R, double *Om, double *u) {
   const int sN = p->sN, M = p->M, ld = sN + 2;
   const size_t P = (size_t)(sN + 2) * (M + 2);
   const double st = p->sigma / p->tau;
   const int N = dir == 0 ? sN : M;
   const double dl = dir == 0 ? p->dL : p->dLx;
+  const size_t step = dir == 0 ? 1 : (size_t)ld;  /* neighbour along the line */
   for (int i = 1; i < N; ++i) {
     const size_t id = dir == 0 ? (size_t)i + (size_t)line * ld : (size_t)line + (size_t)i * ld;
+    /* A_ and B (3242-3257): D(i-1) + D(i) and D(i+1) + D(i) */
+    const double Dm = tg_D(p, V2, id - step), Dc = tg_D(p, V2, id), Dp = tg_D(p, V2, id + step);
     if (dir == 0) {
-      A[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) + 0.5);
-      B[i] = (V2[id] / dl) * ((0.5 * (p->d + p->d) / dl) - 0.5);
+      A[i] = (V2[id] / dl) * ((0.5 * (Dm + Dc) / dl) + 0.5);
+      B[i] = (V2[id] / dl) * ((0.5 * (Dp + Dc) / dl) - 0.5);
     } else {
-      A[i] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
-      B[i] = (V2[id] / (dl * dl)) * 0.5 * (p->d + p->d);
+      A[i] = (V2[id] / (dl * dl)) * 0.5 * (Dm + Dc);
+      B[i] = (V2[id] / (dl * dl)) * 0.5 * (Dp + Dc);
     }
     R[i] = st * (kcur + 0.0) + A[i] + B[i];
     Om[i] = -st * (kcur + 0.0) * C[id];
     Om[i] += p->S * 0.5;
+    if (Nn) Om[i] += (1.0 / p->tau) * (Nn[id] - Np[id]); /* mass exchange (3330-3332) */
     double ts = 0.0;
     if (hs) /* dt_alg 3: the series value of this step */
       ts = hs[id];
@@ -682,6 +695,10 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
   const int J = p->dt_alg == 3 ? (int)p->dt_eps : 0;
   if (p->dt_alg == 3 && (J < 1 || p->beta != 1.0)) return 2;
   if (p->dt_alg == 4 && p->beta != 1.0) return 2;
+  /* mass exchange: N starts at 0 (TG_solver::initial) */
+  double *Nn = p->massN ? (double *)calloc(P, sizeof(double)) : NULL;
+  double *Np = p->massN ? (double *)calloc(P, sizeof(double)) : NULL;
+  if (p->massN && (!Nn || !Np)) return 1;
   /* dt_alg 4: per point the approximations of the x and y sums (Happ1 with
    * offsets (1.5, 0.5), Happ2 with (2, 1); fr_d_t_g_2d.cpp:3444-3462) */
   ta_set *tax = NULL, *tay = NULL;
@@ -728,6 +745,14 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
      * ii = 1..sN-1 (2634-2648).  Lines are independent, so they run in parallel. */
     for (int dir = 0; dir < 2; ++dir) {
       const int nlines = dir == 0 ? M : sN;
+      if (Nn) /* N1 before each half step (2503-2521): nodes i <= sN, j <= M */
+        for (int jj = 0; jj <= M; ++jj)
+          for (int ii = 0; ii <= sN; ++ii) {
+            const size_t id = (size_t)ii + (size_t)jj * (sN + 2);
+            Np[id] = Nn[id];
+            Nn[id] = (1.0 / (2.0 + p->tau * p->massN_a * p->massN_b)) *
+                     (2 * Np[id] + p->tau * p->sigma * p->massN_b * C[id]);
+          }
 #pragma omp parallel
       {
         double *A = (double *)malloc(sizeof(double) * nmax), *B = (double *)malloc(sizeof(double) * nmax);
@@ -736,7 +761,7 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
 #pragma omp for schedule(static)
         for (int line = 1; line < nlines; ++line)
           tg_line(p, V2, C, work, j, dir, line, dir == 0 ? kx : ky, kyh, dir == 0 ? wx : wy, dir == 0 ? hsx : hsy,
-                  A, B, R, Om, u);
+                  Nn, Np, A, B, R, Om, u);
         free(A); free(B); free(R); free(Om); free(u);
       }
     }
@@ -749,7 +774,7 @@ int fho_tg_solve(const fho_tg_params *p, const double *V2, double *C, int steps,
       ta_free(&tax[id]);
       ta_free(&tay[id]);
     }
-  free(tax); free(tay); free(F4);
+  free(tax); free(tay); free(F4); free(Nn); free(Np);
   return 0;
 }
 

@@ -99,6 +99,11 @@ typedef struct {
                          4 two-series approximation (psi = t)               */
   double dt_eps;      /* dt_alg 2: the sums stop at the first |weight| < eps;
                          dt_alg 3 (psi = t): number of series terms          */
+  int massN;          /* mass exchange with a non-soluble phase (N1 stage)   */
+  double massN_a, massN_b;
+  int fixed_d;        /* 1: D = d; 0: D = lambda |v| ka0 / kk per node
+                         (TG_solver_<func,0,0>, fr_d_t_g_2d.cpp:2787-2800)   */
+  double lambda, ka0, kk;
 } fho_tg_params;
 
 /* Runs `steps` TG_solver::calc_step calls (fr_d_t_g_2d.cpp:2552-2718) with

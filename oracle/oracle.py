@@ -34,7 +34,8 @@ class TGParams(C.Structure):
     _fields_ = [("sN", C.c_int), ("M", C.c_int), ("tau", C.c_double), ("alpha", C.c_double),
                 ("beta", C.c_double), ("sigma", C.c_double), ("d", C.c_double), ("C1", C.c_double),
                 ("S", C.c_double), ("dL", C.c_double), ("dLx", C.c_double), ("dt_alg", C.c_int),
-                ("dt_eps", C.c_double)]
+                ("dt_eps", C.c_double), ("massN", C.c_int), ("massN_a", C.c_double), ("massN_b", C.c_double),
+                ("fixed_d", C.c_int), ("lambda_", C.c_double), ("ka0", C.c_double), ("kk", C.c_double)]
 
 
 def build() -> str:
@@ -135,7 +136,16 @@ def h_solve(params: dict, U0: np.ndarray, steps: int):
 
 
 def tg_solve(params: dict, V2: np.ndarray, C0: np.ndarray, steps: int):
-    p = TGParams(**params)
+    """params: the TG_solver fields; optional massN (with massN_a, massN_b,
+    default 0.1 each as the reference's globals) and fixed_d = 0 (with lambda,
+    ka0, kk: D = lambda |v| ka0 / kk per node)."""
+    q = dict(params)
+    q.setdefault("fixed_d", 1)
+    q.setdefault("massN_a", 0.1)
+    q.setdefault("massN_b", 0.1)
+    if "lambda" in q:
+        q["lambda_"] = q.pop("lambda")
+    p = TGParams(**q)
     P = (p.sN + 2) * (p.M + 2)
     V2 = np.ascontiguousarray(V2, dtype=np.float64).reshape(-1)
     Cf = np.ascontiguousarray(C0, dtype=np.float64).reshape(-1).copy()

@@ -111,6 +111,15 @@ def main():
         a4 = [sN, M, 5e-3, alpha, 0.1, 0.3, 0.05, steps, 4, 1e-8]
         two[f"{alpha}_{steps}"] = {"alpha": alpha, "steps": steps, "C": parse(run("tg", a4, list(V2) + list(C0)))["c"][0]}
     dump("tg_adi_two_series.json", two)
+    # TG_solver_ variants: the mass-exchange stage N1 (massN) and the
+    # velocity-dependent diffusion coefficient (TG_solver_<0,0,0>), 40 steps
+    var = {}
+    for key, extra in (("massN", [0, 0.0, 1, 0.5, 2.0]), ("variable_d", [0, 0.0, 0, 0.1, 0.1, 0]),
+                       ("variable_d_massN", [0, 0.0, 1, 0.3, 0.7, 0])):
+        r = parse(run("tg", args[:7] + [40] + extra, list(V2) + list(C0)))
+        var[key] = {"steps": 40, "massN": extra[2], "massN_a": extra[3], "massN_b": extra[4],
+                    "fixed_d": extra[5] if len(extra) > 5 else 1, "dcoef": r["dcoef"][0], "C": r["c"][0]}
+    dump("tg_adi_variants.json", var)
     # Atangana-Baleanu: Mittag-Leffler values, lag weights, solve_and_check error
     ml = []
     for (a, b, z) in [(0.5, 1.0, -0.7), (0.8, 1.0, -1.2), (0.6, 2.0, -0.9), (0.9, 5.0, -0.5),

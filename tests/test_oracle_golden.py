@@ -115,6 +115,24 @@ def test_tg_adi_two_series_matches_reference(key):
     assert 1e-9 < relmax(full, r["C"]) < 1e-5
 
 
+@pytest.mark.parametrize("key", ["massN", "variable_d", "variable_d_massN"])
+def test_tg_adi_variants_match_reference(key):
+    """TG_solver_ with the mass-exchange stage N1 (fr_d_t_g_2d.cpp:2503-2521,
+    3330-3332) and/or the velocity-dependent diffusion coefficient of
+    TG_solver_<0,0,0> (2787-2800), bit for bit against the reference runs."""
+    g = load("tg_adi_restricted.json")  # the same problem
+    r = load("tg_adi_variants.json")[key]
+    lam, ka0, kk = r["dcoef"]
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+             C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"], dt_alg=0, dt_eps=0.0, massN=r["massN"],
+             massN_a=r["massN_a"], massN_b=r["massN_b"], fixed_d=r["fixed_d"], ka0=ka0, kk=kk)
+    p["lambda"] = lam
+    C, _ = O.tg_solve(p, np.array(g["V2"]), np.array(g["C0"]), r["steps"])
+    assert relmax(C, r["C"]) <= 1e-15
+    full = load("tg_adi_40.json")["C"]
+    assert relmax(full, r["C"]) > 0.01  # the variant matters
+
+
 def test_two_series_bookkeeping_counts():
     """The approximation sets stay small: after 2000 layers tens of long and
     short approximations per point and direction, growing slower than the
