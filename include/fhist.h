@@ -299,6 +299,21 @@ int fh_tg_set_series(fh_tg_solver *s, int nterms);
  * at the same time; enable = 0 restores the full history.  Only before the
  * first step of a solve. */
 int fh_tg_set_two_series(fh_tg_solver *s, int enable);
+/* Mass exchange with a non-soluble phase, TG_solver with massN != 0
+ * (TG_solver::N1 fr_d_t_g_2d.cpp:2503-2521 before each half step, the right
+ * parts' (1/tau)(N - prevN) 3330-3332): per node
+ * N' = (2 N + tau sigma b C) / (2 + tau a b) with a = massN_a, b = massN_b (the
+ * reference's globals, 0.1 by default); N starts at 0 with every
+ * fh_tg_set_state.  FH_TG_FP64 or FH_TG_DF64; enable = 0 turns it off.  Only
+ * before the first step of a solve. */
+int fh_tg_set_mass_exchange(fh_tg_solver *s, int enable, double massN_a, double massN_b);
+/* Diffusion coefficient: fixed_d = 1 keeps the constant d of fh_tg_params
+ * (TG_solver_<func,1,kform>); fixed_d = 0 uses D = lambda |v| (ka0 / k) per
+ * node (TG_solver_<func,0,0>::D, fr_d_t_g_2d.cpp:2787-2800, the reference's
+ * lambda = l, ka0 = ka[0], k = its averaged filtration coefficient) in the
+ * coefficients A_, B (3242-3257).  Any mode.  Only before the first step of a
+ * solve. */
+int fh_tg_set_diffusion(fh_tg_solver *s, int fixed_d, double lambda, double ka0, double k);
 /* The host bookkeeping of fh_tg_set_two_series for inspection (no device
  * work, no reference counterpart): per step j = 1 .. max_steps - 1 and
  * direction d (0: x sums, 1: y sums) spans[4 (2 j + d) + 0..2] = {first item,

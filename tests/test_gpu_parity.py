@@ -731,3 +731,66 @@ def test_tg_two_series_limits(ctx):
     with pytest.raises(FhError):
         q.set_two_series(True)
     q.close()
+
+
+@pytest.mark.parametrize("mode_name", ["FH_TG_FP64", "FH_TG_DF64"])
+@pytest.mark.parametrize("key", ["massN", "variable_d", "variable_d_massN"])
+def test_tg_variants_vs_reference(ctx, mode_name, key):
+    """TG_solver_ with the mass-exchange stage and/or the velocity-dependent
+    diffusion coefficient (TG_solver_<0,0,0>) against the reference's own
+    runs of the 12 x 10 problem (40 steps)."""
+    from theses_code_gb300 import _lib
+    from theses_code_gb300.solvers import TGSolver
+    g = json.load(open(os.path.join(G, "tg_adi_restricted.json")))
+    r = json.load(open(os.path.join(G, "tg_adi_variants.json")))[key]
+    p = dict(sN=g["sN"], M=g["M"], tau=g["tau"], alpha=g["alpha"], beta=1.0, sigma=g["sigma"], d=g["d"],
+             C1=g["C1"], S=g["S"], dL=g["dL"], dLx=g["dLx"])
+    s = TGSolver(ctx, p, r["steps"] + 1, getattr(_lib, mode_name))
+    if r["massN"]:
+        s.set_mass_exchange(True, r["massN_a"], r["massN_b"])
+    if not r["fixed_d"]:
+        s.set_diffusion(False, *r["dcoef"])
+    s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+    s.calc_step(r["steps"])
+    assert relmax(s.get_c(), r["C"]) <= TOL_SOLVER
+    # a second solve from the same state (N back to 0)
+    s.set_state(np.array(g["V2"]), np.array(g["C0"]))
+    for n in (7, 33):
+        s.calc_step(n)
+    assert relmax(s.get_c(), r["C"]) <= TOL_SOLVER
+    s.close()
+
+
+def test_tg_variants_larger_grid_and_blocked(ctx):
+    """Both variants together on a 64 x 48 grid (150 steps) against the
+    oracle; the velocity-dependent coefficient in the blocked mode at the
+    mixed-precision bound; the mass exchange refused there."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300._lib import FH_TG_BLOCKED, FhError
+    from theses_code_gb300.solvers import TGSolver
+    p, V2, C0 = workloads.convection_2d(64, 48, alpha=0.7, tau=5e-4, d=0.1, seed=6, C1=0.2, S=0.05)
+    lam, ka0, kk = 5.0, 1.005e-3, 2.0 * math.sqrt(5.0) / (math.pi * 2.5)
+    q = dict(p, massN=1, massN_a=0.4, massN_b=1.5, fixed_d=0, ka0=ka0, kk=kk)
+    q["lambda"] = lam
+    steps = 150
+    ref, _ = O.tg_solve(q, V2, C0, steps)
+    base, _ = O.tg_solve(p, V2, C0, steps)
+    assert relmax(ref, base) > 1e-3
+    s = TGSolver(ctx, p, steps)
+    s.set_mass_exchange(True, 0.4, 1.5)
+    s.set_diffusion(False, lam, ka0, kk)
+    s.set_state(V2, C0)
+    s.calc_step(steps)
+    assert relmax(s.get_c(), ref) <= TOL_SOLVER
+    s.close()
+    qd = dict(p, fixed_d=0, ka0=ka0, kk=kk)
+    qd["lambda"] = lam
+    ref_d, _ = O.tg_solve(qd, V2, C0, steps)
+    b = TGSolver(ctx, p, steps, FH_TG_BLOCKED)
+    with pytest.raises(FhError):
+        b.set_mass_exchange(True, 0.4, 1.5)
+    b.set_diffusion(False, lam, ka0, kk)
+    b.set_state(V2, C0)
+    b.calc_step(steps)
+    assert relmax(b.get_c(), ref_d) <= 1e-9
+    b.close()

@@ -52,7 +52,19 @@ struct fh_tg_dev {
   long long P;
   double tau, alpha, beta, Da, st, d, C1, S, dL, dLx;
   double hcut;  // restricted summing: history weights below hcut are 0 (0: full history)
+  // diffusion coefficient: d (fixed_d), else lambda |v| (ka0 / kk) per node
+  // (TG_solver_<func,0,0>::D, fr_d_t_g_2d.cpp:2787-2800)
+  int fixed_d = 1;
+  double lam = 0.0, ka0 = 0.0, kk = 1.0;
 };
+
+// D at a node of |v|^2 = v2.
+__device__ __forceinline__ double tg_D(const fh_tg_dev &g, double v2) {
+  if (g.fixed_d) return g.d;
+  const double v = sqrt(v2);
+  const double k_ = g.ka0 / g.kk;
+  return g.lam * v * k_;
+}
 
 // History weight w with restricted summing (dt_alg 2, fr_d_t_g_2d.cpp:3356-3380):
 // the reference's sums run from the newest layer pair back and stop at the
@@ -107,6 +119,11 @@ struct fh_tg_solver {
   // slots; the history store keeps only the newest layer pair
   fh_ta *two = nullptr;
   bool one_layer() const { return ser_J || two; }
+  // mass exchange (TG_solver::N1): N per node and the right-part term dN of
+  // the current half step; c1 = 1/(2 + tau a b), tsb = tau sigma b
+  bool massN = false;
+  double mass_c1 = 0.0, mass_tsb = 0.0;
+  fh_dbuf Nn, dN;
   ~fh_tg_solver() {
     if (two) fh_ta_delete(two);
     if (blk) fh_blk_delete(blk);
@@ -139,6 +156,26 @@ __global__ void k_tg_weights(fh_tg_dev g, int j, int kstart, double *__restrict_
   }
 }
 
+// Mass exchange with the non-soluble phase, TG_solver::N1 (fr_d_t_g_2d.cpp:
+// 2503-2521) before each half step over the nodes i <= sN, j <= M:
+// N' = c1 (2 N + tsb C) with c1 = 1/(2 + tau a b), tsb = tau sigma b; the
+// half step's right parts add dN = (1/tau) (N' - N) (3330-3332).  Before the
+// y half step C is the half-step field: Ch on the x lines (rows 1..M-1), C on
+// rows 0 and M, which the x half step leaves alone.
+__global__ void k_tg_n1(fh_tg_dev g, int half, const double *__restrict__ C, const double *__restrict__ Ch,
+                        double c1, double tsb, double *__restrict__ Nn, double *__restrict__ dN) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nn = (long long)(g.sN + 1) * (g.M + 1);
+  if (t >= nn) return;
+  const int i = (int)(t % (g.sN + 1)), j = (int)(t / (g.sN + 1));
+  const long long id = i + (long long)j * g.ld;
+  const double c = (half && j >= 1 && j < g.M) ? Ch[id] : C[id];
+  const double prev = Nn[id];
+  const double nw = c1 * (2 * prev + tsb * c);
+  Nn[id] = nw;
+  dN[id] = (1.0 / g.tau) * (nw - prev);
+}
+
 // Serial factorization of every line (one thread per line): Al[i+1], the
 // pivot factor g_i and the forward-map slope fa_i = g_i A_i, stored at the
 // point of equation i.  dir 0: x lines, dir 1: y lines.  A, B, R in the
@@ -158,13 +195,15 @@ __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2,
   for (int i = 1; i < N; ++i) {
     const long long id = base + i * stride;
     const double v2 = V2[id];
+    // A_ and B (fr_d_t_g_2d.cpp:3242-3257): D(i-1) + D(i) and D(i+1) + D(i)
+    const double Dc = tg_D(g, v2), Dm = tg_D(g, V2[id - stride]), Dp = tg_D(g, V2[id + stride]);
     double A, B;
     if (dir == 0) {
-      A = (v2 / dl) * ((0.5 * (g.d + g.d) / dl) + 0.5);
-      B = (v2 / dl) * ((0.5 * (g.d + g.d) / dl) - 0.5);
+      A = (v2 / dl) * ((0.5 * (Dm + Dc) / dl) + 0.5);
+      B = (v2 / dl) * ((0.5 * (Dp + Dc) / dl) - 0.5);
     } else {
-      A = (v2 / (dl * dl)) * 0.5 * (g.d + g.d);
-      B = A;
+      A = (v2 / (dl * dl)) * 0.5 * (Dm + Dc);
+      B = (v2 / (dl * dl)) * 0.5 * (Dp + Dc);
     }
     const double R = g.st * (kcur + 0.0) + A + B;
     const double den = R - A * alv;
@@ -278,7 +317,8 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
                                                         const double *__restrict__ pfx,
                                                         const double *__restrict__ pbx,
                                                         const double *__restrict__ cw,
-                                                        const float2 *__restrict__ far) {
+                                                        const float2 *__restrict__ far,
+                                                        const double *__restrict__ dN) {
   extern __shared__ double sbuf[];
   const int warp = threadIdx.x >> 5;
   const int line0 = 1 + blockIdx.x * kXLines;
@@ -320,6 +360,7 @@ __global__ void __launch_bounds__(kXThreads) k_tg_xsweep(fh_tg_dev g, double *C,
         if (i < N) {
           double om = kst * c[e];
           om += S2;
+          if (dN) om += dN[base + i];  // mass exchange
           om += st * ts[e];
           fa[fh_sk(i)] = a[e];
           fb[fh_sk(i)] = -gi[e] * om;
@@ -366,7 +407,8 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
                                                         const double *__restrict__ pfy,
                                                         const double *__restrict__ pby,
                                                         const double *__restrict__ cw,
-                                                        const float2 *__restrict__ far, int dfstore) {
+                                                        const float2 *__restrict__ far, int dfstore,
+                                                        const double *__restrict__ dN) {
   extern __shared__ double sbuf[];
   const int warp = threadIdx.x >> 5;
   const int N = g.M;
@@ -412,6 +454,7 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
         t += (kyh + 0.0) * (f[e] - c[e]);  // old[size-2] - old[size-1] (fr_d_t_g_2d.cpp:3478-3481)
         double om = kst * c[e];
         om += S2;
+        if (dN) om += dN[line + (long long)q * g.ld];  // mass exchange
         om += st * t;
         fa[fh_sk(q)] = a[e];
         fb[fh_sk(q)] = -gi[e] * om;
@@ -1564,17 +1607,27 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
     fary = far + s->ldfar;
   }
   fh_prof_mark(ctx, FH_PROF_SWEEP, false);
+  auto n1 = [&](int half) {
+    const long long nn = (long long)(g.sN + 1) * (g.M + 1);
+    k_tg_n1<<<(unsigned)fh_ceil_div(nn, 256), 256, 0, ctx->stream>>>(g, half, s->C.as<double>(), s->Ch.as<double>(),
+                                                                    s->mass_c1, s->mass_tsb, s->Nn.as<double>(),
+                                                                    s->dN.as<double>());
+    return fh_after_launch(ctx, "k_tg_n1");
+  };
+  const double *dNp = s->massN ? s->dN.as<double>() : nullptr;
+  if (s->massN && (rc = n1(0))) return rc;
   const size_t smx = sizeof(double) * kXLines * 5 * (size_t)tg_line_stride(g.sN);
   k_tg_xsweep<<<(unsigned)fh_ceil_div(g.M - 1, kXLines), kXThreads, smx, ctx->stream>>>(
       g, s->C.as<double>(), s->Ch.as<double>(), s->part.as<double>(), g.P, splits, s->fax.as<double>(),
-      s->gx.as<double>(), s->alx.as<double>(), s->pfx.as<double>(), s->pbx.as<double>(), cwj, farx);
+      s->gx.as<double>(), s->alx.as<double>(), s->pfx.as<double>(), s->pbx.as<double>(), cwj, farx, dNp);
   if ((rc = fh_after_launch(ctx, "k_tg_xsweep"))) return rc;
+  if (s->massN && (rc = n1(1))) return rc;
   const size_t smy = sizeof(double) * 4 * 6 * (size_t)tg_line_stride(g.M);
   k_tg_ysweep<<<(unsigned)fh_ceil_div(g.sN - 1, 4), kYThreads, smy, ctx->stream>>>(
       g, s->C.as<double>(), s->Ch.as<double>(), s->D.as<double>() + (s->one_layer() ? 0LL : (long long)j * g.P),
       s->part.as<double>(), g.P,
       splits, s->fay.as<double>(), s->gy.as<double>(), s->aly.as<double>(), s->pfy.as<double>(),
-      s->pby.as<double>(), cwj, fary, s->df ? 1 : 0);
+      s->pby.as<double>(), cwj, fary, s->df ? 1 : 0, dNp);
   fh_prof_mark(ctx, FH_PROF_SWEEP, true);
   if ((rc = fh_after_launch(ctx, "k_tg_ysweep"))) return rc;
   s->tstep++;
@@ -1875,6 +1928,47 @@ int fh_tg_set_two_series(fh_tg_solver *s, int enable) {
   return FH_OK;
 }
 
+int fh_tg_set_mass_exchange(fh_tg_solver *s, int enable, double massN_a, double massN_b) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_mass_exchange: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_mass_exchange: only before the first step of a solve");
+  FH_REQUIRE(ctx, !enable || s->mode != FH_TG_BLOCKED, FH_EINVAL,
+             "fh_tg_set_mass_exchange: the FP64 or DF64 mode only");
+  FH_REQUIRE(ctx, !enable || (std::isfinite(massN_a) && std::isfinite(massN_b) &&
+                              2.0 + s->p.tau * massN_a * massN_b != 0.0),
+             FH_EINVAL, "fh_tg_set_mass_exchange: a = %g, b = %g", massN_a, massN_b);
+  int rc;
+  if (enable && !s->Nn.p) {
+    if ((rc = fh_alloc(ctx, s->Nn, sizeof(double) * (size_t)s->dv.P)) ||
+        (rc = fh_alloc(ctx, s->dN, sizeof(double) * (size_t)s->dv.P)))
+      return rc;
+  }
+  if (!enable) {
+    s->Nn.release();
+    s->dN.release();
+  }
+  s->massN = enable != 0;
+  // the reference's operand order: 1/(2 + (tau a) b) and (tau sigma) b
+  s->mass_c1 = 1.0 / (2.0 + s->p.tau * massN_a * massN_b);
+  s->mass_tsb = s->p.tau * s->p.sigma * massN_b;
+  s->graph.reset();
+  return FH_OK;
+}
+
+int fh_tg_set_diffusion(fh_tg_solver *s, int fixed_d, double lambda, double ka0, double k) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_diffusion: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, s->tstep == 0, FH_EINVAL, "fh_tg_set_diffusion: only before the first step of a solve");
+  FH_REQUIRE(ctx, fixed_d || (std::isfinite(lambda) && std::isfinite(ka0) && std::isfinite(k) && k != 0.0),
+             FH_EINVAL, "fh_tg_set_diffusion: lambda = %g, ka0 = %g, k = %g", lambda, ka0, k);
+  s->dv.fixed_d = fixed_d ? 1 : 0;
+  s->dv.lam = lambda;
+  s->dv.ka0 = ka0;
+  s->dv.kk = fixed_d ? 1.0 : k;
+  s->graph.reset();  // the factor tables are rebuilt at the first step of a solve
+  return FH_OK;
+}
+
 // Zero series accumulators at the start of a solve.
 static int tg_series_reset(fh_tg_solver *s) {
   if (!s->ser_J) return FH_OK;
@@ -1895,6 +1989,7 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
   if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (s->massN) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->Nn.p, 0, s->Nn.bytes, ctx->stream));  // N starts at 0
   if (int rc = tg_series_reset(s)) return rc;
   s->tstep = 0;
   s->j0 = 0;
@@ -1915,6 +2010,7 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
   if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (s->massN) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->Nn.p, 0, s->Nn.bytes, ctx->stream));  // N starts at 0
   if (int rc = tg_series_reset(s)) return rc;
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   s->tstep = 0;
@@ -1971,7 +2067,7 @@ long long fh_tg_device_bytes(const fh_tg_solver *s) {
                            &s->gx,   &s->fax,  &s->pfx,  &s->pbx,  &s->aly,  &s->gy,   &s->fay,  &s->pfy,
                            &s->pby,  &s->far,  &s->Cd,   &s->Chd,  &s->fax2, &s->gx2,  &s->alx2, &s->pfx2,
                            &s->pbx2, &s->fay2, &s->gy2,  &s->aly2, &s->pfy2, &s->pby2, &s->bar,  &s->derr,
-                           &s->mold, &s->H,    &s->ser_tab};
+                           &s->mold, &s->H,    &s->ser_tab, &s->Nn,   &s->dN};
   size_t n = 0;
   for (const fh_dbuf *d : bufs) n += d->bytes;
   if (s->blk) n += fh_blk_bytes(*s->blk);

@@ -158,6 +158,17 @@ class TGSolver:
         stored layers; 0 = full history."""
         check(self.ctx.L.fh_tg_set_series(self.h, int(nterms)), self.ctx.h)
 
+    def set_mass_exchange(self, enable: bool = True, massN_a: float = 0.1, massN_b: float = 0.1):
+        """Mass exchange with a non-soluble phase (the reference's massN, with
+        its globals massN_a, massN_b)."""
+        check(self.ctx.L.fh_tg_set_mass_exchange(self.h, int(bool(enable)), float(massN_a), float(massN_b)),
+              self.ctx.h)
+
+    def set_diffusion(self, fixed_d: bool, lam: float = 0.0, ka0: float = 0.0, k: float = 1.0):
+        """fixed_d False: D = lam |v| (ka0 / k) per node (TG_solver_<func,0,0>)."""
+        check(self.ctx.L.fh_tg_set_diffusion(self.h, int(bool(fixed_d)), float(lam), float(ka0), float(k)),
+              self.ctx.h)
+
     def set_two_series(self, enable: bool = True):
         """Two-series approximation of the history sums (the reference's
         dt_alg 4, psi = t): per node long and short series absorb each new
