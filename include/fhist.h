@@ -330,6 +330,9 @@ int fh_tg_two_series_plan(double alpha, int max_steps, int *nslots, double *dter
 /* TG_solver::calc_step repeated nsteps times. */
 int fh_tg_step(fh_tg_solver *s, int nsteps);
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host);
+/* The non-soluble phase N ((sN+2)*(M+2) values, the reference's b_N) with the
+ * mass exchange on; synchronises the stream. */
+int fh_tg_get_n_host(fh_tg_solver *s, double *N_host);
 /* Device pointer to the current field ((sN+2)*(M+2) doubles, owned by the solver). */
 /* Device bytes the solver holds (history, tables, work buffers); -1 for
  * null.  No reference counterpart (serving admission). */

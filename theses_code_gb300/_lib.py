@@ -82,6 +82,7 @@ _SIGS = {
     "fh_tg_set_series": (_i, [_vp, _i]),
     "fh_tg_set_two_series": (_i, [_vp, _i]),
     "fh_tg_set_mass_exchange": (_i, [_vp, _i, _d, _d]),
+    "fh_tg_get_n_host": (_i, [_vp, _dp]),
     "fh_tg_set_diffusion": (_i, [_vp, _i, _d, _d, _d]),
     "fh_tg_two_series_plan": (_i, [_d, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fh_tg_get_c_host": (_i, [_vp, _dp]),

@@ -2046,6 +2046,17 @@ int fh_tg_step(fh_tg_solver *s, int nsteps) {
   return tg_publish(s);
 }
 
+int fh_tg_get_n_host(fh_tg_solver *s, double *N_host) {
+  FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_get_n_host: null solver");
+  fh_ctx *ctx = s->ctx;
+  FH_REQUIRE(ctx, N_host, FH_EINVAL, "fh_tg_get_n_host: null pointer");
+  FH_REQUIRE(ctx, s->massN, FH_EINVAL, "fh_tg_get_n_host: the mass exchange is off");
+  const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
+  FH_CUDA_TRY(ctx, cudaMemcpyAsync(N_host, s->Nn.p, n, cudaMemcpyDeviceToHost, ctx->stream));
+  FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return FH_OK;
+}
+
 int fh_tg_get_c_host(fh_tg_solver *s, double *C_host) {
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_get_c_host: null solver");
   fh_ctx *ctx = s->ctx;

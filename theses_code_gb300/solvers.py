@@ -182,6 +182,12 @@ class TGSolver:
         """Device memory the solver holds."""
         return int(self.ctx.L.fh_tg_device_bytes(self.h))
 
+    def get_n(self) -> np.ndarray:
+        """The non-soluble phase N (mass exchange on)."""
+        out = np.empty(self.shape[0] * self.shape[1])
+        check(self.ctx.L.fh_tg_get_n_host(self.h, _hptr(out)), self.ctx.h)
+        return out
+
     def get_c(self) -> np.ndarray:
         out = np.empty(self.shape[0] * self.shape[1])
         check(self.ctx.L.fh_tg_get_c_host(self.h, _hptr(out)), self.ctx.h)
