@@ -40,7 +40,7 @@ def test_solve_writes_reference_logs(tmp_path):
         va, vb = float(f[3]), float(f[7])
         assert va == pytest.approx(wa[k + 1][sN // 4 + (M // 2) * ld], rel=1e-5, abs=1e-12)
         assert vb == pytest.approx(wb[k + 1][sN // 4 + (M // 2) * ld], rel=1e-5, abs=1e-12)
-        assert "diffs(avgsq,maxabs,global" in line and len(f) == 15
+        assert "diffs(avgsq,maxabs,global" in line and len(f) == 16
     # log1: sN + 1 lines per save time; C at M/4, M/2, 3M/4 of each solver (+ N of each)
     lines1 = l1.read_text().splitlines()
     kss = [k for k, s_ in enumerate(saves) if s_]

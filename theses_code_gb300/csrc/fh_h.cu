@@ -1589,6 +1589,9 @@ int fh_h_batch_set_mode(fh_h_batch *b, int mode) {
     if ((rc = fh_alloc(ctx, b->D, sizeof(double) * (size_t)b->Ptot * (size_t)b->max_steps))) return rc;
   }
   b->mode = mode;
+  // the blocked mode's bound is 1e-9: Al by the parallel Moebius scan (within
+  // ~1e-10), not by the serial reference-order chain the 1e-12 modes need
+  b->serial_al = mode != FH_H_BLOCKED;
   b->graph.reset();
   return FH_OK;
 }
