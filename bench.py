@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-grid", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side-configs", action="store_true",
+                    help="tg2d: skip the one-solve runs of configs 1, 3 and 4 reported under side_configs")
     ap.add_argument("--config", default="tg2d", choices=["tg2d", "caputo1d", "psi_batch", "ab1d", "serve"])
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=2000.0)
@@ -759,12 +761,51 @@ def run_gb300(args):
             result["rel_err_max_over_output_steps"] = cmp[args.mode]["rel_err_per_output_step"]["max"]
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args) if args.config == "tg2d" else wl.cpu_baseline()
+    if rank == 0 and args.config == "tg2d" and not args.no_side_configs:
+        result["side_configs"] = side_configs(args, dev)
     if rank == 0:
         print(json.dumps(result))
     ctx.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def side_configs(args, dev):
+    """One device-resident solve of each other benchmark configuration with
+    its default mode and step count (config 1: 1000 steps FP64; config 3: the
+    full 5000 steps, blocked; config 4: 20000 steps, blocked), timed with CUDA
+    events on the solver's stream.  Config 3's single solve includes its graph
+    capture (no warm-up solve: it alone takes ~9 s)."""
+    import copy
+
+    import torch
+    from theses_code_gb300._lib import Context
+    out = {}
+    for key, cfgname, mode, steps, warm in (("cfg1_caputo1d", "caputo1d", "fp64", 2000, 1),
+                                            ("cfg3_psi_batch", "psi_batch", "blocked", 5000, 0),
+                                            ("cfg4_ab1d", "ab1d", "blocked", 2000, 1)):
+        a2 = copy.copy(args)
+        a2.config, a2.mode, a2.solve_steps = cfgname, mode, steps
+        ctx = Context(dev)
+        try:
+            w = make_workload(ctx, a2, dev, 0)
+            for _ in range(warm):
+                w.solve_device()
+            ctx.sync()
+            st = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            w.solve_device()
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            out[key] = {"value": w.gps / (ms / 1e3), "unit": METRIC, "ms_per_solve": ms, "mode": mode,
+                        "workload": w.config.get("workload"), "warmup_solves": warm}
+        finally:
+            ctx.close()
+    return out
 
 
 def run_serve(args):

@@ -106,6 +106,20 @@ int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int 
 
 /* Reference Sum-kernel form on stored layers (fr_ocl_call_sum,
  * irrigation_fractional.cpp:1828-1896): S[p] = sum_{t<K} w[t]*(H[(t+1)ldh+p] - H[t ldh+p]). */
+/* Series accumulators of the irrigation model (sum_alg 2, time_summing
+ * irrigation_fractional.cpp:4150-4164; the reference's CUDA/OpenCL Sum kernels
+ * 1224-1561 with sum_alg 2): per point p, for n < J,
+ *   H[n*ldh + p] += c[n] * Dn[p]                      (Htmp update)
+ * then S[p] = (sum_n e[n] * H[n*ldh + p]) / tau     (_kb_row2_fixed_coefs / tau[tstep])
+ * in the reference's operation order.  The caller supplies the step's
+ * coefficients (host arrays of J values): c[n] = g(T)^(n+1) row2_precalc[n]
+ * (zero beyond the precomputed row), e[n] the running factor of
+ * _kb_row2_fixed_coefs (e[0] = g(T_{j+1})^-alpha, e[n] = e[n-1] * -(-alpha - n
+ * + 1) / (n g(T_{j+1}))), tau = tau[tstep]; Dn = the newest layer difference.
+ * J <= FH_SERIES_MAX_TERMS.  H is the caller's J x ldh accumulator array. */
+#define FH_SERIES_MAX_TERMS 256
+int fh_series_sum(fh_ctx *ctx, int J, long long P, const double *c_host, const double *e_host, double tau,
+                  const double *Dn, double *H, long long ldh, double *S);
 int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H,
                           long long ldh, double *S);
 

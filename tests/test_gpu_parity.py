@@ -794,3 +794,37 @@ def test_tg_variants_larger_grid_and_blocked(ctx):
     b.calc_step(steps)
     assert relmax(b.get_c(), ref_d) <= 1e-9
     b.close()
+
+
+@pytest.mark.parametrize("J,P,ldh", [(16, 1000, 1000), (1, 7, 8), (256, 3001, 3072)])
+def test_series_sum(ctx, torch_mod, J, P, ldh):
+    """Series accumulators of the irrigation model (sum_alg 2): the update and
+    the evaluation in the reference's operation order, bit for bit against
+    the same sequence in numpy, over three steps."""
+    torch = torch_mod
+    import ctypes as C
+    from theses_code_gb300._lib import FhError
+    rng = np.random.default_rng(J)
+    H = rng.normal(size=(J, ldh))
+    Hd = dev(torch, H)
+    S = torch.zeros(P, dtype=torch.float64, device="cuda")
+    Href = H.copy()
+    for step in range(3):
+        c = rng.normal(size=J) * 0.1
+        e = rng.normal(size=J)
+        tau = 1e-3 * (1 + step)
+        d = rng.normal(size=P)
+        dd = dev(torch, d)
+        ctx.call("fh_series_sum", J, P, c.ctypes.data_as(C.c_void_p), e.ctypes.data_as(C.c_void_p), tau,
+                 dd.data_ptr(), Hd.data_ptr(), ldh, S.data_ptr())
+        ctx.sync()
+        s = np.zeros(P)
+        for n in range(J):
+            Href[n, :P] = Href[n, :P] + c[n] * d
+            s = s + e[n] * Href[n, :P]
+        s = s / tau
+        assert np.array_equal(S.cpu().numpy(), s)
+        assert np.array_equal(Hd.cpu().numpy()[:, :P], Href[:, :P])
+    with pytest.raises(FhError):
+        ctx.call("fh_series_sum", 0, P, c.ctypes.data_as(C.c_void_p), e.ctypes.data_as(C.c_void_p), 1e-3,
+                 dd.data_ptr(), Hd.data_ptr(), ldh, S.data_ptr())

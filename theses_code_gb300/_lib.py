@@ -56,6 +56,7 @@ _SIGS = {
     "fh_mittag_leffler": (_i, [_vp, _i, _d, _d, _dp, _dp]),
     "fh_history_sum": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_history_sum_layers": (_i, [_vp, _i, _ll, _dp, _dp, _ll, _dp]),
+    "fh_series_sum": (_i, [_vp, _i, _ll, _dp, _dp, _d, _dp, _dp, _ll, _dp]),
     "fh_history_sum_noalloc": (_i, [_vp, _i, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_history_contract_bf16": (_i, [_vp, _i, _ll, _dp, _i, _dp, _ll, _dp, _ll]),
     "fh_tridiag_batched": (_i, [_vp, _i, _i, _dp, _dp, _dp, _dp, _ll, _dp, _dp, _i, _dp, _dp, _ll]),

@@ -330,6 +330,47 @@ int fh_history_sum(fh_ctx *ctx, int M, int K, long long P, const double *W, int 
   return fh_after_launch(ctx, "k_hist_reduce");
 }
 
+// Series accumulators of the irrigation model's sum_alg 2 (time_summing,
+// irrigation_fractional.cpp:4150-4164): per point H[n] += c[n] d (the newest
+// layer difference d) for n < J, then S = (sum_n e[n] H[n]) / tau, in the
+// reference's operation order (no contraction into FMAs).  The step's
+// coefficients travel by value.
+struct fh_series_coefs {
+  double c[FH_SERIES_MAX_TERMS], e[FH_SERIES_MAX_TERMS];
+};
+__global__ void __launch_bounds__(256) k_series_sum(int J, long long P, const fh_series_coefs cf, double tau,
+                                                    const double *__restrict__ Dn, double *__restrict__ H,
+                                                    long long ldh, double *__restrict__ S) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const double d = Dn[p];
+  double sum = 0.0;
+  double *h = H + p;
+  for (int n = 0; n < J; ++n, h += ldh) {
+    const double v = __dadd_rn(*h, __dmul_rn(cf.c[n], d));
+    *h = v;
+    sum = __dadd_rn(sum, __dmul_rn(cf.e[n], v));
+  }
+  S[p] = __ddiv_rn(sum, tau);
+}
+
+int fh_series_sum(fh_ctx *ctx, int J, long long P, const double *c_host, const double *e_host, double tau,
+                  const double *Dn, double *H, long long ldh, double *S) {
+  FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
+  FH_REQUIRE(ctx, J >= 1 && J <= FH_SERIES_MAX_TERMS && P >= 0 && ldh >= P, FH_EINVAL,
+             "fh_series_sum: J = %d (1..%d), P = %lld, ldh = %lld", J, FH_SERIES_MAX_TERMS, P, ldh);
+  FH_REQUIRE(ctx, c_host && e_host && tau != 0.0, FH_EINVAL, "fh_series_sum: coefficients or tau");
+  if (P == 0) return FH_OK;
+  FH_REQUIRE(ctx, Dn && H && S, FH_EINVAL, "fh_series_sum: null pointer");
+  fh_series_coefs cf;
+  for (int n = 0; n < FH_SERIES_MAX_TERMS; ++n) {
+    cf.c[n] = n < J ? c_host[n] : 0.0;
+    cf.e[n] = n < J ? e_host[n] : 0.0;
+  }
+  k_series_sum<<<(unsigned)fh_ceil_div(P, 256), 256, 0, ctx->stream>>>(J, P, cf, tau, Dn, H, ldh, S);
+  return fh_after_launch(ctx, "k_series_sum");
+}
+
 int fh_history_sum_layers(fh_ctx *ctx, int K, long long P, const double *w, const double *H, long long ldh,
                           double *S) {
   FH_REQUIRE(ctx, ctx, FH_EINVAL, "null context");
