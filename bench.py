@@ -693,7 +693,10 @@ def run_gb300(args):
                                                ("weights", FH_PROF_WEIGHTS), ("gemm", FH_PROF_GEMM))}
     ctx.profile(False)
 
-    # end to end through the C ABI with pinned host buffers (H2D inputs, D2H result)
+    # end to end through the C ABI with pinned host buffers (H2D inputs, D2H result);
+    # one untimed call first: leaving the profiled repeat re-captures the
+    # solve graph without the marks, which is set-up, not per-solve work
+    wl.solve_host()
     barrier()
     t0 = time.perf_counter()
     out = None
