@@ -224,6 +224,15 @@ int fh_h_batch_set_u(fh_h_batch *b, const double *U);
  * Whole-batch state setters put every instance back on the batch clock.
  * No reference counterpart (the reference runs one solve per object). */
 int fh_h_batch_restart(fh_h_batch *b, int i, const fh_h_params *p, const double *U0_host);
+/* Small batches (at most 32 instances of at most 2046 interior nodes, FP64
+ * history, no space-fractional instances) run all the steps of one
+ * fh_h_batch_step call in one launch: a cluster of eight CTAs per instance
+ * shares the history sum (distributed shared memory) and one of them solves
+ * the line, step after step, with cluster barriers between.  On by default;
+ * enable = 0 steps such batches kernel by kernel like larger ones (the same
+ * sums within FP64 rounding: the history splits differ).  No reference
+ * counterpart. */
+int fh_h_batch_set_persistent(fh_h_batch *b, int enable);
 int fh_h_batch_get_u_host(fh_h_batch *b, double *U_host);
 /* U of instances [first, first+count) only (concatenated), synchronising the stream. */
 int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_host);

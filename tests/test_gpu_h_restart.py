@@ -84,3 +84,35 @@ def test_restart_twice_and_limits(ctx):
     with pytest.raises(FhError):
         b.restart(1, pa, ua)
     b.close()
+
+
+def test_persistent_path_matches_kernel_by_kernel(ctx):
+    """Small FP64 batches run each call as one launch of clustered CTAs
+    (k_h_persistent); the kernel-by-kernel path and the oracle agree with it
+    over uneven calls and a restart (mixed L1 / psi = t / psi = t^beta, constant
+    and variable coefficients)."""
+    from theses_code_gb300 import workloads
+    from theses_code_gb300.solvers import HSolverBatch
+    params, U0s = _mix()
+    pt = dict(params[1], beta=1.0)
+    params = params + [pt]
+    U0s = U0s + [U0s[1]]
+    res = []
+    for persistent in (True, False):
+        s = HSolverBatch(ctx, params, 300)
+        s.set_persistent(persistent)
+        s.set_u(U0s)
+        for n in (1, 40, 7):
+            s.calc_step(n)
+        pa, ua = workloads.caputo_1d(90, 0.65, 0.5, 1e-3)
+        s.restart(3, pa, ua)
+        s.calc_step(60)
+        res.append(s.get_u())
+        s.close()
+    for k in range(len(params)):
+        if k == 3:
+            ref = O.h_solve(pa, ua, 60)[0]
+        else:
+            ref = O.h_solve(params[k], U0s[k], 108)[0]
+        assert relmax(res[0][k], ref) <= TOL_SOLVER, k
+        assert relmax(res[0][k], res[1][k]) <= TOL_SOLVER, k

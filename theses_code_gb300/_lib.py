@@ -70,6 +70,7 @@ _SIGS = {
     "fh_h_batch_get_u_host": (_i, [_vp, _dp]),
     "fh_h_batch_set_u": (_i, [_vp, _dp]),
     "fh_h_batch_restart": (_i, [_vp, _i, C.POINTER(HParams), _dp]),
+    "fh_h_batch_set_persistent": (_i, [_vp, _i]),
     "fh_h_batch_get_u_range_host": (_i, [_vp, _i, _i, _dp]),
     "fh_h_batch_step": (_i, [_vp, _i]),
     "fh_h_batch_tstep": (_i, [_vp]),

@@ -11,6 +11,8 @@
 // stores layer differences d_t = layer[t+1] - layer[t] at slot t for the
 // concatenated state (layer-major), so the history loads coalesce across
 // neighbouring nodes and instances.
+#include <cooperative_groups.h>
+
 #include <utility>
 #include <vector>
 
@@ -74,6 +76,7 @@ struct fh_h_batch {
   // Al of the variable-coefficient instances serially in the reference order
   // (h_alpha_serial); varcoef: the batch has such instances
   bool serial_al = true, varcoef = false;
+  bool persistent = true;  // small FP64 batches: one launch per call (k_h_persistent)
   std::vector<fh_h_dev_inst> di;  // host copy of inst
   std::vector<int> cap;           // nodes a restarted occupant of each instance may have (segment - 2)
   // space-fractional instances: Toeplitz weights wsp and the sums sV per
@@ -122,27 +125,18 @@ static constexpr int kIbStride = 2 * kIbTerms + 4;
 // at old[1], mt_minimal.cpp:913-917), so slot 0 carries weight 0.
 // Thread i of CTA (x, b) owns slot i = t_lo + x*128 + threadIdx.x (slots below
 // t_lo are not computed); i = max(os - 1, 0) is the current slot.
-__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep_g, int os_g, int t_lo,
-                            double *__restrict__ W_g, int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
-                            const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX_g) {
-  const int b = blockIdx.y;
-  const fh_h_dev_inst I = inst[b];
-  // the instance's own step and slot numbers; its slot i is column I.ob + i
-  const int tstep = tstep_g - I.tb, os = os_g - I.ob;
-  double *W = W_g + I.ob;
-  const double invX = I.tb == 0 ? invX_g : 1.0 / (double)(tstep + 1);
-  const int i = t_lo + blockIdx.x * kHWeightThreads + threadIdx.x;
-  const int nh = os > 1 ? os - 1 : 0;  // history slots
-  if (i > nh) return;
-  const bool cur = i == nh;
+// Weight of slot i of instance b at its step tstep with os saved layers
+// (cur: the current slot's weight, the factor of the newest difference);
+// invX = 1 / (tstep + 1).  The arithmetic of every weight kind as described
+// at k_h_weights.
+__device__ __forceinline__ double h_slot_weight(const fh_h_dev_inst &I, int b, int i, bool cur, int tstep, int os,
+                                                double invX, int ldw, const double *__restrict__ Lb,
+                                                const double *__restrict__ ibt, const double2 *__restrict__ lgt) {
   if (I.weights == FH_W_PSI && I.beta != 1.0) {
     // psi = t^beta: the interval [x0, x0 + 1] in the divided-difference form of
     // fh_ib_diff, with the per-instance series tables and the logs as
     // double-doubles from the table of log(x)
-    if (i == 0 && !cur) {
-      W[(long long)b * ldw] = 0.0;
-      return;
-    }
+    if (i == 0 && !cur) return 0.0;
     const double *Lc = ibt + (long long)b * kIbStride, *Uc = Lc + kIbTerms;
     const int X = tstep + 1, x0 = cur ? tstep : i, x1 = x0 + 1;
     // p - q as a double-double for log values 0 <= p <= q (fast two-sum)
@@ -167,30 +161,37 @@ __global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int t
                                    fh_ib_coef_tab{Lc}, fh_ib_coef_tab{Uc});
     // (X tau)^(1 - alpha beta) / beta with log X from the table: one exp
     const double sc = exp((1.0 - I.alpha * I.beta) * (lX.x + Lc[2 * kIbTerms + 2])) * Lc[2 * kIbTerms + 3];
-    const double w = sc * diff * (1 - I.alpha);
-    if (cur)
-      wc[b] = w;
-    else
-      W[(long long)b * ldw + i] = w;
-    return;
+    return sc * diff * (1 - I.alpha);
   }
+  if (cur)
+    return (I.weights == FH_W_L1)
+               ? 1.0
+               : fh_psi_int_t((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha) *
+                     (1 - I.alpha);
   const int t = i;
-  if (!cur) {
-    double w;
-    if (t == 0)
-      w = 0.0;
-    else if (I.weights == FH_W_L1)
-      w = Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
-    else
-      w = fh_psi_int_t((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha) * (1 - I.alpha);
-    W[(long long)b * ldw + t] = w;
-  }
-  else {
-    wc[b] = (I.weights == FH_W_L1)
-                ? 1.0
-                : fh_psi_int_t((double)tstep, (double)tstep + 1.0, (double)(tstep + 1), I.tau, I.alpha) *
-                      (1 - I.alpha);
-  }
+  if (t == 0) return 0.0;
+  if (I.weights == FH_W_L1) return Lb[(long long)b * ldw + (os - t - 1)];  // L1 weights depend on the lag only
+  return fh_psi_int_t((double)t, (double)t + 1.0, (double)(tstep + 1), I.tau, I.alpha) * (1 - I.alpha);
+}
+
+__global__ void k_h_weights(const fh_h_dev_inst *__restrict__ inst, int n, int tstep_g, int os_g, int t_lo,
+                            double *__restrict__ W_g, int ldw, double *__restrict__ wc, const double *__restrict__ Lb,
+                            const double *__restrict__ ibt, const double2 *__restrict__ lgt, double invX_g) {
+  const int b = blockIdx.y;
+  const fh_h_dev_inst I = inst[b];
+  // the instance's own step and slot numbers; its slot i is column I.ob + i
+  const int tstep = tstep_g - I.tb, os = os_g - I.ob;
+  double *W = W_g + I.ob;
+  const double invX = I.tb == 0 ? invX_g : 1.0 / (double)(tstep + 1);
+  const int i = t_lo + blockIdx.x * kHWeightThreads + threadIdx.x;
+  const int nh = os > 1 ? os - 1 : 0;  // history slots
+  if (i > nh) return;
+  const bool cur = i == nh;
+  const double w = h_slot_weight(I, b, i, cur, tstep, os, invX, ldw, Lb, ibt, lgt);
+  if (cur)
+    wc[b] = w;
+  else
+    W[(long long)b * ldw + i] = w;
 }
 
 // Incomplete-beta series coefficients of every psi instance (fh_ib_tables).
@@ -614,6 +615,72 @@ __global__ void __launch_bounds__(32 * kLineCtaWarps) k_h_line_cta(
   __shared__ fh_aff sma[kLineCtaWarps];
   h_line<kLineCtaWarps, SPACE, kLineAll>(inst[blockIdx.x], blockIdx.x, threadIdx.x, U, wc, part, ldpart, splits, Al,
                                          Bt, sA, sB, sR, sOm, Dnew, append, os, dfstore, sV, smm, sma, serial);
+}
+
+// ------------------------------------------- persistent solves of small batches
+// Batches of few instances run all the steps of a call in one launch: one
+// cluster of kPersCtas CTAs per instance.  Per step CTA r computes the
+// weights of its share of the instance's history slots and their sum over the
+// instance's nodes into its shared memory; after a cluster barrier CTA 0 adds
+// the CTAs' partial sums in rank order (distributed shared memory), solves the
+// line (h_line on eight warps, as k_h_line_cta) and appends the new layer; a
+// second cluster barrier publishes the layer (and frees the partial sums) for
+// the next step.  No kernel boundary and no grid-wide synchronisation: the
+// instances are independent, and a cluster barrier is a hardware barrier that
+// every CTA of the cluster reaches the same number of times.
+constexpr int kPersCtas = 8;
+constexpr int kPersThreads = 32 * kLineCtaWarps;
+constexpr int kPersMaxNodes = 2048;  // nodes of an instance (N + 2) in the partial sums
+constexpr int kPersMaxInst = 32;     // larger batches step kernel by kernel
+
+__global__ void __cluster_dims__(kPersCtas, 1, 1) __launch_bounds__(kPersThreads)
+    k_h_persistent(const fh_h_dev_inst *__restrict__ inst, int tstep0, int os0, int nsteps, double *D,
+                   long long ldd, double *W, int ldw, double *wc, const double *__restrict__ Lb,
+                   const double *__restrict__ ibt, const double2 *__restrict__ lgt, double *U, double *part,
+                   double *Al, double *Bt, double *sA, double *sB, double *sR, double *sOm, int serial) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ double psum[kPersMaxNodes];
+  __shared__ fh_mob smm[kLineCtaWarps];
+  __shared__ fh_aff sma[kLineCtaWarps];
+  const int b = blockIdx.x / kPersCtas;
+  const int r = (int)cl.block_rank();
+  const fh_h_dev_inst I = inst[b];
+  const int np = I.N + 2;
+  double *Wb = W + (long long)b * ldw + I.ob;  // the instance's slot k is column I.ob + k
+  for (int s = 0; s < nsteps; ++s) {
+    const int os_g = os0 + s;
+    const int tstep = tstep0 + s - I.tb, os = os_g - I.ob;
+    const int K = os >= 2 ? os - 1 : 0;  // history slots
+    const double invX = 1.0 / (double)(tstep + 1);
+    const int kch = (K + kPersCtas - 1) / kPersCtas;
+    const int k0 = min(K, r * kch), k1 = min(K, k0 + kch);
+    for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x)
+      Wb[k] = h_slot_weight(I, b, k, false, tstep, os, invX, ldw, Lb, ibt, lgt);
+    if (r == 0 && threadIdx.x == 0)
+      wc[b] = h_slot_weight(I, b, os > 1 ? os - 1 : 0, true, tstep, os, invX, ldw, Lb, ibt, lgt);
+    __syncthreads();
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+      double acc = 0.0;
+      const double *d = D + (long long)(I.ob + k0) * ldd + I.off + p;
+      for (int k = k0; k < k1; ++k, d += ldd) acc = fma(Wb[k], *d, acc);
+      psum[p] = acc;
+    }
+    cl.sync();
+    if (r == 0) {
+      for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        double t = 0.0;
+        for (int q = 0; q < kPersCtas; ++q) t += cl.map_shared_rank(psum, q)[p];
+        part[I.off + p] = t;
+      }
+      __syncthreads();
+      const int append = os_g >= 1;
+      double *Dnew = append ? D + (long long)(os_g - 1) * ldd : nullptr;
+      h_line<kLineCtaWarps, false, kLineAll>(I, b, threadIdx.x, U, wc, part, 0, 1, Al, Bt, sA, sB, sR, sOm, Dnew,
+                                             append, os_g, 0, nullptr, smm, sma, serial);
+    }
+    cl.sync();
+  }
 }
 
 // ---------------------------------------------------- blocked history mode
@@ -1385,12 +1452,39 @@ int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_h
   return FH_OK;
 }
 
+// The persistent path: FP64 history, no space-fractional instances, few
+// instances of at most kPersMaxNodes nodes each.
+static bool h_persistent_ok(const fh_h_batch *b) {
+  if (!b->persistent || b->mode != FH_H_FP64 || b->space || b->n > kPersMaxInst) return false;
+  for (const auto &p : b->hp)
+    if (p.N + 2 > kPersMaxNodes) return false;
+  return true;
+}
+
+static int h_persistent_run(fh_h_batch *b, int nsteps) {
+  fh_ctx *ctx = b->ctx;
+  b->w_ready = -1;
+  fh_prof_mark(ctx, FH_PROF_HISTORY, false);
+  k_h_persistent<<<(unsigned)(b->n * kPersCtas), kPersThreads, 0, ctx->stream>>>(
+      b->inst.as<fh_h_dev_inst>(), b->tstep, b->nsaved, nsteps, b->D.as<double>(), b->Ptot, b->Wp(0),
+      b->max_weights, b->wcp(0), b->Lb.as<double>(), b->ibt.as<double>(), b->lgt.as<double2>(), b->U.as<double>(),
+      b->part.as<double>(), b->Al.as<double>(), b->Bt.as<double>(), b->sA.as<double>(), b->sB.as<double>(),
+      b->sR.as<double>(), b->sOm.as<double>(), b->serial_al ? 1 : 0);
+  fh_prof_mark(ctx, FH_PROF_HISTORY, true);
+  int rc = fh_after_launch(ctx, "k_h_persistent");
+  if (rc) return rc;
+  b->nsaved += nsteps;
+  b->tstep += nsteps;
+  return FH_OK;
+}
+
 int fh_h_batch_step(fh_h_batch *b, int nsteps) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
   fh_ctx *ctx = b->ctx;
   FH_REQUIRE(ctx, nsteps >= 0, FH_EINVAL, "fh_h_batch_step: nsteps < 0");
   FH_REQUIRE(ctx, b->nsaved + nsteps <= b->max_steps, FH_ENOMEM, "fh_h_batch_step: history full (%d + %d > %d)",
              b->nsaved, nsteps, b->max_steps);
+  if (nsteps >= 1 && h_persistent_ok(b)) return h_persistent_run(b, nsteps);
   if (b->use_graph && ctx->graphs && b->nsaved == 0 && nsteps > 1) {
     // whole solve from the initial state: capture once, replay afterwards
     b->w_ready = -1;
@@ -1414,7 +1508,16 @@ int fh_h_batch_step(fh_h_batch *b, int nsteps) {
   return FH_OK;
 }
 
+
+
 int fh_h_batch_tstep(const fh_h_batch *b) { return b ? b->tstep : -1; }
+
+int fh_h_batch_set_persistent(fh_h_batch *b, int enable) {
+  FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");
+  b->persistent = enable != 0;
+  b->graph.reset();
+  return FH_OK;
+}
 
 int fh_h_batch_set_space_order(fh_h_batch *b, const double *gamma_host) {
   FH_REQUIRE(nullptr, b, FH_EINVAL, "null batch");

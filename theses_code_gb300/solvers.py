@@ -107,6 +107,10 @@ class HSolverBatch:
     def calc_step(self, n: int = 1):
         check(self.ctx.L.fh_h_batch_step(self.h, int(n)), self.ctx.h)
 
+    def set_persistent(self, enable: bool):
+        """Small FP64 batches: all steps of a call in one launch (default on)."""
+        check(self.ctx.L.fh_h_batch_set_persistent(self.h, int(bool(enable))), self.ctx.h)
+
     def device_bytes(self) -> int:
         """Device memory the batch holds."""
         return int(self.ctx.L.fh_h_batch_device_bytes(self.h))
