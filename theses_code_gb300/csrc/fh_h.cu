@@ -632,14 +632,30 @@ constexpr int kPersCtas = 8;
 constexpr int kPersThreads = 32 * kLineCtaWarps;
 constexpr int kPersMaxNodes = 2048;  // nodes of an instance (N + 2) in the partial sums
 constexpr int kPersMaxInst = 32;     // larger batches step kernel by kernel
+constexpr int kPersMaxChunk = 3800;  // history slots of one CTA (weights in shared memory, < 48 KiB in all)
+
+// Phase stamps of the persistent solve for profiling builds (-DFH_H_STAMPS):
+// %clock64 at the phase boundaries of the first 1024 steps of CTA 0 of
+// instance 0, read with fh_h_stamps_read.  Empty otherwise.
+#ifdef FH_H_STAMPS
+__device__ long long g_h_stamps[1024 * 8];
+#define H_STAMP(p)                                                              \
+  if (b == 0 && r == 0 && threadIdx.x == 0 && s < 1024) g_h_stamps[s * 8 + (p)] = clock64();
+extern "C" int fh_h_stamps_read(long long *h) {
+  return (int)cudaMemcpyFromSymbol(h, g_h_stamps, sizeof(g_h_stamps));
+}
+#else
+#define H_STAMP(p)
+#endif
 
 __global__ void __cluster_dims__(kPersCtas, 1, 1) __launch_bounds__(kPersThreads)
     k_h_persistent(const fh_h_dev_inst *__restrict__ inst, int tstep0, int os0, int nsteps, double *D,
-                   long long ldd, double *W, int ldw, double *wc, const double *__restrict__ Lb,
+                   long long ldd, int ldw, double *wc, const double *__restrict__ Lb,
                    const double *__restrict__ ibt, const double2 *__restrict__ lgt, double *U, double *part,
                    double *Al, double *Bt, double *sA, double *sB, double *sR, double *sOm, int serial) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double wsh[];  // this CTA's weights of the step (kPersMaxChunk at most)
   __shared__ double psum[kPersMaxNodes];
   __shared__ fh_mob smm[kLineCtaWarps];
   __shared__ fh_aff sma[kLineCtaWarps];
@@ -647,26 +663,39 @@ __global__ void __cluster_dims__(kPersCtas, 1, 1) __launch_bounds__(kPersThreads
   const int r = (int)cl.block_rank();
   const fh_h_dev_inst I = inst[b];
   const int np = I.N + 2;
-  double *Wb = W + (long long)b * ldw + I.ob;  // the instance's slot k is column I.ob + k
   for (int s = 0; s < nsteps; ++s) {
     const int os_g = os0 + s;
     const int tstep = tstep0 + s - I.tb, os = os_g - I.ob;
     const int K = os >= 2 ? os - 1 : 0;  // history slots
     const double invX = 1.0 / (double)(tstep + 1);
     const int kch = (K + kPersCtas - 1) / kPersCtas;
-    const int k0 = min(K, r * kch), k1 = min(K, k0 + kch);
-    for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x)
-      Wb[k] = h_slot_weight(I, b, k, false, tstep, os, invX, ldw, Lb, ibt, lgt);
+    const int k0 = min(K, r * kch), k1 = min(K, k0 + kch), nk = k1 - k0;
+    H_STAMP(0);
+    for (int k = (int)threadIdx.x; k < nk; k += blockDim.x)
+      wsh[k] = h_slot_weight(I, b, k0 + k, false, tstep, os, invX, ldw, Lb, ibt, lgt);
     if (r == 0 && threadIdx.x == 0)
       wc[b] = h_slot_weight(I, b, os > 1 ? os - 1 : 0, true, tstep, os, invX, ldw, Lb, ibt, lgt);
     __syncthreads();
+    H_STAMP(1);
+    // slots of the instance's occupant start at global slot I.ob; eight
+    // independent loads ahead of the multiply-adds
     for (int p = threadIdx.x; p < np; p += blockDim.x) {
       double acc = 0.0;
       const double *d = D + (long long)(I.ob + k0) * ldd + I.off + p;
-      for (int k = k0; k < k1; ++k, d += ldd) acc = fma(Wb[k], *d, acc);
+      int k = 0;
+      for (; k + 8 <= nk; k += 8, d += 8 * ldd) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(d + u * ldd);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc = fma(wsh[k + u], v[u], acc);
+      }
+      for (; k < nk; ++k, d += ldd) acc = fma(wsh[k], __ldcg(d), acc);
       psum[p] = acc;
     }
+    H_STAMP(2);
     cl.sync();
+    H_STAMP(3);
     if (r == 0) {
       for (int p = threadIdx.x; p < np; p += blockDim.x) {
         double t = 0.0;
@@ -674,12 +703,15 @@ __global__ void __cluster_dims__(kPersCtas, 1, 1) __launch_bounds__(kPersThreads
         part[I.off + p] = t;
       }
       __syncthreads();
+      H_STAMP(4);
       const int append = os_g >= 1;
       double *Dnew = append ? D + (long long)(os_g - 1) * ldd : nullptr;
       h_line<kLineCtaWarps, false, kLineAll>(I, b, threadIdx.x, U, wc, part, 0, 1, Al, Bt, sA, sB, sR, sOm, Dnew,
                                              append, os_g, 0, nullptr, smm, sma, serial);
+      H_STAMP(5);
     }
     cl.sync();
+    H_STAMP(6);
   }
 }
 
@@ -1456,6 +1488,7 @@ int fh_h_batch_get_u_range_host(fh_h_batch *b, int first, int count, double *U_h
 // instances of at most kPersMaxNodes nodes each.
 static bool h_persistent_ok(const fh_h_batch *b) {
   if (!b->persistent || b->mode != FH_H_FP64 || b->space || b->n > kPersMaxInst) return false;
+  if ((b->max_steps + kPersCtas - 1) / kPersCtas > kPersMaxChunk) return false;
   for (const auto &p : b->hp)
     if (p.N + 2 > kPersMaxNodes) return false;
   return true;
@@ -1465,9 +1498,10 @@ static int h_persistent_run(fh_h_batch *b, int nsteps) {
   fh_ctx *ctx = b->ctx;
   b->w_ready = -1;
   fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-  k_h_persistent<<<(unsigned)(b->n * kPersCtas), kPersThreads, 0, ctx->stream>>>(
-      b->inst.as<fh_h_dev_inst>(), b->tstep, b->nsaved, nsteps, b->D.as<double>(), b->Ptot, b->Wp(0),
-      b->max_weights, b->wcp(0), b->Lb.as<double>(), b->ibt.as<double>(), b->lgt.as<double2>(), b->U.as<double>(),
+  const size_t smem = sizeof(double) * (size_t)((b->max_steps + kPersCtas - 1) / kPersCtas);
+  k_h_persistent<<<(unsigned)(b->n * kPersCtas), kPersThreads, smem, ctx->stream>>>(
+      b->inst.as<fh_h_dev_inst>(), b->tstep, b->nsaved, nsteps, b->D.as<double>(), b->Ptot, b->max_weights,
+      b->wcp(0), b->Lb.as<double>(), b->ibt.as<double>(), b->lgt.as<double2>(), b->U.as<double>(),
       b->part.as<double>(), b->Al.as<double>(), b->Bt.as<double>(), b->sA.as<double>(), b->sB.as<double>(),
       b->sR.as<double>(), b->sOm.as<double>(), b->serial_al ? 1 : 0);
   fh_prof_mark(ctx, FH_PROF_HISTORY, true);
