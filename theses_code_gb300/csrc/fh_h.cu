@@ -778,6 +778,14 @@ __host__ __device__ inline int hb_cheb_order(int d) {
   const double rho = D + sqrt(D * D - 1.0);
   return (int)ceil(kHbChebBits * 0.6931471805599453 / log(rho)) + 1;
 }
+// The same in the slot direction: the group's slot starts t in
+// [t0, t0 + 127] (half length 63.5) with the nearer of the branch points
+// t = 0 (at t0) and t = X - 1 (beyond the group's last slot by at least d).
+__host__ __device__ inline int hb_cheb_order_t(int dt) {
+  const double D = 1.0 + (double)dt / 63.5;
+  const double rho = D + sqrt(D * D - 1.0);
+  return (int)ceil(kHbChebBits * 0.6931471805599453 / log(rho)) + 1;
+}
 // Leading chunk groups of the block at K that are interpolated.
 static int hb_cheb_groups(int K) {
   const int ng = fh_ngroups(K / kSlcK);
@@ -790,8 +798,13 @@ static int hb_cheb_groups(int K) {
 // row stride kHbChebMax) and, in row 64, the X offsets 31.5 (1 + x_j) of the
 // points x_j = cos((2 j + 1) pi / (2 m)) from K + 3.
 static constexpr size_t kHbChebBlock = (size_t)(kSlcK + 1) * kHbChebMax;
+// Slot-direction tables after them: block m holds L[k][i] at the group's 128
+// slots (x_k = -1 + 2 k / 127) and, in row 128, the slot offsets
+// 63.5 (1 + x_i) from the group's first slot.
+static constexpr size_t kHbChebTBlock = (size_t)(kHbGroupSlots + 1) * kHbChebMax;
+static constexpr size_t kHbChebTBase = (kHbChebMax + 1) * kHbChebBlock;
 static void hb_cheb_table(std::vector<double> &t) {
-  t.assign((kHbChebMax + 1) * kHbChebBlock, 0.0);
+  t.assign(kHbChebTBase + (kHbChebMax + 1) * kHbChebTBlock, 0.0);
   const long double pi = 3.141592653589793238462643383279502884L;
   for (int m = 1; m <= kHbChebMax; ++m) {
     double *T = t.data() + (size_t)m * kHbChebBlock;
@@ -807,6 +820,17 @@ static void hb_cheb_table(std::vector<double> &t) {
         for (int i = 0; i < m; ++i)
           if (i != j) l *= (x - xj[i]) / (xj[j] - xj[i]);
         T[r * kHbChebMax + j] = (double)l;
+      }
+    }
+    double *Tt = t.data() + kHbChebTBase + (size_t)m * kHbChebTBlock;
+    for (int j = 0; j < m; ++j) Tt[kHbGroupSlots * kHbChebMax + j] = (double)(63.5L * (1.0L + xj[j]));
+    for (int k = 0; k < kHbGroupSlots; ++k) {
+      const long double x = -1.0L + 2.0L * (long double)k / 127.0L;
+      for (int j = 0; j < m; ++j) {
+        long double l = 1.0L;
+        for (int i = 0; i < m; ++i)
+          if (i != j) l *= (x - xj[i]) / (xj[j] - xj[i]);
+        Tt[k * kHbChebMax + j] = (double)l;
       }
     }
   }
@@ -826,6 +850,7 @@ __global__ void __launch_bounds__(256) k_hb_wcheb(const fh_h_dev_inst *__restric
   __shared__ double sw[kHbChebMax][kHbGroupSlots];
   __shared__ double sL[kSlcK * kHbChebMax];
   __shared__ double sX[kHbChebMax][3];  // log X_j, 1/X_j, scale of X_j
+  __shared__ double sn[kHbChebMax][kHbChebMax];  // 2D path: weights at the (slot, step) points
   __shared__ unsigned char slo[kHbChebMax][kHbGroupSlots + 1];
   const int b = blockIdx.y, G = blockIdx.x;
   const fh_h_dev_inst I = inst[b];
@@ -848,6 +873,54 @@ __global__ void __launch_bounds__(256) k_hb_wcheb(const fh_h_dev_inst *__restric
                            (1.0 - I.alpha);
   }
   __syncthreads();
+  // Groups after the first (slot starts t >= 128, away from the branch point
+  // t = 0) are interpolated in the slot direction too: the weights at
+  // mt x m points (t_i, X_j) of the interval [t_i, t_i + 1] (the
+  // divided-difference form at real t), then the group's 128 slots at each
+  // X_j from those
+  const int mt = G >= 1 ? hb_cheb_order_t(min(K + 2 - (x0 + kHbGroupSlots - 1), x0)) : kHbChebMax + 1;
+  if (mt <= kHbChebMax) {
+    const double *tabt = cheb + kHbChebTBase + (size_t)mt * kHbChebTBlock;
+    double *sLt = &sv[0][0];  // L[k][i], 128 x kHbChebMax (fits in sv)
+    for (int i = threadIdx.x; i < kHbGroupSlots * kHbChebMax; i += blockDim.x) sLt[i] = tabt[i];
+    const double *Uc = Lc + kIbTerms;
+    for (int i = threadIdx.x; i < mt * m; i += blockDim.x) {
+      const int ti = i / m, j = i - ti * m;
+      const double t = (double)x0 + tabt[kHbGroupSlots * kHbChebMax + ti];
+      const double X = (double)(K + 3) + tab[kSlcK * kHbChebMax + j];
+      double w;
+      if (psi_t) {
+        w = fh_psi_int_t(t, t + 1.0, X, I.tau, I.alpha) * (1.0 - I.alpha);
+      } else {
+        auto lrat = [](double x, double Xv) { return 2.0 * x <= Xv ? log(x / Xv) : log1p((x - Xv) / Xv); };
+        fh_ib_slot q;
+        q.zero0 = false;
+        q.top = false;
+        q.r0 = t * sX[j][1];
+        q.r1 = (t + 1.0) * sX[j][1];
+        q.dr = sX[j][1];
+        q.l1h = lrat(t + 1.0, X);
+        q.l1l = 0.0;
+        q.l0h = lrat(t, X);
+        q.l0l = 0.0;
+        q.ldh = log1p(1.0 / t);
+        q.ldl = 0.0;
+        const double diff = fh_ib_diff(q, I.beta, 1.0 - I.alpha, Lc[2 * kIbTerms + 1],
+                                       [&] { return Lc[2 * kIbTerms]; }, fh_ib_coef_tab{Lc}, fh_ib_coef_tab{Uc});
+        w = sX[j][2] * diff;
+      }
+      sn[ti][j] = w;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m * kHbGroupSlots; i += blockDim.x) {
+      const int j = i / kHbGroupSlots, k = i - j * kHbGroupSlots;
+      const double *Lk = sLt + k * kHbChebMax;
+      double acc = 0.0;
+      for (int ti = 0; ti < mt; ++ti) acc = fma(Lk[ti], sn[ti][j], acc);
+      sw[j][k] = acc;
+    }
+    __syncthreads();
+  } else {
   for (int i = threadIdx.x; i < m * (kHbGroupSlots + 1); i += blockDim.x) {
     const int j = i / (kHbGroupSlots + 1), k = i - j * (kHbGroupSlots + 1);
     const int x = x0 + k;  // x < K + 3 <= X_j
@@ -880,6 +953,7 @@ __global__ void __launch_bounds__(256) k_hb_wcheb(const fh_h_dev_inst *__restric
     sw[j][k] = x0 + k >= 1 ? sX[j][2] * diff : 0.0;  // slot 0 weighs nothing
   }
   __syncthreads();
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nchunks = K / kSlcK;
   for (int r = warp; r < kSlcK; r += blockDim.x >> 5) {
