@@ -778,8 +778,9 @@ def side_configs(args, dev):
     """One device-resident solve of each other benchmark configuration with
     its default mode and step count (config 1: 1000 steps FP64; config 3: the
     full 5000 steps, blocked; config 4: 20000 steps, blocked), timed with CUDA
-    events on the solver's stream.  Config 3's single solve includes its graph
-    capture (no warm-up solve: it alone takes ~9 s)."""
+    events on the solver's stream, and the serving loop (config 5).  Config
+    3's single solve includes its graph capture (no warm-up solve: it alone
+    takes ~9 s)."""
     import copy
 
     import torch
@@ -808,6 +809,19 @@ def side_configs(args, dev):
                         "workload": w.config.get("workload"), "warmup_solves": warm}
         finally:
             ctx.close()
+    # config 5: the serving loop's capacity (64 requests present at t = 0) and
+    # its latency under Poisson arrivals at half that rate
+    from theses_code_gb300 import serve
+    from theses_code_gb300._lib import FH_TG_BLOCKED
+    srv = serve.Server(args.budget_gb * 1e9, chunk=250, max_pool=512, max_active=16)
+    srv.run(serve.make_mix(6, rate=2000.0, seed=101, max_2d=64, steps=(100, 200), nrange=(64, 256)))
+    _, st = srv.run(serve.make_mix(args.requests, rate=args.rate, seed=3, mode_2d=FH_TG_BLOCKED), realtime=False)
+    cap = st["solves_per_s"]
+    _, sl = srv.run(serve.make_mix(args.requests, rate=0.5 * cap, seed=3, mode_2d=FH_TG_BLOCKED), realtime=True)
+    out["cfg5_serve"] = {"value": cap, "unit": "solves/s", "requests": args.requests,
+                         "latency_at_50pct_load": {"offered_per_s": 0.5 * cap, "p50_s": sl["p50_s"],
+                                                   "p99_s": sl["p99_s"],
+                                                   "joined_running_pools": sl["joined_running_pools"]}}
     return out
 
 
