@@ -57,12 +57,6 @@ constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
 }  // namespace
 
-__device__ __forceinline__ float fh_exp2i(int e) {
-  // 2^e as float (0 below the normal range; e stays far below the overflow range here)
-  if (e < -126) return 0.0f;
-  return __int_as_float((e + 127) << 23);
-}
-
 __global__ void __launch_bounds__(kThreads, 1)
     k_far_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, long long P,
                const int8_t *__restrict__ Ew, const int8_t *__restrict__ Ed, long long Ppad,
@@ -555,42 +549,6 @@ __global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, in
   fh_slice_row_group(val, blockIdx.x, K / kBK, m, kBM, Kcap, A3, Ew);
 }
 
-// Slices of a double-float value (hi, lo) scaled by 2^-E, |hi + lo| < 2^(E+7):
-// integer bf16 slices a0..a3 with |a_i| <= 128 and (hi + lo) 2^-E =
-// a0 + a1/2^8 + a2/2^16 + a3/2^24 + r, |r| <= 2^-25 (+ the pair's own rounding).
-// FP32 arithmetic only: the scaling is exact, each remainder is kept exactly as
-// a renormalised pair.
-__device__ __forceinline__ void fh_slice4_pair(float hi, float lo, float scale, __nv_bfloat16 (&b)[kSlices]) {
-  float rh = hi * scale, rl = lo * scale;
-#pragma unroll
-  for (int i = 0; i < kSlices; ++i) {
-    const float a = rintf(rh);
-    b[i] = __float2bfloat16_rn(a);
-    const float th = (rh - a) * 256.0f;  // exact: |rh - a| <= 1/2 and a is the integer nearest rh
-    const float tl = rl * 256.0f;
-    rh = th + tl;                        // fast two-sum (|th| >= |tl| or th == 0)
-    rl = tl - (rh - th);
-  }
-}
-
-// 2^e as float for -126 <= e <= 127.
-__device__ __forceinline__ float fh_exp2f_int(int e) { return __int_as_float((e + 127) << 23); }
-
-// Layers [k0, k0+64) of the double-float history (layer-major (hi, lo) pairs,
-// pitch ldd, P valid points) into the K-major planes H3[s][p][k] and the
-// exponents Ed[k0/64][p].  64 points per CTA, 4 threads per point (16 layers
-// each): coalesced pair loads, FP32 slicing in registers, the 64 x 64 bf16
-// tile of each plane staged in shared memory (pitch 66: conflict-free) and
-// written as full 128-byte rows.  Chunks whose maximum is below 2^-100 are
-// scaled as if it were 2^-100 (their slices carry the value to 2^-132).
-// Per-point exponent E (frexp exponent q of the largest |value|, floored at
-// -100; E = q - 7) of a double-float chunk group.
-__device__ __forceinline__ int fh_point_exp(float mx) {
-  int q = -100;
-  if (mx >= 7.888609052210118e-31f) q = ((__float_as_int(mx) >> 23) & 0xff) - 126;  // 2^-100
-  return q - 7;
-}
-
 // Layers [kg0, kg0 + 64 NCH) of the double-float history (layer-major (hi, lo)
 // pairs, pitch ldd, P valid points), NCH = 1 or 2 chunks of one group, into
 // the K-major planes H3[s][p][k] and the per-point exponents Ed[c][p] (the same
@@ -633,8 +591,8 @@ __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict
 #pragma unroll
   for (int i = 0; i < kL; i += 2) {
     __nv_bfloat16 s0[kSlices], s1[kSlices];
-    fh_slice4_pair(hi[i], lo[i], scale, s0);
-    fh_slice4_pair(hi[i + 1], lo[i + 1], scale, s1);
+    fh_slice_pair<kSlices>(hi[i], lo[i], scale, s0);
+    fh_slice_pair<kSlices>(hi[i + 1], lo[i + 1], scale, s1);
     const int l = qh * kL + i;  // layer within the group
     const int ch = l / kBK, kk = l % kBK;
 #pragma unroll

@@ -31,6 +31,52 @@ __device__ __forceinline__ void fh_slice4(double x, int E, __nv_bfloat16 (&b)[kS
   }
 }
 
+// 2^e as float (0 below the normal range; e stays far below the overflow range here).
+__device__ __forceinline__ float fh_exp2i(int e) {
+  if (e < -126) return 0.0f;
+  return __int_as_float((e + 127) << 23);
+}
+
+// 2^e as float for -126 <= e <= 127.
+__device__ __forceinline__ float fh_exp2f_int(int e) { return __int_as_float((e + 127) << 23); }
+
+// Per-point exponent E (frexp exponent q of the largest |value|, floored at
+// -100; E = q - 7) of a double-float chunk group: every scaled value is below
+// 2^7 in magnitude.
+__device__ __forceinline__ int fh_point_exp(float mx) {
+  int q = -100;
+  if (mx >= 7.888609052210118e-31f) q = ((__float_as_int(mx) >> 23) & 0xff) - 126;  // 2^-100
+  return q - 7;
+}
+
+// Slices of a double-float value (hi, lo) scaled by 2^-E, |hi + lo| < 2^(E+7):
+// NS integer bf16 slices a_i with |a_i| <= 128 and (hi + lo) 2^-E =
+// sum_i a_i / 2^(8 i) + r, |r| <= 2^(-8 NS + 7) (+ the pair's own rounding).
+// FP32 arithmetic only: the scaling is exact, each remainder is kept exactly as
+// a renormalised pair.
+template <int NS>
+__device__ __forceinline__ void fh_slice_pair(float hi, float lo, float scale, __nv_bfloat16 (&b)[NS]) {
+  float rh = hi * scale, rl = lo * scale;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    const float a = rintf(rh);
+    b[i] = __float2bfloat16_rn(a);
+    const float th = (rh - a) * 256.0f;  // exact: |rh - a| <= 1/2 and a is the integer nearest rh
+    const float tl = rl * 256.0f;
+    rh = th + tl;                        // fast two-sum (|th| >= |tl| or th == 0)
+    rl = tl - (rh - th);
+  }
+}
+
+// Byte offset of element (row R, k) in a K-major bf16 tile of 64-element
+// (128-byte) rows with the 128-byte swizzle (8-row atoms of 1024 B; the 16-byte
+// chunk k/8 of row R sits at chunk (k/8) ^ (R % 8)), the layout TMA writes with
+// CU_TENSOR_MAP_SWIZZLE_128B and the tcgen05 descriptors of fh_sm100.cuh read.
+__host__ __device__ __forceinline__ uint32_t fh_sw128_off(int R, int k) {
+  return (uint32_t)(R >> 3) * 1024u + (uint32_t)(R & 7) * 128u + ((uint32_t)(((k >> 3) ^ R) & 7) << 4) +
+         (uint32_t)(k & 7) * 2u;
+}
+
 // Exponent E with max|x| < 2^(E+7); 0 for an all-zero chunk.
 __device__ __forceinline__ int fh_chunk_exp(double mx) {
   if (!(mx > 0.0)) return 0;

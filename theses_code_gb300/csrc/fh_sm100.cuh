@@ -20,6 +20,11 @@ __device__ __forceinline__ void fh_mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void fh_fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// Makes this thread's ordinary shared-memory stores visible to the async proxy
+// (tcgen05.mma operand reads); before the barrier that precedes the MMA issue.
+__device__ __forceinline__ void fh_fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ void fh_mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -103,6 +108,15 @@ __device__ __forceinline__ void fh_tmem_ld16(uint32_t taddr, float (&v)[16]) {
       : "r"(taddr));
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+// 8 consecutive 32-bit columns of this thread's TMEM lane.
+__device__ __forceinline__ void fh_tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void fh_tmem_st16(uint32_t taddr, const float (&v)[16]) {
   asm volatile(

@@ -31,6 +31,7 @@
 #include "fh_common.cuh"
 #include "fh_linescan.cuh"
 #include "fh_sm100.cuh"
+#include "fh_slices.cuh"
 #include "fh_weights.cuh"
 #include "fh_two_series.h"
 
@@ -92,16 +93,22 @@ struct fh_tg_solver {
   bool fused = false;
   int fuse_blocks = 0;
   fh_dbuf bar, derr;
-  // Near rows of sub-block j8 + 8 over the layers [j0, j8) ("old" rows) are
-  // summed on the low-priority stream hs while the sweeps of sub-block j8 run
-  // (on the SMs they leave free); at the start of sub-block j8 + 8 only its
-  // last 8 layers are added to them.  Two buffers by sub-block parity.
+  // Near rows of sub-block j8 + 8 over the oldest layers of the block,
+  // [j0, min(j8, j0 + kSideLayers)) ("old" rows), are summed on the
+  // low-priority stream hs while the sweeps of sub-block j8 run (on the SMs
+  // they leave free); at the start of sub-block j8 + 8 the remaining layers
+  // are added to them on the whole GPU.  Two buffers by sub-block parity.
   cudaStream_t hs = nullptr;
   cudaEvent_t ev_main = nullptr, ev_old = nullptr;
   fh_dbuf mold;
   int old_pending = -1;  // sub-block whose old rows are enqueued on hs, not yet waited for
   int old_ready = -1;    // sub-block whose old rows are complete in mold
+  int old_end = 0;       // the old rows cover the layers [j0, old_end)
   int hs_hi = 0;         // greatest stream priority of the device (for the sweeps)
+  // blocked mode with a per-solve weight table: mid rows on the tensor cores
+  // (k_tg_mid_tc); mws / mwe: every sub-block's weight slices and row exponents
+  bool mid_tc = false;
+  fh_dbuf mws, mwe;
   bool wtab = false;      // Wall/cwall hold every step's weights (computed at step 0)
   fh_blk *blk = nullptr;  // blocked mode: bf16 slice planes and tensor maps
   int j0 = 0;             // first step of the current block (far rows valid when j0 > 0)
@@ -501,6 +508,14 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
 // layers D[j8 .. j-1] of the current 8-step sub-block weighted by
 // w_j(j8 + t), which the sweeps sum themselves (k_tg_mid_df below).
 static constexpr int kSub = 8;  // steps per sub-block of the near history
+// Layers of the old rows summed beside the sweeps (the SMs the cooperative
+// sweep launch leaves free keep pace with the sweeps up to about this many);
+// the rest of a sub-block's older layers are summed on the whole GPU at its
+// start.
+#ifndef FH_TG_SIDE_LAYERS
+#define FH_TG_SIDE_LAYERS 24
+#endif
+static constexpr int kSideLayers = FH_TG_SIDE_LAYERS;
 
 __device__ __forceinline__ void tg_tiny_weights(const double *__restrict__ wt, int nt, float2 *wsm) {
   if (threadIdx.x >= 32 && threadIdx.x < 32 + nt) wsm[threadIdx.x - 32] = fh_df_pair(fh_df_from_double(wt[threadIdx.x - 32]));
@@ -801,6 +816,251 @@ __global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restr
   }
 }
 static constexpr int kMidPPT = 1;  // points per thread of k_tg_mid_df
+
+// ------------------------------------------------ mid rows on the tensor cores
+// Blocked mode, per-solve weight table: the mid rows of sub-block jb over the
+// block's layers [j0, jb) (K = jb - j0 <= 56) as exact bf16-slice products on
+// the tensor cores, like the far rows, with five slices per value (a value is
+// kept to 2^-40 of its point's or row's maximum) and one exponent per point
+// for all K layers.  Per CTA: A = 128 points x 64 layers in five K-major
+// planes that the CTA slices itself from the double-float layers; B = the
+// sub-block's weight slices stacked as 80 rows (slice ib, row n at 16 ib + n,
+// n = 2r + m: x and y rows of step jb + r).  The MMA of data slice ia takes
+// the first (5 - ia) * 16 rows of B and writes TMEM columns 16 ia .. 79, so
+// the product (ia, ib) lands on the columns 16 (ia + ib) of its level: the
+// tensor cores form every product of level <= 4 (15 of 25) with five MMAs
+// per 16 layers and add up each level in the FP32 accumulator.  Slices are
+// integers of magnitude <= 192 (data) and <= 128 (weights), so a level sum
+// (<= 5 products per layer, K <= 64 layers) is an integer below 2^24: exact.
+// The epilogue turns the five level sums into a double-float value, scales
+// it by 2^(Ed + Ew) and adds the base row (far rows of the block).
+constexpr int kMtSl = 5;                           // slices per value
+constexpr int kMtRows = 2 * kSub;                  // x and y rows of 8 steps
+constexpr uint32_t kMtTileA = 128 * 128;           // 128 points x 64 layers bf16
+constexpr uint32_t kMtTileB = kMtRows * 128;       // 16 rows x 64 layers bf16
+constexpr uint32_t kMtWBytes = kMtSl * kMtTileB;   // one sub-block's weight slices (10 KiB)
+constexpr size_t kMtSmem = 1024 + kMtSl * kMtTileA + kMtWBytes + 64;
+constexpr uint32_t kMtTmemCols = 128;              // levels 0..4 x 16 rows = 80 used
+
+// Weight slices of every sub-block's mid rows: CTA sb slices the rows of
+// steps 8 sb .. 8 sb + 7 over the layers [j0, 8 sb) of their block (W: the
+// per-solve table, x row then y row per step, pitch ldw) into the stacked
+// layout above (ws + sb * kMtWBytes) and the row exponents we[16 sb + n].
+// Eight threads per row, eight layers each; FP64 slicing (a0 .. a4 of
+// w 2^-E, E from the row's largest |w|).
+__global__ void __launch_bounds__(128) k_tg_mid_wslice(const double *__restrict__ W, int ldw, int max_steps,
+                                                       uint8_t *__restrict__ ws, int8_t *__restrict__ we) {
+  const int sb = blockIdx.x, jb = sb * kSub, j0 = (jb / kTgBlock) * kTgBlock, K = jb - j0;
+  const int nr = min(kSub, max_steps - jb);
+  const int n = threadIdx.x >> 3, c = threadIdx.x & 7;  // row, 8-layer chunk
+  const int r = n >> 1, m = n & 1;
+  double w[8];
+  double mx = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int k = 8 * c + i;
+    w[i] = (r < nr && k < K) ? W[(long long)(jb + r) * 2 * ldw + (long long)m * ldw + j0 + k] : 0.0;
+    mx = fmax(mx, fabs(w[i]));
+  }
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int E = fh_chunk_exp(mx);
+  uint32_t pk[kMtSl][4];
+#pragma unroll
+  for (int i = 0; i < 8; i += 2) {
+    double x0 = ldexp(w[i], -E), x1 = ldexp(w[i + 1], -E);
+#pragma unroll
+    for (int q = 0; q < kMtSl; ++q) {
+      const double a0 = rint(x0), a1 = rint(x1);
+      __nv_bfloat162 b2;
+      b2.x = __double2bfloat16(a0);
+      b2.y = __double2bfloat16(a1);
+      pk[q][i >> 1] = *reinterpret_cast<const uint32_t *>(&b2);
+      x0 = (x0 - a0) * 256.0;
+      x1 = (x1 - a1) * 256.0;
+    }
+  }
+  uint8_t *dst = ws + (size_t)sb * kMtWBytes;
+#pragma unroll
+  for (int q = 0; q < kMtSl; ++q)
+    *reinterpret_cast<uint4 *>(dst + q * kMtTileB + fh_sw128_off(n, 8 * c)) =
+        make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
+  if (c == 0) we[(size_t)sb * kMtRows + n] = (int8_t)E;
+}
+
+// Slices a0..a4 of a double-float value (hi, lo) scaled by 2^-E (|scaled| <
+// 2^7), as bf16 bit patterns in the high halves of floats: a0..a2 come from
+// hi alone (its 24 bits end at slice 2's scale), then the low word joins
+// (the one FP32 add drops bits below 2^-47 of the point's maximum).  Each a_i
+// is an integer of magnitude <= 192 (a3 takes the low word's share), so its
+// float's high half is its exact bf16 pattern.
+__device__ __forceinline__ void mt_slice5(float hi, float lo, float scale, float (&a)[kMtSl]) {
+  float r = hi * scale;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = rintf(r);
+    r = (r - a[i]) * 256.0f;  // exact
+  }
+  r = fmaf(lo * scale, 16777216.0f, r);
+  a[3] = rintf(r);
+  r = (r - a[3]) * 256.0f;
+  a[4] = rintf(r);
+}
+
+// Mid rows of one sub-block: out[n][p] = base[n][p] + sum_{k < K} w_n(k) D[k][p]
+// for the nr * 2 rows n of the sub-block (weights ws / we from
+// k_tg_mid_wslice), 128 points per CTA, two threads per point (layers
+// [32 h, 32 h + 32) of the point for thread half h); KS = ceil(K/16).  Warp w
+// reads TMEM lanes 32 (w % 4) .. + 31 and rows 8 (w / 4) .. + 7 in the
+// epilogue.  The MMA completion wait is bounded; on expiry the CTA stores
+// nothing and sets *err.
+template <int KS>
+__global__ void __launch_bounds__(256, 2) k_tg_mid_tc(const float2 *__restrict__ D, long long P, int K,
+                                                  const uint8_t *__restrict__ ws, const int8_t *__restrict__ we,
+                                                  int nr, const float2 *__restrict__ base, long long ldbase,
+                                                  float2 *__restrict__ out, long long ldo, int *__restrict__ err) {
+  extern __shared__ uint8_t mt_raw[];
+  __shared__ float mxs[2][128];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int pt = tid & 127, h = tid >> 7;
+  const long long p = (long long)blockIdx.x * 128 + pt;
+  // the point's layers first (the longest latency), then this warp's base rows
+  constexpr int KH = KS >= 2 ? 32 : 16;  // layers per thread half
+  const int k0 = KH * h;
+  const bool mine = 16 * KS > k0;        // this half holds layers of the tile
+  float hi[KH], lo[KH];
+#pragma unroll
+  for (int i = 0; i < KH; ++i) {
+    float2 v = make_float2(0.f, 0.f);
+    if (mine && k0 + i < K && p < P) v = __ldcs(D + (long long)(k0 + i) * P + p);
+    hi[i] = v.x;
+    lo[i] = v.y;
+  }
+  const int r0 = 8 * (warp >> 2);  // epilogue rows of this warp
+  float2 bv[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    bv[i] = (base && p < P && ((r0 + i) >> 1) < nr) ? __ldcs(base + (long long)(r0 + i) * ldbase + p)
+                                                    : make_float2(0.f, 0.f);
+  const uint32_t raw = fh_smem_u32(mt_raw);
+  const uint32_t sA = (raw + 1023u) & ~1023u;
+  uint8_t *gA = mt_raw + (sA - raw);
+  const uint32_t sB = sA + kMtSl * kMtTileA;
+  uint8_t *gB = gA + kMtSl * kMtTileA;
+  const uint32_t bar = sB + kMtWBytes, tslot = bar + 8;
+  volatile uint32_t *tslot_g = reinterpret_cast<volatile uint32_t *>(gB + kMtWBytes + 8);
+  if (tid == 0) {
+    fh_mbar_init(bar, 1);
+    fh_fence_mbar_init();
+  }
+  if (warp == 0) {
+    fh_tmem_alloc(tslot, kMtTmemCols);
+    fh_tmem_relinquish();
+  }
+  const uint4 *wsrc = reinterpret_cast<const uint4 *>(ws);
+  for (int i = tid; i < (int)(kMtWBytes / 16); i += 256) reinterpret_cast<uint4 *>(gB)[i] = __ldg(wsrc + i);
+  float mx = 0.f;
+#pragma unroll
+  for (int i = 0; i < KH; ++i) mx = fmaxf(mx, fabsf(hi[i]));
+  mxs[h][pt] = mx;
+  __syncthreads();
+  const int E = fh_point_exp(fmaxf(mxs[0][pt], mxs[1][pt]));
+  if (mine) {
+    const float scale = fh_exp2f_int(-E);  // -E <= 107
+#pragma unroll
+    for (int c = 0; c < KH / 8; ++c) {
+      uint32_t pk[kMtSl][4];
+#pragma unroll
+      for (int i = 0; i < 8; i += 2) {
+        float a0[kMtSl], a1[kMtSl];
+        mt_slice5(hi[8 * c + i], lo[8 * c + i], scale, a0);
+        mt_slice5(hi[8 * c + i + 1], lo[8 * c + i + 1], scale, a1);
+#pragma unroll
+        for (int q = 0; q < kMtSl; ++q)
+          pk[q][i >> 1] = __byte_perm(__float_as_uint(a0[q]), __float_as_uint(a1[q]), 0x7632);
+      }
+      const uint32_t off = fh_sw128_off(pt, k0 + 8 * c);
+#pragma unroll
+      for (int q = 0; q < kMtSl; ++q)
+        *reinterpret_cast<uint4 *>(gA + q * kMtTileA + off) = make_uint4(pk[q][0], pk[q][1], pk[q][2], pk[q][3]);
+    }
+  }
+  fh_fence_proxy_async_smem();
+  fh_tc_fence_before();
+  __syncthreads();
+  fh_tc_fence_after();
+  const uint32_t tmem = *tslot_g;
+  if (tid == 0) {
+#pragma unroll
+    for (int ia = 0; ia < kMtSl; ++ia) {
+      const uint32_t idesc = fh_idesc_bf16_f32(128, (kMtSl - ia) * kMtRows);
+#pragma unroll
+      for (int kk = 0; kk < KS; ++kk)
+        fh_mma_bf16(tmem + (uint32_t)(kMtRows * ia), fh_desc_kmajor_sw128(sA + ia * kMtTileA + kk * 32),
+                    fh_desc_kmajor_sw128(sB + kk * 32), idesc, (ia > 0 || kk > 0) ? 1u : 0u);
+    }
+    fh_mma_commit(bar);
+  }
+  __syncwarp();  // lanes 1..31 of warp 0 must not spin in the wait while lane 0 issues
+  // bounded wait for the MMAs, sleeping between polls (the other CTA on the SM keeps the issue slots)
+  bool done = false;
+  {
+    const uint64_t t0 = fh_globaltimer();
+    for (;;) {
+      uint32_t d;
+      asm volatile(
+          "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\n selp.u32 %0, 1, 0, q;\n}\n"
+          : "=r"(d)
+          : "r"(bar)
+          : "memory");
+      if (d) {
+        done = true;
+        break;
+      }
+      if (fh_globaltimer() - t0 > FH_WAIT_NS) break;
+      __nanosleep(200);
+    }
+  }
+  const bool ok = __all_sync(0xffffffffu, done);
+  fh_tc_fence_after();
+  // level sums of rows r0 .. r0 + 7 (TMEM lane 32 (warp % 4) + lane is this thread's point)
+  const uint32_t lanes = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)r0;
+  float L[kMtSl][8];
+#pragma unroll
+  for (int l = 0; l < kMtSl; ++l) fh_tmem_ld8(lanes + (uint32_t)(kMtRows * l), L[l]);
+  fh_tmem_wait_ld();
+  if (ok && p < P) {
+    const uint2 ev = __ldg(reinterpret_cast<const uint2 *>(we + r0));
+    const uint32_t ew32[2] = {ev.x, ev.y};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int n = r0 + i;
+      if ((n >> 1) >= nr) continue;
+      // T = L0 + L1/2^8 + L2/2^16 + L3/2^24 + L4/2^32 as (th, tl)
+      const float x1 = L[1][i] * 0.00390625f;
+      float th = L[0][i] + x1;
+      const float bb = th - L[0][i];
+      float tl = (L[0][i] - (th - bb)) + (x1 - bb);
+      tl += L[2][i] * 1.52587890625e-05f;
+      const float tr = th + tl;
+      tl = tl - (tr - th);
+      th = tr;
+      tl += L[3][i] * 5.9604644775390625e-08f + L[4][i] * 2.3283064365386963e-10f;
+      const float sc = fh_exp2i(E + (int)(int8_t)(ew32[i >> 2] >> (8 * (i & 3))));
+      const float vh = th * sc, vl = tl * sc;
+      const float2 b = bv[i];
+      const float s2 = b.x + vh;
+      const float bs = s2 - b.x;
+      const float e = ((b.x - (s2 - bs)) + (vh - bs)) + (b.y + vl);
+      const float hh = s2 + e;
+      out[(long long)n * ldo + p] = make_float2(hh, e - (hh - s2));
+    }
+  }
+  fh_tc_fence_before();
+  __syncthreads();
+  if (warp == 0) fh_tmem_dealloc(tmem, kMtTmemCols);
+  if (!ok && (tid & 31) == 0) atomicOr(err, 1);
+}
 
 // ------------------------------------------------ fused sub-block sweeps
 // One cooperative launch runs both half steps of up to kSub consecutive steps
@@ -1373,6 +1633,28 @@ static int tg_mid(fh_tg_solver *s, cudaStream_t st, int jb, int kb, int ke, cons
   return fh_after_launch(s->ctx, "k_tg_mid_df");
 }
 
+// Mid rows of sub-block jb over all the block's layers [j0, jb) on the tensor
+// cores (k_tg_mid_tc), on top of base (far rows of step jb, or none).
+static int tg_mid_tc(fh_tg_solver *s, cudaStream_t st, int jb, int j0, const float2 *base, long long ldbase,
+                     float2 *out) {
+  const fh_tg_dev &g = s->dv;
+  const int K = jb - j0, KS = (K + 15) / 16, sb = jb / kSub;
+  if (K < 1 || KS > 4) return fh_set_error(s->ctx, FH_EINVAL, "tensor-core mid rows: %d layers", K);
+  const int nr = min(kSub, s->max_steps - jb);
+  const float2 *D = reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)j0 * g.P;
+  const uint8_t *ws = s->mws.as<uint8_t>() + (size_t)sb * kMtWBytes;
+  const int8_t *we = s->mwe.as<int8_t>() + (size_t)sb * kMtRows;
+  const unsigned grid = (unsigned)fh_ceil_div(g.P, 128);
+  int *err = s->derr.as<int>();
+  switch (KS) {
+    case 1: k_tg_mid_tc<1><<<grid, 256, kMtSmem, st>>>(D, g.P, K, ws, we, nr, base, ldbase, out, g.P, err); break;
+    case 2: k_tg_mid_tc<2><<<grid, 256, kMtSmem, st>>>(D, g.P, K, ws, we, nr, base, ldbase, out, g.P, err); break;
+    case 3: k_tg_mid_tc<3><<<grid, 256, kMtSmem, st>>>(D, g.P, K, ws, we, nr, base, ldbase, out, g.P, err); break;
+    default: k_tg_mid_tc<4><<<grid, 256, kMtSmem, st>>>(D, g.P, K, ws, we, nr, base, ldbase, out, g.P, err); break;
+  }
+  return fh_after_launch(s->ctx, "k_tg_mid_tc");
+}
+
 static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int max_n, int *done) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
@@ -1392,10 +1674,12 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       if (j == j8) {
         fh_prof_mark(ctx, FH_PROF_HISTORY, false);
         if (s->old_pending == j8 && (rc = tg_join_old(s))) return rc;
-        if (s->fused && s->old_ready == j8) {
-          // old rows [j0, j8 - 8) are done: add the last 8 layers
-          rc = tg_mid(s, ctx->stream, j8, j8 - kSub, j8, s->mold.as<float2>() + (long long)((j8 / kSub) & 1) * 16 * g.P,
-                      g.P, part);
+        if (s->mid_tc) {
+          rc = tg_mid_tc(s, ctx->stream, j8, j0, farj, s->ldfar, part);
+        } else if (s->fused && s->old_ready == j8) {
+          // old rows [j0, old_end) are done: add the layers after them
+          rc = tg_mid(s, ctx->stream, j8, s->old_end, j8,
+                      s->mold.as<float2>() + (long long)((j8 / kSub) & 1) * 16 * g.P, g.P, part);
         } else {
           rc = tg_mid(s, ctx->stream, j8, j0, j8, farj, s->ldfar, part);
         }
@@ -1452,10 +1736,12 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       at[1].val.priority = s->hs_hi;
       cfg.attrs = at;
       cfg.numAttrs = 2;
-      // old rows of sub-block j8 + 8 (layers [j0, j8), complete before this
-      // launch) on hs, beside the sweeps of this sub-block
+      // old rows of sub-block j8 + 8 (the oldest layers of [j0, j8), complete
+      // before this launch) on hs, beside the sweeps of this sub-block
       const int jn = j8 + kSub;
-      const bool old_next = s->hs && j == j8 && j8 > j0 && jn < s->max_steps && (jn - j0) < kTgBlock;
+      const int ke = min(j8, j0 + kSideLayers);
+      const bool old_next =
+          !s->mid_tc && s->hs && j == j8 && ke > j0 && jn < s->max_steps && (jn - j0) < kTgBlock;
       if (old_next) {
         FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_main, ctx->stream));
         FH_CUDA_TRY(ctx, cudaStreamWaitEvent(s->hs, s->ev_main, 0));
@@ -1467,11 +1753,12 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       if ((rc = fh_after_launch(ctx, "k_tg_sweeps_fused"))) return rc;
       if (old_next) {
         const float2 *farn = (s->blk && j0 > 0) ? s->far.as<float2>() + 2LL * (jn - j0) * s->ldfar : nullptr;
-        if ((rc = tg_mid(s, s->hs, jn, j0, j8, farn, s->ldfar,
+        if ((rc = tg_mid(s, s->hs, jn, j0, ke, farn, s->ldfar,
                          s->mold.as<float2>() + (long long)((jn / kSub) & 1) * 16 * g.P)))
           return rc;
         FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_old, s->hs));
         s->old_pending = jn;
+        s->old_end = ke;
       }
       s->tstep += ns;
       *done = ns;
@@ -1550,8 +1837,13 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
       fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
       dim3 gw((unsigned)fh_ceil_div(s->max_steps, 128), (unsigned)s->max_steps);
       k_tg_weights_all<<<gw, 128, 0, ctx->stream>>>(g, s->max_steps, s->W.as<double>(), ldw, s->cw.as<double>());
-      fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
       if ((rc = fh_after_launch(ctx, "k_tg_weights_all"))) return rc;
+      if (s->mid_tc) {
+        k_tg_mid_wslice<<<(unsigned)fh_ceil_div(s->max_steps, kSub), 128, 0, ctx->stream>>>(
+            s->W.as<double>(), ldw, s->max_steps, s->mws.as<uint8_t>(), s->mwe.as<int8_t>());
+        if ((rc = fh_after_launch(ctx, "k_tg_mid_wslice"))) return rc;
+      }
+      fh_prof_mark(ctx, FH_PROF_WEIGHTS, true);
     }
     Wj = s->W.as<double>() + (long long)j * 2 * ldw;
   } else {
@@ -1778,6 +2070,28 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
     }
     cudaGetLastError();
   }
+  if (s->dfsweep && s->wtab) {
+    // mid rows on the tensor cores: every sub-block's weight slices, error flag
+    const size_t nsub = (size_t)fh_ceil_div(max_steps, kSub);
+    if ((rc = fh_alloc(ctx, s->mws, (size_t)kMtWBytes * nsub)) ||
+        (rc = fh_alloc(ctx, s->mwe, (size_t)kMtRows * nsub)) ||
+        (!s->derr.p && (rc = fh_alloc(ctx, s->derr, sizeof(int))))) {
+      delete s;
+      return rc;
+    }
+    cudaError_t e = cudaFuncSetAttribute(k_tg_mid_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMtSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tg_mid_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMtSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tg_mid_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMtSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tg_mid_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMtSmem);
+    if (e != cudaSuccess) {
+      delete s;
+      return fh_set_error(ctx, FH_ECUDA, "fh_tg_create: mid-row kernel: %s", cudaGetErrorString(e));
+    }
+    s->mid_tc = true;
+  }
   if (mode == FH_TG_BLOCKED && max_steps > kTgBlock) {
     s->blk = fh_blk_new();
     const int kcap = (int)fh_ceil_div(max_steps, kTgBlock) * kTgBlock;
@@ -1988,7 +2302,7 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
-  if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (s->derr.p) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
   if (s->massN) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->Nn.p, 0, s->Nn.bytes, ctx->stream));  // N starts at 0
   if (int rc = tg_series_reset(s)) return rc;
   s->tstep = 0;
@@ -2009,7 +2323,7 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
-  if (s->fused) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
+  if (s->derr.p) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->derr.p, 0, sizeof(int), ctx->stream));
   if (s->massN) FH_CUDA_TRY(ctx, cudaMemsetAsync(s->Nn.p, 0, s->Nn.bytes, ctx->stream));  // N starts at 0
   if (int rc = tg_series_reset(s)) return rc;
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -2064,10 +2378,10 @@ int fh_tg_get_c_host(fh_tg_solver *s, double *C_host) {
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(C_host, s->C.p, n, cudaMemcpyDeviceToHost, ctx->stream));
   FH_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  if (s->fused) {
+  if (s->derr.p) {
     int h = 0;
     FH_CUDA_TRY(ctx, cudaMemcpy(&h, s->derr.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) return fh_set_error(ctx, FH_ETIMEOUT, "fused sweeps: a bounded grid barrier expired");
+    if (h) return fh_set_error(ctx, FH_ETIMEOUT, "a bounded device wait expired (fused sweeps or mid rows)");
   }
   return FH_OK;
 }
@@ -2078,7 +2392,7 @@ long long fh_tg_device_bytes(const fh_tg_solver *s) {
                            &s->gx,   &s->fax,  &s->pfx,  &s->pbx,  &s->aly,  &s->gy,   &s->fay,  &s->pfy,
                            &s->pby,  &s->far,  &s->Cd,   &s->Chd,  &s->fax2, &s->gx2,  &s->alx2, &s->pfx2,
                            &s->pbx2, &s->fay2, &s->gy2,  &s->aly2, &s->pfy2, &s->pby2, &s->bar,  &s->derr,
-                           &s->mold, &s->H,    &s->ser_tab, &s->Nn,   &s->dN};
+                           &s->mold, &s->H,    &s->ser_tab, &s->Nn,   &s->dN,   &s->mws,  &s->mwe};
   size_t n = 0;
   for (const fh_dbuf *d : bufs) n += d->bytes;
   if (s->blk) n += fh_blk_bytes(*s->blk);
