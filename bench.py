@@ -231,7 +231,7 @@ class TG2D(Workload):
         # algorithmic work per solve, by kernel class (interior points; per point-step:
         # 8 B per history layer read, the far pair and the two sums written)
         if blocked:
-            # near part, once per 8-step sub-block j8 (k_tg_mid_df): the older layers
+            # near part, once per 8-step sub-block j8 (k_tg_mid_tc): the older layers
             # of the current 64-step block (double-float pairs, 8 B each), the far
             # pairs of the 8 steps read (128 B, from the second block on) and the 16
             # mid rows written (128 B)
@@ -269,15 +269,16 @@ class TG2D(Workload):
             self.config["dt_eps"] = args.dt_eps
             self.config["restricted_lag"] = self.restricted_lag(p, args.dt_eps, S)
         if blocked:
-            self.class_kernels = {"history": "k_tg_mid_df (near history rows of each 8-step sub-block)",
+            self.class_kernels = {"history": "k_tg_mid_tc (tcgen05, exact bf16 slices: near history rows of each "
+                                             "8-step sub-block)",
                                   "sweep": "k_tg_sweeps_fused (cooperative, 8 steps of x and y sweeps per launch)",
                                   "gemm": "k_far_gemm (tcgen05, exact bf16 slices)"}
-            self.class_profiles = {"history": "k_tg_mid_df_tg512.md", "sweep": "k_tg_sweeps_fused_tg512.md",
+            self.class_profiles = {"history": "k_tg_mid_tc_tg512.md", "sweep": "k_tg_sweeps_fused_tg512.md",
                                    "gemm": "k_far_gemm_tg384_K1024.md"}
         else:
             self.class_profiles = {"history": {"fp64": "k_hist_sum_fp64_tg512x300.md",
                                                "df64": "k_hist_sum_df_tg512.md"}.get(args.mode, "")}
-        self.kernel = {"blocked": "k_tg_mid_df (8-step sub-blocks of the current block) + k_far_gemm (tcgen05, "
+        self.kernel = {"blocked": "k_tg_mid_tc (8-step sub-blocks of the current block) + k_far_gemm (tcgen05, "
                                   "exact bf16 slices)",
                        "df64": "k_hist_sum_df<2>"}.get(args.mode, "k_hist_sum<2>")
 

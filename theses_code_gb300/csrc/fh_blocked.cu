@@ -155,7 +155,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = fh_idesc_bf16_f32(kBM, kBN);
       int gc = 0;  // chunk counter (stage ring)
       int gg = 0;  // group counter (accumulator buffers)
       for (int k = 0; k < my_items && ok; ++k) {
@@ -169,7 +168,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         const uint32_t lv0 = tmem + (uint32_t)(b * kLevels * kBN);
-        uint32_t first[kLevels] = {0, 0, 0, 0};
+        uint32_t first = 0;
         for (int cc = 0; cc < nc; ++cc, ++gc) {
           const int s = gc % kStages;
           if (!fh_mbar_wait(full(s), (gc / kStages) & 1)) {
@@ -180,17 +179,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t sb = base + s * kStageBytes;
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
-            // level l = i + j collects the slice products a_i b_j (exact integers)
-            const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-            const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+            // level l = i + j collects the slice products a_i b_j (exact
+            // integers).  The data planes are consecutive in the stage, so B
+            // rows 64 ib + n are data slice ib: the MMA of weight slice ia
+            // takes data slices 0 .. 3 - ia and writes columns 64 (ia + ib),
+            // the accumulator of level ia + ib (the ia = 0 MMA of the group's
+            // first 16 layers initialises all four levels).
+            const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileA + kk * 32);
 #pragma unroll
-            for (int q = 0; q < 10; ++q) {
-              const int l = ia[q] + ib[q];
-              const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileA + kk * 32);
-              const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileA + ib[q] * kTileB + kk * 32);
-              fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
-              first[l] = 1;
+            for (int ia = 0; ia < kSlices; ++ia) {
+              const uint64_t ad = fh_desc_kmajor_sw128(sb + ia * kTileA + kk * 32);
+              fh_mma_bf16(lv0 + (uint32_t)(ia * kBN), ad, bd, fh_idesc_bf16_f32(kBM, (kSlices - ia) * kBN),
+                          (ia > 0 || first) ? 1u : 0u);
             }
+            first = 1;
           }
           fh_mma_commit(empty(s));
         }
@@ -385,7 +387,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = fh_idesc_bf16_f32(128, kBN);
       int gc = 0;  // chunk counter (stage ring)
       int gg = 0;  // group counter (accumulator buffers)
       for (int k = 0; k < my_items && ok; ++k) {
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           const uint32_t lv0 = tmem + (uint32_t)(b * kLevels * kBN);
-          uint32_t first[kLevels] = {0, 0, 0, 0};
+          uint32_t first = 0;
           for (int cc = 0; cc < nc; ++cc, ++gc) {
             const int s = gc % kStages;
             if (!fh_mbar_wait(full(s), (gc / kStages) & 1)) {
@@ -408,16 +409,17 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t sb = base + s * kStageBytes;
 #pragma unroll
             for (int kk = 0; kk < kBK / 16; ++kk) {
-              const int ia[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-              const int ib[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+              // weight planes consecutive in the stage: B rows 64 ib + n are
+              // weight slice ib, so the MMA of history slice ia writes the
+              // level accumulators ia + ib (as in k_far_gemm)
+              const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileH + kk * 32);
 #pragma unroll
-              for (int q = 0; q < 10; ++q) {
-                const int l = ia[q] + ib[q];
-                const uint64_t ad = fh_desc_kmajor_sw128(sb + ia[q] * kTileH + kk * 32);
-                const uint64_t bd = fh_desc_kmajor_sw128(sb + kSlices * kTileH + ib[q] * kTileW + kk * 32);
-                fh_mma_bf16(lv0 + (uint32_t)(l * kBN), ad, bd, idesc, first[l]);
-                first[l] = 1;
+              for (int ia = 0; ia < kSlices; ++ia) {
+                const uint64_t ad = fh_desc_kmajor_sw128(sb + ia * kTileH + kk * 32);
+                fh_mma_bf16(lv0 + (uint32_t)(ia * kBN), ad, bd, fh_idesc_bf16_f32(128, (kSlices - ia) * kBN),
+                            (ia > 0 || first) ? 1u : 0u);
               }
+              first = 1;
             }
             fh_mma_commit(empty(s));
           }

@@ -93,18 +93,6 @@ struct fh_tg_solver {
   bool fused = false;
   int fuse_blocks = 0;
   fh_dbuf bar, derr;
-  // Near rows of sub-block j8 + 8 over the oldest layers of the block,
-  // [j0, min(j8, j0 + kSideLayers)) ("old" rows), are summed on the
-  // low-priority stream hs while the sweeps of sub-block j8 run (on the SMs
-  // they leave free); at the start of sub-block j8 + 8 the remaining layers
-  // are added to them on the whole GPU.  Two buffers by sub-block parity.
-  cudaStream_t hs = nullptr;
-  cudaEvent_t ev_main = nullptr, ev_old = nullptr;
-  fh_dbuf mold;
-  int old_pending = -1;  // sub-block whose old rows are enqueued on hs, not yet waited for
-  int old_ready = -1;    // sub-block whose old rows are complete in mold
-  int old_end = 0;       // the old rows cover the layers [j0, old_end)
-  int hs_hi = 0;         // greatest stream priority of the device (for the sweeps)
   // blocked mode with a per-solve weight table: mid rows on the tensor cores
   // (k_tg_mid_tc); mws / mwe: every sub-block's weight slices and row exponents
   bool mid_tc = false;
@@ -134,12 +122,6 @@ struct fh_tg_solver {
   ~fh_tg_solver() {
     if (two) fh_ta_delete(two);
     if (blk) fh_blk_delete(blk);
-    if (hs) {
-      cudaStreamSynchronize(hs);
-      cudaStreamDestroy(hs);
-    }
-    if (ev_main) cudaEventDestroy(ev_main);
-    if (ev_old) cudaEventDestroy(ev_old);
   }
 };
 
@@ -506,16 +488,8 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep(fh_tg_dev g, double *C,
 // History right part of step j at a point: one precomputed row rb (the mid
 // row of step j, or its far row, or the near sum) plus the newest nt <= 7
 // layers D[j8 .. j-1] of the current 8-step sub-block weighted by
-// w_j(j8 + t), which the sweeps sum themselves (k_tg_mid_df below).
+// w_j(j8 + t), which the sweeps sum themselves (k_tg_mid_tc below).
 static constexpr int kSub = 8;  // steps per sub-block of the near history
-// Layers of the old rows summed beside the sweeps (the SMs the cooperative
-// sweep launch leaves free keep pace with the sweeps up to about this many);
-// the rest of a sub-block's older layers are summed on the whole GPU at its
-// start.
-#ifndef FH_TG_SIDE_LAYERS
-#define FH_TG_SIDE_LAYERS 24
-#endif
-static constexpr int kSideLayers = FH_TG_SIDE_LAYERS;
 
 __device__ __forceinline__ void tg_tiny_weights(const double *__restrict__ wt, int nt, float2 *wsm) {
   if (threadIdx.x >= 32 && threadIdx.x < 32 + nt) wsm[threadIdx.x - 32] = fh_df_pair(fh_df_from_double(wt[threadIdx.x - 32]));
@@ -713,109 +687,6 @@ __global__ void __launch_bounds__(kYThreads) k_tg_ysweep_df(fh_tg_dev g, float2 
   }
 }
 
-// ------------------------------------------------ mid rows of the near history
-// At the start of sub-block j8 (j8 > j0, the block start) the layers
-// [j0, j8) of the block are summed once for all nr <= 8 steps of the
-// sub-block:  mid[2r + m][p] = far[2(j8 - j0 + r) + m][p]
-//                             + sum_{k in [j0, j8)} w_{j8+r}^m(k) D[k][p]
-// (m = 0 x weights, m = 1 y weights).  Each layer is read once per sub-block
-// instead of once per step; the per-step remainder (the nt <= 7 layers of the
-// sub-block itself) is summed in the sweeps.  Double-float products and
-// TwoSum accumulation as in k_hist_sum_df; two points per thread.
-static constexpr int kMidThreads = 128;
-static constexpr int kMidMaxK = kTgBlock - kSub;  // 56 layers at most
-
-// PPT points per thread (consecutive), (hi, lo) loads of 8 PPT bytes.
-template <int PPT>
-__global__ void __launch_bounds__(kMidThreads) k_tg_mid_df(const float2 *__restrict__ D, long long P, int K,
-                                                          const double *__restrict__ W, int ldw, int nr,
-                                                          const float2 *__restrict__ far, long long ldfar,
-                                                          float2 *__restrict__ out, long long ldo) {
-  constexpr int R = 2 * kSub;
-  __shared__ float2 ws[R][kMidMaxK];
-  for (int i = threadIdx.x; i < R * K; i += blockDim.x) {
-    const int row = i / K, k = i - row * K;
-    const int r = row >> 1, m = row & 1;
-    const double w = r < nr ? W[(long long)r * 2 * ldw + (long long)m * ldw + k] : 0.0;
-    const float wh = __double2float_rn(w);
-    ws[row][k] = make_float2(wh, __double2float_rn(w - (double)wh));
-  }
-  __syncthreads();
-  const long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * PPT;
-  if (p >= P) return;
-  float ah[R][PPT], al[R][PPT];
-#pragma unroll
-  for (int row = 0; row < R; ++row)
-#pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-      if (far && (row >> 1) < nr) {
-        const float2 f = far[(long long)row * ldfar + p + q];
-        ah[row][q] = f.x;
-        al[row][q] = f.y;
-      } else {
-        ah[row][q] = al[row][q] = 0.f;
-      }
-    }
-  auto acc = [](const float2 w, const float dh, const float dl, float &sh, float &sl) {
-    const float ph = w.x * dh;
-    float pl = fmaf(w.x, dh, -ph);
-    pl = fmaf(w.x, dl, pl);
-    pl = fmaf(w.y, dh, pl);
-    const float t = sh + ph;
-    const float bb = t - sh;
-    const float e = (sh - (t - bb)) + (ph - bb);
-    sh = t;
-    sl += e + pl;
-  };
-  const float2 *d = D + p;
-  int k = 0;
-  for (; k + 4 <= K; k += 4) {
-    float2 v[4][PPT];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int q = 0; q < PPT; ++q) v[u][q] = __ldcs(d + (long long)(k + u) * P + q);
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int row = 0; row < R; ++row) {
-        const float2 w = ws[row][k + u];
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) acc(w, v[u][q].x, v[u][q].y, ah[row][q], al[row][q]);
-      }
-    if ((k & 15) == 12) {
-#pragma unroll
-      for (int row = 0; row < R; ++row)
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {  // renormalise (fast two-sum, |ah| >= |al|)
-          const float t = ah[row][q] + al[row][q];
-          al[row][q] = al[row][q] - (t - ah[row][q]);
-          ah[row][q] = t;
-        }
-    }
-  }
-  for (; k < K; ++k) {
-    float2 v[PPT];
-#pragma unroll
-    for (int q = 0; q < PPT; ++q) v[q] = __ldcs(d + (long long)k * P + q);
-#pragma unroll
-    for (int row = 0; row < R; ++row) {
-      const float2 w = ws[row][k];
-#pragma unroll
-      for (int q = 0; q < PPT; ++q) acc(w, v[q].x, v[q].y, ah[row][q], al[row][q]);
-    }
-  }
-#pragma unroll
-  for (int row = 0; row < R; ++row) {
-    if ((row >> 1) >= nr) continue;
-#pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-      const float h = ah[row][q] + al[row][q];
-      out[(long long)row * ldo + p + q] = make_float2(h, al[row][q] - (h - ah[row][q]));
-    }
-  }
-}
-static constexpr int kMidPPT = 1;  // points per thread of k_tg_mid_df
 
 // ------------------------------------------------ mid rows on the tensor cores
 // Blocked mode, per-solve weight table: the mid rows of sub-block jb over the
@@ -1606,33 +1477,10 @@ static int tg_factor(fh_tg_solver *s, const double *cwj) {
 
 // Step j of the double-float sweeps (blocked mode); the block-start work,
 // the weights and the factorization of step j are already enqueued.
-//   per-solve weight table: mid rows at each sub-block start (k_tg_mid_df),
+//   per-solve weight table: mid rows at each sub-block start (k_tg_mid_tc),
 //     the sweeps add the sub-block's own layers [j8, j);
 //   per-step weight row (more steps than the table holds): one near sum over
 //     the block's layers [j0, j) per step, far row folded in.
-// The context stream waits for the old rows still pending on hs.
-static int tg_join_old(fh_tg_solver *s) {
-  if (s->old_pending < 0) return FH_OK;
-  FH_CUDA_TRY(s->ctx, cudaStreamWaitEvent(s->ctx->stream, s->ev_old, 0));
-  s->old_ready = s->old_pending;
-  s->old_pending = -1;
-  return FH_OK;
-}
-
-// Near rows of sub-block jb (steps jb .. jb + 7) over the layers [kb, ke), on
-// top of the rows base (stride lbase between steps' x rows, y row at + lbase/2
-// for the sub-block buffers, far rows otherwise), into out (16 rows of P).
-static int tg_mid(fh_tg_solver *s, cudaStream_t st, int jb, int kb, int ke, const float2 *base, long long ldbase,
-                  float2 *out) {
-  const fh_tg_dev &g = s->dv;
-  const int ldw = s->max_steps;
-  const int nr = min(kSub, s->max_steps - jb);
-  k_tg_mid_df<kMidPPT><<<(unsigned)fh_ceil_div(g.P, (long long)kMidPPT * kMidThreads), kMidThreads, 0, st>>>(
-      reinterpret_cast<const float2 *>(s->D.as<double>()) + (long long)kb * g.P, g.P, ke - kb,
-      s->W.as<double>() + (long long)jb * 2 * ldw + kb, ldw, nr, base, ldbase, out, g.P);
-  return fh_after_launch(s->ctx, "k_tg_mid_df");
-}
-
 // Mid rows of sub-block jb over all the block's layers [j0, jb) on the tensor
 // cores (k_tg_mid_tc), on top of base (far rows of step jb, or none).
 static int tg_mid_tc(fh_tg_solver *s, cudaStream_t st, int jb, int j0, const float2 *base, long long ldbase,
@@ -1673,16 +1521,7 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
     if (j8 > j0) {
       if (j == j8) {
         fh_prof_mark(ctx, FH_PROF_HISTORY, false);
-        if (s->old_pending == j8 && (rc = tg_join_old(s))) return rc;
-        if (s->mid_tc) {
-          rc = tg_mid_tc(s, ctx->stream, j8, j0, farj, s->ldfar, part);
-        } else if (s->fused && s->old_ready == j8) {
-          // old rows [j0, old_end) are done: add the layers after them
-          rc = tg_mid(s, ctx->stream, j8, s->old_end, j8,
-                      s->mold.as<float2>() + (long long)((j8 / kSub) & 1) * 16 * g.P, g.P, part);
-        } else {
-          rc = tg_mid(s, ctx->stream, j8, j0, j8, farj, s->ldfar, part);
-        }
+        rc = tg_mid_tc(s, ctx->stream, j8, j0, farj, s->ldfar, part);
         fh_prof_mark(ctx, FH_PROF_HISTORY, true);
         if (rc) return rc;
       }
@@ -1729,37 +1568,16 @@ static int tg_step_df(fh_tg_solver *s, const double *Wj, const double *cwj, int 
       cfg.blockDim = dim3(kFuseThreads);
       cfg.dynamicSmemBytes = kFuseSmem;
       cfg.stream = ctx->stream;
-      cudaLaunchAttribute at[2];
+      cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeCooperative;
       at[0].val.cooperative = 1;
-      at[1].id = cudaLaunchAttributePriority;  // ahead of the old rows on hs
-      at[1].val.priority = s->hs_hi;
       cfg.attrs = at;
-      cfg.numAttrs = 2;
-      // old rows of sub-block j8 + 8 (the oldest layers of [j0, j8), complete
-      // before this launch) on hs, beside the sweeps of this sub-block
-      const int jn = j8 + kSub;
-      const int ke = min(j8, j0 + kSideLayers);
-      const bool old_next =
-          !s->mid_tc && s->hs && j == j8 && ke > j0 && jn < s->max_steps && (jn - j0) < kTgBlock;
-      if (old_next) {
-        FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_main, ctx->stream));
-        FH_CUDA_TRY(ctx, cudaStreamWaitEvent(s->hs, s->ev_main, 0));
-      }
+      cfg.numAttrs = 1;
       fh_prof_mark(ctx, FH_PROF_SWEEP, false);
       const cudaError_t e = cudaLaunchKernelEx(&cfg, k_tg_sweeps_fused, fa);
       fh_prof_mark(ctx, FH_PROF_SWEEP, true);
       if (e != cudaSuccess) return fh_set_error(ctx, FH_ECUDA, "k_tg_sweeps_fused: %s", cudaGetErrorString(e));
       if ((rc = fh_after_launch(ctx, "k_tg_sweeps_fused"))) return rc;
-      if (old_next) {
-        const float2 *farn = (s->blk && j0 > 0) ? s->far.as<float2>() + 2LL * (jn - j0) * s->ldfar : nullptr;
-        if ((rc = tg_mid(s, s->hs, jn, j0, ke, farn, s->ldfar,
-                         s->mold.as<float2>() + (long long)((jn / kSub) & 1) * 16 * g.P)))
-          return rc;
-        FH_CUDA_TRY(ctx, cudaEventRecord(s->ev_old, s->hs));
-        s->old_pending = jn;
-        s->old_end = ke;
-      }
       s->tstep += ns;
       *done = ns;
       return FH_OK;
@@ -1926,21 +1744,20 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   return FH_OK;
 }
 
-// The sweeps' dynamic shared memory grows with the line length.  The limit is
-// a per-function attribute of the device, shared by every solver in the
-// process, so it only ever grows (a smaller solver created later must not
-// lower it below what an earlier, larger one launches with).
 // Double-float sweeps keep the field as pairs; the FP64 field C (returned by
 // fh_tg_field / fh_tg_get_c_host) is refreshed at the end of every step call.
 static int tg_publish(fh_tg_solver *s) {
-  int rc = tg_join_old(s);  // nothing of the call is left on hs
-  if (rc || !s->dfsweep || s->tstep == 0) return rc;
+  if (!s->dfsweep || s->tstep == 0) return FH_OK;
   fh_ctx *ctx = s->ctx;
   k_from_pairs<<<(unsigned)fh_ceil_div(s->dv.P, 256), 256, 0, ctx->stream>>>(s->Cd.as<float2>(), s->C.as<double>(),
                                                                             s->dv.P);
   return fh_after_launch(ctx, "k_from_pairs");
 }
 
+// The sweeps' dynamic shared memory grows with the line length.  The limit is
+// a per-function attribute of the device, shared by every solver in the
+// process, so it only ever grows (a smaller solver created later must not
+// lower it below what an earlier, larger one launches with).
 static int tg_set_smem_attrs(fh_ctx *ctx, int sN, int M) {
   static std::mutex mu;
   static int cur_x[64], cur_y[64];
@@ -2053,20 +1870,6 @@ int fh_tg_create(fh_ctx *ctx, const fh_tg_params *p, int max_steps, int mode, fh
       }
       s->fused = true;
       s->fuse_blocks = nblk;
-      int lo = 0, hi = 0;
-      cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
-      if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->hs, cudaStreamNonBlocking, lo);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_old, cudaEventDisableTiming);
-      if (e != cudaSuccess) {
-        delete s;
-        return fh_set_error(ctx, FH_ECUDA, "fh_tg_create: history stream: %s", cudaGetErrorString(e));
-      }
-      s->hs_hi = hi;
-      if ((rc = fh_alloc(ctx, s->mold, sizeof(float2) * 2 * 16 * (size_t)g.P, false))) {
-        delete s;
-        return rc;
-      }
     }
     cudaGetLastError();
   }
@@ -2294,11 +2097,6 @@ int fh_tg_set_state(fh_tg_solver *s, const double *V2, const double *C) {
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_state: null solver");
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, V2 && C, FH_EINVAL, "fh_tg_set_state: null pointer");
-  {
-    const int rc0 = tg_join_old(s);
-    if (rc0) return rc0;
-    s->old_ready = -1;
-  }
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2, n, cudaMemcpyDeviceToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C, n, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -2315,11 +2113,6 @@ int fh_tg_set_state_host(fh_tg_solver *s, const double *V2_host, const double *C
   FH_REQUIRE(nullptr, s, FH_EINVAL, "fh_tg_set_state_host: null solver");
   fh_ctx *ctx = s->ctx;
   FH_REQUIRE(ctx, V2_host && C_host, FH_EINVAL, "fh_tg_set_state_host: null pointer");
-  {
-    const int rc0 = tg_join_old(s);
-    if (rc0) return rc0;
-    s->old_ready = -1;
-  }
   const size_t n = sizeof(double) * (size_t)(s->p.sN + 2) * (s->p.M + 2);
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->V2.p, V2_host, n, cudaMemcpyHostToDevice, ctx->stream));
   FH_CUDA_TRY(ctx, cudaMemcpyAsync(s->C.p, C_host, n, cudaMemcpyHostToDevice, ctx->stream));
@@ -2392,7 +2185,7 @@ long long fh_tg_device_bytes(const fh_tg_solver *s) {
                            &s->gx,   &s->fax,  &s->pfx,  &s->pbx,  &s->aly,  &s->gy,   &s->fay,  &s->pfy,
                            &s->pby,  &s->far,  &s->Cd,   &s->Chd,  &s->fax2, &s->gx2,  &s->alx2, &s->pfx2,
                            &s->pbx2, &s->fay2, &s->gy2,  &s->aly2, &s->pfy2, &s->pby2, &s->bar,  &s->derr,
-                           &s->mold, &s->H,    &s->ser_tab, &s->Nn,   &s->dN,   &s->mws,  &s->mwe};
+                           &s->H,    &s->ser_tab, &s->Nn,   &s->dN,   &s->mws,  &s->mwe};
   size_t n = 0;
   for (const fh_dbuf *d : bufs) n += d->bytes;
   if (s->blk) n += fh_blk_bytes(*s->blk);
