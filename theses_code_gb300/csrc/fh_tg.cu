@@ -1184,20 +1184,43 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_tg_sweeps_fused(const tg_fu
   const int line0 = kFuseLines * blockIdx.x;
   auto xl_ok = [&](int l) { return line0 + l >= 1 && line0 + l < g.M; };
   auto yl_ok = [&](int l) { return line0 + l >= 1 && line0 + l < g.sN; };
-  // fixed factor tables
-  for (int v = tid; v < kFuseLines * kFuseNL; v += blockDim.x) {
-    const int l = v / kFuseNL, i = 1 + v % kFuseNL;
-    if (xl_ok(l) && i < Nx) {
-      const long long id = (long long)(line0 + l) * g.ld + i;
-      fa_x[l * kFuseSL + tg_fslot(i)] = a.fax[id];
-      al_x[l * kFuseSL + tg_fslot(i)] = a.alx[id];
-      g_x[l * kFuseNL + i - 1] = a.gx[id];
+  // fixed factor tables: every load of the thread issued at once (the
+  // launch's first step waits for them); x rows coalesced along the row, y
+  // columns with four adjacent columns (one 32-byte sector) per four threads
+  {
+    constexpr int kIt = kFuseLines * kFuseNL / kFuseThreads;
+    float2 vx[kIt][3], vy[kIt][3];
+#pragma unroll
+    for (int u = 0; u < kIt; ++u) {
+      const int v = tid + u * kFuseThreads;
+      const int lx = v / kFuseNL, ix = 1 + v % kFuseNL;
+      const int ly = v % kFuseLines, iy = 1 + v / kFuseLines;
+      const float2 z = make_float2(0.f, 0.f);
+      const bool okx = xl_ok(lx) && ix < Nx, oky = yl_ok(ly) && iy < Ny;
+      const long long idx = (long long)(line0 + lx) * g.ld + ix;
+      const long long idy = line0 + ly + (long long)iy * g.ld;
+      vx[u][0] = okx ? __ldg(a.fax + idx) : z;
+      vx[u][1] = okx ? __ldg(a.alx + idx) : z;
+      vx[u][2] = okx ? __ldg(a.gx + idx) : z;
+      vy[u][0] = oky ? __ldg(a.fay + idy) : z;
+      vy[u][1] = oky ? __ldg(a.aly + idy) : z;
+      vy[u][2] = oky ? __ldg(a.gy + idy) : z;
     }
-    if (yl_ok(l) && i < Ny) {
-      const long long id = line0 + l + (long long)i * g.ld;
-      fa_y[l * kFuseSL + tg_fslot(i)] = a.fay[id];
-      al_y[l * kFuseSL + tg_fslot(i)] = a.aly[id];
-      g_y[l * kFuseNL + i - 1] = a.gy[id];
+#pragma unroll
+    for (int u = 0; u < kIt; ++u) {
+      const int v = tid + u * kFuseThreads;
+      const int lx = v / kFuseNL, ix = 1 + v % kFuseNL;
+      const int ly = v % kFuseLines, iy = 1 + v / kFuseLines;
+      if (xl_ok(lx) && ix < Nx) {
+        fa_x[lx * kFuseSL + tg_fslot(ix)] = vx[u][0];
+        al_x[lx * kFuseSL + tg_fslot(ix)] = vx[u][1];
+        g_x[lx * kFuseNL + ix - 1] = vx[u][2];
+      }
+      if (yl_ok(ly) && iy < Ny) {
+        fa_y[ly * kFuseSL + tg_fslot(iy)] = vy[u][0];
+        al_y[ly * kFuseSL + tg_fslot(iy)] = vy[u][1];
+        g_y[ly * kFuseNL + iy - 1] = vy[u][2];
+      }
     }
   }
   // double-float step constants and sub-block weights, one FP64 conversion per thread
