@@ -165,36 +165,56 @@ __global__ void k_tg_n1(fh_tg_dev g, int half, const double *__restrict__ C, con
   dN[id] = (1.0 / g.tau) * (nw - prev);
 }
 
+// Coefficients of the factorization, one thread per node (coalesced in both
+// directions): A, B and the diagonal R of node i of every line into Ao, Bo
+// and Ro (the fa, pf and pb arrays of the direction, which k_tg_factor
+// overwrites with its results).  dir 0: x lines, dir 1: y lines.  A, B, R in
+// the reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
+__global__ void k_tg_factor_coef(fh_tg_dev g, int dir, const double *__restrict__ V2, const double *__restrict__ cw,
+                                 double *__restrict__ Ao, double *__restrict__ Bo, double *__restrict__ Ro) {
+  const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= g.P) return;
+  const int row = (int)(id / g.ld), col = (int)(id % g.ld);
+  const int line = dir == 0 ? row : col, i = dir == 0 ? col : row;
+  const int nlines = dir == 0 ? g.M : g.sN, N = dir == 0 ? g.sN : g.M;
+  if (line < 1 || line >= nlines || i < 1 || i >= N) return;
+  const long long stride = dir == 0 ? 1 : g.ld;
+  const double dl = dir == 0 ? g.dL : g.dLx;
+  const double kcur = dir == 0 ? cw[0] : cw[1];
+  const double v2 = V2[id];
+  // A_ and B (fr_d_t_g_2d.cpp:3242-3257): D(i-1) + D(i) and D(i+1) + D(i)
+  const double Dc = tg_D(g, v2), Dm = tg_D(g, V2[id - stride]), Dp = tg_D(g, V2[id + stride]);
+  double A, B;
+  if (dir == 0) {
+    A = (v2 / dl) * ((0.5 * (Dm + Dc) / dl) + 0.5);
+    B = (v2 / dl) * ((0.5 * (Dp + Dc) / dl) - 0.5);
+  } else {
+    A = (v2 / (dl * dl)) * 0.5 * (Dm + Dc);
+    B = (v2 / (dl * dl)) * 0.5 * (Dp + Dc);
+  }
+  Ao[id] = A;
+  Bo[id] = B;
+  Ro[id] = g.st * (kcur + 0.0) + A + B;
+}
+
 // Serial factorization of every line (one thread per line): Al[i+1], the
 // pivot factor g_i and the forward-map slope fa_i = g_i A_i, stored at the
-// point of equation i.  dir 0: x lines, dir 1: y lines.  A, B, R in the
-// reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
-__global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2, const double *__restrict__ cw,
-                            double *__restrict__ al, double *__restrict__ gg, double *__restrict__ fa,
-                            double *__restrict__ pf, double *__restrict__ pb) {
+// point of equation i, then the chunk prefix products pf, pb of the slopes.
+__global__ void k_tg_factor(fh_tg_dev g, int dir, double *__restrict__ al, double *__restrict__ gg,
+                            double *__restrict__ fa, double *__restrict__ pf, double *__restrict__ pb) {
   const int line = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int nlines = dir == 0 ? g.M : g.sN;
   if (line >= nlines) return;
   const int N = dir == 0 ? g.sN : g.M;
   const long long base = dir == 0 ? (long long)line * g.ld : line;
   const long long stride = dir == 0 ? 1 : g.ld;
-  const double dl = dir == 0 ? g.dL : g.dLx;
-  const double kcur = dir == 0 ? cw[0] : cw[1];
+  // fa, pf and pb hold A, B and R of every node (k_tg_factor_coef); only the
+  // recurrence through alv is serial
   double alv = dir == 0 ? 0.0 : 1.0;
+#pragma unroll 4
   for (int i = 1; i < N; ++i) {
     const long long id = base + i * stride;
-    const double v2 = V2[id];
-    // A_ and B (fr_d_t_g_2d.cpp:3242-3257): D(i-1) + D(i) and D(i+1) + D(i)
-    const double Dc = tg_D(g, v2), Dm = tg_D(g, V2[id - stride]), Dp = tg_D(g, V2[id + stride]);
-    double A, B;
-    if (dir == 0) {
-      A = (v2 / dl) * ((0.5 * (Dm + Dc) / dl) + 0.5);
-      B = (v2 / dl) * ((0.5 * (Dp + Dc) / dl) - 0.5);
-    } else {
-      A = (v2 / (dl * dl)) * 0.5 * (Dm + Dc);
-      B = (v2 / (dl * dl)) * 0.5 * (Dp + Dc);
-    }
-    const double R = g.st * (kcur + 0.0) + A + B;
+    const double A = fa[id], B = pf[id], R = pb[id];
     const double den = R - A * alv;
     const double aln = B / den;
     const double gi = (aln == 0.0 && B == 0.0) ? 1.0 / den : aln / B;
@@ -226,13 +246,46 @@ __global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ V2,
 // All step weights of a solve in one launch: row j of Wall holds
 // [kb(k,0.5,0,1) for k < j | kb(k,1,0,1) for k < j] (x and y rows, pitch ldw),
 // cwall[4j..4j+2] the three current weights of step j.
-__global__ void k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ Wall, int ldw,
-                                 double *__restrict__ cwall) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+// psi = t (beta 1): slot [k, k+1] of row j takes fh_psi_int_t's bound terms
+// pow(|1 - tau x / gtj|, 1 - alpha) at x = k and x = k + 1, and its row factor
+// gtj / gtj * pow(gtj, 1 - alpha): each is computed once per CTA (the same
+// operations, so the same values) instead of once per slot.
+constexpr int kWallThreads = 128;
+__global__ void __launch_bounds__(kWallThreads) k_tg_weights_all(fh_tg_dev g, int nsteps, double *__restrict__ Wall,
+                                                                 int ldw, double *__restrict__ cwall) {
+  __shared__ double bnd[2][kWallThreads + 1], rowf[2];
+  const int k = blockIdx.x * kWallThreads + threadIdx.x;
   const int j = blockIdx.y;
   if (j >= nsteps) return;
   double *W = Wall + (long long)j * 2 * ldw;
-  if (k < j) {
+  const int k0 = blockIdx.x * kWallThreads;
+  if (g.beta == 1.0) {
+    if (k0 < j) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const double gtj = g.tau * ((double)j + (h ? 1.0 : 0.5));
+        for (int b = threadIdx.x; b <= kWallThreads; b += kWallThreads) {
+          const int x = k0 + b;
+          bnd[h][b] = x <= j ? pow(fabs(1.0 - (g.tau * (double)x) / gtj), 1 - g.alpha) : 0.0;
+        }
+        if (threadIdx.x == 0) {
+          double v = gtj / gtj;
+          v *= pow(gtj, 1 - g.alpha);
+          rowf[h] = v;
+        }
+      }
+      __syncthreads();
+      if (k < j) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const double v2 = -(bnd[h][threadIdx.x + 1] - bnd[h][threadIdx.x]) / (1 - g.alpha);
+          double sum = 0.0;
+          sum += v2 * rowf[h];
+          W[(long long)h * ldw + k] = tg_hw(g, g.Da * sum);
+        }
+      }
+    }
+  } else if (k < j) {
     const double s0 = (double)k + 0.0;
     W[k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta));
     W[ldw + k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta));
@@ -1476,14 +1529,19 @@ static constexpr int kFactorThreads = 8;
 static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
-      g, 0, s->V2.as<double>(), cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(),
-      s->pfx.as<double>(), s->pbx.as<double>());
-  int rc = fh_after_launch(ctx, "k_tg_factor(x)");
+  const unsigned cgrid = (unsigned)fh_ceil_div(g.P, 256);
+  k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), cwj, s->fax.as<double>(),
+                                                   s->pfx.as<double>(), s->pbx.as<double>());
+  int rc = fh_after_launch(ctx, "k_tg_factor_coef(x)");
   if (rc) return rc;
+  k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), cwj, s->fay.as<double>(),
+                                                   s->pfy.as<double>(), s->pby.as<double>());
+  if ((rc = fh_after_launch(ctx, "k_tg_factor_coef(y)"))) return rc;
+  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
+      g, 0, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(), s->pfx.as<double>(), s->pbx.as<double>());
+  if ((rc = fh_after_launch(ctx, "k_tg_factor(x)"))) return rc;
   k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
-      g, 1, s->V2.as<double>(), cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(),
-      s->pfy.as<double>(), s->pby.as<double>());
+      g, 1, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(), s->pfy.as<double>(), s->pby.as<double>());
   if ((rc = fh_after_launch(ctx, "k_tg_factor(y)"))) return rc;
   if (s->dfsweep) {
     const fh_dbuf *src[10] = {&s->fax, &s->gx, &s->alx, &s->pfx, &s->pbx, &s->fay, &s->gy, &s->aly, &s->pfy, &s->pby};
@@ -1676,8 +1734,9 @@ static int tg_one_step(fh_tg_solver *s, int max_n, int *done) {
   if (s->wtab) {
     if (j == 0) {
       fh_prof_mark(ctx, FH_PROF_WEIGHTS, false);
-      dim3 gw((unsigned)fh_ceil_div(s->max_steps, 128), (unsigned)s->max_steps);
-      k_tg_weights_all<<<gw, 128, 0, ctx->stream>>>(g, s->max_steps, s->W.as<double>(), ldw, s->cw.as<double>());
+      dim3 gw((unsigned)fh_ceil_div(s->max_steps, kWallThreads), (unsigned)s->max_steps);
+      k_tg_weights_all<<<gw, kWallThreads, 0, ctx->stream>>>(g, s->max_steps, s->W.as<double>(), ldw,
+                                                            s->cw.as<double>());
       if ((rc = fh_after_launch(ctx, "k_tg_weights_all"))) return rc;
       if (s->mid_tc) {
         k_tg_mid_wslice<<<(unsigned)fh_ceil_div(s->max_steps, kSub), 128, 0, ctx->stream>>>(
