@@ -551,23 +551,23 @@ __global__ void k_blk_split_rows(const double *__restrict__ W, long long ldw, in
   fh_slice_row_group(val, blockIdx.x, K / kBK, m, kBM, Kcap, A3, Ew);
 }
 
-// Layers [kg0, kg0 + 64 NCH) of the double-float history (layer-major (hi, lo)
-// pairs, pitch ldd, P valid points), NCH = 1 or 2 chunks of one group, into
-// the K-major planes H3[s][p][k] and the per-point exponents Ed[c][p] (the same
-// for both chunks of a group).  64 points per CTA, 4 threads per point (16 NCH
-// layers each): coalesced pair loads, FP32 slicing in registers, the 64 x 64
-// bf16 tile of each plane and chunk staged in shared memory (pitch 66:
-// conflict-free) and written as full 128-byte rows.  Points whose maximum is
-// below 2^-100 are scaled as if it were 2^-100 (their slices carry the value
-// to 2^-132).
+// The even chunk of a chunk pair, layers [kg0, kg0 + 64) of the double-float
+// history (layer-major (hi, lo) pairs, layer k at row k - kd0, pitch ldd, P
+// valid points), into the K-major planes H3[s][p][k] and the per-point
+// exponents Ed[c][p] of its own maximum (k_blk_convert_df_odd raises them to
+// the pair's).  64 points per CTA, 4 threads per point (16 layers each):
+// coalesced pair loads, FP32 slicing in registers, the 64 x 64 bf16 tile of
+// each plane staged in shared memory (pitch 66: conflict-free) and written as
+// full 128-byte rows.  Points whose maximum is below 2^-100 are scaled as if
+// it were 2^-100 (their slices carry the value to 2^-132).
 constexpr int kCvPts = 64;
 constexpr int kCvPitch = kBK + 2;  // bf16 per staged row
 constexpr size_t kCvSmemPerChunk = sizeof(__nv_bfloat16) * kSlices * kCvPts * kCvPitch;
-template <int NCH>
 __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict__ D, long long ldd, int kd0, long long P,
                                                         long long Ppad, int kg0, int Kcap,
                                                         __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
-  extern __shared__ __align__(16) __nv_bfloat16 cvout[];  // [NCH][kSlices][kCvPts * kCvPitch]
+  constexpr int NCH = 1;
+  extern __shared__ __align__(16) __nv_bfloat16 cvout[];  // [kSlices][kCvPts * kCvPitch]
   __shared__ float qmax[4][kCvPts];
   constexpr int kL = 16 * NCH;  // layers per thread
   const long long p0 = (long long)blockIdx.x * kCvPts;
@@ -623,6 +623,102 @@ __global__ void __launch_bounds__(256) k_blk_convert_df(const float2 *__restrict
     v.z = src[2];
     v.w = src[3];
     reinterpret_cast<uint4 *>(H3 + c * plane + pr * Kcap + kg0 + ch * kBK)[lane & 7] = v;
+  }
+}
+
+// The odd chunk c of a chunk pair (layers [kc0, kc0 + 64) of the
+// double-float history, layer k at row k - kd0 of D):
+// both chunks of the pair take the exponent of their joint maximum, which is
+// max(Ed[c-1][p], E(odd maximum)) since the even chunk was converted alone
+// with its own.  The odd chunk is sliced with it, and the even chunk is read
+// and sliced again only at the points where the odd chunk raised it; the
+// planes and exponents equal those of slicing both chunks with the pair's
+// exponent, with half the traffic wherever nothing is raised.
+__global__ void __launch_bounds__(256) k_blk_convert_df_odd(const float2 *__restrict__ D, long long ldd, int kd0,
+                                                          long long P, long long Ppad, int kc0, int Kcap,
+                                                          __nv_bfloat16 *__restrict__ H3, int8_t *__restrict__ Ed) {
+  extern __shared__ __align__(16) __nv_bfloat16 cvout[];  // [2][kSlices][kCvPts * kCvPitch]
+  __shared__ float qmax[4][kCvPts];
+  __shared__ int Es[kCvPts], redo[kCvPts];
+  constexpr int kL = 16;  // layers per thread
+  const int c = kc0 / kBK, kg0 = kc0 - kBK;
+  const long long p0 = (long long)blockIdx.x * kCvPts;
+  const int pt = threadIdx.x & (kCvPts - 1);
+  const int qh = threadIdx.x >> 6;  // layers qh*kL .. qh*kL + kL - 1 of a chunk
+  const long long p = p0 + pt;
+  float hi[kL], lo[kL];
+  float mx = 0.f;
+#pragma unroll
+  for (int i = 0; i < kL; ++i) {
+    float2 v = make_float2(0.f, 0.f);
+    if (p < P) v = __ldcs(D + (long long)(kc0 - kd0 + qh * kL + i) * ldd + p);
+    hi[i] = v.x;
+    lo[i] = v.y;
+    mx = fmaxf(mx, fabsf(v.x));
+  }
+  qmax[qh][pt] = mx;
+  __syncthreads();
+  if (qh == 0) {
+    const int Eo = fh_point_exp(fmaxf(fmaxf(qmax[0][pt], qmax[1][pt]), fmaxf(qmax[2][pt], qmax[3][pt])));
+    const int Ee = p < Ppad ? (int)Ed[(long long)(c - 1) * Ppad + p] : Eo;
+    const int E = Eo > Ee ? Eo : Ee;
+    Es[pt] = E;
+    redo[pt] = Eo > Ee;
+    if (p < Ppad) {
+      Ed[(long long)c * Ppad + p] = (int8_t)E;
+      if (Eo > Ee) Ed[(long long)(c - 1) * Ppad + p] = (int8_t)E;
+    }
+  }
+  __syncthreads();
+  const int E = Es[pt];
+  const bool rd = redo[pt] != 0;
+  const float scale = fh_exp2f_int(-E);  // -E <= 107
+  auto slice_to = [&](int ch) {
+#pragma unroll
+    for (int i = 0; i < kL; i += 2) {
+      __nv_bfloat16 s0[kSlices], s1[kSlices];
+      fh_slice_pair<kSlices>(hi[i], lo[i], scale, s0);
+      fh_slice_pair<kSlices>(hi[i + 1], lo[i + 1], scale, s1);
+      const int kk = qh * kL + i;
+#pragma unroll
+      for (int q = 0; q < kSlices; ++q) {
+        __nv_bfloat162 w;
+        w.x = s0[q];
+        w.y = s1[q];
+        *reinterpret_cast<__nv_bfloat162 *>(
+            &cvout[((size_t)ch * kSlices + q) * kCvPts * kCvPitch + pt * kCvPitch + kk]) = w;
+      }
+    }
+  };
+  slice_to(1);
+  if (rd) {
+#pragma unroll
+    for (int i = 0; i < kL; ++i) {
+      float2 v = make_float2(0.f, 0.f);
+      if (p < P) v = __ldcs(D + (long long)(kg0 - kd0 + qh * kL + i) * ldd + p);
+      hi[i] = v.x;
+      lo[i] = v.y;
+    }
+    slice_to(0);
+  }
+  __syncthreads();
+  // rows of 64 layers (128 B) per point, plane and chunk; a warp writes 4 rows
+  // per pass; the even chunk's rows only where it was sliced again
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long plane = Ppad * (long long)Kcap;
+  for (int r = warp * 4 + (lane >> 3); r < 2 * kSlices * kCvPts; r += 8 * 4) {
+    const int chc = r / kCvPts, row = r - chc * kCvPts;  // chc = chunk * kSlices + plane
+    const int ch = chc / kSlices, q = chc - ch * kSlices;
+    const long long pr = p0 + row;
+    if (pr >= Ppad || (ch == 0 && !redo[row])) continue;
+    const uint32_t *src =
+        reinterpret_cast<const uint32_t *>(&cvout[(size_t)chc * kCvPts * kCvPitch + row * kCvPitch + (lane & 7) * 8]);
+    uint4 v;
+    v.x = src[0];
+    v.y = src[1];
+    v.z = src[2];
+    v.w = src[3];
+    reinterpret_cast<uint4 *>(H3 + q * plane + pr * Kcap + kg0 + ch * kBK)[lane & 7] = v;
   }
 }
 
@@ -735,7 +831,7 @@ int fh_blk_init(fh_ctx *ctx, fh_blk &b, long long P, int Kcap) {
   FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_far_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
   FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(sizeof(double) * 2 * kBK * 64)));
-  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df_odd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(2 * kCvSmemPerChunk)));
   return FH_OK;
 }
@@ -752,10 +848,10 @@ int fh_blk_convert(fh_ctx *ctx, fh_blk &b, const double *D, long long ldd, int k
   if (df) {
     const float2 *Dp = reinterpret_cast<const float2 *>(D);
     if (nch == 2)
-      k_blk_convert_df<2><<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
-          Dp, ldd, 0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+      k_blk_convert_df_odd<<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
+          Dp, ldd, 0, b.P, b.Ppad, k0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
     else
-      k_blk_convert_df<1><<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
+      k_blk_convert_df<<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
           Dp, ldd, 0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
     return fh_after_launch(ctx, "k_blk_convert_df");
   }
@@ -885,24 +981,24 @@ int fh_hblk_init(fh_ctx *ctx, fh_hblk &b, long long P, int Kcap, int ninst, cons
   if ((rc = make_map(ctx, &b.mapH, b.H3.p, (unsigned long long)Kcap, (unsigned long long)b.Ppad, 128))) return rc;
   if ((rc = make_map(ctx, &b.mapW, b.W3.p, (unsigned long long)Kcap, (unsigned long long)b.R, kBN))) return rc;
   FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_hb_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
-  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  FH_CUDA_TRY(ctx, cudaFuncSetAttribute(k_blk_convert_df_odd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(2 * kCvSmemPerChunk)));
   return FH_OK;
 }
 
 // Converts history chunk c (layers [64c, 64c + 64)) held in a ring of
 // (hi, lo) pairs (ring row r = layer r mod 128, pitch ldd); an odd chunk
-// completes its group and both chunks are (re)converted with the group's
-// per-point exponents, so the ring must still hold the even partner.
+// completes its group and raises the group's per-point exponents, the even
+// partner sliced again where they rise, so the ring must still hold it.
 int fh_hblk_convert(fh_ctx *ctx, fh_hblk &b, const float2 *ring, long long ldd, int c) {
   FH_REQUIRE(ctx, c >= 0 && (c + 1) * kBK <= b.Kcap, FH_EINVAL, "batched contraction: chunk %d", c);
   const int kg0 = ((c & 1) ? c - 1 : c) * kBK;
   const int kd0 = (kg0 / 128) * 128;  // layer held in ring row 0
   if (c & 1)
-    k_blk_convert_df<2><<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
-        ring, ldd, kd0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
+    k_blk_convert_df_odd<<<(unsigned)(b.Ppad / kCvPts), 256, 2 * kCvSmemPerChunk, ctx->stream>>>(
+        ring, ldd, kd0, b.P, b.Ppad, c * kBK, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
   else
-    k_blk_convert_df<1><<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
+    k_blk_convert_df<<<(unsigned)(b.Ppad / kCvPts), 256, kCvSmemPerChunk, ctx->stream>>>(
         ring, ldd, kd0, b.P, b.Ppad, kg0, b.Kcap, b.H3.as<__nv_bfloat16>(), b.Ed.as<int8_t>());
   return fh_after_launch(ctx, "k_blk_convert_df");
 }
