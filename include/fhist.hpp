@@ -67,11 +67,12 @@ class TG_solver {
   int tstep = 0;              // completed full steps
   std::vector<double> b_C;    // field, idx = i + j*(sN+2)
   std::vector<double> V2;     // |v|^2 per node
+  std::vector<double> b_N;    // non-soluble phase (mass exchange on), filled by get_n()
 
   TG_solver(Context &ctx, const fh_tg_params &p, int max_steps, int mode = FH_TG_FP64)
       : sN(p.sN), _M(p.M), tau(p.tau), alpha(p.alpha), func_power(p.beta), sigma(p.sigma), d_value(p.d),
         C1(p.C1), _S(p.S), sdL(p.dL), dLx(p.dLx), b_C(size_t(p.sN + 2) * (p.M + 2), 0.0),
-        V2(size_t(p.sN + 2) * (p.M + 2), 0.0), ctx_(ctx) {
+        V2(size_t(p.sN + 2) * (p.M + 2), 0.0), b_N(size_t(p.sN + 2) * (p.M + 2), 0.0), ctx_(ctx) {
     ctx_.check(fh_tg_create(ctx_.get(), &p, max_steps, mode, &s_));
   }
   ~TG_solver() {
@@ -90,6 +91,16 @@ class TG_solver {
   void set_restricted(double dt_eps) { ctx_.check(fh_tg_set_restricted(s_, dt_eps)); }
   // dt_alg 3 with dt_eps = nterms (series expansion, psi = t), 0 = full history
   void set_series(int nterms) { ctx_.check(fh_tg_set_series(s_, nterms)); }
+  // dt_alg 4 (two-series approximation, psi = t), before the first step
+  void set_two_series(bool enable = true) { ctx_.check(fh_tg_set_two_series(s_, enable ? 1 : 0)); }
+  // massN: mass exchange with the non-soluble phase (the globals massN_a, massN_b)
+  void set_mass_exchange(bool enable, double massN_a, double massN_b) {
+    ctx_.check(fh_tg_set_mass_exchange(s_, enable ? 1 : 0, massN_a, massN_b));
+  }
+  // TG_solver_<func, fixed_d, 0>: fixed_d false gives D = lambda |v| (ka0 / k) per node
+  void set_diffusion(bool fixed_d, double lambda, double ka0, double k) {
+    ctx_.check(fh_tg_set_diffusion(s_, fixed_d ? 1 : 0, lambda, ka0, k));
+  }
   // TG_solver::calc_step (fr_d_t_g_2d.cpp:2552): x half step, y half step
   void calc_step() { calc_steps(1); }
   void calc_steps(int n) {
@@ -98,7 +109,10 @@ class TG_solver {
   }
   // device field -> b_C
   void get() { ctx_.check(fh_tg_get_c_host(s_, b_C.data())); }
+  // device N -> b_N (mass exchange on)
+  void get_n() { ctx_.check(fh_tg_get_n_host(s_, b_N.data())); }
   const double *device_field() const { return fh_tg_field(s_); }
+  long long device_bytes() const { return fh_tg_device_bytes(s_); }
 
  private:
   Context &ctx_;
@@ -142,7 +156,26 @@ class H_solver_batch {
   }
   // space-derivative order per instance (gamma < 1: fractional in z), before the first step
   void set_space_order(const std::vector<double> &gamma) { ctx_.check(fh_h_batch_set_space_order(b_, gamma.data())); }
+  // FH_H_FP64, FH_H_DF64 or FH_H_BLOCKED, before the first step
+  void set_mode(int mode) { ctx_.check(fh_h_batch_set_mode(b_, mode)); }
+  // small FP64 batches: all steps of a call in one launch (default on)
+  void set_persistent(bool enable) { ctx_.check(fh_h_batch_set_persistent(b_, enable ? 1 : 0)); }
+  // instance i starts a new solve (continuous batching) from U0 (p.N + 2 values,
+  // p.N at most the instance's node count at creation); the others go on.
+  // U is laid out again for the new node count and refreshed from the device.
+  void restart(int i, const fh_h_params &p, const std::vector<double> &U0) {
+    ctx_.check(fh_h_batch_restart(b_, i, &p, U0.data()));
+    params[size_t(i)] = p;
+    size_t o = 0;
+    for (size_t q = 0; q < params.size(); ++q) {
+      offset_[q] = o;
+      o += size_t(params[q].N) + 2;
+    }
+    U.assign(size_t(fh_h_batch_state_size(b_)), 0.0);
+    get();
+  }
   void get() { ctx_.check(fh_h_batch_get_u_host(b_, U.data())); }
+  long long device_bytes() const { return fh_h_batch_device_bytes(b_); }
 
  private:
   Context &ctx_;

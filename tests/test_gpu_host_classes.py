@@ -30,5 +30,5 @@ def test_host_classes_match_oracle(host_parity_bin):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     names = [line.split()[0] for line in r.stdout.strip().splitlines()]
-    assert names == ["tg_solver_fp64", "tg_solver_df64", "tg_solver_blocked", "h_solver_l1", "h_solver_psi",
-                     "ab_solver"]
+    assert names == ["tg_solver_fp64", "tg_solver_df64", "tg_solver_blocked", "tg_solver_massN_variable_d",
+                     "tg_solver_two_series", "h_solver_l1", "h_solver_psi", "h_batch_restart", "ab_solver"]
