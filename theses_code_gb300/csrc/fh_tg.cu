@@ -166,12 +166,12 @@ __global__ void k_tg_n1(fh_tg_dev g, int half, const double *__restrict__ C, con
 }
 
 // Coefficients of the factorization, one thread per node (coalesced in both
-// directions): A, B and the diagonal R of node i of every line into Ao, Bo
-// and Ro (the fa, pf and pb arrays of the direction, which k_tg_factor
-// overwrites with its results).  dir 0: x lines, dir 1: y lines.  A, B, R in
-// the reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
-__global__ void k_tg_factor_coef(fh_tg_dev g, int dir, const double *__restrict__ V2, const double *__restrict__ cw,
-                                 double *__restrict__ Ao, double *__restrict__ Bo, double *__restrict__ Ro) {
+// directions): A and B of node i of every line into Ao and Bo (the pf and pb
+// arrays of the direction, which k_tg_factor reads in its serial pass and then
+// overwrites with its prefix products).  dir 0: x lines, dir 1: y lines.  A, B
+// in the reference's arithmetic (fr_d_t_g_2d.cpp:2579-2584, 2636-2641).
+__global__ void k_tg_factor_coef(fh_tg_dev g, int dir, const double *__restrict__ V2, double *__restrict__ Ao,
+                                 double *__restrict__ Bo) {
   const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= g.P) return;
   const int row = (int)(id / g.ld), col = (int)(id % g.ld);
@@ -180,7 +180,6 @@ __global__ void k_tg_factor_coef(fh_tg_dev g, int dir, const double *__restrict_
   if (line < 1 || line >= nlines || i < 1 || i >= N) return;
   const long long stride = dir == 0 ? 1 : g.ld;
   const double dl = dir == 0 ? g.dL : g.dLx;
-  const double kcur = dir == 0 ? cw[0] : cw[1];
   const double v2 = V2[id];
   // A_ and B (fr_d_t_g_2d.cpp:3242-3257): D(i-1) + D(i) and D(i+1) + D(i)
   const double Dc = tg_D(g, v2), Dm = tg_D(g, V2[id - stride]), Dp = tg_D(g, V2[id + stride]);
@@ -194,37 +193,161 @@ __global__ void k_tg_factor_coef(fh_tg_dev g, int dir, const double *__restrict_
   }
   Ao[id] = A;
   Bo[id] = B;
-  Ro[id] = g.st * (kcur + 0.0) + A + B;
 }
 
-// Serial factorization of every line (one thread per line): Al[i+1], the
-// pivot factor g_i and the forward-map slope fa_i = g_i A_i, stored at the
-// point of equation i, then the chunk prefix products pf, pb of the slopes.
-__global__ void k_tg_factor(fh_tg_dev g, int dir, double *__restrict__ al, double *__restrict__ gg,
-                            double *__restrict__ fa, double *__restrict__ pf, double *__restrict__ pb) {
+// Serial pass of the factorization (one thread per line).  The reference's
+// pivot recurrence Al_{i+1} = B_i / den_i, den_i = R_i - A_i Al_i, g_i =
+// Al_{i+1} / B_i (= 1 / den_i) runs as its continuant, Al_i = P_i / Q_i:
+//   P_{i+1} = B_i Q_i,  Q_{i+1} = R_i Q_i - A_i P_i  (= den_i Q_i),
+// two FP64 operations per node on the serial path instead of an FP64
+// division (whose latency set the pace: ~1.3 us per node); P and Q are
+// rescaled by a power of two when |Q| leaves [2^-400, 2^400] (exact, the
+// ratios stay).  Stores P_{i+1} (al), Q_{i+1} (gg) and Q_i (fa) of node i;
+// k_tg_factor_ratio turns them into Al, g and fa = g A.  pf and pb hold A
+// and B (k_tg_factor_coef) and are not written here.
+__global__ void k_tg_factor(fh_tg_dev g, int dir, const double *__restrict__ cw, double *__restrict__ al,
+                            double *__restrict__ gg, double *__restrict__ fa, const double *__restrict__ pf,
+                            const double *__restrict__ pb) {
   const int line = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int nlines = dir == 0 ? g.M : g.sN;
   if (line >= nlines) return;
   const int N = dir == 0 ? g.sN : g.M;
   const long long base = dir == 0 ? (long long)line * g.ld : line;
   const long long stride = dir == 0 ? 1 : g.ld;
-  // fa, pf and pb hold A, B and R of every node (k_tg_factor_coef); only the
-  // recurrence through alv is serial
-  double alv = dir == 0 ? 0.0 : 1.0;
+  const double kcur = dir == 0 ? cw[0] : cw[1];
+  double P = dir == 0 ? 0.0 : 1.0, Q = 1.0;
 #pragma unroll 4
   for (int i = 1; i < N; ++i) {
     const long long id = base + i * stride;
-    const double A = fa[id], B = pf[id], R = pb[id];
-    const double den = R - A * alv;
-    const double aln = B / den;
-    const double gi = (aln == 0.0 && B == 0.0) ? 1.0 / den : aln / B;
+    const double A = pf[id], B = pb[id];
+    const double R = g.st * (kcur + 0.0) + A + B;
+    const double Pn = B * Q, Qn = R * Q - A * P;
+    al[id] = Pn;
+    gg[id] = Qn;
+    fa[id] = Q;
+    P = Pn;
+    Q = Qn;
+    const double m = fabs(Q);
+    if (m > 0x1p400 || m < 0x1p-400) {
+      const int e = ilogb(Q);
+      P = scalbn(P, -e);
+      Q = scalbn(Q, -e);
+    }
+  }
+}
+
+// Ratios of the serial pass, one thread per node: Al_{i+1} = P_{i+1} / Q_{i+1},
+// g_i = Q_i / Q_{i+1}, fa_i = g_i A_i.
+__global__ void k_tg_factor_ratio(fh_tg_dev g, int dir, double *__restrict__ al, double *__restrict__ gg,
+                                  double *__restrict__ fa, const double *__restrict__ pf) {
+  const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= g.P) return;
+  const int row = (int)(id / g.ld), col = (int)(id % g.ld);
+  const int line = dir == 0 ? row : col, i = dir == 0 ? col : row;
+  const int nlines = dir == 0 ? g.M : g.sN, N = dir == 0 ? g.sN : g.M;
+  if (line < 1 || line >= nlines || i < 1 || i >= N) return;
+  const double Qn = gg[id];
+  const double gi = fa[id] / Qn;
+  al[id] = al[id] / Qn;
+  gg[id] = gi;
+  fa[id] = gi * pf[id];
+}
+
+// The whole factorization of one line per warp, for lines whose five
+// per-node arrays fit in shared memory: the coefficients A, B (lanes over the
+// nodes, as k_tg_factor_coef), the continuant chain (lane 0, as k_tg_factor,
+// from shared memory instead of global loads on the serial path), the ratios
+// (lanes, as k_tg_factor_ratio) and the chunk prefix products (lane c its
+// chunk c, as k_tg_factor_prefix); the same operations, so the same values.
+constexpr int kFactorLineArrays = 5;
+__global__ void __launch_bounds__(32) k_tg_factor_line(fh_tg_dev g, int dir, const double *__restrict__ V2,
+                                                       const double *__restrict__ cw, double *__restrict__ al,
+                                                       double *__restrict__ gg, double *__restrict__ fa,
+                                                       double *__restrict__ pf, double *__restrict__ pb) {
+  extern __shared__ double fsm[];
+  const int line = 1 + blockIdx.x, lane = threadIdx.x;
+  const int N = dir == 0 ? g.sN : g.M;
+  const long long base = dir == 0 ? (long long)line * g.ld : line;
+  const long long stride = dir == 0 ? 1 : g.ld;
+  double *sA = fsm, *sB = sA + N, *sP = sB + N, *sQn = sP + N, *sQ = sQn + N;
+  const double dl = dir == 0 ? g.dL : g.dLx;
+  for (int i = 1 + lane; i < N; i += 32) {
+    const long long id = base + i * stride;
+    const double v2 = V2[id];
+    const double Dc = tg_D(g, v2), Dm = tg_D(g, V2[id - stride]), Dp = tg_D(g, V2[id + stride]);
+    double A, B;
+    if (dir == 0) {
+      A = (v2 / dl) * ((0.5 * (Dm + Dc) / dl) + 0.5);
+      B = (v2 / dl) * ((0.5 * (Dp + Dc) / dl) - 0.5);
+    } else {
+      A = (v2 / (dl * dl)) * 0.5 * (Dm + Dc);
+      B = (v2 / (dl * dl)) * 0.5 * (Dp + Dc);
+    }
+    sA[i] = A;
+    sB[i] = B;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const double kcur = dir == 0 ? cw[0] : cw[1];
+    double P = dir == 0 ? 0.0 : 1.0, Q = 1.0;
+    for (int i = 1; i < N; ++i) {
+      const double A = sA[i], B = sB[i];
+      const double R = g.st * (kcur + 0.0) + A + B;
+      const double Pn = B * Q, Qn = R * Q - A * P;
+      sP[i] = Pn;
+      sQn[i] = Qn;
+      sQ[i] = Q;
+      P = Pn;
+      Q = Qn;
+      const double m = fabs(Q);
+      if (m > 0x1p400 || m < 0x1p-400) {
+        const int e = ilogb(Q);
+        P = scalbn(P, -e);
+        Q = scalbn(Q, -e);
+      }
+    }
+  }
+  __syncwarp();
+  for (int i = 1 + lane; i < N; i += 32) {
+    const long long id = base + i * stride;
+    const double Qn = sQn[i];
+    const double gi = sQ[i] / Qn;
+    const double aln = sP[i] / Qn;
+    const double fai = gi * sA[i];
     al[id] = aln;
     gg[id] = gi;
-    fa[id] = gi * A;
-    alv = aln;
+    fa[id] = fai;
+    sP[i] = aln;
+    sQ[i] = fai;
   }
-  // chunk prefix products of the forward slopes and of the backward slopes in
-  // the lane chunking of fh_line_solve_prefix
+  __syncwarp();
+  const int chf = fh_chunk_f(N), chb = fh_chunk_b(N);
+  const int f0 = 1 + lane * chf, f1 = min(N, f0 + chf);
+  double p = 1.0;
+  for (int i = f0; i < f1; ++i) {
+    p = (i == f0) ? sQ[i] : p * sQ[i];
+    pf[base + i * stride] = p;
+  }
+  const double al1 = dir == 0 ? 0.0 : 1.0;
+  const int b0 = lane * chb, b1 = min(N, b0 + chb);
+  double q = 1.0;
+  for (int i = b1 - 1; i >= b0; --i) {
+    const double a = (i >= 1) ? sP[i] : al1;
+    q = (i == b1 - 1) ? a : q * a;
+    pb[base + i * stride] = q;
+  }
+}
+
+// Chunk prefix products of the forward slopes fa and of the backward slopes
+// Al in the lane chunking of fh_line_solve_prefix (one thread per line).
+__global__ void k_tg_factor_prefix(fh_tg_dev g, int dir, const double *__restrict__ al, const double *__restrict__ fa,
+                                   double *__restrict__ pf, double *__restrict__ pb) {
+  const int line = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int nlines = dir == 0 ? g.M : g.sN;
+  if (line >= nlines) return;
+  const int N = dir == 0 ? g.sN : g.M;
+  const long long base = dir == 0 ? (long long)line * g.ld : line;
+  const long long stride = dir == 0 ? 1 : g.ld;
   const int chf = fh_chunk_f(N), chb = fh_chunk_b(N);
   double p = 1.0;
   for (int i = 1; i < N; ++i) {
@@ -285,10 +408,23 @@ __global__ void __launch_bounds__(kWallThreads) k_tg_weights_all(fh_tg_dev g, in
         }
       }
     }
-  } else if (k < j) {
-    const double s0 = (double)k + 0.0;
-    W[k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta));
-    W[ldw + k] = tg_hw(g, g.Da * fh_psi_int(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta));
+  } else if (k0 < j) {
+    // psi = t^beta: the series tables of a = 1/beta, b = 1 - alpha, once per CTA
+    __shared__ double Lc[kIbTerms], Uc[kIbTerms], cst[2];
+    const double a = 1.0 / g.beta, b = 1.0 - g.alpha;
+    if (threadIdx.x == 0) {
+      fh_ib_tables(a, b, Lc, Uc);
+      cst[0] = pow(kIbLowMax, a);
+      cst[1] = exp(lgamma(a) + lgamma(b) - lgamma(a + b));
+    }
+    __syncthreads();
+    if (k < j) {
+      const double s0 = (double)k + 0.0;
+      W[k] = tg_hw(g, g.Da * fh_psi_int_pre(s0, s0 + 1.0, (double)j + 0.5, g.tau, g.alpha, g.beta, Lc, Uc, cst[0],
+                                            cst[1]));
+      W[ldw + k] = tg_hw(g, g.Da * fh_psi_int_pre(s0, s0 + 1.0, (double)j + 1.0, g.tau, g.alpha, g.beta, Lc, Uc,
+                                                  cst[0], cst[1]));
+    }
   }
   if (k == 0) {
     const double jj = (double)j;
@@ -1522,27 +1658,57 @@ __global__ void k_from_pairs(const float2 *__restrict__ y, double *__restrict__ 
 
 static constexpr int kWeightTableMaxSteps = 4096;  // 2 x 4096^2 doubles = 268 MB
 
-// One line per thread, serial FP64 recurrences with divisions: few threads per
-// CTA spread the lines over many SMs (their FP64 units are the limit).
+// One line per thread, serial FP64 recurrences: few threads per CTA spread the
+// lines over many SMs (each chain is paced by FP64 latency).
 static constexpr int kFactorThreads = 8;
 
 static int tg_factor(fh_tg_solver *s, const double *cwj) {
   fh_ctx *ctx = s->ctx;
   const fh_tg_dev &g = s->dv;
-  const unsigned cgrid = (unsigned)fh_ceil_div(g.P, 256);
-  k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), cwj, s->fax.as<double>(),
-                                                   s->pfx.as<double>(), s->pbx.as<double>());
-  int rc = fh_after_launch(ctx, "k_tg_factor_coef(x)");
-  if (rc) return rc;
-  k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), cwj, s->fay.as<double>(),
-                                                   s->pfy.as<double>(), s->pby.as<double>());
-  if ((rc = fh_after_launch(ctx, "k_tg_factor_coef(y)"))) return rc;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
-      g, 0, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(), s->pfx.as<double>(), s->pbx.as<double>());
-  if ((rc = fh_after_launch(ctx, "k_tg_factor(x)"))) return rc;
-  k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
-      g, 1, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(), s->pfy.as<double>(), s->pby.as<double>());
-  if ((rc = fh_after_launch(ctx, "k_tg_factor(y)"))) return rc;
+  int rc;
+  const size_t lsm = sizeof(double) * kFactorLineArrays * (size_t)std::max(g.sN, g.M);
+  if (lsm <= 48 * 1024) {
+    // one warp per line
+    k_tg_factor_line<<<(unsigned)(g.M - 1), 32, lsm, ctx->stream>>>(g, 0, s->V2.as<double>(), cwj,
+                                                                   s->alx.as<double>(), s->gx.as<double>(),
+                                                                   s->fax.as<double>(), s->pfx.as<double>(),
+                                                                   s->pbx.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_line(x)"))) return rc;
+    k_tg_factor_line<<<(unsigned)(g.sN - 1), 32, lsm, ctx->stream>>>(g, 1, s->V2.as<double>(), cwj,
+                                                                    s->aly.as<double>(), s->gy.as<double>(),
+                                                                    s->fay.as<double>(), s->pfy.as<double>(),
+                                                                    s->pby.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_line(y)"))) return rc;
+  } else {
+    // longer lines: the same passes as separate launches over global memory
+    const unsigned cgrid = (unsigned)fh_ceil_div(g.P, 256);
+    k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 0, s->V2.as<double>(), s->pfx.as<double>(),
+                                                     s->pbx.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_coef(x)"))) return rc;
+    k_tg_factor_coef<<<cgrid, 256, 0, ctx->stream>>>(g, 1, s->V2.as<double>(), s->pfy.as<double>(),
+                                                     s->pby.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_coef(y)"))) return rc;
+    k_tg_factor<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
+        g, 0, cwj, s->alx.as<double>(), s->gx.as<double>(), s->fax.as<double>(), s->pfx.as<double>(),
+        s->pbx.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor(x)"))) return rc;
+    k_tg_factor<<<(unsigned)fh_ceil_div(g.sN, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
+        g, 1, cwj, s->aly.as<double>(), s->gy.as<double>(), s->fay.as<double>(), s->pfy.as<double>(),
+        s->pby.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor(y)"))) return rc;
+    k_tg_factor_ratio<<<cgrid, 256, 0, ctx->stream>>>(g, 0, s->alx.as<double>(), s->gx.as<double>(),
+                                                      s->fax.as<double>(), s->pfx.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_ratio(x)"))) return rc;
+    k_tg_factor_ratio<<<cgrid, 256, 0, ctx->stream>>>(g, 1, s->aly.as<double>(), s->gy.as<double>(),
+                                                      s->fay.as<double>(), s->pfy.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_ratio(y)"))) return rc;
+    k_tg_factor_prefix<<<(unsigned)fh_ceil_div(g.M, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
+        g, 0, s->alx.as<double>(), s->fax.as<double>(), s->pfx.as<double>(), s->pbx.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_prefix(x)"))) return rc;
+    k_tg_factor_prefix<<<(unsigned)fh_ceil_div(g.sN, kFactorThreads), kFactorThreads, 0, ctx->stream>>>(
+        g, 1, s->aly.as<double>(), s->fay.as<double>(), s->pfy.as<double>(), s->pby.as<double>());
+    if ((rc = fh_after_launch(ctx, "k_tg_factor_prefix(y)"))) return rc;
+  }
   if (s->dfsweep) {
     const fh_dbuf *src[10] = {&s->fax, &s->gx, &s->alx, &s->pfx, &s->pbx, &s->fay, &s->gy, &s->aly, &s->pfy, &s->pby};
     fh_dbuf *dst[10] = {&s->fax2, &s->gx2, &s->alx2, &s->pfx2, &s->pbx2,

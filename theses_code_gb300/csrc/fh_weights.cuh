@@ -159,6 +159,32 @@ __device__ __forceinline__ double fh_psi_int_t(double x0, double x1, double X, d
 // beta != 1: the divided-difference form above; the coefficients are built in
 // a local table once per call (this form serves per-solve and per-block weight
 // tables; the batched per-step weights read per-instance tables instead).
+// beta != 1 with the coefficient tables of fh_ib_tables(1/beta, 1 - alpha),
+// rlo = pow(kIbLowMax, 1/beta) and btot = B(1/beta, 1 - alpha) supplied by the
+// caller (computed once for many slots).
+__device__ __forceinline__ double fh_psi_int_pre(double x0, double x1, double X, double tau, double alpha,
+                                                 double beta, const double *Lc, const double *Uc, double rlo,
+                                                 double btot) {
+  const double b = 1.0 - alpha;
+  fh_ib_slot q;
+  q.zero0 = !(x0 > 0.0);
+  q.top = !(x1 < X);
+  q.r0 = x0 / X;
+  q.r1 = x1 / X;
+  q.dr = (x1 - x0) / X;
+  auto lrat = [](double x, double X) { return 2.0 * x <= X ? log(x / X) : log1p((x - X) / X); };
+  q.l1h = q.top ? 0.0 : lrat(x1, X);
+  q.l1l = 0.0;
+  q.l0h = q.zero0 ? 0.0 : lrat(x0, X);
+  q.l0l = 0.0;
+  q.ldh = q.zero0 ? 0.0 : log1p((x1 - x0) / x0);
+  q.ldl = 0.0;
+  const fh_ib_coef_tab lc{Lc}, uc{Uc};
+  const double diff = fh_ib_diff(q, beta, b, rlo, [&] { return btot; }, lc, uc);
+  const double T = X * tau;
+  return pow(T, 1.0 - alpha * beta) / beta * diff;
+}
+
 __device__ __forceinline__ double fh_psi_int(double x0, double x1, double X, double tau, double alpha,
                                              double beta) {
   if (beta == 1.0) return fh_psi_int_t(x0, x1, X, tau, alpha);
