@@ -54,3 +54,23 @@ def test_ctx_create_fails_cleanly_without_gpu(lib):
     rc = L.fh_ctx_create(0, ctypes.byref(h))
     assert rc == _lib.FH_ECUDA and not h.value
     assert b"device" in L.fh_last_error(None)
+
+
+def test_host_classes_compile_and_link(lib, tmp_path):
+    """include/fhist.hpp compiles against the C header and the C++ host parity
+    program links against the library and the oracle (it runs on a GPU in
+    tests/test_gpu_host_classes.py)."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from oracle import oracle as O
+    O.build()
+    pkg = os.path.join(REPO, "theses_code_gb300")
+    orc = os.path.join(REPO, "oracle", "_build")
+    out = str(tmp_path / "host_parity")
+    cmd = ["g++", "-std=c++17", "-Wall", "-Werror", os.path.join(REPO, "tests", "cpp", "host_parity.cpp"),
+           "-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "oracle"),
+           "-I", "/usr/local/cuda/include", "-L", pkg, "-lfhist", "-L", orc, "-lfh_oracle", "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
