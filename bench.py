@@ -779,7 +779,8 @@ def side_configs(args, dev):
     """One device-resident solve of each other benchmark configuration with
     its default mode and step count (config 1: 1000 steps FP64; config 3: the
     full 5000 steps, blocked; config 4: 20000 steps, blocked), timed with CUDA
-    events on the solver's stream, and the serving loop (config 5).  Config
+    events on the solver's stream, the serving loop (config 5) and the
+    irrigation model's series-accumulator kernel (sum_alg 2).  Config
     3's single solve includes its graph capture (no warm-up solve: it alone
     takes ~9 s)."""
     import copy
@@ -810,6 +811,47 @@ def side_configs(args, dev):
                         "workload": w.config.get("workload"), "warmup_solves": warm}
         finally:
             ctx.close()
+    # the irrigation model's series accumulators (sum_alg 2, fh_series_sum):
+    # one call per step over 2048 x 2048 points with 20 terms; per point the
+    # newest difference is read, the 20 accumulators read and written and the
+    # sum written: 16 J + 16 bytes
+    try:
+        import ctypes as C
+        ctx = Context(dev)
+        try:
+            J, P = 20, 2048 * 2048
+            gen = torch.Generator(device=f"cuda:{dev}").manual_seed(5)
+            H = torch.randn(J, P, dtype=torch.float64, device=f"cuda:{dev}", generator=gen)
+            Dn = torch.randn(P, dtype=torch.float64, device=f"cuda:{dev}", generator=gen) * 1e-3
+            S = torch.empty(P, dtype=torch.float64, device=f"cuda:{dev}")
+            rng = np.random.default_rng(5)
+            c = np.ascontiguousarray(rng.normal(size=J) * 1e-3)
+            e = np.ascontiguousarray(rng.normal(size=J))
+            torch.cuda.synchronize(dev)
+
+            def call():
+                ctx.call("fh_series_sum", J, P, c.ctypes.data_as(C.c_void_p), e.ctypes.data_as(C.c_void_p), 1.0,
+                         Dn.data_ptr(), H.data_ptr(), P, S.data_ptr())
+            for _ in range(3):
+                call()
+            st = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            n = 20
+            e0.record(st)
+            for _ in range(n):
+                call()
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / n
+            gbs = (16.0 * J + 16.0) * P / (ms / 1e3) / 1e9
+            out["sumalg2_series_sum"] = {"value": gbs, "unit": "GB/s", "frac_of_hbm": gbs / peaks()["hbm"],
+                                         "ms_per_call": ms, "terms": J, "points": P,
+                                         "fp64_ops_per_point": 4 * J}
+        finally:
+            ctx.close()
+    except Exception as ex:  # a measurement beside the headline: report, do not abort the line
+        out["sumalg2_series_sum"] = {"error": str(ex)[:200]}
     # config 5: the serving loop's capacity (64 requests present at t = 0) and
     # its latency under Poisson arrivals at half that rate
     from theses_code_gb300 import serve
